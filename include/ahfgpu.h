@@ -1,0 +1,205 @@
+/*
+ * ahfgpu.h -- C ABI of the GB300 unbinding + halo-property stage of AHF.
+ *
+ * The stage replaced is the per-halo sequence that AHF runs after gathering
+ * a halo's particles (src/libahf/ahf_halos_sfc.c:140-156):
+ *
+ *     sort_halo_particles(halo);      src/libahf/ahf_halos.c:5786-5894
+ *     rem_outsideRvir(halo, 0);       src/libahf/ahf_halos.c:3687-3889
+ *     rem_unbound(halo);              src/libahf/ahf_halos.c:3292-3607
+ *     rem_outsideRvir(halo, 1);
+ *     HaloProfiles(halo);             src/libahf/ahf_halos.c:3961-5261
+ *
+ * In AHF that sequence runs once per halo inside the OpenMP loop at
+ * src/libahf/ahf_halos.c:504-510 (one call of
+ * ahf_halos_sfc_constructHalo(HALO*), declared in
+ * src/libahf/ahf_halos_sfc.h:15-16).  Here the caller gathers every halo on
+ * the host, packs the lists into one CSR batch and makes ONE call; the
+ * library returns, per halo, the fields that the five functions above write
+ * into HALO, the profile arrays that c_profile() would hold, and the kept
+ * particle list in radial order.
+ *
+ * Conventions: all pointers are plain host pointers unless the function name
+ * ends in _device; sizes are 64-bit; nothing here uses C++ or CUDA types.
+ * Every function returns AHFGPU_OK (0) or a negative AHFGPU_ERR_* code and
+ * never calls exit(); ahfgpu_last_error() gives the message of the last
+ * failure on the calling thread.
+ */
+#ifndef AHFGPU_H
+#define AHFGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AHFGPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define AHFGPU_OK              0
+#define AHFGPU_ERR_INVALID    -1   /* malformed batch or parameters          */
+#define AHFGPU_ERR_OOM        -2   /* host or device allocation failed       */
+#define AHFGPU_ERR_CUDA       -3   /* a CUDA runtime call failed             */
+#define AHFGPU_ERR_TIMEOUT    -4   /* a bounded device wait ran out          */
+#define AHFGPU_ERR_NO_DEVICE  -5   /* no usable sm_103 device                */
+#define AHFGPU_ERR_CAPACITY   -6   /* a size exceeds a documented maximum    */
+#define AHFGPU_ERR_STATE      -7   /* call sequence error (e.g. no init)     */
+
+/* ---- execution forms --------------------------------------------------- */
+typedef enum {
+  /* Halos one at a time, in batch order, FP64 arithmetic; bound sets are
+   * bit-exact with the reference (exact sequential replay on device for any
+   * halo with a particle inside the rounding band). */
+  AHFGPU_PLAIN_FP64    = 0,
+  /* Every halo of the batch in one persistent launch (size-sorted work
+   * queue), FP64 arithmetic, same exactness rule as the plain form. */
+  AHFGPU_BATCHED_FP64  = 1,
+  /* Batched, FP32 positions/velocities/keys with compensated (two-sum) FP32
+   * scans, FP64 edge normalisation and an FP64 re-test of near-threshold
+   * particles; membership equals the FP64 reference. */
+  AHFGPU_BATCHED_FP32C = 2
+} ahfgpu_mode;
+
+/* ---- parameters (AHF.input keys and the ahf_halos() unit factors) -------
+ * Fill exactly as src/libahf/ahf_halos.c:199-221 computes them:
+ *   r_fac = simu.boxsize*global.a;       x_fac = simu.boxsize;
+ *   v_fac = simu.boxsize/simu.t_unit/global.a;  m_fac = simu.pmass;
+ *   rho_fac = simu.pmass/pow3(simu.boxsize);
+ *   phi_fac = Grav*simu.pmass/(simu.boxsize*global.a);
+ *   Hubble = calc_Hubble(a); ovlim = global.ovlim; rho_vir = global.rho_vir.
+ * VescTune = simu.AHF_VTUNE (AHF.input VescTune), MINPART =
+ * simu.AHF_MINPART (AHF.input NminPerHalo, >= 4).                           */
+typedef struct {
+  double  VescTune;
+  int64_t MINPART;
+  double  ovlim;
+  double  rho_vir;
+  double  r_fac, x_fac, v_fac, m_fac, rho_fac, phi_fac, Hubble;
+} ahfgpu_params;
+
+/* ---- input batch ---------------------------------------------------------
+ * Halo h owns entries [off[h], off[h+1]) of the particle arrays, in the
+ * order ahf_halos_sfc_gatherParts() produced them.  Positions are box units
+ * in [0,1), velocities are AHF internal momenta (struct particle .pos/.mom,
+ * src/tdef.h:36-77).  w is the MULTIMASS weight (NULL = all 1.0, the default
+ * build).  gidx is the particle's index in global.fst_part and is what the
+ * kept list returns (NULL = return the entry index inside the batch).  id is
+ * optional and only carried through.  cx/cy/cz are HALO.pos.               */
+typedef struct {
+  int64_t         nhalo;
+  const uint64_t *off;                    /* [nhalo+1], off[0] == 0        */
+  const float    *x, *y, *z;              /* [off[nhalo]]                  */
+  const float    *vx, *vy, *vz;           /* [off[nhalo]]                  */
+  const float    *w;                      /* [off[nhalo]] or NULL          */
+  const uint64_t *gidx;                   /* [off[nhalo]] or NULL          */
+  const double   *cx, *cy, *cz;           /* [nhalo]                       */
+} ahfgpu_batch;
+
+/* ---- per-halo result ---------------------------------------------------- */
+#define AHFGPU_HALO_EMPTY        0x001u  /* n == 0: nothing ran (ahf_halos_sfc.c:122)   */
+#define AHFGPU_HALO_RAN_SORT     0x002u  /* sort_halo_particles ran                     */
+#define AHFGPU_HALO_RAN_RVIR0    0x004u  /* rem_outsideRvir(.,0) ran                    */
+#define AHFGPU_HALO_RAN_UNBIND   0x008u  /* rem_unbound ran                             */
+#define AHFGPU_HALO_RAN_RVIR1    0x010u  /* rem_outsideRvir(.,1) ran                    */
+#define AHFGPU_HALO_RAN_PROFILE  0x020u  /* HaloProfiles ran                            */
+#define AHFGPU_HALO_NO_MBP       0x040u  /* no most-bound particle (mbp_offset = -1)    */
+#define AHFGPU_HALO_REPLAYED     0x100u  /* exact sequential replay was used            */
+#define AHFGPU_HALO_NOBOUND      0x200u  /* an unbinding pass kept no particle          */
+
+typedef struct {
+  uint64_t npart;          /* HALO.npart after the stage                       */
+  int32_t  nbins;          /* HALO.prof.nbins, 0 when HaloProfiles did not run */
+  uint32_t flags;          /* AHFGPU_HALO_* bits                               */
+  int32_t  niter;          /* rem_unbound iterations (0 if it did not run)     */
+  int32_t  fix_rounds;     /* max bulk-velocity fixpoint rounds (diagnostic)   */
+  double   M_vir, R_vir, ovdens, Phi0;
+  double   vel[3];
+  double   sigV, v_esc2, V2_max, R_max, r2;
+  double   lambda, lambdaE, Ekin, Epot, SurfP;
+  double   pos_com[3], com_offset;
+  double   pos_mbp[3], vel_mbp[3], mbp_offset;
+  double   AngMom[3], axis[3], E1[3], E2[3], E3[3];
+  double   fMhires, cNFW, R1, cR1;
+} ahfgpu_halo;
+
+/* Profile arrays, one row of AHFGPU_PROF_NFIELDS doubles per bin, fields in
+ * the order of HALOPROFILE (src/tdef.h:591-688).                            */
+enum {
+  AHFGPU_PROF_R = 0, AHFGPU_PROF_NPART, AHFGPU_PROF_NVPART, AHFGPU_PROF_OVDENS,
+  AHFGPU_PROF_DENS, AHFGPU_PROF_V2_CIRC, AHFGPU_PROF_V_ESC2, AHFGPU_PROF_SIG_V,
+  AHFGPU_PROF_EKIN, AHFGPU_PROF_EPOT, AHFGPU_PROF_LX, AHFGPU_PROF_LY,
+  AHFGPU_PROF_LZ, AHFGPU_PROF_AXIS1, AHFGPU_PROF_E1X, AHFGPU_PROF_E1Y,
+  AHFGPU_PROF_E1Z, AHFGPU_PROF_AXIS2, AHFGPU_PROF_E2X, AHFGPU_PROF_E2Y,
+  AHFGPU_PROF_E2Z, AHFGPU_PROF_AXIS3, AHFGPU_PROF_E3X, AHFGPU_PROF_E3Y,
+  AHFGPU_PROF_E3Z, AHFGPU_PROF_NFIELDS
+};
+
+typedef struct {
+  uint64_t n_particles_in;   /* off[nhalo]                                    */
+  uint64_t n_kept;           /* member_off[nhalo]                             */
+  uint64_t n_retest;         /* particles routed to the FP64 re-test          */
+  uint64_t n_replay_halos;   /* halos finished by the exact sequential replay */
+  uint64_t n_key_ties;       /* equal radial keys met by the sort             */
+  uint64_t n_launches;       /* kernels launched by the call                  */
+  double   ms_device;        /* device time of the compute kernels (ms)       */
+  double   ms_total;         /* wall time of the whole call (ms)              */
+} ahfgpu_stats;
+
+/* Library-owned result; release with ahfgpu_result_free().                  */
+typedef struct {
+  int64_t      nhalo;
+  ahfgpu_halo *halo;         /* [nhalo]                                        */
+  uint64_t    *member_off;   /* [nhalo+1]                                      */
+  uint64_t    *member;       /* kept gidx (or entry index), radial order       */
+  uint64_t    *prof_off;     /* [nhalo+1], in bins                             */
+  double      *prof;         /* [prof_off[nhalo]][AHFGPU_PROF_NFIELDS]         */
+  ahfgpu_stats stats;
+  void        *priv;         /* library bookkeeping, do not touch              */
+} ahfgpu_result;
+
+/* ---- entry points -------------------------------------------------------- */
+
+/* Select and initialise a CUDA device (AHF's startrun-time set-up).  Safe to
+ * call more than once; a later call with another device re-initialises.     */
+int ahfgpu_init(int device);
+
+/* Release every device and host resource the library holds.                 */
+int ahfgpu_shutdown(void);
+
+/* Replaces the per-halo loop body of src/libahf/ahf_halos.c:504-510
+ * (ahf_halos_sfc_constructHalo, src/libahf/ahf_halos_sfc.c:118-169, minus its
+ * gather at :137).  Host batch in, host result out (copies are inside).     */
+int ahfgpu_construct_halos(const ahfgpu_params *params,
+                           const ahfgpu_batch  *batch,
+                           ahfgpu_result       *result,
+                           ahfgpu_mode          mode);
+
+/* Same stage with every pointer of `batch` already in device memory; the
+ * results stay on the device in library-owned buffers (valid until the next
+ * call or ahfgpu_shutdown) and are described by `dres` (device pointers,
+ * member_off/prof_off included).  `stream` is a cudaStream_t or NULL for the
+ * library's own stream.  Used when the caller keeps a snapshot resident.    */
+int ahfgpu_construct_halos_device(const ahfgpu_params *params,
+                                  const ahfgpu_batch  *batch,
+                                  ahfgpu_result       *dres,
+                                  ahfgpu_mode          mode,
+                                  void                *stream);
+
+/* Copy the device-resident result of the last _device call into a host
+ * result (library-owned host arrays; free with ahfgpu_result_free).          */
+int ahfgpu_fetch_result(ahfgpu_result *result);
+
+void ahfgpu_result_free(ahfgpu_result *result);
+
+/* Message of the last failure on this thread (empty when none); returns the
+ * untruncated length.                                                       */
+int ahfgpu_last_error(char *buf, size_t len);
+
+const char *ahfgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AHFGPU_H */

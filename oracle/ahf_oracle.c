@@ -1,0 +1,792 @@
+/*
+ * ahf_oracle.c -- CPU restatement of AHF's per-halo unbinding + property
+ * stage, used as the parity oracle of the GPU library.
+ *
+ * TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke()
+ * as the checker and by bench.py's CPU-baseline leg.  The product never
+ * calls it.
+ *
+ * Each function restates one reference routine (cited file:line, paths
+ * inside the AHF source tree) in the reference's own operation order, in
+ * FP64 with FP contraction off, so that results are bit-identical to the
+ * reference wherever the reference is deterministic.  Two routines of the
+ * reference are Numerical-Recipes code (indexx, jacobi); they are NOT
+ * restated: the radial sort here is a stable merge sort on (key, list
+ * position) and the 3x3 eigen-solver is a cyclic Jacobi written from the
+ * textbook rotation formulas.  Consequences: (i) exactly equal radial keys
+ * and exactly equal |mom|^2 among the innermost MINPART/2 particles are
+ * ordered by list position (the reference's order for such ties is that of
+ * its quicksort); (ii) eigenvectors agree with the reference up to sign.
+ */
+#include "ahf_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* src/param.h:125 and :124 (single-precision build), src/param.h:45       */
+#define OR_MACHINE_ZERO 5e-16
+#define OR_ZERO         1e-6
+#define OR_GRAV         4.3006485e-9
+/* src/libahf/ahf_halos.c:3985 FourPiThird with PI of src/libutility/utility.h */
+#define OR_PI           3.14159265358979323846264338
+/* src/param.h:26 AHF_Rmax_r2_NIGNORE with AHFparticle_Rmax_r2 on (define.h) */
+#define OR_NIGNORE      5
+#define OR_HIRES_W      1.0  /* src/param.h:16 AHF_HIRES_DM_WEIGHT */
+
+typedef struct {
+  const ahfgpu_params *p;
+  const ahfgpu_batch  *b;
+  double cx, cy, cz;
+  /* current member list: batch entry indices */
+  uint64_t *ipart;
+  uint64_t  npart;
+  /* outputs */
+  ahfgpu_halo out;
+  double     *prof;   /* [nbins][NFIELDS] */
+} halo_work;
+
+static inline double wgt(const ahfgpu_batch *b, uint64_t e)
+{
+  return b->w ? (double)b->w[e] : 1.0;
+}
+
+/* signed offset with both periodic wraps (ahf_halos.c:3505-3516) */
+static inline double wrap_s(double d)
+{
+  if (d > 0.5) d -= 1.0;
+  if (d < -0.5) d += 1.0;
+  return d;
+}
+
+/* fabs + single wrap (ahf_halos.c:3381-3389, 3838-3845) */
+static inline double wrap_a(double d)
+{
+  d = fabs(d);
+  if (d > 0.5) d -= 1.0;
+  return d;
+}
+
+static inline double sq(double a) { return a * a; }
+
+/* ------------------------------------------------------------------------
+ * sort_halo_particles, src/libahf/ahf_halos.c:5786-5894: key dR^2 with the
+ * signed wrap (:5816-5843), ascending (:5846), permute ipart (:5850-5856).
+ * Own stable merge sort; ties keep list order.
+ * ---------------------------------------------------------------------- */
+static uint64_t merge_sort_by_key(uint64_t n, const double *key, uint64_t *ord, uint64_t *tmp)
+{
+  uint64_t ties = 0;
+  for (uint64_t width = 1; width < n; width *= 2) {
+    for (uint64_t lo = 0; lo < n; lo += 2 * width) {
+      uint64_t mid = lo + width < n ? lo + width : n;
+      uint64_t hi = lo + 2 * width < n ? lo + 2 * width : n;
+      uint64_t i = lo, j = mid, k = lo;
+      while (i < mid && j < hi) {
+        if (key[ord[j]] < key[ord[i]]) tmp[k++] = ord[j++];
+        else tmp[k++] = ord[i++];
+      }
+      while (i < mid) tmp[k++] = ord[i++];
+      while (j < hi) tmp[k++] = ord[j++];
+    }
+    memcpy(ord, tmp, n * sizeof(uint64_t));
+  }
+  for (uint64_t i = 1; i < n; i++)
+    if (key[ord[i]] == key[ord[i - 1]]) ties++;
+  return ties;
+}
+
+static uint64_t sort_halo_particles(halo_work *h)
+{
+  const ahfgpu_batch *b = h->b;
+  uint64_t n = h->npart;
+  if (n < (uint64_t)h->p->MINPART) return 0;
+  double *key = (double *)malloc(n * sizeof(double));
+  uint64_t *ord = (uint64_t *)malloc(n * sizeof(uint64_t));
+  uint64_t *tmp = (uint64_t *)malloc(n * sizeof(uint64_t));
+  uint64_t *np = (uint64_t *)malloc(n * sizeof(uint64_t));
+  for (uint64_t i = 0; i < n; i++) {
+    uint64_t e = h->ipart[i];
+    double dX = wrap_s((double)b->x[e] - h->cx);
+    double dY = wrap_s((double)b->y[e] - h->cy);
+    double dZ = wrap_s((double)b->z[e] - h->cz);
+    key[i] = (sq(dX) + sq(dY)) + sq(dZ);
+    ord[i] = i;
+  }
+  uint64_t ties = merge_sort_by_key(n, key, ord, tmp);
+  for (uint64_t i = 0; i < n; i++) np[i] = h->ipart[ord[i]];
+  memcpy(h->ipart, np, n * sizeof(uint64_t));
+  free(key); free(ord); free(tmp); free(np);
+  h->out.flags |= AHFGPU_HALO_RAN_SORT;
+  return ties;
+}
+
+/* distance of a member, fabs form (identical value to the signed form) */
+static inline double member_dist(const halo_work *h, uint64_t e)
+{
+  const ahfgpu_batch *b = h->b;
+  double dX = wrap_a((double)b->x[e] - h->cx);
+  double dY = wrap_a((double)b->y[e] - h->cy);
+  double dZ = wrap_a((double)b->z[e] - h->cz);
+  return sqrt((sq(dX) + sq(dY)) + sq(dZ));
+}
+
+/* ------------------------------------------------------------------------
+ * rem_outsideRvir, src/libahf/ahf_halos.c:3687-3889 (AHFprofilerise off):
+ * walk outwards while ovdens >= ovlim; the first failing particle is kept
+ * (:3818-3861).  Phi0 reset on the first call (:3870-3871).
+ * ---------------------------------------------------------------------- */
+static void rem_outsideRvir(halo_work *h, int icall)
+{
+  const ahfgpu_params *p = h->p;
+  if (h->npart < (uint64_t)p->MINPART) return;
+  double ovdens_vir = p->ovlim;
+  uint64_t j = 0, nsph = 0;
+  double M = 0.0, R = -1.0, ov = 2 * ovdens_vir;
+  while (j < h->npart && ov >= ovdens_vir) {
+    uint64_t e = h->ipart[j];
+    M += wgt(h->b, e);
+    R = member_dist(h, e);
+    double V = 4. * OR_PI / 3. * (R * R * R);
+    ov = M / V * p->rho_fac / p->rho_vir;
+    nsph++;
+    j++;
+  }
+  h->npart = nsph;
+  h->out.M_vir = M;
+  h->out.R_vir = R;
+  h->out.ovdens = ov;
+  if (icall == 0) h->out.Phi0 = 0.0;
+  h->out.flags |= icall == 0 ? AHFGPU_HALO_RAN_RVIR0 : AHFGPU_HALO_RAN_RVIR1;
+}
+
+/* ------------------------------------------------------------------------
+ * rem_unbound, src/libahf/ahf_halos.c:3292-3607.
+ * ---------------------------------------------------------------------- */
+static void rem_unbound(halo_work *h)
+{
+  const ahfgpu_params *p = h->p;
+  const ahfgpu_batch *b = h->b;
+  if (h->npart < (uint64_t)p->MINPART) return;
+  double v2_tune = sq(p->VescTune);
+  uint64_t no_vbulk = (uint64_t)(p->MINPART / 2);
+  uint64_t nremove = 4;
+  int niter = 0;
+  double R_vir = 0.0;            /* reference: uninitialised until a bound particle */
+  uint64_t *bound = (uint64_t *)malloc((h->npart ? h->npart : 1) * sizeof(uint64_t));
+
+  h->out.flags |= AHFGPU_HALO_RAN_UNBIND;
+  while (nremove > 3) {
+    niter++;
+    /* Phi0 pass, :3343-3426 */
+    double I_now = 0.0, I_prev = 0.0, d_prev = 0.0, M_r = 0.0, Phi0 = 0.0, dist = 0.0;
+    for (uint64_t j = 0; j < h->npart; j++) {
+      uint64_t e = h->ipart[j];
+      M_r += wgt(b, e);
+      dist = member_dist(h, e);
+      if (dist > OR_MACHINE_ZERO) {
+        I_now = M_r / sq(dist);
+        double I_mid = (I_now + I_prev) / 2.;
+        double dr = dist - d_prev;
+        Phi0 += I_mid * dr;
+      }
+      d_prev = dist;
+      I_prev = I_now;
+    }
+    Phi0 += M_r / dist;                                /* :3423 */
+    h->out.Phi0 = Phi0;
+
+    /* bulk-velocity seed, :3441-3470 */
+    uint64_t js;
+    if (niter == 1) {
+      /* rank no_vbulk/2 (1-based) of float |mom|^2 among the innermost
+       * no_vbulk members; ties by list position. */
+      float m2[64];
+      uint64_t pos[64];
+      uint64_t nv = no_vbulk < 64 ? no_vbulk : 64;
+      for (uint64_t j = 0; j < nv; j++) {
+        uint64_t e = h->ipart[j];
+        float mx = b->vx[e], my = b->vy[e], mz = b->vz[e];
+        volatile float t = mx * mx;
+        t = t + my * my;
+        t = t + mz * mz;
+        m2[j] = t;
+        pos[j] = j;
+      }
+      for (uint64_t i = 1; i < nv; i++) {          /* stable insertion sort */
+        float kv = m2[i]; uint64_t kp = pos[i]; uint64_t k = i;
+        while (k > 0 && m2[k - 1] > kv) { m2[k] = m2[k - 1]; pos[k] = pos[k - 1]; k--; }
+        m2[k] = kv; pos[k] = kp;
+      }
+      js = pos[no_vbulk / 2 - 1];
+    } else {
+      js = 0;
+    }
+    uint64_t es = h->ipart[js];
+    double w0 = wgt(b, es);
+    double M_vel = w0;
+    double VXc = w0 * b->vx[es], VYc = w0 * b->vy[es], VZc = w0 * b->vz[es];
+
+    /* bound pass, :3478-3583 */
+    nremove = 0;
+    I_now = 0.0; I_prev = 0.0; d_prev = 0.0; M_r = 0.0;
+    double M_vir = 0.0, Phi = 0.0;
+    uint64_t nb = 0;
+    for (uint64_t j = 0; j < h->npart; j++) {
+      uint64_t e = h->ipart[j];
+      double weight = wgt(b, e);
+      M_r += weight;
+      double dX = wrap_s((double)b->x[e] - h->cx);
+      double dY = wrap_s((double)b->y[e] - h->cy);
+      double dZ = wrap_s((double)b->z[e] - h->cz);
+      dist = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+      double v_esc2;
+      if (dist > OR_MACHINE_ZERO) {
+        I_now = M_r / sq(dist);
+        double I_mid = (I_now + I_prev) / 2.;
+        double dr = dist - d_prev;
+        Phi += I_mid * dr;
+        v_esc2 = (2 * fabs(Phi - Phi0) * p->phi_fac);
+      } else {
+        v_esc2 = 1e30;
+      }
+      double VXp = (double)b->vx[e], VYp = (double)b->vy[e], VZp = (double)b->vz[e];
+      double dVX = (VXp - VXc / M_vel) * p->v_fac + p->Hubble * (dX) * p->r_fac;
+      double dVY = (VYp - VYc / M_vel) * p->v_fac + p->Hubble * (dY) * p->r_fac;
+      double dVZ = (VZp - VZc / M_vel) * p->v_fac + p->Hubble * (dZ) * p->r_fac;
+      double vel2 = (sq(dVX) + sq(dVY)) + sq(dVZ);
+      if (vel2 > v2_tune * v_esc2) {
+        nremove++;
+      } else {
+        M_vel += weight;
+        VXc += weight * b->vx[e];
+        VYc += weight * b->vy[e];
+        VZc += weight * b->vz[e];
+        bound[nb++] = e;
+        M_vir += weight;
+        R_vir = dist;
+      }
+      I_prev = I_now;
+      d_prev = dist;
+    }
+    memcpy(h->ipart, bound, nb * sizeof(uint64_t));
+    if (nb == 0) h->out.flags |= AHFGPU_HALO_NOBOUND;
+    h->npart = nb;
+    h->out.M_vir = M_vir;
+    h->out.R_vir = R_vir;
+    if (((double)(h->npart)) < ((double)(p->MINPART))) break;
+  }
+  h->out.niter = niter;
+  free(bound);
+}
+
+/* ------------------------------------------------------------------------
+ * Numerics used by HaloProfiles
+ * ---------------------------------------------------------------------- */
+
+/* smooth3, src/libutility/general.c:548-573 */
+static void smooth3(double *data, int64_t nbins, int nsmooth, double *tmp)
+{
+  if (nsmooth == 0 || nbins < 3) return;
+  for (int j = 0; j < nsmooth; j++) {
+    tmp[0] = (data[0] + data[1]) / 2.;
+    for (int64_t i = 1; i < nbins - 1; i++)
+      tmp[i] = (data[i - 1] + data[i] + data[i + 1]) / 3.;
+    tmp[nbins - 1] = (data[nbins - 1] + data[nbins - 2]) / 2.;
+    memcpy(data, tmp, (size_t)nbins * sizeof(double));
+  }
+}
+
+/* find_max, src/libutility/general.c:608-650: first strict maximum of the
+ * smoothed copy over [0, nbins-2]; the right-hand approach of the reference
+ * revisits only indices already scanned and never moves the pick.         */
+static void find_max(const double *x, const double *y_raw, int64_t nbins, int ismooth,
+                     double *x_max, double *y_max)
+{
+  double *y = (double *)malloc((size_t)(nbins > 0 ? nbins : 1) * sizeof(double));
+  double *tmp = (double *)malloc((size_t)(nbins > 0 ? nbins : 1) * sizeof(double));
+  memcpy(y, y_raw, (size_t)nbins * sizeof(double));
+  smooth3(y, nbins, ismooth, tmp);
+  double ymax = -10.0;
+  int64_t i0 = nbins - 1;
+  for (int64_t i = 0; i < nbins - 1; i++)
+    if (y[i] > ymax) { ymax = y[i]; i0 = i; }
+  int64_t i1 = i0;
+  for (int64_t i = (nbins - 1 + i0) / 2; i > i0; i--)
+    if (y[i] > ymax) { ymax = y[i]; i1 = i; }
+  *x_max = (x[i0] + x[i1]) / 2;
+  *y_max = (y_raw[i0] + y_raw[i1]) / 2;
+  free(y); free(tmp);
+}
+
+/* Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations
+ * (Golub & Van Loan, "Matrix Computations", sym.schur2 + cyclic sweep).
+ * On return d[k] are eigenvalues and column k of v the eigenvector.       */
+static void jacobi3(const double a_in[3][3], double d[3], double v[3][3])
+{
+  double a[3][3];
+  memcpy(a, a_in, sizeof(a));
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) v[i][j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 64; sweep++) {
+    double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+    if (off == 0.0) break;
+    for (int pp = 0; pp < 2; pp++) {
+      for (int qq = pp + 1; qq < 3; qq++) {
+        double apq = a[pp][qq];
+        if (apq == 0.0) continue;
+        double app = a[pp][pp], aqq = a[qq][qq];
+        /* negligible element relative to both diagonal entries */
+        if (sweep > 3 && fabs(app) + 100.0 * fabs(apq) == fabs(app) &&
+            fabs(aqq) + 100.0 * fabs(apq) == fabs(aqq)) {
+          a[pp][qq] = a[qq][pp] = 0.0;
+          continue;
+        }
+        double tau = (aqq - app) / (2.0 * apq);
+        double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+        double c = 1.0 / sqrt(1.0 + t * t);
+        double s = t * c;
+        /* A <- J^T A J with J the (pp,qq) rotation [c s; -s c] */
+        for (int k = 0; k < 3; k++) {
+          double akp = a[k][pp], akq = a[k][qq];
+          a[k][pp] = c * akp - s * akq;
+          a[k][qq] = s * akp + c * akq;
+        }
+        for (int k = 0; k < 3; k++) {
+          double apk = a[pp][k], aqk = a[qq][k];
+          a[pp][k] = c * apk - s * aqk;
+          a[qq][k] = s * apk + c * aqk;
+        }
+        a[pp][qq] = a[qq][pp] = 0.0;
+        for (int k = 0; k < 3; k++) {
+          double vkp = v[k][pp], vkq = v[k][qq];
+          v[k][pp] = c * vkp - s * vkq;
+          v[k][qq] = s * vkp + c * vkq;
+        }
+      }
+    }
+  }
+  for (int k = 0; k < 3; k++) d[k] = a[k][k];
+}
+
+/* get_axes, src/libutility/specific.c:135-178: eigenvalues descending
+ * (axis1 largest); column 0/1/2 of itensor = eigenvector of axis1/2/3.     */
+static void get_axes(double it[3][3], double *axis1, double *axis2, double *axis3)
+{
+  double d[3], v[3][3];
+  jacobi3((const double (*)[3])it, d, v);
+  int o[3] = {0, 1, 2};
+  for (int i = 1; i < 3; i++) {                 /* stable, descending */
+    int k = o[i], j = i;
+    while (j > 0 && d[o[j - 1]] < d[k]) { o[j] = o[j - 1]; j--; }
+    o[j] = k;
+  }
+  *axis1 = d[o[0]]; *axis2 = d[o[1]]; *axis3 = d[o[2]];
+  for (int c = 0; c < 3; c++)
+    for (int r = 0; r < 3; r++) it[r][c] = v[r][o[c]];
+}
+
+/* binning_parameter, src/libutility/specific.c:259-322 */
+static void binning_parameter(const halo_work *h, int *nbins, double *dist_min, double *dist_max)
+{
+  const ahfgpu_batch *b = h->b;
+  int nb = (int)(6.2 * (log10((double)h->npart)) - 3.5);
+  nb *= 1;
+  if (nb < 2) nb = 2;
+  *nbins = nb;
+  long npart = (long)floor(((double)h->p->MINPART / 10.) + 0.5);
+  *dist_min = -1.0;
+  while (npart < (long)h->npart - 1 && *dist_min < OR_MACHINE_ZERO) {
+    uint64_t e = h->ipart[npart];
+    double dX = fabs(b->x[e] - h->cx), dY = fabs(b->y[e] - h->cy), dZ = fabs(b->z[e] - h->cz);
+    if (dX > 0.5) dX = 1.0 - dX;
+    if (dY > 0.5) dY = 1.0 - dY;
+    if (dZ > 0.5) dZ = 1.0 - dZ;
+    *dist_min = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+    npart++;
+  }
+  uint64_t e = h->ipart[h->npart - 1];
+  double dX = fabs(b->x[e] - h->cx), dY = fabs(b->y[e] - h->cy), dZ = fabs(b->z[e] - h->cz);
+  if (dX > 0.5) dX = 1.0 - dX;
+  if (dY > 0.5) dY = 1.0 - dY;
+  if (dZ > 0.5) dZ = 1.0 - dZ;
+  *dist_max = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+  if (*dist_min < OR_MACHINE_ZERO) *dist_min = *dist_max / 2.;
+}
+
+/* calc_cNFW, src/libutility/specific.c:2041-2072 (bisection on [2.2,100]) */
+static double cnfw_root(double c, double v2r) { return 0.216 * c / (log(1 + c) - c / (1 + c)) - v2r; }
+static double calc_cNFW(double V2_max, double V2_vir)
+{
+  double r = V2_max / V2_vir;
+  if (r <= 1 || r > 5.9) return -1;
+  double a = 2.2, bb = 100, c;
+  while (bb - a > 1e-3) {
+    c = (a + bb) / 2;
+    if (cnfw_root(a, r) * cnfw_root(c, r) > 0) a = c; else bb = c;
+  }
+  return (a + bb) / 2.0;
+}
+
+/* calc_R1 / calc_cR1, src/libutility/specific.c:1977-2018 */
+static double cr1_root(double c, double R1)
+{
+  return (c - 2.0 * log(1.0 + c) + c / (1.0 + c)) / (c * (log(1.0 + c) - c / (1.0 + c))) - R1;
+}
+static double calc_R1(const double *prof, int nbins)
+{
+#define PR(i, f) prof[(size_t)(i) * AHFGPU_PROF_NFIELDS + (f)]
+  double r0h = PR(0, AHFGPU_PROF_R) / 2.0;
+  double R1 = (r0h * r0h * r0h) * PR(0, AHFGPU_PROF_DENS) * (PR(0, AHFGPU_PROF_R));
+  for (int i = 1; i < nbins; i++) {
+    double rmid = (PR(i, AHFGPU_PROF_R) + PR(i - 1, AHFGPU_PROF_R)) / 2.0;
+    double dr = PR(i, AHFGPU_PROF_R) - PR(i - 1, AHFGPU_PROF_R);
+    R1 += (rmid * rmid * rmid) * PR(i, AHFGPU_PROF_DENS) * dr;
+  }
+#undef PR
+  return 4 * OR_PI * R1;
+}
+static double calc_cR1(double R1)
+{
+  if (R1 <= 0.19 || 0.585 <= R1) return -1.0;
+  double a = 1.0, bb = 500.0, c;
+  while (bb - a > 1e-3) {
+    c = (a + bb) / 2;
+    if (cr1_root(a, R1) * cr1_root(c, R1) > 0) a = c; else bb = c;
+  }
+  return (a + bb) / 2.0;
+}
+
+/* calc_lambdaE, src/libahf/ahf_halos.c:3937-3953 */
+static double calc_lambdaE(const ahfgpu_params *p, double absL, double Mhalo, double Mass,
+                           double Ekin, double Epot)
+{
+  double t1 = sqrt(p->m_fac * Mhalo);
+  t1 = t1 * t1 * t1;
+  double t2 = Ekin * p->m_fac * (p->v_fac * p->v_fac);
+  double t3 = Epot * p->m_fac * p->phi_fac;
+  t2 = fabs(t2 + t3);
+  t2 = sqrt(t2);
+  t1 = t2 / t1;
+  t2 = p->m_fac * p->r_fac * p->v_fac * absL;
+  t2 = t2 / (p->m_fac * Mass);
+  t3 = t1 * t2;
+  return t3 / OR_GRAV;
+}
+
+/* ------------------------------------------------------------------------
+ * HaloProfiles, src/libahf/ahf_halos.c:3961-5261 (default flags:
+ * AHFparticle_Rmax_r2, no GAS_PARTICLES, no AHFshellshape).
+ * ---------------------------------------------------------------------- */
+static void HaloProfiles(halo_work *h)
+{
+  const ahfgpu_params *p = h->p;
+  const ahfgpu_batch *b = h->b;
+  if (h->npart < (uint64_t)p->MINPART) return;
+  const double FourPiThird = 4. * OR_PI / 3.;
+  int nbins;
+  double dist_min, dist_max;
+  binning_parameter(h, &nbins, &dist_min, &dist_max);
+  double ldist_min = log10(dist_min), ldist_max = log10(dist_max);
+  double ldr = (ldist_max - ldist_min) / (double)nbins;
+  h->prof = (double *)calloc((size_t)nbins * AHFGPU_PROF_NFIELDS, sizeof(double));
+  h->out.nbins = nbins;
+  uint64_t n = h->npart;
+  double *Vcirc2 = (double *)calloc(n, sizeof(double));
+  double *dens_r2 = (double *)calloc(n, sizeof(double));
+  double *ovdens = (double *)calloc(n, sizeof(double));
+  double *radius = (double *)calloc(n, sizeof(double));
+
+  double Phi0 = h->out.Phi0, Phi = 0.0, pre_dist = 0.0, I_prev = 0.0, I_now = 0.0;
+  uint64_t npart = 0;
+  double M_prev = 0, V_prev = 0.0, M_sphere_prev = 0.0, prev_dist = 0.0;
+  double M_sphere = 0.0, VXc = 0.0, VYc = 0.0, VZc = 0.0;
+  double a11 = 0, a22 = 0, a33 = 0, a12 = 0, a13 = 0, a23 = 0;
+  double sig_v = 0, Lx = 0, Ly = 0, Lz = 0, CoM[3] = {0, 0, 0};
+  double Epot = 0, Ekin = 0, Emin = 1e30, v_esc2 = 0.0;
+  int64_t mb = -1;
+  double M_hires = 0.0, M_lores = 0.0;
+  const double Xc = h->cx, Yc = h->cy, Zc = h->cz;
+  uint64_t jpart = 0;
+  double cur_dist = -1.0;
+
+  for (int ibin = 0; ibin < nbins; ibin++) {
+    double lcur_rad = ldist_min + ((double)ibin + 1) * ldr;
+    double cur_rad = pow(10., lcur_rad);
+    if (ibin == nbins - 1) cur_rad = dist_max + OR_ZERO;
+    while (cur_dist < cur_rad && jpart < n) {
+      uint64_t e = h->ipart[jpart];
+      npart++;
+      double weight = wgt(b, e);
+      if (b->w) {
+        if (fabs(weight - OR_HIRES_W) < OR_ZERO) M_hires += weight;
+        else if (weight > OR_HIRES_W) M_lores += weight;
+      } else {
+        M_hires += weight;
+      }
+      M_sphere += weight;
+      double dX = wrap_s((double)b->x[e] - Xc);
+      double dY = wrap_s((double)b->y[e] - Yc);
+      double dZ = wrap_s((double)b->z[e] - Zc);
+      cur_dist = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+      CoM[0] += weight * (Xc + dX);
+      CoM[1] += weight * (Yc + dY);
+      CoM[2] += weight * (Zc + dZ);
+      a11 += weight * dX * dX;
+      a22 += weight * dY * dY;
+      a33 += weight * dZ * dZ;
+      a12 += weight * dX * dY;
+      a13 += weight * dX * dZ;
+      a23 += weight * dY * dZ;
+      VXc += weight * b->vx[e];
+      VYc += weight * b->vy[e];
+      VZc += weight * b->vz[e];
+      double VXp = (double)b->vx[e], VYp = (double)b->vy[e], VZp = (double)b->vz[e];
+      double dVX = (VXp - VXc / M_sphere);
+      double dVY = (VYp - VYc / M_sphere);
+      double dVZ = (VZp - VZc / M_sphere);
+      Lx += weight * (dY * dVZ - dZ * dVY);
+      Ly += weight * (dZ * dVX - dX * dVZ);
+      Lz += weight * (dX * dVY - dY * dVX);
+      dVX += p->Hubble * dX * p->r_fac / p->v_fac;
+      dVY += p->Hubble * dY * p->r_fac / p->v_fac;
+      dVZ += p->Hubble * dZ * p->r_fac / p->v_fac;
+      double Tpart = weight * ((sq(dVX) + sq(dVY)) + sq(dVZ));
+      double Upart;
+      if (cur_dist > OR_MACHINE_ZERO) {
+        I_now = M_sphere / sq(cur_dist);
+        double I_mid = (I_now + I_prev) / 2.;
+        Phi += I_mid * (cur_dist - pre_dist);
+        Upart = (Phi - Phi0) * weight;
+      } else {
+        Upart = (Phi - Phi0) * weight;
+      }
+      v_esc2 = 2 * fabs(Upart) / weight;
+      I_prev = I_now;
+      pre_dist = cur_dist;
+      Epot += Upart;
+      sig_v += Tpart;
+      Ekin += Tpart;
+      double Epart = (0.5 * Tpart + Upart);
+      if (Epart < Emin) { Emin = Epart; mb = (int64_t)e; }
+      radius[jpart] = cur_dist;
+      ovdens[jpart] = M_sphere / (FourPiThird * (cur_dist * cur_dist * cur_dist));
+      double dV = FourPiThird * ((cur_dist * cur_dist * cur_dist) - (prev_dist * prev_dist * prev_dist));
+      double dM = M_sphere - M_sphere_prev;
+      Vcirc2[jpart] = M_sphere / cur_dist;
+      M_sphere_prev = M_sphere;
+      double rm = (cur_dist + prev_dist) / 2.;
+      dens_r2[jpart] = dM / dV * (rm * rm);
+      prev_dist = cur_dist;
+      jpart++;
+    }
+    double Volume = FourPiThird * (cur_rad * cur_rad * cur_rad);
+    double dM = M_sphere - M_prev;
+    double dV = Volume - V_prev;
+    double itensor[3][3], axis1, axis2, axis3;
+    if (npart > 10) {
+      itensor[0][0] = a11; itensor[1][1] = a22; itensor[2][2] = a33;
+      itensor[0][1] = a12; itensor[1][0] = a12;
+      itensor[0][2] = a13; itensor[2][0] = a13;
+      itensor[1][2] = a23; itensor[2][1] = a23;
+      get_axes(itensor, &axis1, &axis2, &axis3);
+    } else {
+      memset(itensor, 0, sizeof(itensor));
+      axis1 = 1; axis2 = 0; axis3 = 0;
+    }
+    double *row = h->prof + (size_t)ibin * AHFGPU_PROF_NFIELDS;
+    row[AHFGPU_PROF_R] = cur_rad;
+    row[AHFGPU_PROF_NPART] = (double)npart;
+    row[AHFGPU_PROF_NVPART] = M_sphere;
+    row[AHFGPU_PROF_OVDENS] = M_sphere / Volume;
+    row[AHFGPU_PROF_DENS] = dV > 0 ? dM / dV : 0.0;
+    row[AHFGPU_PROF_V2_CIRC] = M_sphere / cur_rad;
+    row[AHFGPU_PROF_V_ESC2] = v_esc2;
+    row[AHFGPU_PROF_SIG_V] = sqrt(sig_v / M_sphere);
+    row[AHFGPU_PROF_EKIN] = 0.5 * Ekin;
+    row[AHFGPU_PROF_EPOT] = 0.5 * Epot;
+    row[AHFGPU_PROF_LX] = Lx;
+    row[AHFGPU_PROF_LY] = Ly;
+    row[AHFGPU_PROF_LZ] = Lz;
+    row[AHFGPU_PROF_E1X] = itensor[0][0];
+    row[AHFGPU_PROF_E1Y] = itensor[1][0];
+    row[AHFGPU_PROF_E1Z] = itensor[2][0];
+    row[AHFGPU_PROF_E2X] = itensor[0][1];
+    row[AHFGPU_PROF_E2Y] = itensor[1][1];
+    row[AHFGPU_PROF_E2Z] = itensor[2][1];
+    row[AHFGPU_PROF_E3X] = itensor[0][2];
+    row[AHFGPU_PROF_E3Y] = itensor[1][2];
+    row[AHFGPU_PROF_E3Z] = itensor[2][2];
+    row[AHFGPU_PROF_AXIS1] = 1.0;
+    if (axis1 > 0.) {
+      row[AHFGPU_PROF_AXIS2] = sqrt(axis2 / axis1);
+      row[AHFGPU_PROF_AXIS3] = sqrt(axis3 / axis1);
+    } else {
+      row[AHFGPU_PROF_AXIS2] = 0.0;
+      row[AHFGPU_PROF_AXIS3] = 0.0;
+    }
+    M_prev = M_sphere;
+    V_prev = Volume;
+  }
+  for (int k = 0; k < 3; k++) CoM[k] = fmod(CoM[k] / M_sphere + 1., 1.);
+
+  double x_max, y_max, r2, R_max;
+  int64_t np5 = (int64_t)n - OR_NIGNORE;
+  find_max(radius + OR_NIGNORE, dens_r2 + OR_NIGNORE, np5, 3, &x_max, &y_max);
+  r2 = x_max;
+  find_max(radius + OR_NIGNORE, Vcirc2 + OR_NIGNORE, np5, 1, &x_max, &y_max);
+  R_max = x_max;
+  int64_t ib = 0;
+  while (radius[ib] < x_max && ib < (int64_t)n - 1) ib++;
+  double M_max = ovdens[ib] * FourPiThird * (radius[ib] * radius[ib] * radius[ib]);
+  double V_max = M_max / R_max;
+  free(ovdens); free(Vcirc2); free(radius); free(dens_r2);
+
+  const double *last = h->prof + (size_t)(nbins - 1) * AHFGPU_PROF_NFIELDS;
+  Lx = last[AHFGPU_PROF_LX]; Ly = last[AHFGPU_PROF_LY]; Lz = last[AHFGPU_PROF_LZ];
+  double absAngMom = sqrt((sq(Lx) + sq(Ly)) + sq(Lz));
+  ahfgpu_halo *o = &h->out;
+  o->M_vir = M_sphere;
+  o->vel[0] = VXc / M_sphere; o->vel[1] = VYc / M_sphere; o->vel[2] = VZc / M_sphere;
+  o->R_max = R_max;
+  o->V2_max = V_max;
+  o->r2 = r2;
+  o->sigV = last[AHFGPU_PROF_SIG_V];
+  o->v_esc2 = last[AHFGPU_PROF_V_ESC2];
+  o->Ekin = last[AHFGPU_PROF_EKIN];
+  o->Epot = last[AHFGPU_PROF_EPOT];
+  o->axis[0] = last[AHFGPU_PROF_AXIS1]; o->axis[1] = last[AHFGPU_PROF_AXIS2]; o->axis[2] = last[AHFGPU_PROF_AXIS3];
+  o->E1[0] = last[AHFGPU_PROF_E1X]; o->E1[1] = last[AHFGPU_PROF_E1Y]; o->E1[2] = last[AHFGPU_PROF_E1Z];
+  o->E2[0] = last[AHFGPU_PROF_E2X]; o->E2[1] = last[AHFGPU_PROF_E2Y]; o->E2[2] = last[AHFGPU_PROF_E2Z];
+  o->E3[0] = last[AHFGPU_PROF_E3X]; o->E3[1] = last[AHFGPU_PROF_E3Y]; o->E3[2] = last[AHFGPU_PROF_E3Z];
+  if (absAngMom > 0) {
+    o->AngMom[0] = Lx / absAngMom; o->AngMom[1] = Ly / absAngMom; o->AngMom[2] = Lz / absAngMom;
+    o->lambda = absAngMom / o->M_vir / sqrt(2. * o->M_vir * o->R_vir);
+    o->lambda *= p->v_fac * sqrt(p->r_fac / (OR_GRAV * p->m_fac));
+    o->lambdaE = calc_lambdaE(p, absAngMom, o->M_vir, o->M_vir, o->Ekin, o->Epot);
+  } else {
+    o->AngMom[0] = o->AngMom[1] = o->AngMom[2] = 0.0;
+    o->lambda = 0.0;
+    o->lambdaE = 0.0;
+  }
+  o->cNFW = calc_cNFW(o->V2_max, o->M_vir / o->R_vir);
+  o->R1 = calc_R1(h->prof, nbins) / o->M_vir / o->R_vir;
+  o->cR1 = calc_cR1(o->R1);
+  {
+    const double *pl = h->prof + (size_t)(nbins - 2) * AHFGPU_PROF_NFIELDS;
+    double Ts = 2.0 * (last[AHFGPU_PROF_EKIN] - pl[AHFGPU_PROF_EKIN]);
+    double frad = fabs(pl[AHFGPU_PROF_R] / last[AHFGPU_PROF_R]);
+    o->SurfP = -0.125 * ((1. + frad) * (1. + frad) * (1. + frad)) / (1. - (frad * frad * frad)) * Ts;
+  }
+  o->fMhires = M_hires > 0 ? M_hires / (M_hires + M_lores) : 0.0;
+  if (mb >= 0) {
+    double dX = fabs(b->x[mb] - Xc), dY = fabs(b->y[mb] - Yc), dZ = fabs(b->z[mb] - Zc);
+    if (dX > 0.5) dX -= 1.0;
+    if (dY > 0.5) dY -= 1.0;
+    if (dZ > 0.5) dZ -= 1.0;
+    o->mbp_offset = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+    o->pos_mbp[0] = b->x[mb]; o->pos_mbp[1] = b->y[mb]; o->pos_mbp[2] = b->z[mb];
+    o->vel_mbp[0] = b->vx[mb]; o->vel_mbp[1] = b->vy[mb]; o->vel_mbp[2] = b->vz[mb];
+  } else {
+    o->mbp_offset = -1.0;
+    o->flags |= AHFGPU_HALO_NO_MBP;
+  }
+  {
+    double dX = fabs(CoM[0] - Xc), dY = fabs(CoM[1] - Yc), dZ = fabs(CoM[2] - Zc);
+    if (dX > 0.5) dX -= 1.0;
+    if (dY > 0.5) dY -= 1.0;
+    if (dZ > 0.5) dZ -= 1.0;
+    o->com_offset = sqrt((sq(dX) + sq(dY)) + sq(dZ));
+  }
+  o->pos_com[0] = CoM[0]; o->pos_com[1] = CoM[1]; o->pos_com[2] = CoM[2];
+  o->flags |= AHFGPU_HALO_RAN_PROFILE;
+}
+
+/* ahf_halos_sfc_constructHalo minus the gather, src/libahf/ahf_halos_sfc.c:118-169 */
+static uint64_t construct_halo(halo_work *h)
+{
+  uint64_t ties = 0;
+  if (h->npart == 0) { h->out.flags |= AHFGPU_HALO_EMPTY; return 0; }
+  ties = sort_halo_particles(h);
+  rem_outsideRvir(h, 0);
+  rem_unbound(h);
+  rem_outsideRvir(h, 1);
+  HaloProfiles(h);
+  h->out.npart = h->npart;
+  return ties;
+}
+
+int ahforacle_max_threads(void)
+{
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int ahforacle_construct_halos(const ahfgpu_params *params, const ahfgpu_batch *batch,
+                              ahfgpu_result *res, int nthreads)
+{
+  if (!params || !batch || !res || batch->nhalo < 0 || !batch->off) return AHFGPU_ERR_INVALID;
+  if (params->MINPART < 4) return AHFGPU_ERR_INVALID;
+  int64_t nh = batch->nhalo;
+  memset(res, 0, sizeof(*res));
+  res->nhalo = nh;
+  halo_work *hw = (halo_work *)calloc((size_t)(nh > 0 ? nh : 1), sizeof(halo_work));
+  if (!hw) return AHFGPU_ERR_OOM;
+  uint64_t ties = 0;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads) reduction(+:ties)
+#endif
+  for (int64_t i = 0; i < nh; i++) {
+    halo_work *h = &hw[i];
+    h->p = params;
+    h->b = batch;
+    h->cx = batch->cx[i]; h->cy = batch->cy[i]; h->cz = batch->cz[i];
+    uint64_t o0 = batch->off[i], o1 = batch->off[i + 1];
+    h->npart = o1 - o0;
+    h->ipart = (uint64_t *)malloc((h->npart ? h->npart : 1) * sizeof(uint64_t));
+    for (uint64_t j = 0; j < h->npart; j++) h->ipart[j] = o0 + j;
+    ties += construct_halo(h);
+  }
+  /* pack */
+  res->halo = (ahfgpu_halo *)calloc((size_t)(nh > 0 ? nh : 1), sizeof(ahfgpu_halo));
+  res->member_off = (uint64_t *)calloc((size_t)nh + 1, sizeof(uint64_t));
+  res->prof_off = (uint64_t *)calloc((size_t)nh + 1, sizeof(uint64_t));
+  for (int64_t i = 0; i < nh; i++) {
+    res->member_off[i + 1] = res->member_off[i] + hw[i].npart;
+    res->prof_off[i + 1] = res->prof_off[i] + (uint64_t)hw[i].out.nbins;
+  }
+  res->member = (uint64_t *)malloc((res->member_off[nh] ? res->member_off[nh] : 1) * sizeof(uint64_t));
+  res->prof = (double *)malloc((res->prof_off[nh] ? res->prof_off[nh] : 1) * AHFGPU_PROF_NFIELDS * sizeof(double));
+  for (int64_t i = 0; i < nh; i++) {
+    halo_work *h = &hw[i];
+    h->out.npart = h->npart;
+    res->halo[i] = h->out;
+    for (uint64_t j = 0; j < h->npart; j++)
+      res->member[res->member_off[i] + j] = batch->gidx ? batch->gidx[h->ipart[j]] : h->ipart[j];
+    if (h->out.nbins)
+      memcpy(res->prof + res->prof_off[i] * AHFGPU_PROF_NFIELDS, h->prof,
+             (size_t)h->out.nbins * AHFGPU_PROF_NFIELDS * sizeof(double));
+    free(h->ipart);
+    free(h->prof);
+  }
+  free(hw);
+  res->stats.n_particles_in = nh ? batch->off[nh] : 0;
+  res->stats.n_kept = res->member_off[nh];
+  res->stats.n_key_ties = ties;
+  return AHFGPU_OK;
+}
+
+void ahforacle_result_free(ahfgpu_result *r)
+{
+  if (!r) return;
+  free(r->halo); free(r->member_off); free(r->member); free(r->prof_off); free(r->prof);
+  memset(r, 0, sizeof(*r));
+}

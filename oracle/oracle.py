@@ -1,0 +1,93 @@
+"""Python loader for the parity oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() (as the checker) and bench.py's CPU
+baseline leg import this module.  It loads
+
+  oracle/_build/libahforacle.so   the C restatement (ahf_oracle.c), and
+  oracle/_ref/libahfref[_mm].so   the reference's own routines driven by
+                                  ref_harness.c (only where they were built)
+
+and returns ahf_gb300.abi.HostResult objects, the same shape the GPU library
+returns.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+from ahf_gb300.abi import HostResult, Params, Result, make_batch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIBS: dict = {}
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the restatement (and the reference harness when the reference
+    tree is present and `ref` is not False)."""
+    targets = ["oracle"]
+    refdir = os.environ.get("AHF_REFERENCE", "/root/reference")
+    if ref is not False and os.path.isfile(os.path.join(refdir, "src/libahf/ahf_halos.c")):
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={refdir}", *targets], check=True)
+
+
+def _load(path: str, prefix: str):
+    if path in _LIBS:
+        return _LIBS[path]
+    lib = C.CDLL(path)
+    fn = getattr(lib, f"{prefix}_construct_halos")
+    fn.argtypes = [C.POINTER(Params), C.c_void_p, C.POINTER(Result), C.c_int]
+    fn.restype = C.c_int
+    fr = getattr(lib, f"{prefix}_result_free")
+    fr.argtypes = [C.POINTER(Result)]
+    fr.restype = None
+    _LIBS[path] = (lib, fn, fr)
+    return _LIBS[path]
+
+
+def oracle_path() -> str:
+    return os.path.join(HERE, "_build", "libahforacle.so")
+
+
+def ref_path(multimass: bool) -> str:
+    return os.path.join(HERE, "_ref", "libahfref_mm.so" if multimass else "libahfref.so")
+
+
+def have_ref(multimass: bool = False) -> bool:
+    return os.path.isfile(ref_path(multimass))
+
+
+def _run(path, prefix, params, lists, nthreads):
+    lib, fn, fr = _load(path, prefix)
+    b, keep = make_batch(lists)
+    r = Result()
+    rc = fn(C.byref(params), C.cast(C.pointer(b), C.c_void_p), C.byref(r), int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"{prefix}_construct_halos failed: {rc}")
+    try:
+        return HostResult(r)
+    finally:
+        fr(C.byref(r))
+        del keep
+
+
+def run_oracle(params, lists, nthreads: int = 1) -> HostResult:
+    """The C restatement, `nthreads` OpenMP threads (<=0: all)."""
+    if not os.path.isfile(oracle_path()):
+        build(ref=False)
+    return _run(oracle_path(), "ahforacle", params, lists, nthreads)
+
+
+def run_reference(params, lists, nthreads: int = 1) -> HostResult:
+    """The reference's own routines (needs oracle/_ref built here)."""
+    mm = lists.w is not None
+    if not have_ref(mm):
+        raise FileNotFoundError(ref_path(mm))
+    return _run(ref_path(mm), "ahfref", params, lists, nthreads)
+
+
+def max_threads() -> int:
+    lib, _, _ = _load(oracle_path(), "ahforacle")
+    lib.ahforacle_max_threads.restype = C.c_int
+    return int(lib.ahforacle_max_threads())
