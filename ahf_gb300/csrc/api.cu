@@ -1,0 +1,574 @@
+// api.cu -- the extern "C" boundary (include/ahfgpu.h) of the GB300
+// unbinding + halo-property stage: device set-up, batch validation and
+// planning, work-space management, kernel launches, result packing and the
+// copies to and from the host.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace ahfgpu {
+size_t fp64_smem_bytes();
+void launch_fp64(const DevParams& P, const DevBatch& B, const Work& W, int grid, int single, cudaStream_t st);
+int fp64_max_blocks_per_sm();
+}  // namespace ahfgpu
+
+using namespace ahfgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(e_ == cudaErrorMemoryAllocation ? AHFGPU_ERR_OOM : AHFGPU_ERR_CUDA,    \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+// growable device buffer
+struct DBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  int ensure(size_t bytes) {
+    if (bytes <= cap) return AHFGPU_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 8, 256);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(AHFGPU_ERR_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+    }
+    cap = want;
+    return AHFGPU_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct Ctx {
+  bool init = false;
+  int device = -1;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int fp64_bps = 1, fp32c_bps = 1;
+  // inputs copied from the host (host API)
+  DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
+  // work space
+  DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
+  DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
+  // packed results (device)
+  DBuf member_off, member, prof_off, prof;
+  // last device result description
+  int64_t last_nhalo = -1;
+  uint64_t last_nkept = 0, last_nbins = 0;
+  ahfgpu_stats last_stats{};
+};
+
+Ctx g;
+
+// ---------------------------------------------------------------------------
+// small packing kernels
+
+__global__ void k_scan_counts(const ahfgpu_halo* halo, int64_t nh, int which, uint64_t* out) {
+  // single block: exclusive scan of npart (which=0) or nbins (which=1)
+  __shared__ unsigned long long part[1024];
+  unsigned long long carry = 0;
+  for (int64_t base = 0; base < nh; base += blockDim.x) {
+    int64_t i = base + threadIdx.x;
+    unsigned long long v = 0;
+    if (i < nh) v = which == 0 ? halo[i].npart : (unsigned long long)halo[i].nbins;
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+      unsigned long long t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+      __syncthreads();
+      part[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nh) out[i + 1] = carry + part[threadIdx.x];
+    unsigned long long tot = part[blockDim.x - 1];
+    __syncthreads();
+    carry += tot;
+  }
+  if (threadIdx.x == 0) out[0] = 0;
+}
+
+__global__ void k_pack_members(const ahfgpu_halo* halo, const uint64_t* off, const uint64_t* stage,
+                               const uint64_t* moff, uint64_t* member, int64_t nh) {
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t h = warp; h < nh; h += nw) {
+    uint64_t n = halo[h].npart, src = off[h], dst = moff[h];
+    for (uint64_t i = lane; i < n; i += 32) member[dst + i] = stage[src + i];
+  }
+}
+
+__global__ void k_pack_prof(const ahfgpu_halo* halo, const uint64_t* cap_off, const double* stage,
+                            const uint64_t* poff, double* prof, int64_t nh) {
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t h = warp; h < nh; h += nw) {
+    uint64_t nb = (uint64_t)halo[h].nbins;
+    uint64_t cnt = nb * AHFGPU_PROF_NFIELDS;
+    const double* s = stage + cap_off[h] * AHFGPU_PROF_NFIELDS;
+    double* d = prof + poff[h] * AHFGPU_PROF_NFIELDS;
+    for (uint64_t i = lane; i < cnt; i += 32) d[i] = s[i];
+  }
+}
+
+// min / max of the weights (exactness check of FP64 mass prefixes)
+__global__ void k_weight_range(const float* w, uint64_t n, float* out) {
+  float mn = INFINITY, mx = 0.f;
+  int bad = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    float v = w[i];
+    if (!(v > 0.f) || !isfinite(v)) bad = 1;
+    else { mn = fminf(mn, v); mx = fmaxf(mx, v); }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin((int*)&out[0], __float_as_int(mn));   // positive floats order as ints
+    atomicMax((int*)&out[1], __float_as_int(mx));
+    if (bad) atomicMax((int*)&out[2], 1);
+  }
+}
+
+__global__ void k_init_wred(float* out) {
+  out[0] = INFINITY;
+  out[1] = 0.f;
+  ((int*)out)[2] = 0;
+}
+
+int ensure_init() {
+  if (!g.init) return fail(AHFGPU_ERR_STATE, "ahfgpu_init() has not been called");
+  CK(cudaSetDevice(g.device));
+  return AHFGPU_OK;
+}
+
+int nbins_cap(uint64_t n, int64_t minpart) {
+  if (n < (uint64_t)minpart || n == 0) return 0;
+  int nb = (int)(6.2 * log10((double)n) - 3.5);
+  nb = std::max(2, nb) + 1;            // +1: device log10 may differ by an ulp
+  return std::min(nb, kMaxBins);
+}
+
+struct Plan {
+  int64_t nhalo = 0;
+  uint64_t N = 0, maxn = 0, nbins_total = 0;
+  std::vector<int32_t> queue;
+  std::vector<uint64_t> prof_cap_off;
+};
+
+int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, Plan& pl) {
+  if (!p) return fail(AHFGPU_ERR_INVALID, "params is NULL");
+  if (p->MINPART < 4) return fail(AHFGPU_ERR_INVALID, "MINPART must be >= 4 (got %lld)", (long long)p->MINPART);
+  if (!(p->VescTune > 0) || !(p->rho_vir > 0) || !(p->v_fac > 0))
+    return fail(AHFGPU_ERR_INVALID, "non-positive VescTune, rho_vir or v_fac");
+  if (nh < 0) return fail(AHFGPU_ERR_INVALID, "nhalo < 0");
+  if (nh > 0x7fffffff) return fail(AHFGPU_ERR_CAPACITY, "nhalo %lld exceeds 2^31-1", (long long)nh);
+  pl.nhalo = nh;
+  if (nh == 0) return AHFGPU_OK;
+  if (!off) return fail(AHFGPU_ERR_INVALID, "off is NULL");
+  if (off[0] != 0) return fail(AHFGPU_ERR_INVALID, "off[0] != 0");
+  pl.prof_cap_off.assign(nh + 1, 0);
+  for (int64_t h = 0; h < nh; h++) {
+    if (off[h + 1] < off[h]) return fail(AHFGPU_ERR_INVALID, "off not monotone at halo %lld", (long long)h);
+    uint64_t n = off[h + 1] - off[h];
+    if (n > 0xffffffffull) return fail(AHFGPU_ERR_CAPACITY, "halo %lld has %llu > 2^32-1 particles", (long long)h,
+                                       (unsigned long long)n);
+    pl.maxn = std::max(pl.maxn, n);
+    pl.prof_cap_off[h + 1] = pl.prof_cap_off[h] + (uint64_t)nbins_cap(n, p->MINPART);
+  }
+  pl.N = off[nh];
+  pl.nbins_total = pl.prof_cap_off[nh];
+  pl.queue.resize(nh);
+  std::iota(pl.queue.begin(), pl.queue.end(), 0);
+  std::stable_sort(pl.queue.begin(), pl.queue.end(),
+                   [&](int32_t a, int32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  return AHFGPU_OK;
+}
+
+int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
+  const uint64_t N = std::max<uint64_t>(pl.N, 1);
+  int rc;
+#define EN(buf, bytes) if ((rc = (buf).ensure(bytes)) != AHFGPU_OK) return rc
+  EN(g.keyA, N * 8); EN(g.keyB, N * 8); EN(g.idxA, N * 4); EN(g.idxB, N * 4);
+  EN(g.sdx, N * 8); EN(g.sdy, N * 8); EN(g.sdz, N * 8); EN(g.sd, N * 8);
+  EN(g.svx, N * 4); EN(g.svy, N * 4); EN(g.svz, N * 4); EN(g.sw, N * 4);
+  EN(g.seid, N * 4); EN(g.phi, N * 8); EN(g.flag, N); EN(g.nflag, N);
+  EN(g.pa, N * 8); EN(g.pb, N * 8); EN(g.pc, N * 8); EN(g.pd, N * 8);
+  EN(g.stack, (size_t)nblocks * stack_cap * sizeof(uint4));
+  EN(g.halo, std::max<int64_t>(pl.nhalo, 1) * sizeof(ahfgpu_halo));
+  EN(g.mem_stage, N * 8);
+  EN(g.prof_stage, std::max<uint64_t>(pl.nbins_total, 1) * AHFGPU_PROF_NFIELDS * 8);
+  EN(g.prof_cap_off, (pl.nhalo + 1) * 8);
+  EN(g.queue, std::max<int64_t>(pl.nhalo, 1) * 4);
+  EN(g.qhead, 64);
+  EN(g.counters, 64);
+  EN(g.err, 64);
+  EN(g.wred, 64);
+  EN(g.member_off, (pl.nhalo + 1) * 8);
+  EN(g.member, N * 8);
+  EN(g.prof_off, (pl.nhalo + 1) * 8);
+  EN(g.prof, std::max<uint64_t>(pl.nbins_total, 1) * AHFGPU_PROF_NFIELDS * 8);
+#undef EN
+  return AHFGPU_OK;
+}
+
+// Runs the stage on a device-resident batch.  Results stay in g.* buffers.
+int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t* host_off, ahfgpu_mode mode,
+               cudaStream_t st, ahfgpu_stats* stats) {
+  Plan pl;
+  int rc = validate_and_plan(prm, host_off, db->nhalo, pl);
+  if (rc) return rc;
+  if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64)
+    return fail(AHFGPU_ERR_INVALID, "mode %d is not available in this build", (int)mode);
+  const int bps = g.fp64_bps;
+  const int grid = std::max(1, g.nsm * bps);
+  const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(pl.maxn / 512 + 64, 64), 1u << 20);
+  if ((rc = ensure_work(pl, grid, stack_cap))) return rc;
+  const int64_t nh = pl.nhalo;
+  stats->n_particles_in = pl.N;
+  if (nh == 0) {
+    CK(cudaMemsetAsync(g.member_off.p, 0, 8, st));
+    CK(cudaMemsetAsync(g.prof_off.p, 0, 8, st));
+    g.last_nhalo = 0; g.last_nkept = 0; g.last_nbins = 0;
+    return AHFGPU_OK;
+  }
+  CK(cudaMemcpyAsync(g.prof_cap_off.p, pl.prof_cap_off.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(g.queue.p, pl.queue.data(), nh * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemsetAsync(g.qhead.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.counters.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.err.p, 0, 64, st));
+
+  DevParams P{};
+  P.VescTune = prm->VescTune;
+  P.v2_tune = prm->VescTune * prm->VescTune;
+  P.MINPART = prm->MINPART;
+  P.ovlim = prm->ovlim;
+  P.rho_vir = prm->rho_vir;
+  P.r_fac = prm->r_fac; P.x_fac = prm->x_fac; P.v_fac = prm->v_fac; P.m_fac = prm->m_fac;
+  P.rho_fac = prm->rho_fac; P.phi_fac = prm->phi_fac; P.Hubble = prm->Hubble;
+  P.has_w = db->w != nullptr;
+  P.force_serial = 0;
+  uint64_t launches = 0;
+  if (db->w) {
+    // FP64 mass prefixes are exact when every partial sum is a multiple of
+    // the smallest weight's quantum below 2^53 of them.
+    k_init_wred<<<1, 1, 0, st>>>(g.wred.as<float>());
+    k_weight_range<<<g.nsm * 4, 256, 0, st>>>(db->w, pl.N, g.wred.as<float>());
+    launches += 2;
+    float wr[3];
+    CK(cudaMemcpyAsync(wr, g.wred.p, 12, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int bad = 0;
+    memcpy(&bad, &wr[2], 4);
+    if (bad) return fail(AHFGPU_ERR_INVALID, "weights must be positive and finite");
+    double q = std::ldexp(1.0, std::ilogb((double)wr[0]) - 23);
+    double bound = (double)pl.maxn * (double)wr[1] / q;
+    if (!(bound < 4503599627370496.0)) P.force_serial = 1;   // 2^52
+  }
+
+  DevBatch B{};
+  B.nhalo = nh;
+  B.off = db->off;
+  B.x = db->x; B.y = db->y; B.z = db->z;
+  B.vx = db->vx; B.vy = db->vy; B.vz = db->vz;
+  B.w = db->w;
+  B.gidx = db->gidx;
+  B.cx = db->cx; B.cy = db->cy; B.cz = db->cz;
+
+  Work W{};
+  W.keyA = g.keyA.as<uint64_t>(); W.keyB = g.keyB.as<uint64_t>();
+  W.idxA = g.idxA.as<uint32_t>(); W.idxB = g.idxB.as<uint32_t>();
+  W.sdx = g.sdx.as<double>(); W.sdy = g.sdy.as<double>(); W.sdz = g.sdz.as<double>(); W.sd = g.sd.as<double>();
+  W.svx = g.svx.as<float>(); W.svy = g.svy.as<float>(); W.svz = g.svz.as<float>(); W.sw = g.sw.as<float>();
+  W.seid = g.seid.as<uint32_t>();
+  W.phi = g.phi.as<double>();
+  W.flag = g.flag.as<uint8_t>();
+  W.nflag = g.nflag.as<uint8_t>();
+  W.prof_a = g.pa.as<double>(); W.prof_b = g.pb.as<double>(); W.prof_c = g.pc.as<double>(); W.prof_d = g.pd.as<double>();
+  W.sort_stack = g.stack.as<uint4>();
+  W.stack_cap = stack_cap;
+  W.halo = g.halo.as<ahfgpu_halo>();
+  W.mem_stage = g.mem_stage.as<uint64_t>();
+  W.prof_stage = g.prof_stage.as<double>();
+  W.prof_cap_off = g.prof_cap_off.as<uint64_t>();
+  W.queue_head = g.qhead.as<unsigned int>();
+  W.queue = g.queue.as<int32_t>();
+  W.nqueue = (int)nh;
+  W.counters = g.counters.as<unsigned long long>();
+  W.err = g.err.as<int>();
+
+  CK(cudaEventRecord(g.ev0, st));
+  if (mode == AHFGPU_PLAIN_FP64) {
+    // one halo at a time, in batch order
+    for (int64_t h = 0; h < nh; h++) {
+      launch_fp64(P, B, W, 1, (int)h, st);
+      launches++;
+    }
+  } else {
+    launch_fp64(P, B, W, grid, -1, st);
+    launches++;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(g.ev1, st));
+  // pack
+  k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 0, g.member_off.as<uint64_t>());
+  k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 1, g.prof_off.as<uint64_t>());
+  int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
+  k_pack_members<<<pg, 256, 0, st>>>(W.halo, db->off, W.mem_stage, g.member_off.as<uint64_t>(),
+                                      g.member.as<uint64_t>(), nh);
+  k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
+                                   g.prof.as<double>(), nh);
+  launches += 4;
+  CK(cudaGetLastError());
+  uint64_t tails[2];
+  unsigned long long cnt[3];
+  int derr = 0;
+  CK(cudaMemcpyAsync(&tails[0], g.member_off.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&tails[1], g.prof_off.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(cnt, g.counters.p, 24, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&derr, g.err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr == kErrWorklist) return fail(AHFGPU_ERR_CAPACITY, "radial sort worklist overflow");
+  if (derr) return fail(AHFGPU_ERR_CUDA, "device error code %d", derr);
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
+  stats->ms_device = ms;
+  stats->n_kept = tails[0];
+  stats->n_retest = cnt[0];
+  stats->n_replay_halos = cnt[1];
+  stats->n_key_ties = cnt[2];
+  stats->n_launches = launches;
+  g.last_nhalo = nh;
+  g.last_nkept = tails[0];
+  g.last_nbins = tails[1];
+  return AHFGPU_OK;
+}
+
+void fill_dres(ahfgpu_result* r) {
+  memset(r, 0, sizeof(*r));
+  r->nhalo = g.last_nhalo;
+  r->halo = g.halo.as<ahfgpu_halo>();
+  r->member_off = g.member_off.as<uint64_t>();
+  r->member = g.member.as<uint64_t>();
+  r->prof_off = g.prof_off.as<uint64_t>();
+  r->prof = g.prof.as<double>();
+  r->stats = g.last_stats;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ahfgpu_init(int device) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(AHFGPU_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+  }
+  if (device < 0 || device >= n) return fail(AHFGPU_ERR_NO_DEVICE, "device %d out of range [0,%d)", device, n);
+  if (g.init && g.device == device) return AHFGPU_OK;
+  if (g.init) ahfgpu_shutdown();
+  CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(AHFGPU_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103a", device, prop.major,
+                prop.minor);
+  g.device = device;
+  g.nsm = prop.multiProcessorCount;
+  CK(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+  CK(cudaEventCreate(&g.ev0));
+  CK(cudaEventCreate(&g.ev1));
+  g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
+  CK(cudaGetLastError());
+  g.init = true;
+  g_err.clear();
+  return AHFGPU_OK;
+}
+
+int ahfgpu_shutdown(void) {
+  if (!g.init) return AHFGPU_OK;
+  cudaSetDevice(g.device);
+  cudaDeviceSynchronize();
+  DBuf* bufs[] = {&g.in_off, &g.in_x, &g.in_y, &g.in_z, &g.in_vx, &g.in_vy, &g.in_vz, &g.in_w, &g.in_gidx,
+                  &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
+                  &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
+                  &g.pc, &g.pd, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
+                  &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
+  for (DBuf* b : bufs) b->release();
+  if (g.ev0) cudaEventDestroy(g.ev0);
+  if (g.ev1) cudaEventDestroy(g.ev1);
+  if (g.stream) cudaStreamDestroy(g.stream);
+  g = Ctx();
+  return AHFGPU_OK;
+}
+
+int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* dres,
+                                  ahfgpu_mode mode, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!batch || !dres) return fail(AHFGPU_ERR_INVALID, "batch/result is NULL");
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  int64_t nh = batch->nhalo;
+  std::vector<uint64_t> off(nh > 0 ? nh + 1 : 1, 0);
+  if (nh > 0) {
+    if (!batch->off) return fail(AHFGPU_ERR_INVALID, "off is NULL");
+    CK(cudaMemcpyAsync(off.data(), batch->off, (nh + 1) * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  ahfgpu_stats s{};
+  rc = run_device(params, batch, off.data(), mode, st, &s);
+  if (rc) return rc;
+  s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  g.last_stats = s;
+  fill_dres(dres);
+  return AHFGPU_OK;
+}
+
+static int copy_in(const ahfgpu_batch* hb, ahfgpu_batch* db, cudaStream_t st) {
+  int64_t nh = hb->nhalo;
+  uint64_t N = nh > 0 ? hb->off[nh] : 0;
+  int rc;
+  *db = *hb;
+  auto up = [&](DBuf& buf, const void* src, size_t bytes, const void** dst) -> int {
+    if (!src) { *dst = nullptr; return AHFGPU_OK; }
+    int r = buf.ensure(std::max<size_t>(bytes, 8));
+    if (r) return r;
+    cudaError_t e = cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return fail(AHFGPU_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
+    *dst = buf.p;
+    return AHFGPU_OK;
+  };
+  if (nh == 0) return AHFGPU_OK;
+  if (!hb->x || !hb->y || !hb->z || !hb->vx || !hb->vy || !hb->vz || !hb->cx || !hb->cy || !hb->cz)
+    return fail(AHFGPU_ERR_INVALID, "a required batch array is NULL");
+  if ((rc = up(g.in_off, hb->off, (nh + 1) * 8, (const void**)&db->off))) return rc;
+  if ((rc = up(g.in_x, hb->x, N * 4, (const void**)&db->x))) return rc;
+  if ((rc = up(g.in_y, hb->y, N * 4, (const void**)&db->y))) return rc;
+  if ((rc = up(g.in_z, hb->z, N * 4, (const void**)&db->z))) return rc;
+  if ((rc = up(g.in_vx, hb->vx, N * 4, (const void**)&db->vx))) return rc;
+  if ((rc = up(g.in_vy, hb->vy, N * 4, (const void**)&db->vy))) return rc;
+  if ((rc = up(g.in_vz, hb->vz, N * 4, (const void**)&db->vz))) return rc;
+  if ((rc = up(g.in_w, hb->w, N * 4, (const void**)&db->w))) return rc;
+  if ((rc = up(g.in_gidx, hb->gidx, N * 8, (const void**)&db->gidx))) return rc;
+  if ((rc = up(g.in_cx, hb->cx, nh * 8, (const void**)&db->cx))) return rc;
+  if ((rc = up(g.in_cy, hb->cy, nh * 8, (const void**)&db->cy))) return rc;
+  if ((rc = up(g.in_cz, hb->cz, nh * 8, (const void**)&db->cz))) return rc;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_fetch_result(ahfgpu_result* r) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!r) return fail(AHFGPU_ERR_INVALID, "result is NULL");
+  if (g.last_nhalo < 0) return fail(AHFGPU_ERR_STATE, "no device result to fetch");
+  memset(r, 0, sizeof(*r));
+  int64_t nh = g.last_nhalo;
+  r->nhalo = nh;
+  r->halo = (ahfgpu_halo*)malloc(std::max<int64_t>(nh, 1) * sizeof(ahfgpu_halo));
+  r->member_off = (uint64_t*)malloc((nh + 1) * 8);
+  r->member = (uint64_t*)malloc(std::max<uint64_t>(g.last_nkept, 1) * 8);
+  r->prof_off = (uint64_t*)malloc((nh + 1) * 8);
+  r->prof = (double*)malloc(std::max<uint64_t>(g.last_nbins, 1) * AHFGPU_PROF_NFIELDS * 8);
+  if (!r->halo || !r->member_off || !r->member || !r->prof_off || !r->prof) {
+    ahfgpu_result_free(r);
+    return fail(AHFGPU_ERR_OOM, "host allocation of the result failed");
+  }
+  cudaStream_t st = g.stream;
+  CK(cudaStreamSynchronize(0));
+  if (nh > 0) CK(cudaMemcpyAsync(r->halo, g.halo.p, nh * sizeof(ahfgpu_halo), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(r->member_off, g.member_off.p, (nh + 1) * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(r->prof_off, g.prof_off.p, (nh + 1) * 8, cudaMemcpyDeviceToHost, st));
+  if (g.last_nkept) CK(cudaMemcpyAsync(r->member, g.member.p, g.last_nkept * 8, cudaMemcpyDeviceToHost, st));
+  if (g.last_nbins)
+    CK(cudaMemcpyAsync(r->prof, g.prof.p, g.last_nbins * AHFGPU_PROF_NFIELDS * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  r->stats = g.last_stats;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,
+                           ahfgpu_mode mode) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!batch || !result) return fail(AHFGPU_ERR_INVALID, "batch/result is NULL");
+  memset(result, 0, sizeof(*result));
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t st = g.stream;
+  Plan pl;
+  if ((rc = validate_and_plan(params, batch->off, batch->nhalo, pl))) return rc;
+  ahfgpu_batch db;
+  if ((rc = copy_in(batch, &db, st))) return rc;
+  ahfgpu_stats s{};
+  rc = run_device(params, &db, batch->off, mode, st, &s);
+  if (rc) return rc;
+  g.last_stats = s;
+  if ((rc = ahfgpu_fetch_result(result))) return rc;
+  s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  result->stats = s;
+  g.last_stats = s;
+  return AHFGPU_OK;
+}
+
+void ahfgpu_result_free(ahfgpu_result* r) {
+  if (!r) return;
+  free(r->halo);
+  free(r->member_off);
+  free(r->member);
+  free(r->prof_off);
+  free(r->prof);
+  memset(r, 0, sizeof(*r));
+}
+
+int ahfgpu_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    size_t n = std::min(len - 1, g_err.size());
+    memcpy(buf, g_err.data(), n);
+    buf[n] = 0;
+  }
+  return (int)g_err.size();
+}
+
+const char* ahfgpu_version(void) { return "ahfgpu 1.0 (sm_103a)"; }
+
+}  // extern "C"

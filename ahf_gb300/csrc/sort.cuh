@@ -1,0 +1,242 @@
+// sort.cuh -- block-level segmented radial sort of one halo's (key, slot)
+// pairs.  Replaces the index sort of sort_halo_particles
+// (src/libahf/ahf_halos.c:5846, an NR quicksort) with a deterministic total
+// order: ascending key, ties by list position -- the order a stable sort
+// gives.
+//
+// Lists up to kChunk pairs are sorted in shared memory (bitonic network on
+// the composite (key, slot)).  Longer lists take an MSD bucket pass: keys are
+// offset by the list minimum and split into up to kSortBuckets buckets by
+// their high bits (histogram in shared memory, scatter with atomics into the
+// B buffers), after which runs of consecutive buckets that fit a chunk are
+// sorted in shared memory straight into the A buffers.  A bucket that is
+// still larger than half a chunk is pushed on a per-CTA worklist and split
+// again over its own (narrower) key range; a range whose keys are all equal
+// is split by slot instead.  Scatter order inside a bucket is irrelevant
+// because every chunk is finally sorted on the full composite key.
+#pragma once
+
+#include "common.cuh"
+
+namespace ahfgpu {
+
+constexpr int kChunk = 2048;          // pairs sorted in shared memory at once
+constexpr int kHalfChunk = kChunk / 2;
+constexpr int kSortBuckets = 4096;
+
+struct SortSmem {
+  uint64_t key[kChunk];
+  uint32_t idx[kChunk];
+  uint32_t hist[kSortBuckets];
+  uint64_t red_u64[64];
+  int sp;                 // worklist depth
+  int seg_lo, seg_hi;     // current run of buckets
+  int flag;
+};
+
+__device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb, uint32_t ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// Sort `cnt` (<= kChunk) pairs from (ks, is)[lo..] into (kd, id)[lo..].
+// In-place (ks == kd) is allowed: the data goes through shared memory.
+__device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
+                                uint64_t lo, int cnt, SortSmem& S) {
+  int P = 1;
+  while (P < cnt) P <<= 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    if (i < cnt) {
+      S.key[i] = ks[lo + i];
+      S.idx[i] = is[lo + i];
+    } else {
+      S.key[i] = ~0ull;
+      S.idx[i] = 0xffffffffu;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < P; i += blockDim.x) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          uint64_t a = S.key[i], b = S.key[ixj];
+          uint32_t ia = S.idx[i], ib = S.idx[ixj];
+          bool up = (i & k) == 0;
+          bool gt = pair_less(b, ib, a, ia);
+          if (gt == up) {
+            S.key[i] = b; S.key[ixj] = a;
+            S.idx[i] = ib; S.idx[ixj] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    kd[lo + i] = S.key[i];
+    id[lo + i] = S.idx[i];
+  }
+  __syncthreads();
+}
+
+// Block min/max over a u64 sequence.
+__device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, SortSmem& S) {
+  const unsigned FULL = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) {
+    uint64_t a = __shfl_xor_sync(FULL, mn, off);
+    uint64_t b = __shfl_xor_sync(FULL, mx, off);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { S.red_u64[wid] = mn; S.red_u64[32 + wid] = mx; }
+  __syncthreads();
+  mn = ~0ull; mx = 0;
+  for (int w = 0; w < nw; w++) {
+    mn = S.red_u64[w] < mn ? S.red_u64[w] : mn;
+    mx = S.red_u64[32 + w] > mx ? S.red_u64[32 + w] : mx;
+  }
+  __syncthreads();
+}
+
+// Sort (keyA, idxA)[o, o+n) in place by (key, slot).  Uses (keyB, idxB) and
+// the CTA's worklist `stack` (capacity cap) as scratch.  Returns false when
+// the worklist overflows (the caller reports kErrWorklist).
+__device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
+                            uint64_t n, uint4* stack, int cap, SortSmem& S) {
+  if (n <= 1) return true;
+  if (n <= (uint64_t)kChunk) {
+    smem_sort_chunk(keyA, idxA, keyA, idxA, o, (int)n, S);
+    return true;
+  }
+  // worklist entry: x = lo(low 32), y = lo(high 32), z = count, w = src(bit0) | by_slot(bit1)
+  if (threadIdx.x == 0) {
+    stack[0] = make_uint4((uint32_t)o, (uint32_t)(o >> 32), (uint32_t)n, 0u);
+    S.sp = 1;
+    S.flag = 0;
+  }
+  __syncthreads();
+  while (true) {
+    int sp = S.sp;
+    if (sp == 0 || S.flag) break;
+    uint4 e = stack[sp - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) S.sp = sp - 1;
+    uint64_t lo = (uint64_t)e.x | ((uint64_t)e.y << 32);
+    uint32_t cnt = e.z;
+    int src = e.w & 1;
+    int by_slot = (e.w >> 1) & 1;
+    uint64_t* ks = src ? keyB : keyA;
+    uint32_t* is = src ? idxB : idxA;
+    uint64_t* kd = src ? keyA : keyB;
+    uint32_t* id = src ? idxA : idxB;
+    if (cnt <= (uint32_t)kChunk) {
+      __syncthreads();
+      smem_sort_chunk(ks, is, keyA, idxA, lo, (int)cnt, S);
+      continue;
+    }
+    // range of the bucketing key
+    uint64_t mn = ~0ull, mx = 0;
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+      uint64_t k = by_slot ? (uint64_t)is[lo + i] : ks[lo + i];
+      mn = k < mn ? k : mn;
+      mx = k > mx ? k : mx;
+    }
+    block_minmax_u64(mn, mx, S);
+    if (!by_slot && mn == mx) {
+      // all keys equal: order by slot
+      by_slot = 1;
+      mn = ~0ull; mx = 0;
+      for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+        uint64_t k = (uint64_t)is[lo + i];
+        mn = k < mn ? k : mn;
+        mx = k > mx ? k : mx;
+      }
+      block_minmax_u64(mn, mx, S);
+    }
+    uint64_t range = mx - mn;
+    int nb = 16;
+    while (nb < kSortBuckets && (uint64_t)nb * 128 < cnt) nb <<= 1;
+    int shift = 0;
+    while ((range >> shift) >= (uint64_t)nb) shift++;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) S.hist[b] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+      uint64_t k = by_slot ? (uint64_t)is[lo + i] : ks[lo + i];
+      atomicAdd(&S.hist[(int)((k - mn) >> shift)], 1u);
+    }
+    __syncthreads();
+    // exclusive scan of the histogram (thread 0; nb <= 4096)
+    if (threadIdx.x == 0) {
+      uint32_t run = 0;
+      for (int b = 0; b < nb; b++) {
+        uint32_t c = S.hist[b];
+        S.hist[b] = run;
+        run += c;
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+      uint64_t k = ks[lo + i];
+      uint32_t s = is[lo + i];
+      uint64_t bk = by_slot ? (uint64_t)s : k;
+      uint32_t pos = atomicAdd(&S.hist[(int)((bk - mn) >> shift)], 1u);
+      kd[lo + pos] = k;
+      id[lo + pos] = s;
+    }
+    __syncthreads();
+    // hist[b] is now the END of bucket b; walk runs of buckets
+    if (threadIdx.x == 0) { S.seg_lo = 0; }
+    __syncthreads();
+    while (true) {
+      int b0 = S.seg_lo;
+      if (b0 >= nb) break;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        uint32_t start = b0 == 0 ? 0u : S.hist[b0 - 1];
+        uint32_t size0 = S.hist[b0] - start;
+        int b1 = b0 + 1;
+        if (size0 > (uint32_t)kHalfChunk) {
+          // big bucket: push (data now in the other buffer)
+          if (S.sp >= cap) {
+            S.flag = 1;
+          } else {
+            uint64_t blo = lo + start;
+            stack[S.sp] = make_uint4((uint32_t)blo, (uint32_t)(blo >> 32), size0,
+                                     (uint32_t)((1 - src) | (by_slot << 1)));
+            S.sp = S.sp + 1;
+          }
+          S.seg_hi = -1;  // nothing to sort here
+        } else {
+          // extend the run while it stays within a chunk and meets no big bucket
+          while (b1 < nb) {
+            uint32_t sb = S.hist[b1 - 1];
+            uint32_t szb = S.hist[b1] - sb;
+            if (szb > (uint32_t)kHalfChunk) break;
+            if (S.hist[b1] - start > (uint32_t)kChunk) break;
+            b1++;
+          }
+          S.seg_hi = b1;
+        }
+        S.seg_lo = b1;
+        // stash run bounds in red_u64
+        S.red_u64[0] = start;
+        S.red_u64[1] = S.hist[b1 - 1];
+      }
+      __syncthreads();
+      if (S.flag) break;
+      if (S.seg_hi >= 0) {
+        uint64_t s0 = S.red_u64[0], s1 = S.red_u64[1];
+        int c = (int)(s1 - s0);
+        if (c > 0) smem_sort_chunk(kd, id, keyA, idxA, lo + s0, c, S);
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+  }
+  bool ok = S.flag == 0;
+  __syncthreads();
+  return ok;
+}
+
+}  // namespace ahfgpu

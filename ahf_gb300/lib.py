@@ -1,0 +1,164 @@
+"""Python binding of libahfgpu.so (the C ABI in include/ahfgpu.h).
+
+This is the host-side mirror of the reference's call site: one
+``construct_halos`` call stands for the per-halo loop of
+src/libahf/ahf_halos.c:504-510 (ahf_halos_sfc_constructHalo minus the
+gather).  There is no CPU fallback: if the CUDA library cannot be loaded or
+no sm_103 device is present, every call raises ``AhfGpuError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import Batch, HostResult, Params, Result, make_batch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libahfgpu.so")
+
+SYMBOLS = [
+    "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
+    "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version",
+]
+
+
+class AhfGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ahfgpu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+_inited_device = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(path):
+        raise AhfGpuError(abi.AHFGPU_ERR_STATE, f"{path} not built (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    lib.ahfgpu_init.argtypes = [C.c_int]
+    lib.ahfgpu_init.restype = C.c_int
+    lib.ahfgpu_shutdown.argtypes = []
+    lib.ahfgpu_shutdown.restype = C.c_int
+    lib.ahfgpu_construct_halos.argtypes = [C.POINTER(Params), C.POINTER(Batch), C.POINTER(Result), C.c_int]
+    lib.ahfgpu_construct_halos.restype = C.c_int
+    lib.ahfgpu_construct_halos_device.argtypes = [C.POINTER(Params), C.POINTER(Batch), C.POINTER(Result),
+                                                  C.c_int, C.c_void_p]
+    lib.ahfgpu_construct_halos_device.restype = C.c_int
+    lib.ahfgpu_fetch_result.argtypes = [C.POINTER(Result)]
+    lib.ahfgpu_fetch_result.restype = C.c_int
+    lib.ahfgpu_result_free.argtypes = [C.POINTER(Result)]
+    lib.ahfgpu_result_free.restype = None
+    lib.ahfgpu_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    lib.ahfgpu_last_error.restype = C.c_int
+    lib.ahfgpu_version.argtypes = []
+    lib.ahfgpu_version.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    lib.ahfgpu_last_error(buf, len(buf))
+    return buf.value.decode()
+
+
+def check(rc: int) -> None:
+    if rc != abi.AHFGPU_OK:
+        raise AhfGpuError(rc, last_error())
+
+
+def init(device: int = 0) -> None:
+    global _inited_device
+    lib = load()
+    if _inited_device == device:
+        return
+    check(lib.ahfgpu_init(device))
+    _inited_device = device
+
+
+def shutdown() -> None:
+    global _inited_device
+    if _lib is not None:
+        check(_lib.ahfgpu_shutdown())
+    _inited_device = None
+
+
+def mode_id(mode) -> int:
+    return abi.MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+def construct_halos(params: Params, lists, mode="batched_fp64", device: int = 0) -> HostResult:
+    """Host batch in, host result out (the drop-in call)."""
+    init(device)
+    lib = load()
+    b, keep = make_batch(lists)
+    r = Result()
+    check(lib.ahfgpu_construct_halos(C.byref(params), C.byref(b), C.byref(r), mode_id(mode)))
+    try:
+        return HostResult(r)
+    finally:
+        lib.ahfgpu_result_free(C.byref(r))
+        del keep
+
+
+def construct_halos_raw(params: Params, batch: Batch, mode) -> Result:
+    """Host-pointer call returning the library-owned Result (caller frees
+    with free_result); used where the caller already holds a Batch."""
+    lib = load()
+    r = Result()
+    check(lib.ahfgpu_construct_halos(C.byref(params), C.byref(batch), C.byref(r), mode_id(mode)))
+    return r
+
+
+def free_result(r: Result) -> None:
+    load().ahfgpu_result_free(C.byref(r))
+
+
+def device_batch(t: dict) -> Batch:
+    """Batch of device pointers from torch CUDA tensors (keys of HaloLists)."""
+    b = Batch()
+    b.nhalo = int(t["off"].numel() - 1)
+
+    def p(name, ct):
+        v = t.get(name)
+        return C.cast(C.c_void_p(v.data_ptr() if v is not None else None), C.POINTER(ct))
+
+    b.off = p("off", C.c_uint64)
+    for n in ("x", "y", "z", "vx", "vy", "vz", "w"):
+        setattr(b, n, p(n, C.c_float))
+    b.gidx = p("gidx", C.c_uint64)
+    for n in ("cx", "cy", "cz"):
+        setattr(b, n, p(n, C.c_double))
+    return b
+
+
+def construct_halos_device(params: Params, dbatch: Batch, mode, stream: int | None = None) -> Result:
+    """Device batch in, device-resident result description out."""
+    lib = load()
+    r = Result()
+    check(lib.ahfgpu_construct_halos_device(C.byref(params), C.byref(dbatch), C.byref(r), mode_id(mode),
+                                            C.c_void_p(stream) if stream else None))
+    return r
+
+
+def fetch_result() -> HostResult:
+    lib = load()
+    r = Result()
+    check(lib.ahfgpu_fetch_result(C.byref(r)))
+    try:
+        return HostResult(r)
+    finally:
+        lib.ahfgpu_result_free(C.byref(r))
+
+
+def version() -> str:
+    return load().ahfgpu_version().decode()

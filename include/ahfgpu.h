@@ -37,6 +37,12 @@ extern "C" {
 
 #define AHFGPU_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define AHFGPU_API __attribute__((visibility("default")))
+#else
+#define AHFGPU_API
+#endif
+
 /* ---- status codes ------------------------------------------------------ */
 #define AHFGPU_OK              0
 #define AHFGPU_ERR_INVALID    -1   /* malformed batch or parameters          */
@@ -163,15 +169,15 @@ typedef struct {
 
 /* Select and initialise a CUDA device (AHF's startrun-time set-up).  Safe to
  * call more than once; a later call with another device re-initialises.     */
-int ahfgpu_init(int device);
+AHFGPU_API int ahfgpu_init(int device);
 
 /* Release every device and host resource the library holds.                 */
-int ahfgpu_shutdown(void);
+AHFGPU_API int ahfgpu_shutdown(void);
 
 /* Replaces the per-halo loop body of src/libahf/ahf_halos.c:504-510
  * (ahf_halos_sfc_constructHalo, src/libahf/ahf_halos_sfc.c:118-169, minus its
  * gather at :137).  Host batch in, host result out (copies are inside).     */
-int ahfgpu_construct_halos(const ahfgpu_params *params,
+AHFGPU_API int ahfgpu_construct_halos(const ahfgpu_params *params,
                            const ahfgpu_batch  *batch,
                            ahfgpu_result       *result,
                            ahfgpu_mode          mode);
@@ -181,7 +187,7 @@ int ahfgpu_construct_halos(const ahfgpu_params *params,
  * call or ahfgpu_shutdown) and are described by `dres` (device pointers,
  * member_off/prof_off included).  `stream` is a cudaStream_t or NULL for the
  * library's own stream.  Used when the caller keeps a snapshot resident.    */
-int ahfgpu_construct_halos_device(const ahfgpu_params *params,
+AHFGPU_API int ahfgpu_construct_halos_device(const ahfgpu_params *params,
                                   const ahfgpu_batch  *batch,
                                   ahfgpu_result       *dres,
                                   ahfgpu_mode          mode,
@@ -189,15 +195,15 @@ int ahfgpu_construct_halos_device(const ahfgpu_params *params,
 
 /* Copy the device-resident result of the last _device call into a host
  * result (library-owned host arrays; free with ahfgpu_result_free).          */
-int ahfgpu_fetch_result(ahfgpu_result *result);
+AHFGPU_API int ahfgpu_fetch_result(ahfgpu_result *result);
 
-void ahfgpu_result_free(ahfgpu_result *result);
+AHFGPU_API void ahfgpu_result_free(ahfgpu_result *result);
 
 /* Message of the last failure on this thread (empty when none); returns the
  * untruncated length.                                                       */
-int ahfgpu_last_error(char *buf, size_t len);
+AHFGPU_API int ahfgpu_last_error(char *buf, size_t len);
 
-const char *ahfgpu_version(void);
+AHFGPU_API const char *ahfgpu_version(void);
 
 #ifdef __cplusplus
 }
