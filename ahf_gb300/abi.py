@@ -121,6 +121,7 @@ class Stats(C.Structure):
         ("n_retest", C.c_uint64),
         ("n_replay_halos", C.c_uint64),
         ("n_key_ties", C.c_uint64),
+        ("n_fp64_halos", C.c_uint64),
         ("n_launches", C.c_uint64),
         ("ms_device", C.c_double),
         ("ms_total", C.c_double),

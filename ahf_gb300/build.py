@@ -21,6 +21,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "api.cu": [],
     "halo_fp64.cu": ["--fmad=false"],
+    "halo_fp32c.cu": ["--fmad=false"],
 }
 
 

@@ -21,6 +21,8 @@ namespace ahfgpu {
 size_t fp64_smem_bytes();
 void launch_fp64(const DevParams& P, const DevBatch& B, const Work& W, int grid, int single, cudaStream_t st);
 int fp64_max_blocks_per_sm();
+void launch_fp32c(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st);
+int fp32c_max_blocks_per_sm();
 }  // namespace ahfgpu
 
 using namespace ahfgpu;
@@ -84,6 +86,7 @@ struct Ctx {
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
   DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
+  DBuf fdh, fdl, fdx, fdy, fdz, exlist, excount;
   DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
   // packed results (device)
   DBuf member_off, member, prof_off, prof;
@@ -197,6 +200,8 @@ struct Plan {
 int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, Plan& pl) {
   if (!p) return fail(AHFGPU_ERR_INVALID, "params is NULL");
   if (p->MINPART < 4) return fail(AHFGPU_ERR_INVALID, "MINPART must be >= 4 (got %lld)", (long long)p->MINPART);
+  if (p->MINPART > 128)
+    return fail(AHFGPU_ERR_CAPACITY, "MINPART %lld exceeds the supported maximum of 128", (long long)p->MINPART);
   if (!(p->VescTune > 0) || !(p->rho_vir > 0) || !(p->v_fac > 0))
     return fail(AHFGPU_ERR_INVALID, "non-positive VescTune, rho_vir or v_fac");
   if (nh < 0) return fail(AHFGPU_ERR_INVALID, "nhalo < 0");
@@ -232,6 +237,8 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.svx, N * 4); EN(g.svy, N * 4); EN(g.svz, N * 4); EN(g.sw, N * 4);
   EN(g.seid, N * 4); EN(g.phi, N * 8); EN(g.flag, N); EN(g.nflag, N);
   EN(g.pa, N * 8); EN(g.pb, N * 8); EN(g.pc, N * 8); EN(g.pd, N * 8);
+  EN(g.fdh, N * 4); EN(g.fdl, N * 4); EN(g.fdx, N * 4); EN(g.fdy, N * 4); EN(g.fdz, N * 4);
+  EN(g.exlist, std::max<int64_t>(pl.nhalo, 1) * 4); EN(g.excount, 64);
   EN(g.stack, (size_t)nblocks * stack_cap * sizeof(uint4));
   EN(g.halo, std::max<int64_t>(pl.nhalo, 1) * sizeof(ahfgpu_halo));
   EN(g.mem_stage, N * 8);
@@ -256,9 +263,9 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   Plan pl;
   int rc = validate_and_plan(prm, host_off, db->nhalo, pl);
   if (rc) return rc;
-  if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64)
-    return fail(AHFGPU_ERR_INVALID, "mode %d is not available in this build", (int)mode);
-  const int bps = g.fp64_bps;
+  if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64 && mode != AHFGPU_BATCHED_FP32C)
+    return fail(AHFGPU_ERR_INVALID, "unknown mode %d", (int)mode);
+  const int bps = std::max(g.fp64_bps, g.fp32c_bps);
   const int grid = std::max(1, g.nsm * bps);
   const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(pl.maxn / 512 + 64, 64), 1u << 20);
   if ((rc = ensure_work(pl, grid, stack_cap))) return rc;
@@ -275,6 +282,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   CK(cudaMemsetAsync(g.qhead.p, 0, 64, st));
   CK(cudaMemsetAsync(g.counters.p, 0, 64, st));
   CK(cudaMemsetAsync(g.err.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.halo.p, 0, nh * sizeof(ahfgpu_halo), st));
 
   DevParams P{};
   P.VescTune = prm->VescTune;
@@ -286,6 +294,10 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   P.rho_fac = prm->rho_fac; P.phi_fac = prm->phi_fac; P.Hubble = prm->Hubble;
   P.has_w = db->w != nullptr;
   P.force_serial = 0;
+  {
+    const char* fe = getenv("AHFGPU_FORCE_EXACT");   // test hook
+    P.force_exact = (fe && fe[0] == '1') ? 1 : 0;
+  }
   uint64_t launches = 0;
   if (db->w) {
     // FP64 mass prefixes are exact when every partial sum is a multiple of
@@ -334,6 +346,11 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   W.nqueue = (int)nh;
   W.counters = g.counters.as<unsigned long long>();
   W.err = g.err.as<int>();
+  W.fdh = g.fdh.as<float>(); W.fdl = g.fdl.as<float>();
+  W.fdx = g.fdx.as<float>(); W.fdy = g.fdy.as<float>(); W.fdz = g.fdz.as<float>();
+  W.exact_list = g.exlist.as<int>();
+  W.exact_count = g.excount.as<unsigned>();
+  CK(cudaMemsetAsync(g.excount.p, 0, 64, st));
 
   CK(cudaEventRecord(g.ev0, st));
   if (mode == AHFGPU_PLAIN_FP64) {
@@ -342,9 +359,25 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
       launch_fp64(P, B, W, 1, (int)h, st);
       launches++;
     }
-  } else {
-    launch_fp64(P, B, W, grid, -1, st);
+  } else if (mode == AHFGPU_BATCHED_FP64) {
+    launch_fp64(P, B, W, g.nsm * g.fp64_bps, -1, st);
     launches++;
+  } else {
+    launch_fp32c(P, B, W, g.nsm * g.fp32c_bps, st);
+    launches++;
+    // haloes whose FP64 re-test stayed inside the rounding band: FP64 form
+    unsigned nex = 0;
+    CK(cudaMemcpyAsync(&nex, g.excount.p, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (nex > 0) {
+      Work W2 = W;
+      W2.queue = g.exlist.as<int32_t>();
+      W2.nqueue = (int)nex;
+      W2.queue_head = g.qhead.as<unsigned int>() + 1;
+      launch_fp64(P, B, W2, std::min<int>(g.nsm * g.fp64_bps, (int)nex), -1, st);
+      launches++;
+    }
+    stats->n_fp64_halos = nex;
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(g.ev1, st));
@@ -419,6 +452,7 @@ int ahfgpu_init(int device) {
   CK(cudaEventCreate(&g.ev0));
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
+  g.fp32c_bps = std::max(1, fp32c_max_blocks_per_sm());
   CK(cudaGetLastError());
   g.init = true;
   g_err.clear();
@@ -432,7 +466,7 @@ int ahfgpu_shutdown(void) {
   DBuf* bufs[] = {&g.in_off, &g.in_x, &g.in_y, &g.in_z, &g.in_vx, &g.in_vy, &g.in_vz, &g.in_w, &g.in_gidx,
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
-                  &g.pc, &g.pd, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
+                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.exlist, &g.excount, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
   if (g.ev0) cudaEventDestroy(g.ev0);

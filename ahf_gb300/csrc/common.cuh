@@ -30,6 +30,7 @@ struct DevParams {
   double r_fac, x_fac, v_fac, m_fac, rho_fac, phi_fac, Hubble;
   int has_w;
   int force_serial;   // weight sums not exact in FP64: replay every halo
+  int force_exact;    // test hook: every unbinding iteration in exact order
 };
 
 // Input batch, device pointers (entries of halo h: [off[h], off[h+1])).
@@ -51,6 +52,10 @@ struct Work {
   float *svx, *svy, *svz, *sw;
   uint32_t* seid;         // entry index (within the halo) of sorted slot i
   double* phi;            // potential prefix of the current pass
+  float *fdh, *fdl;       // FP32C: distance as float-float
+  float *fdx, *fdy, *fdz; // FP32C: offsets from the centre
+  int* exact_list;        // FP32C: haloes handed to the FP64 form
+  unsigned* exact_count;
   uint8_t* flag;          // member (1) / removed (0) per sorted slot
   uint8_t* nflag;         // fixpoint flags of the next round
   double *prof_a, *prof_b, *prof_c, *prof_d;  // per-member profile arrays

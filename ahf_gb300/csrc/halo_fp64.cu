@@ -25,15 +25,13 @@
 
 #include "common.cuh"
 #include "sort.cuh"
+#include "finish.cuh"
 
 namespace ahfgpu {
 
 constexpr int kT = 256;                 // threads per CTA
 constexpr double kEps = 1.1102230246251565e-16;  // 2^-53
 
-struct Bin {
-  double npart, M, Lx, Ly, Lz, T, U, a11, a22, a33, a12, a13, a23, vesc2;
-};
 
 struct HaloSmem {
   SortSmem sort;
@@ -342,10 +340,167 @@ __device__ void serial_unbind(const HaloCtx& c, uint64_t n1, const DevParams& P,
 }
 
 // ---------------------------------------------------------------------------
-// Parallel rem_unbound.  Returns false when a particle's bound decision lies
-// inside the rounding band (the caller then replays serially).
+// Warp-sequential prefix sums in exactly the order of a C loop: one FP64
+// rounding per addition, left to right, starting from s0.  The 32 lanes load
+// 32 addends at a time and every lane performs the same chain of additions
+// on the broadcast values, so the prefix costs one dependent DADD per
+// element.  incl=1: out[i] = s0 + a[0] + ... + a[i];  incl=0: out[i] = the
+// sum before a[i].  Returns the total.  `a` and `out` may alias.
+__device__ double warp_chain(const double* a, double* out, uint64_t n, double s0, int incl) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  double s = s0;
+  for (uint64_t base = 0; base < n; base += 32) {
+    uint64_t i = base + lane;
+    double t = i < n ? a[i] : 0.0;
+    double mine = s;
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      double tk = __shfl_sync(FULL, t, k);
+      if (!incl && k == lane) mine = s;
+      s += tk;
+      if (incl && k == lane) mine = s;
+    }
+    if (i < n) out[i] = mine;
+  }
+  return s;
+}
+
+// One rem_unbound iteration (ahf_halos.c:3343-3583) in exactly the
+// reference's summation order, for a halo whose parallel evaluation left a
+// particle inside the rounding band.  Members: flag bit0 of slots [0, n1);
+// bit1 holds the speculated bound flags on entry and the exact ones on exit.
+// The order-dependent sums (potential integral, running bulk velocity) are
+// warp chains; the bound tests are re-evaluated in parallel until no flag
+// changes (the recurrence is triangular, so the fixpoint is the sequential
+// result).  Returns Phi0; *mb/*nb/*rlast: kept mass, count, last distance.
+__device__ double exact_iteration(const HaloCtx& c, uint64_t n1, const DevParams& P, const Work& W, HaloSmem& S,
+                                  uint64_t js, double* mb, long long* nbo, double* rlast, bool* any_b,
+                                  int* rounds_out) {
+  const uint64_t o = c.o;
+  double* term = W.phi + o;
+  double* ax = W.prof_b + o;
+  double* ay = W.prof_c + o;
+  double* az = W.prof_d + o;
+  // potential terms of the members (0 elsewhere)
+  double carryM = 0.0, carryD = 0.0;
+  for (uint64_t base = 0; base < n1; base += blockDim.x) {
+    uint64_t i = base + threadIdx.x;
+    bool mem = i < n1 && (W.flag[o + i] & 1);
+    double w = mem ? (double)W.sw[o + i] : 0.0;
+    double d = mem ? W.sd[o + i] : 0.0;
+    bool any;
+    double lastd;
+    double dprev = block_last_excl(mem, d, carryD, &any, &lastd, S.lastd, S.lasti);
+    double v[1] = {w}, tot[1];
+    block_scan<1>(v, tot, S.scan);
+    double M = carryM + v[0];
+    double t = 0.0;
+    if (mem && d > kMachineZero) {
+      double Mprev = M - w;
+      double Iprev = dprev > kMachineZero ? Mprev / (dprev * dprev) : 0.0;
+      double Inow = M / (d * d);
+      t = ((Inow + Iprev) / 2.) * (d - dprev);
+    }
+    if (i < n1) term[i] = t;
+    carryM += tot[0];
+    carryD = lastd;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double s = warp_chain(term, term, n1, 0.0, 1);
+    if (threadIdx.x == 0) S.bd[12] = s;
+  }
+  __syncthreads();
+  const double Phi0 = S.bd[12] + carryM / carryD;
+  const double w0 = (double)W.sw[o + js];
+  const double sVX = w0 * (double)W.svx[o + js], sVY = w0 * (double)W.svy[o + js], sVZ = w0 * (double)W.svz[o + js];
+  int rounds = 0;
+  double Mb = 0, Rl = 0;
+  long long nb = 0;
+  bool anyb = false;
+  while (true) {
+    rounds++;
+    // addends of the running bulk velocity under the current flags
+    for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) {
+      uint8_t f = W.flag[o + i];
+      bool b = (f & 1) && ((f >> 1) & 1);
+      double w = b ? (double)W.sw[o + i] : 0.0;
+      ax[i] = b ? w * (double)W.svx[o + i] : 0.0;
+      ay[i] = b ? w * (double)W.svy[o + i] : 0.0;
+      az[i] = b ? w * (double)W.svz[o + i] : 0.0;
+    }
+    __syncthreads();
+    int warp = threadIdx.x >> 5;
+    if (warp == 0) warp_chain(ax, ax, n1, sVX, 0);
+    else if (warp == 1) warp_chain(ay, ay, n1, sVY, 0);
+    else if (warp == 2) warp_chain(az, az, n1, sVZ, 0);
+    __syncthreads();
+    int changed = 0;
+    double cMV = w0, carryMb = 0.0, carryR = 0.0;
+    long long carryNb = 0;
+    bool anyR = false;
+    for (uint64_t base = 0; base < n1; base += blockDim.x) {
+      uint64_t i = base + threadIdx.x;
+      bool valid = i < n1;
+      uint8_t f = valid ? W.flag[o + i] : 0;
+      bool mem = f & 1;
+      bool b = mem && ((f >> 1) & 1);
+      double w = mem ? (double)W.sw[o + i] : 0.0;
+      double cw = b ? w : 0.0;
+      double v[1] = {cw}, ex[1], tot[1];
+      block_scan_excl<1>(v, ex, tot, S.scan);
+      bool nbv = false;
+      double d = 0.0;
+      if (mem) {
+        double M_vel = cMV + ex[0];
+        d = W.sd[o + i];
+        double dX = W.sdx[o + i], dY = W.sdy[o + i], dZ = W.sdz[o + i];
+        double v_esc2;
+        if (d > kMachineZero) v_esc2 = (2 * fabs(term[i] - Phi0) * P.phi_fac);
+        else v_esc2 = 1e30;
+        double VXp = (double)W.svx[o + i], VYp = (double)W.svy[o + i], VZp = (double)W.svz[o + i];
+        double dVX = (VXp - ax[i] / M_vel) * P.v_fac + P.Hubble * (dX) * P.r_fac;
+        double dVY = (VYp - ay[i] / M_vel) * P.v_fac + P.Hubble * (dY) * P.r_fac;
+        double dVZ = (VZp - az[i] / M_vel) * P.v_fac + P.Hubble * (dZ) * P.r_fac;
+        double vel2 = (dVX * dVX + dVY * dVY) + dVZ * dVZ;
+        nbv = !(vel2 > P.v2_tune * v_esc2);
+        if (nbv != b) changed = 1;
+        W.flag[o + i] = (uint8_t)(1 | (nbv ? 2 : 0));
+      }
+      int tcnt;
+      block_scan_int(b ? 1 : 0, &tcnt, S.iscan);
+      bool any;
+      double lastR;
+      block_last_excl(b, d, carryR, &any, &lastR, S.lastd, S.lasti);
+      carryR = lastR;
+      anyR |= any;
+      carryMb += tot[0];
+      carryNb += tcnt;
+      cMV += tot[0];
+    }
+    if (!__syncthreads_or(changed)) {
+      Mb = carryMb;
+      nb = carryNb;
+      Rl = carryR;
+      anyb = anyR;
+      break;
+    }
+  }
+  *mb = Mb;
+  *nbo = nb;
+  *rlast = Rl;
+  *any_b = anyb;
+  *rounds_out = rounds;
+  return Phi0;
+}
+
+// ---------------------------------------------------------------------------
+// Parallel rem_unbound.  An iteration whose bound decisions include one
+// inside the rounding band is redone by exact_iteration (*replayed set).
 __device__ bool parallel_unbind(const HaloCtx& c, uint64_t n1, const DevParams& P, const Work& W, HaloSmem& S,
-                                float vmax, double* out, int* niter_out, int* nobound_out, int* rounds_out) {
+                                float vmax, double* out, int* niter_out, int* nobound_out, int* rounds_out,
+                                int* replayed) {
   const uint64_t o = c.o;
   uint64_t no_vbulk = (uint64_t)(P.MINPART / 2);
   uint64_t nremove = 4;
@@ -478,9 +633,19 @@ __device__ bool parallel_unbind(const HaloCtx& c, uint64_t n1, const DevParams& 
       if (rounds >= kMaxFixRounds) { amb_any = true; break; }
     }
     if (rounds > maxrounds) maxrounds = rounds;
-    if (amb_any) {
-      *rounds_out = maxrounds;
-      return false;
+    if (amb_any || P.force_exact) {
+      // a decision lies inside the rounding band: redo this iteration in
+      // the reference's exact summation order
+      long long nbx;
+      double mbx, rlx;
+      bool anyb;
+      int rr;
+      Phi0 = exact_iteration(c, n1, P, W, S, js, &mbx, &nbx, &rlx, &anyb, &rr);
+      Mb = mbx;
+      nb = nbx;
+      Rlast = anyb ? rlx : R_vir;
+      *replayed = 1;
+      if (rr > maxrounds) maxrounds = rr;
     }
     // members <- bound
     for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) {
@@ -503,95 +668,6 @@ __device__ bool parallel_unbind(const HaloCtx& c, uint64_t n1, const DevParams& 
   *nobound_out = nobound;
   *rounds_out = maxrounds;
   return true;
-}
-
-// ---------------------------------------------------------------------------
-// numerics of the per-bin / per-halo finish (one thread)
-
-// symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (Golub & Van
-// Loan, sym.schur2 + cyclic sweep); column k of v is the eigenvector of d[k]
-__device__ void jacobi3(const double ain[3][3], double d[3], double v[3][3]) {
-  double a[3][3];
-  for (int i = 0; i < 3; i++)
-    for (int j = 0; j < 3; j++) { a[i][j] = ain[i][j]; v[i][j] = (i == j) ? 1.0 : 0.0; }
-  for (int sweep = 0; sweep < 64; sweep++) {
-    double off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
-    if (off == 0.0) break;
-    for (int pp = 0; pp < 2; pp++) {
-      for (int qq = pp + 1; qq < 3; qq++) {
-        double apq = a[pp][qq];
-        if (apq == 0.0) continue;
-        double app = a[pp][pp], aqq = a[qq][qq];
-        if (sweep > 3 && fabs(app) + 100.0 * fabs(apq) == fabs(app) &&
-            fabs(aqq) + 100.0 * fabs(apq) == fabs(aqq)) {
-          a[pp][qq] = a[qq][pp] = 0.0;
-          continue;
-        }
-        double tau = (aqq - app) / (2.0 * apq);
-        double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-        double cs = 1.0 / sqrt(1.0 + t * t);
-        double sn = t * cs;
-        for (int k = 0; k < 3; k++) {
-          double akp = a[k][pp], akq = a[k][qq];
-          a[k][pp] = cs * akp - sn * akq;
-          a[k][qq] = sn * akp + cs * akq;
-        }
-        for (int k = 0; k < 3; k++) {
-          double apk = a[pp][k], aqk = a[qq][k];
-          a[pp][k] = cs * apk - sn * aqk;
-          a[qq][k] = sn * apk + cs * aqk;
-        }
-        a[pp][qq] = a[qq][pp] = 0.0;
-        for (int k = 0; k < 3; k++) {
-          double vkp = v[k][pp], vkq = v[k][qq];
-          v[k][pp] = cs * vkp - sn * vkq;
-          v[k][qq] = sn * vkp + cs * vkq;
-        }
-      }
-    }
-  }
-  for (int k = 0; k < 3; k++) d[k] = a[k][k];
-}
-
-// get_axes, src/libutility/specific.c:135-178 (own eigen-solver)
-__device__ void get_axes(double it[3][3], double* a1, double* a2, double* a3) {
-  double d[3], v[3][3];
-  jacobi3(it, d, v);
-  int ord[3] = {0, 1, 2};
-  for (int i = 1; i < 3; i++) {
-    int k = ord[i], j = i;
-    while (j > 0 && d[ord[j - 1]] < d[k]) { ord[j] = ord[j - 1]; j--; }
-    ord[j] = k;
-  }
-  *a1 = d[ord[0]]; *a2 = d[ord[1]]; *a3 = d[ord[2]];
-  for (int cc = 0; cc < 3; cc++)
-    for (int r = 0; r < 3; r++) it[r][cc] = v[r][ord[cc]];
-}
-
-__device__ double cnfw_root(double cc, double v2r) { return 0.216 * cc / (log(1 + cc) - cc / (1 + cc)) - v2r; }
-// calc_cNFW, src/libutility/specific.c:2041-2072
-__device__ double calc_cNFW(double V2_max, double V2_vir) {
-  double r = V2_max / V2_vir;
-  if (r <= 1 || r > 5.9) return -1;
-  double a = 2.2, b = 100, cc;
-  while (b - a > 1e-3) {
-    cc = (a + b) / 2;
-    if (cnfw_root(a, r) * cnfw_root(cc, r) > 0) a = cc; else b = cc;
-  }
-  return (a + b) / 2.0;
-}
-__device__ double cr1_root(double cc, double R1) {
-  return (cc - 2.0 * log(1.0 + cc) + cc / (1.0 + cc)) / (cc * (log(1.0 + cc) - cc / (1.0 + cc))) - R1;
-}
-// calc_cR1, src/libutility/specific.c:1993-2018
-__device__ double calc_cR1(double R1) {
-  if (R1 <= 0.19 || 0.585 <= R1) return -1.0;
-  double a = 1.0, b = 500.0, cc;
-  while (b - a > 1e-3) {
-    cc = (a + b) / 2;
-    if (cr1_root(a, R1) * cr1_root(cc, R1) > 0) a = cc; else b = cc;
-  }
-  return (a + b) / 2.0;
 }
 
 // smooth3 (src/libutility/general.c:548-573), `ns` passes over y[0..m),
@@ -815,54 +891,8 @@ __device__ void profiles(const HaloCtx& c, uint64_t n1, uint64_t n2, const DevPa
     cr += tn;
     __syncthreads();
   }
-  // per-bin rows
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
-    const Bin& R = S.bins[b];
-    double cur_rad = S.edge[b];
-    double Volume = FPT * (cur_rad * cur_rad * cur_rad);
-    double Mprev = b > 0 ? S.bins[b - 1].M : 0.0;
-    double Vprev = b > 0 ? FPT * (S.edge[b - 1] * S.edge[b - 1] * S.edge[b - 1]) : 0.0;
-    double dM = R.M - Mprev;
-    double dV = Volume - Vprev;
-    double it[3][3], ax1, ax2, ax3;
-    if (R.npart > 10) {
-      it[0][0] = R.a11; it[1][1] = R.a22; it[2][2] = R.a33;
-      it[0][1] = R.a12; it[1][0] = R.a12;
-      it[0][2] = R.a13; it[2][0] = R.a13;
-      it[1][2] = R.a23; it[2][1] = R.a23;
-      get_axes(it, &ax1, &ax2, &ax3);
-    } else {
-      for (int x = 0; x < 3; x++)
-        for (int y = 0; y < 3; y++) it[x][y] = 0.0;
-      ax1 = 1; ax2 = 0; ax3 = 0;
-    }
-    double* row = rows + (uint64_t)b * AHFGPU_PROF_NFIELDS;
-    row[AHFGPU_PROF_R] = cur_rad;
-    row[AHFGPU_PROF_NPART] = R.npart;
-    row[AHFGPU_PROF_NVPART] = R.M;
-    row[AHFGPU_PROF_OVDENS] = R.M / Volume;
-    row[AHFGPU_PROF_DENS] = dV > 0 ? dM / dV : 0.0;
-    row[AHFGPU_PROF_V2_CIRC] = R.M / cur_rad;
-    row[AHFGPU_PROF_V_ESC2] = R.vesc2;
-    row[AHFGPU_PROF_SIG_V] = sqrt(R.T / R.M);
-    row[AHFGPU_PROF_EKIN] = 0.5 * R.T;
-    row[AHFGPU_PROF_EPOT] = 0.5 * R.U;
-    row[AHFGPU_PROF_LX] = R.Lx;
-    row[AHFGPU_PROF_LY] = R.Ly;
-    row[AHFGPU_PROF_LZ] = R.Lz;
-    row[AHFGPU_PROF_E1X] = it[0][0]; row[AHFGPU_PROF_E1Y] = it[1][0]; row[AHFGPU_PROF_E1Z] = it[2][0];
-    row[AHFGPU_PROF_E2X] = it[0][1]; row[AHFGPU_PROF_E2Y] = it[1][1]; row[AHFGPU_PROF_E2Z] = it[2][1];
-    row[AHFGPU_PROF_E3X] = it[0][2]; row[AHFGPU_PROF_E3Y] = it[1][2]; row[AHFGPU_PROF_E3Z] = it[2][2];
-    row[AHFGPU_PROF_AXIS1] = 1.0;
-    if (ax1 > 0.) {
-      row[AHFGPU_PROF_AXIS2] = sqrt(ax2 / ax1);
-      row[AHFGPU_PROF_AXIS3] = sqrt(ax3 / ax1);
-    } else {
-      row[AHFGPU_PROF_AXIS2] = 0.0;
-      row[AHFGPU_PROF_AXIS3] = 0.0;
-    }
-  }
+  write_bin_rows(S.bins, S.edge, nbins, rows);
   __syncthreads();
   // find_max on dens_r2 (3 smoothings) and Vcirc2 (1), both from slot nignore
   uint64_t m = n2 - kNignore;
@@ -892,89 +922,9 @@ __device__ void profiles(const HaloCtx& c, uint64_t n1, uint64_t n2, const DevPa
     uint64_t ib = lo;
     double M_max = ovd[ib] * FPT * (radius[ib] * radius[ib] * radius[ib]);
     double V_max = M_max / R_max;
-    const double* last = rows + (uint64_t)(nbins - 1) * AHFGPU_PROF_NFIELDS;
-    const double* pl = rows + (uint64_t)(nbins - 2) * AHFGPU_PROF_NFIELDS;
-    double Lx = last[AHFGPU_PROF_LX], Ly = last[AHFGPU_PROF_LY], Lz = last[AHFGPU_PROF_LZ];
-    double absL = sqrt((Lx * Lx + Ly * Ly) + Lz * Lz);
-    double Msph = cM;
-    hout.M_vir = Msph;
-    hout.vel[0] = cVX / Msph; hout.vel[1] = cVY / Msph; hout.vel[2] = cVZ / Msph;
-    hout.R_max = R_max;
-    hout.V2_max = V_max;
-    hout.r2 = r2;
-    hout.sigV = last[AHFGPU_PROF_SIG_V];
-    hout.v_esc2 = last[AHFGPU_PROF_V_ESC2];
-    hout.Ekin = last[AHFGPU_PROF_EKIN];
-    hout.Epot = last[AHFGPU_PROF_EPOT];
-    hout.axis[0] = last[AHFGPU_PROF_AXIS1]; hout.axis[1] = last[AHFGPU_PROF_AXIS2]; hout.axis[2] = last[AHFGPU_PROF_AXIS3];
-    hout.E1[0] = last[AHFGPU_PROF_E1X]; hout.E1[1] = last[AHFGPU_PROF_E1Y]; hout.E1[2] = last[AHFGPU_PROF_E1Z];
-    hout.E2[0] = last[AHFGPU_PROF_E2X]; hout.E2[1] = last[AHFGPU_PROF_E2Y]; hout.E2[2] = last[AHFGPU_PROF_E2Z];
-    hout.E3[0] = last[AHFGPU_PROF_E3X]; hout.E3[1] = last[AHFGPU_PROF_E3Y]; hout.E3[2] = last[AHFGPU_PROF_E3Z];
-    if (absL > 0) {
-      hout.AngMom[0] = Lx / absL; hout.AngMom[1] = Ly / absL; hout.AngMom[2] = Lz / absL;
-      hout.lambda = absL / hout.M_vir / sqrt(2. * hout.M_vir * hout.R_vir);
-      hout.lambda *= P.v_fac * sqrt(P.r_fac / (kGrav * P.m_fac));
-      // calc_lambdaE, ahf_halos.c:3937-3953
-      double t1 = sqrt(P.m_fac * hout.M_vir);
-      t1 = t1 * t1 * t1;
-      double t2 = hout.Ekin * P.m_fac * (P.v_fac * P.v_fac);
-      double t3 = hout.Epot * P.m_fac * P.phi_fac;
-      t2 = fabs(t2 + t3);
-      t2 = sqrt(t2);
-      t1 = t2 / t1;
-      t2 = P.m_fac * P.r_fac * P.v_fac * absL;
-      t2 = t2 / (P.m_fac * hout.M_vir);
-      t3 = t1 * t2;
-      hout.lambdaE = t3 / kGrav;
-    } else {
-      hout.AngMom[0] = hout.AngMom[1] = hout.AngMom[2] = 0.0;
-      hout.lambda = 0.0;
-      hout.lambdaE = 0.0;
-    }
-    hout.cNFW = calc_cNFW(hout.V2_max, hout.M_vir / hout.R_vir);
-    {
-      // calc_R1, src/libutility/specific.c:1977-1991
-      double r0h = rows[AHFGPU_PROF_R] / 2.0;
-      double R1 = (r0h * r0h * r0h) * rows[AHFGPU_PROF_DENS] * (rows[AHFGPU_PROF_R]);
-      for (int b = 1; b < nbins; b++) {
-        const double* rb = rows + (uint64_t)b * AHFGPU_PROF_NFIELDS;
-        const double* ra = rb - AHFGPU_PROF_NFIELDS;
-        double rmid = (rb[AHFGPU_PROF_R] + ra[AHFGPU_PROF_R]) / 2.0;
-        double drr = rb[AHFGPU_PROF_R] - ra[AHFGPU_PROF_R];
-        R1 += (rmid * rmid * rmid) * rb[AHFGPU_PROF_DENS] * drr;
-      }
-      hout.R1 = 4 * kPi * R1 / hout.M_vir / hout.R_vir;
-    }
-    hout.cR1 = calc_cR1(hout.R1);
-    {
-      double Ts = 2.0 * (last[AHFGPU_PROF_EKIN] - pl[AHFGPU_PROF_EKIN]);
-      double frad = fabs(pl[AHFGPU_PROF_R] / last[AHFGPU_PROF_R]);
-      hout.SurfP = -0.125 * ((1. + frad) * (1. + frad) * (1. + frad)) / (1. - (frad * frad * frad)) * Ts;
-    }
-    double Mhi = cs[14], Mlo = cs[15];
-    hout.fMhires = Mhi > 0 ? Mhi / (Mhi + Mlo) : 0.0;
-    if (mbslot >= 0) {
-      uint64_t e = o + W.seid[o + mbslot];
-      double dX = fabs(B.x[e] - c.cx), dY = fabs(B.y[e] - c.cy), dZ = fabs(B.z[e] - c.cz);
-      if (dX > 0.5) dX -= 1.0;
-      if (dY > 0.5) dY -= 1.0;
-      if (dZ > 0.5) dZ -= 1.0;
-      hout.mbp_offset = sqrt((dX * dX + dY * dY) + dZ * dZ);
-      hout.pos_mbp[0] = B.x[e]; hout.pos_mbp[1] = B.y[e]; hout.pos_mbp[2] = B.z[e];
-      hout.vel_mbp[0] = B.vx[e]; hout.vel_mbp[1] = B.vy[e]; hout.vel_mbp[2] = B.vz[e];
-    } else {
-      hout.mbp_offset = -1.0;
-      hout.flags |= AHFGPU_HALO_NO_MBP;
-    }
-    double CoM[3] = {fmod(cs[5] / Msph + 1., 1.), fmod(cs[6] / Msph + 1., 1.), fmod(cs[7] / Msph + 1., 1.)};
-    {
-      double dX = fabs(CoM[0] - c.cx), dY = fabs(CoM[1] - c.cy), dZ = fabs(CoM[2] - c.cz);
-      if (dX > 0.5) dX -= 1.0;
-      if (dY > 0.5) dY -= 1.0;
-      if (dZ > 0.5) dZ -= 1.0;
-      hout.com_offset = sqrt((dX * dX + dY * dY) + dZ * dZ);
-    }
-    hout.pos_com[0] = CoM[0]; hout.pos_com[1] = CoM[1]; hout.pos_com[2] = CoM[2];
+    long long mbe = mbslot >= 0 ? (long long)(o + W.seid[o + mbslot]) : -1;
+    finish_scalars(rows, nbins, cM, cVX, cVY, cVZ, cs[5], cs[6], cs[7], cs[14], cs[15], mbe, r2, R_max, V_max,
+                   P, B, c.cx, c.cy, c.cz, hout);
     hout.nbins = nbins;
     hout.flags |= AHFGPU_HALO_RAN_PROFILE;
   }
@@ -1030,7 +980,10 @@ __device__ void process_halo(int h, const DevParams& P, const DevBatch& B, const
   compute_keys(c, B, W);
   bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.o, c.n, stack, W.stack_cap, S.sort);
   if (!ok) {
-    if (threadIdx.x == 0) atomicExch(W.err, kErrWorklist);
+    if (threadIdx.x == 0) {
+      atomicExch(W.err, kErrWorklist);
+      W.halo[h] = hout;   // npart 0: nothing is packed for this halo
+    }
     __syncthreads();
     return;
   }
@@ -1050,9 +1003,15 @@ __device__ void process_halo(int h, const DevParams& P, const DevBatch& B, const
   uint64_t ncur = n1;
   if (n1 >= (uint64_t)P.MINPART) {
     double uo[4];
-    int niter = 0, nob = 0, rounds = 0;
-    bool pok = P.force_serial ? false : parallel_unbind(c, n1, P, W, S, vmax, uo, &niter, &nob, &rounds);
+    int niter = 0, nob = 0, rounds = 0, replayed = 0;
+    bool pok = P.force_serial ? false
+                              : parallel_unbind(c, n1, P, W, S, vmax, uo, &niter, &nob, &rounds, &replayed);
+    if (replayed && threadIdx.x == 0) {
+      atomicAdd(&W.counters[1], 1ull);
+      hout.flags |= AHFGPU_HALO_REPLAYED;
+    }
     if (!pok) {
+      // weights whose FP64 sums are not exact: one thread, reference order
       if (threadIdx.x == 0) {
         serial_unbind(c, n1, P, W, uo, &niter, &nob);
         S.bd[8] = uo[0]; S.bd[9] = uo[1]; S.bd[10] = uo[2]; S.bd[11] = uo[3];
@@ -1097,7 +1056,7 @@ __device__ void process_halo(int h, const DevParams& P, const DevBatch& B, const
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kT) halo_fp64_kernel(DevParams P, DevBatch B, Work W, int single) {
+__global__ void __launch_bounds__(kT, 1) halo_fp64_kernel(DevParams P, DevBatch B, Work W, int single) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   HaloSmem& S = *reinterpret_cast<HaloSmem*>(smem_raw);
   uint4* stack = W.sort_stack + (uint64_t)blockIdx.x * W.stack_cap;

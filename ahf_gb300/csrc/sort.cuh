@@ -40,7 +40,7 @@ __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb,
 
 // Sort `cnt` (<= kChunk) pairs from (ks, is)[lo..] into (kd, id)[lo..].
 // In-place (ks == kd) is allowed: the data goes through shared memory.
-__device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
+static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
                                 uint64_t lo, int cnt, SortSmem& S) {
   int P = 1;
   while (P < cnt) P <<= 1;
@@ -102,7 +102,7 @@ __device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, Sor
 // Sort (keyA, idxA)[o, o+n) in place by (key, slot).  Uses (keyB, idxB) and
 // the CTA's worklist `stack` (capacity cap) as scratch.  Returns false when
 // the worklist overflows (the caller reports kErrWorklist).
-__device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
+static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
                             uint64_t n, uint4* stack, int cap, SortSmem& S) {
   if (n <= 1) return true;
   if (n <= (uint64_t)kChunk) {

@@ -235,6 +235,16 @@ def _sample_spheres(tab, sel, nfw_counts, bg_counts, gen, device):
     return pos, vel, counts
 
 
+def _to_ahf_units(pos, vel, box, v_fac):
+    """Mpc/h, km/s -> box units in [0,1) (float32) and AHF momenta (float32)."""
+    pb = torch.remainder(pos / box, 1.0)
+    pb = torch.where(pb >= 1.0, torch.zeros_like(pb), pb)
+    pf = pb.to(torch.float32)
+    pf = torch.where(pf >= 1.0, torch.zeros_like(pf), pf)
+    mom = (vel.to(torch.float64) / v_fac).to(torch.float32)
+    return pf, mom
+
+
 def generate(name: str, scale: float = 1.0, device: str = "cpu", multimass: bool = False,
              seed: int | None = None, max_particles: int | None = None, as_numpy: bool = True) -> HaloLists:
     """Build the particle lists of workload `name` (see module docstring).
@@ -256,11 +266,12 @@ def generate(name: str, scale: float = 1.0, device: str = "cpu", multimass: bool
     nbg = rng.poisson(bg_density * 4.0 / 3.0 * math.pi * (1.5 * tab["rvir"]) ** 3)
     gen = torch.Generator(device=device)
     gen.manual_seed(int(rng.integers(1 << 62)))
-    sel = np.arange(nh)
-    pos, vel, counts = _sample_spheres(tab, sel, tab["npart"], nbg, gen, device)
-    # subhalo particles join their host's list; host particles inside a
-    # subhalo's 1.5 R_vir join the subhalo's list.
+    v_fac = box * H0          # a = 1
     if cfg["subs"] and np.any(tab["host"] >= 0):
+        sel = np.arange(nh)
+        pos, vel, counts = _sample_spheres(tab, sel, tab["npart"], nbg, gen, device)
+        # subhalo particles join their host's list; host particles inside a
+        # subhalo's 1.5 R_vir join the subhalo's list.
         starts = np.concatenate([[0], np.cumsum(counts)])
         parts_pos = [pos[starts[h]:starts[h + 1]] for h in range(nh)]
         parts_vel = [vel[starts[h]:starts[h + 1]] for h in range(nh)]
@@ -274,16 +285,32 @@ def generate(name: str, scale: float = 1.0, device: str = "cpu", multimass: bool
             parts_pos[s] = torch.cat([parts_pos[s], own_pos[h][near]])
             parts_vel[s] = torch.cat([parts_vel[s], own_vel[h][near]])
         counts = np.array([len(p) for p in parts_pos], np.int64)
-        pos = torch.cat(parts_pos)
-        vel = torch.cat(parts_vel)
+        chunks = [(torch.cat(parts_pos), torch.cat(parts_vel))]
+    else:
+        # chunks of haloes (bounded temporary memory for the 4e8-particle case)
+        counts = (tab["npart"] + nbg).astype(np.int64)
+        chunks = []
+        h0 = 0
+        budget = 40_000_000
+        while h0 < nh:
+            h1 = h0 + 1
+            acc = counts[h0]
+            while h1 < nh and acc + counts[h1] <= budget:
+                acc += counts[h1]
+                h1 += 1
+            sel = np.arange(h0, h1)
+            pos, vel, _ = _sample_spheres(tab, sel, tab["npart"][sel], nbg[sel], gen, device)
+            chunks.append(_to_ahf_units(pos, vel, box, v_fac))
+            del pos, vel
+            h0 = h1
     off = np.zeros(nh + 1, np.uint64)
     off[1:] = np.cumsum(counts)
-    pb = torch.remainder(pos / box, 1.0)
-    pb = torch.where(pb >= 1.0, torch.zeros_like(pb), pb)
-    pf = pb.to(torch.float32)
-    pf = torch.where(pf >= 1.0, torch.zeros_like(pf), pf)
-    v_fac = box * H0          # a = 1
-    mom = (vel.to(torch.float64) / v_fac).to(torch.float32)
+    if cfg["subs"] and np.any(tab["host"] >= 0):
+        pf, mom = _to_ahf_units(chunks[0][0], chunks[0][1], box, v_fac)
+    else:
+        pf = torch.cat([c[0] for c in chunks]) if len(chunks) > 1 else chunks[0][0]
+        mom = torch.cat([c[1] for c in chunks]) if len(chunks) > 1 else chunks[0][1]
+    del chunks
     N = int(off[-1])
     w = None
     if multimass:

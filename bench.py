@@ -1,0 +1,418 @@
+"""Benchmark of the unbinding + halo-property stage (one JSON line).
+
+Workload (default): the 1e5-halo snapshot "cfg3" -- 1e5 particle lists with
+N_p ~ N^-1.56 on [20, 2e6] (sum ~ 4e8), float32 positions/velocities, equal
+masses, 64-bit ids -- generated seeded and synthetic on the GPU (AHF ships no
+data).  A step is one call of the stage over the whole batch.
+
+  value   particles/s with the batch resident in HBM (ahfgpu_construct_halos_
+          device), CUDA events on the stream the library runs on
+  e2e     the same through the host API ahfgpu_construct_halos with pinned
+          host buffers: host->device copy of the particle lists and device->
+          host copy of the kept lists, properties and profiles every step
+  roofline  dominant kernel: algorithmic bytes per launch / its CUDA-event
+          duration, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (the reference's algorithm restated in C; the
+          reference's own code where it was built) on all host cores, on a
+          bounded sample of the same haloes
+
+`--impl reference` times that CPU implementation alone on the same workload
+(rank 0; other ranks exit).  Under torchrun every rank processes its own
+full-size batch (seed + rank): weak scaling, no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particles unbound/s"
+UNIT = "particles/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg3")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--mode", default=None, help="form timed for `value` (default: fastest built)")
+    ap.add_argument("--forms", default="all", help="comma list of extra forms to time once, or none")
+    ap.add_argument("--cpu-particles", type=float, default=6e7, help="CPU baseline sample size")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--multimass", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- helpers
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(ws, x: float) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        # median over samples under load (upper half of the clock samples)
+        s = np.sort(np.array(sm))
+        load = s[len(s) // 2:] if len(s) > 3 else s
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": float(max(mx)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str, kernel: str):
+    """Per-particle DRAM traffic of the dominant kernel from the committed ncu
+    summary (profiles/<kernel>_<workload>.md, line 'dram_bytes_per_particle: X')."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    if not os.path.isfile(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("dram_bytes_per_particle:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def alg_bytes(n_in: np.ndarray, res_halo, has_w: bool) -> float:
+    """Compulsory bytes of one call: pos+vel (+mass) read once per gathered
+    particle, the 8-byte id of each kept particle read and written, the centre
+    in, the profile rows and ~256 B of properties out."""
+    nb = res_halo["npart"].astype(np.float64)
+    nbins = res_halo["nbins"].astype(np.float64)
+    per_p = 24.0 + (4.0 if has_w else 0.0)
+    return float(per_p * n_in.sum() + 16.0 * nb.sum() + (24.0 + 256.0) * len(n_in) + 8.0 * 25.0 * nbins.sum())
+
+
+def cpu_sample(n_in: np.ndarray, target: float, seed: int = 99) -> np.ndarray:
+    """Deterministic random subset of haloes with about `target` particles,
+    drawn so the size mix follows the full batch."""
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(len(n_in))
+    cs = np.cumsum(n_in[order])
+    k = int(np.searchsorted(cs, target)) + 1
+    return np.sort(order[:max(1, min(k, len(order)))])
+
+
+def host_lists(lists):
+    """numpy copy of a torch-resident HaloLists."""
+    return lists.to_numpy()
+
+
+def run_cpu(params, lists_np, sample, nthreads):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    sub = lists_np.select(sample)
+    kind = "port"
+    fn = O.run_oracle
+    if O.have_ref(sub.w is not None):
+        kind, fn = "reference", O.run_reference
+    t0 = time.perf_counter()
+    fn(params, sub, nthreads)
+    dt = time.perf_counter() - t0
+    return sub.n, dt, kind
+
+
+# ---------------------------------------------------------------- arms
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    import torch
+    from ahf_gb300 import synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build(ref=None)
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    lists = synth.generate(args.workload, scale=args.scale, device=dev, multimass=args.multimass, as_numpy=True)
+    params = synth.params_for(lists)
+    n_in = np.diff(lists.off.astype(np.int64))
+    nthreads = os.cpu_count() or 1
+    per_step = min(args.cpu_particles, float(n_in.sum()))
+    times, parts, kind = [], [], "port"
+    for s in range(args.warmup + args.steps):
+        samp = cpu_sample(n_in, per_step, seed=1000 + s)
+        n, dt, kind = run_cpu(params, lists, samp, nthreads)
+        if s >= args.warmup:
+            times.append(dt)
+            parts.append(n)
+    value = float(np.sum(parts) / np.sum(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: 1e5 halo particle lists, N_p ~ N^-1.56 on [20,2e6]",
+                   "n_halos": int(len(n_in)), "n_particles": int(n_in.sum()), "scale": args.scale,
+                   "multimass": args.multimass},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
+                         "sample": f"per step a seeded random subset of ~{per_step:.3g} particles of the workload"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def ours_arm(args, ws, rank, local):
+    import ctypes as C
+
+    import torch
+    from ahf_gb300 import abi, lib, synth
+    from ahf_gb300 import build as B
+
+    B.build()
+    torch.cuda.set_device(local)
+    lib.init(local)
+    mode = args.mode or "batched_fp64"
+    seed = synth.CONFIGS[args.workload]["seed"] + rank
+    lists = synth.generate(args.workload, scale=args.scale, device="cuda", multimass=args.multimass,
+                           seed=seed, as_numpy=False)
+    params = synth.params_for(lists)
+    n_in = np.diff(lists.off.astype(np.int64))
+    N = int(n_in.sum())
+    t = {"off": torch.as_tensor(lists.off.astype(np.int64)).cuda()}
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+        t[k] = getattr(lists, k)
+    t["gidx"] = lists.gidx
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(lists, k)).cuda()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    db = lib.device_batch(t)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    def step(m):
+        r = lib.construct_halos_device(params, db, m, sh)
+        return r
+
+    # warm-up
+    for _ in range(args.warmup):
+        r = step(mode)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kern_ms, launches = [], 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        r = step(mode)
+        kern_ms.append(r.stats.ms_device)
+        launches += r.stats.n_launches
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    barrier(ws)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_max = allmax(ws, ms)
+    total_parts = allsum(ws, float(N))
+    value = total_parts / (ms_max / 1e3)
+    res = lib.fetch_result()
+    stats = r.stats
+    balg = alg_bytes(n_in, res.halo, lists.w is not None)
+    kms = float(np.mean(kern_ms))
+    hbm, peak_kind = peaks()
+    achieved = balg / (kms / 1e3) / 1e9
+    tpp = ncu_traffic(args.workload, "halo_fp64_kernel")
+    traffic = tpp * N if tpp is not None else None
+
+    # other forms, once each (same workload)
+    forms = {}
+    if args.forms != "none":
+        want = ["batched_fp64", "plain_fp64"] if args.forms == "all" else args.forms.split(",")
+        for f in want:
+            if f == mode:
+                forms[f] = {"value": value, "ms_per_step": ms}
+                continue
+            try:
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                step(f)
+                a.record(stream)
+                rr = step(f)
+                b.record(stream)
+                torch.cuda.synchronize()
+                fms = a.elapsed_time(b)
+                forms[f] = {"value": N / (fms / 1e3), "ms_per_step": fms, "replay_halos": rr.stats.n_replay_halos}
+            except lib.AhfGpuError as e:
+                forms[f] = {"unavailable": str(e)}
+
+    # e2e through the host API with pinned buffers
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
+            v = getattr(lists, k)
+            if v is None:
+                host[k] = None
+                continue
+            hp = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+            hp.copy_(v)
+            host[k] = hp
+        hb = abi.Batch()
+        off_np = np.ascontiguousarray(lists.off.astype(np.uint64))
+        cen = {k: np.ascontiguousarray(getattr(lists, k)) for k in ("cx", "cy", "cz")}
+        hb.nhalo = len(n_in)
+        hb.off = off_np.ctypes.data_as(C.POINTER(C.c_uint64))
+        for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+            setattr(hb, k, C.cast(C.c_void_p(host[k].data_ptr() if host[k] is not None else None),
+                                  C.POINTER(C.c_float)))
+        hb.gidx = C.cast(C.c_void_p(host["gidx"].data_ptr()), C.POINTER(C.c_uint64))
+        for k in ("cx", "cy", "cz"):
+            setattr(hb, k, cen[k].ctypes.data_as(C.POINTER(C.c_double)))
+        torch.cuda.synchronize()
+        for _ in range(max(1, min(args.warmup, 2))):
+            rr = lib.construct_halos_raw(params, hb, mode)
+            lib.free_result(rr)
+        barrier(ws)
+        e2e_steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(e2e_steps):
+            rr = lib.construct_halos_raw(params, hb, mode)
+            nk = rr.stats.n_kept
+            d2h = nk * 8 + len(n_in) * (C.sizeof(abi.Halo) + 16) + 8 * 25 * int(res.prof_off[-1])
+            lib.free_result(rr)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / e2e_steps
+        dt = allmax(ws, dt)
+        h2d = N * (24 + (4 if lists.w is not None else 0) + 8) + len(n_in) * 32
+        e2e = {"value": total_parts / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "ms_per_step": dt * 1e3}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        lists_np = host_lists(lists)
+        samp = cpu_sample(n_in, args.cpu_particles)
+        nthreads = os.cpu_count() or 1
+        n, dt, kind = run_cpu(params, lists_np, samp, nthreads)
+        cpu = {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": kind,
+               "sample": f"seeded random subset of {len(samp)} haloes / {n} particles of the workload, "
+                         f"{nthreads} OpenMP threads, {dt:.2f} s"}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if "fp64" in mode else "f32+f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: 1e5 halo particle lists, N_p ~ N^-1.56 on [20,2e6], "
+                               f"float32 pos/vel, 64-bit ids, equal masses" + (" (two species)" if args.multimass else ""),
+                   "form": mode, "n_halos": int(len(n_in)), "n_particles": N, "n_kept": int(stats.n_kept),
+                   "scale": args.scale, "l2": "inputs (%.1f GB) larger than L2 (129 MB): no flush" % (N * 32 / 1e9),
+                   "parallelism": f"{ws} independent replica(s), haloes sharded by rank"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "halo_fp64_kernel" if "fp64" in mode else "halo_fp32c_kernel",
+                     "alg_bytes_per_launch": balg, "kernel_ms": kms},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": ck,
+        "gpu_launches": int(launches),
+        "forms": forms,
+        "replay_halos": int(stats.n_replay_halos),
+        "key_ties": int(stats.n_key_ties),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, ws, rank)
+    else:
+        ours_arm(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

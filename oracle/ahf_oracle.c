@@ -733,7 +733,7 @@ int ahforacle_construct_halos(const ahfgpu_params *params, const ahfgpu_batch *b
                               ahfgpu_result *res, int nthreads)
 {
   if (!params || !batch || !res || batch->nhalo < 0 || !batch->off) return AHFGPU_ERR_INVALID;
-  if (params->MINPART < 4) return AHFGPU_ERR_INVALID;
+  if (params->MINPART < 4 || params->MINPART > 128) return AHFGPU_ERR_INVALID;
   int64_t nh = batch->nhalo;
   memset(res, 0, sizeof(*res));
   res->nhalo = nh;

@@ -123,3 +123,52 @@ def _eig_ok(a, b, axis, j, etol):
         gaps.append(np.abs(r[:, j] - r[:, j + 1]))
     degenerate = np.min(np.stack(gaps), 0) < 1e-6
     return zero | degenerate | (dot >= 1.0 - etol)
+
+
+def compare_fp32c(got, exp, rtol_ns=1e-6, rtol_other=1e-4):
+    """FP32-compensated bar: kept lists identical (in order), stage flags and
+    counts identical, the spec properties (M_vir, R_vir, V2_max, R_max,
+    pos_com, bulk velocity, sigV, lambda, lambdaE) within 1e-6 relative, the
+    other per-halo properties and the profile rows within 1e-4 (relative, or
+    absolute against the field's scale where the value itself is a small
+    difference such as com_offset or an eigenvector component)."""
+    bad = []
+    mo_g, mo_e = _get(got, "member_off"), _get(exp, "member_off")
+    if not np.array_equal(mo_g, mo_e):
+        nd = int(np.sum(np.diff(mo_g.astype(np.int64)) != np.diff(mo_e.astype(np.int64))))
+        bad.append(f"member counts differ in {nd} haloes")
+    elif not np.array_equal(_get(got, "member"), _get(exp, "member")):
+        bad.append("member ids/order differ")
+    for k in ("npart", "nbins"):
+        if not np.array_equal(_halo(got, k), _halo(exp, k)):
+            bad.append(f"{k} differs in {int(np.sum(_halo(got, k) != _halo(exp, k)))} haloes")
+    fg = _halo(got, "flags") & HALO_STAGE_MASK
+    fe = _halo(exp, "flags") & HALO_STAGE_MASK
+    if not np.array_equal(fg, fe):
+        bad.append(f"stage flags differ in {int(np.sum(fg != fe))} haloes")
+    nob = (_halo(exp, "flags") & 0x200) != 0
+    for k in NORTH_STAR:
+        e = rel_err(_halo(got, k), _halo(exp, k))
+        if k == "R_vir":
+            e = e[~nob]
+        if e.size and np.max(e) > rtol_ns:
+            bad.append(f"{k}: max rel err {np.max(e):.3e} (north-star bar {rtol_ns:g})")
+    loose = ["ovdens", "Phi0", "v_esc2", "r2", "Ekin", "Epot", "pos_mbp", "vel_mbp", "fMhires", "axis"]
+    for k in loose:
+        e = rel_err(_halo(got, k), _halo(exp, k), 1e-30)
+        if e.size and np.max(e) > rtol_other:
+            bad.append(f"{k}: max rel err {np.max(e):.3e}")
+    for k, scale in (("com_offset", "R_vir"), ("mbp_offset", "R_vir")):
+        d = np.abs(_halo(got, k) - _halo(exp, k)) / np.maximum(np.abs(_halo(exp, scale)), 1e-300)
+        if d.size and np.max(d) > rtol_other:
+            bad.append(f"{k}: max err/R_vir {np.max(d):.3e}")
+    pg, pe = _get(got, "prof"), _get(exp, "prof")
+    if pg.shape != pe.shape:
+        bad.append(f"profile shape {pg.shape} vs {pe.shape}")
+    elif pg.size:
+        cols = [i for i, f in enumerate(PROF_FIELDS) if not f.startswith("E") or f in ("Ekin", "Epot")]
+        e = rel_err(pg[:, cols], pe[:, cols], 1e-30)
+        if np.max(e) > rtol_other:
+            c = cols[int(np.argmax(e.max(0)))]
+            bad.append(f"profile {PROF_FIELDS[c]}: max rel err {np.max(e):.3e}")
+    return bad
