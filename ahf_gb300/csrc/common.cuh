@@ -54,6 +54,7 @@ struct Work {
   double* phi;            // potential prefix of the current pass
   float *fdh, *fdl;       // FP32C: distance as float-float
   float *fdx, *fdy, *fdz; // FP32C: offsets from the centre
+  float *fdxl, *fdyl, *fdzl;  // FP32C: low parts of the offsets
   int* exact_list;        // FP32C: haloes handed to the FP64 form
   unsigned* exact_count;
   uint8_t* flag;          // member (1) / removed (0) per sorted slot

@@ -250,13 +250,15 @@ __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
 __device__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
   unsigned long long ties = 0;
   const uint64_t o = c.o;
+  // mark ambiguous adjacent pairs first (flag is free until gather32)
+  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x)
+    W.flag[o + i] = (i + 1 < c.n && W.keyA[o + i + 1] - W.keyA[o + i] <= 512ull) ? 1 : 0;
+  __syncthreads();
   for (uint64_t i = threadIdx.x; i + 1 < c.n; i += blockDim.x) {
-    bool amb = W.keyA[o + i + 1] - W.keyA[o + i] <= 512ull;
-    bool amb_prev = i > 0 && (W.keyA[o + i] - W.keyA[o + i - 1] <= 512ull);
-    if (!amb || amb_prev) continue;
-    // run [i, j]
+    if (!W.flag[o + i] || (i > 0 && W.flag[o + i - 1])) continue;
+    // run [i, j] of mutually ambiguous neighbours, owned by this thread
     uint64_t j = i + 1;
-    while (j + 1 < c.n && W.keyA[o + j + 1] - W.keyA[o + j] <= 512ull) j++;
+    while (j + 1 < c.n && W.flag[o + j]) j++;
     // insertion sort of the run by (reference key, slot)
     for (uint64_t a = i + 1; a <= j; a++) {
       uint32_t sa = W.idxA[o + a];
@@ -296,9 +298,15 @@ __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W) {
     ff d = ff_sqrt(key_d2(sqkey(dx, dy, dz)));
     W.fdh[s] = d.hi;
     W.fdl[s] = d.lo;
-    W.fdx[s] = __fmul_rn(__ll2float_rn(dx), s62);
-    W.fdy[s] = __fmul_rn(__ll2float_rn(dy), s62);
-    W.fdz[s] = __fmul_rn(__ll2float_rn(dz), s62);
+    // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
+    // centre-of-mass sums)
+    float hx = __ll2float_rn(dx), hy = __ll2float_rn(dy), hz = __ll2float_rn(dz);
+    W.fdx[s] = __fmul_rn(hx, s62);
+    W.fdy[s] = __fmul_rn(hy, s62);
+    W.fdz[s] = __fmul_rn(hz, s62);
+    W.fdxl[s] = __fmul_rn(__ll2float_rn(dx - __float2ll_rn(hx)), s62);
+    W.fdyl[s] = __fmul_rn(__ll2float_rn(dy - __float2ll_rn(hy)), s62);
+    W.fdzl[s] = __fmul_rn(__ll2float_rn(dz - __float2ll_rn(hz)), s62);
     W.svx[s] = B.vx[e];
     W.svy[s] = B.vy[e];
     W.svz[s] = B.vz[e];
@@ -844,25 +852,29 @@ __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W,
 // inertia tensor, 14/15 high/low resolution mass.  VX.. are the momentum
 // prefixes INCLUDING the particle (the reference updates VXc first).
 __device__ __forceinline__ void prof_terms(const DevParams& P, float w, float vx, float vy, float vz, float dx,
-                                           float dy, float dz, ff d, ff dp, ff M, ff VX, ff VY, ff VZ, ff cxf,
-                                           ff cyf, ff czf, float Hrv, ff (&tm)[16], float* Tout) {
-  float Mf = ff_f(M);
-  float dVX = __fsub_rn(vx, __fdiv_rn(ff_f(VX), Mf));
-  float dVY = __fsub_rn(vy, __fdiv_rn(ff_f(VY), Mf));
-  float dVZ = __fsub_rn(vz, __fdiv_rn(ff_f(VZ), Mf));
+                                           float dy, float dz, float dxl, float dyl, float dzl, ff d, ff dp, ff M,
+                                           ff VX, ff VY, ff VZ, ff cxf, ff cyf, ff czf, float Hrv, ff (&tm)[16],
+                                           float* Tout) {
+  // velocity relative to the running bulk velocity, float-float
+  ff gX = ff_sub(fff(vx), ff_div(VX, M));
+  ff gY = ff_sub(fff(vy), ff_div(VY, M));
+  ff gZ = ff_sub(fff(vz), ff_div(VZ, M));
+  float dVX = ff_f(gX), dVY = ff_f(gY), dVZ = ff_f(gZ);
   tm[0] = phi_term(M, w, d, dp);
   tm[1] = two_prod(w, __fsub_rn(__fmul_rn(dy, dVZ), __fmul_rn(dz, dVY)));
   tm[2] = two_prod(w, __fsub_rn(__fmul_rn(dz, dVX), __fmul_rn(dx, dVZ)));
   tm[3] = two_prod(w, __fsub_rn(__fmul_rn(dx, dVY), __fmul_rn(dy, dVX)));
-  dVX = __fadd_rn(dVX, __fmul_rn(Hrv, dx));
-  dVY = __fadd_rn(dVY, __fmul_rn(Hrv, dy));
-  dVZ = __fadd_rn(dVZ, __fmul_rn(Hrv, dz));
-  float T = __fmul_rn(w, __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ)));
-  *Tout = T;
-  tm[4] = fff(T);
-  tm[5] = ff_mulf(ff_add(cxf, fff(dx)), w);
-  tm[6] = ff_mulf(ff_add(cyf, fff(dy)), w);
-  tm[7] = ff_mulf(ff_add(czf, fff(dz)), w);
+  // Hubble drag, then the kinetic term (float-float: Ekin + Epot cancels in
+  // lambdaE)
+  gX = ff_add(gX, ff_mulf(two_sum(dx, dxl), Hrv));
+  gY = ff_add(gY, ff_mulf(two_sum(dy, dyl), Hrv));
+  gZ = ff_add(gZ, ff_mulf(two_sum(dz, dzl), Hrv));
+  ff T = ff_mulf(ff_add(ff_add(ff_mul(gX, gX), ff_mul(gY, gY)), ff_mul(gZ, gZ)), w);
+  *Tout = ff_f(T);
+  tm[4] = T;
+  tm[5] = ff_mulf(ff_add(cxf, two_sum(dx, dxl)), w);
+  tm[6] = ff_mulf(ff_add(cyf, two_sum(dy, dyl)), w);
+  tm[7] = ff_mulf(ff_add(czf, two_sum(dz, dzl)), w);
   tm[8] = two_prod(__fmul_rn(w, dx), dx);
   tm[9] = two_prod(__fmul_rn(w, dy), dy);
   tm[10] = two_prod(__fmul_rn(w, dz), dz);
@@ -943,6 +955,7 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
+    float dxl[kItems], dyl[kItems], dzl[kItems];
     ff d[kItems];
     int nm = 0;
     bool any = false;
@@ -952,11 +965,13 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
       uint64_t i = i0 + k;
       m[k] = i < n1 && (W.flag[o + i] & 1);
       w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
+      dxl[k] = dyl[k] = dzl[k] = 0.f;
       d[k] = ffz();
       if (m[k]) {
         w[k] = W.sw[o + i];
         vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
         dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
+        dxl[k] = W.fdxl[o + i]; dyl[k] = W.fdyl[o + i]; dzl[k] = W.fdzl[o + i];
         d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
         nm++; any = true; lastm = d[k];
       }
@@ -998,7 +1013,7 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
         Mr[k] = M;
         if (!m[k]) continue;
         ff tm[16];
-        prof_terms(P, w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], d[k], dp, M,
+        prof_terms(P, w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], dp, M,
                    ff_add(ff_add(c1[1], e1[1]), l1[k][1]), ff_add(ff_add(c1[2], e1[2]), l1[k][2]),
                    ff_add(ff_add(c1[3], e1[3]), l1[k][3]), cxf, cyf, czf, Hrv, tm, &Tp[k]);
 #pragma unroll
@@ -1120,7 +1135,8 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
               if (!m[kk]) continue;
               ff tm[16];
               float tdummy;
-              prof_terms(P, w[kk], vx[kk], vy[kk], vz[kk], dx[kk], dy[kk], dz[kk], d[kk], dq, Mr[kk],
+              prof_terms(P, w[kk], vx[kk], vy[kk], vz[kk], dx[kk], dy[kk], dz[kk], dxl[kk], dyl[kk], dzl[kk], d[kk],
+                         dq, Mr[kk],
                          ff_add(ff_add(c1[1], e1[1]), l1[kk][1]), ff_add(ff_add(c1[2], e1[2]), l1[kk][2]),
                          ff_add(ff_add(c1[3], e1[3]), l1[kk][3]), cxf, cyf, czf, Hrv, tm, &tdummy);
               for (int q = 0; q < 16; q++) run[q] = ff_add(run[q], tm[q]);

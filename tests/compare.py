@@ -152,7 +152,10 @@ def compare_fp32c(got, exp, rtol_ns=1e-6, rtol_other=1e-4):
         if k == "R_vir":
             e = e[~nob]
         if e.size and np.max(e) > rtol_ns:
-            bad.append(f"{k}: max rel err {np.max(e):.3e} (north-star bar {rtol_ns:g})")
+            ee = e.reshape(len(e), -1).max(1)
+            i = int(np.argmax(ee))
+            bad.append(f"{k}: max rel err {np.max(e):.3e} (north-star bar {rtol_ns:g}) halo {i}: "
+                       f"{_halo(got, k)[i]} vs {_halo(exp, k)[i]}")
     loose = ["ovdens", "Phi0", "v_esc2", "r2", "Ekin", "Epot", "pos_mbp", "vel_mbp", "fMhires", "axis"]
     for k in loose:
         e = rel_err(_halo(got, k), _halo(exp, k), 1e-30)
@@ -166,9 +169,22 @@ def compare_fp32c(got, exp, rtol_ns=1e-6, rtol_other=1e-4):
     if pg.shape != pe.shape:
         bad.append(f"profile shape {pg.shape} vs {pe.shape}")
     elif pg.size:
-        cols = [i for i, f in enumerate(PROF_FIELDS) if not f.startswith("E") or f in ("Ekin", "Epot")]
+        cols = [i for i, f in enumerate(PROF_FIELDS)
+                if (not f.startswith("E") or f in ("Ekin", "Epot")) and f not in ("Lx", "Ly", "Lz")]
         e = rel_err(pg[:, cols], pe[:, cols], 1e-30)
         if np.max(e) > rtol_other:
             c = cols[int(np.argmax(e.max(0)))]
             bad.append(f"profile {PROF_FIELDS[c]}: max rel err {np.max(e):.3e}")
+        # angular momentum per bin: absolute, against the halo's total |L|
+        po = _get(exp, "prof_off")
+        li = [PROF_FIELDS.index(f) for f in ("Lx", "Ly", "Lz")]
+        worst = 0.0
+        for h in range(len(po) - 1):
+            a, b = int(po[h]), int(po[h + 1])
+            if b <= a:
+                continue
+            scale = np.linalg.norm(pe[b - 1, li]) + 1e-300
+            worst = max(worst, float(np.max(np.abs(pg[a:b, li] - pe[a:b, li])) / scale))
+        if worst > rtol_other:
+            bad.append(f"profile L: max abs err / |L_total| {worst:.3e}")
     return bad
