@@ -21,7 +21,10 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = {
     "api.cu": [],
     "halo_fp64.cu": ["--fmad=false"],
-    "halo_fp32c.cu": ["--fmad=false"],
+    "fp32c_class0.cu": ["--fmad=false"],
+    "fp32c_class1.cu": ["--fmad=false"],
+    "fp32c_class2.cu": ["--fmad=false"],
+    "fp32c_dispatch.cu": [],
 }
 
 

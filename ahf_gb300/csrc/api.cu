@@ -21,8 +21,10 @@ namespace ahfgpu {
 size_t fp64_smem_bytes();
 void launch_fp64(const DevParams& P, const DevBatch& B, const Work& W, int grid, int single, cudaStream_t st);
 int fp64_max_blocks_per_sm();
-void launch_fp32c(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st);
-int fp32c_max_blocks_per_sm();
+void launch_fp32c(int cls, const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st);
+int fp32c_max_blocks_per_sm(int cls);
+uint64_t fp32c_class_max(int cls);
+void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
 }  // namespace ahfgpu
 
 using namespace ahfgpu;
@@ -81,7 +83,9 @@ struct Ctx {
   int nsm = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int fp64_bps = 1, fp32c_bps = 1;
+  int fp64_bps = 1, fp32c_bps[3] = {1, 1, 1};
+  cudaStream_t cls_stream[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
   // inputs copied from the host (host API)
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
@@ -194,6 +198,7 @@ struct Plan {
   int64_t nhalo = 0;
   uint64_t N = 0, maxn = 0, nbins_total = 0;
   std::vector<int32_t> queue;
+  int cls_begin[4] = {0, 0, 0, 0};   // queue positions of the FP32C size classes (largest class first)
   std::vector<uint64_t> prof_cap_off;
 };
 
@@ -225,6 +230,14 @@ int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, P
   std::iota(pl.queue.begin(), pl.queue.end(), 0);
   std::stable_sort(pl.queue.begin(), pl.queue.end(),
                    [&](int32_t a, int32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  // the queue is largest first: class 2 (largest) occupies the front
+  int64_t qp = 0;
+  pl.cls_begin[0] = 0;
+  while (qp < nh && off[pl.queue[qp] + 1] - off[pl.queue[qp]] > fp32c_class_max(1)) qp++;
+  pl.cls_begin[1] = (int)qp;
+  while (qp < nh && off[pl.queue[qp] + 1] - off[pl.queue[qp]] > fp32c_class_max(0)) qp++;
+  pl.cls_begin[2] = (int)qp;
+  pl.cls_begin[3] = (int)nh;
   return AHFGPU_OK;
 }
 
@@ -266,8 +279,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   if (rc) return rc;
   if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64 && mode != AHFGPU_BATCHED_FP32C)
     return fail(AHFGPU_ERR_INVALID, "unknown mode %d", (int)mode);
-  const int bps = std::max(g.fp64_bps, g.fp32c_bps);
-  const int grid = std::max(1, g.nsm * bps);
+  const int grid = std::max(1, g.nsm * std::max(g.fp64_bps, g.fp32c_bps[2] + g.fp32c_bps[1]));
   const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(pl.maxn / 512 + 64, 64), 1u << 20);
   if ((rc = ensure_work(pl, grid, stack_cap))) return rc;
   const int64_t nh = pl.nhalo;
@@ -294,6 +306,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   P.r_fac = prm->r_fac; P.x_fac = prm->x_fac; P.v_fac = prm->v_fac; P.m_fac = prm->m_fac;
   P.rho_fac = prm->rho_fac; P.phi_fac = prm->phi_fac; P.Hubble = prm->Hubble;
   P.has_w = db->w != nullptr;
+  P.f_ovlim = (float)prm->ovlim;
+  P.f_rvrf = (float)(prm->rho_vir / prm->rho_fac);
   P.force_serial = 0;
   {
     const char* fe = getenv("AHFGPU_FORCE_EXACT");   // test hook
@@ -365,8 +379,28 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
     launch_fp64(P, B, W, g.nsm * g.fp64_bps, -1, st);
     launches++;
   } else {
-    launch_fp32c(P, B, W, g.nsm * g.fp32c_bps, st);
-    launches++;
+    // size classes on their own streams, largest first; each class has its
+    // own queue, queue head and worklist region
+    CK(cudaEventRecord(g.ev_fork, st));
+    int stack_base = 0;
+    for (int k = 0; k < 3; k++) {
+      int cls = 2 - k;                      // queue segment k holds class 2-k
+      int q0 = pl.cls_begin[k], q1 = pl.cls_begin[k + 1];
+      if (q1 <= q0) continue;
+      int gr = std::min(g.nsm * g.fp32c_bps[cls], q1 - q0);
+      Work Wc = W;
+      Wc.queue = g.queue.as<int32_t>() + q0;
+      Wc.nqueue = q1 - q0;
+      Wc.queue_head = g.qhead.as<unsigned int>() + 2 + k;
+      Wc.sort_stack = g.stack.as<uint4>() + (size_t)stack_base * stack_cap;
+      stack_base += gr;
+      cudaStream_t cs = g.cls_stream[cls];
+      CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
+      launch_fp32c(cls, P, B, Wc, gr, cs);
+      CK(cudaEventRecord(g.ev_join[cls], cs));
+      CK(cudaStreamWaitEvent(st, g.ev_join[cls], 0));
+      launches++;
+    }
     // haloes whose FP64 re-test stayed inside the rounding band: FP64 form
     unsigned nex = 0;
     CK(cudaMemcpyAsync(&nex, g.excount.p, 4, cudaMemcpyDeviceToHost, st));
@@ -381,6 +415,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
     }
     stats->n_fp64_halos = nex;
   }
+  launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
+  launches++;
   CK(cudaGetLastError());
   CK(cudaEventRecord(g.ev1, st));
   // pack
@@ -454,7 +490,12 @@ int ahfgpu_init(int device) {
   CK(cudaEventCreate(&g.ev0));
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
-  g.fp32c_bps = std::max(1, fp32c_max_blocks_per_sm());
+  for (int k = 0; k < 3; k++) {
+    g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
+    CK(cudaStreamCreateWithFlags(&g.cls_stream[k], cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&g.ev_join[k], cudaEventDisableTiming));
+  }
+  CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
   CK(cudaGetLastError());
   g.init = true;
   g_err.clear();
@@ -471,6 +512,11 @@ int ahfgpu_shutdown(void) {
                   &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.exlist, &g.excount, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
+  for (int k = 0; k < 3; k++) {
+    if (g.cls_stream[k]) cudaStreamDestroy(g.cls_stream[k]);
+    if (g.ev_join[k]) cudaEventDestroy(g.ev_join[k]);
+  }
+  if (g.ev_fork) cudaEventDestroy(g.ev_fork);
   if (g.ev0) cudaEventDestroy(g.ev0);
   if (g.ev1) cudaEventDestroy(g.ev1);
   if (g.stream) cudaStreamDestroy(g.stream);

@@ -31,6 +31,8 @@ struct DevParams {
   int has_w;
   int force_serial;   // weight sums not exact in FP64: replay every halo
   int force_exact;    // test hook: every unbinding iteration in exact order
+  float f_ovlim;      // ovlim as float
+  float f_rvrf;       // rho_vir / rho_fac as float
 };
 
 // Input batch, device pointers (entries of halo h: [off[h], off[h+1])).

@@ -158,7 +158,8 @@ static __device__ void write_bin_rows(const Bin* bins, const double* edge, int n
 }
 
 // Integral properties at the end of HaloProfiles (ahf_halos.c:4870-5018),
-// one thread.  cM.. are the totals over the final members, mbe the entry of
+// one thread.  cNFW and cR1 (bisections) are filled afterwards for all
+// haloes at once by concentration_kernel.  cM.. are the totals over the final members, mbe the entry of
 // the most bound particle (-1: none).
 static __device__ void finish_scalars(const double* rows, int nbins, double cM, double cVX, double cVY, double cVZ,
                                double cCx, double cCy, double cCz, double Mhi, double Mlo, long long mbe,
@@ -203,7 +204,6 @@ static __device__ void finish_scalars(const double* rows, int nbins, double cM, 
       hout.lambda = 0.0;
       hout.lambdaE = 0.0;
     }
-    hout.cNFW = calc_cNFW(hout.V2_max, hout.M_vir / hout.R_vir);
     {
       // calc_R1, src/libutility/specific.c:1977-1991
       double r0h = rows[AHFGPU_PROF_R] / 2.0;
@@ -217,7 +217,6 @@ static __device__ void finish_scalars(const double* rows, int nbins, double cM, 
       }
       hout.R1 = 4 * kPi * R1 / hout.M_vir / hout.R_vir;
     }
-    hout.cR1 = calc_cR1(hout.R1);
     {
       double Ts = 2.0 * (last[AHFGPU_PROF_EKIN] - pl[AHFGPU_PROF_EKIN]);
       double frad = fabs(pl[AHFGPU_PROF_R] / last[AHFGPU_PROF_R]);

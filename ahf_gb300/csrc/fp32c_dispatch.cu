@@ -1,0 +1,32 @@
+// fp32c_dispatch.cu -- size classes of the FP32-compensated form: class 0
+// takes lists of up to 512 particles with one-warp CTAs (8 haloes in flight
+// per SM), class 1 lists up to 16384 with four-warp CTAs, class 2 the rest
+// with eight-warp CTAs.
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace ahfgpu {
+
+void launch_fp32c_class0(const DevParams&, const DevBatch&, const Work&, int, cudaStream_t);
+void launch_fp32c_class1(const DevParams&, const DevBatch&, const Work&, int, cudaStream_t);
+void launch_fp32c_class2(const DevParams&, const DevBatch&, const Work&, int, cudaStream_t);
+int fp32c_occupancy_class0();
+int fp32c_occupancy_class1();
+int fp32c_occupancy_class2();
+
+uint64_t fp32c_class_max(int cls) { return cls == 0 ? 512 : cls == 1 ? 16384 : ~0ull; }
+
+void launch_fp32c(int cls, const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
+  if (cls == 0) launch_fp32c_class0(P, B, W, grid, st);
+  else if (cls == 1) launch_fp32c_class1(P, B, W, grid, st);
+  else launch_fp32c_class2(P, B, W, grid, st);
+}
+
+int fp32c_max_blocks_per_sm(int cls) {
+  if (cls == 0) return fp32c_occupancy_class0();
+  if (cls == 1) return fp32c_occupancy_class1();
+  return fp32c_occupancy_class2();
+}
+
+}  // namespace ahfgpu

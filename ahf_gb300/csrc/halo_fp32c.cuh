@@ -1,4 +1,4 @@
-// halo_fp32c.cu -- FP32-compensated batched form of AHF's per-halo
+// halo_fp32c.cuh -- FP32-compensated batched form of AHF's per-halo
 // unbinding + property stage.
 //
 // One persistent grid; each CTA takes haloes from a largest-first queue and
@@ -27,6 +27,7 @@
 // float-float prefixes (n_retest).  If the FP64 re-test is itself inside the
 // reference-rounding band, the halo is queued for the FP64 form, which
 // resolves it in the reference's exact summation order.
+#pragma once
 #include <cstdint>
 #include <cmath>
 
@@ -37,17 +38,17 @@
 
 namespace ahfgpu {
 
-constexpr int kT32 = 256;
-constexpr int kItems = 4;
-constexpr int kTile = kT32 * kItems;
+constexpr int kItems = 4;                 // consecutive slots per thread
 constexpr double kEps64 = 1.1102230246251565e-16;
 constexpr float kBand1 = 2e-5f;      // relative band of the FP32 decisions
 
+template <class SS>
 struct F32Smem {
-  SortSmem sort;
+  SS sort;
   float scan[32 * 2 * 16];
   int iscan[96];
   float lasth[32], lastl[32];
+  double lastd[32];
   int lasti[32];
   double edge[kMaxBins];
   Bin bins[kMaxBins];
@@ -70,27 +71,27 @@ struct Ctx32 {
 // exclusive scan of NC float-float channels; ex = sum over lower threads,
 // tot = block total
 template <int NC>
-__device__ __forceinline__ void bscan_ff(const ff (&v)[NC], ff (&ex)[NC], ff (&tot)[NC], float* sm) {
+__device__ __noinline__ void bscan_ff(const ff (&v)[NC], ff (&ex)[NC], ff (&tot)[NC], float* sm) {
   const unsigned FULL = 0xffffffffu;
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   ff inc[NC];
-#pragma unroll
+#pragma unroll (NC <= 4 ? NC : 1)
   for (int c = 0; c < NC; c++) inc[c] = v[c];
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-#pragma unroll
+#pragma unroll (NC <= 4 ? NC : 1)
     for (int c = 0; c < NC; c++) {
       ff y = {__shfl_up_sync(FULL, inc[c].hi, off), __shfl_up_sync(FULL, inc[c].lo, off)};
       if (lane >= off) inc[c] = ff_add(y, inc[c]);
     }
   }
   if (lane == 31) {
-#pragma unroll
+#pragma unroll (NC <= 4 ? NC : 1)
     for (int c = 0; c < NC; c++) { sm[(wid * NC + c) * 2] = inc[c].hi; sm[(wid * NC + c) * 2 + 1] = inc[c].lo; }
   }
   __syncthreads();
   if (wid == 0) {
-#pragma unroll
+#pragma unroll (NC <= 4 ? NC : 1)
     for (int c = 0; c < NC; c++) {
       ff t = lane < nw ? ff{sm[(lane * NC + c) * 2], sm[(lane * NC + c) * 2 + 1]} : ffz();
 #pragma unroll
@@ -102,7 +103,7 @@ __device__ __forceinline__ void bscan_ff(const ff (&v)[NC], ff (&ex)[NC], ff (&t
     }
   }
   __syncthreads();
-#pragma unroll
+#pragma unroll (NC <= 4 ? NC : 1)
   for (int c = 0; c < NC; c++) {
     ff wp = wid > 0 ? ff{sm[((wid - 1) * NC + c) * 2], sm[((wid - 1) * NC + c) * 2 + 1]} : ffz();
     ff prev = {__shfl_up_sync(FULL, inc[c].hi, 1), __shfl_up_sync(FULL, inc[c].lo, 1)};
@@ -115,7 +116,8 @@ __device__ __forceinline__ void bscan_ff(const ff (&v)[NC], ff (&ex)[NC], ff (&t
 // exclusive "last value" over threads: value of the nearest lower thread with
 // has=true, else carry; any/last describe the whole block (last = carry when
 // no thread has one)
-__device__ __forceinline__ ff blast_ff(bool has, ff val, ff carry, ff* last, F32Smem& S) {
+template <class SM>
+__device__ __forceinline__ ff blast_ff(bool has, ff val, ff carry, ff* last, SM& S) {
   const unsigned FULL = 0xffffffffu;
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned m = __ballot_sync(FULL, has);
@@ -138,14 +140,16 @@ __device__ __forceinline__ ff blast_ff(bool has, ff val, ff carry, ff* last, F32
   return res;
 }
 
-__device__ __forceinline__ int bscan_int_ex(int v, int* tot, F32Smem& S) {
+template <class SM>
+__device__ __forceinline__ int bscan_int_ex(int v, int* tot, SM& S) {
   int t;
   int inc = block_scan_int(v, &t, S.iscan);
   *tot = t;
   return inc - v;
 }
 
-__device__ __forceinline__ long long bmin_ll(long long v, F32Smem& S) {
+template <class SM>
+__device__ __forceinline__ long long bmin_ll(long long v, SM& S) {
   for (int off = 16; off > 0; off >>= 1) {
     long long o = __shfl_xor_sync(0xffffffffu, v, off);
     v = o < v ? o : v;
@@ -225,7 +229,7 @@ __device__ __forceinline__ ff key_d2(uint64_t key) {
 }
 
 // the reference's FP64 squared distance of an entry (ahf_halos.c:5816-5843)
-__device__ __forceinline__ double ref_key(const DevBatch& B, uint64_t e, double cx, double cy, double cz) {
+static __device__ __noinline__ double ref_key(const DevBatch& B, uint64_t e, double cx, double cy, double cz) {
   double dX = wrap_s((double)B.x[e] - cx);
   double dY = wrap_s((double)B.y[e] - cy);
   double dZ = wrap_s((double)B.z[e] - cz);
@@ -233,7 +237,7 @@ __device__ __forceinline__ double ref_key(const DevBatch& B, uint64_t e, double 
 }
 
 // ---------------------------------------------------------------------------
-__device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
+static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
   for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x) {
     uint64_t e = c.o + i;
     long long dx = wrapfix(fixp(B.x[e]) - c.fx);
@@ -247,7 +251,7 @@ __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
 
 // Runs of adjacent keys closer than the reference's rounding are put in the
 // order of the reference's FP64 keys (ties by slot).  Returns exact ties.
-__device__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
+static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
   unsigned long long ties = 0;
   const uint64_t o = c.o;
   // mark ambiguous adjacent pairs first (flag is free until gather32)
@@ -286,7 +290,7 @@ __device__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, c
   return ties;
 }
 
-__device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W) {
+static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W) {
   const float s62 = pow2f(-62);
   for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x) {
     uint64_t s = c.o + i;
@@ -318,15 +322,20 @@ __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W) {
 }
 
 // exact reference distance of the entry in slot s (fabs form, ahf_halos.c:3381-3389)
-__device__ __forceinline__ double ref_dist(const Ctx32& c, const DevBatch& B, const Work& W, uint64_t s) {
+static __device__ __noinline__ double ref_dist(const Ctx32& c, const DevBatch& B, const Work& W, uint64_t s) {
   uint64_t e = c.o + W.seid[s];
   return sqrt(ref_key(B, e, c.cx, c.cy, c.cz));
 }
 
-__device__ __forceinline__ bool dpos(ff d) { return ff_d(d) > kMachineZero; }
+// d > MACHINE_ZERO in float-float (5e-16 = MZH + MZL exactly to ~2^-48)
+__device__ __forceinline__ bool dpos(ff d) {
+  const float MZH = 4.99999997e-16f;              // float nearest 5e-16
+  const float MZL = 2.9753098e-24f;               // 5e-16 - MZH
+  return d.hi > MZH || (d.hi == MZH && d.lo > MZL);
+}
 
 // potential-integral term of a member (ahf_halos.c:3398-3418)
-__device__ __forceinline__ ff phi_term(ff M, float w, ff d, ff dp) {
+static __device__ __noinline__ ff phi_term(ff M, float w, ff d, ff dp) {
   if (!dpos(d)) return ffz();
   ff Mp = ff_sub(M, fff(w));
   ff In = ff_div(M, ff_mul(d, d));
@@ -337,13 +346,12 @@ __device__ __forceinline__ ff phi_term(ff M, float w, ff d, ff dp) {
 
 // FP32 overdensity test with band; FP64 re-test inside the band.  Returns
 // fail (ovdens < ovlim).  M: mass prefix, d: distance (float-float).
-__device__ __forceinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
+static __device__ __noinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
                                         uint64_t s, ff M, ff d, unsigned* nret) {
   const float V43f = (float)(4. * kPi / 3.);
   float df = ff_f(d);
-  float ov = __fdiv_rn(__fdiv_rn(ff_f(M), __fmul_rn(V43f, __fmul_rn(__fmul_rn(df, df), df))),
-                       (float)(P.rho_vir / P.rho_fac));
-  float lim = (float)P.ovlim;
+  float ov = __fdiv_rn(__fdiv_rn(ff_f(M), __fmul_rn(V43f, __fmul_rn(__fmul_rn(df, df), df))), P.f_rvrf);
+  float lim = P.f_ovlim;
   if (isfinite(ov) && fabsf(ov - lim) <= kBand1 * lim) {
     (*nret)++;
     double R = ref_dist(c, B, W, s);
@@ -357,12 +365,13 @@ __device__ __forceinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, const
 // ---------------------------------------------------------------------------
 // rem_outsideRvir(.,0) over all slots, fused with the potential prefix of
 // the first unbinding iteration.  Returns n1; sets *Phi0 (float-float).
-__device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, F32Smem& S,
+template <class SM>
+static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                               ff* Phi0, double* mo, unsigned* nret) {
   ff cM = ffz(), cPhi = ffz();
   long long stop = -1;
   ff stopM = ffz(), stopD = ffz(), stopPhi = ffz();
-  for (uint64_t base = 0; base < c.n; base += kTile) {
+  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     float w[kItems];
     ff d[kItems], dp;
@@ -449,7 +458,7 @@ __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Work& W, 
 // FP64 re-test of a bound decision (reference operation order, own inputs,
 // prefixes from the float-float scans).  Sets *amb when the result is inside
 // the reference's rounding band.
-__device__ __forceinline__ bool retest_bound(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
+static __device__ __noinline__ bool retest_bound(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
                                              uint64_t s, uint64_t pos, uint64_t n1, ff Phi, ff Phi0, ff VX,
                                              ff VY, ff VZ, ff Mv, float vmax, bool* amb) {
   uint64_t e = c.o + W.seid[s];
@@ -495,7 +504,8 @@ struct IterOut {
   int rounds;
 };
 
-__device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, F32Smem& S,
+template <class SM>
+static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                             uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out, unsigned* nret) {
   const uint64_t o = c.o;
   const float vf = (float)P.v_fac, Hr = (float)(P.Hubble * P.r_fac), v2t = (float)P.v2_tune;
@@ -509,7 +519,7 @@ __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, co
   long long cNb = 0, last_slot = -1, rv = -1;
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
-  for (uint64_t base = 0; base < n1; base += kTile) {
+  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
@@ -665,7 +675,7 @@ __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, co
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
-      if (i < n1) W.flag[o + i] = b[k] ? 1 : 0;
+      if (i < n1) W.flag[o + i] = (uint8_t)((m[k] ? 1 : 0) | (b[k] ? 2 : 0));
     }
     cM = ff_add(cM, totM[0]);
     cPhi = ff_add(cPhi, totP[0]);
@@ -689,9 +699,251 @@ __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, co
 }
 
 // ---------------------------------------------------------------------------
+// Warp-sequential prefix in exactly a C loop's order (one FP64 rounding per
+// addition); see halo_fp64.cu.  incl: out[i] includes a[i].
+static __device__ double chain64(const double* a, double* out, uint64_t n, double s0, int incl) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31;
+  double s = s0;
+  for (uint64_t base = 0; base < n; base += 32) {
+    uint64_t i = base + lane;
+    double t = i < n ? a[i] : 0.0;
+    double mine = s;
+#pragma unroll
+    for (int k = 0; k < 32; k++) {
+      double tk = __shfl_sync(FULL, t, k);
+      if (!incl && k == lane) mine = s;
+      s += tk;
+      if (incl && k == lane) mine = s;
+    }
+    if (i < n) out[i] = mine;
+  }
+  return s;
+}
+
+// One rem_unbound iteration in the reference's exact summation order, for a
+// pass whose FP64 re-test stayed inside the rounding band.  Members: flag
+// bit0 of [0, n1); bit1 = speculated bound flags on entry, exact on exit.
+// Per-member distances and offsets are recomputed in FP64 from the inputs
+// exactly as the reference computes them; the order-dependent sums are warp
+// chains.  Returns kept count/mass, last kept slot.
+template <class SM>
+static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                             uint64_t n1, uint64_t js, long long* nb_out, double* mb_out, long long* last_out) {
+  const uint64_t o = c.o;
+  double* term = W.phi + o;
+  double* d64 = W.prof_a + o;
+  double* ax = W.prof_b + o;
+  double* ay = W.prof_c + o;
+  double* az = W.prof_d + o;
+  double* dsm = reinterpret_cast<double*>(S.scan);
+  double carryM = 0.0, carryD = 0.0;
+  for (uint64_t base = 0; base < n1; base += blockDim.x) {
+    uint64_t i = base + threadIdx.x;
+    bool mem = i < n1 && (W.flag[o + i] & 1);
+    double w = mem ? (double)W.sw[o + i] : 0.0;
+    double d = mem ? ref_dist(c, B, W, o + i) : 0.0;
+    if (i < n1) d64[i] = d;
+    bool any;
+    double lastd;
+    double dprev = block_last_excl(mem, d, carryD, &any, &lastd, S.lastd, S.lasti);
+    double v[1] = {w}, tot[1];
+    block_scan<1>(v, tot, dsm);
+    double M = carryM + v[0];
+    double t = 0.0;
+    if (mem && d > kMachineZero) {
+      double Mprev = M - w;
+      double Iprev = dprev > kMachineZero ? Mprev / (dprev * dprev) : 0.0;
+      double Inow = M / (d * d);
+      t = ((Inow + Iprev) / 2.) * (d - dprev);
+    }
+    if (i < n1) term[i] = t;
+    carryM += tot[0];
+    carryD = lastd;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double s = chain64(term, term, n1, 0.0, 1);
+    if (threadIdx.x == 0) S.bd[20] = s;
+  }
+  __syncthreads();
+  const double Phi0 = S.bd[20] + carryM / carryD;
+  const double w0 = (double)W.sw[o + js];
+  const double sVX = w0 * (double)W.svx[o + js], sVY = w0 * (double)W.svy[o + js], sVZ = w0 * (double)W.svz[o + js];
+  long long nb = 0, last = -1;
+  double Mb = 0.0;
+  int nwarps = blockDim.x >> 5;
+  while (true) {
+    for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) {
+      uint8_t f = W.flag[o + i];
+      bool b = (f & 1) && ((f >> 1) & 1);
+      double w = b ? (double)W.sw[o + i] : 0.0;
+      ax[i] = b ? w * (double)W.svx[o + i] : 0.0;
+      ay[i] = b ? w * (double)W.svy[o + i] : 0.0;
+      az[i] = b ? w * (double)W.svz[o + i] : 0.0;
+    }
+    __syncthreads();
+    int warp = threadIdx.x >> 5;
+    if (nwarps >= 3) {
+      if (warp == 0) chain64(ax, ax, n1, sVX, 0);
+      else if (warp == 1) chain64(ay, ay, n1, sVY, 0);
+      else if (warp == 2) chain64(az, az, n1, sVZ, 0);
+    } else if (warp == 0) {
+      chain64(ax, ax, n1, sVX, 0);
+      chain64(ay, ay, n1, sVY, 0);
+      chain64(az, az, n1, sVZ, 0);
+    }
+    __syncthreads();
+    int changed = 0;
+    double cMV = w0, cMb = 0.0;
+    long long cNb = 0, cLast = -1;
+    for (uint64_t base = 0; base < n1; base += blockDim.x) {
+      uint64_t i = base + threadIdx.x;
+      uint8_t f = i < n1 ? W.flag[o + i] : 0;
+      bool mem = f & 1;
+      bool b = mem && ((f >> 1) & 1);
+      double w = mem ? (double)W.sw[o + i] : 0.0;
+      double cw = b ? w : 0.0;
+      double v[1] = {cw}, ex[1], tot[1];
+      block_scan_excl<1>(v, ex, tot, dsm);
+      if (mem) {
+        double M_vel = cMV + ex[0];
+        uint64_t e = o + W.seid[o + i];
+        double dX = wrap_s((double)B.x[e] - c.cx), dY = wrap_s((double)B.y[e] - c.cy), dZ = wrap_s((double)B.z[e] - c.cz);
+        double d = d64[i];
+        double v_esc2 = d > kMachineZero ? (2 * fabs(term[i] - Phi0) * P.phi_fac) : 1e30;
+        double VXp = (double)W.svx[o + i], VYp = (double)W.svy[o + i], VZp = (double)W.svz[o + i];
+        double dVX = (VXp - ax[i] / M_vel) * P.v_fac + P.Hubble * (dX) * P.r_fac;
+        double dVY = (VYp - ay[i] / M_vel) * P.v_fac + P.Hubble * (dY) * P.r_fac;
+        double dVZ = (VZp - az[i] / M_vel) * P.v_fac + P.Hubble * (dZ) * P.r_fac;
+        double vel2 = (dVX * dVX + dVY * dVY) + dVZ * dVZ;
+        bool nbv = !(vel2 > P.v2_tune * v_esc2);
+        if (nbv != b) changed = 1;
+        W.flag[o + i] = (uint8_t)(1 | (nbv ? 2 : 0));
+      }
+      int tcnt;
+      block_scan_int(b ? 1 : 0, &tcnt, S.iscan);
+      unsigned bb = __ballot_sync(0xffffffffu, b);
+      int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      if (lane == 0) S.iscan[64 + wid] = bb ? (wid * 32 + 31 - __clz(bb)) : -1;
+      __syncthreads();
+      int lt = -1;
+      for (int q = 0; q < nwarps; q++) lt = max(lt, S.iscan[64 + q]);
+      __syncthreads();
+      if (lt >= 0) cLast = (long long)(base + lt);
+      cMb += tot[0];
+      cMV += tot[0];
+      cNb += tcnt;
+    }
+    if (!__syncthreads_or(changed)) {
+      nb = cNb;
+      Mb = cMb;
+      last = cLast;
+      break;
+    }
+  }
+  if (threadIdx.x == 0) S.bd[21] = Phi0;
+  __syncthreads();
+  *nb_out = nb;
+  *mb_out = Mb;
+  *last_out = last;
+}
+
+// potential zero point Phi0 of the members in [0, n1) (the Phi0 pass,
+// ahf_halos.c:3343-3426), float-float
+template <class SM>
+static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, SM& S, uint64_t n1) {
+  const uint64_t o = c.o;
+  ff cM = ffz(), cPhi = ffz(), cD = ffz();
+  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
+    uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
+    bool m[kItems];
+    float w[kItems];
+    ff d[kItems];
+    bool any = false;
+    ff lastm = ffz();
+    ff accM = ffz(), locM[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      uint64_t i = i0 + k;
+      m[k] = i < n1 && (W.flag[o + i] & 1);
+      w[k] = m[k] ? W.sw[o + i] : 0.f;
+      d[k] = m[k] ? ff{W.fdh[o + i], W.fdl[o + i]} : ffz();
+      if (m[k]) { accM = ff_add(accM, fff(w[k])); any = true; lastm = d[k]; }
+      locM[k] = accM;
+    }
+    ff exM[1], totM[1], vM[1] = {accM};
+    bscan_ff<1>(vM, exM, totM, S.scan);
+    ff blockLast;
+    ff dp = blast_ff(any, lastm, cD, &blockLast, S);
+    ff accP = ffz();
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      if (!m[k]) continue;
+      accP = ff_add(accP, phi_term(ff_add(ff_add(cM, exM[0]), locM[k]), w[k], d[k], dp));
+      dp = d[k];
+    }
+    ff exP[1], totP[1], vP[1] = {accP};
+    bscan_ff<1>(vP, exP, totP, S.scan);
+    cM = ff_add(cM, totM[0]);
+    cPhi = ff_add(cPhi, totP[0]);
+    cD = blockLast;
+  }
+  return ff_add(cPhi, ff_div(cM, cD));
+}
+
+// rem_outsideRvir(.,1) over the members of [0, n1): slot of the first member
+// failing the overdensity test (-1: none) and the mass prefix there
+template <class SM>
+static __device__ long long rvir_pass32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                                 uint64_t n1, ff* Mfail, unsigned* nret) {
+  const uint64_t o = c.o;
+  ff cM = ffz();
+  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
+    uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
+    bool m[kItems];
+    float w[kItems];
+    ff accM = ffz(), locM[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      uint64_t i = i0 + k;
+      m[k] = i < n1 && (W.flag[o + i] & 1);
+      w[k] = m[k] ? W.sw[o + i] : 0.f;
+      if (m[k]) accM = ff_add(accM, fff(w[k]));
+      locM[k] = accM;
+    }
+    ff exM[1], totM[1], vM[1] = {accM};
+    bscan_ff<1>(vM, exM, totM, S.scan);
+    long long myfail = 0x7fffffffffffffffll;
+    ff fM = ffz();
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      if (!m[k] || myfail != 0x7fffffffffffffffll) continue;
+      ff M = ff_add(ff_add(cM, exM[0]), locM[k]);
+      if (ov_fail(c, B, W, P, o + i0 + k, M, ff{W.fdh[o + i0 + k], W.fdl[o + i0 + k]}, nret)) {
+        myfail = (long long)(i0 + k);
+        fM = M;
+      }
+    }
+    long long f = bmin_ll(myfail, S);
+    if (f != 0x7fffffffffffffffll) {
+      if (myfail == f) { S.bf[0] = fM.hi; S.bf[1] = fM.lo; }
+      __syncthreads();
+      *Mfail = ff{S.bf[0], S.bf[1]};
+      __syncthreads();
+      return f;
+    }
+    cM = ff_add(cM, totM[0]);
+  }
+  *Mfail = cM;
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
 // seed slot of the bulk velocity (ahf_halos.c:3441-3470)
-__device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevParams& P, int niter, uint64_t n1,
-                              F32Smem& S) {
+template <class SM>
+static __device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevParams& P, int niter, uint64_t n1,
+                              SM& S) {
   if (threadIdx.x == 0) {
     uint64_t js = 0;
     if (niter == 1) {
@@ -727,7 +979,7 @@ __device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevParams& P,
 // ---------------------------------------------------------------------------
 // smoothed maximum with an FP64 re-check of every FP32 candidate
 // (find_max, src/libutility/general.c:608-650, on ranks nignore..n2-1)
-__device__ double raw64(const Ctx32& c, const DevBatch& B, const Work& W, const double* d64c, int which,
+static __device__ __noinline__ double raw64(const Ctx32& c, const DevBatch& B, const Work& W, const double* d64c, int which,
                         uint64_t r) {
   // which 0: dens_r2 (ahf_halos.c:4610-4616), 1: Vcirc2 (:4612)
   const float2* Mff = reinterpret_cast<const float2*>(W.prof_b + c.o);
@@ -745,14 +997,14 @@ __device__ double raw64(const Ctx32& c, const DevBatch& B, const Work& W, const 
   return dM / dV * (rm * rm);
 }
 
-__device__ double rank_dist64(const Ctx32& c, const DevBatch& B, const Work& W, uint64_t r) {
+static __device__ __noinline__ double rank_dist64(const Ctx32& c, const DevBatch& B, const Work& W, uint64_t r) {
   const uint32_t* ent = reinterpret_cast<const uint32_t*>(W.prof_d + c.o);
   return sqrt(ref_key(B, c.o + ent[r], c.cx, c.cy, c.cz));
 }
 
 // FP64 smoothed value at index i of the array y[j] = raw(j + kNignore),
 // j in [0, m), after ns passes of smooth3
-__device__ double smooth_at64(const Ctx32& c, const DevBatch& B, const Work& W, int which, uint64_t m, int ns,
+static __device__ __noinline__ double smooth_at64(const Ctx32& c, const DevBatch& B, const Work& W, int which, uint64_t m, int ns,
                               uint64_t i) {
   double lvl[8][8];
   long long lo = (long long)i - ns, hi = (long long)i + ns;
@@ -782,7 +1034,8 @@ __device__ double smooth_at64(const Ctx32& c, const DevBatch& B, const Work& W, 
   return lvl[ns][i - lo];
 }
 
-__device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W, F32Smem& S, int which, int ns,
+template <class SM>
+static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W, SM& S, int which, int ns,
                                uint64_t n2, unsigned* nret) {
   uint64_t m = n2 - kNignore;
   float* y = reinterpret_cast<float*>(W.prof_c + c.o) + (which ? 0 : n2);
@@ -851,7 +1104,7 @@ __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W,
 // integral, 1-3 angular momentum, 4 kinetic T, 5-7 centre of mass, 8-13
 // inertia tensor, 14/15 high/low resolution mass.  VX.. are the momentum
 // prefixes INCLUDING the particle (the reference updates VXc first).
-__device__ __forceinline__ void prof_terms(const DevParams& P, float w, float vx, float vy, float vz, float dx,
+static __device__ __noinline__ void prof_terms(const DevParams& P, float w, float vx, float vy, float vz, float dx,
                                            float dy, float dz, float dxl, float dyl, float dzl, ff d, ff dp, ff M,
                                            ff VX, ff VY, ff VZ, ff cxf, ff cyf, ff czf, float Hrv, ff (&tm)[16],
                                            float* Tout) {
@@ -893,7 +1146,8 @@ __device__ __forceinline__ void prof_terms(const DevParams& P, float w, float vx
 
 // ---------------------------------------------------------------------------
 // HaloProfiles (ahf_halos.c:3961-5261) over the n2 members of [0, n1)
-__device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, F32Smem& S,
+template <class SM>
+static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                            uint64_t n1, uint64_t n2, ff Phi0, ahfgpu_halo& hout, unsigned* nret) {
   const uint64_t o = c.o;
   const double FPT = 4. * kPi / 3.;
@@ -929,14 +1183,14 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
     double dmax = rank_dist64(c, B, W, n2 - 1);
     if (dmin < kMachineZero) dmin = dmax / 2.;
     double ld0 = log10(dmin), ld1 = log10(dmax);
-    double ldr = (ld1 - ld0) / (double)nb;
-    for (int b = 0; b < nb; b++) {
-      double e = pow(10., ld0 + ((double)b + 1) * ldr);
-      if (b == nb - 1) e = dmax + kZero;
-      S.edge[b] = e;
-    }
+    S.bd[2] = ld0;
+    S.bd[3] = (ld1 - ld0) / (double)nb;
+    S.bd[1] = dmax;
     S.bi[0] = nb;
   }
+  __syncthreads();
+  for (int b = threadIdx.x; b < S.bi[0]; b += blockDim.x)
+    S.edge[b] = b == S.bi[0] - 1 ? S.bd[1] + kZero : pow(10., S.bd[2] + ((double)b + 1) * S.bd[3]);
   __syncthreads();
   const int nbins = S.bi[0];
   const float vf = (float)P.v_fac;
@@ -951,7 +1205,7 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
   int cr = 0;
   double Ebest = 1e30;
   long long Eslot = -1;
-  for (uint64_t base = 0; base < n1; base += kTile) {
+  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
@@ -1208,7 +1462,7 @@ __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, con
 }
 
 // ---------------------------------------------------------------------------
-__device__ void write_members32(const Ctx32& c, uint64_t nlist, const DevBatch& B, const Work& W) {
+static __device__ void write_members32(const Ctx32& c, uint64_t nlist, const DevBatch& B, const Work& W) {
   int carry = 0;
   __shared__ int isc[64];
   for (uint64_t base = 0; base < nlist; base += blockDim.x) {
@@ -1225,7 +1479,8 @@ __device__ void write_members32(const Ctx32& c, uint64_t nlist, const DevBatch& 
   __syncthreads();
 }
 
-__device__ void process_halo32(int h, const DevParams& P, const DevBatch& B, const Work& W, F32Smem& S,
+template <class SM>
+static __device__ void process_halo32(int h, const DevParams& P, const DevBatch& B, const Work& W, SM& S,
                                uint4* stack) {
   Ctx32 c;
   c.h = h;
@@ -1291,23 +1546,50 @@ __device__ void process_halo32(int h, const DevParams& P, const DevBatch& B, con
     uint64_t npart = n1;
     uint64_t nremove = 4;
     int niter = 0, maxr = 0, nob = 0;
-    double R_vir = 0.0, M_vir = 0.0;
+    double R_vir = 0.0, M_vir = 0.0, Phi0_exact = 0.0;
     ff Phi0_used = Phi0;
     IterOut it;
+    bool last_exact = false;
+    int nexact = 0;
     while (nremove > 3) {
       niter++;
       uint64_t js = seed_slot(c, W, P, niter, n1, S);
       Phi0_used = Phi0;
       unbind_pass(c, B, W, P, S, n1, Phi0, js, vmax, it, &nret);
-      if (it.amb) { to_fp64 = true; break; }
+      last_exact = it.amb != 0;
+      if (last_exact) {
+        // a bound decision inside the reference's rounding band: redo this
+        // iteration in the reference's exact summation order
+        long long nbx, lsx;
+        double mbx;
+        exact_iter32(c, B, W, P, S, n1, js, &nbx, &mbx, &lsx);
+        Phi0_used = ff_from_d(S.bd[21]);
+        Phi0_exact = S.bd[21];
+        it.nb = nbx;
+        it.Mb = ff_from_d(mbx);
+        it.last_slot = lsx;
+        nexact++;
+      }
+      // members <- bound
+      for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) W.flag[c.o + i] = (W.flag[c.o + i] >> 1) & 1;
+      __syncthreads();
       if (it.rounds > maxr) maxr = it.rounds;
       nremove = npart - (uint64_t)it.nb;
       npart = (uint64_t)it.nb;
       if (it.nb == 0) nob = 1;
       M_vir = ff_d(it.Mb);
       if (it.last_slot >= 0) R_vir = ref_dist(c, B, W, c.o + it.last_slot);
-      Phi0 = it.Phi0n;
+      Phi0 = last_exact ? (npart > 0 ? phi0_pass32(c, W, S, n1) : ffz()) : it.Phi0n;
       if (((double)npart) < ((double)P.MINPART)) break;
+    }
+    if (nexact && threadIdx.x == 0) {
+      atomicAdd(&W.counters[1], 1ull);
+      hout.flags |= AHFGPU_HALO_REPLAYED;
+    }
+    if (last_exact && npart >= (uint64_t)P.MINPART) {
+      ff Mf;
+      it.rv_slot = rvir_pass32(c, B, W, P, S, n1, &Mf, &nret);
+      it.rv_M = Mf;
     }
     if (!to_fp64) {
       if (threadIdx.x == 0) {
@@ -1315,7 +1597,7 @@ __device__ void process_halo32(int h, const DevParams& P, const DevBatch& B, con
         if (nob) hout.flags |= AHFGPU_HALO_NOBOUND;
         hout.M_vir = M_vir;
         hout.R_vir = R_vir;
-        hout.Phi0 = ff_d(Phi0_used);
+        hout.Phi0 = last_exact ? Phi0_exact : ff_d(Phi0_used);
         hout.niter = niter;
         hout.fix_rounds = maxr;
       }
@@ -1373,9 +1655,11 @@ __device__ void process_halo32(int h, const DevParams& P, const DevBatch& B, con
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kT32, 1) halo_fp32c_kernel(DevParams P, DevBatch B, Work W) {
+template <int T, class SS>
+__global__ void __launch_bounds__(T) halo_fp32c_kernel(DevParams P, DevBatch B, Work W) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  F32Smem& S = *reinterpret_cast<F32Smem*>(smem_raw);
+  using SM = F32Smem<SS>;
+  SM& S = *reinterpret_cast<SM*>(smem_raw);
   uint4* stack = W.sort_stack + (uint64_t)blockIdx.x * W.stack_cap;
   while (true) {
     if (threadIdx.x == 0) S.bi[15] = (int)atomicAdd(W.queue_head, 1u);
@@ -1385,17 +1669,6 @@ __global__ void __launch_bounds__(kT32, 1) halo_fp32c_kernel(DevParams P, DevBat
     if (q >= W.nqueue) break;
     process_halo32(W.queue[q], P, B, W, S, stack);
   }
-}
-
-void launch_fp32c(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<<<grid, kT32, sizeof(F32Smem), st>>>(P, B, W);
-}
-
-int fp32c_max_blocks_per_sm() {
-  int nb = 0;
-  cudaFuncSetAttribute(halo_fp32c_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(F32Smem));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel, kT32, sizeof(F32Smem));
-  return nb;
 }
 
 }  // namespace ahfgpu

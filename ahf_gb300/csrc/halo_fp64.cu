@@ -753,16 +753,15 @@ __device__ void profiles(const HaloCtx& c, uint64_t n1, uint64_t n2, const DevPa
     double dmax = radius[n2 - 1];
     if (dmin < kMachineZero) dmin = dmax / 2.;
     double ld0 = log10(dmin), ld1 = log10(dmax);
-    double ldr = (ld1 - ld0) / (double)nb;
-    for (int b = 0; b < nb; b++) {
-      double e = pow(10., ld0 + ((double)b + 1) * ldr);
-      if (b == nb - 1) e = dmax + kZero;
-      S.edge[b] = e;
-    }
+    S.bd[2] = ld0;
+    S.bd[3] = (ld1 - ld0) / (double)nb;
     S.bi[0] = nb;
     S.bd[0] = dmin;
     S.bd[1] = dmax;
   }
+  __syncthreads();
+  for (int b = threadIdx.x; b < S.bi[0]; b += blockDim.x)
+    S.edge[b] = b == S.bi[0] - 1 ? S.bd[1] + kZero : pow(10., S.bd[2] + ((double)b + 1) * S.bd[3]);
   __syncthreads();
   const int nbins = S.bi[0];
   const double Phi0 = hout.Phi0;
@@ -1072,6 +1071,21 @@ __global__ void __launch_bounds__(kT, 1) halo_fp64_kernel(DevParams P, DevBatch 
     if (q >= W.nqueue) break;
     process_halo(W.queue[q], P, B, W, S, stack);
   }
+}
+
+// cNFW (src/libutility/specific.c:2041-2072) and cR1 (:1993-2018) of every
+// halo whose profile pass ran: one thread per halo, after the halo kernels.
+__global__ void concentration_kernel(ahfgpu_halo* halo, int64_t nh) {
+  for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += (int64_t)gridDim.x * blockDim.x) {
+    ahfgpu_halo& o = halo[h];
+    if (!(o.flags & AHFGPU_HALO_RAN_PROFILE)) continue;
+    o.cNFW = calc_cNFW(o.V2_max, o.M_vir / o.R_vir);
+    o.cR1 = calc_cR1(o.R1);
+  }
+}
+
+void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st) {
+  concentration_kernel<<<grid, 128, 0, st>>>(halo, nh);
 }
 
 size_t fp64_smem_bytes() { return sizeof(HaloSmem); }

@@ -21,18 +21,22 @@
 namespace ahfgpu {
 
 constexpr int kChunk = 2048;          // pairs sorted in shared memory at once
-constexpr int kHalfChunk = kChunk / 2;
 constexpr int kSortBuckets = 4096;
 
-struct SortSmem {
-  uint64_t key[kChunk];
-  uint32_t idx[kChunk];
-  uint32_t hist[kSortBuckets];
+// CH: pairs sorted in shared memory at once; NB: most buckets of one pass
+template <int CH, int NB>
+struct SortSmemT {
+  static constexpr int kCh = CH;
+  static constexpr int kNb = NB;
+  uint64_t key[CH];
+  uint32_t idx[CH];
+  uint32_t hist[NB];
   uint64_t red_u64[64];
   int sp;                 // worklist depth
   int seg_lo, seg_hi;     // current run of buckets
   int flag;
 };
+using SortSmem = SortSmemT<kChunk, kSortBuckets>;
 
 __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb, uint32_t ib) {
   return ka < kb || (ka == kb && ia < ib);
@@ -40,8 +44,9 @@ __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb,
 
 // Sort `cnt` (<= kChunk) pairs from (ks, is)[lo..] into (kd, id)[lo..].
 // In-place (ks == kd) is allowed: the data goes through shared memory.
+template <class SS>
 static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
-                                uint64_t lo, int cnt, SortSmem& S) {
+                                       uint64_t lo, int cnt, SS& S) {
   int P = 1;
   while (P < cnt) P <<= 1;
   for (int i = threadIdx.x; i < P; i += blockDim.x) {
@@ -80,7 +85,8 @@ static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, u
 }
 
 // Block min/max over a u64 sequence.
-__device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, SortSmem& S) {
+template <class SS>
+__device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, SS& S) {
   const unsigned FULL = 0xffffffffu;
   for (int off = 16; off > 0; off >>= 1) {
     uint64_t a = __shfl_xor_sync(FULL, mn, off);
@@ -102,8 +108,12 @@ __device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, Sor
 // Sort (keyA, idxA)[o, o+n) in place by (key, slot).  Uses (keyB, idxB) and
 // the CTA's worklist `stack` (capacity cap) as scratch.  Returns false when
 // the worklist overflows (the caller reports kErrWorklist).
+template <class SS>
 static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
-                            uint64_t n, uint4* stack, int cap, SortSmem& S) {
+                                   uint64_t n, uint4* stack, int cap, SS& S) {
+  constexpr int kChunk = SS::kCh;
+  constexpr int kHalfChunk = SS::kCh / 2;
+  constexpr int kSortBuckets = SS::kNb;
   if (n <= 1) return true;
   if (n <= (uint64_t)kChunk) {
     smem_sort_chunk(keyA, idxA, keyA, idxA, o, (int)n, S);

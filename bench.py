@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--mode", default=None, help="form timed for `value` (default: fastest built)")
     ap.add_argument("--forms", default="all", help="comma list of extra forms to time once, or none")
     ap.add_argument("--cpu-particles", type=float, default=6e7, help="CPU baseline sample size")
+    ap.add_argument("--plain-particles", type=float, default=2e7, help="plain FP64 form sample size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--multimass", action="store_true")
@@ -182,6 +183,24 @@ def cpu_sample(n_in: np.ndarray, target: float, seed: int = 99) -> np.ndarray:
     return np.sort(order[:max(1, min(k, len(order)))])
 
 
+def _device_subset(lists, halos):
+    """torch dict of a halo subset of a device-resident HaloLists."""
+    import torch
+    halos = np.asarray(halos, np.int64)
+    off = lists.off.astype(np.int64)
+    cnt = off[halos + 1] - off[halos]
+    noff = np.zeros(len(halos) + 1, np.int64)
+    noff[1:] = np.cumsum(cnt)
+    idx = torch.as_tensor(np.concatenate([np.arange(off[h], off[h + 1]) for h in halos]), device="cuda")
+    t = {"off": torch.as_tensor(noff, device="cuda")}
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
+        v = getattr(lists, k)
+        t[k] = None if v is None else v[idx].contiguous()
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(lists, k)[halos], device="cuda")
+    return t
+
+
 def host_lists(lists):
     """numpy copy of a torch-resident HaloLists."""
     return lists.to_numpy()
@@ -249,7 +268,7 @@ def ours_arm(args, ws, rank, local):
     B.build()
     torch.cuda.set_device(local)
     lib.init(local)
-    mode = args.mode or "batched_fp64"
+    mode = args.mode or "batched_fp32c"
     seed = synth.CONFIGS[args.workload]["seed"] + rank
     lists = synth.generate(args.workload, scale=args.scale, device="cuda", multimass=args.multimass,
                            seed=seed, as_numpy=False)
@@ -296,33 +315,47 @@ def ours_arm(args, ws, rank, local):
     value = total_parts / (ms_max / 1e3)
     res = lib.fetch_result()
     stats = r.stats
+    headline_stats = {"replay_halos": int(stats.n_replay_halos), "key_ties": int(stats.n_key_ties),
+                      "retests": int(stats.n_retest), "fp64_halos": int(stats.n_fp64_halos)}
     balg = alg_bytes(n_in, res.halo, lists.w is not None)
     kms = float(np.mean(kern_ms))
     hbm, peak_kind = peaks()
     achieved = balg / (kms / 1e3) / 1e9
-    tpp = ncu_traffic(args.workload, "halo_fp64_kernel")
+    kname = "halo_fp64_kernel" if "fp64" in mode else "halo_fp32c_kernel"
+    tpp = ncu_traffic(args.workload, kname)
     traffic = tpp * N if tpp is not None else None
 
     # other forms, once each (same workload)
     forms = {}
     if args.forms != "none":
-        want = ["batched_fp64", "plain_fp64"] if args.forms == "all" else args.forms.split(",")
+        want = ["batched_fp32c", "batched_fp64", "plain_fp64"] if args.forms == "all" else args.forms.split(",")
         for f in want:
             if f == mode:
-                forms[f] = {"value": value, "ms_per_step": ms}
+                forms[f] = {"value": value, "ms_per_step": ms, "sample": "whole workload"}
                 continue
             try:
+                db_f, nf, desc = db, N, "whole workload"
+                if f == "plain_fp64":
+                    # one launch per halo: timed on a bounded random sample of the haloes
+                    samp = cpu_sample(n_in, args.plain_particles, seed=7)
+                    sub = _device_subset(lists, samp)
+                    db_f, nf = lib.device_batch(sub), int(n_in[samp].sum())
+                    desc = f"seeded random subset of {len(samp)} haloes / {nf} particles"
                 torch.cuda.synchronize()
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                step(f)
+                lib.construct_halos_device(params, db_f, f, sh)
                 a.record(stream)
-                rr = step(f)
+                rr = lib.construct_halos_device(params, db_f, f, sh)
                 b.record(stream)
                 torch.cuda.synchronize()
                 fms = a.elapsed_time(b)
-                forms[f] = {"value": N / (fms / 1e3), "ms_per_step": fms, "replay_halos": rr.stats.n_replay_halos}
+                forms[f] = {"value": nf / (fms / 1e3), "ms_per_step": fms, "sample": desc,
+                            "replay_halos": int(rr.stats.n_replay_halos)}
             except lib.AhfGpuError as e:
                 forms[f] = {"unavailable": str(e)}
+        # leave the last result of the headline form in place for fetch_result()
+        step(mode)
+        torch.cuda.synchronize()
 
     # e2e through the host API with pinned buffers
     e2e = None
@@ -389,15 +422,14 @@ def ours_arm(args, ws, rank, local):
                    "parallelism": f"{ws} independent replica(s), haloes sharded by rank"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "halo_fp64_kernel" if "fp64" in mode else "halo_fp32c_kernel",
+                     "kernel": kname,
                      "alg_bytes_per_launch": balg, "kernel_ms": kms},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": ck,
         "gpu_launches": int(launches),
         "forms": forms,
-        "replay_halos": int(stats.n_replay_halos),
-        "key_ties": int(stats.n_key_ties),
+        "diagnostics": headline_stats,
     }
     print(json.dumps(line), flush=True)
 
