@@ -25,6 +25,7 @@ UNITS = {
     "fp32c_class1.cu": ["--fmad=false"],
     "fp32c_class2.cu": ["--fmad=false"],
     "fp32c_dispatch.cu": [],
+    "noalloc.cu": [],
 }
 
 

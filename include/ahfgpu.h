@@ -206,6 +206,34 @@ AHFGPU_API int ahfgpu_last_error(char *buf, size_t len);
 
 AHFGPU_API const char *ahfgpu_version(void);
 
+/* ---- no-allocation variant ----------------------------------------------
+ * No counterpart in the reference (AHF has no GPU path).  For callers that
+ * cannot allocate device memory (a CUDA-graph capture of a larger pipeline,
+ * a host-owned pre-partitioned memory pool, a plugin with a fixed device
+ * budget): the batched FP64 stage with every byte of work space taken from
+ * one static device array of about 16 MB that each GPU loading the library
+ * holds until exit.  All pointers are device pointers; the batch is as for
+ * ahfgpu_construct_halos_device; nothing is allocated.
+ * Outputs (caller-owned): out_halo[nhalo]; halo h's kept list in radial order
+ * at out_member[off[h] .. off[h] + out_halo[h].npart) (out_member has
+ * off[nhalo] entries); profile rows of halo h at
+ * out_prof[(h * AHFGPU_NOALLOC_MAX_BINS + b) * AHFGPU_PROF_NFIELDS + f].
+ * Larger batches return AHFGPU_ERR_CAPACITY.  The first call on a device
+ * sets the array up and must precede any stream capture; calls that overlap
+ * on the GPU share the array and race.  stream: cudaStream_t or NULL. */
+#define AHFGPU_NOALLOC_MAX_PARTICLES 131072
+#define AHFGPU_NOALLOC_MAX_HALOS     8192
+#define AHFGPU_NOALLOC_MAX_BINS      64
+AHFGPU_API int ahfgpu_construct_halos_noalloc(const ahfgpu_params *params,
+                                              const ahfgpu_batch  *batch,
+                                              ahfgpu_halo         *out_halo,
+                                              uint64_t            *out_member,
+                                              double              *out_prof,
+                                              void                *stream);
+/* Message of the last failure of ahfgpu_construct_halos_noalloc on this
+ * thread; returns the untruncated length. */
+AHFGPU_API int ahfgpu_noalloc_last_error(char *buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif
