@@ -1,0 +1,63 @@
+"""Small, self-contained cases of the stage for profilers (ncu).
+
+    python -m ahf_gb300.profcase small [mode]   # 3000 haloes of <= 512 particles
+    python -m ahf_gb300.profcase medium [mode]  # 300 haloes of 2048..16384 particles
+    python -m ahf_gb300.profcase big [mode]     # one halo of ~2e5 particles
+    python -m ahf_gb300.profcase full [mode]    # the whole 1e5-halo workload
+
+Each runs the stage twice on a device-resident batch cut from the seeded
+1e5-halo workload (cfg3) and prints the device time and diagnostics.
+mode: batched_fp32c (default), batched_fp64, plain_fp64.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+
+def subset(lists, halos):
+    import torch
+    halos = np.asarray(halos, np.int64)
+    off = lists.off.astype(np.int64)
+    cnt = off[halos + 1] - off[halos]
+    noff = np.zeros(len(halos) + 1, np.int64)
+    noff[1:] = np.cumsum(cnt)
+    idx = torch.as_tensor(np.concatenate([np.arange(off[h], off[h + 1]) for h in halos]), device="cuda")
+    t = {"off": torch.as_tensor(noff, device="cuda")}
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
+        v = getattr(lists, k)
+        t[k] = None if v is None else v[idx].contiguous()
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(lists, k)[halos], device="cuda")
+    return t
+
+
+def main(argv):
+    from . import lib, synth
+    which = argv[0] if argv else "small"
+    mode = argv[1] if len(argv) > 1 else "batched_fp32c"
+    lib.init(0)
+    scale = 1.0 if which == "full" else 0.05
+    L = synth.generate("cfg3", scale=scale, device="cuda", as_numpy=False)
+    p = synth.params_for(L)
+    n = np.diff(L.off.astype(np.int64))
+    if which == "small":
+        sel = np.nonzero(n <= 512)[0][:3000]
+    elif which == "medium":
+        sel = np.nonzero((n > 2048) & (n <= 16384))[0][:300]
+    elif which == "big":
+        sel = np.array([int(np.argmin(np.abs(n - 200000)))])
+    else:
+        sel = np.arange(len(n))
+    db = lib.device_batch(subset(L, sel))
+    for _ in range(2):
+        r = lib.construct_halos_device(p, db, mode)
+    res = lib.fetch_result()
+    print(f"{which} {mode}: haloes {len(sel)} particles {int(n[sel].sum())} ms {r.stats.ms_device:.3f} "
+          f"fix_rounds max {res.halo['fix_rounds'].max()} niter mean {res.halo['niter'].mean():.2f} "
+          f"retests {r.stats.n_retest} exact_iterations {r.stats.n_replay_halos}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
