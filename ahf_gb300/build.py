@@ -60,7 +60,10 @@ def _stale() -> bool:
     return False
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, defines: tuple = (), out: str | None = None) -> str:
+    """Compile every unit and link LIB (or `out`, with extra -D `defines`)."""
+    if defines or out:
+        return _build_variant(list(defines), out or LIB, verbose)
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
@@ -73,6 +76,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
     return LIB
+
+
+def _build_variant(defines, out, verbose):
+    bdir = os.path.join(os.path.dirname(os.path.abspath(out)), "_build_variant")
+    os.makedirs(bdir, exist_ok=True)
+    objs = []
+    for src, extra in UNITS.items():
+        obj = os.path.join(bdir, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc(), *ARCH, *COMMON, *extra, *[f"-D{d}" for d in defines], "-c", os.path.join(CSRC, src), "-o", obj]
+        objs.append((cmd, obj))
+    with cf.ThreadPoolExecutor(max_workers=len(objs)) as ex:
+        res = list(ex.map(lambda c: subprocess.run(c[0], capture_output=True, text=True), objs))
+    for r in res:
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr)
+    r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", out, *[o for _, o in objs], "-cudart", "static"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    return out
 
 
 if __name__ == "__main__":

@@ -90,10 +90,10 @@ struct Ctx {
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
   DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
-  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, exlist, excount;
+  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql, exlist, excount;
   DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
   // packed results (device)
-  DBuf member_off, member, prof_off, prof;
+  DBuf member_off, member, prof_off, prof, phase;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -251,7 +251,7 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.seid, N * 4); EN(g.phi, N * 8); EN(g.flag, N); EN(g.nflag, N);
   EN(g.pa, N * 8); EN(g.pb, N * 8); EN(g.pc, N * 8); EN(g.pd, N * 8);
   EN(g.fdh, N * 4); EN(g.fdl, N * 4); EN(g.fdx, N * 4); EN(g.fdy, N * 4); EN(g.fdz, N * 4);
-  EN(g.fdxl, N * 4); EN(g.fdyl, N * 4); EN(g.fdzl, N * 4);
+  EN(g.fdxl, N * 4); EN(g.fdyl, N * 4); EN(g.fdzl, N * 4); EN(g.fqh, N * 4); EN(g.fql, N * 4);
   EN(g.exlist, std::max<int64_t>(pl.nhalo, 1) * 4); EN(g.excount, 64);
   EN(g.stack, (size_t)nblocks * stack_cap * sizeof(uint4));
   EN(g.halo, std::max<int64_t>(pl.nhalo, 1) * sizeof(ahfgpu_halo));
@@ -364,8 +364,13 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   W.fdh = g.fdh.as<float>(); W.fdl = g.fdl.as<float>();
   W.fdx = g.fdx.as<float>(); W.fdy = g.fdy.as<float>(); W.fdz = g.fdz.as<float>();
   W.fdxl = g.fdxl.as<float>(); W.fdyl = g.fdyl.as<float>(); W.fdzl = g.fdzl.as<float>();
+  W.fqh = g.fqh.as<float>(); W.fql = g.fql.as<float>();
   W.exact_list = g.exlist.as<int>();
   W.exact_count = g.excount.as<unsigned>();
+#ifdef AHFGPU_PHASE_TIMERS
+  if ((rc = g.phase.ensure(16 * 8))) return rc;
+  W.phase = g.phase.as<unsigned long long>();
+#endif
   CK(cudaMemsetAsync(g.excount.p, 0, 64, st));
 
   CK(cudaEventRecord(g.ev0, st));
@@ -509,7 +514,7 @@ int ahfgpu_shutdown(void) {
   DBuf* bufs[] = {&g.in_off, &g.in_x, &g.in_y, &g.in_z, &g.in_vx, &g.in_vy, &g.in_vz, &g.in_w, &g.in_gidx,
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
-                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.exlist, &g.excount, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
+                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.exlist, &g.excount, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
   for (int k = 0; k < 3; k++) {
@@ -652,5 +657,16 @@ int ahfgpu_last_error(char* buf, size_t len) {
 }
 
 const char* ahfgpu_version(void) { return "ahfgpu 1.0 (sm_103a)"; }
+
+#ifdef AHFGPU_PHASE_TIMERS
+// instrumented builds: per-phase SM cycles summed over the last call's CTAs
+AHFGPU_API int ahfgpu_debug_phase(unsigned long long* out, int reset) {
+  if (!g.phase.p) return AHFGPU_ERR_STATE;
+  cudaDeviceSynchronize();
+  cudaMemcpy(out, g.phase.p, 16 * 8, cudaMemcpyDeviceToHost);
+  if (reset) cudaMemset(g.phase.p, 0, 16 * 8);
+  return AHFGPU_OK;
+}
+#endif
 
 }  // extern "C"

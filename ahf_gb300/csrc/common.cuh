@@ -57,6 +57,7 @@ struct Work {
   float *fdh, *fdl;       // FP32C: distance as float-float
   float *fdx, *fdy, *fdz; // FP32C: offsets from the centre
   float *fdxl, *fdyl, *fdzl;  // FP32C: low parts of the offsets
+  float *fqh, *fql;       // FP32C: 1/d^2 as float-float
   int* exact_list;        // FP32C: haloes handed to the FP64 form
   unsigned* exact_count;
   uint8_t* flag;          // member (1) / removed (0) per sorted slot
@@ -75,9 +76,27 @@ struct Work {
   const int32_t* queue;   // halo indices, largest first
   int nqueue;
   unsigned long long* counters;  // [0] retest, [1] replay, [2] key ties
+  unsigned long long* phase;     // per-phase SM cycles (instrumented builds only)
   int* err;
 };
 
+
+// Optional per-phase cycle counters (build with -DAHFGPU_PHASE_TIMERS).
+#ifdef AHFGPU_PHASE_TIMERS
+#define PT_BEGIN long long _pt = clock64();
+#define PT_MARK(W, k)                                              \
+  do {                                                             \
+    __syncthreads();                                               \
+    if (threadIdx.x == 0 && (W).phase) {                           \
+      long long _t = clock64();                                    \
+      atomicAdd(&(W).phase[k], (unsigned long long)(_t - _pt));    \
+      _pt = _t;                                                    \
+    }                                                              \
+  } while (0)
+#else
+#define PT_BEGIN
+#define PT_MARK(W, k) do { } while (0)
+#endif
 
 // ---------------------------------------------------------------------------
 // periodic wraps (src/libahf/ahf_halos.c:3505-3516 signed, :3381-3389 fabs)

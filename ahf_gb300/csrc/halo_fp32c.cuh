@@ -49,6 +49,7 @@ struct F32Smem {
   int iscan[96];
   float lasth[32], lastl[32];
   double lastd[32];
+  float lastv[32 * 4];
   int lasti[32];
   double edge[kMaxBins];
   Bin bins[kMaxBins];
@@ -146,6 +147,143 @@ __device__ __forceinline__ int bscan_int_ex(int v, int* tot, SM& S) {
   int inc = block_scan_int(v, &t, S.iscan);
   *tot = t;
   return inc - v;
+}
+
+// exclusive FP32 scan of NC channels over thread totals (fixed tree)
+template <int NC>
+__device__ __forceinline__ void bscan_f(const float (&v)[NC], float (&ex)[NC], float (&tot)[NC], float* sm) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  float inc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; c++) inc[c] = v[c];
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      float y = __shfl_up_sync(FULL, inc[c], off);
+      if (lane >= off) inc[c] = __fadd_rn(y, inc[c]);
+    }
+  }
+  if (lane == 31) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) sm[wid * NC + c] = inc[c];
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      float t = lane < nw ? sm[lane * NC + c] : 0.f;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        float y = __shfl_up_sync(FULL, t, off);
+        if (lane >= off) t = __fadd_rn(y, t);
+      }
+      if (lane < nw) sm[lane * NC + c] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < NC; c++) {
+    float wp = wid > 0 ? sm[(wid - 1) * NC + c] : 0.f;
+    float prev = __shfl_up_sync(FULL, inc[c], 1);
+    ex[c] = lane > 0 ? __fadd_rn(wp, prev) : wp;
+    tot[c] = sm[(nw - 1) * NC + c];
+  }
+  __syncthreads();
+}
+
+// block total of NC float-float channels (the same in every thread)
+template <int NC>
+__device__ __noinline__ void breduce_ff(const ff (&v)[NC], ff (&tot)[NC], float* sm) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll (NC <= 4 ? NC : 1)
+  for (int c = 0; c < NC; c++) {
+    ff x = v[c];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      ff y = {__shfl_xor_sync(FULL, x.hi, off), __shfl_xor_sync(FULL, x.lo, off)};
+      x = lane < (lane ^ off) ? ff_add(x, y) : ff_add(y, x);
+    }
+    if (lane == 0) { sm[(wid * NC + c) * 2] = x.hi; sm[(wid * NC + c) * 2 + 1] = x.lo; }
+  }
+  __syncthreads();
+#pragma unroll (NC <= 4 ? NC : 1)
+  for (int c = 0; c < NC; c++) {
+    ff t = ffz();
+    for (int w = 0; w < nw; w++) t = ff_add(t, ff{sm[(w * NC + c) * 2], sm[(w * NC + c) * 2 + 1]});
+    tot[c] = t;
+  }
+  __syncthreads();
+}
+
+// block total of NC float channels
+template <int NC>
+__device__ __noinline__ void breduce_f(const float (&v)[NC], float (&tot)[NC], float* sm) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll (NC <= 4 ? NC : 1)
+  for (int c = 0; c < NC; c++) {
+    float x = v[c];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      float y = __shfl_xor_sync(FULL, x, off);
+      x = lane < (lane ^ off) ? __fadd_rn(x, y) : __fadd_rn(y, x);
+    }
+    if (lane == 0) sm[wid * NC + c] = x;
+  }
+  __syncthreads();
+#pragma unroll (NC <= 4 ? NC : 1)
+  for (int c = 0; c < NC; c++) {
+    float t = 0.f;
+    for (int w = 0; w < nw; w++) t = __fadd_rn(t, sm[w * NC + c]);
+    tot[c] = t;
+  }
+  __syncthreads();
+}
+
+// exclusive "last value" over threads with a 4-float payload (distance and
+// inverse squared distance of the last member, both float-float)
+template <class SM>
+__device__ __forceinline__ void blast4(bool has, const float (&val)[4], const float (&carry)[4], float (&res)[4],
+                                       float (&last)[4], SM& S) {
+  const unsigned FULL = 0xffffffffu;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned m = __ballot_sync(FULL, has);
+  int lastlane = m ? (31 - __clz(m)) : 0;
+  float wv[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) wv[j] = __shfl_sync(FULL, val[j], lastlane);
+  if (lane == 0) {
+    S.lasti[wid] = m ? 1 : 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) S.lastv[wid * 4 + j] = wv[j];
+  }
+  __syncthreads();
+  float fl[4] = {carry[0], carry[1], carry[2], carry[3]};
+  for (int w = wid - 1; w >= 0; w--)
+    if (S.lasti[w]) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) fl[j] = S.lastv[w * 4 + j];
+      break;
+    }
+  unsigned below = m & ((1u << lane) - 1u);
+  int src = below ? (31 - __clz(below)) : 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    float mine = __shfl_sync(FULL, val[j], src);
+    res[j] = below ? mine : fl[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) last[j] = carry[j];
+  for (int w = nw - 1; w >= 0; w--)
+    if (S.lasti[w]) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) last[j] = S.lastv[w * 4 + j];
+      break;
+    }
+  __syncthreads();
 }
 
 template <class SM>
@@ -299,9 +437,13 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
     long long dx = wrapfix(fixp(B.x[e]) - c.fx);
     long long dy = wrapfix(fixp(B.y[e]) - c.fy);
     long long dz = wrapfix(fixp(B.z[e]) - c.fz);
-    ff d = ff_sqrt(key_d2(sqkey(dx, dy, dz)));
+    ff d2 = key_d2(sqkey(dx, dy, dz));
+    ff d = ff_sqrt(d2);
+    ff q = d2.hi > 0.f ? ff_div(fff(1.f), d2) : ffz();
     W.fdh[s] = d.hi;
     W.fdl[s] = d.lo;
+    W.fqh[s] = q.hi;
+    W.fql[s] = q.lo;
     // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
     // centre-of-mass sums)
     float hx = __ll2float_rn(dx), hy = __ll2float_rn(dy), hz = __ll2float_rn(dz);
@@ -344,6 +486,19 @@ static __device__ __noinline__ ff phi_term(ff M, float w, ff d, ff dp) {
   return ff_mul(Im, ff_sub(d, dp));
 }
 
+// potential-integral term with the stored 1/d^2 of this and the previous
+// member (no division): ((M/d^2 + Mp/dp^2)/2) (d - dp)
+__device__ __forceinline__ ff phi_termq(ff M, float w, ff d, ff q, ff dp, ff qp) {
+  if (!dpos(d)) return ffz();
+  ff Mp = ff_sub(M, fff(w));
+  ff In = ff_mul(M, q);
+  ff Ip = dpos(dp) ? ff_mul(Mp, qp) : ffz();
+  ff Im = ff_add(In, Ip);
+  Im.hi = __fmul_rn(Im.hi, 0.5f);
+  Im.lo = __fmul_rn(Im.lo, 0.5f);
+  return ff_mul(Im, ff_sub(d, dp));
+}
+
 // FP32 overdensity test with band; FP64 re-test inside the band.  Returns
 // fail (ovdens < ovlim).  M: mass prefix, d: distance (float-float).
 static __device__ __noinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
@@ -374,7 +529,7 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     float w[kItems];
-    ff d[kItems], dp;
+    ff d[kItems], q[kItems], dp, qp;
     ff locM[kItems];
     ff accM = ffz();
 #pragma unroll
@@ -383,10 +538,13 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
       bool v = i < c.n;
       w[k] = v ? W.sw[c.o + i] : 0.f;
       d[k] = v ? ff{W.fdh[c.o + i], W.fdl[c.o + i]} : ffz();
+      q[k] = v ? ff{W.fqh[c.o + i], W.fql[c.o + i]} : ffz();
       accM = ff_add(accM, fff(w[k]));
       locM[k] = accM;
     }
-    dp = (i0 > 0 && i0 < c.n) ? ff{W.fdh[c.o + i0 - 1], W.fdl[c.o + i0 - 1]} : ffz();
+    bool hasp = i0 > 0 && i0 < c.n;
+    dp = hasp ? ff{W.fdh[c.o + i0 - 1], W.fdl[c.o + i0 - 1]} : ffz();
+    qp = hasp ? ff{W.fqh[c.o + i0 - 1], W.fql[c.o + i0 - 1]} : ffz();
     ff ex[1], tot[1];
     ff vv[1] = {accM};
     bscan_ff<1>(vv, ex, tot, S.scan);
@@ -398,7 +556,8 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
       uint64_t i = i0 + k;
       Mk[k] = ff_add(base_M, locM[k]);
       ff prevd = k == 0 ? dp : d[k - 1];
-      term[k] = i < c.n ? phi_term(Mk[k], w[k], d[k], prevd) : ffz();
+      ff prevq = k == 0 ? qp : q[k - 1];
+      term[k] = i < c.n ? phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq) : ffz();
       accT = ff_add(accT, term[k]);
       term[k] = accT;     // thread-local inclusive
     }
@@ -492,97 +651,211 @@ static __device__ __noinline__ bool retest_bound(const Ctx32& c, const DevBatch&
 // ---------------------------------------------------------------------------
 // One rem_unbound iteration (ahf_halos.c:3336-3601) in one pass over slots
 // [0, n1) with members in flag bit0.  In: Phi0 of this iteration, seed slot.
-// Out: flags bit0 <- bound; next-iteration Phi0; kept count/mass; last kept
-// slot; the rvir1 candidate (first kept slot failing the overdensity test).
+// Out: flag bit1 = bound (bit0 kept); next-iteration Phi0; kept count/mass;
+// last kept slot; the rvir1 candidate (first kept slot failing the
+// overdensity test).  amb: some decision stayed inside the reference-rounding
+// band (the caller redoes the iteration exactly).
 struct IterOut {
   long long nb;
   ff Mb, Phi0n;
   long long last_slot;
   long long rv_slot;   // first failing kept slot or -1
   ff rv_M, rv_d;
-  int amb;             // needs the FP64 form
+  int amb;
   int rounds;
 };
 
 template <class SM>
 static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                            uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out, unsigned* nret) {
+                                   uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out, unsigned* nret) {
   const uint64_t o = c.o;
   const float vf = (float)P.v_fac, Hr = (float)(P.Hubble * P.r_fac), v2t = (float)P.v2_tune;
   const float pf2 = (float)(2.0 * P.phi_fac);
+  const float V43f = (float)(4. * kPi / 3.);
   const float w0 = W.sw[o + js];
-  // carries
-  ff cM = ffz(), cPhi = ffz(), cD = ffz();
+  ff cM = ffz(), cPhi = ffz();
+  float cD[4] = {0.f, 0.f, 0.f, 0.f};
   ff cVX = two_prod(w0, W.svx[o + js]), cVY = two_prod(w0, W.svy[o + js]), cVZ = two_prod(w0, W.svz[o + js]);
   ff cMv = fff(w0);
-  ff cMb = ffz(), cPhiN = ffz(), cDb = ffz();
+  ff cMb = ffz(), cPhiN = ffz();
+  float cDb[4] = {0.f, 0.f, 0.f, 0.f};
   long long cNb = 0, last_slot = -1, rv = -1;
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
-    uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
+    const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
-    ff d[kItems];
+    ff d[kItems], q[kItems];
     bool any_m = false;
-    ff lastm = ffz();
+    float lastm[4] = {0.f, 0.f, 0.f, 0.f};
+    ff accM = ffz(), locM[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       m[k] = i < n1 && (W.flag[o + i] & 1);
       w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
-      d[k] = ffz();
+      d[k] = q[k] = ffz();
       if (m[k]) {
         w[k] = W.sw[o + i];
         vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
         dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
         d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
+        q[k] = ff{W.fqh[o + i], W.fql[o + i]};
         any_m = true;
-        lastm = d[k];
+        lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
+        accM = ff_add(accM, fff(w[k]));
       }
+      locM[k] = accM;
     }
-    // member mass prefix, previous member distance, potential prefix
-    ff accM = ffz(), locM[kItems];
-#pragma unroll
-    for (int k = 0; k < kItems; k++) { if (m[k]) accM = ff_add(accM, fff(w[k])); locM[k] = accM; }
+    // member mass prefix, previous member, potential prefix
     ff exM[1], totM[1], vM[1] = {accM};
     bscan_ff<1>(vM, exM, totM, S.scan);
-    ff blockLast;
-    ff dprev0 = blast_ff(any_m, lastm, cD, &blockLast, S);
+    float dprev[4], blockLast[4];
+    blast4(any_m, lastm, cD, dprev, blockLast, S);
     ff Mk[kItems], phi[kItems], accP = ffz();
-    ff dp = dprev0;
+    {
+      ff dp = {dprev[0], dprev[1]}, qp = {dprev[2], dprev[3]};
+      ff baseM = ff_add(cM, exM[0]);
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      Mk[k] = ff_add(ff_add(cM, exM[0]), locM[k]);
-      if (m[k]) {
-        accP = ff_add(accP, phi_term(Mk[k], w[k], d[k], dp));
-        dp = d[k];
+      for (int k = 0; k < kItems; k++) {
+        Mk[k] = ff_add(baseM, locM[k]);
+        if (m[k]) {
+          accP = ff_add(accP, phi_termq(Mk[k], w[k], d[k], q[k], dp, qp));
+          dp = d[k];
+          qp = q[k];
+        }
+        phi[k] = accP;
       }
-      phi[k] = accP;
     }
     ff exP[1], totP[1], vP[1] = {accP};
     bscan_ff<1>(vP, exP, totP, S.scan);
     float thr[kItems];
+    {
+      ff basePhi = ff_add(cPhi, exP[0]);
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        phi[k] = ff_add(basePhi, phi[k]);
+        float A = fabsf(ff_f(ff_sub(phi[k], Phi0)));
+        thr[k] = dpos(d[k]) ? __fmul_rn(v2t, __fmul_rn(pf2, A)) : __fmul_rn(v2t, 1e30f);
+      }
+    }
+    // tile fixpoint of the bound flags.  FP32 decisions use momenta relative
+    // to the tile's reference bulk velocity Vr = cV/cMv (small, random
+    // deviations u = v - Vr), so V = Vr + (R + sum w u)/Mv with R = cV - Vr cMv
+    // kept in float-float; each decision carries a first-order bound on its
+    // FP32 error.  Float-float prefixes (for the FP64 re-test) are built only
+    // in rounds where some decision falls inside its bound.
+    const float fe = 5.9604645e-08f;   // 2^-24
+    const float Vrx = ff_f(ff_div(cVX, cMv)), Vry = ff_f(ff_div(cVY, cMv)), Vrz = ff_f(ff_div(cVZ, cMv));
+    const float Rx = ff_f(ff_sub(cVX, ff_mul(fff(Vrx), cMv)));
+    const float Ry = ff_f(ff_sub(cVY, ff_mul(fff(Vry), cMv)));
+    const float Rz = ff_f(ff_sub(cVZ, ff_mul(fff(Vrz), cMv)));
+    float ux[kItems], uy[kItems], uz[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
-      phi[k] = ff_add(ff_add(cPhi, exP[0]), phi[k]);
-      float A = fabsf(ff_f(ff_sub(phi[k], Phi0)));
-      thr[k] = dpos(d[k]) ? __fmul_rn(v2t, __fmul_rn(pf2, A)) : __fmul_rn(v2t, 1e30f);
+      ux[k] = __fsub_rn(vx[k], Vrx);
+      uy[k] = __fsub_rn(vy[k], Vry);
+      uz[k] = __fsub_rn(vz[k], Vrz);
     }
-    // tile fixpoint of the bound flags
     bool b[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) b[k] = m[k];
     int rounds = 0;
-    ff tVX, tVY, tVZ, tMv;
     bool amb_tile = false;
     while (true) {
       rounds++;
-      ff ax = ffz(), ay = ffz(), az = ffz(), am = ffz();
-      ff lx[kItems], ly[kItems], lz[kItems], lm[kItems];
+      float fx[kItems], fy[kItems], fz[kItems], fm[kItems], fa[kItems];
+      float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f, sa = 0.f;
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        lx[k] = ax; ly[k] = ay; lz[k] = az; lm[k] = am;     // exclusive within thread
+        fx[k] = sx; fy[k] = sy; fz[k] = sz; fm[k] = sm; fa[k] = sa;
+        if (b[k]) {
+          float wx = __fmul_rn(w[k], ux[k]), wy = __fmul_rn(w[k], uy[k]), wz = __fmul_rn(w[k], uz[k]);
+          sx = __fadd_rn(sx, wx);
+          sy = __fadd_rn(sy, wy);
+          sz = __fadd_rn(sz, wz);
+          sm = __fadd_rn(sm, w[k]);
+          sa = __fadd_rn(sa, __fadd_rn(__fadd_rn(fabsf(wx), fabsf(wy)), fabsf(wz)));
+        }
+      }
+      float ex5[5], tot5[5], v5[5] = {sx, sy, sz, sm, sa};
+      bscan_f<5>(v5, ex5, tot5, S.scan);
+      int changed = 0;
+      bool need[kItems];
+      bool any_need = false;
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        need[k] = false;
+        if (!m[k]) continue;
+        float Ux = __fadd_rn(ex5[0], fx[k]), Uy = __fadd_rn(ex5[1], fy[k]), Uz = __fadd_rn(ex5[2], fz[k]);
+        float Mv = __fadd_rn(cMv.hi, __fadd_rn(ex5[3], fm[k]));
+        float Asum = __fadd_rn(ex5[4], fa[k]);
+        float rmv = __fdiv_rn(1.f, Mv);
+        float Dx = __fmul_rn(__fadd_rn(Rx, Ux), rmv), Dy = __fmul_rn(__fadd_rn(Ry, Uy), rmv),
+              Dz = __fmul_rn(__fadd_rn(Rz, Uz), rmv);
+        float hx = __fmul_rn(Hr, dx[k]), hy = __fmul_rn(Hr, dy[k]), hz = __fmul_rn(Hr, dz[k]);
+        float dVX = __fadd_rn(__fmul_rn(__fsub_rn(ux[k], Dx), vf), hx);
+        float dVY = __fadd_rn(__fmul_rn(__fsub_rn(uy[k], Dy), vf), hy);
+        float dVZ = __fadd_rn(__fmul_rn(__fsub_rn(uz[k], Dz), vf), hz);
+        float vel2 = __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ));
+        // error bound: tile-sum error (depth <= 16 per component), the rest
+        // a few roundings of each magnitude involved; x2 slack
+        float eD = __fmul_rn(__fadd_rn(__fmul_rn(16.f * fe, Asum), __fmul_rn(fe, __fadd_rn(fabsf(Rx) + fabsf(Ry),
+                                                                                            fabsf(Rz)))), rmv);
+        float mag = __fadd_rn(__fmul_rn(__fadd_rn(fabsf(ux[k]) + fabsf(uy[k]) + fabsf(uz[k]),
+                                                  fabsf(Dx) + fabsf(Dy) + fabsf(Dz)), vf),
+                              fabsf(hx) + fabsf(hy) + fabsf(hz));
+        float edv = __fadd_rn(__fmul_rn(eD, vf), __fmul_rn(4.f * fe, mag));
+        float sdv = fabsf(dVX) + fabsf(dVY) + fabsf(dVZ);
+        float err = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(2.f * sdv, edv), __fmul_rn(3.f, __fmul_rn(edv, edv))),
+                                             __fmul_rn(8.f * fe, __fadd_rn(vel2, thr[k]))));
+        float margin = __fsub_rn(thr[k], vel2);
+        if (fabsf(margin) > err && isfinite(margin) && isfinite(err)) {
+          bool nb = margin >= 0.f;
+          if (nb != b[k]) { b[k] = nb; changed = 1; }
+        } else {
+          need[k] = true;
+          any_need = true;
+        }
+      }
+      if (__syncthreads_or(any_need ? 1 : 0)) {
+        // exact float-float prefixes of this round's flags
+        ff ax = ffz(), ay = ffz(), az = ffz(), am = ffz(), lx[kItems], ly[kItems], lz[kItems], lm[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          lx[k] = ax; ly[k] = ay; lz[k] = az; lm[k] = am;
+          if (b[k]) {
+            ax = ff_add(ax, two_prod(w[k], vx[k]));
+            ay = ff_add(ay, two_prod(w[k], vy[k]));
+            az = ff_add(az, two_prod(w[k], vz[k]));
+            am = ff_add(am, fff(w[k]));
+          }
+        }
+        ff e4[4], t4[4], a4[4] = {ax, ay, az, am};
+        bscan_ff<4>(a4, e4, t4, S.scan);
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+          if (!need[k]) continue;
+          (*nret)++;
+          bool amb = false;
+          bool nb = retest_bound(c, B, W, P, o + i0 + k, i0 + k, n1, phi[k], Phi0,
+                                 ff_add(ff_add(cVX, e4[0]), lx[k]), ff_add(ff_add(cVY, e4[1]), ly[k]),
+                                 ff_add(ff_add(cVZ, e4[2]), lz[k]), ff_add(ff_add(cMv, e4[3]), lm[k]), vmax, &amb);
+          if (amb) amb_tile = true;
+          if (nb != b[k]) { b[k] = nb; changed = 1; }
+        }
+      }
+      if (!__syncthreads_or(changed)) break;
+      if (rounds >= kMaxFixRounds) { amb_tile = true; break; }
+    }
+    if (rounds > maxr) maxr = rounds;
+    amb_any |= __syncthreads_or(amb_tile ? 1 : 0);
+    // carries of the running bulk velocity: float-float tile totals
+    {
+      ff ax = ffz(), ay = ffz(), az = ffz(), am = ffz();
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
         if (b[k]) {
           ax = ff_add(ax, two_prod(w[k], vx[k]));
           ay = ff_add(ay, two_prod(w[k], vy[k]));
@@ -590,74 +863,62 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
           am = ff_add(am, fff(w[k]));
         }
       }
-      ff ex4[4], tot4[4], v4[4] = {ax, ay, az, am};
-      bscan_ff<4>(v4, ex4, tot4, S.scan);
-      tVX = tot4[0]; tVY = tot4[1]; tVZ = tot4[2]; tMv = tot4[3];
-      int changed = 0;
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        if (!m[k]) continue;
-        ff VX = ff_add(ff_add(cVX, ex4[0]), lx[k]);
-        ff VY = ff_add(ff_add(cVY, ex4[1]), ly[k]);
-        ff VZ = ff_add(ff_add(cVZ, ex4[2]), lz[k]);
-        ff Mv = ff_add(ff_add(cMv, ex4[3]), lm[k]);
-        float mvf = ff_f(Mv);
-        float bx = __fsub_rn(vx[k], __fdiv_rn(ff_f(VX), mvf));
-        float by = __fsub_rn(vy[k], __fdiv_rn(ff_f(VY), mvf));
-        float bz = __fsub_rn(vz[k], __fdiv_rn(ff_f(VZ), mvf));
-        float dVX = __fadd_rn(__fmul_rn(bx, vf), __fmul_rn(Hr, dx[k]));
-        float dVY = __fadd_rn(__fmul_rn(by, vf), __fmul_rn(Hr, dy[k]));
-        float dVZ = __fadd_rn(__fmul_rn(bz, vf), __fmul_rn(Hr, dz[k]));
-        float vel2 = __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ));
-        float margin = __fsub_rn(thr[k], vel2);
-        bool nb;
-        if (fabsf(margin) > kBand1 * fmaxf(thr[k], vel2) && isfinite(margin)) {
-          nb = margin >= 0.f;
-        } else {
-          (*nret)++;
-          bool amb = false;
-          nb = retest_bound(c, B, W, P, o + i0 + k, i0 + k, n1, phi[k], Phi0, VX, VY, VZ, Mv, vmax, &amb);
-          if (amb) amb_tile = true;
-        }
-        if (nb != b[k]) { b[k] = nb; changed = 1; }
-      }
-      if (!__syncthreads_or(changed)) break;
-      if (rounds >= kMaxFixRounds) { amb_tile = true; break; }
+      ff t4[4], a4[4] = {ax, ay, az, am};
+      breduce_ff<4>(a4, t4, S.scan);
+      cVX = ff_add(cVX, t4[0]); cVY = ff_add(cVY, t4[1]); cVZ = ff_add(cVZ, t4[2]); cMv = ff_add(cMv, t4[3]);
     }
-    if (rounds > maxr) maxr = rounds;
-    amb_any |= __syncthreads_or(amb_tile ? 1 : 0);
     // next-iteration channels over the kept particles
     ff accB = ffz(), locB[kItems];
     bool any_b = false;
-    ff lastb = ffz();
+    float lastb[4] = {0.f, 0.f, 0.f, 0.f};
     int nbl = 0;
     long long lslot = -1;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
-      if (b[k]) { accB = ff_add(accB, fff(w[k])); any_b = true; lastb = d[k]; nbl++; lslot = (long long)(i0 + k); }
+      if (b[k]) {
+        accB = ff_add(accB, fff(w[k]));
+        any_b = true;
+        lastb[0] = d[k].hi; lastb[1] = d[k].lo; lastb[2] = q[k].hi; lastb[3] = q[k].lo;
+        nbl++;
+        lslot = (long long)(i0 + k);
+      }
       locB[k] = accB;
     }
     ff exB[1], totB[1], vB[1] = {accB};
     bscan_ff<1>(vB, exB, totB, S.scan);
-    ff blastB;
-    ff dpb = blast_ff(any_b, lastb, cDb, &blastB, S);
+    float dpb4[4], blastB[4];
+    blast4(any_b, lastb, cDb, dpb4, blastB, S);
     int tnb;
     bscan_int_ex(nbl, &tnb, S);
     ff accN = ffz();
     long long myfail = 0x7fffffffffffffffll;
     ff fM = ffz(), fD = ffz();
+    {
+      ff dpb = {dpb4[0], dpb4[1]}, qpb = {dpb4[2], dpb4[3]};
+      ff baseB = ff_add(cMb, exB[0]);
+      const float lim = P.f_ovlim, rvrf = P.f_rvrf;
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      if (!b[k]) continue;
-      ff Mb = ff_add(ff_add(cMb, exB[0]), locB[k]);
-      accN = ff_add(accN, phi_term(Mb, w[k], d[k], dpb));
-      dpb = d[k];
-      if (rv < 0 && myfail == 0x7fffffffffffffffll) {
-        if (ov_fail(c, B, W, P, o + i0 + k, Mb, d[k], nret)) { myfail = (long long)(i0 + k); fM = Mb; fD = d[k]; }
+      for (int k = 0; k < kItems; k++) {
+        if (!b[k]) continue;
+        ff Mb = ff_add(baseB, locB[k]);
+        accN = ff_add(accN, phi_termq(Mb, w[k], d[k], q[k], dpb, qpb));
+        dpb = d[k];
+        qpb = q[k];
+        if (rv < 0 && myfail == 0x7fffffffffffffffll) {
+          // cheap FP32 screen; the banded test (with FP64 re-test) only near ovlim
+          float df = d[k].hi;
+          float ov = __fdiv_rn(__fdiv_rn(Mb.hi, __fmul_rn(V43f, __fmul_rn(__fmul_rn(df, df), df))), rvrf);
+          if (!(ov > lim * (1.f + 4.f * kBand1)) &&
+              ov_fail(c, B, W, P, o + i0 + k, Mb, d[k], nret)) {
+            myfail = (long long)(i0 + k);
+            fM = Mb;
+            fD = d[k];
+          }
+        }
       }
     }
-    ff exN[1], totN[1], vN[1] = {accN};
-    bscan_ff<1>(vN, exN, totN, S.scan);
+    ff totN[1], vN[1] = {accN};
+    breduce_ff<1>(vN, totN, S.scan);
     if (rv < 0) {
       long long f = bmin_ll(myfail, S);
       if (f != 0x7fffffffffffffffll) {
@@ -671,7 +932,6 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     }
     long long ls = -bmin_ll(-lslot, S);
     if (ls >= 0) last_slot = ls;
-    // write flags
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
@@ -679,16 +939,15 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     }
     cM = ff_add(cM, totM[0]);
     cPhi = ff_add(cPhi, totP[0]);
-    cD = blockLast;
-    cVX = ff_add(cVX, tVX); cVY = ff_add(cVY, tVY); cVZ = ff_add(cVZ, tVZ); cMv = ff_add(cMv, tMv);
+#pragma unroll
+    for (int j = 0; j < 4; j++) { cD[j] = blockLast[j]; cDb[j] = blastB[j]; }
     cMb = ff_add(cMb, totB[0]);
     cPhiN = ff_add(cPhiN, totN[0]);
-    cDb = blastB;
     cNb += tnb;
   }
   out.nb = cNb;
   out.Mb = cMb;
-  out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(cMb, cDb)) : ffz();
+  out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(cMb, ff{cDb[0], cDb[1]})) : ffz();
   out.last_slot = last_slot;
   out.rv_slot = rv;
   out.rv_M = rvM;
@@ -854,14 +1113,15 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
 template <class SM>
 static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, SM& S, uint64_t n1) {
   const uint64_t o = c.o;
-  ff cM = ffz(), cPhi = ffz(), cD = ffz();
+  ff cM = ffz(), cPhi = ffz();
+  float cD[4] = {0.f, 0.f, 0.f, 0.f};
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems];
-    ff d[kItems];
+    ff d[kItems], q[kItems];
     bool any = false;
-    ff lastm = ffz();
+    float lastm[4] = {0.f, 0.f, 0.f, 0.f};
     ff accM = ffz(), locM[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
@@ -869,27 +1129,35 @@ static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, SM& S, uint64_t 
       m[k] = i < n1 && (W.flag[o + i] & 1);
       w[k] = m[k] ? W.sw[o + i] : 0.f;
       d[k] = m[k] ? ff{W.fdh[o + i], W.fdl[o + i]} : ffz();
-      if (m[k]) { accM = ff_add(accM, fff(w[k])); any = true; lastm = d[k]; }
+      q[k] = m[k] ? ff{W.fqh[o + i], W.fql[o + i]} : ffz();
+      if (m[k]) {
+        accM = ff_add(accM, fff(w[k]));
+        any = true;
+        lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
+      }
       locM[k] = accM;
     }
     ff exM[1], totM[1], vM[1] = {accM};
     bscan_ff<1>(vM, exM, totM, S.scan);
-    ff blockLast;
-    ff dp = blast_ff(any, lastm, cD, &blockLast, S);
+    float dp4[4], blockLast[4];
+    blast4(any, lastm, cD, dp4, blockLast, S);
+    ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
     ff accP = ffz();
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       if (!m[k]) continue;
-      accP = ff_add(accP, phi_term(ff_add(ff_add(cM, exM[0]), locM[k]), w[k], d[k], dp));
+      accP = ff_add(accP, phi_termq(ff_add(ff_add(cM, exM[0]), locM[k]), w[k], d[k], q[k], dp, qp));
       dp = d[k];
+      qp = q[k];
     }
-    ff exP[1], totP[1], vP[1] = {accP};
-    bscan_ff<1>(vP, exP, totP, S.scan);
+    ff totP[1], vP[1] = {accP};
+    breduce_ff<1>(vP, totP, S.scan);
     cM = ff_add(cM, totM[0]);
     cPhi = ff_add(cPhi, totP[0]);
-    cD = blockLast;
+#pragma unroll
+    for (int j = 0; j < 4; j++) cD[j] = blockLast[j];
   }
-  return ff_add(cPhi, ff_div(cM, cD));
+  return ff_add(cPhi, ff_div(cM, ff{cD[0], cD[1]}));
 }
 
 // rem_outsideRvir(.,1) over the members of [0, n1): slot of the first member
@@ -1100,48 +1368,79 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   return BI < 0 || !(BV > -10.0) ? m - 1 : (uint64_t)BI;
 }
 
-// HaloProfiles per-particle terms (ahf_halos.c:4320-4420): 0 potential
-// integral, 1-3 angular momentum, 4 kinetic T, 5-7 centre of mass, 8-13
-// inertia tensor, 14/15 high/low resolution mass.  VX.. are the momentum
-// prefixes INCLUDING the particle (the reference updates VXc first).
-static __device__ __noinline__ void prof_terms(const DevParams& P, float w, float vx, float vy, float vz, float dx,
-                                           float dy, float dz, float dxl, float dyl, float dzl, ff d, ff dp, ff M,
-                                           ff VX, ff VY, ff VZ, ff cxf, ff cyf, ff czf, float Hrv, ff (&tm)[16],
-                                           float* Tout) {
-  // velocity relative to the running bulk velocity, float-float
-  ff gX = ff_sub(fff(vx), ff_div(VX, M));
-  ff gY = ff_sub(fff(vy), ff_div(VY, M));
-  ff gZ = ff_sub(fff(vz), ff_div(VZ, M));
-  float dVX = ff_f(gX), dVY = ff_f(gY), dVZ = ff_f(gZ);
-  tm[0] = phi_term(M, w, d, dp);
-  tm[1] = two_prod(w, __fsub_rn(__fmul_rn(dy, dVZ), __fmul_rn(dz, dVY)));
-  tm[2] = two_prod(w, __fsub_rn(__fmul_rn(dz, dVX), __fmul_rn(dx, dVZ)));
-  tm[3] = two_prod(w, __fsub_rn(__fmul_rn(dx, dVY), __fmul_rn(dy, dVX)));
-  // Hubble drag, then the kinetic term (float-float: Ekin + Epot cancels in
-  // lambdaE)
-  gX = ff_add(gX, ff_mulf(two_sum(dx, dxl), Hrv));
-  gY = ff_add(gY, ff_mulf(two_sum(dy, dyl), Hrv));
-  gZ = ff_add(gZ, ff_mulf(two_sum(dz, dzl), Hrv));
-  ff T = ff_mulf(ff_add(ff_add(ff_mul(gX, gX), ff_mul(gY, gY)), ff_mul(gZ, gZ)), w);
-  *Tout = ff_f(T);
-  tm[4] = T;
-  tm[5] = ff_mulf(ff_add(cxf, two_sum(dx, dxl)), w);
-  tm[6] = ff_mulf(ff_add(cyf, two_sum(dy, dyl)), w);
-  tm[7] = ff_mulf(ff_add(czf, two_sum(dz, dzl)), w);
-  tm[8] = two_prod(__fmul_rn(w, dx), dx);
-  tm[9] = two_prod(__fmul_rn(w, dy), dy);
-  tm[10] = two_prod(__fmul_rn(w, dz), dz);
-  tm[11] = two_prod(__fmul_rn(w, dx), dy);
-  tm[12] = two_prod(__fmul_rn(w, dx), dz);
-  tm[13] = two_prod(__fmul_rn(w, dy), dz);
-  tm[14] = ffz();
-  tm[15] = ffz();
-  if (P.has_w) {
-    if (fabsf(w - 1.0f) < (float)kZero) tm[14] = fff(w);
-    else if (w > 1.0f) tm[15] = fff(w);
+// HaloProfiles per-particle terms (ahf_halos.c:4320-4420).  VX.. are the
+// momentum prefixes INCLUDING the particle (the reference updates VXc
+// first).  The velocity relative to the running bulk velocity is
+// float-float (one float division plus its residual), so the kinetic term
+// T stays accurate where Ekin + Epot cancels (lambdaE).
+struct PTerms {
+  ff phi, T, cx, cy, cz;   // potential term, kinetic term, w dX, w dY, w dZ
+  float g[11];             // Lx, Ly, Lz, a11, a22, a33, a12, a13, a23, Mhi, Mlo
+};
+
+__device__ __forceinline__ ff rel_vel(float v, ff V, ff M) {
+  float b = __fdiv_rn(V.hi, M.hi);
+  ff r = ff_sub(V, ff_mulf(M, b));
+  ff Vb = ff_quick(b, __fdiv_rn(r.hi, M.hi));
+  return ff_sub(fff(v), Vb);
+}
+
+__device__ __forceinline__ void pterms(float w, float vx, float vy, float vz, float dx, float dy, float dz,
+                                       float dxl, float dyl, float dzl, ff d, ff q, ff dp, ff qp, ff M, ff VX,
+                                       ff VY, ff VZ, float Hrv, int has_w, PTerms& t) {
+  ff gx = rel_vel(vx, VX, M), gy = rel_vel(vy, VY, M), gz = rel_vel(vz, VZ, M);
+  float gxf = ff_f(gx), gyf = ff_f(gy), gzf = ff_f(gz);
+  t.phi = phi_termq(M, w, d, q, dp, qp);
+  t.g[0] = __fmul_rn(w, __fsub_rn(__fmul_rn(dy, gzf), __fmul_rn(dz, gyf)));
+  t.g[1] = __fmul_rn(w, __fsub_rn(__fmul_rn(dz, gxf), __fmul_rn(dx, gzf)));
+  t.g[2] = __fmul_rn(w, __fsub_rn(__fmul_rn(dx, gyf), __fmul_rn(dy, gxf)));
+  gx = ff_add(gx, ff_mulf(two_sum(dx, dxl), Hrv));
+  gy = ff_add(gy, ff_mulf(two_sum(dy, dyl), Hrv));
+  gz = ff_add(gz, ff_mulf(two_sum(dz, dzl), Hrv));
+  t.T = ff_mulf(ff_add(ff_add(ff_mul(gx, gx), ff_mul(gy, gy)), ff_mul(gz, gz)), w);
+  t.cx = ff_add(two_prod(w, dx), fff(__fmul_rn(w, dxl)));
+  t.cy = ff_add(two_prod(w, dy), fff(__fmul_rn(w, dyl)));
+  t.cz = ff_add(two_prod(w, dz), fff(__fmul_rn(w, dzl)));
+  float wx = __fmul_rn(w, dx), wy = __fmul_rn(w, dy), wz = __fmul_rn(w, dz);
+  t.g[3] = __fmul_rn(wx, dx);
+  t.g[4] = __fmul_rn(wy, dy);
+  t.g[5] = __fmul_rn(wz, dz);
+  t.g[6] = __fmul_rn(wx, dy);
+  t.g[7] = __fmul_rn(wx, dz);
+  t.g[8] = __fmul_rn(wy, dz);
+  t.g[9] = 0.f;
+  t.g[10] = 0.f;
+  if (has_w) {
+    if (fabsf(w - 1.0f) < (float)kZero) t.g[9] = w;
+    else if (w > 1.0f) t.g[10] = w;
   } else {
-    tm[14] = fff(w);
+    t.g[9] = w;
   }
+}
+
+// out-of-line copy for the (rare) bin-end recomputation
+static __device__ __noinline__ void pterms_ool(float w, float vx, float vy, float vz, float dx, float dy, float dz,
+                                               float dxl, float dyl, float dzl, ff d, ff q, ff dp, ff qp, ff M,
+                                               ff VX, ff VY, ff VZ, float Hrv, int has_w, PTerms& t) {
+  pterms(w, vx, vy, vz, dx, dy, dz, dxl, dyl, dzl, d, q, dp, qp, M, VX, VY, VZ, Hrv, has_w, t);
+}
+
+// FP64 energy 0.5 T + U of a most-bound candidate (ahf_halos.c:4380-4420)
+static __device__ __noinline__ double mbp_energy64(const Ctx32& c, const DevBatch& B, const Work& W,
+                                                   const DevParams& P, uint64_t s, ff M, ff VX, ff VY, ff VZ,
+                                                   ff phi, ff Phi0, float w) {
+  uint64_t e = c.o + W.seid[s];
+  double dX = wrap_s((double)B.x[e] - c.cx), dY = wrap_s((double)B.y[e] - c.cy), dZ = wrap_s((double)B.z[e] - c.cz);
+  double Md = ff_d(M);
+  double dVX = ((double)B.vx[e] - ff_d(VX) / Md), dVY = ((double)B.vy[e] - ff_d(VY) / Md),
+         dVZ = ((double)B.vz[e] - ff_d(VZ) / Md);
+  dVX += P.Hubble * dX * P.r_fac / P.v_fac;
+  dVY += P.Hubble * dY * P.r_fac / P.v_fac;
+  dVZ += P.Hubble * dZ * P.r_fac / P.v_fac;
+  double wk = (double)w;
+  double Tpart = wk * ((dVX * dVX + dVY * dVY) + dVZ * dVZ);
+  double Upart = (ff_d(phi) - ff_d(Phi0)) * wk;
+  return 0.5 * Tpart + Upart;
 }
 
 // ---------------------------------------------------------------------------
@@ -1197,44 +1496,52 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   const float Hrv = (float)(P.Hubble * P.r_fac / P.v_fac);
   const double cxd = c.cx, cyd = c.cy, czd = c.cz;
   const ff cxf = ff_from_d(cxd), cyf = ff_from_d(cyd), czf = ff_from_d(czd);
-  ff c1[4] = {ffz(), ffz(), ffz(), ffz()};          // M, VX, VY, VZ
-  ff c2[16];
+  ff c1[4] = {ffz(), ffz(), ffz(), ffz()};   // M, VX, VY, VZ (inclusive prefixes)
+  ff cPhi = ffz(), cU = ffz();
+  ff cf[4] = {ffz(), ffz(), ffz(), ffz()};   // T, sum w dX, sum w dY, sum w dZ
+  float cg[11];                              // Lx, Ly, Lz, a11, a22, a33, a12, a13, a23, Mhi, Mlo
 #pragma unroll
-  for (int k = 0; k < 16; k++) c2[k] = ffz();        // phi, Lx,Ly,Lz, T, CoMx..z, a11..a23, Mhi, Mlo
-  ff cU = ffz(), cD = ffz();
+  for (int j = 0; j < 11; j++) cg[j] = 0.f;
+  ff cgc[11];                                // float-float carries of the float channels
+#pragma unroll
+  for (int j = 0; j < 11; j++) cgc[j] = ffz();
+  float cD[4] = {0.f, 0.f, 0.f, 0.f};
   int cr = 0;
   double Ebest = 1e30;
   long long Eslot = -1;
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
-    uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
+    const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
     float dxl[kItems], dyl[kItems], dzl[kItems];
-    ff d[kItems];
+    ff d[kItems], q[kItems];
     int nm = 0;
     bool any = false;
-    ff lastm = ffz();
+    float lastm[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       m[k] = i < n1 && (W.flag[o + i] & 1);
       w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
       dxl[k] = dyl[k] = dzl[k] = 0.f;
-      d[k] = ffz();
+      d[k] = q[k] = ffz();
       if (m[k]) {
         w[k] = W.sw[o + i];
         vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
         dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
         dxl[k] = W.fdxl[o + i]; dyl[k] = W.fdyl[o + i]; dzl[k] = W.fdzl[o + i];
         d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
-        nm++; any = true; lastm = d[k];
+        q[k] = ff{W.fqh[o + i], W.fql[o + i]};
+        nm++; any = true;
+        lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
       }
     }
     int tn;
     int rank0 = bscan_int_ex(nm, &tn, S) + cr;
-    ff blockLast;
-    ff dp0 = blast_ff(any, lastm, cD, &blockLast, S);
-    // scan 1: mass and momentum prefixes (inclusive, include the particle)
+    float dp4[4], blockLast[4];
+    blast4(any, lastm, cD, dp4, blockLast, S);
+    // scan 1: mass and momentum prefixes (inclusive: the reference adds the
+    // particle before using them)
     ff a1[4] = {ffz(), ffz(), ffz(), ffz()}, l1[kItems][4];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
@@ -1245,34 +1552,42 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         a1[3] = ff_add(a1[3], two_prod(w[k], vz[k]));
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++) l1[k][q] = a1[q];
+      for (int j = 0; j < 4; j++) l1[k][j] = a1[j];
     }
     ff e1[4], t1[4];
     bscan_ff<4>(a1, e1, t1, S.scan);
-    // per-particle terms (thread totals); per-item phi terms kept for U
-    ff a2[16];
+    ff b1[4];
 #pragma unroll
-    for (int q = 0; q < 16; q++) a2[q] = ffz();
+    for (int j = 0; j < 4; j++) b1[j] = ff_add(c1[j], e1[j]);
+    // per-particle terms, thread totals; bin ends of this tile
+    ff tf[4] = {ffz(), ffz(), ffz(), ffz()}, tphi = ffz();
+    float tg[11];
+#pragma unroll
+    for (int j = 0; j < 11; j++) tg[j] = 0.f;
     float Tp[kItems];
     ff pt[kItems];
-    ff Mr[kItems];
+    bool has_end = false;
     {
-      ff dp = dp0;
+      ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
       int r = rank0;
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
         Tp[k] = 0.f;
         pt[k] = ffz();
-        ff M = ff_add(ff_add(c1[0], e1[0]), l1[k][0]);
-        Mr[k] = M;
         if (!m[k]) continue;
-        ff tm[16];
-        prof_terms(P, w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], dp, M,
-                   ff_add(ff_add(c1[1], e1[1]), l1[k][1]), ff_add(ff_add(c1[2], e1[2]), l1[k][2]),
-                   ff_add(ff_add(c1[3], e1[3]), l1[k][3]), cxf, cyf, czf, Hrv, tm, &Tp[k]);
+        ff M = ff_add(b1[0], l1[k][0]);
+        PTerms t;
+        pterms(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], q[k], dp, qp, M,
+               ff_add(b1[1], l1[k][1]), ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), Hrv, P.has_w, t);
+        pt[k] = t.phi;
+        tphi = ff_add(tphi, t.phi);
+        Tp[k] = ff_f(t.T);
+        tf[0] = ff_add(tf[0], t.T);
+        tf[1] = ff_add(tf[1], t.cx);
+        tf[2] = ff_add(tf[2], t.cy);
+        tf[3] = ff_add(tf[3], t.cz);
 #pragma unroll
-        for (int q = 0; q < 16; q++) a2[q] = ff_add(a2[q], tm[q]);
-        pt[k] = tm[0];
+        for (int j = 0; j < 11; j++) tg[j] = __fadd_rn(tg[j], t.g[j]);
         // per-rank arrays (ahf_halos.c:4598-4616)
         Mff[r] = make_float2(M.hi, M.lo);
         float df = ff_f(d[k]);
@@ -1282,30 +1597,54 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         float dV = __fmul_rn((float)FPT, ff_f(ff_sub(d3, p3)));
         float rm = __fmul_rn(__fadd_rn(df, ff_f(dp)), 0.5f);
         dr2[r] = __fmul_rn(__fdiv_rn(w[k], dV), __fmul_rn(rm, rm));
+        // bin boundary after this particle?
+        double dd = ff_d(d[k]);
+        int bnext = 0;
+        while (bnext < nbins && !(dd < S.edge[bnext])) bnext++;
+        double dpd = ff_d(dp);
+        int bcur = 0;
+        if (r > 0) { while (bcur < nbins && !(dpd < S.edge[bcur])) bcur++; }
+        if (bnext > bcur || (uint64_t)(r + 1) == n2) has_end = true;
         dp = d[k];
+        qp = q[k];
         r++;
       }
     }
-    ff e2[16], t2[16];
-    bscan_ff<16>(a2, e2, t2, S.scan);
-    // potential energy and most-bound candidates
-    ff phi[kItems], aU = ffz(), lU[kItems];
+    // potential: per-particle prefix (needed for U of every particle)
+    ff ePh[1], tPh[1], vPh[1] = {tphi};
+    bscan_ff<1>(vPh, ePh, tPh, S.scan);
+    ff phi[kItems], tU = ffz();
     float Ef[kItems];
-    ff runp = ffz();
+    {
+      ff run = ff_add(cPhi, ePh[0]);
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      runp = ff_add(runp, pt[k]);
-      phi[k] = ff_add(ff_add(c2[0], e2[0]), runp);
-      Ef[k] = 3.0e38f;
-      if (m[k]) {
-        ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
-        aU = ff_add(aU, U);
-        Ef[k] = __fadd_rn(__fmul_rn(0.5f, Tp[k]), ff_f(U));
+      for (int k = 0; k < kItems; k++) {
+        run = ff_add(run, pt[k]);
+        phi[k] = run;
+        Ef[k] = 3.0e38f;
+        if (m[k]) {
+          ff U = ff_mulf(ff_sub(run, Phi0), w[k]);
+          tU = ff_add(tU, U);
+          Ef[k] = __fadd_rn(__fmul_rn(0.5f, Tp[k]), ff_f(U));
+        }
       }
-      lU[k] = aU;
     }
-    ff eU[1], tU[1], vU[1] = {aU};
-    bscan_ff<1>(vU, eU, tU, S.scan);
+    // channels needed only at bin ends: full scans in tiles with a bin end,
+    // block totals otherwise
+    const bool tile_end = __syncthreads_or(has_end ? 1 : 0) != 0;
+    ff ef5[5], tf5[5], af5[5] = {tf[0], tf[1], tf[2], tf[3], tU};
+    float eg[11], tgt[11];
+    if (tile_end) {
+      bscan_ff<5>(af5, ef5, tf5, S.scan);
+      bscan_f<11>(tg, eg, tgt, S.scan);
+    } else {
+      breduce_ff<5>(af5, tf5, S.scan);
+      breduce_f<11>(tg, tgt, S.scan);
+#pragma unroll
+      for (int j = 0; j < 5; j++) ef5[j] = ffz();
+#pragma unroll
+      for (int j = 0; j < 11; j++) eg[j] = 0.f;
+    }
     // most bound particle: FP32 screen, FP64 decision
     float emin = 3.0e38f;
 #pragma unroll
@@ -1316,7 +1655,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       if (lane == 0) S.bf[wid] = emin;
       __syncthreads();
       float tmin = 3.0e38f;
-      for (int q = 0; q < nw; q++) tmin = fminf(tmin, S.bf[q]);
+      for (int qq = 0; qq < nw; qq++) tmin = fminf(tmin, S.bf[qq]);
       __syncthreads();
       float ref = fminf(tmin, (float)Ebest);
       float cut = ref + 1e-4f * fabsf(ref) + 1e-30f;
@@ -1326,22 +1665,8 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       for (int k = 0; k < kItems; k++) {
         if (!m[k] || !(Ef[k] <= cut)) continue;
         (*nret)++;
-        uint64_t e = o + W.seid[o + i0 + k];
-        double dX = wrap_s((double)B.x[e] - cxd), dY = wrap_s((double)B.y[e] - cyd), dZ = wrap_s((double)B.z[e] - czd);
-        ff M = Mr[k];
-        double Md = ff_d(M);
-        ff VX = ff_add(ff_add(c1[1], e1[1]), l1[k][1]);
-        ff VY = ff_add(ff_add(c1[2], e1[2]), l1[k][2]);
-        ff VZ = ff_add(ff_add(c1[3], e1[3]), l1[k][3]);
-        double dVX = ((double)B.vx[e] - ff_d(VX) / Md), dVY = ((double)B.vy[e] - ff_d(VY) / Md),
-               dVZ = ((double)B.vz[e] - ff_d(VZ) / Md);
-        dVX += P.Hubble * dX * P.r_fac / P.v_fac;
-        dVY += P.Hubble * dY * P.r_fac / P.v_fac;
-        dVZ += P.Hubble * dZ * P.r_fac / P.v_fac;
-        double wk = (double)w[k];
-        double Tpart = wk * ((dVX * dVX + dVY * dVY) + dVZ * dVZ);
-        double Upart = (ff_d(phi[k]) - ff_d(Phi0)) * wk;
-        double E = 0.5 * Tpart + Upart;
+        double E = mbp_energy64(c, B, W, P, o + i0 + k, ff_add(b1[0], l1[k][0]), ff_add(b1[1], l1[k][1]),
+                                ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), phi[k], Phi0, w[k]);
         if (E < bE) { bE = E; bs = (long long)(i0 + k); }
       }
       for (int off = 16; off > 0; off >>= 1) {
@@ -1354,88 +1679,94 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       __syncthreads();
       double TE = 1e300;
       long long TS = -1;
-      for (int q = 0; q < nw; q++) {
-        double oE = S.bd[q];
-        long long oi = S.bl[q];
+      for (int qq = 0; qq < nw; qq++) {
+        double oE = S.bd[qq];
+        long long oi = S.bl[qq];
         bool take = oi >= 0 && (TS < 0 || oE < TE || (oE == TE && oi < TS));
         if (take) { TE = oE; TS = oi; }
       }
       __syncthreads();
       if (TS >= 0 && TE < Ebest) { Ebest = TE; Eslot = TS; }
     }
-    // bin records at bin ends
-    {
-      ff dpk = dp0;
+    // bin records at bin ends (cumulative values over the members so far)
+    if (tile_end && has_end) {
+      ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
       int r = rank0;
+      ff runf[5];
+      float rung[11];
 #pragma unroll
+      for (int j = 0; j < 5; j++) runf[j] = ff_add(j < 4 ? cf[j] : cU, ef5[j]);
+#pragma unroll
+      for (int j = 0; j < 11; j++) rung[j] = __fadd_rn(cg[j], eg[j]);
+      ff runU = ff_add(cU, ef5[4]);
       for (int k = 0; k < kItems; k++) {
         if (!m[k]) continue;
-        double dpd = ff_d(dpk), dd = ff_d(d[k]);
+        ff M = ff_add(b1[0], l1[k][0]);
+        PTerms t;
+        pterms_ool(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], q[k], dp, qp, M,
+                   ff_add(b1[1], l1[k][1]), ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), Hrv, P.has_w, t);
+        runf[0] = ff_add(runf[0], t.T);
+        for (int j = 0; j < 11; j++) rung[j] = __fadd_rn(rung[j], t.g[j]);
+        ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
+        runU = ff_add(runU, U);
+        double dd = ff_d(d[k]), dpd = ff_d(dp);
         int bcur = 0;
         if (r > 0) { while (bcur < nbins && !(dpd < S.edge[bcur])) bcur++; }
         int bnext = 0;
         while (bnext < nbins && !(dd < S.edge[bnext])) bnext++;
         bool last = (uint64_t)(r + 1) == n2;
         int bend = last ? nbins : bnext;
-        if (bend > bcur) {
-          ff Mk = ff_add(ff_add(c1[0], e1[0]), l1[k][0]);
-          // cumulative channels at this item: recompute the terms of items <= k
-          ff run[16];
-#pragma unroll
-          for (int q = 0; q < 16; q++) run[q] = ff_add(c2[q], e2[q]);
-          {
-            ff dq = dp0;
-            for (int kk = 0; kk <= k; kk++) {
-              if (!m[kk]) continue;
-              ff tm[16];
-              float tdummy;
-              prof_terms(P, w[kk], vx[kk], vy[kk], vz[kk], dx[kk], dy[kk], dz[kk], dxl[kk], dyl[kk], dzl[kk], d[kk],
-                         dq, Mr[kk],
-                         ff_add(ff_add(c1[1], e1[1]), l1[kk][1]), ff_add(ff_add(c1[2], e1[2]), l1[kk][2]),
-                         ff_add(ff_add(c1[3], e1[3]), l1[kk][3]), cxf, cyf, czf, Hrv, tm, &tdummy);
-              for (int q = 0; q < 16; q++) run[q] = ff_add(run[q], tm[q]);
-              dq = d[kk];
-            }
-          }
-          double Phid = ff_d(phi[k]);
-          double Upart = (Phid - ff_d(Phi0)) * (double)w[k];
-          ff Uc = ff_add(ff_add(cU, eU[0]), lU[k]);
-          for (int b = bcur; b < bend; b++) {
-            Bin& R = S.bins[b];
-            R.npart = (double)(r + 1);
-            R.M = ff_d(Mk);
-            R.Lx = ff_d(run[1]);
-            R.Ly = ff_d(run[2]);
-            R.Lz = ff_d(run[3]);
-            R.T = ff_d(run[4]);
-            R.U = ff_d(Uc);
-            R.a11 = ff_d(run[8]);
-            R.a22 = ff_d(run[9]);
-            R.a33 = ff_d(run[10]);
-            R.a12 = ff_d(run[11]);
-            R.a13 = ff_d(run[12]);
-            R.a23 = ff_d(run[13]);
-            R.vesc2 = 2 * fabs(Upart) / (double)w[k];
-          }
+        for (int bb = bcur; bb < bend; bb++) {
+          Bin& R = S.bins[bb];
+          R.npart = (double)(r + 1);
+          R.M = ff_d(M);
+          R.Lx = ff_d(ff_add(cgc[0], fff(rung[0])));
+          R.Ly = ff_d(ff_add(cgc[1], fff(rung[1])));
+          R.Lz = ff_d(ff_add(cgc[2], fff(rung[2])));
+          R.T = ff_d(runf[0]);
+          R.U = ff_d(runU);
+          R.a11 = ff_d(ff_add(cgc[3], fff(rung[3])));
+          R.a22 = ff_d(ff_add(cgc[4], fff(rung[4])));
+          R.a33 = ff_d(ff_add(cgc[5], fff(rung[5])));
+          R.a12 = ff_d(ff_add(cgc[6], fff(rung[6])));
+          R.a13 = ff_d(ff_add(cgc[7], fff(rung[7])));
+          R.a23 = ff_d(ff_add(cgc[8], fff(rung[8])));
+          R.vesc2 = 2 * fabs((ff_d(phi[k]) - ff_d(Phi0)) * (double)w[k]) / (double)w[k];
         }
-        dpk = d[k];
+        dp = d[k];
+        qp = q[k];
         r++;
       }
     }
+    // carries
 #pragma unroll
-    for (int q = 0; q < 4; q++) c1[q] = ff_add(c1[q], t1[q]);
+    for (int j = 0; j < 4; j++) c1[j] = ff_add(c1[j], t1[j]);
+    cPhi = ff_add(cPhi, tPh[0]);
 #pragma unroll
-    for (int q = 0; q < 16; q++) c2[q] = ff_add(c2[q], t2[q]);
-    cU = ff_add(cU, tU[0]);
-    cD = blockLast;
+    for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], tf5[j]);
+    cU = ff_add(cU, tf5[4]);
+#pragma unroll
+    for (int j = 0; j < 11; j++) { cgc[j] = ff_add(cgc[j], fff(tgt[j])); cg[j] = 0.f; }
+#pragma unroll
+    for (int j = 0; j < 4; j++) cD[j] = blockLast[j];
     cr += tn;
     __syncthreads();
   }
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
+#ifdef AHFGPU_PHASE_TIMERS
+  long long _pp = clock64();
+#endif
   write_bin_rows(S.bins, S.edge, nbins, rows);
   __syncthreads();
+#ifdef AHFGPU_PHASE_TIMERS
+  if (threadIdx.x == 0 && W.phase) { long long t = clock64(); atomicAdd(&W.phase[8], (unsigned long long)(t - _pp)); _pp = t; }
+#endif
   uint64_t i_r2 = find_max32(c, B, W, S, 0, 3, n2, nret);
   uint64_t i_rm = find_max32(c, B, W, S, 1, 1, n2, nret);
+#ifdef AHFGPU_PHASE_TIMERS
+  __syncthreads();
+  if (threadIdx.x == 0 && W.phase) { long long t = clock64(); atomicAdd(&W.phase[9], (unsigned long long)(t - _pp)); }
+#endif
   if (threadIdx.x == 0) {
     double r2 = rank_dist64(c, B, W, kNignore + i_r2);
     double x_max = rank_dist64(c, B, W, kNignore + i_rm);
@@ -1453,8 +1784,10 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     double M_max = ovd * FPT * (rb * rb * rb);
     double V_max = M_max / R_max;
     long long mbe = Eslot >= 0 ? (long long)(o + W.seid[o + Eslot]) : -1;
-    finish_scalars(rows, nbins, ff_d(c1[0]), ff_d(c1[1]), ff_d(c1[2]), ff_d(c1[3]), ff_d(c2[5]), ff_d(c2[6]),
-                   ff_d(c2[7]), ff_d(c2[14]), ff_d(c2[15]), mbe, r2, R_max, V_max, P, B, c.cx, c.cy, c.cz, hout);
+    double Mt = ff_d(c1[0]);
+    finish_scalars(rows, nbins, Mt, ff_d(c1[1]), ff_d(c1[2]), ff_d(c1[3]), Mt * c.cx + ff_d(cf[1]),
+                   Mt * c.cy + ff_d(cf[2]), Mt * c.cz + ff_d(cf[3]), ff_d(cgc[9]), ff_d(cgc[10]), mbe, r2, R_max,
+                   V_max, P, B, c.cx, c.cy, c.cz, hout);
     hout.nbins = nbins;
     hout.flags |= AHFGPU_HALO_RAN_PROFILE;
   }
@@ -1513,8 +1846,11 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     __syncthreads();
     return;
   }
+  PT_BEGIN;
   keys32(c, B, W);
+  PT_MARK(W, 0);
   bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.o, c.n, stack, W.stack_cap, S.sort);
+  PT_MARK(W, 1);
   if (!ok) {
     if (threadIdx.x == 0) { atomicExch(W.err, kErrWorklist); W.halo[h] = hout; }
     __syncthreads();
@@ -1536,9 +1872,11 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     hout.flags |= AHFGPU_HALO_RAN_SORT | AHFGPU_HALO_RAN_RVIR0;
     if (ties) atomicAdd(&W.counters[2], ties);
   }
+  PT_MARK(W, 2);
   double mo[3];
   ff Phi0;
   uint64_t n1 = rvir0_phi(c, B, W, P, S, &Phi0, mo, &nret);
+  PT_MARK(W, 3);
   if (threadIdx.x == 0) { hout.M_vir = mo[0]; hout.R_vir = mo[1]; hout.ovdens = mo[2]; hout.Phi0 = 0.0; }
   uint64_t nlist = c.n, ncur = n1;
   bool to_fp64 = false;
@@ -1586,6 +1924,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       atomicAdd(&W.counters[1], 1ull);
       hout.flags |= AHFGPU_HALO_REPLAYED;
     }
+    PT_MARK(W, 4);
     if (last_exact && npart >= (uint64_t)P.MINPART) {
       ff Mf;
       it.rv_slot = rvir_pass32(c, B, W, P, S, n1, &Mf, &nret);
@@ -1629,7 +1968,9 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
           hout.ovdens = M / V * P.rho_fac / P.rho_vir;
         }
         __syncthreads();
+        PT_MARK(W, 5);
         if (ncur >= (uint64_t)P.MINPART) profiles32(c, B, W, P, S, n1, ncur, Phi0_used, hout, &nret);
+        PT_MARK(W, 6);
       }
     }
   }
@@ -1647,6 +1988,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     return;
   }
   write_members32(c, nlist, B, W);
+  PT_MARK(W, 7);
   if (threadIdx.x == 0) {
     hout.npart = ncur;
     W.halo[h] = hout;

@@ -17,7 +17,7 @@ from . import abi
 from .abi import Batch, HostResult, Params, Result, make_batch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libahfgpu.so")
+LIB_PATH = os.environ.get("AHFGPU_LIB", os.path.join(HERE, "libahfgpu.so"))
 
 SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
