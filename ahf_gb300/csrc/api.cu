@@ -497,7 +497,12 @@ int ahfgpu_init(int device) {
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
-    CK(cudaStreamCreateWithFlags(&g.cls_stream[k], cudaStreamNonBlocking));
+    // larger classes get higher priority: their CTAs are scheduled first and
+    // the small-halo classes fill SMs as they free up
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    int pr = k == 2 ? hi : (k == 1 ? (lo + hi) / 2 : lo);
+    CK(cudaStreamCreateWithPriority(&g.cls_stream[k], cudaStreamNonBlocking, pr));
     CK(cudaEventCreateWithFlags(&g.ev_join[k], cudaEventDisableTiming));
   }
   CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
