@@ -46,6 +46,8 @@ template <class SS>
 struct F32Smem {
   SS sort;
   float scan[32 * 2 * 16];
+  uint4 rec[16 * 4];       // two halves of 8 warp records (WRec, 64 bytes each)
+  float eup[kMaxBins], edn[kMaxBins];   // float neighbours of the bin edges
   int iscan[96];
   float lasth[32], lastl[32];
   double lastd[32];
@@ -302,6 +304,245 @@ __device__ __forceinline__ long long bmin_ll(long long v, SM& S) {
 }
 
 // ---------------------------------------------------------------------------
+// Exact running sums of masses and momenta: 64-bit fixed point with a
+// per-halo scale 2^s chosen so that the whole list sums below 2^61.  Integer
+// addition is associative, so every block-level prefix equals the sequential
+// sum of the same (rounded) terms; a term loses only bits below 2^-s.
+
+struct Fix {
+  int sm, sv;          // mass and momentum scale exponents
+  float fm, fv;        // 2^sm, 2^sv
+  float im, iv;        // 2^-sm, 2^-sv
+  double dm, dv;       // 2^-sm, 2^-sv
+  double vq;           // bound of the quantisation error of a bulk-velocity component
+  float vqf;           // 3 vq v_fac (FP32 test)
+};
+
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
+
+// round(x 2^s) for |x 2^s| < 2^62 (the scaling by 2^s is exact)
+__device__ __forceinline__ long long f2fix(float x, float scale) { return __float2ll_rn(__fmul_rn(x, scale)); }
+
+// w v in fixed point: the exact product (two floats) rounded to the grid
+__device__ __forceinline__ long long wv2fix(float w, float v, float scale, int has_w) {
+  if (!has_w) return f2fix(v, scale);
+  float p = __fmul_rn(w, v);
+  float e = __fmaf_rn(w, v, -p);
+  return f2fix(p, scale) + f2fix(e, scale);
+}
+
+// fixed point -> float-float (relative error <= 2^-48)
+__device__ __forceinline__ ff i2ff(long long v, float iscale) {
+  float h = __ll2float_rn(v);
+  float l = __ll2float_rn(v - __float2ll_rn(h));
+  ff r = ff_quick(h, l);
+  return ff{__fmul_rn(r.hi, iscale), __fmul_rn(r.lo, iscale)};
+}
+
+__device__ __forceinline__ float i2f(long long v, float iscale) { return __fmul_rn(__ll2float_rn(v), iscale); }
+
+// per-halo scales from the list length and the largest weight / velocity
+__device__ __forceinline__ Fix make_fix(uint64_t n, float wmax, float wmin, float vmax, double v_fac) {
+  Fix F;
+  double nb = (double)n + 2.0;
+  int e;
+  frexp(nb * (double)wmax, &e);
+  F.sm = min(max(61 - e, -100), 100);
+  double bv = nb * (double)wmax * (double)vmax;
+  if (!(bv > 1e-30)) bv = 1e-30;
+  frexp(bv, &e);
+  F.sv = min(max(61 - e, -100), 100);
+  F.fm = pow2f(F.sm); F.im = pow2f(-F.sm);
+  F.fv = pow2f(F.sv); F.iv = pow2f(-F.sv);
+  F.dm = ldexp(1.0, -F.sm); F.dv = ldexp(1.0, -F.sv);
+  // |V_j - exact| <= (j lsb_v / 2 + |V_j| j lsb_m / 2) / (j wmin); x2 slack
+  double wl = wmin > 0.f ? (double)wmin : 1e-30;
+  F.vq = (F.dv + (double)vmax * F.dm) / wl;
+  F.vqf = (float)(3.0 * F.vq * v_fac);
+  return F;
+}
+
+// ---------------------------------------------------------------------------
+// One-barrier block scans.  Each warp scans its lanes with shuffles and
+// leaves its total in a 64-byte record; after one barrier every thread folds
+// the records of the lower warps in warp order (a fixed order, so results
+// are deterministic).  Successive calls alternate between the two halves of
+// the record buffer (`par`, uniform over the block), so a record is never
+// rewritten while a slower warp may still be reading it.
+
+struct __align__(16) WRec {
+  long long a[4];      // int64 sums
+  long long slot;      // payload slot of the warp's last valid lane
+  int cnt, valid;
+  float p[4];          // payload of the warp's last valid lane
+};
+
+template <class SM>
+__device__ __forceinline__ WRec* wrec(SM& S, int& par) {
+  WRec* r = reinterpret_cast<WRec*>(&S.rec[(par & 1) * 32]);
+  par++;
+  return r;
+}
+
+// 4 int64 sums + a count + the "last valid" payload (4 floats and a slot).
+// ex/excnt: sums over lower threads; pe/pslot: payload of the nearest lower
+// valid thread (carry cp/cslot if none); tot/pb: block totals / last.
+template <class SM>
+__device__ __forceinline__ void scan_bound(const long long (&a)[4], int cnt, bool has, const float (&p)[4],
+                                           long long slot, const float (&cp)[4], long long cslot,
+                                           long long (&ex)[4], long long (&tot)[4], int& excnt, int& totcnt,
+                                           float (&pe)[4], long long& pslot, float (&pb)[4], long long& pbslot,
+                                           SM& S, int& par) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long inc[4];
+  int ic = cnt;
+#pragma unroll
+  for (int c = 0; c < 4; c++) inc[c] = a[c];
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+      long long y = __shfl_up_sync(FULL, inc[c], off);
+      if (lane >= off) inc[c] += y;
+    }
+    int yc = __shfl_up_sync(FULL, ic, off);
+    if (lane >= off) ic += yc;
+  }
+  const unsigned m = __ballot_sync(FULL, has);
+  const unsigned below = m & ((1u << lane) - 1u);
+  const int src = below ? (31 - __clz(below)) : 0;
+  const int ll = m ? (31 - __clz(m)) : 0;
+  float mp[4], wp[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    mp[j] = __shfl_sync(FULL, p[j], src);
+    wp[j] = __shfl_sync(FULL, p[j], ll);
+  }
+  long long ms = __shfl_sync(FULL, slot, src);
+  long long wsl = __shfl_sync(FULL, slot, ll);
+  WRec* R = wrec(S, par);
+  if (lane == 31) {
+    WRec& r = R[wid];
+#pragma unroll
+    for (int c = 0; c < 4; c++) r.a[c] = inc[c];
+    r.cnt = ic;
+    r.valid = m != 0u;
+#pragma unroll
+    for (int j = 0; j < 4; j++) r.p[j] = wp[j];
+    r.slot = wsl;
+  }
+  __syncthreads();
+  long long e[4] = {0, 0, 0, 0};
+  int ec = 0;
+  float lp[4] = {cp[0], cp[1], cp[2], cp[3]};
+  long long ls = cslot;
+  for (int w = 0; w < wid; w++) {
+    const WRec& r = R[w];
+#pragma unroll
+    for (int c = 0; c < 4; c++) e[c] += r.a[c];
+    ec += r.cnt;
+    if (r.valid) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) lp[j] = r.p[j];
+      ls = r.slot;
+    }
+  }
+  long long t[4] = {e[0], e[1], e[2], e[3]};
+  int tc = ec;
+  float bp[4] = {lp[0], lp[1], lp[2], lp[3]};
+  long long bs = ls;
+  for (int w = wid; w < nw; w++) {
+    const WRec& r = R[w];
+#pragma unroll
+    for (int c = 0; c < 4; c++) t[c] += r.a[c];
+    tc += r.cnt;
+    if (r.valid) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) bp[j] = r.p[j];
+      bs = r.slot;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    ex[c] = e[c] + (inc[c] - a[c]);
+    tot[c] = t[c];
+  }
+  excnt = ec + (ic - cnt);
+  totcnt = tc;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    pe[j] = below ? mp[j] : lp[j];
+    pb[j] = bp[j];
+  }
+  pslot = below ? ms : ls;
+  pbslot = bs;
+}
+
+// one float-float sum (exclusive prefix and block total) and one int64
+// minimum (block minimum)
+template <class SM>
+__device__ __forceinline__ void scan_ff_min(ff v, long long mn, ff& ex, ff& tot, long long& bmin, SM& S, int& par) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  ff inc = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    ff y = {__shfl_up_sync(FULL, inc.hi, off), __shfl_up_sync(FULL, inc.lo, off)};
+    if (lane >= off) inc = ff_add(y, inc);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    long long o = __shfl_xor_sync(FULL, mn, off);
+    mn = o < mn ? o : mn;
+  }
+  ff prev = {__shfl_up_sync(FULL, inc.hi, 1), __shfl_up_sync(FULL, inc.lo, 1)};
+  WRec* R = wrec(S, par);
+  if (lane == 31) {
+    R[wid].p[0] = inc.hi;
+    R[wid].p[1] = inc.lo;
+    R[wid].a[0] = mn;
+  }
+  __syncthreads();
+  ff e = ffz();
+  long long bm = 0x7fffffffffffffffll;
+  for (int w = 0; w < wid; w++) {
+    e = ff_add(e, ff{R[w].p[0], R[w].p[1]});
+    bm = R[w].a[0] < bm ? R[w].a[0] : bm;
+  }
+  ff t = e;
+  for (int w = wid; w < nw; w++) {
+    t = ff_add(t, ff{R[w].p[0], R[w].p[1]});
+    bm = R[w].a[0] < bm ? R[w].a[0] : bm;
+  }
+  ex = lane > 0 ? ff_add(e, prev) : e;
+  tot = t;
+  bmin = bm;
+}
+
+// one int64 sum: exclusive prefix and block total
+template <class SM>
+__device__ __forceinline__ void scan_i64(long long v, long long& ex, long long& tot, SM& S, int& par) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  long long inc = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    long long y = __shfl_up_sync(FULL, inc, off);
+    if (lane >= off) inc += y;
+  }
+  WRec* R = wrec(S, par);
+  if (lane == 31) R[wid].a[0] = inc;
+  __syncthreads();
+  long long e = 0;
+  for (int w = 0; w < wid; w++) e += R[w].a[0];
+  long long t = e;
+  for (int w = wid; w < nw; w++) t += R[w].a[0];
+  ex = e + (inc - v);
+  tot = t;
+}
+
+// ---------------------------------------------------------------------------
 // fixed-point geometry
 
 // float in [0,1) -> 2^-62 fixed point (exact for x >= 2^-38)
@@ -350,8 +591,6 @@ __device__ __forceinline__ uint64_t sqkey(long long dx, long long dy, long long 
   }
   return ((unsigned long long)(E + 1) << 56) | ((m << 1) >> 8);
 }
-
-__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
 
 // key -> squared distance (box units^2) as float-float
 __device__ __forceinline__ ff key_d2(uint64_t key) {
@@ -428,8 +667,12 @@ static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, 
   return ties;
 }
 
-static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W) {
+// gathers the sorted slots; lim = {max |v| component, max w, min w}
+template <class SM>
+static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                                float (&lim)[3]) {
   const float s62 = pow2f(-62);
+  float vm = 0.f, wx = 0.f, wn = 3.0e38f;
   for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x) {
     uint64_t s = c.o + i;
     uint32_t j = W.idxA[s];
@@ -453,13 +696,32 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
     W.fdxl[s] = __fmul_rn(__ll2float_rn(dx - __float2ll_rn(hx)), s62);
     W.fdyl[s] = __fmul_rn(__ll2float_rn(dy - __float2ll_rn(hy)), s62);
     W.fdzl[s] = __fmul_rn(__ll2float_rn(dz - __float2ll_rn(hz)), s62);
-    W.svx[s] = B.vx[e];
-    W.svy[s] = B.vy[e];
-    W.svz[s] = B.vz[e];
-    W.sw[s] = B.w ? B.w[e] : 1.0f;
+    float vx = B.vx[e], vy = B.vy[e], vz = B.vz[e], w = B.w ? B.w[e] : 1.0f;
+    W.svx[s] = vx;
+    W.svy[s] = vy;
+    W.svz[s] = vz;
+    W.sw[s] = w;
     W.seid[s] = j;
     W.flag[s] = 1;
+    vm = fmaxf(vm, fmaxf(fabsf(vx), fmaxf(fabsf(vy), fabsf(vz))));
+    wx = fmaxf(wx, w);
+    wn = fminf(wn, w);
   }
+  for (int off = 16; off > 0; off >>= 1) {
+    vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, off));
+    wx = fmaxf(wx, __shfl_xor_sync(0xffffffffu, wx, off));
+    wn = fminf(wn, __shfl_xor_sync(0xffffffffu, wn, off));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { S.scan[3 * wid] = vm; S.scan[3 * wid + 1] = wx; S.scan[3 * wid + 2] = wn; }
+  __syncthreads();
+  lim[0] = 0.f; lim[1] = 0.f; lim[2] = 3.0e38f;
+  for (int w = 0; w < nw; w++) {
+    lim[0] = fmaxf(lim[0], S.scan[3 * w]);
+    lim[1] = fmaxf(lim[1], S.scan[3 * w + 1]);
+    lim[2] = fminf(lim[2], S.scan[3 * w + 2]);
+  }
+  if (!P.has_w) { lim[1] = 1.f; lim[2] = 1.f; }
   __syncthreads();
 }
 
@@ -519,66 +781,72 @@ static __device__ __noinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, c
 
 // ---------------------------------------------------------------------------
 // rem_outsideRvir(.,0) over all slots, fused with the potential prefix of
-// the first unbinding iteration.  Returns n1; sets *Phi0 (float-float).
+// the first unbinding iteration (stored, float-float inclusive, in phi for
+// the slots that stay).  Returns n1; sets *Phi0 (float-float).
 template <class SM>
 static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                              ff* Phi0, double* mo, unsigned* nret) {
-  ff cM = ffz(), cPhi = ffz();
+                                     const Fix& F, ff* Phi0, double* mo, unsigned* nret, int& par) {
+  const float V43f = (float)(4. * kPi / 3.);
+  const float ovk = __fmul_rn(__fmul_rn(P.f_ovlim, P.f_rvrf), V43f);
+  float2* phs = reinterpret_cast<float2*>(W.phi + c.o);
+  long long cM = 0;
+  ff cPhi = ffz();
   long long stop = -1;
   ff stopM = ffz(), stopD = ffz(), stopPhi = ffz();
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     float w[kItems];
     ff d[kItems], q[kItems], dp, qp;
-    ff locM[kItems];
-    ff accM = ffz();
+    long long fw[kItems], acc = 0;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       bool v = i < c.n;
-      w[k] = v ? W.sw[c.o + i] : 0.f;
+      w[k] = v ? (P.has_w ? W.sw[c.o + i] : 1.f) : 0.f;
       d[k] = v ? ff{W.fdh[c.o + i], W.fdl[c.o + i]} : ffz();
       q[k] = v ? ff{W.fqh[c.o + i], W.fql[c.o + i]} : ffz();
-      accM = ff_add(accM, fff(w[k]));
-      locM[k] = accM;
+      fw[k] = f2fix(w[k], F.fm);
+      acc += fw[k];
     }
     bool hasp = i0 > 0 && i0 < c.n;
     dp = hasp ? ff{W.fdh[c.o + i0 - 1], W.fdl[c.o + i0 - 1]} : ffz();
     qp = hasp ? ff{W.fqh[c.o + i0 - 1], W.fql[c.o + i0 - 1]} : ffz();
-    ff ex[1], tot[1];
-    ff vv[1] = {accM};
-    bscan_ff<1>(vv, ex, tot, S.scan);
-    ff base_M = ff_add(cM, ex[0]);
-    ff term[kItems], accT = ffz();
-    ff Mk[kItems];
-#pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      Mk[k] = ff_add(base_M, locM[k]);
-      ff prevd = k == 0 ? dp : d[k - 1];
-      ff prevq = k == 0 ? qp : q[k - 1];
-      term[k] = i < c.n ? phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq) : ffz();
-      accT = ff_add(accT, term[k]);
-      term[k] = accT;     // thread-local inclusive
-    }
-    ff exT[1], totT[1];
-    ff vt[1] = {accT};
-    bscan_ff<1>(vt, exT, totT, S.scan);
-    ff basePhi = ff_add(cPhi, exT[0]);
+    long long exM, totM;
+    scan_i64(acc, exM, totM, S, par);
+    long long rM = cM + exM;
+    ff term[kItems], accT = ffz(), Mk[kItems];
     long long myfail = 0x7fffffffffffffffll;
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
+      rM += fw[k];
+      Mk[k] = i2ff(rM, F.im);
+      ff prevd = k == 0 ? dp : d[k - 1];
+      ff prevq = k == 0 ? qp : q[k - 1];
+      if (i < c.n) accT = ff_add(accT, phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq));
+      term[k] = accT;     // thread-local inclusive
       if (i < c.n && myfail == 0x7fffffffffffffffll) {
-        if (ov_fail(c, B, W, P, c.o + i, Mk[k], d[k], nret)) myfail = (long long)i;
+        float rhs = __fmul_rn(ovk, __fmul_rn(__fmul_rn(d[k].hi, d[k].hi), d[k].hi));
+        if (!(Mk[k].hi > __fmul_rn(rhs, 1.f + 4.f * kBand1)) && ov_fail(c, B, W, P, c.o + i, Mk[k], d[k], nret))
+          myfail = (long long)i;
       }
     }
-    long long f = bmin_ll(myfail, S);
+    ff exT, totT;
+    long long f;
+    scan_ff_min(accT, myfail, exT, totT, f, S, par);
+    ff basePhi = ff_add(cPhi, exT);
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      long long i = (long long)(i0 + k);
+      if (i < (long long)c.n && i <= f) {
+        ff v = ff_add(basePhi, term[k]);
+        phs[i] = make_float2(v.hi, v.lo);
+      }
+    }
     if (f != 0x7fffffffffffffffll) {
       if ((long long)i0 <= f && f < (long long)(i0 + kItems)) {
         int k = (int)(f - (long long)i0);
         ff phi = ff_add(basePhi, term[k]);
-        S.bd[0] = ff_d(Mk[k]); S.bd[1] = ff_d(phi);
         S.bf[0] = Mk[k].hi; S.bf[1] = Mk[k].lo; S.bf[2] = d[k].hi; S.bf[3] = d[k].lo;
         S.bf[4] = phi.hi; S.bf[5] = phi.lo;
       }
@@ -588,13 +856,13 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
       __syncthreads();
       break;
     }
-    cM = ff_add(cM, tot[0]);
-    cPhi = ff_add(cPhi, totT[0]);
+    cM += totM;
+    cPhi = ff_add(cPhi, totT);
   }
   uint64_t n1;
   if (stop < 0) {
     n1 = c.n;
-    stopM = cM;
+    stopM = i2ff(cM, F.im);
     stopPhi = cPhi;
     stopD = ff{W.fdh[c.o + c.n - 1], W.fdl[c.o + c.n - 1]};
   } else {
@@ -615,46 +883,74 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
 
 // ---------------------------------------------------------------------------
 // FP64 re-test of a bound decision (reference operation order, own inputs,
-// prefixes from the float-float scans).  Sets *amb when the result is inside
-// the reference's rounding band.
+// exact fixed-point running sums, float-float potential).  Sets *amb when the
+// result is inside the reference's rounding band.
 static __device__ __noinline__ bool retest_bound(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
-                                             uint64_t s, uint64_t pos, uint64_t n1, ff Phi, ff Phi0, ff VX,
-                                             ff VY, ff VZ, ff Mv, float vmax, bool* amb) {
+                                             uint64_t s, uint64_t pos, uint64_t n1, double phi, double phi0,
+                                             double VXc, double VYc, double VZc, double M_vel, float vmax, double vq,
+                                             bool* amb) {
   uint64_t e = c.o + W.seid[s];
   double dX = wrap_s((double)B.x[e] - c.cx);
   double dY = wrap_s((double)B.y[e] - c.cy);
   double dZ = wrap_s((double)B.z[e] - c.cz);
   double d = sqrt((dX * dX + dY * dY) + dZ * dZ);
-  double phi = ff_d(Phi), phi0 = ff_d(Phi0);
   double v_esc2 = d > kMachineZero ? (2 * fabs(phi - phi0) * P.phi_fac) : 1e30;
-  double M_vel = ff_d(Mv);
   double VXp = (double)B.vx[e], VYp = (double)B.vy[e], VZp = (double)B.vz[e];
   double hx = P.Hubble * (dX) * P.r_fac, hy = P.Hubble * (dY) * P.r_fac, hz = P.Hubble * (dZ) * P.r_fac;
-  double dVX = (VXp - ff_d(VX) / M_vel) * P.v_fac + hx;
-  double dVY = (VYp - ff_d(VY) / M_vel) * P.v_fac + hy;
-  double dVZ = (VZp - ff_d(VZ) / M_vel) * P.v_fac + hz;
+  double dVX = (VXp - VXc / M_vel) * P.v_fac + hx;
+  double dVY = (VYp - VYc / M_vel) * P.v_fac + hy;
+  double dVZ = (VZp - VZc / M_vel) * P.v_fac + hz;
   double vel2 = (dVX * dVX + dVY * dVY) + dVZ * dVZ;
   double thr = P.v2_tune * v_esc2;
   // band: the reference's sequential sums differ from exact ones by at most
-  // ~(j+1)u of their absolute sums; the float-float prefixes by ~2^-40
+  // ~(j+1)u of their absolute sums; the float-float potential by ~2^-40, the
+  // fixed-point bulk velocity by vq
   double g = 2.0 * ((double)pos + 64.0) * kEps64 + 9.1e-13;
   double gn = 2.0 * ((double)n1 + 64.0) * kEps64 + 9.1e-13;
   double A = fabs(phi - phi0);
   double dthr = d > kMachineZero ? thr * ((gn * fabs(phi0) * 2.0) / fmax(A, 1e-300) + 8 * kEps64) : thr * 8 * kEps64;
   double sb = (double)vmax * P.v_fac;
-  double ddv = g * sb + 6.0 * kEps64 * (2.0 * sb + fabs(hx) + fabs(hy) + fabs(hz));
+  double ddv = g * sb + 6.0 * kEps64 * (2.0 * sb + fabs(hx) + fabs(hy) + fabs(hz)) + vq * P.v_fac;
   double dvel2 = 2.0 * 1.7320508075688772 * sqrt(vel2) * ddv + 3.0 * ddv * ddv + 8 * kEps64 * vel2;
   if (fabs(vel2 - thr) <= 2.5 * (dthr + dvel2)) *amb = true;
   return !(vel2 > thr);
 }
 
+// FP32 bound test of a member against exact running sums (fixed point):
+// 1 bound, 0 unbound, -1 inside the bound of its own rounding errors
+__device__ __forceinline__ int bound32(float vx, float vy, float vz, float dx, float dy, float dz, float thr,
+                                       float ethr, long long Mi, long long Xi, long long Yi, long long Zi,
+                                       const Fix& F, float vf, float Hr) {
+  const float fe = 5.9604645e-08f;   // 2^-24
+  float rM = __frcp_rn(i2f(Mi, F.im));
+  float Vx = __fmul_rn(i2f(Xi, F.iv), rM), Vy = __fmul_rn(i2f(Yi, F.iv), rM), Vz = __fmul_rn(i2f(Zi, F.iv), rM);
+  float hx = __fmul_rn(Hr, dx), hy = __fmul_rn(Hr, dy), hz = __fmul_rn(Hr, dz);
+  float dVX = __fadd_rn(__fmul_rn(__fsub_rn(vx, Vx), vf), hx);
+  float dVY = __fadd_rn(__fmul_rn(__fsub_rn(vy, Vy), vf), hy);
+  float dVZ = __fadd_rn(__fmul_rn(__fsub_rn(vz, Vz), vf), hz);
+  float vel2 = __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ));
+  // error bound: each component a few roundings of the magnitudes involved
+  // (the bulk velocity carries four), the squares and sums a few more; x2
+  float mag = __fadd_rn(__fmul_rn(__fadd_rn(fabsf(vx) + fabsf(vy) + fabsf(vz), fabsf(Vx) + fabsf(Vy) + fabsf(Vz)), vf),
+                        fabsf(hx) + fabsf(hy) + fabsf(hz));
+  float edv = __fadd_rn(__fmul_rn(8.f * fe, mag), F.vqf);
+  float sdv = fabsf(dVX) + fabsf(dVY) + fabsf(dVZ);
+  float err = __fadd_rn(__fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(2.f * sdv, edv), __fmul_rn(3.f, __fmul_rn(edv, edv))),
+                                                 __fmul_rn(8.f * fe, __fadd_rn(vel2, thr)))), ethr);
+  float margin = __fsub_rn(thr, vel2);
+  if (isfinite(margin) && isfinite(err) && fabsf(margin) > err) return margin >= 0.f ? 1 : 0;
+  return -1;
+}
+
 // ---------------------------------------------------------------------------
 // One rem_unbound iteration (ahf_halos.c:3336-3601) in one pass over slots
-// [0, n1) with members in flag bit0.  In: Phi0 of this iteration, seed slot.
-// Out: flag bit1 = bound (bit0 kept); next-iteration Phi0; kept count/mass;
-// last kept slot; the rvir1 candidate (first kept slot failing the
-// overdensity test).  amb: some decision stayed inside the reference-rounding
-// band (the caller redoes the iteration exactly).
+// [0, n1) with members in flag bit0 and their potential prefix (float-float,
+// inclusive) in phi.  In: Phi0 of this iteration, seed slot.  Out: flag bit1
+// = bound (bit0 kept); the potential prefix of the kept particles (the next
+// iteration's members) written over phi; next-iteration Phi0; kept
+// count/mass; last kept slot; the rvir1 candidate (first kept slot failing
+// the overdensity test).  amb: some decision stayed inside the reference-
+// rounding band (the caller redoes the iteration exactly).
 struct IterOut {
   long long nb;
   ff Mb, Phi0n;
@@ -667,249 +963,150 @@ struct IterOut {
 
 template <class SM>
 static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                                   uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out, unsigned* nret) {
+                                   const Fix& F, uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out,
+                                   unsigned* nret, int& par) {
   const uint64_t o = c.o;
   const float vf = (float)P.v_fac, Hr = (float)(P.Hubble * P.r_fac), v2t = (float)P.v2_tune;
   const float pf2 = (float)(2.0 * P.phi_fac);
   const float V43f = (float)(4. * kPi / 3.);
+  const float ovk = __fmul_rn(__fmul_rn(P.f_ovlim, P.f_rvrf), V43f);
+  const double phi0d = ff_d(Phi0);
+  // absolute error of the float-float potential prefixes (chained carries)
+  const float ethr = (float)(((double)n1 * 3e-17 + 1e-10) * fabs(phi0d) * (double)v2t * (double)pf2);
+  float2* phs = reinterpret_cast<float2*>(W.phi + o);
+  const int has_w = P.has_w;
+  // running sums of the bound particles; the bulk velocity starts from the
+  // seed particle (ahf_halos.c:3441-3470)
   const float w0 = W.sw[o + js];
-  ff cM = ffz(), cPhi = ffz();
-  float cD[4] = {0.f, 0.f, 0.f, 0.f};
-  ff cVX = two_prod(w0, W.svx[o + js]), cVY = two_prod(w0, W.svy[o + js]), cVZ = two_prod(w0, W.svz[o + js]);
-  ff cMv = fff(w0);
-  ff cMb = ffz(), cPhiN = ffz();
+  const long long sM = f2fix(w0, F.fm);
+  const long long sX = wv2fix(w0, W.svx[o + js], F.fv, 1), sY = wv2fix(w0, W.svy[o + js], F.fv, 1),
+                  sZ = wv2fix(w0, W.svz[o + js], F.fv, 1);
+  long long cM = 0, cX = 0, cY = 0, cZ = 0, cNb = 0;
   float cDb[4] = {0.f, 0.f, 0.f, 0.f};
-  long long cNb = 0, last_slot = -1, rv = -1;
+  long long cLs = -1;
+  ff cPhiN = ffz();
+  long long rv = -1;
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
-    bool m[kItems];
-    float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
+    bool m[kItems], b[kItems];
+    float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems], thr[kItems];
     ff d[kItems], q[kItems];
-    bool any_m = false;
-    float lastm[4] = {0.f, 0.f, 0.f, 0.f};
-    ff accM = ffz(), locM[kItems];
+    long long fw[kItems], fx[kItems], fy[kItems], fz[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       m[k] = i < n1 && (W.flag[o + i] & 1);
-      w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
+      w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = thr[k] = 0.f;
       d[k] = q[k] = ffz();
+      fw[k] = fx[k] = fy[k] = fz[k] = 0;
       if (m[k]) {
-        w[k] = W.sw[o + i];
+        w[k] = has_w ? W.sw[o + i] : 1.f;
         vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
         dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
         d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
         q[k] = ff{W.fqh[o + i], W.fql[o + i]};
-        any_m = true;
-        lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
-        accM = ff_add(accM, fff(w[k]));
-      }
-      locM[k] = accM;
-    }
-    // member mass prefix, previous member, potential prefix
-    ff exM[1], totM[1], vM[1] = {accM};
-    bscan_ff<1>(vM, exM, totM, S.scan);
-    float dprev[4], blockLast[4];
-    blast4(any_m, lastm, cD, dprev, blockLast, S);
-    ff Mk[kItems], phi[kItems], accP = ffz();
-    {
-      ff dp = {dprev[0], dprev[1]}, qp = {dprev[2], dprev[3]};
-      ff baseM = ff_add(cM, exM[0]);
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        Mk[k] = ff_add(baseM, locM[k]);
-        if (m[k]) {
-          accP = ff_add(accP, phi_termq(Mk[k], w[k], d[k], q[k], dp, qp));
-          dp = d[k];
-          qp = q[k];
-        }
-        phi[k] = accP;
-      }
-    }
-    ff exP[1], totP[1], vP[1] = {accP};
-    bscan_ff<1>(vP, exP, totP, S.scan);
-    float thr[kItems];
-    {
-      ff basePhi = ff_add(cPhi, exP[0]);
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        phi[k] = ff_add(basePhi, phi[k]);
-        float A = fabsf(ff_f(ff_sub(phi[k], Phi0)));
+        float2 ph = phs[i];
+        float A = fabsf(ff_f(ff_sub(ff{ph.x, ph.y}, Phi0)));
         thr[k] = dpos(d[k]) ? __fmul_rn(v2t, __fmul_rn(pf2, A)) : __fmul_rn(v2t, 1e30f);
+        fw[k] = f2fix(w[k], F.fm);
+        fx[k] = wv2fix(w[k], vx[k], F.fv, has_w);
+        fy[k] = wv2fix(w[k], vy[k], F.fv, has_w);
+        fz[k] = wv2fix(w[k], vz[k], F.fv, has_w);
       }
     }
-    // tile fixpoint of the bound flags.  FP32 decisions use momenta relative
-    // to the tile's reference bulk velocity Vr = cV/cMv (small, random
-    // deviations u = v - Vr), so V = Vr + (R + sum w u)/Mv with R = cV - Vr cMv
-    // kept in float-float; each decision carries a first-order bound on its
-    // FP32 error.  Float-float prefixes (for the FP64 re-test) are built only
-    // in rounds where some decision falls inside its bound.
-    const float fe = 5.9604645e-08f;   // 2^-24
-    const float Vrx = ff_f(ff_div(cVX, cMv)), Vry = ff_f(ff_div(cVY, cMv)), Vrz = ff_f(ff_div(cVZ, cMv));
-    const float Rx = ff_f(ff_sub(cVX, ff_mul(fff(Vrx), cMv)));
-    const float Ry = ff_f(ff_sub(cVY, ff_mul(fff(Vry), cMv)));
-    const float Rz = ff_f(ff_sub(cVZ, ff_mul(fff(Vrz), cMv)));
-    float ux[kItems], uy[kItems], uz[kItems];
+    // first guess of the flags: the bulk velocity at the start of the tile
+    {
+      const float rM = __frcp_rn(i2f(sM + cM, F.im));
+      const float Vx = __fmul_rn(i2f(sX + cX, F.iv), rM), Vy = __fmul_rn(i2f(sY + cY, F.iv), rM),
+                  Vz = __fmul_rn(i2f(sZ + cZ, F.iv), rM);
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      ux[k] = __fsub_rn(vx[k], Vrx);
-      uy[k] = __fsub_rn(vy[k], Vry);
-      uz[k] = __fsub_rn(vz[k], Vrz);
+      for (int k = 0; k < kItems; k++) {
+        float dVX = __fadd_rn(__fmul_rn(__fsub_rn(vx[k], Vx), vf), __fmul_rn(Hr, dx[k]));
+        float dVY = __fadd_rn(__fmul_rn(__fsub_rn(vy[k], Vy), vf), __fmul_rn(Hr, dy[k]));
+        float dVZ = __fadd_rn(__fmul_rn(__fsub_rn(vz[k], Vz), vf), __fmul_rn(Hr, dz[k]));
+        float vel2 = __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ));
+        b[k] = m[k] && !(vel2 > thr[k]);
+      }
     }
-    bool b[kItems];
-#pragma unroll
-    for (int k = 0; k < kItems; k++) b[k] = m[k];
+    // fixpoint of the bound flags: each round scans the flags of the previous
+    // round exactly and re-decides every member (the recurrence is
+    // triangular, so the flags settle from the front of the tile)
+    long long ex[4], tot[4];
+    int excnt, totcnt;
+    float pe[4], pb[4];
+    long long pslot, pbslot;
     int rounds = 0;
     bool amb_tile = false;
     while (true) {
       rounds++;
-      float fx[kItems], fy[kItems], fz[kItems], fm[kItems], fa[kItems];
-      float sx = 0.f, sy = 0.f, sz = 0.f, sm = 0.f, sa = 0.f;
+      long long a[4] = {0, 0, 0, 0};
+      int cnt = 0;
+      bool has = false;
+      float p[4] = {0.f, 0.f, 0.f, 0.f};
+      long long ps = -1;
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        fx[k] = sx; fy[k] = sy; fz[k] = sz; fm[k] = sm; fa[k] = sa;
         if (b[k]) {
-          float wx = __fmul_rn(w[k], ux[k]), wy = __fmul_rn(w[k], uy[k]), wz = __fmul_rn(w[k], uz[k]);
-          sx = __fadd_rn(sx, wx);
-          sy = __fadd_rn(sy, wy);
-          sz = __fadd_rn(sz, wz);
-          sm = __fadd_rn(sm, w[k]);
-          sa = __fadd_rn(sa, __fadd_rn(__fadd_rn(fabsf(wx), fabsf(wy)), fabsf(wz)));
+          a[0] += fw[k]; a[1] += fx[k]; a[2] += fy[k]; a[3] += fz[k];
+          cnt++;
+          has = true;
+          p[0] = d[k].hi; p[1] = d[k].lo; p[2] = q[k].hi; p[3] = q[k].lo;
+          ps = (long long)(i0 + k);
         }
       }
-      float ex5[5], tot5[5], v5[5] = {sx, sy, sz, sm, sa};
-      bscan_f<5>(v5, ex5, tot5, S.scan);
+      scan_bound(a, cnt, has, p, ps, cDb, cLs, ex, tot, excnt, totcnt, pe, pslot, pb, pbslot, S, par);
+      long long rM = sM + cM + ex[0], rX = sX + cX + ex[1], rY = sY + cY + ex[2], rZ = sZ + cZ + ex[3];
       int changed = 0;
-      bool need[kItems];
-      bool any_need = false;
+      bool nb[kItems];
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        need[k] = false;
-        if (!m[k]) continue;
-        float Ux = __fadd_rn(ex5[0], fx[k]), Uy = __fadd_rn(ex5[1], fy[k]), Uz = __fadd_rn(ex5[2], fz[k]);
-        float Mv = __fadd_rn(cMv.hi, __fadd_rn(ex5[3], fm[k]));
-        float Asum = __fadd_rn(ex5[4], fa[k]);
-        float rmv = __fdiv_rn(1.f, Mv);
-        float Dx = __fmul_rn(__fadd_rn(Rx, Ux), rmv), Dy = __fmul_rn(__fadd_rn(Ry, Uy), rmv),
-              Dz = __fmul_rn(__fadd_rn(Rz, Uz), rmv);
-        float hx = __fmul_rn(Hr, dx[k]), hy = __fmul_rn(Hr, dy[k]), hz = __fmul_rn(Hr, dz[k]);
-        float dVX = __fadd_rn(__fmul_rn(__fsub_rn(ux[k], Dx), vf), hx);
-        float dVY = __fadd_rn(__fmul_rn(__fsub_rn(uy[k], Dy), vf), hy);
-        float dVZ = __fadd_rn(__fmul_rn(__fsub_rn(uz[k], Dz), vf), hz);
-        float vel2 = __fadd_rn(__fadd_rn(__fmul_rn(dVX, dVX), __fmul_rn(dVY, dVY)), __fmul_rn(dVZ, dVZ));
-        // error bound: tile-sum error (depth <= 16 per component), the rest
-        // a few roundings of each magnitude involved; x2 slack
-        float eD = __fmul_rn(__fadd_rn(__fmul_rn(16.f * fe, Asum), __fmul_rn(fe, __fadd_rn(fabsf(Rx) + fabsf(Ry),
-                                                                                            fabsf(Rz)))), rmv);
-        float mag = __fadd_rn(__fmul_rn(__fadd_rn(fabsf(ux[k]) + fabsf(uy[k]) + fabsf(uz[k]),
-                                                  fabsf(Dx) + fabsf(Dy) + fabsf(Dz)), vf),
-                              fabsf(hx) + fabsf(hy) + fabsf(hz));
-        float edv = __fadd_rn(__fmul_rn(eD, vf), __fmul_rn(4.f * fe, mag));
-        float sdv = fabsf(dVX) + fabsf(dVY) + fabsf(dVZ);
-        float err = __fmul_rn(2.f, __fadd_rn(__fadd_rn(__fmul_rn(2.f * sdv, edv), __fmul_rn(3.f, __fmul_rn(edv, edv))),
-                                             __fmul_rn(8.f * fe, __fadd_rn(vel2, thr[k]))));
-        float margin = __fsub_rn(thr[k], vel2);
-        if (fabsf(margin) > err && isfinite(margin) && isfinite(err)) {
-          bool nb = margin >= 0.f;
-          if (nb != b[k]) { b[k] = nb; changed = 1; }
-        } else {
-          need[k] = true;
-          any_need = true;
-        }
-      }
-      if (__syncthreads_or(any_need ? 1 : 0)) {
-        // exact float-float prefixes of this round's flags
-        ff ax = ffz(), ay = ffz(), az = ffz(), am = ffz(), lx[kItems], ly[kItems], lz[kItems], lm[kItems];
-#pragma unroll
-        for (int k = 0; k < kItems; k++) {
-          lx[k] = ax; ly[k] = ay; lz[k] = az; lm[k] = am;
-          if (b[k]) {
-            ax = ff_add(ax, two_prod(w[k], vx[k]));
-            ay = ff_add(ay, two_prod(w[k], vy[k]));
-            az = ff_add(az, two_prod(w[k], vz[k]));
-            am = ff_add(am, fff(w[k]));
+        nb[k] = b[k];
+        if (m[k]) {
+          int r = bound32(vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], thr[k], ethr, rM, rX, rY, rZ, F, vf, Hr);
+          if (r < 0) {
+            (*nret)++;
+            bool amb = false;
+            float2 ph = phs[i0 + k];
+            r = retest_bound(c, B, W, P, o + i0 + k, i0 + k, n1, ff_d(ff{ph.x, ph.y}), phi0d, (double)rX * F.dv,
+                             (double)rY * F.dv, (double)rZ * F.dv, (double)rM * F.dm, vmax, F.vq, &amb) ? 1 : 0;
+            if (amb) amb_tile = true;
           }
+          nb[k] = r != 0;
+          if (nb[k] != b[k]) changed = 1;
         }
-        ff e4[4], t4[4], a4[4] = {ax, ay, az, am};
-        bscan_ff<4>(a4, e4, t4, S.scan);
-#pragma unroll
-        for (int k = 0; k < kItems; k++) {
-          if (!need[k]) continue;
-          (*nret)++;
-          bool amb = false;
-          bool nb = retest_bound(c, B, W, P, o + i0 + k, i0 + k, n1, phi[k], Phi0,
-                                 ff_add(ff_add(cVX, e4[0]), lx[k]), ff_add(ff_add(cVY, e4[1]), ly[k]),
-                                 ff_add(ff_add(cVZ, e4[2]), lz[k]), ff_add(ff_add(cMv, e4[3]), lm[k]), vmax, &amb);
-          if (amb) amb_tile = true;
-          if (nb != b[k]) { b[k] = nb; changed = 1; }
-        }
+        if (b[k]) { rM += fw[k]; rX += fx[k]; rY += fy[k]; rZ += fz[k]; }
       }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) b[k] = nb[k];
       if (!__syncthreads_or(changed)) break;
       if (rounds >= kMaxFixRounds) { amb_tile = true; break; }
     }
     if (rounds > maxr) maxr = rounds;
+    if (P.force_exact) amb_tile = true;
     amb_any |= __syncthreads_or(amb_tile ? 1 : 0);
-    // carries of the running bulk velocity: float-float tile totals
-    {
-      ff ax = ffz(), ay = ffz(), az = ffz(), am = ffz();
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        if (b[k]) {
-          ax = ff_add(ax, two_prod(w[k], vx[k]));
-          ay = ff_add(ay, two_prod(w[k], vy[k]));
-          az = ff_add(az, two_prod(w[k], vz[k]));
-          am = ff_add(am, fff(w[k]));
-        }
-      }
-      ff t4[4], a4[4] = {ax, ay, az, am};
-      breduce_ff<4>(a4, t4, S.scan);
-      cVX = ff_add(cVX, t4[0]); cVY = ff_add(cVY, t4[1]); cVZ = ff_add(cVZ, t4[2]); cMv = ff_add(cMv, t4[3]);
-    }
-    // next-iteration channels over the kept particles
-    ff accB = ffz(), locB[kItems];
-    bool any_b = false;
-    float lastb[4] = {0.f, 0.f, 0.f, 0.f};
-    int nbl = 0;
-    long long lslot = -1;
-#pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      if (b[k]) {
-        accB = ff_add(accB, fff(w[k]));
-        any_b = true;
-        lastb[0] = d[k].hi; lastb[1] = d[k].lo; lastb[2] = q[k].hi; lastb[3] = q[k].lo;
-        nbl++;
-        lslot = (long long)(i0 + k);
-      }
-      locB[k] = accB;
-    }
-    ff exB[1], totB[1], vB[1] = {accB};
-    bscan_ff<1>(vB, exB, totB, S.scan);
-    float dpb4[4], blastB[4];
-    blast4(any_b, lastb, cDb, dpb4, blastB, S);
-    int tnb;
-    bscan_int_ex(nbl, &tnb, S);
-    ff accN = ffz();
+    // next iteration: potential prefix of the kept particles, rvir1 candidate
+    ff accN = ffz(), pn[kItems];
     long long myfail = 0x7fffffffffffffffll;
     ff fM = ffz(), fD = ffz();
     {
-      ff dpb = {dpb4[0], dpb4[1]}, qpb = {dpb4[2], dpb4[3]};
-      ff baseB = ff_add(cMb, exB[0]);
-      const float lim = P.f_ovlim, rvrf = P.f_rvrf;
+      long long rMb = cM + ex[0];
+      ff dp = {pe[0], pe[1]}, qp = {pe[2], pe[3]};
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
+        pn[k] = accN;
         if (!b[k]) continue;
-        ff Mb = ff_add(baseB, locB[k]);
-        accN = ff_add(accN, phi_termq(Mb, w[k], d[k], q[k], dpb, qpb));
-        dpb = d[k];
-        qpb = q[k];
+        rMb += fw[k];
+        ff Mb = i2ff(rMb, F.im);
+        accN = ff_add(accN, phi_termq(Mb, w[k], d[k], q[k], dp, qp));
+        pn[k] = accN;
+        dp = d[k];
+        qp = q[k];
         if (rv < 0 && myfail == 0x7fffffffffffffffll) {
-          // cheap FP32 screen; the banded test (with FP64 re-test) only near ovlim
-          float df = d[k].hi;
-          float ov = __fdiv_rn(__fdiv_rn(Mb.hi, __fmul_rn(V43f, __fmul_rn(__fmul_rn(df, df), df))), rvrf);
-          if (!(ov > lim * (1.f + 4.f * kBand1)) &&
-              ov_fail(c, B, W, P, o + i0 + k, Mb, d[k], nret)) {
+          // FP32 screen; the banded test (with FP64 re-test) only near ovlim
+          float rhs = __fmul_rn(ovk, __fmul_rn(__fmul_rn(d[k].hi, d[k].hi), d[k].hi));
+          if (!(Mb.hi > __fmul_rn(rhs, 1.f + 4.f * kBand1)) && ov_fail(c, B, W, P, o + i0 + k, Mb, d[k], nret)) {
             myfail = (long long)(i0 + k);
             fM = Mb;
             fD = d[k];
@@ -917,38 +1114,42 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
         }
       }
     }
-    ff totN[1], vN[1] = {accN};
-    breduce_ff<1>(vN, totN, S.scan);
-    if (rv < 0) {
-      long long f = bmin_ll(myfail, S);
-      if (f != 0x7fffffffffffffffll) {
-        if (myfail == f) { S.bf[0] = fM.hi; S.bf[1] = fM.lo; S.bf[2] = fD.hi; S.bf[3] = fD.lo; }
-        __syncthreads();
-        rv = f;
-        rvM = ff{S.bf[0], S.bf[1]};
-        rvD = ff{S.bf[2], S.bf[3]};
-        __syncthreads();
+    ff exN, totN;
+    long long fmin;
+    scan_ff_min(accN, myfail, exN, totN, fmin, S, par);
+    {
+      ff baseN = ff_add(cPhiN, exN);
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        if (!b[k]) continue;
+        ff v = ff_add(baseN, pn[k]);
+        phs[i0 + k] = make_float2(v.hi, v.lo);
       }
     }
-    long long ls = -bmin_ll(-lslot, S);
-    if (ls >= 0) last_slot = ls;
+    if (rv < 0 && fmin != 0x7fffffffffffffffll) {
+      if (myfail == fmin) { S.bf[0] = fM.hi; S.bf[1] = fM.lo; S.bf[2] = fD.hi; S.bf[3] = fD.lo; }
+      __syncthreads();
+      rv = fmin;
+      rvM = ff{S.bf[0], S.bf[1]};
+      rvD = ff{S.bf[2], S.bf[3]};
+      __syncthreads();
+    }
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       if (i < n1) W.flag[o + i] = (uint8_t)((m[k] ? 1 : 0) | (b[k] ? 2 : 0));
     }
-    cM = ff_add(cM, totM[0]);
-    cPhi = ff_add(cPhi, totP[0]);
+    cM += tot[0]; cX += tot[1]; cY += tot[2]; cZ += tot[3];
+    cNb += totcnt;
+    cPhiN = ff_add(cPhiN, totN);
 #pragma unroll
-    for (int j = 0; j < 4; j++) { cD[j] = blockLast[j]; cDb[j] = blastB[j]; }
-    cMb = ff_add(cMb, totB[0]);
-    cPhiN = ff_add(cPhiN, totN[0]);
-    cNb += tnb;
+    for (int j = 0; j < 4; j++) cDb[j] = pb[j];
+    cLs = pbslot;
   }
   out.nb = cNb;
-  out.Mb = cMb;
-  out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(cMb, ff{cDb[0], cDb[1]})) : ffz();
-  out.last_slot = last_slot;
+  out.Mb = i2ff(cM, F.im);
+  out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(out.Mb, ff{cDb[0], cDb[1]})) : ffz();
+  out.last_slot = cLs;
   out.rv_slot = rv;
   out.rv_M = rvM;
   out.rv_d = rvD;
@@ -1109,55 +1310,75 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
 }
 
 // potential zero point Phi0 of the members in [0, n1) (the Phi0 pass,
-// ahf_halos.c:3343-3426), float-float
+// ahf_halos.c:3343-3426), float-float; stores the members' potential prefix
+// (inclusive) in phi
 template <class SM>
-static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, SM& S, uint64_t n1) {
+static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams& P, SM& S, const Fix& F, uint64_t n1,
+                                 int& par) {
   const uint64_t o = c.o;
-  ff cM = ffz(), cPhi = ffz();
+  float2* phs = reinterpret_cast<float2*>(W.phi + o);
+  long long cM = 0, cs = -1;
+  ff cPhi = ffz();
   float cD[4] = {0.f, 0.f, 0.f, 0.f};
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems];
     ff d[kItems], q[kItems];
+    long long fw[kItems];
+    long long a[4] = {0, 0, 0, 0};
+    int cnt = 0;
     bool any = false;
     float lastm[4] = {0.f, 0.f, 0.f, 0.f};
-    ff accM = ffz(), locM[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       m[k] = i < n1 && (W.flag[o + i] & 1);
-      w[k] = m[k] ? W.sw[o + i] : 0.f;
+      w[k] = m[k] ? (P.has_w ? W.sw[o + i] : 1.f) : 0.f;
       d[k] = m[k] ? ff{W.fdh[o + i], W.fdl[o + i]} : ffz();
       q[k] = m[k] ? ff{W.fqh[o + i], W.fql[o + i]} : ffz();
+      fw[k] = f2fix(w[k], F.fm);
       if (m[k]) {
-        accM = ff_add(accM, fff(w[k]));
+        a[0] += fw[k];
+        cnt++;
         any = true;
         lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
       }
-      locM[k] = accM;
     }
-    ff exM[1], totM[1], vM[1] = {accM};
-    bscan_ff<1>(vM, exM, totM, S.scan);
-    float dp4[4], blockLast[4];
-    blast4(any, lastm, cD, dp4, blockLast, S);
-    ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
-    ff accP = ffz();
+    long long ex[4], tot[4], ps, pbs;
+    int excnt, totcnt;
+    float pe[4], pb[4];
+    scan_bound(a, cnt, any, lastm, -1, cD, cs, ex, tot, excnt, totcnt, pe, ps, pb, pbs, S, par);
+    ff dp = {pe[0], pe[1]}, qp = {pe[2], pe[3]};
+    long long rM = cM + ex[0];
+    ff accP = ffz(), pt[kItems];
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
+      pt[k] = accP;
       if (!m[k]) continue;
-      accP = ff_add(accP, phi_termq(ff_add(ff_add(cM, exM[0]), locM[k]), w[k], d[k], q[k], dp, qp));
+      rM += fw[k];
+      accP = ff_add(accP, phi_termq(i2ff(rM, F.im), w[k], d[k], q[k], dp, qp));
+      pt[k] = accP;
       dp = d[k];
       qp = q[k];
     }
-    ff totP[1], vP[1] = {accP};
-    breduce_ff<1>(vP, totP, S.scan);
-    cM = ff_add(cM, totM[0]);
-    cPhi = ff_add(cPhi, totP[0]);
+    ff exP, totP;
+    long long dummy;
+    scan_ff_min(accP, 0, exP, totP, dummy, S, par);
+    ff baseP = ff_add(cPhi, exP);
 #pragma unroll
-    for (int j = 0; j < 4; j++) cD[j] = blockLast[j];
+    for (int k = 0; k < kItems; k++) {
+      if (!m[k]) continue;
+      ff v = ff_add(baseP, pt[k]);
+      phs[i0 + k] = make_float2(v.hi, v.lo);
+    }
+    cM += tot[0];
+    cPhi = ff_add(cPhi, totP);
+#pragma unroll
+    for (int j = 0; j < 4; j++) cD[j] = pb[j];
   }
-  return ff_add(cPhi, ff_div(cM, ff{cD[0], cD[1]}));
+  __syncthreads();
+  return ff_add(cPhi, ff_div(i2ff(cM, F.im), ff{cD[0], cD[1]}));
 }
 
 // rem_outsideRvir(.,1) over the members of [0, n1): slot of the first member
@@ -1374,23 +1595,23 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
 // float-float (one float division plus its residual), so the kinetic term
 // T stays accurate where Ekin + Epot cancels (lambdaE).
 struct PTerms {
-  ff phi, T, cx, cy, cz;   // potential term, kinetic term, w dX, w dY, w dZ
+  ff T, cx, cy, cz;        // kinetic term, w dX, w dY, w dZ
   float g[11];             // Lx, Ly, Lz, a11, a22, a33, a12, a13, a23, Mhi, Mlo
 };
 
-__device__ __forceinline__ ff rel_vel(float v, ff V, ff M) {
-  float b = __fdiv_rn(V.hi, M.hi);
+__device__ __forceinline__ ff rel_vel(float v, ff V, ff M, float rM) {
+  float b = __fmul_rn(V.hi, rM);
   ff r = ff_sub(V, ff_mulf(M, b));
-  ff Vb = ff_quick(b, __fdiv_rn(r.hi, M.hi));
+  ff Vb = ff_quick(b, __fmul_rn(r.hi, rM));
   return ff_sub(fff(v), Vb);
 }
 
 __device__ __forceinline__ void pterms(float w, float vx, float vy, float vz, float dx, float dy, float dz,
-                                       float dxl, float dyl, float dzl, ff d, ff q, ff dp, ff qp, ff M, ff VX,
-                                       ff VY, ff VZ, float Hrv, int has_w, PTerms& t) {
-  ff gx = rel_vel(vx, VX, M), gy = rel_vel(vy, VY, M), gz = rel_vel(vz, VZ, M);
+                                       float dxl, float dyl, float dzl, ff M, ff VX, ff VY, ff VZ, float Hrv,
+                                       int has_w, PTerms& t) {
+  const float rM = __frcp_rn(M.hi);
+  ff gx = rel_vel(vx, VX, M, rM), gy = rel_vel(vy, VY, M, rM), gz = rel_vel(vz, VZ, M, rM);
   float gxf = ff_f(gx), gyf = ff_f(gy), gzf = ff_f(gz);
-  t.phi = phi_termq(M, w, d, q, dp, qp);
   t.g[0] = __fmul_rn(w, __fsub_rn(__fmul_rn(dy, gzf), __fmul_rn(dz, gyf)));
   t.g[1] = __fmul_rn(w, __fsub_rn(__fmul_rn(dz, gxf), __fmul_rn(dx, gzf)));
   t.g[2] = __fmul_rn(w, __fsub_rn(__fmul_rn(dx, gyf), __fmul_rn(dy, gxf)));
@@ -1420,9 +1641,26 @@ __device__ __forceinline__ void pterms(float w, float vx, float vy, float vz, fl
 
 // out-of-line copy for the (rare) bin-end recomputation
 static __device__ __noinline__ void pterms_ool(float w, float vx, float vy, float vz, float dx, float dy, float dz,
-                                               float dxl, float dyl, float dzl, ff d, ff q, ff dp, ff qp, ff M,
-                                               ff VX, ff VY, ff VZ, float Hrv, int has_w, PTerms& t) {
-  pterms(w, vx, vy, vz, dx, dy, dz, dxl, dyl, dzl, d, q, dp, qp, M, VX, VY, VZ, Hrv, has_w, t);
+                                               float dxl, float dyl, float dzl, ff M, ff VX, ff VY, ff VZ,
+                                               float Hrv, int has_w, PTerms& t) {
+  pterms(w, vx, vy, vz, dx, dy, dz, dxl, dyl, dzl, M, VX, VY, VZ, Hrv, has_w, t);
+}
+
+// edge_b <= x, exact: a float comparison against the float neighbours of
+// the FP64 edge, FP64 only when x.hi lies between them
+template <class SM>
+__device__ __forceinline__ bool edge_le(const SM& S, int b, ff x) {
+  if (x.hi > S.eup[b]) return true;
+  if (x.hi < S.edn[b]) return false;
+  return S.edge[b] <= ff_d(x);
+}
+
+// number of bin edges <= x, counting on from `from` (edges ascend)
+template <class SM>
+__device__ __forceinline__ int edges_le(const SM& S, int nbins, ff x, int from) {
+  int b = from;
+  while (b < nbins && edge_le(S, b, x)) b++;
+  return b;
 }
 
 // FP64 energy 0.5 T + U of a most-bound candidate (ahf_halos.c:4380-4420)
@@ -1447,7 +1685,8 @@ static __device__ __noinline__ double mbp_energy64(const Ctx32& c, const DevBatc
 // HaloProfiles (ahf_halos.c:3961-5261) over the n2 members of [0, n1)
 template <class SM>
 static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                           uint64_t n1, uint64_t n2, ff Phi0, ahfgpu_halo& hout, unsigned* nret) {
+                                  const Fix& F, uint64_t n1, uint64_t n2, ff Phi0, ahfgpu_halo& hout, unsigned* nret,
+                                  int& par) {
   const uint64_t o = c.o;
   const double FPT = 4. * kPi / 3.;
   float2* Rff = reinterpret_cast<float2*>(W.prof_a + o);   // radius (float-float) per rank
@@ -1488,16 +1727,23 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     S.bi[0] = nb;
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < S.bi[0]; b += blockDim.x)
-    S.edge[b] = b == S.bi[0] - 1 ? S.bd[1] + kZero : pow(10., S.bd[2] + ((double)b + 1) * S.bd[3]);
+  for (int b = threadIdx.x; b < S.bi[0]; b += blockDim.x) {
+    double e = b == S.bi[0] - 1 ? S.bd[1] + kZero : pow(10., S.bd[2] + ((double)b + 1) * S.bd[3]);
+    S.edge[b] = e;
+    float f = __double2float_rn(e);
+    float up = f, dn = f;
+    if ((double)f < e) up = nextafterf(f, 3.0e38f);
+    if ((double)f > e) dn = nextafterf(f, -3.0e38f);
+    S.eup[b] = up;
+    S.edn[b] = dn;
+  }
   __syncthreads();
   const int nbins = S.bi[0];
-  const float vf = (float)P.v_fac;
   const float Hrv = (float)(P.Hubble * P.r_fac / P.v_fac);
-  const double cxd = c.cx, cyd = c.cy, czd = c.cz;
-  const ff cxf = ff_from_d(cxd), cyf = ff_from_d(cyd), czf = ff_from_d(czd);
-  ff c1[4] = {ffz(), ffz(), ffz(), ffz()};   // M, VX, VY, VZ (inclusive prefixes)
-  ff cPhi = ffz(), cU = ffz();
+  const int has_w = P.has_w;
+  const float2* phs = reinterpret_cast<const float2*>(W.phi + o);
+  long long cM = 0, cX = 0, cY = 0, cZ = 0;   // fixed-point running sums (inclusive prefixes)
+  ff cU = ffz();
   ff cf[4] = {ffz(), ffz(), ffz(), ffz()};   // T, sum w dX, sum w dY, sum w dZ
   float cg[11];                              // Lx, Ly, Lz, a11, a22, a33, a12, a13, a23, Mhi, Mlo
 #pragma unroll
@@ -1514,7 +1760,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
     float dxl[kItems], dyl[kItems], dzl[kItems];
-    ff d[kItems], q[kItems];
+    ff d[kItems], q[kItems], phi[kItems];
+    long long fw[kItems], fx[kItems], fy[kItems], fz[kItems];
+    long long a[4] = {0, 0, 0, 0};
     int nm = 0;
     bool any = false;
     float lastm[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1524,109 +1772,83 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       m[k] = i < n1 && (W.flag[o + i] & 1);
       w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
       dxl[k] = dyl[k] = dzl[k] = 0.f;
-      d[k] = q[k] = ffz();
+      d[k] = q[k] = phi[k] = ffz();
+      fw[k] = fx[k] = fy[k] = fz[k] = 0;
       if (m[k]) {
-        w[k] = W.sw[o + i];
+        w[k] = has_w ? W.sw[o + i] : 1.f;
         vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
         dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
         dxl[k] = W.fdxl[o + i]; dyl[k] = W.fdyl[o + i]; dzl[k] = W.fdzl[o + i];
         d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
         q[k] = ff{W.fqh[o + i], W.fql[o + i]};
+        float2 ph = phs[i];
+        phi[k] = ff{ph.x, ph.y};
+        fw[k] = f2fix(w[k], F.fm);
+        fx[k] = wv2fix(w[k], vx[k], F.fv, has_w);
+        fy[k] = wv2fix(w[k], vy[k], F.fv, has_w);
+        fz[k] = wv2fix(w[k], vz[k], F.fv, has_w);
+        a[0] += fw[k]; a[1] += fx[k]; a[2] += fy[k]; a[3] += fz[k];
         nm++; any = true;
         lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
       }
     }
-    int tn;
-    int rank0 = bscan_int_ex(nm, &tn, S) + cr;
+    // mass and momentum prefixes (inclusive: the reference adds the
+    // particle before using them), ranks, the previous member
+    long long ex[4], tot[4], ps, pbs;
+    int excnt, tn;
     float dp4[4], blockLast[4];
-    blast4(any, lastm, cD, dp4, blockLast, S);
-    // scan 1: mass and momentum prefixes (inclusive: the reference adds the
-    // particle before using them)
-    ff a1[4] = {ffz(), ffz(), ffz(), ffz()}, l1[kItems][4];
-#pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      if (m[k]) {
-        a1[0] = ff_add(a1[0], fff(w[k]));
-        a1[1] = ff_add(a1[1], two_prod(w[k], vx[k]));
-        a1[2] = ff_add(a1[2], two_prod(w[k], vy[k]));
-        a1[3] = ff_add(a1[3], two_prod(w[k], vz[k]));
-      }
-#pragma unroll
-      for (int j = 0; j < 4; j++) l1[k][j] = a1[j];
-    }
-    ff e1[4], t1[4];
-    bscan_ff<4>(a1, e1, t1, S.scan);
-    ff b1[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) b1[j] = ff_add(c1[j], e1[j]);
+    scan_bound(a, nm, any, lastm, -1, cD, -1, ex, tot, excnt, tn, dp4, ps, blockLast, pbs, S, par);
+    const int rank0 = cr + excnt;
     // per-particle terms, thread totals; bin ends of this tile
-    ff tf[4] = {ffz(), ffz(), ffz(), ffz()}, tphi = ffz();
+    ff tf[4] = {ffz(), ffz(), ffz(), ffz()}, tU = ffz();
     float tg[11];
 #pragma unroll
     for (int j = 0; j < 11; j++) tg[j] = 0.f;
-    float Tp[kItems];
-    ff pt[kItems];
+    float Ef[kItems];
+    ff Mk[kItems];
     bool has_end = false;
     {
       ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
       int r = rank0;
+      long long rM = cM + ex[0], rX = cX + ex[1], rY = cY + ex[2], rZ = cZ + ex[3];
+      int bcur = r > 0 ? edges_le(S, nbins, dp, 0) : 0;
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        Tp[k] = 0.f;
-        pt[k] = ffz();
+        Ef[k] = 3.0e38f;
+        Mk[k] = ffz();
         if (!m[k]) continue;
-        ff M = ff_add(b1[0], l1[k][0]);
+        rM += fw[k]; rX += fx[k]; rY += fy[k]; rZ += fz[k];
+        ff M = i2ff(rM, F.im);
+        Mk[k] = M;
         PTerms t;
-        pterms(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], q[k], dp, qp, M,
-               ff_add(b1[1], l1[k][1]), ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), Hrv, P.has_w, t);
-        pt[k] = t.phi;
-        tphi = ff_add(tphi, t.phi);
-        Tp[k] = ff_f(t.T);
+        pterms(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], M, i2ff(rX, F.iv),
+               i2ff(rY, F.iv), i2ff(rZ, F.iv), Hrv, has_w, t);
+        float Tp = ff_f(t.T);
         tf[0] = ff_add(tf[0], t.T);
         tf[1] = ff_add(tf[1], t.cx);
         tf[2] = ff_add(tf[2], t.cy);
         tf[3] = ff_add(tf[3], t.cz);
 #pragma unroll
         for (int j = 0; j < 11; j++) tg[j] = __fadd_rn(tg[j], t.g[j]);
-        // per-rank arrays (ahf_halos.c:4598-4616)
+        ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
+        tU = ff_add(tU, U);
+        Ef[k] = __fadd_rn(__fmul_rn(0.5f, Tp), ff_f(U));
+        // per-rank arrays (ahf_halos.c:4598-4616): FP32 screens of find_max
         Mff[r] = make_float2(M.hi, M.lo);
         float df = ff_f(d[k]);
-        vc2[r] = __fdiv_rn(ff_f(M), df);
+        vc2[r] = __fdividef(ff_f(M), df);
         ff d3 = ff_mul(ff_mul(d[k], d[k]), d[k]);
         ff p3 = ff_mul(ff_mul(dp, dp), dp);
         float dV = __fmul_rn((float)FPT, ff_f(ff_sub(d3, p3)));
         float rm = __fmul_rn(__fadd_rn(df, ff_f(dp)), 0.5f);
-        dr2[r] = __fmul_rn(__fdiv_rn(w[k], dV), __fmul_rn(rm, rm));
+        dr2[r] = __fmul_rn(__fdividef(w[k], dV), __fmul_rn(rm, rm));
         // bin boundary after this particle?
-        double dd = ff_d(d[k]);
-        int bnext = 0;
-        while (bnext < nbins && !(dd < S.edge[bnext])) bnext++;
-        double dpd = ff_d(dp);
-        int bcur = 0;
-        if (r > 0) { while (bcur < nbins && !(dpd < S.edge[bcur])) bcur++; }
+        int bnext = edges_le(S, nbins, d[k], bcur);
         if (bnext > bcur || (uint64_t)(r + 1) == n2) has_end = true;
+        bcur = bnext;
         dp = d[k];
         qp = q[k];
         r++;
-      }
-    }
-    // potential: per-particle prefix (needed for U of every particle)
-    ff ePh[1], tPh[1], vPh[1] = {tphi};
-    bscan_ff<1>(vPh, ePh, tPh, S.scan);
-    ff phi[kItems], tU = ffz();
-    float Ef[kItems];
-    {
-      ff run = ff_add(cPhi, ePh[0]);
-#pragma unroll
-      for (int k = 0; k < kItems; k++) {
-        run = ff_add(run, pt[k]);
-        phi[k] = run;
-        Ef[k] = 3.0e38f;
-        if (m[k]) {
-          ff U = ff_mulf(ff_sub(run, Phi0), w[k]);
-          tU = ff_add(tU, U);
-          Ef[k] = __fadd_rn(__fmul_rn(0.5f, Tp[k]), ff_f(U));
-        }
       }
     }
     // channels needed only at bin ends: full scans in tiles with a bin end,
@@ -1661,12 +1883,15 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       float cut = ref + 1e-4f * fabsf(ref) + 1e-30f;
       double bE = 1e300;
       long long bs = -1;
+      long long rX = cX + ex[1], rY = cY + ex[2], rZ = cZ + ex[3];
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
-        if (!m[k] || !(Ef[k] <= cut)) continue;
+        if (!m[k]) continue;
+        rX += fx[k]; rY += fy[k]; rZ += fz[k];
+        if (!(Ef[k] <= cut)) continue;
         (*nret)++;
-        double E = mbp_energy64(c, B, W, P, o + i0 + k, ff_add(b1[0], l1[k][0]), ff_add(b1[1], l1[k][1]),
-                                ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), phi[k], Phi0, w[k]);
+        double E = mbp_energy64(c, B, W, P, o + i0 + k, Mk[k], i2ff(rX, F.iv), i2ff(rY, F.iv), i2ff(rZ, F.iv),
+                                phi[k], Phi0, w[k]);
         if (E < bE) { bE = E; bs = (long long)(i0 + k); }
       }
       for (int off = 16; off > 0; off >>= 1) {
@@ -1690,7 +1915,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     }
     // bin records at bin ends (cumulative values over the members so far)
     if (tile_end && has_end) {
-      ff dp = {dp4[0], dp4[1]}, qp = {dp4[2], dp4[3]};
+      ff dp = {dp4[0], dp4[1]};
       int r = rank0;
       ff runf[5];
       float rung[11];
@@ -1699,21 +1924,20 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
 #pragma unroll
       for (int j = 0; j < 11; j++) rung[j] = __fadd_rn(cg[j], eg[j]);
       ff runU = ff_add(cU, ef5[4]);
+      long long rX = cX + ex[1], rY = cY + ex[2], rZ = cZ + ex[3];
+      int bcur = r > 0 ? edges_le(S, nbins, dp, 0) : 0;
       for (int k = 0; k < kItems; k++) {
         if (!m[k]) continue;
-        ff M = ff_add(b1[0], l1[k][0]);
+        rX += fx[k]; rY += fy[k]; rZ += fz[k];
+        ff M = Mk[k];
         PTerms t;
-        pterms_ool(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], d[k], q[k], dp, qp, M,
-                   ff_add(b1[1], l1[k][1]), ff_add(b1[2], l1[k][2]), ff_add(b1[3], l1[k][3]), Hrv, P.has_w, t);
+        pterms_ool(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], M, i2ff(rX, F.iv),
+                   i2ff(rY, F.iv), i2ff(rZ, F.iv), Hrv, has_w, t);
         runf[0] = ff_add(runf[0], t.T);
         for (int j = 0; j < 11; j++) rung[j] = __fadd_rn(rung[j], t.g[j]);
         ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
         runU = ff_add(runU, U);
-        double dd = ff_d(d[k]), dpd = ff_d(dp);
-        int bcur = 0;
-        if (r > 0) { while (bcur < nbins && !(dpd < S.edge[bcur])) bcur++; }
-        int bnext = 0;
-        while (bnext < nbins && !(dd < S.edge[bnext])) bnext++;
+        int bnext = edges_le(S, nbins, d[k], bcur);
         bool last = (uint64_t)(r + 1) == n2;
         int bend = last ? nbins : bnext;
         for (int bb = bcur; bb < bend; bb++) {
@@ -1733,15 +1957,12 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
           R.a23 = ff_d(ff_add(cgc[8], fff(rung[8])));
           R.vesc2 = 2 * fabs((ff_d(phi[k]) - ff_d(Phi0)) * (double)w[k]) / (double)w[k];
         }
-        dp = d[k];
-        qp = q[k];
+        bcur = bnext;
         r++;
       }
     }
     // carries
-#pragma unroll
-    for (int j = 0; j < 4; j++) c1[j] = ff_add(c1[j], t1[j]);
-    cPhi = ff_add(cPhi, tPh[0]);
+    cM += tot[0]; cX += tot[1]; cY += tot[2]; cZ += tot[3];
 #pragma unroll
     for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], tf5[j]);
     cU = ff_add(cU, tf5[4]);
@@ -1784,8 +2005,8 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     double M_max = ovd * FPT * (rb * rb * rb);
     double V_max = M_max / R_max;
     long long mbe = Eslot >= 0 ? (long long)(o + W.seid[o + Eslot]) : -1;
-    double Mt = ff_d(c1[0]);
-    finish_scalars(rows, nbins, Mt, ff_d(c1[1]), ff_d(c1[2]), ff_d(c1[3]), Mt * c.cx + ff_d(cf[1]),
+    double Mt = (double)cM * F.dm;
+    finish_scalars(rows, nbins, Mt, (double)cX * F.dv, (double)cY * F.dv, (double)cZ * F.dv, Mt * c.cx + ff_d(cf[1]),
                    Mt * c.cy + ff_d(cf[2]), Mt * c.cz + ff_d(cf[3]), ff_d(cgc[9]), ff_d(cgc[10]), mbe, r2, R_max,
                    V_max, P, B, c.cx, c.cy, c.cz, hout);
     hout.nbins = nbins;
@@ -1857,17 +2078,11 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     return;
   }
   unsigned long long ties = fix_near_ties(c, B, W);
-  gather32(c, B, W);
-  // max |v| component (FP64 band of the re-test)
-  float vm = 0.f;
-  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x)
-    vm = fmaxf(vm, fmaxf(fabsf(W.svx[c.o + i]), fmaxf(fabsf(W.svy[c.o + i]), fabsf(W.svz[c.o + i]))));
-  for (int off = 16; off > 0; off >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, off));
-  if ((threadIdx.x & 31) == 0) S.bf[8 + (threadIdx.x >> 5)] = vm;
-  __syncthreads();
-  float vmax = 0.f;
-  for (int w = 0; w < (int)(blockDim.x >> 5); w++) vmax = fmaxf(vmax, S.bf[8 + w]);
-  __syncthreads();
+  float lim[3];
+  gather32(c, B, W, P, S, lim);
+  const float vmax = lim[0];
+  const Fix F = make_fix(c.n, lim[1], lim[2], vmax, P.v_fac);
+  int par = 0;
   if (threadIdx.x == 0) {
     hout.flags |= AHFGPU_HALO_RAN_SORT | AHFGPU_HALO_RAN_RVIR0;
     if (ties) atomicAdd(&W.counters[2], ties);
@@ -1875,7 +2090,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   PT_MARK(W, 2);
   double mo[3];
   ff Phi0;
-  uint64_t n1 = rvir0_phi(c, B, W, P, S, &Phi0, mo, &nret);
+  uint64_t n1 = rvir0_phi(c, B, W, P, S, F, &Phi0, mo, &nret, par);
   PT_MARK(W, 3);
   if (threadIdx.x == 0) { hout.M_vir = mo[0]; hout.R_vir = mo[1]; hout.ovdens = mo[2]; hout.Phi0 = 0.0; }
   uint64_t nlist = c.n, ncur = n1;
@@ -1893,7 +2108,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       niter++;
       uint64_t js = seed_slot(c, W, P, niter, n1, S);
       Phi0_used = Phi0;
-      unbind_pass(c, B, W, P, S, n1, Phi0, js, vmax, it, &nret);
+      unbind_pass(c, B, W, P, S, F, n1, Phi0, js, vmax, it, &nret, par);
       last_exact = it.amb != 0;
       if (last_exact) {
         // a bound decision inside the reference's rounding band: redo this
@@ -1917,7 +2132,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       if (it.nb == 0) nob = 1;
       M_vir = ff_d(it.Mb);
       if (it.last_slot >= 0) R_vir = ref_dist(c, B, W, c.o + it.last_slot);
-      Phi0 = last_exact ? (npart > 0 ? phi0_pass32(c, W, S, n1) : ffz()) : it.Phi0n;
+      Phi0 = last_exact ? (npart > 0 ? phi0_pass32(c, W, P, S, F, n1, par) : ffz()) : it.Phi0n;
       if (((double)npart) < ((double)P.MINPART)) break;
     }
     if (nexact && threadIdx.x == 0) {
@@ -1969,7 +2184,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
         }
         __syncthreads();
         PT_MARK(W, 5);
-        if (ncur >= (uint64_t)P.MINPART) profiles32(c, B, W, P, S, n1, ncur, Phi0_used, hout, &nret);
+        if (ncur >= (uint64_t)P.MINPART) profiles32(c, B, W, P, S, F, n1, ncur, Phi0_used, hout, &nret, par);
         PT_MARK(W, 6);
       }
     }
