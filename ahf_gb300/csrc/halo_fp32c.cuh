@@ -615,13 +615,25 @@ static __device__ __noinline__ double ref_key(const DevBatch& B, uint64_t e, dou
 
 // ---------------------------------------------------------------------------
 static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
-  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x) {
-    uint64_t e = c.o + i;
-    long long dx = wrapfix(fixp(B.x[e]) - c.fx);
-    long long dy = wrapfix(fixp(B.y[e]) - c.fy);
-    long long dz = wrapfix(fixp(B.z[e]) - c.fz);
-    W.keyA[e] = sqkey(dx, dy, dz);
-    W.idxA[e] = (uint32_t)i;
+  constexpr int G = 4;   // entries in flight per thread
+  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
+    float px[G], py[G], pz[G];
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      px[k] = py[k] = pz[k] = 0.f;
+      if (i < c.n) { px[k] = __ldg(B.x + c.o + i); py[k] = __ldg(B.y + c.o + i); pz[k] = __ldg(B.z + c.o + i); }
+    }
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i >= c.n) continue;
+      long long dx = wrapfix(fixp(px[k]) - c.fx);
+      long long dy = wrapfix(fixp(py[k]) - c.fy);
+      long long dz = wrapfix(fixp(pz[k]) - c.fz);
+      W.keyA[c.o + i] = sqkey(dx, dy, dz);
+      W.idxA[c.o + i] = (uint32_t)i;
+    }
   }
   __syncthreads();
 }
@@ -673,39 +685,61 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
                                 float (&lim)[3]) {
   const float s62 = pow2f(-62);
   float vm = 0.f, wx = 0.f, wn = 3.0e38f;
-  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x) {
-    uint64_t s = c.o + i;
-    uint32_t j = W.idxA[s];
-    uint64_t e = c.o + j;
-    long long dx = wrapfix(fixp(B.x[e]) - c.fx);
-    long long dy = wrapfix(fixp(B.y[e]) - c.fy);
-    long long dz = wrapfix(fixp(B.z[e]) - c.fz);
-    ff d2 = key_d2(sqkey(dx, dy, dz));
-    ff d = ff_sqrt(d2);
-    ff q = d2.hi > 0.f ? ff_div(fff(1.f), d2) : ffz();
-    W.fdh[s] = d.hi;
-    W.fdl[s] = d.lo;
-    W.fqh[s] = q.hi;
-    W.fql[s] = q.lo;
-    // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
-    // centre-of-mass sums)
-    float hx = __ll2float_rn(dx), hy = __ll2float_rn(dy), hz = __ll2float_rn(dz);
-    W.fdx[s] = __fmul_rn(hx, s62);
-    W.fdy[s] = __fmul_rn(hy, s62);
-    W.fdz[s] = __fmul_rn(hz, s62);
-    W.fdxl[s] = __fmul_rn(__ll2float_rn(dx - __float2ll_rn(hx)), s62);
-    W.fdyl[s] = __fmul_rn(__ll2float_rn(dy - __float2ll_rn(hy)), s62);
-    W.fdzl[s] = __fmul_rn(__ll2float_rn(dz - __float2ll_rn(hz)), s62);
-    float vx = B.vx[e], vy = B.vy[e], vz = B.vz[e], w = B.w ? B.w[e] : 1.0f;
-    W.svx[s] = vx;
-    W.svy[s] = vy;
-    W.svz[s] = vz;
-    W.sw[s] = w;
-    W.seid[s] = j;
-    W.flag[s] = 1;
-    vm = fmaxf(vm, fmaxf(fabsf(vx), fmaxf(fabsf(vy), fabsf(vz))));
-    wx = fmaxf(wx, w);
-    wn = fminf(wn, w);
+  constexpr int G = 4;   // entries in flight per thread (the reads are random)
+  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
+    uint32_t jj[G];
+    float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      jj[k] = i < c.n ? W.idxA[c.o + i] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      px[k] = py[k] = pz[k] = pvx[k] = pvy[k] = pvz[k] = 0.f;
+      pw[k] = 1.f;
+      if (i < c.n) {
+        uint64_t e = c.o + jj[k];
+        px[k] = __ldg(B.x + e); py[k] = __ldg(B.y + e); pz[k] = __ldg(B.z + e);
+        pvx[k] = __ldg(B.vx + e); pvy[k] = __ldg(B.vy + e); pvz[k] = __ldg(B.vz + e);
+        if (B.w) pw[k] = __ldg(B.w + e);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i >= c.n) continue;
+      uint64_t s = c.o + i;
+      long long dx = wrapfix(fixp(px[k]) - c.fx);
+      long long dy = wrapfix(fixp(py[k]) - c.fy);
+      long long dz = wrapfix(fixp(pz[k]) - c.fz);
+      ff d2 = key_d2(sqkey(dx, dy, dz));
+      ff d = ff_sqrt(d2);
+      ff q = d2.hi > 0.f ? ff_div(fff(1.f), d2) : ffz();
+      W.fdh[s] = d.hi;
+      W.fdl[s] = d.lo;
+      W.fqh[s] = q.hi;
+      W.fql[s] = q.lo;
+      // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
+      // centre-of-mass sums)
+      float hx = __ll2float_rn(dx), hy = __ll2float_rn(dy), hz = __ll2float_rn(dz);
+      W.fdx[s] = __fmul_rn(hx, s62);
+      W.fdy[s] = __fmul_rn(hy, s62);
+      W.fdz[s] = __fmul_rn(hz, s62);
+      W.fdxl[s] = __fmul_rn(__ll2float_rn(dx - __float2ll_rn(hx)), s62);
+      W.fdyl[s] = __fmul_rn(__ll2float_rn(dy - __float2ll_rn(hy)), s62);
+      W.fdzl[s] = __fmul_rn(__ll2float_rn(dz - __float2ll_rn(hz)), s62);
+      W.svx[s] = pvx[k];
+      W.svy[s] = pvy[k];
+      W.svz[s] = pvz[k];
+      W.sw[s] = pw[k];
+      W.seid[s] = jj[k];
+      W.flag[s] = 1;
+      vm = fmaxf(vm, fmaxf(fabsf(pvx[k]), fmaxf(fabsf(pvy[k]), fabsf(pvz[k]))));
+      wx = fmaxf(wx, pw[k]);
+      wn = fminf(wn, pw[k]);
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, off));
@@ -1523,34 +1557,71 @@ static __device__ __noinline__ double smooth_at64(const Ctx32& c, const DevBatch
   return lvl[ns][i - lo];
 }
 
-template <class SM>
-static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W, SM& S, int which, int ns,
-                               uint64_t n2, unsigned* nret) {
-  uint64_t m = n2 - kNignore;
-  float* y = reinterpret_cast<float*>(W.prof_c + c.o) + (which ? 0 : n2);
-  float* t0 = reinterpret_cast<float*>(W.phi + c.o);
-  float* t1 = t0 + n2;
-  // y holds raw FP32 values at ranks; smooth a copy of [nignore, n2)
-  for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) t0[i] = y[kNignore + i];
-  __syncthreads();
-  float* cur = t0;
-  float* nxt = t1;
-  if (ns > 0 && m >= 3) {
-    for (int p = 0; p < ns; p++) {
-      for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        float r;
-        if (i == 0) r = __fdiv_rn(__fadd_rn(cur[0], cur[1]), 2.f);
-        else if (i == m - 1) r = __fdiv_rn(__fadd_rn(cur[m - 1], cur[m - 2]), 2.f);
-        else r = __fdiv_rn(__fadd_rn(__fadd_rn(cur[i - 1], cur[i]), cur[i + 1]), 3.f);
-        nxt[i] = r;
-      }
-      __syncthreads();
-      float* sw = cur; cur = nxt; nxt = sw;
+// FP32 value at index i of y after ns passes of smooth3 (general.c:548-573),
+// for an index within ns of either end: the passes are run on the window
+// [i-ns, i+ns] (values that would need data outside it are never used)
+static __device__ __noinline__ float smooth_edge32(const float* y, uint64_t m, int ns, uint64_t i) {
+  float lvl[8][8];
+  long long lo = (long long)i - ns, hi = (long long)i + ns;
+  if (lo < 0) lo = 0;
+  if (hi > (long long)m - 1) hi = (long long)m - 1;
+  int w = (int)(hi - lo + 1);
+  for (int t = 0; t < w; t++) lvl[0][t] = y[lo + t];
+  for (int p = 1; p <= ns; p++) {
+    for (int t = 0; t < w; t++) {
+      long long j = lo + t;
+      float v;
+      if (j == 0) v = __fdiv_rn(__fadd_rn(lvl[p - 1][t], lvl[p - 1][t + 1]), 2.f);
+      else if (j == (long long)m - 1) v = __fdiv_rn(__fadd_rn(lvl[p - 1][t], lvl[p - 1][t - 1]), 2.f);
+      else if (t == 0 || t == w - 1) v = 0.f;   // outside the window of i
+      else v = __fdiv_rn(__fadd_rn(__fadd_rn(lvl[p - 1][t - 1], lvl[p - 1][t]), lvl[p - 1][t + 1]), 3.f);
+      lvl[p][t] = v;
     }
   }
-  // FP32 maximum over [0, m-2]
+  return lvl[ns][i - lo];
+}
+
+// Smoothed maximum (find_max, src/libutility/general.c:608-650, on ranks
+// nignore..n2-1).  FP32 screen: away from the ends ns passes of smooth3 are
+// one stencil ((1,1,1)/3 for one pass, (1,3,6,7,6,3,1)/27 for three); every
+// value within 1e-4 of the FP32 maximum is re-evaluated exactly in FP64.
+template <class SM>
+static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W, SM& S, int which, int ns,
+                                      uint64_t n2, unsigned* nret) {
+  const uint64_t m = n2 - kNignore;
+  const float* y = reinterpret_cast<const float*>(W.prof_c + c.o) + (which ? 0 : n2) + kNignore;
+  float* sv = reinterpret_cast<float*>(W.phi + c.o);
+  // smoothed FP32 values and their maximum over [0, m-2]
   float best = -10.f;
-  for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) best = fmaxf(best, isnan(cur[i]) ? -10.f : cur[i]);
+  for (uint64_t base = 0; base < m; base += (uint64_t)blockDim.x * 4) {
+    float v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      v[k] = -10.f;
+      if (i >= m) continue;
+      if (ns == 0 || m < 3) {
+        v[k] = y[i];
+      } else if (i < (uint64_t)ns || i + ns > m - 1) {
+        v[k] = smooth_edge32(y, m, ns, i);
+      } else if (ns == 1) {
+        v[k] = __fmul_rn(__fadd_rn(__fadd_rn(y[i - 1], y[i]), y[i + 1]), 0.33333334f);
+      } else {
+        float a = __fadd_rn(y[i - 3], y[i + 3]);
+        float b3 = __fadd_rn(y[i - 2], y[i + 2]);
+        float c6 = __fadd_rn(y[i - 1], y[i + 1]);
+        v[k] = __fmul_rn(__fadd_rn(__fadd_rn(a, __fmul_rn(3.f, b3)), __fadd_rn(__fmul_rn(6.f, c6), __fmul_rn(7.f, y[i]))),
+                         0.037037037f);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i >= m) continue;
+      sv[i] = v[k];
+      if (i + 1 < m) best = fmaxf(best, isnan(v[k]) ? -10.f : v[k]);
+    }
+  }
   for (int off = 16; off > 0; off >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, off));
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (lane == 0) S.bf[wid] = best;
@@ -1563,7 +1634,7 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   double bv = -10.0;
   long long bi = -1;
   for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
-    float v = cur[i];
+    float v = sv[i];
     if (!(v >= thr)) continue;
     (*nret)++;
     double v64 = smooth_at64(c, B, W, which, m, ns, i);

@@ -4,8 +4,11 @@
 // order: ascending key, ties by list position -- the order a stable sort
 // gives.
 //
-// Lists up to kChunk pairs are sorted in shared memory (bitonic network on
-// the composite (key, slot)).  Longer lists take an MSD bucket pass: keys are
+// Lists up to kChunk pairs are sorted in shared memory: one counting pass by
+// the leading bits of (key - chunk minimum) into about one bin per pair, then
+// each thread insertion-sorts its bins on the composite (key, slot); a chunk
+// whose keys crowd into a few bins takes a bitonic network on the composite
+// instead.  Longer lists take an MSD bucket pass: keys are
 // offset by the list minimum and split into up to kSortBuckets buckets by
 // their high bits (histogram in shared memory, scatter with atomics into the
 // B buffers), after which runs of consecutive buckets that fit a chunk are
@@ -30,11 +33,15 @@ struct SortSmemT {
   static constexpr int kNb = NB;
   uint64_t key[CH];
   uint32_t idx[CH];
-  uint32_t hist[NB];
+  uint64_t key2[CH];      // chunk pairs in bin order
+  uint32_t idx2[CH];
+  uint32_t hist[NB];      // MSD pass
+  uint32_t h2[CH];        // chunk counting pass
   uint64_t red_u64[64];
   int sp;                 // worklist depth
   int seg_lo, seg_hi;     // current run of buckets
   int flag;
+  int crowd;              // chunk: some bin too full for an insertion sort
 };
 using SortSmem = SortSmemT<kChunk, kSortBuckets>;
 
@@ -42,21 +49,35 @@ __device__ __forceinline__ bool pair_less(uint64_t ka, uint32_t ia, uint64_t kb,
   return ka < kb || (ka == kb && ia < ib);
 }
 
-// Sort `cnt` (<= kChunk) pairs from (ks, is)[lo..] into (kd, id)[lo..].
-// In-place (ks == kd) is allowed: the data goes through shared memory.
+// Block min/max over a u64 sequence.
 template <class SS>
-static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
-                                       uint64_t lo, int cnt, SS& S) {
+__device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, SS& S) {
+  const unsigned FULL = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) {
+    uint64_t a = __shfl_xor_sync(FULL, mn, off);
+    uint64_t b = __shfl_xor_sync(FULL, mx, off);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) { S.red_u64[wid] = mn; S.red_u64[32 + wid] = mx; }
+  __syncthreads();
+  mn = ~0ull; mx = 0;
+  for (int w = 0; w < nw; w++) {
+    mn = S.red_u64[w] < mn ? S.red_u64[w] : mn;
+    mx = S.red_u64[32 + w] > mx ? S.red_u64[32 + w] : mx;
+  }
+  __syncthreads();
+}
+
+// Bitonic network on S.key/S.idx[0, cnt) (padded to a power of two), in place.
+template <class SS>
+static __device__ void bitonic_smem(int cnt, SS& S) {
   int P = 1;
   while (P < cnt) P <<= 1;
-  for (int i = threadIdx.x; i < P; i += blockDim.x) {
-    if (i < cnt) {
-      S.key[i] = ks[lo + i];
-      S.idx[i] = is[lo + i];
-    } else {
-      S.key[i] = ~0ull;
-      S.idx[i] = 0xffffffffu;
-    }
+  for (int i = cnt + threadIdx.x; i < P; i += blockDim.x) {
+    S.key[i] = ~0ull;
+    S.idx[i] = 0xffffffffu;
   }
   __syncthreads();
   for (int k = 2; k <= P; k <<= 1) {
@@ -77,30 +98,100 @@ static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, u
       __syncthreads();
     }
   }
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-    kd[lo + i] = S.key[i];
-    id[lo + i] = S.idx[i];
-  }
-  __syncthreads();
 }
 
-// Block min/max over a u64 sequence.
+// Sort `cnt` (<= kChunk) pairs from (ks, is)[lo..] into (kd, id)[lo..].
+// In-place (ks == kd) is allowed: the data goes through shared memory.
 template <class SS>
-__device__ __forceinline__ void block_minmax_u64(uint64_t& mn, uint64_t& mx, SS& S) {
-  const unsigned FULL = 0xffffffffu;
-  for (int off = 16; off > 0; off >>= 1) {
-    uint64_t a = __shfl_xor_sync(FULL, mn, off);
-    uint64_t b = __shfl_xor_sync(FULL, mx, off);
-    mn = a < mn ? a : mn;
-    mx = b > mx ? b : mx;
+static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, uint64_t* kd, uint32_t* id,
+                                       uint64_t lo, int cnt, SS& S) {
+  constexpr int kCrowd = 48;    // largest bin sorted by insertion
+  uint64_t mn = ~0ull, mx = 0;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    uint64_t k = ks[lo + i];
+    S.key[i] = k;
+    S.idx[i] = is[lo + i];
+    mn = k < mn ? k : mn;
+    mx = k > mx ? k : mx;
   }
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (lane == 0) { S.red_u64[wid] = mn; S.red_u64[32 + wid] = mx; }
+  block_minmax_u64(mn, mx, S);   // includes the barriers
+  int nb = 1;
+  while (nb < cnt) nb <<= 1;
+  if (nb > SS::kCh) nb = SS::kCh;
+  const uint64_t range = mx - mn;
+  int shift = 0;
+  while ((range >> shift) >= (uint64_t)nb) shift++;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) S.h2[b] = 0;
+  if (threadIdx.x == 0) S.crowd = 0;
   __syncthreads();
-  mn = ~0ull; mx = 0;
-  for (int w = 0; w < nw; w++) {
-    mn = S.red_u64[w] < mn ? S.red_u64[w] : mn;
-    mx = S.red_u64[32 + w] > mx ? S.red_u64[32 + w] : mx;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) atomicAdd(&S.h2[(int)((S.key[i] - mn) >> shift)], 1u);
+  __syncthreads();
+  // exclusive scan of the bin counts: contiguous runs of bins per thread
+  {
+    const int T = blockDim.x;
+    const int per = (nb + T - 1) / T;
+    const int b0 = threadIdx.x * per;
+    const int b1 = min(b0 + per, nb);
+    uint32_t run = 0;
+    for (int b = b0; b < b1; b++) run += S.h2[b];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t inc = run;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      uint32_t y = __shfl_up_sync(FULL, inc, off);
+      if (lane >= off) inc += y;
+    }
+    uint32_t* wt = reinterpret_cast<uint32_t*>(S.red_u64);
+    if (lane == 31) wt[wid] = inc;
+    __syncthreads();
+    uint32_t base = inc - run;
+    for (int w = 0; w < wid; w++) base += wt[w];
+    (void)nw;
+    for (int b = b0; b < b1; b++) {
+      uint32_t c = S.h2[b];
+      S.h2[b] = base;
+      base += c;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    uint64_t k = S.key[i];
+    uint32_t pos = atomicAdd(&S.h2[(int)((k - mn) >> shift)], 1u);
+    S.key2[pos] = k;
+    S.idx2[pos] = S.idx[i];
+  }
+  __syncthreads();
+  // h2[b] is now the end of bin b: insertion sort of each bin by one thread
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    int s0 = b ? (int)S.h2[b - 1] : 0, s1 = (int)S.h2[b];
+    if (s1 - s0 < 2) continue;
+    if (s1 - s0 > kCrowd) { S.crowd = 1; continue; }
+    for (int a = s0 + 1; a < s1; a++) {
+      uint64_t ka = S.key2[a];
+      uint32_t ia = S.idx2[a];
+      int c = a;
+      while (c > s0 && pair_less(ka, ia, S.key2[c - 1], S.idx2[c - 1])) {
+        S.key2[c] = S.key2[c - 1];
+        S.idx2[c] = S.idx2[c - 1];
+        c--;
+      }
+      S.key2[c] = ka;
+      S.idx2[c] = ia;
+    }
+  }
+  __syncthreads();
+  if (S.crowd) {
+    bitonic_smem(cnt, S);
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      kd[lo + i] = S.key[i];
+      id[lo + i] = S.idx[i];
+    }
+  } else {
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      kd[lo + i] = S.key2[i];
+      id[lo + i] = S.idx2[i];
+    }
   }
   __syncthreads();
 }
