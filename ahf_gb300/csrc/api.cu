@@ -242,7 +242,8 @@ int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, P
 }
 
 int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
-  const uint64_t N = std::max<uint64_t>(pl.N, 1);
+  // per-slot arrays also hold the FP32C alignment gaps (slot_base)
+  const uint64_t N = std::max<uint64_t>(pl.N, 1) + 3 * (uint64_t)pl.nhalo + 16;
   int rc;
 #define EN(buf, bytes) if ((rc = (buf).ensure(bytes)) != AHFGPU_OK) return rc
   EN(g.keyA, N * 8); EN(g.keyB, N * 8); EN(g.idxA, N * 4); EN(g.idxB, N * 4);

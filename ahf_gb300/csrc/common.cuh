@@ -81,6 +81,13 @@ struct Work {
 };
 
 
+// First slot of halo h in the FP32C per-slot work arrays: a multiple of 4
+// (16-byte aligned float arrays), at least off[h] + n_h before the next
+// halo's; the arrays hold N + 3 nhalo + 16 slots.
+__host__ __device__ __forceinline__ uint64_t slot_base(uint64_t off, int64_t h) {
+  return (off + 3ull * (uint64_t)h + 3ull) & ~3ull;
+}
+
 // Optional per-phase cycle counters (build with -DAHFGPU_PHASE_TIMERS).
 #ifdef AHFGPU_PHASE_TIMERS
 #define PT_BEGIN long long _pt = clock64();
@@ -93,9 +100,26 @@ struct Work {
       _pt = _t;                                                    \
     }                                                              \
   } while (0)
+// sub-phase marks without a barrier (thread 0's clock) and event counts
+#define PT_T0 long long _q = clock64();
+#define PT_T(W, k)                                                 \
+  do {                                                             \
+    if (threadIdx.x == 0 && (W).phase) {                           \
+      long long _t = clock64();                                    \
+      atomicAdd(&(W).phase[k], (unsigned long long)(_t - _q));     \
+      _q = _t;                                                     \
+    }                                                              \
+  } while (0)
+#define PT_ADD(W, k, v)                                                              \
+  do {                                                                               \
+    if (threadIdx.x == 0 && (W).phase) atomicAdd(&(W).phase[k], (unsigned long long)(v)); \
+  } while (0)
 #else
 #define PT_BEGIN
 #define PT_MARK(W, k) do { } while (0)
+#define PT_T0
+#define PT_T(W, k) do { } while (0)
+#define PT_ADD(W, k, v) do { } while (0)
 #endif
 
 // ---------------------------------------------------------------------------

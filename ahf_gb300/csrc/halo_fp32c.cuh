@@ -64,6 +64,7 @@ struct F32Smem {
 struct Ctx32 {
   int h;
   uint64_t o, n;
+  uint64_t s;              // first slot of the halo's work arrays (a multiple of 4)
   double cx, cy, cz;
   long long fx, fy, fz;    // centre in 2^-62 box units
 };
@@ -316,6 +317,7 @@ struct Fix {
   double dm, dv;       // 2^-sm, 2^-sv
   double vq;           // bound of the quantisation error of a bulk-velocity component
   float vqf;           // 3 vq v_fac (FP32 test)
+  long long w1;        // weight 1 in fixed point
 };
 
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
@@ -331,15 +333,54 @@ __device__ __forceinline__ long long wv2fix(float w, float v, float scale, int h
   return f2fix(p, scale) + f2fix(e, scale);
 }
 
-// fixed point -> float-float (relative error <= 2^-48)
+// 64-bit integer -> float without 64-bit conversion instructions (those
+// run at the FP64 rate): two 32-bit conversions, one rounding each, and an
+// FMA (within 1.5 ulp)
+__device__ __forceinline__ float l2f(long long v) {
+  float hi = __int2float_rn((int)(v >> 32));
+  float lo = __uint2float_rn((unsigned)(v & 0xffffffffll));
+  return __fmaf_rn(hi, 4294967296.f, lo);
+}
+
+// fixed point -> float-float: three exact 24-bit pieces (relative error
+// <= 2^-47)
 __device__ __forceinline__ ff i2ff(long long v, float iscale) {
-  float h = __ll2float_rn(v);
-  float l = __ll2float_rn(v - __float2ll_rn(h));
-  ff r = ff_quick(h, l);
+  float f2 = __fmul_rn(__int2float_rn((int)(v >> 48)), 281474976710656.f);                // 2^48
+  float f1 = __fmul_rn(__uint2float_rn((unsigned)(v >> 24) & 0xffffffu), 16777216.f);   // 2^24
+  float f0 = __uint2float_rn((unsigned)v & 0xffffffu);
+  ff r = ff_add(two_sum(f2, f1), fff(f0));
   return ff{__fmul_rn(r.hi, iscale), __fmul_rn(r.lo, iscale)};
 }
 
-__device__ __forceinline__ float i2f(long long v, float iscale) { return __fmul_rn(__ll2float_rn(v), iscale); }
+__device__ __forceinline__ float i2f(long long v, float iscale) { return __fmul_rn(l2f(v), iscale); }
+
+// Four consecutive slots of a per-slot array.  Halo slot ranges start at a
+// multiple of 4 (slot_base) and tiles at multiples of 4 slots, so every group
+// is 16-byte aligned (8-byte arrays: 32-byte); a group may run up to 3 slots
+// past the halo's last slot, into its own alignment gap (never another
+// halo's slots).
+__device__ __forceinline__ void ld4f(const float* p, float (&v)[4]) {
+  float4 t = *reinterpret_cast<const float4*>(p);
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4ff(const double* p, ff (&v)[4]) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  float4 a = q[0], b = q[1];
+  v[0] = ff{a.x, a.y}; v[1] = ff{a.z, a.w}; v[2] = ff{b.x, b.y}; v[3] = ff{b.z, b.w};
+}
+__device__ __forceinline__ unsigned ld4u8(const uint8_t* p) { return *reinterpret_cast<const unsigned*>(p); }
+__device__ __forceinline__ void ld4ll(const long long* p, long long (&v)[4]) {
+  const longlong2* q = reinterpret_cast<const longlong2*>(p);
+  longlong2 a = q[0], b = q[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+// fixed-point weights and momenta of the sorted slots (FP32C), written once
+// by the gather into the FP64 form's offset arrays
+__device__ __forceinline__ long long* fix_w(const Work& W) { return reinterpret_cast<long long*>(W.sd); }
+__device__ __forceinline__ long long* fix_x(const Work& W) { return reinterpret_cast<long long*>(W.sdx); }
+__device__ __forceinline__ long long* fix_y(const Work& W) { return reinterpret_cast<long long*>(W.sdy); }
+__device__ __forceinline__ long long* fix_z(const Work& W) { return reinterpret_cast<long long*>(W.sdz); }
 
 // per-halo scales from the list length and the largest weight / velocity
 __device__ __forceinline__ Fix make_fix(uint64_t n, float wmax, float wmin, float vmax, double v_fac) {
@@ -359,6 +400,7 @@ __device__ __forceinline__ Fix make_fix(uint64_t n, float wmax, float wmin, floa
   double wl = wmin > 0.f ? (double)wmin : 1e-30;
   F.vq = (F.dv + (double)vmax * F.dm) / wl;
   F.vqf = (float)(3.0 * F.vq * v_fac);
+  F.w1 = f2fix(1.f, F.fm);
   return F;
 }
 
@@ -600,8 +642,9 @@ __device__ __forceinline__ ff key_d2(uint64_t key) {
   unsigned long long h24 = mant >> 33, l24 = (mant >> 9) & 0xffffffull;
   // value = mant * 2^(E-56) * 2^-124
   int eh = E - 56 - 124 + 33, el = E - 56 - 124 + 9;
-  float hi = __fmul_rn((float)h24, pow2f(eh));
-  float lo = el >= -126 ? __fmul_rn((float)l24, pow2f(el)) : 0.f;
+  // two power-of-two factors keep each in the normal range (eh >= -147)
+  float hi = __fmul_rn(__fmul_rn(__uint2float_rn((unsigned)h24), pow2f(eh + 64)), pow2f(-64));
+  float lo = __fmul_rn(__fmul_rn(__uint2float_rn((unsigned)l24), pow2f(el + 64)), pow2f(-64));
   return ff_quick(hi, lo);
 }
 
@@ -614,95 +657,23 @@ static __device__ __noinline__ double ref_key(const DevBatch& B, uint64_t e, dou
 }
 
 // ---------------------------------------------------------------------------
-static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W) {
-  constexpr int G = 4;   // entries in flight per thread
-  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
-    float px[G], py[G], pz[G];
-#pragma unroll
-    for (int k = 0; k < G; k++) {
-      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      px[k] = py[k] = pz[k] = 0.f;
-      if (i < c.n) { px[k] = __ldg(B.x + c.o + i); py[k] = __ldg(B.y + c.o + i); pz[k] = __ldg(B.z + c.o + i); }
-    }
-#pragma unroll
-    for (int k = 0; k < G; k++) {
-      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      if (i >= c.n) continue;
-      long long dx = wrapfix(fixp(px[k]) - c.fx);
-      long long dy = wrapfix(fixp(py[k]) - c.fy);
-      long long dz = wrapfix(fixp(pz[k]) - c.fz);
-      W.keyA[c.o + i] = sqkey(dx, dy, dz);
-      W.idxA[c.o + i] = (uint32_t)i;
-    }
-  }
-  __syncthreads();
-}
-
-// Runs of adjacent keys closer than the reference's rounding are put in the
-// order of the reference's FP64 keys (ties by slot).  Returns exact ties.
-static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
-  unsigned long long ties = 0;
-  const uint64_t o = c.o;
-  // mark ambiguous adjacent pairs first (flag is free until gather32)
-  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x)
-    W.flag[o + i] = (i + 1 < c.n && W.keyA[o + i + 1] - W.keyA[o + i] <= 512ull) ? 1 : 0;
-  __syncthreads();
-  for (uint64_t i = threadIdx.x; i + 1 < c.n; i += blockDim.x) {
-    if (!W.flag[o + i] || (i > 0 && W.flag[o + i - 1])) continue;
-    // run [i, j] of mutually ambiguous neighbours, owned by this thread
-    uint64_t j = i + 1;
-    while (j + 1 < c.n && W.flag[o + j]) j++;
-    // insertion sort of the run by (reference key, slot)
-    for (uint64_t a = i + 1; a <= j; a++) {
-      uint32_t sa = W.idxA[o + a];
-      uint64_t ka = W.keyA[o + a];
-      double ra = ref_key(B, o + sa, c.cx, c.cy, c.cz);
-      uint64_t b = a;
-      while (b > i) {
-        uint32_t sb = W.idxA[o + b - 1];
-        double rb = ref_key(B, o + sb, c.cx, c.cy, c.cz);
-        if (rb < ra || (rb == ra && sb < sa)) break;
-        W.idxA[o + b] = sb;
-        W.keyA[o + b] = W.keyA[o + b - 1];
-        b--;
-      }
-      W.idxA[o + b] = sa;
-      W.keyA[o + b] = ka;
-    }
-    for (uint64_t a = i; a < j; a++) {
-      double r0 = ref_key(B, o + W.idxA[o + a], c.cx, c.cy, c.cz);
-      double r1 = ref_key(B, o + W.idxA[o + a + 1], c.cx, c.cy, c.cz);
-      if (r0 == r1) ties++;
-    }
-  }
-  __syncthreads();
-  return ties;
-}
-
-// gathers the sorted slots; lim = {max |v| component, max w, min w}
+// squared-distance keys of the list; lim = {max |v| component, max w, min w}
 template <class SM>
-static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                                float (&lim)[3]) {
-  const float s62 = pow2f(-62);
+static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                              float (&lim)[3]) {
+  constexpr int G = 4;   // entries in flight per thread
   float vm = 0.f, wx = 0.f, wn = 3.0e38f;
-  constexpr int G = 4;   // entries in flight per thread (the reads are random)
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
-    uint32_t jj[G];
-    float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
+    float px[G], py[G], pz[G], pv[G], pw[G];
 #pragma unroll
     for (int k = 0; k < G; k++) {
       uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      jj[k] = i < c.n ? W.idxA[c.o + i] : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < G; k++) {
-      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      px[k] = py[k] = pz[k] = pvx[k] = pvy[k] = pvz[k] = 0.f;
+      px[k] = py[k] = pz[k] = pv[k] = 0.f;
       pw[k] = 1.f;
       if (i < c.n) {
-        uint64_t e = c.o + jj[k];
+        const uint64_t e = c.o + i;
         px[k] = __ldg(B.x + e); py[k] = __ldg(B.y + e); pz[k] = __ldg(B.z + e);
-        pvx[k] = __ldg(B.vx + e); pvy[k] = __ldg(B.vy + e); pvz[k] = __ldg(B.vz + e);
+        pv[k] = fmaxf(fabsf(__ldg(B.vx + e)), fmaxf(fabsf(__ldg(B.vy + e)), fabsf(__ldg(B.vz + e))));
         if (B.w) pw[k] = __ldg(B.w + e);
       }
     }
@@ -710,33 +681,12 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
     for (int k = 0; k < G; k++) {
       uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
       if (i >= c.n) continue;
-      uint64_t s = c.o + i;
       long long dx = wrapfix(fixp(px[k]) - c.fx);
       long long dy = wrapfix(fixp(py[k]) - c.fy);
       long long dz = wrapfix(fixp(pz[k]) - c.fz);
-      ff d2 = key_d2(sqkey(dx, dy, dz));
-      ff d = ff_sqrt(d2);
-      ff q = d2.hi > 0.f ? ff_div(fff(1.f), d2) : ffz();
-      W.fdh[s] = d.hi;
-      W.fdl[s] = d.lo;
-      W.fqh[s] = q.hi;
-      W.fql[s] = q.lo;
-      // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
-      // centre-of-mass sums)
-      float hx = __ll2float_rn(dx), hy = __ll2float_rn(dy), hz = __ll2float_rn(dz);
-      W.fdx[s] = __fmul_rn(hx, s62);
-      W.fdy[s] = __fmul_rn(hy, s62);
-      W.fdz[s] = __fmul_rn(hz, s62);
-      W.fdxl[s] = __fmul_rn(__ll2float_rn(dx - __float2ll_rn(hx)), s62);
-      W.fdyl[s] = __fmul_rn(__ll2float_rn(dy - __float2ll_rn(hy)), s62);
-      W.fdzl[s] = __fmul_rn(__ll2float_rn(dz - __float2ll_rn(hz)), s62);
-      W.svx[s] = pvx[k];
-      W.svy[s] = pvy[k];
-      W.svz[s] = pvz[k];
-      W.sw[s] = pw[k];
-      W.seid[s] = jj[k];
-      W.flag[s] = 1;
-      vm = fmaxf(vm, fmaxf(fabsf(pvx[k]), fmaxf(fabsf(pvy[k]), fabsf(pvz[k]))));
+      W.keyA[c.s + i] = sqkey(dx, dy, dz);
+      W.idxA[c.s + i] = (uint32_t)i;
+      vm = fmaxf(vm, pv[k]);
       wx = fmaxf(wx, pw[k]);
       wn = fminf(wn, pw[k]);
     }
@@ -756,6 +706,110 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
     lim[2] = fminf(lim[2], S.scan[3 * w + 2]);
   }
   if (!P.has_w) { lim[1] = 1.f; lim[2] = 1.f; }
+  __syncthreads();
+}
+
+// Runs of adjacent keys closer than the reference's rounding are put in the
+// order of the reference's FP64 keys (ties by slot).  Returns exact ties.
+static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
+  unsigned long long ties = 0;
+  const uint64_t o = c.s;
+  // mark ambiguous adjacent pairs first (flag is free until gather32)
+  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x)
+    W.flag[o + i] = (i + 1 < c.n && W.keyA[o + i + 1] - W.keyA[o + i] <= 512ull) ? 1 : 0;
+  __syncthreads();
+  for (uint64_t i = threadIdx.x; i + 1 < c.n; i += blockDim.x) {
+    if (!W.flag[o + i] || (i > 0 && W.flag[o + i - 1])) continue;
+    // run [i, j] of mutually ambiguous neighbours, owned by this thread
+    uint64_t j = i + 1;
+    while (j + 1 < c.n && W.flag[o + j]) j++;
+    // insertion sort of the run by (reference key, slot)
+    for (uint64_t a = i + 1; a <= j; a++) {
+      uint32_t sa = W.idxA[o + a];
+      uint64_t ka = W.keyA[o + a];
+      double ra = ref_key(B, c.o + sa, c.cx, c.cy, c.cz);
+      uint64_t b = a;
+      while (b > i) {
+        uint32_t sb = W.idxA[o + b - 1];
+        double rb = ref_key(B, c.o + sb, c.cx, c.cy, c.cz);
+        if (rb < ra || (rb == ra && sb < sa)) break;
+        W.idxA[o + b] = sb;
+        W.keyA[o + b] = W.keyA[o + b - 1];
+        b--;
+      }
+      W.idxA[o + b] = sa;
+      W.keyA[o + b] = ka;
+    }
+    for (uint64_t a = i; a < j; a++) {
+      double r0 = ref_key(B, c.o + W.idxA[o + a], c.cx, c.cy, c.cz);
+      double r1 = ref_key(B, c.o + W.idxA[o + a + 1], c.cx, c.cy, c.cz);
+      if (r0 == r1) ties++;
+    }
+  }
+  __syncthreads();
+  return ties;
+}
+
+// gathers the sorted slots, with the fixed-point weights and momenta
+static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, const Fix& F) {
+  const float s62 = pow2f(-62);
+  constexpr int G = 4;   // entries in flight per thread (the reads are random)
+  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
+    uint32_t jj[G];
+    float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      jj[k] = i < c.n ? W.idxA[c.s + i] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      px[k] = py[k] = pz[k] = pvx[k] = pvy[k] = pvz[k] = 0.f;
+      pw[k] = 1.f;
+      if (i < c.n) {
+        uint64_t e = c.o + jj[k];
+        px[k] = __ldg(B.x + e); py[k] = __ldg(B.y + e); pz[k] = __ldg(B.z + e);
+        pvx[k] = __ldg(B.vx + e); pvy[k] = __ldg(B.vy + e); pvz[k] = __ldg(B.vz + e);
+        if (B.w) pw[k] = __ldg(B.w + e);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i >= c.n) continue;
+      uint64_t s = c.s + i;
+      long long dx = wrapfix(fixp(px[k]) - c.fx);
+      long long dy = wrapfix(fixp(py[k]) - c.fy);
+      long long dz = wrapfix(fixp(pz[k]) - c.fz);
+      ff d2 = key_d2(sqkey(dx, dy, dz));
+      ff d = ff_sqrt(d2);
+      ff q = d2.hi > 0.f ? ff_div(fff(1.f), d2) : ffz();
+      W.fdh[s] = d.hi;
+      W.fdl[s] = d.lo;
+      W.fqh[s] = q.hi;
+      W.fql[s] = q.lo;
+      // offsets as float-float (hi kept for the FP32 arithmetic, lo for the
+      // centre-of-mass sums)
+      ff ox = i2ff(dx, s62), oy = i2ff(dy, s62), oz = i2ff(dz, s62);
+      W.fdx[s] = ox.hi;
+      W.fdy[s] = oy.hi;
+      W.fdz[s] = oz.hi;
+      W.fdxl[s] = ox.lo;
+      W.fdyl[s] = oy.lo;
+      W.fdzl[s] = oz.lo;
+      W.svx[s] = pvx[k];
+      W.svy[s] = pvy[k];
+      W.svz[s] = pvz[k];
+      W.sw[s] = pw[k];
+      W.seid[s] = jj[k];
+      W.flag[s] = 1;
+      fix_w(W)[s] = f2fix(pw[k], F.fm);
+      fix_x(W)[s] = wv2fix(pw[k], pvx[k], F.fv, P.has_w);
+      fix_y(W)[s] = wv2fix(pw[k], pvy[k], F.fv, P.has_w);
+      fix_z(W)[s] = wv2fix(pw[k], pvz[k], F.fv, P.has_w);
+    }
+  }
   __syncthreads();
 }
 
@@ -822,29 +876,38 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
                                      const Fix& F, ff* Phi0, double* mo, unsigned* nret, int& par) {
   const float V43f = (float)(4. * kPi / 3.);
   const float ovk = __fmul_rn(__fmul_rn(P.f_ovlim, P.f_rvrf), V43f);
-  float2* phs = reinterpret_cast<float2*>(W.phi + c.o);
+  float2* phs = reinterpret_cast<float2*>(W.phi + c.s);
   long long cM = 0;
   ff cPhi = ffz();
   long long stop = -1;
   ff stopM = ffz(), stopD = ffz(), stopPhi = ffz();
-  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * kItems) {
+  const uint64_t tile = (uint64_t)blockDim.x * kItems;
+  for (uint64_t base = 0; base < c.n; base += tile) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     float w[kItems];
     ff d[kItems], q[kItems], dp, qp;
     long long fw[kItems], acc = 0;
+    {
+      float dh[kItems], dl[kItems], qh[kItems], ql[kItems];
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      bool v = i < c.n;
-      w[k] = v ? (P.has_w ? W.sw[c.o + i] : 1.f) : 0.f;
-      d[k] = v ? ff{W.fdh[c.o + i], W.fdl[c.o + i]} : ffz();
-      q[k] = v ? ff{W.fqh[c.o + i], W.fql[c.o + i]} : ffz();
-      fw[k] = f2fix(w[k], F.fm);
-      acc += fw[k];
+      for (int k = 0; k < kItems; k++) { w[k] = 1.f; fw[k] = F.w1; dh[k] = dl[k] = qh[k] = ql[k] = 0.f; }
+      if (i0 < c.n) {
+        if (P.has_w) { ld4f(W.sw + c.s + i0, w); ld4ll(fix_w(W) + c.s + i0, fw); }
+        ld4f(W.fdh + c.s + i0, dh); ld4f(W.fdl + c.s + i0, dl);
+        ld4f(W.fqh + c.s + i0, qh); ld4f(W.fql + c.s + i0, ql);
+      }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        bool v = i0 + k < c.n;
+        if (!v) { w[k] = 0.f; fw[k] = 0; }
+        d[k] = v ? ff{dh[k], dl[k]} : ffz();
+        q[k] = v ? ff{qh[k], ql[k]} : ffz();
+        acc += fw[k];
+      }
     }
     bool hasp = i0 > 0 && i0 < c.n;
-    dp = hasp ? ff{W.fdh[c.o + i0 - 1], W.fdl[c.o + i0 - 1]} : ffz();
-    qp = hasp ? ff{W.fqh[c.o + i0 - 1], W.fql[c.o + i0 - 1]} : ffz();
+    dp = hasp ? ff{W.fdh[c.s + i0 - 1], W.fdl[c.s + i0 - 1]} : ffz();
+    qp = hasp ? ff{W.fqh[c.s + i0 - 1], W.fql[c.s + i0 - 1]} : ffz();
     long long exM, totM;
     scan_i64(acc, exM, totM, S, par);
     long long rM = cM + exM;
@@ -861,7 +924,7 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
       term[k] = accT;     // thread-local inclusive
       if (i < c.n && myfail == 0x7fffffffffffffffll) {
         float rhs = __fmul_rn(ovk, __fmul_rn(__fmul_rn(d[k].hi, d[k].hi), d[k].hi));
-        if (!(Mk[k].hi > __fmul_rn(rhs, 1.f + 4.f * kBand1)) && ov_fail(c, B, W, P, c.o + i, Mk[k], d[k], nret))
+        if (!(Mk[k].hi > __fmul_rn(rhs, 1.f + 4.f * kBand1)) && ov_fail(c, B, W, P, c.s + i, Mk[k], d[k], nret))
           myfail = (long long)i;
       }
     }
@@ -898,19 +961,19 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
     n1 = c.n;
     stopM = i2ff(cM, F.im);
     stopPhi = cPhi;
-    stopD = ff{W.fdh[c.o + c.n - 1], W.fdl[c.o + c.n - 1]};
+    stopD = ff{W.fdh[c.s + c.n - 1], W.fdl[c.s + c.n - 1]};
   } else {
     n1 = (uint64_t)stop + 1;
   }
   // outputs in FP64 for the cut particle (as rem_outsideRvir computes them)
-  double R = ref_dist(c, B, W, c.o + n1 - 1);
+  double R = ref_dist(c, B, W, c.s + n1 - 1);
   double M = ff_d(stopM);
   double V = 4. * kPi / 3. * (R * R * R);
   mo[0] = M;
   mo[1] = R;
   mo[2] = M / V * P.rho_fac / P.rho_vir;
   *Phi0 = ff_add(stopPhi, ff_div(stopM, stopD));
-  for (uint64_t i = n1 + threadIdx.x; i < c.n; i += blockDim.x) W.flag[c.o + i] = 0;
+  for (uint64_t i = n1 + threadIdx.x; i < c.n; i += blockDim.x) W.flag[c.s + i] = 0;
   __syncthreads();
   return n1;
 }
@@ -999,7 +1062,7 @@ template <class SM>
 static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                    const Fix& F, uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out,
                                    unsigned* nret, int& par) {
-  const uint64_t o = c.o;
+  const uint64_t o = c.s;
   const float vf = (float)P.v_fac, Hr = (float)(P.Hubble * P.r_fac), v2t = (float)P.v2_tune;
   const float pf2 = (float)(2.0 * P.phi_fac);
   const float V43f = (float)(4. * kPi / 3.);
@@ -1011,10 +1074,8 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   const int has_w = P.has_w;
   // running sums of the bound particles; the bulk velocity starts from the
   // seed particle (ahf_halos.c:3441-3470)
-  const float w0 = W.sw[o + js];
-  const long long sM = f2fix(w0, F.fm);
-  const long long sX = wv2fix(w0, W.svx[o + js], F.fv, 1), sY = wv2fix(w0, W.svy[o + js], F.fv, 1),
-                  sZ = wv2fix(w0, W.svz[o + js], F.fv, 1);
+  const long long sM = fix_w(W)[o + js];
+  const long long sX = fix_x(W)[o + js], sY = fix_y(W)[o + js], sZ = fix_z(W)[o + js];
   long long cM = 0, cX = 0, cY = 0, cZ = 0, cNb = 0;
   float cDb[4] = {0.f, 0.f, 0.f, 0.f};
   long long cLs = -1;
@@ -1022,34 +1083,49 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   long long rv = -1;
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
-  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
+  const uint64_t tile = (uint64_t)blockDim.x * kItems;
+  for (uint64_t base = 0; base < n1; base += tile) {
+    PT_T0;
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems], b[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems], thr[kItems];
     ff d[kItems], q[kItems];
     long long fw[kItems], fx[kItems], fy[kItems], fz[kItems];
+    unsigned f4 = 0u;
+    {
+      float dh[kItems], dl[kItems], qh[kItems], ql[kItems];
+      ff ph[kItems];
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      m[k] = i < n1 && (W.flag[o + i] & 1);
-      w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = thr[k] = 0.f;
-      d[k] = q[k] = ffz();
-      fw[k] = fx[k] = fy[k] = fz[k] = 0;
-      if (m[k]) {
-        w[k] = has_w ? W.sw[o + i] : 1.f;
-        vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
-        dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
-        d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
-        q[k] = ff{W.fqh[o + i], W.fql[o + i]};
-        float2 ph = phs[i];
-        float A = fabsf(ff_f(ff_sub(ff{ph.x, ph.y}, Phi0)));
-        thr[k] = dpos(d[k]) ? __fmul_rn(v2t, __fmul_rn(pf2, A)) : __fmul_rn(v2t, 1e30f);
-        fw[k] = f2fix(w[k], F.fm);
-        fx[k] = wv2fix(w[k], vx[k], F.fv, has_w);
-        fy[k] = wv2fix(w[k], vy[k], F.fv, has_w);
-        fz[k] = wv2fix(w[k], vz[k], F.fv, has_w);
+      for (int k = 0; k < kItems; k++) {
+        w[k] = 1.f;
+        vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = dh[k] = dl[k] = qh[k] = ql[k] = 0.f;
+        ph[k] = ffz();
+      }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
+      if (i0 < n1) {
+        f4 = ld4u8(W.flag + o + i0);
+        if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
+        ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
+        ld4f(W.fdx + o + i0, dx); ld4f(W.fdy + o + i0, dy); ld4f(W.fdz + o + i0, dz);
+        ld4f(W.fdh + o + i0, dh); ld4f(W.fdl + o + i0, dl);
+        ld4f(W.fqh + o + i0, qh); ld4f(W.fql + o + i0, ql);
+        ld4ff(W.phi + o + i0, ph);
+        ld4ll(fix_x(W) + o + i0, fx); ld4ll(fix_y(W) + o + i0, fy); ld4ll(fix_z(W) + o + i0, fz);
+      }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        m[k] = i0 + k < n1 && ((f4 >> (8 * k)) & 1u);
+        d[k] = ff{dh[k], dl[k]};
+        q[k] = ff{qh[k], ql[k]};
+        thr[k] = 0.f;
+        if (m[k]) {
+          float A = fabsf(ff_f(ff_sub(ph[k], Phi0)));
+          thr[k] = dpos(d[k]) ? __fmul_rn(v2t, __fmul_rn(pf2, A)) : __fmul_rn(v2t, 1e30f);
+        }
       }
     }
+    PT_T(W, 10);
     // first guess of the flags: the bulk velocity at the start of the tile
     {
       const float rM = __frcp_rn(i2f(sM + cM, F.im));
@@ -1117,9 +1193,12 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
       if (!__syncthreads_or(changed)) break;
       if (rounds >= kMaxFixRounds) { amb_tile = true; break; }
     }
+    PT_T(W, 11);
+    PT_ADD(W, 14, rounds);
+    PT_ADD(W, 15, 1);
     if (rounds > maxr) maxr = rounds;
     if (P.force_exact) amb_tile = true;
-    amb_any |= __syncthreads_or(amb_tile ? 1 : 0);
+    amb_any |= amb_tile ? 1 : 0;
     // next iteration: potential prefix of the kept particles, rvir1 candidate
     ff accN = ffz(), pn[kItems];
     long long myfail = 0x7fffffffffffffffll;
@@ -1168,11 +1247,14 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
       rvD = ff{S.bf[2], S.bf[3]};
       __syncthreads();
     }
+    if (i0 < n1) {
+      unsigned nf = f4;
 #pragma unroll
-    for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      if (i < n1) W.flag[o + i] = (uint8_t)((m[k] ? 1 : 0) | (b[k] ? 2 : 0));
+      for (int k = 0; k < kItems; k++)
+        if (i0 + k < n1) nf = (nf & ~(0xffu << (8 * k))) | ((unsigned)((m[k] ? 1 : 0) | (b[k] ? 2 : 0)) << (8 * k));
+      *reinterpret_cast<unsigned*>(W.flag + o + i0) = nf;
     }
+    PT_T(W, 12);
     cM += tot[0]; cX += tot[1]; cY += tot[2]; cZ += tot[3];
     cNb += totcnt;
     cPhiN = ff_add(cPhiN, totN);
@@ -1187,7 +1269,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   out.rv_slot = rv;
   out.rv_M = rvM;
   out.rv_d = rvD;
-  out.amb = amb_any;
+  out.amb = __syncthreads_or(amb_any);
   out.rounds = maxr;
   __syncthreads();
 }
@@ -1224,7 +1306,7 @@ static __device__ double chain64(const double* a, double* out, uint64_t n, doubl
 template <class SM>
 static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                              uint64_t n1, uint64_t js, long long* nb_out, double* mb_out, long long* last_out) {
-  const uint64_t o = c.o;
+  const uint64_t o = c.s;
   double* term = W.phi + o;
   double* d64 = W.prof_a + o;
   double* ax = W.prof_b + o;
@@ -1302,7 +1384,7 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
       block_scan_excl<1>(v, ex, tot, dsm);
       if (mem) {
         double M_vel = cMV + ex[0];
-        uint64_t e = o + W.seid[o + i];
+        uint64_t e = c.o + W.seid[o + i];
         double dX = wrap_s((double)B.x[e] - c.cx), dY = wrap_s((double)B.y[e] - c.cy), dZ = wrap_s((double)B.z[e] - c.cz);
         double d = d64[i];
         double v_esc2 = d > kMachineZero ? (2 * fabs(term[i] - Phi0) * P.phi_fac) : 1e30;
@@ -1349,7 +1431,7 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
 template <class SM>
 static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams& P, SM& S, const Fix& F, uint64_t n1,
                                  int& par) {
-  const uint64_t o = c.o;
+  const uint64_t o = c.s;
   float2* phs = reinterpret_cast<float2*>(W.phi + o);
   long long cM = 0, cs = -1;
   ff cPhi = ffz();
@@ -1364,14 +1446,22 @@ static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams&
     int cnt = 0;
     bool any = false;
     float lastm[4] = {0.f, 0.f, 0.f, 0.f};
+    unsigned f4 = 0u;
+    float dh[kItems], dl[kItems], qh[kItems], ql[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; k++) { w[k] = 1.f; fw[k] = F.w1; dh[k] = dl[k] = qh[k] = ql[k] = 0.f; }
+    if (i0 < n1) {
+      f4 = ld4u8(W.flag + o + i0);
+      if (P.has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
+      ld4f(W.fdh + o + i0, dh); ld4f(W.fdl + o + i0, dl);
+      ld4f(W.fqh + o + i0, qh); ld4f(W.fql + o + i0, ql);
+    }
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      m[k] = i < n1 && (W.flag[o + i] & 1);
-      w[k] = m[k] ? (P.has_w ? W.sw[o + i] : 1.f) : 0.f;
-      d[k] = m[k] ? ff{W.fdh[o + i], W.fdl[o + i]} : ffz();
-      q[k] = m[k] ? ff{W.fqh[o + i], W.fql[o + i]} : ffz();
-      fw[k] = f2fix(w[k], F.fm);
+      m[k] = i0 + k < n1 && ((f4 >> (8 * k)) & 1u);
+      if (!m[k]) { w[k] = 0.f; fw[k] = 0; }
+      d[k] = m[k] ? ff{dh[k], dl[k]} : ffz();
+      q[k] = m[k] ? ff{qh[k], ql[k]} : ffz();
       if (m[k]) {
         a[0] += fw[k];
         cnt++;
@@ -1420,7 +1510,7 @@ static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams&
 template <class SM>
 static __device__ long long rvir_pass32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                  uint64_t n1, ff* Mfail, unsigned* nret) {
-  const uint64_t o = c.o;
+  const uint64_t o = c.s;
   ff cM = ffz();
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
     uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
@@ -1475,7 +1565,7 @@ static __device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevPar
       uint32_t pos[64];
       uint64_t nv = no_vbulk < 64 ? no_vbulk : 64;
       for (uint64_t j = 0; j < nv; j++) {
-        float mx = W.svx[c.o + j], my = W.svy[c.o + j], mz = W.svz[c.o + j];
+        float mx = W.svx[c.s + j], my = W.svy[c.s + j], mz = W.svz[c.s + j];
         m2[j] = __fadd_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)), __fmul_rn(mz, mz));
         pos[j] = (uint32_t)j;
       }
@@ -1489,7 +1579,7 @@ static __device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevPar
       }
       js = pos[no_vbulk / 2 - 1];
     } else {
-      while (js < n1 && !(W.flag[c.o + js] & 1)) js++;
+      while (js < n1 && !(W.flag[c.s + js] & 1)) js++;
     }
     S.bl[8] = (long long)js;
   }
@@ -1505,7 +1595,7 @@ static __device__ uint64_t seed_slot(const Ctx32& c, const Work& W, const DevPar
 static __device__ __noinline__ double raw64(const Ctx32& c, const DevBatch& B, const Work& W, const double* d64c, int which,
                         uint64_t r) {
   // which 0: dens_r2 (ahf_halos.c:4610-4616), 1: Vcirc2 (:4612)
-  const float2* Mff = reinterpret_cast<const float2*>(W.prof_b + c.o);
+  const float2* Mff = reinterpret_cast<const float2*>(W.prof_b + c.s);
   float2 mr = Mff[r];
   double M = (double)mr.x + (double)mr.y;
   double d = d64c[1];
@@ -1521,7 +1611,7 @@ static __device__ __noinline__ double raw64(const Ctx32& c, const DevBatch& B, c
 }
 
 static __device__ __noinline__ double rank_dist64(const Ctx32& c, const DevBatch& B, const Work& W, uint64_t r) {
-  const uint32_t* ent = reinterpret_cast<const uint32_t*>(W.prof_d + c.o);
+  const uint32_t* ent = reinterpret_cast<const uint32_t*>(W.prof_d + c.s);
   return sqrt(ref_key(B, c.o + ent[r], c.cx, c.cy, c.cz));
 }
 
@@ -1589,8 +1679,8 @@ template <class SM>
 static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const Work& W, SM& S, int which, int ns,
                                       uint64_t n2, unsigned* nret) {
   const uint64_t m = n2 - kNignore;
-  const float* y = reinterpret_cast<const float*>(W.prof_c + c.o) + (which ? 0 : n2) + kNignore;
-  float* sv = reinterpret_cast<float*>(W.phi + c.o);
+  const float* y = reinterpret_cast<const float*>(W.prof_c + c.s) + (which ? 0 : n2) + kNignore;
+  float* sv = reinterpret_cast<float*>(W.phi + c.s);
   // smoothed FP32 values and their maximum over [0, m-2]
   float best = -10.f;
   for (uint64_t base = 0; base < m; base += (uint64_t)blockDim.x * 4) {
@@ -1758,7 +1848,7 @@ template <class SM>
 static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                   const Fix& F, uint64_t n1, uint64_t n2, ff Phi0, ahfgpu_halo& hout, unsigned* nret,
                                   int& par) {
-  const uint64_t o = c.o;
+  const uint64_t o = c.s;
   const double FPT = 4. * kPi / 3.;
   float2* Rff = reinterpret_cast<float2*>(W.prof_a + o);   // radius (float-float) per rank
   float2* Mff = reinterpret_cast<float2*>(W.prof_b + o);   // mass prefix per rank
@@ -1826,7 +1916,8 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   int cr = 0;
   double Ebest = 1e30;
   long long Eslot = -1;
-  for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
+  const uint64_t tile = (uint64_t)blockDim.x * kItems;
+  for (uint64_t base = 0; base < n1; base += tile) {
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
@@ -1837,27 +1928,40 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     int nm = 0;
     bool any = false;
     float lastm[4] = {0.f, 0.f, 0.f, 0.f};
+    {
+      unsigned f4 = 0u;
+      float dh[kItems], dl[kItems], qh[kItems], ql[kItems];
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        w[k] = 1.f;
+        vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = dxl[k] = dyl[k] = dzl[k] = 0.f;
+        dh[k] = dl[k] = qh[k] = ql[k] = 0.f;
+        phi[k] = ffz();
+      }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
+      if (i0 < n1) {
+        f4 = ld4u8(W.flag + o + i0);
+        if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
+        ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
+        ld4f(W.fdx + o + i0, dx); ld4f(W.fdy + o + i0, dy); ld4f(W.fdz + o + i0, dz);
+        ld4f(W.fdxl + o + i0, dxl); ld4f(W.fdyl + o + i0, dyl); ld4f(W.fdzl + o + i0, dzl);
+        ld4f(W.fdh + o + i0, dh); ld4f(W.fdl + o + i0, dl);
+        ld4f(W.fqh + o + i0, qh); ld4f(W.fql + o + i0, ql);
+        ld4ff(W.phi + o + i0, phi);
+        ld4ll(fix_x(W) + o + i0, fx); ld4ll(fix_y(W) + o + i0, fy); ld4ll(fix_z(W) + o + i0, fz);
+      }
+#pragma unroll
+      for (int k = 0; k < kItems; k++) {
+        m[k] = i0 + k < n1 && ((f4 >> (8 * k)) & 1u);
+        d[k] = ff{dh[k], dl[k]};
+        q[k] = ff{qh[k], ql[k]};
+      }
+    }
 #pragma unroll
     for (int k = 0; k < kItems; k++) {
-      uint64_t i = i0 + k;
-      m[k] = i < n1 && (W.flag[o + i] & 1);
-      w[k] = vx[k] = vy[k] = vz[k] = dx[k] = dy[k] = dz[k] = 0.f;
-      dxl[k] = dyl[k] = dzl[k] = 0.f;
-      d[k] = q[k] = phi[k] = ffz();
-      fw[k] = fx[k] = fy[k] = fz[k] = 0;
+      if (!m[k]) { fw[k] = fx[k] = fy[k] = fz[k] = 0; }
       if (m[k]) {
-        w[k] = has_w ? W.sw[o + i] : 1.f;
-        vx[k] = W.svx[o + i]; vy[k] = W.svy[o + i]; vz[k] = W.svz[o + i];
-        dx[k] = W.fdx[o + i]; dy[k] = W.fdy[o + i]; dz[k] = W.fdz[o + i];
-        dxl[k] = W.fdxl[o + i]; dyl[k] = W.fdyl[o + i]; dzl[k] = W.fdzl[o + i];
-        d[k] = ff{W.fdh[o + i], W.fdl[o + i]};
-        q[k] = ff{W.fqh[o + i], W.fql[o + i]};
-        float2 ph = phs[i];
-        phi[k] = ff{ph.x, ph.y};
-        fw[k] = f2fix(w[k], F.fm);
-        fx[k] = wv2fix(w[k], vx[k], F.fv, has_w);
-        fy[k] = wv2fix(w[k], vy[k], F.fv, has_w);
-        fz[k] = wv2fix(w[k], vz[k], F.fv, has_w);
         a[0] += fw[k]; a[1] += fx[k]; a[2] += fy[k]; a[3] += fz[k];
         nm++; any = true;
         lastm[0] = d[k].hi; lastm[1] = d[k].lo; lastm[2] = q[k].hi; lastm[3] = q[k].lo;
@@ -2075,7 +2179,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     double ovd = Mb / (FPT * (rb * rb * rb));
     double M_max = ovd * FPT * (rb * rb * rb);
     double V_max = M_max / R_max;
-    long long mbe = Eslot >= 0 ? (long long)(o + W.seid[o + Eslot]) : -1;
+    long long mbe = Eslot >= 0 ? (long long)(c.o + W.seid[o + Eslot]) : -1;
     double Mt = (double)cM * F.dm;
     finish_scalars(rows, nbins, Mt, (double)cX * F.dv, (double)cY * F.dv, (double)cZ * F.dv, Mt * c.cx + ff_d(cf[1]),
                    Mt * c.cy + ff_d(cf[2]), Mt * c.cz + ff_d(cf[3]), ff_d(cgc[9]), ff_d(cgc[10]), mbe, r2, R_max,
@@ -2092,11 +2196,11 @@ static __device__ void write_members32(const Ctx32& c, uint64_t nlist, const Dev
   __shared__ int isc[64];
   for (uint64_t base = 0; base < nlist; base += blockDim.x) {
     uint64_t i = base + threadIdx.x;
-    bool mem = i < nlist && (W.flag[c.o + i] & 1);
+    bool mem = i < nlist && (W.flag[c.s + i] & 1);
     int tot;
     int r = block_scan_int(mem ? 1 : 0, &tot, isc) - 1 + carry;
     if (mem) {
-      uint64_t e = c.o + W.seid[c.o + i];
+      uint64_t e = c.o + W.seid[c.s + i];
       W.mem_stage[c.o + r] = B.gidx ? B.gidx[e] : e;
     }
     carry += tot;
@@ -2111,6 +2215,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   c.h = h;
   c.o = B.off[h];
   c.n = B.off[h + 1] - c.o;
+  c.s = slot_base(c.o, h);
   c.cx = B.cx[h]; c.cy = B.cy[h]; c.cz = B.cz[h];
   c.fx = llrint(c.cx * 4611686018427387904.0);   // 2^62
   c.fy = llrint(c.cy * 4611686018427387904.0);
@@ -2139,9 +2244,10 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     return;
   }
   PT_BEGIN;
-  keys32(c, B, W);
+  float lim[3];
+  keys32(c, B, W, P, S, lim);
   PT_MARK(W, 0);
-  bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.o, c.n, stack, W.stack_cap, S.sort);
+  bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.s, c.n, stack, W.stack_cap, S.sort);
   PT_MARK(W, 1);
   if (!ok) {
     if (threadIdx.x == 0) { atomicExch(W.err, kErrWorklist); W.halo[h] = hout; }
@@ -2149,10 +2255,9 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     return;
   }
   unsigned long long ties = fix_near_ties(c, B, W);
-  float lim[3];
-  gather32(c, B, W, P, S, lim);
   const float vmax = lim[0];
   const Fix F = make_fix(c.n, lim[1], lim[2], vmax, P.v_fac);
+  gather32(c, B, W, P, F);
   int par = 0;
   if (threadIdx.x == 0) {
     hout.flags |= AHFGPU_HALO_RAN_SORT | AHFGPU_HALO_RAN_RVIR0;
@@ -2195,14 +2300,14 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
         nexact++;
       }
       // members <- bound
-      for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) W.flag[c.o + i] = (W.flag[c.o + i] >> 1) & 1;
+      for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = (W.flag[c.s + i] >> 1) & 1;
       __syncthreads();
       if (it.rounds > maxr) maxr = it.rounds;
       nremove = npart - (uint64_t)it.nb;
       npart = (uint64_t)it.nb;
       if (it.nb == 0) nob = 1;
       M_vir = ff_d(it.Mb);
-      if (it.last_slot >= 0) R_vir = ref_dist(c, B, W, c.o + it.last_slot);
+      if (it.last_slot >= 0) R_vir = ref_dist(c, B, W, c.s + it.last_slot);
       Phi0 = last_exact ? (npart > 0 ? phi0_pass32(c, W, P, S, F, n1, par) : ffz()) : it.Phi0n;
       if (((double)npart) < ((double)P.MINPART)) break;
     }
@@ -2231,13 +2336,13 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       if (npart >= (uint64_t)P.MINPART) {
         // rem_outsideRvir(.,1): the candidate of the last pass
         if (it.rv_slot >= 0) {
-          for (uint64_t i = (uint64_t)it.rv_slot + 1 + threadIdx.x; i < n1; i += blockDim.x) W.flag[c.o + i] = 0;
+          for (uint64_t i = (uint64_t)it.rv_slot + 1 + threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = 0;
           __syncthreads();
         }
         int tot = 0, carry = 0;
         for (uint64_t base = 0; base < n1; base += blockDim.x) {
           uint64_t i = base + threadIdx.x;
-          bool mem = i < n1 && (W.flag[c.o + i] & 1);
+          bool mem = i < n1 && (W.flag[c.s + i] & 1);
           block_scan_int(mem ? 1 : 0, &tot, S.iscan);
           carry += tot;
         }
@@ -2245,7 +2350,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
         if (threadIdx.x == 0) {
           long long ls = it.rv_slot;
           if (ls < 0) ls = it.last_slot;
-          double R = ref_dist(c, B, W, c.o + ls);
+          double R = ref_dist(c, B, W, c.s + ls);
           double M = it.rv_slot >= 0 ? ff_d(it.rv_M) : M_vir;
           double V = 4. * kPi / 3. * (R * R * R);
           hout.flags |= AHFGPU_HALO_RAN_RVIR1;
