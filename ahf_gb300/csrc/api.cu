@@ -90,7 +90,7 @@ struct Ctx {
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
   DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
-  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql, exlist, excount;
+  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql;
   DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
   // packed results (device)
   DBuf member_off, member, prof_off, prof, phase;
@@ -129,14 +129,20 @@ __global__ void k_scan_counts(const ahfgpu_halo* halo, int64_t nh, int which, ui
   if (threadIdx.x == 0) out[0] = 0;
 }
 
-__global__ void k_pack_members(const ahfgpu_halo* halo, const uint64_t* off, const uint64_t* stage,
-                               const uint64_t* moff, uint64_t* member, int64_t nh) {
-  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t h = warp; h < nh; h += nw) {
-    uint64_t n = halo[h].npart, src = off[h], dst = moff[h];
-    for (uint64_t i = lane; i < n; i += 32) member[dst + i] = stage[src + i];
+// kept ids into the packed CSR list, one output element per thread: the
+// halo of output j is the last h with moff[h] <= j (binary search; the lanes
+// of a warp mostly share it, so the probes are broadcasts)
+__global__ void k_pack_members(const uint64_t* off, const uint64_t* stage, const uint64_t* moff, uint64_t* member,
+                               int64_t nh) {
+  const uint64_t total = moff[nh];
+  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total;
+       j += (uint64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = nh - 1;
+    while (lo < hi) {
+      int64_t mid = (lo + hi + 1) >> 1;
+      if (moff[mid] <= j) lo = mid; else hi = mid - 1;
+    }
+    member[j] = stage[off[lo] + (j - moff[lo])];
   }
 }
 
@@ -253,7 +259,6 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.pa, N * 8); EN(g.pb, N * 8); EN(g.pc, N * 8); EN(g.pd, N * 8);
   EN(g.fdh, N * 4); EN(g.fdl, N * 4); EN(g.fdx, N * 4); EN(g.fdy, N * 4); EN(g.fdz, N * 4);
   EN(g.fdxl, N * 4); EN(g.fdyl, N * 4); EN(g.fdzl, N * 4); EN(g.fqh, N * 4); EN(g.fql, N * 4);
-  EN(g.exlist, std::max<int64_t>(pl.nhalo, 1) * 4); EN(g.excount, 64);
   EN(g.stack, (size_t)nblocks * stack_cap * sizeof(uint4));
   EN(g.halo, std::max<int64_t>(pl.nhalo, 1) * sizeof(ahfgpu_halo));
   EN(g.mem_stage, N * 8);
@@ -366,13 +371,10 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   W.fdx = g.fdx.as<float>(); W.fdy = g.fdy.as<float>(); W.fdz = g.fdz.as<float>();
   W.fdxl = g.fdxl.as<float>(); W.fdyl = g.fdyl.as<float>(); W.fdzl = g.fdzl.as<float>();
   W.fqh = g.fqh.as<float>(); W.fql = g.fql.as<float>();
-  W.exact_list = g.exlist.as<int>();
-  W.exact_count = g.excount.as<unsigned>();
 #ifdef AHFGPU_PHASE_TIMERS
   if ((rc = g.phase.ensure(16 * 8))) return rc;
   W.phase = g.phase.as<unsigned long long>();
 #endif
-  CK(cudaMemsetAsync(g.excount.p, 0, 64, st));
 
   CK(cudaEventRecord(g.ev0, st));
   if (mode == AHFGPU_PLAIN_FP64) {
@@ -407,19 +409,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
       CK(cudaStreamWaitEvent(st, g.ev_join[cls], 0));
       launches++;
     }
-    // haloes whose FP64 re-test stayed inside the rounding band: FP64 form
-    unsigned nex = 0;
-    CK(cudaMemcpyAsync(&nex, g.excount.p, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (nex > 0) {
-      Work W2 = W;
-      W2.queue = g.exlist.as<int32_t>();
-      W2.nqueue = (int)nex;
-      W2.queue_head = g.qhead.as<unsigned int>() + 1;
-      launch_fp64(P, B, W2, std::min<int>(g.nsm * g.fp64_bps, (int)nex), -1, st);
-      launches++;
-    }
-    stats->n_fp64_halos = nex;
+    stats->n_fp64_halos = 0;   // every halo is resolved inside the FP32C kernels
   }
   launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
   launches++;
@@ -429,8 +419,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 0, g.member_off.as<uint64_t>());
   k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 1, g.prof_off.as<uint64_t>());
   int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
-  k_pack_members<<<pg, 256, 0, st>>>(W.halo, db->off, W.mem_stage, g.member_off.as<uint64_t>(),
-                                      g.member.as<uint64_t>(), nh);
+  k_pack_members<<<g.nsm * 8, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(),
+                                             g.member.as<uint64_t>(), nh);
   k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
                                    g.prof.as<double>(), nh);
   launches += 4;
@@ -513,14 +503,17 @@ int ahfgpu_init(int device) {
   return AHFGPU_OK;
 }
 
+static void host_spare_release();
+
 int ahfgpu_shutdown(void) {
+  host_spare_release();
   if (!g.init) return AHFGPU_OK;
   cudaSetDevice(g.device);
   cudaDeviceSynchronize();
   DBuf* bufs[] = {&g.in_off, &g.in_x, &g.in_y, &g.in_z, &g.in_vx, &g.in_vy, &g.in_vz, &g.in_w, &g.in_gidx,
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
-                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.exlist, &g.excount, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
+                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
   for (int k = 0; k < 3; k++) {
@@ -590,6 +583,49 @@ static int copy_in(const ahfgpu_batch* hb, ahfgpu_batch* db, cudaStream_t st) {
   return AHFGPU_OK;
 }
 
+// Result arrays live in page-locked host blocks (device-to-host copies run
+// at link speed instead of through a bounce buffer).  A block handed out in
+// a result comes back on ahfgpu_result_free and is kept for the next fetch.
+struct HostBlock {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+static HostBlock g_spare;                    // one cached block
+static std::vector<HostBlock> g_lent;        // blocks held by results
+
+static void* host_block_get(size_t bytes) {
+  if (g_spare.p && g_spare.cap >= bytes) {
+    g_lent.push_back(g_spare);
+    void* p = g_spare.p;
+    g_spare = HostBlock{};
+    return p;
+  }
+  if (g_spare.p) { cudaFreeHost(g_spare.p); g_spare = HostBlock{}; }
+  void* p = nullptr;
+  size_t cap = bytes + bytes / 8 + 4096;
+  if (cudaMallocHost(&p, cap) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  g_lent.push_back(HostBlock{p, cap});
+  return p;
+}
+
+static void host_spare_release() {
+  if (g_spare.p) cudaFreeHost(g_spare.p);
+  g_spare = HostBlock{};
+}
+
+static bool host_block_put(void* p) {
+  for (size_t i = 0; i < g_lent.size(); i++) {
+    if (g_lent[i].p != p) continue;
+    HostBlock b = g_lent[i];
+    g_lent.erase(g_lent.begin() + (long)i);
+    if (!g_spare.p) g_spare = b;
+    else if (b.cap > g_spare.cap) { cudaFreeHost(g_spare.p); g_spare = b; }
+    else cudaFreeHost(b.p);
+    return true;
+  }
+  return false;
+}
+
 int ahfgpu_fetch_result(ahfgpu_result* r) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -598,14 +634,27 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
   memset(r, 0, sizeof(*r));
   int64_t nh = g.last_nhalo;
   r->nhalo = nh;
-  r->halo = (ahfgpu_halo*)malloc(std::max<int64_t>(nh, 1) * sizeof(ahfgpu_halo));
-  r->member_off = (uint64_t*)malloc((nh + 1) * 8);
-  r->member = (uint64_t*)malloc(std::max<uint64_t>(g.last_nkept, 1) * 8);
-  r->prof_off = (uint64_t*)malloc((nh + 1) * 8);
-  r->prof = (double*)malloc(std::max<uint64_t>(g.last_nbins, 1) * AHFGPU_PROF_NFIELDS * 8);
-  if (!r->halo || !r->member_off || !r->member || !r->prof_off || !r->prof) {
-    ahfgpu_result_free(r);
-    return fail(AHFGPU_ERR_OOM, "host allocation of the result failed");
+  const size_t b_halo = ((size_t)std::max<int64_t>(nh, 1) * sizeof(ahfgpu_halo) + 255) & ~(size_t)255;
+  const size_t b_off = ((size_t)(nh + 1) * 8 + 255) & ~(size_t)255;
+  const size_t b_mem = ((size_t)std::max<uint64_t>(g.last_nkept, 1) * 8 + 255) & ~(size_t)255;
+  const size_t b_prof = (size_t)std::max<uint64_t>(g.last_nbins, 1) * AHFGPU_PROF_NFIELDS * 8;
+  char* blk = (char*)host_block_get(b_halo + 2 * b_off + b_mem + b_prof);
+  if (blk) {
+    r->halo = (ahfgpu_halo*)blk;
+    r->member_off = (uint64_t*)(blk + b_halo);
+    r->prof_off = (uint64_t*)(blk + b_halo + b_off);
+    r->member = (uint64_t*)(blk + b_halo + 2 * b_off);
+    r->prof = (double*)(blk + b_halo + 2 * b_off + b_mem);
+  } else {
+    r->halo = (ahfgpu_halo*)malloc(b_halo);
+    r->member_off = (uint64_t*)malloc(b_off);
+    r->member = (uint64_t*)malloc(b_mem);
+    r->prof_off = (uint64_t*)malloc(b_off);
+    r->prof = (double*)malloc(b_prof);
+    if (!r->halo || !r->member_off || !r->member || !r->prof_off || !r->prof) {
+      ahfgpu_result_free(r);
+      return fail(AHFGPU_ERR_OOM, "host allocation of the result failed");
+    }
   }
   cudaStream_t st = g.stream;
   CK(cudaStreamSynchronize(0));
@@ -645,11 +694,13 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
 
 void ahfgpu_result_free(ahfgpu_result* r) {
   if (!r) return;
-  free(r->halo);
-  free(r->member_off);
-  free(r->member);
-  free(r->prof_off);
-  free(r->prof);
+  if (!(r->halo && host_block_put(r->halo))) {
+    free(r->halo);
+    free(r->member_off);
+    free(r->member);
+    free(r->prof_off);
+    free(r->prof);
+  }
   memset(r, 0, sizeof(*r));
 }
 

@@ -1053,6 +1053,7 @@ struct IterOut {
   ff Mb, Phi0n;
   long long last_slot;
   long long rv_slot;   // first failing kept slot or -1
+  long long rv_cnt;    // kept particles up to and including rv_slot
   ff rv_M, rv_d;
   int amb;
   int rounds;
@@ -1080,7 +1081,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   float cDb[4] = {0.f, 0.f, 0.f, 0.f};
   long long cLs = -1;
   ff cPhiN = ffz();
-  long long rv = -1;
+  long long rv = -1, rvC = 0;
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
@@ -1201,16 +1202,17 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     amb_any |= amb_tile ? 1 : 0;
     // next iteration: potential prefix of the kept particles, rvir1 candidate
     ff accN = ffz(), pn[kItems];
-    long long myfail = 0x7fffffffffffffffll;
+    long long myfail = 0x7fffffffffffffffll, fC = 0;
     ff fM = ffz(), fD = ffz();
     {
-      long long rMb = cM + ex[0];
+      long long rMb = cM + ex[0], rC = cNb + excnt;
       ff dp = {pe[0], pe[1]}, qp = {pe[2], pe[3]};
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
         pn[k] = accN;
         if (!b[k]) continue;
         rMb += fw[k];
+        rC++;
         ff Mb = i2ff(rMb, F.im);
         accN = ff_add(accN, phi_termq(Mb, w[k], d[k], q[k], dp, qp));
         pn[k] = accN;
@@ -1223,6 +1225,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
             myfail = (long long)(i0 + k);
             fM = Mb;
             fD = d[k];
+            fC = rC;
           }
         }
       }
@@ -1240,11 +1243,12 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
       }
     }
     if (rv < 0 && fmin != 0x7fffffffffffffffll) {
-      if (myfail == fmin) { S.bf[0] = fM.hi; S.bf[1] = fM.lo; S.bf[2] = fD.hi; S.bf[3] = fD.lo; }
+      if (myfail == fmin) { S.bf[0] = fM.hi; S.bf[1] = fM.lo; S.bf[2] = fD.hi; S.bf[3] = fD.lo; S.bl[10] = fC; }
       __syncthreads();
       rv = fmin;
       rvM = ff{S.bf[0], S.bf[1]};
       rvD = ff{S.bf[2], S.bf[3]};
+      rvC = S.bl[10];
       __syncthreads();
     }
     if (i0 < n1) {
@@ -1267,6 +1271,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(out.Mb, ff{cDb[0], cDb[1]})) : ffz();
   out.last_slot = cLs;
   out.rv_slot = rv;
+  out.rv_cnt = rvC;
   out.rv_M = rvM;
   out.rv_d = rvD;
   out.amb = __syncthreads_or(amb_any);
@@ -2270,7 +2275,6 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   PT_MARK(W, 3);
   if (threadIdx.x == 0) { hout.M_vir = mo[0]; hout.R_vir = mo[1]; hout.ovdens = mo[2]; hout.Phi0 = 0.0; }
   uint64_t nlist = c.n, ncur = n1;
-  bool to_fp64 = false;
   if (n1 >= (uint64_t)P.MINPART) {
     uint64_t npart = n1;
     uint64_t nremove = 4;
@@ -2321,24 +2325,24 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       it.rv_slot = rvir_pass32(c, B, W, P, S, n1, &Mf, &nret);
       it.rv_M = Mf;
     }
-    if (!to_fp64) {
-      if (threadIdx.x == 0) {
-        hout.flags |= AHFGPU_HALO_RAN_UNBIND;
-        if (nob) hout.flags |= AHFGPU_HALO_NOBOUND;
-        hout.M_vir = M_vir;
-        hout.R_vir = R_vir;
-        hout.Phi0 = last_exact ? Phi0_exact : ff_d(Phi0_used);
-        hout.niter = niter;
-        hout.fix_rounds = maxr;
+    if (threadIdx.x == 0) {
+      hout.flags |= AHFGPU_HALO_RAN_UNBIND;
+      if (nob) hout.flags |= AHFGPU_HALO_NOBOUND;
+      hout.M_vir = M_vir;
+      hout.R_vir = R_vir;
+      hout.Phi0 = last_exact ? Phi0_exact : ff_d(Phi0_used);
+      hout.niter = niter;
+      hout.fix_rounds = maxr;
+    }
+    ncur = npart;
+    nlist = n1;
+    if (npart >= (uint64_t)P.MINPART) {
+      // rem_outsideRvir(.,1): the candidate of the last pass
+      if (it.rv_slot >= 0) {
+        for (uint64_t i = (uint64_t)it.rv_slot + 1 + threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = 0;
+        __syncthreads();
       }
-      ncur = npart;
-      nlist = n1;
-      if (npart >= (uint64_t)P.MINPART) {
-        // rem_outsideRvir(.,1): the candidate of the last pass
-        if (it.rv_slot >= 0) {
-          for (uint64_t i = (uint64_t)it.rv_slot + 1 + threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = 0;
-          __syncthreads();
-        }
+      if (last_exact) {
         int tot = 0, carry = 0;
         for (uint64_t base = 0; base < n1; base += blockDim.x) {
           uint64_t i = base + threadIdx.x;
@@ -2347,37 +2351,28 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
           carry += tot;
         }
         ncur = (uint64_t)carry;
-        if (threadIdx.x == 0) {
-          long long ls = it.rv_slot;
-          if (ls < 0) ls = it.last_slot;
-          double R = ref_dist(c, B, W, c.s + ls);
-          double M = it.rv_slot >= 0 ? ff_d(it.rv_M) : M_vir;
-          double V = 4. * kPi / 3. * (R * R * R);
-          hout.flags |= AHFGPU_HALO_RAN_RVIR1;
-          hout.M_vir = M;
-          hout.R_vir = R;
-          hout.ovdens = M / V * P.rho_fac / P.rho_vir;
-        }
-        __syncthreads();
-        PT_MARK(W, 5);
-        if (ncur >= (uint64_t)P.MINPART) profiles32(c, B, W, P, S, F, n1, ncur, Phi0_used, hout, &nret, par);
-        PT_MARK(W, 6);
+      } else {
+        ncur = it.rv_slot >= 0 ? (uint64_t)it.rv_cnt : npart;
       }
+      if (threadIdx.x == 0) {
+        long long ls = it.rv_slot;
+        if (ls < 0) ls = it.last_slot;
+        double R = ref_dist(c, B, W, c.s + ls);
+        double M = it.rv_slot >= 0 ? ff_d(it.rv_M) : M_vir;
+        double V = 4. * kPi / 3. * (R * R * R);
+        hout.flags |= AHFGPU_HALO_RAN_RVIR1;
+        hout.M_vir = M;
+        hout.R_vir = R;
+        hout.ovdens = M / V * P.rho_fac / P.rho_vir;
+      }
+      __syncthreads();
+      PT_MARK(W, 5);
+      if (ncur >= (uint64_t)P.MINPART) profiles32(c, B, W, P, S, F, n1, ncur, Phi0_used, hout, &nret, par);
+      PT_MARK(W, 6);
     }
   }
   atomicAdd(&nret_s, nret);
   __syncthreads();
-  if (to_fp64) {
-    // the FP64 form resolves this halo in the reference's summation order
-    if (threadIdx.x == 0) {
-      unsigned k = atomicAdd(W.exact_count, 1u);
-      W.exact_list[k] = h;
-      W.halo[h] = hout;
-      atomicAdd(&W.counters[0], (unsigned long long)nret_s);
-    }
-    __syncthreads();
-    return;
-  }
   write_members32(c, nlist, B, W);
   PT_MARK(W, 7);
   if (threadIdx.x == 0) {
