@@ -90,7 +90,7 @@ struct Ctx {
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
   DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
-  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql;
+  DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql, rec;
   DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
   // packed results (device)
   DBuf member_off, member, prof_off, prof, phase;
@@ -259,6 +259,7 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.pa, N * 8); EN(g.pb, N * 8); EN(g.pc, N * 8); EN(g.pd, N * 8);
   EN(g.fdh, N * 4); EN(g.fdl, N * 4); EN(g.fdx, N * 4); EN(g.fdy, N * 4); EN(g.fdz, N * 4);
   EN(g.fdxl, N * 4); EN(g.fdyl, N * 4); EN(g.fdzl, N * 4); EN(g.fqh, N * 4); EN(g.fql, N * 4);
+  EN(g.rec, N * 32);
   EN(g.stack, (size_t)nblocks * stack_cap * sizeof(uint4));
   EN(g.halo, std::max<int64_t>(pl.nhalo, 1) * sizeof(ahfgpu_halo));
   EN(g.mem_stage, N * 8);
@@ -348,6 +349,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
 
   Work W{};
   W.keyA = g.keyA.as<uint64_t>(); W.keyB = g.keyB.as<uint64_t>();
+  W.rec = g.rec.as<float4>();
   W.idxA = g.idxA.as<uint32_t>(); W.idxB = g.idxB.as<uint32_t>();
   W.sdx = g.sdx.as<double>(); W.sdy = g.sdy.as<double>(); W.sdz = g.sdz.as<double>(); W.sd = g.sd.as<double>();
   W.svx = g.svx.as<float>(); W.svy = g.svy.as<float>(); W.svz = g.svz.as<float>(); W.sw = g.sw.as<float>();
@@ -513,7 +515,7 @@ int ahfgpu_shutdown(void) {
   DBuf* bufs[] = {&g.in_off, &g.in_x, &g.in_y, &g.in_z, &g.in_vx, &g.in_vy, &g.in_vz, &g.in_w, &g.in_gidx,
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
-                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
+                  &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.rec, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
   for (int k = 0; k < 3; k++) {

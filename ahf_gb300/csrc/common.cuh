@@ -58,6 +58,7 @@ struct Work {
   float *fdx, *fdy, *fdz; // FP32C: offsets from the centre
   float *fdxl, *fdyl, *fdzl;  // FP32C: low parts of the offsets
   float *fqh, *fql;       // FP32C: 1/d^2 as float-float
+  float4* rec;            // FP32C: per entry {x, y, z, vx} {vy, vz, gidx lo, gidx hi} (two float4)
   uint8_t* flag;          // member (1) / removed (0) per sorted slot
   uint8_t* nflag;         // fixpoint flags of the next round
   double *prof_a, *prof_b, *prof_c, *prof_d;  // per-member profile arrays

@@ -63,10 +63,58 @@ static __device__ void jacobi3(const double ain[3][3], double d[3], double v[3][
   for (int k = 0; k < 3; k++) d[k] = a[k][k];
 }
 
+// the same cyclic Jacobi in FP32 (the FP32-compensated form, whose inertia
+// sums are themselves FP32-accurate): about one sixteenth of the FP64 cost
+static __device__ void jacobi3f(const double ain[3][3], double dout[3], double vout[3][3]) {
+  float a[3][3], v[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) { a[i][j] = (float)ain[i][j]; v[i][j] = (i == j) ? 1.f : 0.f; }
+  for (int sweep = 0; sweep < 32; sweep++) {
+    float off = fabsf(a[0][1]) + fabsf(a[0][2]) + fabsf(a[1][2]);
+    if (off == 0.f) break;
+    for (int pp = 0; pp < 2; pp++) {
+      for (int qq = pp + 1; qq < 3; qq++) {
+        float apq = a[pp][qq];
+        if (apq == 0.f) continue;
+        float app = a[pp][pp], aqq = a[qq][qq];
+        if (sweep > 3 && fabsf(app) + 100.f * fabsf(apq) == fabsf(app) &&
+            fabsf(aqq) + 100.f * fabsf(apq) == fabsf(aqq)) {
+          a[pp][qq] = a[qq][pp] = 0.f;
+          continue;
+        }
+        float tau = (aqq - app) / (2.f * apq);
+        float t = (tau >= 0.f ? 1.f : -1.f) / (fabsf(tau) + sqrtf(1.f + tau * tau));
+        float cs = 1.f / sqrtf(1.f + t * t);
+        float sn = t * cs;
+        for (int k = 0; k < 3; k++) {
+          float akp = a[k][pp], akq = a[k][qq];
+          a[k][pp] = cs * akp - sn * akq;
+          a[k][qq] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < 3; k++) {
+          float apk = a[pp][k], aqk = a[qq][k];
+          a[pp][k] = cs * apk - sn * aqk;
+          a[qq][k] = sn * apk + cs * aqk;
+        }
+        a[pp][qq] = a[qq][pp] = 0.f;
+        for (int k = 0; k < 3; k++) {
+          float vkp = v[k][pp], vkq = v[k][qq];
+          v[k][pp] = cs * vkp - sn * vkq;
+          v[k][qq] = sn * vkp + cs * vkq;
+        }
+      }
+    }
+  }
+  for (int k = 0; k < 3; k++) {
+    dout[k] = (double)a[k][k];
+    for (int j = 0; j < 3; j++) vout[k][j] = (double)v[k][j];
+  }
+}
+
 // get_axes, src/libutility/specific.c:135-178 (own eigen-solver)
-static __device__ void get_axes(double it[3][3], double* a1, double* a2, double* a3) {
+static __device__ void get_axes(double it[3][3], double* a1, double* a2, double* a3, bool f32 = false) {
   double d[3], v[3][3];
-  jacobi3(it, d, v);
+  if (f32) jacobi3f(it, d, v); else jacobi3(it, d, v);
   int ord[3] = {0, 1, 2};
   for (int i = 1; i < 3; i++) {
     int k = ord[i], j = i;
@@ -107,7 +155,9 @@ static __device__ double calc_cR1(double R1) {
 
 // Profile rows of HaloProfiles' per-bin block (ahf_halos.c:4632-4868) from
 // the cumulative bin records; one thread per bin.
-static __device__ void write_bin_rows(const Bin* bins, const double* edge, int nbins, double* rows) {
+// f32eig: FP32 eigen-solver (FP32-compensated form)
+static __device__ void write_bin_rows(const Bin* bins, const double* edge, int nbins, double* rows,
+                                      bool f32eig = false) {
   const double FPT = 4. * kPi / 3.;
   for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
     const Bin& R = bins[b];
@@ -123,7 +173,7 @@ static __device__ void write_bin_rows(const Bin* bins, const double* edge, int n
       it[0][1] = R.a12; it[1][0] = R.a12;
       it[0][2] = R.a13; it[2][0] = R.a13;
       it[1][2] = R.a23; it[2][1] = R.a23;
-      get_axes(it, &ax1, &ax2, &ax3);
+      get_axes(it, &ax1, &ax2, &ax3, f32eig);
     } else {
       for (int x = 0; x < 3; x++)
         for (int y = 0; y < 3; y++) it[x][y] = 0.0;

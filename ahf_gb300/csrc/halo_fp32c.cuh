@@ -664,16 +664,19 @@ static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W, 
   constexpr int G = 4;   // entries in flight per thread
   float vm = 0.f, wx = 0.f, wn = 3.0e38f;
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
-    float px[G], py[G], pz[G], pv[G], pw[G];
+    float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
+    unsigned long long pg[G];
 #pragma unroll
     for (int k = 0; k < G; k++) {
       uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      px[k] = py[k] = pz[k] = pv[k] = 0.f;
+      px[k] = py[k] = pz[k] = pvx[k] = pvy[k] = pvz[k] = 0.f;
       pw[k] = 1.f;
+      pg[k] = 0;
       if (i < c.n) {
         const uint64_t e = c.o + i;
         px[k] = __ldg(B.x + e); py[k] = __ldg(B.y + e); pz[k] = __ldg(B.z + e);
-        pv[k] = fmaxf(fabsf(__ldg(B.vx + e)), fmaxf(fabsf(__ldg(B.vy + e)), fabsf(__ldg(B.vz + e))));
+        pvx[k] = __ldg(B.vx + e); pvy[k] = __ldg(B.vy + e); pvz[k] = __ldg(B.vz + e);
+        pg[k] = B.gidx ? __ldg(reinterpret_cast<const unsigned long long*>(B.gidx) + e) : e;
         if (B.w) pw[k] = __ldg(B.w + e);
       }
     }
@@ -686,7 +689,11 @@ static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W, 
       long long dz = wrapfix(fixp(pz[k]) - c.fz);
       W.keyA[c.s + i] = sqkey(dx, dy, dz);
       W.idxA[c.s + i] = (uint32_t)i;
-      vm = fmaxf(vm, pv[k]);
+      // the entry as one 32-byte record: the gather reads one sector per entry
+      W.rec[2 * (c.s + i)] = make_float4(px[k], py[k], pz[k], pvx[k]);
+      W.rec[2 * (c.s + i) + 1] = make_float4(pvy[k], pvz[k], __uint_as_float((unsigned)pg[k]),
+                                             __uint_as_float((unsigned)(pg[k] >> 32)));
+      vm = fmaxf(vm, fmaxf(fabsf(pvx[k]), fmaxf(fabsf(pvy[k]), fabsf(pvz[k]))));
       wx = fmaxf(wx, pw[k]);
       wn = fminf(wn, pw[k]);
     }
@@ -757,6 +764,7 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
     uint32_t jj[G];
     float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
+    unsigned pgl[G], pgh[G];
 #pragma unroll
     for (int k = 0; k < G; k++) {
       uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
@@ -768,10 +776,11 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
       px[k] = py[k] = pz[k] = pvx[k] = pvy[k] = pvz[k] = 0.f;
       pw[k] = 1.f;
       if (i < c.n) {
-        uint64_t e = c.o + jj[k];
-        px[k] = __ldg(B.x + e); py[k] = __ldg(B.y + e); pz[k] = __ldg(B.z + e);
-        pvx[k] = __ldg(B.vx + e); pvy[k] = __ldg(B.vy + e); pvz[k] = __ldg(B.vz + e);
-        if (B.w) pw[k] = __ldg(B.w + e);
+        float4 r0 = W.rec[2 * (c.s + jj[k])], r1 = W.rec[2 * (c.s + jj[k]) + 1];
+        px[k] = r0.x; py[k] = r0.y; pz[k] = r0.z; pvx[k] = r0.w; pvy[k] = r1.x; pvz[k] = r1.y;
+        pgl[k] = __float_as_uint(r1.z);
+        pgh[k] = __float_as_uint(r1.w);
+        if (B.w) pw[k] = __ldg(B.w + c.o + jj[k]);
       }
     }
 #pragma unroll
@@ -803,6 +812,7 @@ static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W
       W.svz[s] = pvz[k];
       W.sw[s] = pw[k];
       W.seid[s] = jj[k];
+      W.keyB[s] = ((unsigned long long)pgh[k] << 32) | pgl[k];   // output id of the slot
       W.flag[s] = 1;
       fix_w(W)[s] = f2fix(pw[k], F.fm);
       fix_x(W)[s] = wv2fix(pw[k], pvx[k], F.fv, P.has_w);
@@ -1624,30 +1634,30 @@ static __device__ __noinline__ double rank_dist64(const Ctx32& c, const DevBatch
 // j in [0, m), after ns passes of smooth3
 static __device__ __noinline__ double smooth_at64(const Ctx32& c, const DevBatch& B, const Work& W, int which, uint64_t m, int ns,
                               uint64_t i) {
-  double lvl[8][8];
+  double lvl[8][8], dd[9];
   long long lo = (long long)i - ns, hi = (long long)i + ns;
   if (lo < 0) lo = 0;
   if (hi > (long long)m - 1) hi = (long long)m - 1;
   int w = (int)(hi - lo + 1);
-  for (int t = 0; t < w; t++) {
-    uint64_t r = (uint64_t)(lo + t) + kNignore;
-    double dd[2];
-    dd[1] = rank_dist64(c, B, W, r);
-    dd[0] = r > 0 ? rank_dist64(c, B, W, r - 1) : 0.0;
-    lvl[0][t] = raw64(c, B, W, dd, which, r);
+  // reference distances of ranks lo-1 .. hi (each once)
+  for (int t = 0; t <= w; t++) {
+    long long r = lo + t - 1 + kNignore;
+    dd[t] = r >= 0 ? rank_dist64(c, B, W, (uint64_t)r) : 0.0;
   }
+  for (int t = 0; t < w; t++) lvl[0][t] = raw64(c, B, W, &dd[t], which, (uint64_t)(lo + t) + kNignore);
   if (ns == 0 || m < 3) return lvl[0][i - lo];
+  // pass p is needed only within ns - p of i
   for (int p = 1; p <= ns; p++) {
     for (int t = 0; t < w; t++) {
       long long j = lo + t;
+      long long dist = j > (long long)i ? j - (long long)i : (long long)i - j;
+      if (dist > ns - p) continue;
       double v;
       if (j == 0) v = (lvl[p - 1][t] + lvl[p - 1][t + 1]) / 2.;
       else if (j == (long long)m - 1) v = (lvl[p - 1][t] + lvl[p - 1][t - 1]) / 2.;
-      else if (t == 0 || t == w - 1) v = 0.0;   // outside the window of i
       else v = (lvl[p - 1][t - 1] + lvl[p - 1][t] + lvl[p - 1][t + 1]) / 3.;
       lvl[p][t] = v;
     }
-    // the window shrinks by one per pass except at array ends
   }
   return lvl[ns][i - lo];
 }
@@ -1725,7 +1735,8 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   for (int w = 0; w < nw; w++) B32 = fmaxf(B32, S.bf[w]);
   __syncthreads();
   // candidates: within 1e-4 of the FP32 maximum -> FP64 smoothed value
-  float thr = isinf(B32) ? B32 : B32 - 1e-4f * fabsf(B32) - 1e-30f;
+  // (the FP32 values are within ~1e-6 of the FP64 ones)
+  float thr = isinf(B32) ? B32 : B32 - 2e-5f * fabsf(B32) - 1e-30f;
   double bv = -10.0;
   long long bi = -1;
   for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
@@ -1863,14 +1874,21 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   // ranks -> distances (binning_parameter needs them)
   {
     int carry = 0;
-    for (uint64_t base = 0; base < n1; base += blockDim.x) {
-      uint64_t i = base + threadIdx.x;
-      bool mem = i < n1 && (W.flag[o + i] & 1);
+    for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * 4) {
+      const uint64_t i0 = base + (uint64_t)threadIdx.x * 4;
+      unsigned f4 = i0 < n1 ? ld4u8(W.flag + o + i0) : 0u;
+      int cnt = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++) cnt += (i0 + k < n1 && ((f4 >> (8 * k)) & 1u)) ? 1 : 0;
       int tot;
-      int r = block_scan_int(mem ? 1 : 0, &tot, S.iscan) - 1 + carry;
-      if (mem) {
-        Rff[r] = make_float2(W.fdh[o + i], W.fdl[o + i]);
-        ent[r] = W.seid[o + i];
+      int r = block_scan_int(cnt, &tot, S.iscan) - cnt + carry;
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        if (i0 + k < n1 && ((f4 >> (8 * k)) & 1u)) {
+          Rff[r] = make_float2(W.fdh[o + i0 + k], W.fdl[o + i0 + k]);
+          ent[r] = W.seid[o + i0 + k];
+          r++;
+        }
       }
       carry += tot;
     }
@@ -2157,7 +2175,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
 #ifdef AHFGPU_PHASE_TIMERS
   long long _pp = clock64();
 #endif
-  write_bin_rows(S.bins, S.edge, nbins, rows);
+  write_bin_rows(S.bins, S.edge, nbins, rows, true);
   __syncthreads();
 #ifdef AHFGPU_PHASE_TIMERS
   if (threadIdx.x == 0 && W.phase) { long long t = clock64(); atomicAdd(&W.phase[8], (unsigned long long)(t - _pp)); _pp = t; }
@@ -2197,16 +2215,19 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
 
 // ---------------------------------------------------------------------------
 static __device__ void write_members32(const Ctx32& c, uint64_t nlist, const DevBatch& B, const Work& W) {
-  int carry = 0;
   __shared__ int isc[64];
-  for (uint64_t base = 0; base < nlist; base += blockDim.x) {
-    uint64_t i = base + threadIdx.x;
-    bool mem = i < nlist && (W.flag[c.s + i] & 1);
+  int carry = 0;
+  for (uint64_t base = 0; base < nlist; base += (uint64_t)blockDim.x * 4) {
+    const uint64_t i0 = base + (uint64_t)threadIdx.x * 4;
+    unsigned f4 = i0 < nlist ? ld4u8(W.flag + c.s + i0) : 0u;
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) cnt += (i0 + k < nlist && ((f4 >> (8 * k)) & 1u)) ? 1 : 0;
     int tot;
-    int r = block_scan_int(mem ? 1 : 0, &tot, isc) - 1 + carry;
-    if (mem) {
-      uint64_t e = c.o + W.seid[c.s + i];
-      W.mem_stage[c.o + r] = B.gidx ? B.gidx[e] : e;
+    int r = block_scan_int(cnt, &tot, isc) - cnt + carry;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (i0 + k < nlist && ((f4 >> (8 * k)) & 1u)) W.mem_stage[c.o + r++] = W.keyB[c.s + i0 + k];
     }
     carry += tot;
   }
