@@ -318,7 +318,9 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   P.force_serial = 0;
   {
     const char* fe = getenv("AHFGPU_FORCE_EXACT");   // test hook
-    P.force_exact = (fe && fe[0] == '1') ? 1 : 0;
+    // 1: every unbinding iteration in the reference's exact order;
+    // 2 (FP32C): one decision per tile through the exact resolution
+    P.force_exact = (fe && fe[0] == '1') ? 1 : (fe && fe[0] == '2') ? 2 : 0;
   }
   uint64_t launches = 0;
   if (db->w) {
@@ -374,7 +376,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   W.fdxl = g.fdxl.as<float>(); W.fdyl = g.fdyl.as<float>(); W.fdzl = g.fdzl.as<float>();
   W.fqh = g.fqh.as<float>(); W.fql = g.fql.as<float>();
 #ifdef AHFGPU_PHASE_TIMERS
-  if ((rc = g.phase.ensure(16 * 8))) return rc;
+  // 16 phase counters, then per halo {start ns, end ns, SM cycles, SM id}
+  if ((rc = g.phase.ensure((16 + 4 * (size_t)nh) * 8))) return rc;
   W.phase = g.phase.as<unsigned long long>();
 #endif
 
@@ -411,7 +414,6 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
       CK(cudaStreamWaitEvent(st, g.ev_join[cls], 0));
       launches++;
     }
-    stats->n_fp64_halos = 0;   // every halo is resolved inside the FP32C kernels
   }
   launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
   launches++;
@@ -428,11 +430,11 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   launches += 4;
   CK(cudaGetLastError());
   uint64_t tails[2];
-  unsigned long long cnt[3];
+  unsigned long long cnt[4];
   int derr = 0;
   CK(cudaMemcpyAsync(&tails[0], g.member_off.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&tails[1], g.prof_off.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(cnt, g.counters.p, 24, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(cnt, g.counters.p, 32, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(&derr, g.err.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (derr == kErrWorklist) return fail(AHFGPU_ERR_CAPACITY, "radial sort worklist overflow");
@@ -444,6 +446,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t*
   stats->n_retest = cnt[0];
   stats->n_replay_halos = cnt[1];
   stats->n_key_ties = cnt[2];
+  stats->n_fp64_halos = mode == AHFGPU_BATCHED_FP32C ? cnt[3] : 0;
   stats->n_launches = launches;
   g.last_nhalo = nh;
   g.last_nkept = tails[0];
@@ -719,6 +722,13 @@ const char* ahfgpu_version(void) { return "ahfgpu 1.0 (sm_103a)"; }
 
 #ifdef AHFGPU_PHASE_TIMERS
 // instrumented builds: per-phase SM cycles summed over the last call's CTAs
+AHFGPU_API int ahfgpu_debug_halo_times(unsigned long long* out, long long nh) {
+  if (!g.phase.p) return AHFGPU_ERR_STATE;
+  cudaDeviceSynchronize();
+  cudaMemcpy(out, g.phase.as<unsigned long long>() + 16, (size_t)nh * 4 * 8, cudaMemcpyDeviceToHost);
+  return AHFGPU_OK;
+}
+
 AHFGPU_API int ahfgpu_debug_phase(unsigned long long* out, int reset) {
   if (!g.phase.p) return AHFGPU_ERR_STATE;
   cudaDeviceSynchronize();

@@ -74,7 +74,7 @@ struct Work {
   unsigned int* queue_head;
   const int32_t* queue;   // halo indices, largest first
   int nqueue;
-  unsigned long long* counters;  // [0] retest, [1] replay, [2] key ties
+  unsigned long long* counters;  // [0] retest, [1] exact-order haloes, [2] key ties, [3] whole replays
   unsigned long long* phase;     // per-phase SM cycles (instrumented builds only)
   int* err;
 };

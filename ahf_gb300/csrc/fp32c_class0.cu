@@ -6,14 +6,14 @@
 namespace ahfgpu {
 
 void launch_fp32c_class0(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<32, SortSmemT<512, 16>><<<grid, 32, sizeof(F32Smem<SortSmemT<512, 16>>), st>>>(P, B, W);
+  halo_fp32c_kernel<32, SortSmemT<512, 16>><<<grid, 32, sizeof(F32Smem<SortSmemT<512, 16>, 32>), st>>>(P, B, W);
 }
 
 int fp32c_occupancy_class0() {
   int nb = 0;
   cudaFuncSetAttribute(halo_fp32c_kernel<32, SortSmemT<512, 16>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(F32Smem<SortSmemT<512, 16>>));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<32, SortSmemT<512, 16>>, 32, sizeof(F32Smem<SortSmemT<512, 16>>));
+                       (int)sizeof(F32Smem<SortSmemT<512, 16>, 32>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<32, SortSmemT<512, 16>>, 32, sizeof(F32Smem<SortSmemT<512, 16>, 32>));
   return nb;
 }
 

@@ -6,14 +6,14 @@
 namespace ahfgpu {
 
 void launch_fp32c_class1(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<128, SortSmemT<2048, 1024>><<<grid, 128, sizeof(F32Smem<SortSmemT<2048, 1024>>), st>>>(P, B, W);
+  halo_fp32c_kernel<128, SortSmemT<2048, 1024>><<<grid, 128, sizeof(F32Smem<SortSmemT<2048, 1024>, 128>), st>>>(P, B, W);
 }
 
 int fp32c_occupancy_class1() {
   int nb = 0;
   cudaFuncSetAttribute(halo_fp32c_kernel<128, SortSmemT<2048, 1024>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(F32Smem<SortSmemT<2048, 1024>>));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<128, SortSmemT<2048, 1024>>, 128, sizeof(F32Smem<SortSmemT<2048, 1024>>));
+                       (int)sizeof(F32Smem<SortSmemT<2048, 1024>, 128>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<128, SortSmemT<2048, 1024>>, 128, sizeof(F32Smem<SortSmemT<2048, 1024>, 128>));
   return nb;
 }
 

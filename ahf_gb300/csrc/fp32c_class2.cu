@@ -6,14 +6,14 @@
 namespace ahfgpu {
 
 void launch_fp32c_class2(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<256, SortSmemT<2048, 4096>><<<grid, 256, sizeof(F32Smem<SortSmemT<2048, 4096>>), st>>>(P, B, W);
+  halo_fp32c_kernel<256, SortSmemT<2048, 4096>><<<grid, 256, sizeof(F32Smem<SortSmemT<2048, 4096>, 256>), st>>>(P, B, W);
 }
 
 int fp32c_occupancy_class2() {
   int nb = 0;
   cudaFuncSetAttribute(halo_fp32c_kernel<256, SortSmemT<2048, 4096>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(F32Smem<SortSmemT<2048, 4096>>));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<256, SortSmemT<2048, 4096>>, 256, sizeof(F32Smem<SortSmemT<2048, 4096>>));
+                       (int)sizeof(F32Smem<SortSmemT<2048, 4096>, 256>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<256, SortSmemT<2048, 4096>>, 256, sizeof(F32Smem<SortSmemT<2048, 4096>, 256>));
   return nb;
 }
 

@@ -42,9 +42,28 @@ constexpr int kItems = 4;                 // consecutive slots per thread
 constexpr double kEps64 = 1.1102230246251565e-16;
 constexpr float kBand1 = 2e-5f;      // relative band of the FP32 decisions
 
-template <class SS>
+// Per-thread staging of a tile's per-slot inputs (classes with >= 128
+// threads): each thread copies its own four slots of every array with
+// cp.async one tile ahead, into one of two buffers, and reads them back after
+// cp.async.wait_group -- no other thread touches its bytes, so no barrier is
+// needed.  Layout of a buffer: the flags (4 B per thread), eleven 16-byte
+// arrays (w, vx, vy, vz, dx, dy, dz, d hi, d lo, q hi, q lo) and five 32-byte
+// arrays (potential prefix, fixed-point w, vx, vy, vz), each thread-major.
+template <int T>
+struct StageGeo {
+  static constexpr int k16 = T * 4;
+  static constexpr int k32 = k16 + 11 * T * 16;
+  static constexpr int kBuf = k32 + 5 * T * 32;
+};
+
+template <class SS, int T = 256>
 struct F32Smem {
-  SS sort;
+  static constexpr int kT = T;
+  static constexpr int kStage = T >= 128 ? 2 * StageGeo<T>::kBuf : 0;
+  union {
+    SS sort;
+    __align__(16) unsigned char stage[kStage > 0 ? kStage : 16];
+  };
   float scan[32 * 2 * 16];
   uint4 rec[16 * 4];       // two halves of 8 warp records (WRec, 64 bytes each)
   float eup[kMaxBins], edn[kMaxBins];   // float neighbours of the bin edges
@@ -59,6 +78,12 @@ struct F32Smem {
   long long bl[16];
   int bi[16];
   float bf[16];
+  // slots whose FP64 re-test stayed inside the reference-rounding band in the
+  // last unbinding pass, with the flag the pass settled on
+  int amb_n, amb_ovf;
+  long long amb_slot[32];
+  int amb_b[32];
+  double amb_m[32];
 };
 
 struct Ctx32 {
@@ -354,6 +379,13 @@ __device__ __forceinline__ ff i2ff(long long v, float iscale) {
 
 __device__ __forceinline__ float i2f(long long v, float iscale) { return __fmul_rn(l2f(v), iscale); }
 
+// mass prefix as float-float: with unit weights it is the particle count
+// (exact in one float below 2^24), else the fixed-point sum
+__device__ __forceinline__ ff mass_ff(long long fixsum, long long count, int has_w, float iscale) {
+  if (!has_w && count < (1ll << 24)) return ff{(float)count, 0.f};
+  return i2ff(fixsum, iscale);
+}
+
 // Four consecutive slots of a per-slot array.  Halo slot ranges start at a
 // multiple of 4 (slot_base) and tiles at multiples of 4 slots, so every group
 // is 16-byte aligned (8-byte arrays: 32-byte); a group may run up to 3 slots
@@ -369,6 +401,18 @@ __device__ __forceinline__ void ld4ff(const double* p, ff (&v)[4]) {
   v[0] = ff{a.x, a.y}; v[1] = ff{a.z, a.w}; v[2] = ff{b.x, b.y}; v[3] = ff{b.z, b.w};
 }
 __device__ __forceinline__ unsigned ld4u8(const uint8_t* p) { return *reinterpret_cast<const unsigned*>(p); }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 __device__ __forceinline__ void ld4ll(const long long* p, long long (&v)[4]) {
   const longlong2* q = reinterpret_cast<const longlong2*>(p);
   longlong2 a = q[0], b = q[1];
@@ -381,6 +425,60 @@ __device__ __forceinline__ long long* fix_w(const Work& W) { return reinterpret_
 __device__ __forceinline__ long long* fix_x(const Work& W) { return reinterpret_cast<long long*>(W.sdx); }
 __device__ __forceinline__ long long* fix_y(const Work& W) { return reinterpret_cast<long long*>(W.sdy); }
 __device__ __forceinline__ long long* fix_z(const Work& W) { return reinterpret_cast<long long*>(W.sdz); }
+
+// issue the copies of this thread's four slots (i0..i0+3) of a tile into
+// stage buffer `buf`; always commits one group (empty past the list end)
+template <class SM>
+__device__ __forceinline__ void stage_issue(SM& S, int buf, const Work& W, uint64_t o, uint64_t i0, uint64_t n1,
+                                            int has_w) {
+  using G = StageGeo<SM::kT>;
+  constexpr int T = SM::kT;
+  unsigned char* b = S.stage + buf * G::kBuf;
+  const int t = threadIdx.x;
+  if (i0 < n1) {
+    const uint64_t s = o + i0;
+    cp_async4(b + t * 4, W.flag + s);
+    const float* a16[11] = {W.sw, W.svx, W.svy, W.svz, W.fdx, W.fdy, W.fdz, W.fdh, W.fdl, W.fqh, W.fql};
+#pragma unroll
+    for (int a = 0; a < 11; a++) {
+      if (a == 0 && !has_w) continue;
+      cp_async16(b + G::k16 + a * T * 16 + t * 16, a16[a] + s);
+    }
+    const unsigned char* a32[5] = {reinterpret_cast<const unsigned char*>(W.phi + s),
+                                   reinterpret_cast<const unsigned char*>(fix_w(W) + s),
+                                   reinterpret_cast<const unsigned char*>(fix_x(W) + s),
+                                   reinterpret_cast<const unsigned char*>(fix_y(W) + s),
+                                   reinterpret_cast<const unsigned char*>(fix_z(W) + s)};
+#pragma unroll
+    for (int a = 0; a < 5; a++) {
+      if (a == 1 && !has_w) continue;
+      cp_async16(b + G::k32 + a * T * 32 + t * 32, a32[a]);
+      cp_async16(b + G::k32 + a * T * 32 + t * 32 + 16, a32[a] + 16);
+    }
+  }
+  cp_async_commit();
+}
+
+template <class SM>
+__device__ __forceinline__ const unsigned char* stage_buf(SM& S, int buf) {
+  return S.stage + buf * StageGeo<SM::kT>::kBuf;
+}
+template <class SM>
+__device__ __forceinline__ void st_f(const unsigned char* b, int a, float (&v)[4]) {
+  ld4f(reinterpret_cast<const float*>(b + StageGeo<SM::kT>::k16 + a * SM::kT * 16 + threadIdx.x * 16), v);
+}
+template <class SM>
+__device__ __forceinline__ void st_ll(const unsigned char* b, int a, long long (&v)[4]) {
+  ld4ll(reinterpret_cast<const long long*>(b + StageGeo<SM::kT>::k32 + a * SM::kT * 32 + threadIdx.x * 32), v);
+}
+template <class SM>
+__device__ __forceinline__ void st_ff(const unsigned char* b, int a, ff (&v)[4]) {
+  ld4ff(reinterpret_cast<const double*>(b + StageGeo<SM::kT>::k32 + a * SM::kT * 32 + threadIdx.x * 32), v);
+}
+template <class SM>
+__device__ __forceinline__ unsigned st_flag(const unsigned char* b) {
+  return *reinterpret_cast<const unsigned*>(b + threadIdx.x * 4);
+}
 
 // per-halo scales from the list length and the largest weight / velocity
 __device__ __forceinline__ Fix make_fix(uint64_t n, float wmax, float wmin, float vmax, double v_fac) {
@@ -859,6 +957,18 @@ __device__ __forceinline__ ff phi_termq(ff M, float w, ff d, ff q, ff dp, ff qp)
   return ff_mul(Im, ff_sub(d, dp));
 }
 
+// the same with the mass prefixes exact floats (unit weights: particle
+// counts M and M - 1)
+__device__ __forceinline__ ff phi_termq_c(float M, float Mp, ff d, ff q, ff dp, ff qp) {
+  if (!dpos(d)) return ffz();
+  ff In = ff_mulf(q, M);
+  ff Ip = dpos(dp) ? ff_mulf(qp, Mp) : ffz();
+  ff Im = ff_add(In, Ip);
+  Im.hi = __fmul_rn(Im.hi, 0.5f);
+  Im.lo = __fmul_rn(Im.lo, 0.5f);
+  return ff_mul(Im, ff_sub(d, dp));
+}
+
 // FP32 overdensity test with band; FP64 re-test inside the band.  Returns
 // fail (ovdens < ovlim).  M: mass prefix, d: distance (float-float).
 static __device__ __noinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
@@ -927,10 +1037,14 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
     for (int k = 0; k < kItems; k++) {
       uint64_t i = i0 + k;
       rM += fw[k];
-      Mk[k] = i2ff(rM, F.im);
+      Mk[k] = mass_ff(rM, (long long)(i + 1), P.has_w, F.im);
       ff prevd = k == 0 ? dp : d[k - 1];
       ff prevq = k == 0 ? qp : q[k - 1];
-      if (i < c.n) accT = ff_add(accT, phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq));
+      if (i < c.n) {
+        const bool cnt_mass = !P.has_w && i + 1 < (1ull << 24);
+        accT = ff_add(accT, cnt_mass ? phi_termq_c((float)(i + 1), (float)i, d[k], q[k], prevd, prevq)
+                                     : phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq));
+      }
       term[k] = accT;     // thread-local inclusive
       if (i < c.n && myfail == 0x7fffffffffffffffll) {
         float rhs = __fmul_rn(ovk, __fmul_rn(__fmul_rn(d[k].hi, d[k].hi), d[k].hi));
@@ -1095,10 +1209,14 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   ff rvM = ffz(), rvD = ffz();
   int amb_any = 0, maxr = 0;
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
-  for (uint64_t base = 0; base < n1; base += tile) {
+  if (threadIdx.x == 0) { S.amb_n = 0; S.amb_ovf = P.force_exact == 1 ? 1 : 0; }
+  __syncthreads();
+  if (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
+  int tix = 0;
+  for (uint64_t base = 0; base < n1; base += tile, tix++) {
     PT_T0;
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
-    bool m[kItems], b[kItems];
+    bool m[kItems], b[kItems], ambk[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems], thr[kItems];
     ff d[kItems], q[kItems];
     long long fw[kItems], fx[kItems], fy[kItems], fz[kItems];
@@ -1114,7 +1232,21 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
       }
 #pragma unroll
       for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
-      if (i0 < n1) {
+      if (SM::kStage > 0) {
+        // this tile's inputs were copied one tile ago; start the next tile's
+        stage_issue(S, (tix & 1) ^ 1, W, o, i0 + tile, n1, has_w);
+        cp_async_wait<1>();
+        if (i0 < n1) {
+          const unsigned char* sb = stage_buf(S, tix & 1);
+          f4 = st_flag<SM>(sb);
+          if (has_w) { st_f<SM>(sb, 0, w); st_ll<SM>(sb, 1, fw); }
+          st_f<SM>(sb, 1, vx); st_f<SM>(sb, 2, vy); st_f<SM>(sb, 3, vz);
+          st_f<SM>(sb, 4, dx); st_f<SM>(sb, 5, dy); st_f<SM>(sb, 6, dz);
+          st_f<SM>(sb, 7, dh); st_f<SM>(sb, 8, dl); st_f<SM>(sb, 9, qh); st_f<SM>(sb, 10, ql);
+          st_ff<SM>(sb, 0, ph);
+          st_ll<SM>(sb, 2, fx); st_ll<SM>(sb, 3, fy); st_ll<SM>(sb, 4, fz);
+        }
+      } else if (i0 < n1) {
         f4 = ld4u8(W.flag + o + i0);
         if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
         ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
@@ -1160,6 +1292,8 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     long long pslot, pbslot;
     int rounds = 0;
     bool amb_tile = false;
+#pragma unroll
+    for (int k = 0; k < kItems; k++) ambk[k] = false;
     while (true) {
       rounds++;
       long long a[4] = {0, 0, 0, 0};
@@ -1186,13 +1320,14 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
         nb[k] = b[k];
         if (m[k]) {
           int r = bound32(vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], thr[k], ethr, rM, rX, rY, rZ, F, vf, Hr);
+          ambk[k] = false;
           if (r < 0) {
             (*nret)++;
             bool amb = false;
             float2 ph = phs[i0 + k];
             r = retest_bound(c, B, W, P, o + i0 + k, i0 + k, n1, ff_d(ff{ph.x, ph.y}), phi0d, (double)rX * F.dv,
                              (double)rY * F.dv, (double)rZ * F.dv, (double)rM * F.dm, vmax, F.vq, &amb) ? 1 : 0;
-            if (amb) amb_tile = true;
+            ambk[k] = amb;
           }
           nb[k] = r != 0;
           if (nb[k] != b[k]) changed = 1;
@@ -1208,7 +1343,23 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     PT_ADD(W, 14, rounds);
     PT_ADD(W, 15, 1);
     if (rounds > maxr) maxr = rounds;
-    if (P.force_exact) amb_tile = true;
+    if (amb_tile) S.amb_ovf = 1;   // fixpoint cap reached
+    // test hook 2: the first member of each of the first 16 tiles is treated
+    // as ambiguous
+    if (P.force_exact == 2 && i0 == base && tix < 16) {
+#pragma unroll
+      for (int k = 0; k < kItems; k++)
+        if (m[k]) { ambk[k] = true; break; }
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; k++) {
+      if (!ambk[k]) continue;
+      amb_tile = true;
+      int q = atomicAdd(&S.amb_n, 1);
+      if (q < 32) { S.amb_slot[q] = (long long)(i0 + k); S.amb_b[q] = b[k] ? 1 : 0; }
+      else S.amb_ovf = 1;
+    }
+    if (P.force_exact == 1) amb_tile = true;
     amb_any |= amb_tile ? 1 : 0;
     // next iteration: potential prefix of the kept particles, rvir1 candidate
     ff accN = ffz(), pn[kItems];
@@ -1223,8 +1374,10 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
         if (!b[k]) continue;
         rMb += fw[k];
         rC++;
-        ff Mb = i2ff(rMb, F.im);
-        accN = ff_add(accN, phi_termq(Mb, w[k], d[k], q[k], dp, qp));
+        ff Mb = mass_ff(rMb, rC, has_w, F.im);
+        const bool cnt_mass = !has_w && rC < (1ll << 24);
+        accN = ff_add(accN, cnt_mass ? phi_termq_c((float)rC, (float)(rC - 1), d[k], q[k], dp, qp)
+                                     : phi_termq(Mb, w[k], d[k], q[k], dp, qp));
         pn[k] = accN;
         dp = d[k];
         qp = q[k];
@@ -1276,6 +1429,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     for (int j = 0; j < 4; j++) cDb[j] = pb[j];
     cLs = pbslot;
   }
+  if (SM::kStage > 0) cp_async_wait<0>();
   out.nb = cNb;
   out.Mb = i2ff(cM, F.im);
   out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(out.Mb, ff{cDb[0], cDb[1]})) : ffz();
@@ -1312,21 +1466,21 @@ static __device__ double chain64(const double* a, double* out, uint64_t n, doubl
   return s;
 }
 
-// One rem_unbound iteration in the reference's exact summation order, for a
-// pass whose FP64 re-test stayed inside the rounding band.  Members: flag
-// bit0 of [0, n1); bit1 = speculated bound flags on entry, exact on exit.
-// Per-member distances and offsets are recomputed in FP64 from the inputs
-// exactly as the reference computes them; the order-dependent sums are warp
-// chains.  Returns kept count/mass, last kept slot.
+// FP64 potential prefix of the exact paths: the sort-key array, free after
+// the gather (the stored float-float prefix in phi stays intact)
+__device__ __forceinline__ double* exact_term(const Work& W, uint64_t o) {
+  return reinterpret_cast<double*>(W.keyA) + o;
+}
+
+// The Phi0 pass of rem_unbound (ahf_halos.c:3343-3426) over the members of
+// [0, n1) in the reference's exact order: per-member FP64 distances d64 and
+// the potential prefix (inclusive, sequential FP64 sums) in term; returns
+// Phi0.
 template <class SM>
-static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
-                             uint64_t n1, uint64_t js, long long* nb_out, double* mb_out, long long* last_out) {
+static __device__ double exact_potential(const Ctx32& c, const DevBatch& B, const Work& W, SM& S, uint64_t n1) {
   const uint64_t o = c.s;
-  double* term = W.phi + o;
+  double* term = exact_term(W, o);
   double* d64 = W.prof_a + o;
-  double* ax = W.prof_b + o;
-  double* ay = W.prof_c + o;
-  double* az = W.prof_d + o;
   double* dsm = reinterpret_cast<double*>(S.scan);
   double carryM = 0.0, carryD = 0.0;
   for (uint64_t base = 0; base < n1; base += blockDim.x) {
@@ -1359,6 +1513,136 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
   }
   __syncthreads();
   const double Phi0 = S.bd[20] + carryM / carryD;
+  __syncthreads();
+  return Phi0;
+}
+
+// The bound test of one member in the reference's operation order
+// (ahf_halos.c:3528-3561) from exact potential and running sums.
+static __device__ __noinline__ bool exact_bound(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P,
+                                                uint64_t j, double phi, double Phi0, double d, double VXc, double VYc,
+                                                double VZc, double M_vel) {
+  const uint64_t o = c.s;
+  uint64_t e = c.o + W.seid[o + j];
+  double dX = wrap_s((double)B.x[e] - c.cx), dY = wrap_s((double)B.y[e] - c.cy), dZ = wrap_s((double)B.z[e] - c.cz);
+  double v_esc2 = d > kMachineZero ? (2 * fabs(phi - Phi0) * P.phi_fac) : 1e30;
+  double VXp = (double)W.svx[o + j], VYp = (double)W.svy[o + j], VZp = (double)W.svz[o + j];
+  double dVX = (VXp - VXc / M_vel) * P.v_fac + P.Hubble * (dX) * P.r_fac;
+  double dVY = (VYp - VYc / M_vel) * P.v_fac + P.Hubble * (dY) * P.r_fac;
+  double dVZ = (VZp - VZc / M_vel) * P.v_fac + P.Hubble * (dZ) * P.r_fac;
+  double vel2 = (dVX * dVX + dVY * dVY) + dVZ * dVZ;
+  return !(vel2 > P.v2_tune * v_esc2);
+}
+
+// Exact resolution of the decisions an unbinding pass left inside the
+// reference-rounding band (recorded in S.amb_*): the potential in the
+// reference's order over all members, the bound-only momentum chains up to
+// the last recorded slot, the bound mass before each.  Every other decision
+// of the pass already equals the reference's (its band is rigorous), so when
+// each recorded decision stands the pass's flags are the reference's: returns
+// true.  false: some decision differs, the iteration goes through
+// exact_iter32.
+template <class SM>
+static __device__ bool exact_resolve(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                                     uint64_t n1, uint64_t js) {
+  __syncthreads();
+  if (S.amb_ovf || S.amb_n <= 0) return false;
+  const int na = S.amb_n < 32 ? S.amb_n : 32;
+  const uint64_t o = c.s;
+  const double Phi0 = exact_potential(c, B, W, S, n1);
+  // recorded slots in ascending order (thread 0; at most 32)
+  if (threadIdx.x == 0) {
+    for (int a = 1; a < na; a++) {
+      long long ks = S.amb_slot[a];
+      int kb = S.amb_b[a], q = a;
+      while (q > 0 && S.amb_slot[q - 1] > ks) { S.amb_slot[q] = S.amb_slot[q - 1]; S.amb_b[q] = S.amb_b[q - 1]; q--; }
+      S.amb_slot[q] = ks;
+      S.amb_b[q] = kb;
+    }
+  }
+  __syncthreads();
+  const uint64_t nl = (uint64_t)S.amb_slot[na - 1] + 1;
+  double* ax = W.prof_b + o;
+  double* ay = W.prof_c + o;
+  double* az = W.prof_d + o;
+  double* dsm = reinterpret_cast<double*>(S.scan);
+  const double w0 = (double)W.sw[o + js];
+  const double sVX = w0 * (double)W.svx[o + js], sVY = w0 * (double)W.svy[o + js], sVZ = w0 * (double)W.svz[o + js];
+  for (uint64_t i = threadIdx.x; i < nl; i += blockDim.x) {
+    uint8_t f = W.flag[o + i];
+    bool b = (f & 1) && ((f >> 1) & 1);
+    double w = b ? (double)W.sw[o + i] : 0.0;
+    ax[i] = b ? w * (double)W.svx[o + i] : 0.0;
+    ay[i] = b ? w * (double)W.svy[o + i] : 0.0;
+    az[i] = b ? w * (double)W.svz[o + i] : 0.0;
+  }
+  __syncthreads();
+  {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    if (nwarps >= 3) {
+      if (warp == 0) chain64(ax, ax, nl, sVX, 0);
+      else if (warp == 1) chain64(ay, ay, nl, sVY, 0);
+      else if (warp == 2) chain64(az, az, nl, sVZ, 0);
+    } else if (warp == 0) {
+      chain64(ax, ax, nl, sVX, 0);
+      chain64(ay, ay, nl, sVY, 0);
+      chain64(az, az, nl, sVZ, 0);
+    }
+  }
+  __syncthreads();
+  // bound mass before each recorded slot: FP64 sums of the weights are exact
+  // (checked on the host), so block sums over the segments between slots
+  double Mrun = w0;
+  uint64_t lo = 0;
+  for (int a = 0; a < na; a++) {
+    const uint64_t hi = (uint64_t)S.amb_slot[a];
+    double part = 0.0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      uint8_t f = W.flag[o + i];
+      if ((f & 1) && ((f >> 1) & 1)) part += (double)W.sw[o + i];
+    }
+    double v[1] = {part}, tot[1];
+    block_scan<1>(v, tot, dsm);
+    Mrun += tot[0];
+    if (threadIdx.x == 0) S.amb_m[a] = Mrun;
+    lo = hi;
+  }
+  __syncthreads();
+  int bad = 0;
+  if ((int)threadIdx.x < na) {
+    const int a = threadIdx.x;
+    const uint64_t j = (uint64_t)S.amb_slot[a];
+    const double* term = exact_term(W, o);
+    const double* d64 = W.prof_a + o;
+    bool nbv = exact_bound(c, B, W, P, j, term[j], Phi0, d64[j], ax[j], ay[j], az[j], S.amb_m[a]);
+    if ((nbv ? 1 : 0) != S.amb_b[a]) bad = 1;
+#ifdef AHFGPU_DEBUG_RESOLVE
+    if ((nbv ? 1 : 0) != S.amb_b[a])
+      printf("resolve mismatch h %d slot %lld of n1 %llu: exact %d pass %d phi %.17g Phi0 %.17g d %.17g V %.17g M %.17g\n", c.h,
+             (long long)j, (unsigned long long)n1, (int)nbv, S.amb_b[a], term[j], Phi0, d64[j], ax[j], S.amb_m[a]);
+#endif
+  }
+  return !__syncthreads_or(bad);
+}
+
+// One rem_unbound iteration in the reference's exact summation order, for a
+// pass whose FP64 re-test stayed inside the rounding band and whose
+// ambiguous decision changed.  Members: flag bit0 of [0, n1); bit1 =
+// speculated bound flags on entry, exact on exit.  Per-member distances and
+// offsets are recomputed in FP64 from the inputs exactly as the reference
+// computes them; the order-dependent sums are warp chains.  Returns kept
+// count/mass, last kept slot.
+template <class SM>
+static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
+                             uint64_t n1, uint64_t js, long long* nb_out, double* mb_out, long long* last_out) {
+  const uint64_t o = c.s;
+  double* term = exact_term(W, o);
+  double* d64 = W.prof_a + o;
+  double* ax = W.prof_b + o;
+  double* ay = W.prof_c + o;
+  double* az = W.prof_d + o;
+  double* dsm = reinterpret_cast<double*>(S.scan);
+  const double Phi0 = exact_potential(c, B, W, S, n1);
   const double w0 = (double)W.sw[o + js];
   const double sVX = w0 * (double)W.svx[o + js], sVY = w0 * (double)W.svy[o + js], sVZ = w0 * (double)W.svz[o + js];
   long long nb = 0, last = -1;
@@ -1734,9 +2018,24 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   float B32 = -10.f;
   for (int w = 0; w < nw; w++) B32 = fmaxf(B32, S.bf[w]);
   __syncthreads();
-  // candidates: within 1e-4 of the FP32 maximum -> FP64 smoothed value
-  // (the FP32 values are within ~1e-6 of the FP64 ones)
+  // candidates: within 2e-5 of the FP32 maximum (the FP32 values are within
+  // ~1e-6 of the FP64 ones).  A single candidate is the maximum; several
+  // are decided on their FP64 smoothed values.
   float thr = isinf(B32) ? B32 : B32 - 2e-5f * fabsf(B32) - 1e-30f;
+  int ncand = 0;
+  long long first = -1;
+  for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
+    if (sv[i] >= thr) {
+      if (first < 0) first = (long long)i;
+      ncand++;
+    }
+  }
+  const int multi = __syncthreads_or(ncand > 1 ? 1 : 0);
+  const int nthr = __syncthreads_count(ncand > 0 ? 1 : 0);
+  if (!multi && nthr <= 1) {
+    long long f = -bmin_ll(-first, S);
+    return f < 0 ? m - 1 : (uint64_t)f;
+  }
   double bv = -10.0;
   long long bi = -1;
   for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
@@ -1940,7 +2239,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   double Ebest = 1e30;
   long long Eslot = -1;
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
-  for (uint64_t base = 0; base < n1; base += tile) {
+  if (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
+  int tix = 0;
+  for (uint64_t base = 0; base < n1; base += tile, tix++) {
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
     bool m[kItems];
     float w[kItems], vx[kItems], vy[kItems], vz[kItems], dx[kItems], dy[kItems], dz[kItems];
@@ -1963,7 +2264,21 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       }
 #pragma unroll
       for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
-      if (i0 < n1) {
+      if (SM::kStage > 0) {
+        stage_issue(S, (tix & 1) ^ 1, W, o, i0 + tile, n1, has_w);
+        if (i0 < n1) { ld4f(W.fdxl + o + i0, dxl); ld4f(W.fdyl + o + i0, dyl); ld4f(W.fdzl + o + i0, dzl); }
+        cp_async_wait<1>();
+        if (i0 < n1) {
+          const unsigned char* sb = stage_buf(S, tix & 1);
+          f4 = st_flag<SM>(sb);
+          if (has_w) { st_f<SM>(sb, 0, w); st_ll<SM>(sb, 1, fw); }
+          st_f<SM>(sb, 1, vx); st_f<SM>(sb, 2, vy); st_f<SM>(sb, 3, vz);
+          st_f<SM>(sb, 4, dx); st_f<SM>(sb, 5, dy); st_f<SM>(sb, 6, dz);
+          st_f<SM>(sb, 7, dh); st_f<SM>(sb, 8, dl); st_f<SM>(sb, 9, qh); st_f<SM>(sb, 10, ql);
+          st_ff<SM>(sb, 0, phi);
+          st_ll<SM>(sb, 2, fx); st_ll<SM>(sb, 3, fy); st_ll<SM>(sb, 4, fz);
+        }
+      } else if (i0 < n1) {
         f4 = ld4u8(W.flag + o + i0);
         if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
         ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
@@ -2016,7 +2331,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         Mk[k] = ffz();
         if (!m[k]) continue;
         rM += fw[k]; rX += fx[k]; rY += fy[k]; rZ += fz[k];
-        ff M = i2ff(rM, F.im);
+        ff M = mass_ff(rM, (long long)r + 1, has_w, F.im);
         Mk[k] = M;
         PTerms t;
         pterms(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], M, i2ff(rX, F.iv),
@@ -2171,6 +2486,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     cr += tn;
     __syncthreads();
   }
+  if (SM::kStage > 0) cp_async_wait<0>();
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
 #ifdef AHFGPU_PHASE_TIMERS
   long long _pp = clock64();
@@ -2193,7 +2509,12 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     uint64_t lo = 0, hi = n2 - 1;
     while (lo < hi) {
       uint64_t mid = (lo + hi) / 2;
-      if (rank_dist64(c, B, W, mid) < x_max) lo = mid + 1; else hi = mid;
+      // float-float radius of the rank (48 bits of the exact distance);
+      // the reference's FP64 distance only when the two are that close
+      const float2* Rr = reinterpret_cast<const float2*>(W.prof_a + c.s);
+      double rf = (double)Rr[mid].x + (double)Rr[mid].y;
+      bool below = fabs(rf - x_max) > 1e-13 * x_max ? rf < x_max : rank_dist64(c, B, W, mid) < x_max;
+      if (below) lo = mid + 1; else hi = mid;
     }
     uint64_t ib = lo;
     double rb = rank_dist64(c, B, W, ib);
@@ -2249,10 +2570,9 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   __shared__ ahfgpu_halo hout;
   __shared__ unsigned nret_s;
   if (threadIdx.x == 0) {
-    char* p = (char*)&hout;
-    for (unsigned k = 0; k < sizeof(ahfgpu_halo); k++) p[k] = 0;
     nret_s = 0;
   }
+  for (unsigned k = threadIdx.x; k < sizeof(ahfgpu_halo) / 8; k += blockDim.x) reinterpret_cast<uint64_t*>(&hout)[k] = 0;
   __syncthreads();
   unsigned nret = 0;
   if (c.n == 0) {
@@ -2270,6 +2590,11 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     return;
   }
   PT_BEGIN;
+#ifdef AHFGPU_PHASE_TIMERS
+  unsigned long long _g0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(_g0));
+  const long long _c0 = clock64();
+#endif
   float lim[3];
   keys32(c, B, W, P, S, lim);
   PT_MARK(W, 0);
@@ -2299,7 +2624,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   if (n1 >= (uint64_t)P.MINPART) {
     uint64_t npart = n1;
     uint64_t nremove = 4;
-    int niter = 0, maxr = 0, nob = 0;
+    int niter = 0, maxr = 0, nob = 0, nfull = 0;
     double R_vir = 0.0, M_vir = 0.0, Phi0_exact = 0.0;
     ff Phi0_used = Phi0;
     IterOut it;
@@ -2310,10 +2635,16 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       uint64_t js = seed_slot(c, W, P, niter, n1, S);
       Phi0_used = Phi0;
       unbind_pass(c, B, W, P, S, F, n1, Phi0, js, vmax, it, &nret, par);
-      last_exact = it.amb != 0;
+      last_exact = false;
+      if (it.amb != 0) {
+        // a bound decision inside the reference's rounding band: decide it in
+        // the reference's exact summation order; if it differs from the
+        // pass's, redo the whole iteration in that order
+        nexact++;
+        last_exact = !exact_resolve(c, B, W, P, S, n1, js);
+      }
       if (last_exact) {
-        // a bound decision inside the reference's rounding band: redo this
-        // iteration in the reference's exact summation order
+        nfull++;
         long long nbx, lsx;
         double mbx;
         exact_iter32(c, B, W, P, S, n1, js, &nbx, &mbx, &lsx);
@@ -2322,7 +2653,6 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
         it.nb = nbx;
         it.Mb = ff_from_d(mbx);
         it.last_slot = lsx;
-        nexact++;
       }
       // members <- bound
       for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = (W.flag[c.s + i] >> 1) & 1;
@@ -2336,6 +2666,7 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
       Phi0 = last_exact ? (npart > 0 ? phi0_pass32(c, W, P, S, F, n1, par) : ffz()) : it.Phi0n;
       if (((double)npart) < ((double)P.MINPART)) break;
     }
+    if (nfull && threadIdx.x == 0) atomicAdd(&W.counters[3], 1ull);
     if (nexact && threadIdx.x == 0) {
       atomicAdd(&W.counters[1], 1ull);
       hout.flags |= AHFGPU_HALO_REPLAYED;
@@ -2396,6 +2727,18 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   __syncthreads();
   write_members32(c, nlist, B, W);
   PT_MARK(W, 7);
+#ifdef AHFGPU_PHASE_TIMERS
+  if (threadIdx.x == 0 && W.phase) {
+    unsigned long long g1;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    W.phase[16 + 4 * h] = _g0;
+    W.phase[16 + 4 * h + 1] = g1;
+    W.phase[16 + 4 * h + 2] = (unsigned long long)(clock64() - _c0);
+    W.phase[16 + 4 * h + 3] = smid;
+  }
+#endif
   if (threadIdx.x == 0) {
     hout.npart = ncur;
     W.halo[h] = hout;
@@ -2404,10 +2747,12 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   __syncthreads();
 }
 
+static_assert(sizeof(ahfgpu_halo) % 8 == 0, "the halo record is cleared in 8-byte words");
+
 template <int T, class SS>
 __global__ void __launch_bounds__(T) halo_fp32c_kernel(DevParams P, DevBatch B, Work W) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  using SM = F32Smem<SS>;
+  using SM = F32Smem<SS, T>;
   SM& S = *reinterpret_cast<SM*>(smem_raw);
   uint4* stack = W.sort_stack + (uint64_t)blockIdx.x * W.stack_cap;
   while (true) {

@@ -148,7 +148,8 @@ typedef struct {
   uint64_t n_retest;         /* particles routed to the FP64 re-test          */
   uint64_t n_replay_halos;   /* halos finished by the exact sequential replay */
   uint64_t n_key_ties;       /* equal radial keys met by the sort             */
-  uint64_t n_fp64_halos;     /* FP32C: haloes finished by the FP64 form       */
+  uint64_t n_fp64_halos;     /* FP32C: haloes with an unbinding iteration
+                                replayed whole in the reference's FP64 order */
   uint64_t n_launches;       /* kernels launched by the call                  */
   double   ms_device;        /* device time of the compute kernels (ms)       */
   double   ms_total;         /* wall time of the whole call (ms)              */

@@ -158,3 +158,30 @@ def test_fp32c_matches_oracle(gpu, oracle_built, case):
     got = gpu.construct_halos(params, L, "batched_fp32c")
     bad = compare_fp32c(got, exp)
     assert not bad, bad
+
+
+@pytest.mark.parametrize("hook", ["1", "2"])
+def test_fp32c_exact_paths_match_oracle(gpu, oracle_built, monkeypatch, hook):
+    """The FP32C exact paths taken when an FP64 re-test falls inside the
+    reference-rounding band: hook 1 replays every unbinding iteration in the
+    reference's order (exact_iter32); hook 2 sends one decision per tile
+    through the exact resolution (exact potential and momentum chains, the
+    decision re-made in FP64).  Kept lists identical to the reference's."""
+    for name, kw in (("cfg1", {}), ("cfg3", dict(scale=0.002, max_particles=60000)),
+                     ("cfg3", dict(scale=0.002, max_particles=60000, multimass=True))):
+        params, L = _synthetic(name, **kw)
+        exp = oracle_built.run_oracle(params, L, 0)
+        monkeypatch.delenv("AHFGPU_FORCE_EXACT", raising=False)
+        plain = gpu.construct_halos(params, L, "batched_fp32c")
+        monkeypatch.setenv("AHFGPU_FORCE_EXACT", hook)
+        got = gpu.construct_halos(params, L, "batched_fp32c")
+        bad = compare_fp32c(got, exp)
+        assert not bad, (name, kw, bad)
+        assert got.stats["n_replay_halos"] > 0
+        if hook == "1":
+            assert got.stats["n_fp64_halos"] > 0
+        else:
+            # the extra recorded decisions were certain ones: the exact
+            # resolution confirms each, so no more iterations are replayed
+            # whole than without the hook
+            assert got.stats["n_fp64_halos"] == plain.stats["n_fp64_halos"]
