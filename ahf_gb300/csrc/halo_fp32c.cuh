@@ -2236,8 +2236,17 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   for (int j = 0; j < 11; j++) cgc[j] = ffz();
   float cD[4] = {0.f, 0.f, 0.f, 0.f};
   int cr = 0;
-  double Ebest = 1e30;
-  long long Eslot = -1;
+  // per-thread sums of the channels needed only at bin ends, folded into the
+  // uniform carries (cf, cU, cgc) at the next tile with a bin end: tiles
+  // without one need no block reduction
+  ff pacc[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) pacc[j] = ffz();
+  // most bound particle, per thread: the warp's running FP32 minimum as the
+  // screen, FP64 energies of the candidates; one block reduction at the end
+  float pEmin = 3.0e38f;
+  double pEbest = 1e300;
+  long long pEslot = -1;
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
   if (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
   int tix = 0;
@@ -2370,61 +2379,47 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     ff ef5[5], tf5[5], af5[5] = {tf[0], tf[1], tf[2], tf[3], tU};
     float eg[11], tgt[11];
     if (tile_end) {
+      // everything before this tile into the carries, then this tile's scans
+      ff ptot[16];
+      breduce_ff<16>(pacc, ptot, S.scan);
+#pragma unroll
+      for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], ptot[j]);
+      cU = ff_add(cU, ptot[4]);
+#pragma unroll
+      for (int j = 0; j < 11; j++) cgc[j] = ff_add(cgc[j], ptot[5 + j]);
+#pragma unroll
+      for (int j = 0; j < 16; j++) pacc[j] = ffz();
       bscan_ff<5>(af5, ef5, tf5, S.scan);
       bscan_f<11>(tg, eg, tgt, S.scan);
     } else {
-      breduce_ff<5>(af5, tf5, S.scan);
-      breduce_f<11>(tg, tgt, S.scan);
 #pragma unroll
-      for (int j = 0; j < 5; j++) ef5[j] = ffz();
+      for (int j = 0; j < 5; j++) { pacc[j] = ff_add(pacc[j], af5[j]); tf5[j] = ffz(); ef5[j] = ffz(); }
 #pragma unroll
-      for (int j = 0; j < 11; j++) eg[j] = 0.f;
+      for (int j = 0; j < 11; j++) { pacc[5 + j] = ff_add(pacc[5 + j], fff(tg[j])); tgt[j] = 0.f; eg[j] = 0.f; }
     }
-    // most bound particle: FP32 screen, FP64 decision
-    float emin = 3.0e38f;
-#pragma unroll
-    for (int k = 0; k < kItems; k++) emin = fminf(emin, Ef[k]);
-    for (int off = 16; off > 0; off >>= 1) emin = fminf(emin, __shfl_xor_sync(0xffffffffu, emin, off));
+    // most bound particle: FP32 screen against the warp's running minimum
+    // (this tile included), FP64 energy of each candidate; the best per
+    // thread is reduced over the block once, after the last tile
     {
-      int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-      if (lane == 0) S.bf[wid] = emin;
-      __syncthreads();
       float tmin = 3.0e38f;
-      for (int qq = 0; qq < nw; qq++) tmin = fminf(tmin, S.bf[qq]);
-      __syncthreads();
-      float ref = fminf(tmin, (float)Ebest);
-      float cut = ref + 1e-4f * fabsf(ref) + 1e-30f;
-      double bE = 1e300;
-      long long bs = -1;
+#pragma unroll
+      for (int k = 0; k < kItems; k++) tmin = fminf(tmin, Ef[k]);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, off));
+      pEmin = fminf(pEmin, tmin);
+      const float cut = pEmin + 1e-4f * fabsf(pEmin) + 1e-30f;
       long long rX = cX + ex[1], rY = cY + ex[2], rZ = cZ + ex[3];
 #pragma unroll
       for (int k = 0; k < kItems; k++) {
         if (!m[k]) continue;
         rX += fx[k]; rY += fy[k]; rZ += fz[k];
-        if (!(Ef[k] <= cut)) continue;
-        (*nret)++;
-        double E = mbp_energy64(c, B, W, P, o + i0 + k, Mk[k], i2ff(rX, F.iv), i2ff(rY, F.iv), i2ff(rZ, F.iv),
-                                phi[k], Phi0, w[k]);
-        if (E < bE) { bE = E; bs = (long long)(i0 + k); }
+        if (Ef[k] <= cut) {
+          (*nret)++;
+          double E = mbp_energy64(c, B, W, P, o + i0 + k, Mk[k], i2ff(rX, F.iv), i2ff(rY, F.iv), i2ff(rZ, F.iv),
+                                  phi[k], Phi0, w[k]);
+          if (E < pEbest) { pEbest = E; pEslot = (long long)(i0 + k); }
+        }
       }
-      for (int off = 16; off > 0; off >>= 1) {
-        double oE = __shfl_xor_sync(0xffffffffu, bE, off);
-        long long oi = __shfl_xor_sync(0xffffffffu, bs, off);
-        bool take = oi >= 0 && (bs < 0 || oE < bE || (oE == bE && oi < bs));
-        if (take) { bE = oE; bs = oi; }
-      }
-      if (lane == 0) { S.bd[wid] = bE; S.bl[wid & 7] = bs; }
-      __syncthreads();
-      double TE = 1e300;
-      long long TS = -1;
-      for (int qq = 0; qq < nw; qq++) {
-        double oE = S.bd[qq];
-        long long oi = S.bl[qq];
-        bool take = oi >= 0 && (TS < 0 || oE < TE || (oE == TE && oi < TS));
-        if (take) { TE = oE; TS = oi; }
-      }
-      __syncthreads();
-      if (TS >= 0 && TE < Ebest) { Ebest = TE; Eslot = TS; }
     }
     // bin records at bin ends (cumulative values over the members so far)
     if (tile_end && has_end) {
@@ -2487,6 +2482,37 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     __syncthreads();
   }
   if (SM::kStage > 0) cp_async_wait<0>();
+  {
+    ff ptot[16];
+    breduce_ff<16>(pacc, ptot, S.scan);
+#pragma unroll
+    for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], ptot[j]);
+    cU = ff_add(cU, ptot[4]);
+#pragma unroll
+    for (int j = 0; j < 11; j++) cgc[j] = ff_add(cgc[j], ptot[5 + j]);
+  }
+  long long Eslot = -1;
+  {
+    double bE = pEbest;
+    long long bs = pEslot;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) {
+      double oE = __shfl_xor_sync(0xffffffffu, bE, off);
+      long long oi = __shfl_xor_sync(0xffffffffu, bs, off);
+      bool take = oi >= 0 && (bs < 0 || oE < bE || (oE == bE && oi < bs));
+      if (take) { bE = oE; bs = oi; }
+    }
+    if (lane == 0) { S.bd[wid] = bE; S.bl[wid & 7] = bs; }
+    __syncthreads();
+    double TE = 1e300;
+    for (int qq = 0; qq < nw; qq++) {
+      double oE = S.bd[qq];
+      long long oi = S.bl[qq];
+      bool take = oi >= 0 && (Eslot < 0 || oE < TE || (oE == TE && oi < Eslot));
+      if (take) { TE = oE; Eslot = oi; }
+    }
+    __syncthreads();
+  }
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
 #ifdef AHFGPU_PHASE_TIMERS
   long long _pp = clock64();
