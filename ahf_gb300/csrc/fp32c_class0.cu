@@ -1,19 +1,26 @@
 // fp32c_class0.cu -- instantiation of the FP32-compensated halo kernel for
-// size class 0 (32 threads per CTA, shared-memory sort SortSmemT<512, 16>).  One
+// size class 0 (64 threads per CTA, shared-memory sort SortSmemT<512, 16>).  One
 // translation unit per class so the classes compile in parallel.
 #include "halo_fp32c.cuh"
 
+#ifndef AHFGPU_CLASS0_T
+#define AHFGPU_CLASS0_T 64
+#endif
+
 namespace ahfgpu {
 
+constexpr int kT0 = AHFGPU_CLASS0_T;
+using SS0 = SortSmemT<512, 16>;
+
 void launch_fp32c_class0(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<32, SortSmemT<512, 16>><<<grid, 32, sizeof(F32Smem<SortSmemT<512, 16>, 32>), st>>>(P, B, W);
+  halo_fp32c_kernel<kT0, SS0><<<grid, kT0, sizeof(F32Smem<SS0, kT0>), st>>>(P, B, W);
 }
 
 int fp32c_occupancy_class0() {
   int nb = 0;
-  cudaFuncSetAttribute(halo_fp32c_kernel<32, SortSmemT<512, 16>>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(F32Smem<SortSmemT<512, 16>, 32>));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<32, SortSmemT<512, 16>>, 32, sizeof(F32Smem<SortSmemT<512, 16>, 32>));
+  cudaFuncSetAttribute(halo_fp32c_kernel<kT0, SS0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(F32Smem<SS0, kT0>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<kT0, SS0>, kT0, sizeof(F32Smem<SS0, kT0>));
   return nb;
 }
 

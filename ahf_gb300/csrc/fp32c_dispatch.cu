@@ -1,5 +1,5 @@
 // fp32c_dispatch.cu -- size classes of the FP32-compensated form: class 0
-// takes lists of up to 512 particles with one-warp CTAs (8 haloes in flight
+// takes lists of up to 512 particles with two-warp CTAs (4 haloes in flight
 // per SM), class 1 lists up to 16384 with four-warp CTAs, class 2 the rest
 // with eight-warp CTAs.
 #include <cstdint>
