@@ -38,7 +38,7 @@
 
 namespace ahfgpu {
 
-constexpr int kItems = 4;                 // consecutive slots per thread
+constexpr int kItems = 4;                 // consecutive slots per thread (default; per class: F32Smem::kItems)
 constexpr double kEps64 = 1.1102230246251565e-16;
 constexpr float kBand1 = 2e-5f;      // relative band of the FP32 decisions
 
@@ -59,6 +59,7 @@ struct StageGeo {
 template <class SS, int T = 256>
 struct F32Smem {
   static constexpr int kT = T;
+  static constexpr int kItems = T >= 128 ? 4 : 2;   // consecutive slots per thread
   static constexpr int kStage = T >= 128 ? 2 * StageGeo<T>::kBuf : 0;
   union {
     SS sort;
@@ -395,12 +396,31 @@ __device__ __forceinline__ void ld4f(const float* p, float (&v)[4]) {
   float4 t = *reinterpret_cast<const float4*>(p);
   v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
 }
+__device__ __forceinline__ void ld4f(const float* p, float (&v)[2]) {
+  float2 t = *reinterpret_cast<const float2*>(p);
+  v[0] = t.x; v[1] = t.y;
+}
 __device__ __forceinline__ void ld4ff(const double* p, ff (&v)[4]) {
   const float4* q = reinterpret_cast<const float4*>(p);
   float4 a = q[0], b = q[1];
   v[0] = ff{a.x, a.y}; v[1] = ff{a.z, a.w}; v[2] = ff{b.x, b.y}; v[3] = ff{b.z, b.w};
 }
+__device__ __forceinline__ void ld4ff(const double* p, ff (&v)[2]) {
+  float4 a = *reinterpret_cast<const float4*>(p);
+  v[0] = ff{a.x, a.y}; v[1] = ff{a.z, a.w};
+}
 __device__ __forceinline__ unsigned ld4u8(const uint8_t* p) { return *reinterpret_cast<const unsigned*>(p); }
+// N consecutive flags (N = 4 or 2) as the low bytes of an unsigned, and back
+template <int N>
+__device__ __forceinline__ unsigned ldnu8(const uint8_t* p) {
+  if (N == 4) return *reinterpret_cast<const unsigned*>(p);
+  return *reinterpret_cast<const unsigned short*>(p);
+}
+template <int N>
+__device__ __forceinline__ void stnu8(uint8_t* p, unsigned v) {
+  if (N == 4) *reinterpret_cast<unsigned*>(p) = v;
+  else *reinterpret_cast<unsigned short*>(p) = (unsigned short)v;
+}
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
@@ -417,6 +437,10 @@ __device__ __forceinline__ void ld4ll(const long long* p, long long (&v)[4]) {
   const longlong2* q = reinterpret_cast<const longlong2*>(p);
   longlong2 a = q[0], b = q[1];
   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void ld4ll(const long long* p, long long (&v)[2]) {
+  longlong2 a = *reinterpret_cast<const longlong2*>(p);
+  v[0] = a.x; v[1] = a.y;
 }
 
 // fixed-point weights and momenta of the sorted slots (FP32C), written once
@@ -994,6 +1018,7 @@ static __device__ __noinline__ bool ov_fail(const Ctx32& c, const DevBatch& B, c
 template <class SM>
 static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                      const Fix& F, ff* Phi0, double* mo, unsigned* nret, int& par) {
+  constexpr int kItems = SM::kItems;
   const float V43f = (float)(4. * kPi / 3.);
   const float ovk = __fmul_rn(__fmul_rn(P.f_ovlim, P.f_rvrf), V43f);
   float2* phs = reinterpret_cast<float2*>(W.phi + c.s);
@@ -1187,6 +1212,7 @@ template <class SM>
 static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                    const Fix& F, uint64_t n1, ff Phi0, uint64_t js, float vmax, IterOut& out,
                                    unsigned* nret, int& par) {
+  constexpr int kItems = SM::kItems;
   const uint64_t o = c.s;
   const float vf = (float)P.v_fac, Hr = (float)(P.Hubble * P.r_fac), v2t = (float)P.v2_tune;
   const float pf2 = (float)(2.0 * P.phi_fac);
@@ -1211,7 +1237,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
   if (threadIdx.x == 0) { S.amb_n = 0; S.amb_ovf = P.force_exact == 1 ? 1 : 0; }
   __syncthreads();
-  if (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
+  if constexpr (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
   int tix = 0;
   for (uint64_t base = 0; base < n1; base += tile, tix++) {
     PT_T0;
@@ -1232,7 +1258,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
       }
 #pragma unroll
       for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
-      if (SM::kStage > 0) {
+      if constexpr (SM::kStage > 0) {
         // this tile's inputs were copied one tile ago; start the next tile's
         stage_issue(S, (tix & 1) ^ 1, W, o, i0 + tile, n1, has_w);
         cp_async_wait<1>();
@@ -1247,7 +1273,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
           st_ll<SM>(sb, 2, fx); st_ll<SM>(sb, 3, fy); st_ll<SM>(sb, 4, fz);
         }
       } else if (i0 < n1) {
-        f4 = ld4u8(W.flag + o + i0);
+        f4 = ldnu8<kItems>(W.flag + o + i0);
         if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
         ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
         ld4f(W.fdx + o + i0, dx); ld4f(W.fdy + o + i0, dy); ld4f(W.fdz + o + i0, dz);
@@ -1419,7 +1445,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
 #pragma unroll
       for (int k = 0; k < kItems; k++)
         if (i0 + k < n1) nf = (nf & ~(0xffu << (8 * k))) | ((unsigned)((m[k] ? 1 : 0) | (b[k] ? 2 : 0)) << (8 * k));
-      *reinterpret_cast<unsigned*>(W.flag + o + i0) = nf;
+      stnu8<kItems>(W.flag + o + i0, nf);
     }
     PT_T(W, 12);
     cM += tot[0]; cX += tot[1]; cY += tot[2]; cZ += tot[3];
@@ -1429,7 +1455,7 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
     for (int j = 0; j < 4; j++) cDb[j] = pb[j];
     cLs = pbslot;
   }
-  if (SM::kStage > 0) cp_async_wait<0>();
+  if constexpr (SM::kStage > 0) cp_async_wait<0>();
   out.nb = cNb;
   out.Mb = i2ff(cM, F.im);
   out.Phi0n = cNb > 0 ? ff_add(cPhiN, ff_div(out.Mb, ff{cDb[0], cDb[1]})) : ffz();
@@ -1730,6 +1756,7 @@ static __device__ void exact_iter32(const Ctx32& c, const DevBatch& B, const Wor
 template <class SM>
 static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams& P, SM& S, const Fix& F, uint64_t n1,
                                  int& par) {
+  constexpr int kItems = SM::kItems;
   const uint64_t o = c.s;
   float2* phs = reinterpret_cast<float2*>(W.phi + o);
   long long cM = 0, cs = -1;
@@ -1750,7 +1777,7 @@ static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams&
 #pragma unroll
     for (int k = 0; k < kItems; k++) { w[k] = 1.f; fw[k] = F.w1; dh[k] = dl[k] = qh[k] = ql[k] = 0.f; }
     if (i0 < n1) {
-      f4 = ld4u8(W.flag + o + i0);
+      f4 = ldnu8<kItems>(W.flag + o + i0);
       if (P.has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
       ld4f(W.fdh + o + i0, dh); ld4f(W.fdl + o + i0, dl);
       ld4f(W.fqh + o + i0, qh); ld4f(W.fql + o + i0, ql);
@@ -1809,6 +1836,7 @@ static __device__ ff phi0_pass32(const Ctx32& c, const Work& W, const DevParams&
 template <class SM>
 static __device__ long long rvir_pass32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                  uint64_t n1, ff* Mfail, unsigned* nret) {
+  constexpr int kItems = SM::kItems;
   const uint64_t o = c.s;
   ff cM = ffz();
   for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * kItems) {
@@ -2163,6 +2191,7 @@ template <class SM>
 static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                                   const Fix& F, uint64_t n1, uint64_t n2, ff Phi0, ahfgpu_halo& hout, unsigned* nret,
                                   int& par) {
+  constexpr int kItems = SM::kItems;
   const uint64_t o = c.s;
   const double FPT = 4. * kPi / 3.;
   float2* Rff = reinterpret_cast<float2*>(W.prof_a + o);   // radius (float-float) per rank
@@ -2248,7 +2277,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   double pEbest = 1e300;
   long long pEslot = -1;
   const uint64_t tile = (uint64_t)blockDim.x * kItems;
-  if (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
+  if constexpr (SM::kStage > 0) stage_issue(S, 0, W, o, (uint64_t)threadIdx.x * kItems, n1, has_w);
   int tix = 0;
   for (uint64_t base = 0; base < n1; base += tile, tix++) {
     const uint64_t i0 = base + (uint64_t)threadIdx.x * kItems;
@@ -2273,7 +2302,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       }
 #pragma unroll
       for (int k = 0; k < kItems; k++) { fw[k] = F.w1; fx[k] = fy[k] = fz[k] = 0; }
-      if (SM::kStage > 0) {
+      if constexpr (SM::kStage > 0) {
         stage_issue(S, (tix & 1) ^ 1, W, o, i0 + tile, n1, has_w);
         if (i0 < n1) { ld4f(W.fdxl + o + i0, dxl); ld4f(W.fdyl + o + i0, dyl); ld4f(W.fdzl + o + i0, dzl); }
         cp_async_wait<1>();
@@ -2288,7 +2317,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
           st_ll<SM>(sb, 2, fx); st_ll<SM>(sb, 3, fy); st_ll<SM>(sb, 4, fz);
         }
       } else if (i0 < n1) {
-        f4 = ld4u8(W.flag + o + i0);
+        f4 = ldnu8<kItems>(W.flag + o + i0);
         if (has_w) { ld4f(W.sw + o + i0, w); ld4ll(fix_w(W) + o + i0, fw); }
         ld4f(W.svx + o + i0, vx); ld4f(W.svy + o + i0, vy); ld4f(W.svz + o + i0, vz);
         ld4f(W.fdx + o + i0, dx); ld4f(W.fdy + o + i0, dy); ld4f(W.fdz + o + i0, dz);
@@ -2481,7 +2510,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     cr += tn;
     __syncthreads();
   }
-  if (SM::kStage > 0) cp_async_wait<0>();
+  if constexpr (SM::kStage > 0) cp_async_wait<0>();
   {
     ff ptot[16];
     breduce_ff<16>(pacc, ptot, S.scan);
