@@ -234,8 +234,11 @@ int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, P
   pl.nbins_total = pl.prof_cap_off[nh];
   pl.queue.resize(nh);
   std::iota(pl.queue.begin(), pl.queue.end(), 0);
-  std::stable_sort(pl.queue.begin(), pl.queue.end(),
-                   [&](int32_t a, int32_t b) { return off[a + 1] - off[a] > off[b + 1] - off[b]; });
+  // largest first, ties by index (a deterministic total order)
+  std::sort(pl.queue.begin(), pl.queue.end(), [&](int32_t a, int32_t b) {
+    uint64_t na = off[a + 1] - off[a], nb = off[b + 1] - off[b];
+    return na > nb || (na == nb && a < b);
+  });
   // the queue is largest first: class 2 (largest) occupies the front
   int64_t qp = 0;
   pl.cls_begin[0] = 0;
@@ -279,11 +282,9 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
 }
 
 // Runs the stage on a device-resident batch.  Results stay in g.* buffers.
-int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const uint64_t* host_off, ahfgpu_mode mode,
+int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl, ahfgpu_mode mode,
                cudaStream_t st, ahfgpu_stats* stats) {
-  Plan pl;
-  int rc = validate_and_plan(prm, host_off, db->nhalo, pl);
-  if (rc) return rc;
+  int rc;
   if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64 && mode != AHFGPU_BATCHED_FP32C)
     return fail(AHFGPU_ERR_INVALID, "unknown mode %d", (int)mode);
   const int grid = std::max(1, g.nsm * std::max(g.fp64_bps, g.fp32c_bps[2] + g.fp32c_bps[1]));
@@ -548,7 +549,9 @@ int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batc
     CK(cudaStreamSynchronize(st));
   }
   ahfgpu_stats s{};
-  rc = run_device(params, batch, off.data(), mode, st, &s);
+  Plan pl;
+  if ((rc = validate_and_plan(params, off.data(), nh, pl))) return rc;
+  rc = run_device(params, batch, pl, mode, st, &s);
   if (rc) return rc;
   s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   g.last_stats = s;
@@ -687,7 +690,7 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
   ahfgpu_batch db;
   if ((rc = copy_in(batch, &db, st))) return rc;
   ahfgpu_stats s{};
-  rc = run_device(params, &db, batch->off, mode, st, &s);
+  rc = run_device(params, &db, pl, mode, st, &s);
   if (rc) return rc;
   g.last_stats = s;
   if ((rc = ahfgpu_fetch_result(result))) return rc;

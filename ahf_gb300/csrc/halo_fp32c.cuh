@@ -783,7 +783,7 @@ static __device__ __noinline__ double ref_key(const DevBatch& B, uint64_t e, dou
 template <class SM>
 static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, SM& S,
                               float (&lim)[3]) {
-  constexpr int G = 4;   // entries in flight per thread
+  constexpr int G = 8;   // entries in flight per thread
   float vm = 0.f, wx = 0.f, wn = 3.0e38f;
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
     float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];
@@ -882,7 +882,7 @@ static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, 
 // gathers the sorted slots, with the fixed-point weights and momenta
 static __device__ void gather32(const Ctx32& c, const DevBatch& B, const Work& W, const DevParams& P, const Fix& F) {
   const float s62 = pow2f(-62);
-  constexpr int G = 4;   // entries in flight per thread (the reads are random)
+  constexpr int G = 8;   // entries in flight per thread (the reads are random)
   for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
     uint32_t jj[G];
     float px[G], py[G], pz[G], pvx[G], pvy[G], pvz[G], pw[G];

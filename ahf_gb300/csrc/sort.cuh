@@ -237,11 +237,22 @@ static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* key
       continue;
     }
     // range of the bucketing key
+    constexpr int U = 8;   // elements in flight per thread in the streaming loops
     uint64_t mn = ~0ull, mx = 0;
-    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      uint64_t k = by_slot ? (uint64_t)is[lo + i] : ks[lo + i];
-      mn = k < mn ? k : mn;
-      mx = k > mx ? k : mx;
+    for (uint32_t base = 0; base < cnt; base += blockDim.x * U) {
+      uint64_t kk[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        kk[u] = i < cnt ? (by_slot ? (uint64_t)is[lo + i] : ks[lo + i]) : ~0ull;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        if (i >= cnt) continue;
+        mn = kk[u] < mn ? kk[u] : mn;
+        mx = kk[u] > mx ? kk[u] : mx;
+      }
     }
     block_minmax_u64(mn, mx, S);
     if (!by_slot && mn == mx) {
@@ -262,28 +273,63 @@ static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* key
     while ((range >> shift) >= (uint64_t)nb) shift++;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) S.hist[b] = 0;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      uint64_t k = by_slot ? (uint64_t)is[lo + i] : ks[lo + i];
-      atomicAdd(&S.hist[(int)((k - mn) >> shift)], 1u);
-    }
-    __syncthreads();
-    // exclusive scan of the histogram (thread 0; nb <= 4096)
-    if (threadIdx.x == 0) {
-      uint32_t run = 0;
-      for (int b = 0; b < nb; b++) {
-        uint32_t c = S.hist[b];
-        S.hist[b] = run;
-        run += c;
+    for (uint32_t base = 0; base < cnt; base += blockDim.x * U) {
+      uint64_t kk[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        kk[u] = i < cnt ? (by_slot ? (uint64_t)is[lo + i] : ks[lo + i]) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        if (i < cnt) atomicAdd(&S.hist[(int)((kk[u] - mn) >> shift)], 1u);
       }
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
-      uint64_t k = ks[lo + i];
-      uint32_t s = is[lo + i];
-      uint64_t bk = by_slot ? (uint64_t)s : k;
-      uint32_t pos = atomicAdd(&S.hist[(int)((bk - mn) >> shift)], 1u);
-      kd[lo + pos] = k;
-      id[lo + pos] = s;
+    // exclusive scan of the histogram: contiguous runs of buckets per thread
+    {
+      const int per = (nb + (int)blockDim.x - 1) / (int)blockDim.x;
+      const int b0 = threadIdx.x * per, b1 = min(b0 + per, nb);
+      uint32_t run = 0;
+      for (int b = b0; b < b1; b++) run += S.hist[b];
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      uint32_t inc = run;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc += y;
+      }
+      uint32_t* wt = reinterpret_cast<uint32_t*>(S.red_u64);
+      if (lane == 31) wt[wid] = inc;
+      __syncthreads();
+      uint32_t b = inc - run;
+      for (int w = 0; w < wid; w++) b += wt[w];
+      for (int q = b0; q < b1; q++) {
+        uint32_t c = S.hist[q];
+        S.hist[q] = b;
+        b += c;
+      }
+    }
+    __syncthreads();
+    for (uint32_t base = 0; base < cnt; base += blockDim.x * U) {
+      uint64_t kk[U];
+      uint32_t ss[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        kk[u] = i < cnt ? ks[lo + i] : 0;
+        ss[u] = i < cnt ? is[lo + i] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        uint32_t i = base + threadIdx.x + u * blockDim.x;
+        if (i >= cnt) continue;
+        uint64_t bk = by_slot ? (uint64_t)ss[u] : kk[u];
+        uint32_t pos = atomicAdd(&S.hist[(int)((bk - mn) >> shift)], 1u);
+        kd[lo + pos] = kk[u];
+        id[lo + pos] = ss[u];
+      }
     }
     __syncthreads();
     // hist[b] is now the END of bucket b; walk runs of buckets

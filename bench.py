@@ -388,17 +388,21 @@ def ours_arm(args, ws, rank, local):
         e2e_steps = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
         d2h = 0
+        lib_total, lib_dev = [], []
         for _ in range(e2e_steps):
             rr = lib.construct_halos_raw(params, hb, mode)
             nk = rr.stats.n_kept
             d2h = nk * 8 + len(n_in) * (C.sizeof(abi.Halo) + 16) + 8 * 25 * int(res.prof_off[-1])
+            lib_total.append(rr.stats.ms_total)
+            lib_dev.append(rr.stats.ms_device)
             lib.free_result(rr)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / e2e_steps
         dt = allmax(ws, dt)
         h2d = N * (24 + (4 if lists.w is not None else 0) + 8) + len(n_in) * 32
         e2e = {"value": total_parts / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "ms_per_step": dt * 1e3}
+               "ms_per_step": dt * 1e3, "ms_in_library": float(np.mean(lib_total)),
+               "ms_device": float(np.mean(lib_dev))}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
