@@ -125,6 +125,11 @@ class Stats(C.Structure):
         ("n_launches", C.c_uint64),
         ("ms_device", C.c_double),
         ("ms_total", C.c_double),
+        ("ms_plan", C.c_double),
+        ("ms_h2d", C.c_double),
+        ("ms_h2d_first", C.c_double),
+        ("ms_pack", C.c_double),
+        ("ms_d2h", C.c_double),
     ]
 
 

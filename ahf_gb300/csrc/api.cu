@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -82,10 +83,14 @@ struct Ctx {
   int device = -1;
   int nsm = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev_cp0 = nullptr;
   int fp64_bps = 1, fp32c_bps[3] = {1, 1, 1};
-  cudaStream_t cls_stream[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[3] = {nullptr, nullptr, nullptr};
+  // FP32C launches: one stream per (queue part, size class); part 0 is the
+  // queue prefix whose inputs the host path copies first
+  cudaStream_t seg_stream[2][3] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[2][3] = {};
+  cudaStream_t copy_stream = nullptr;       // host-to-device input copies
+  cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
   // inputs copied from the host (host API)
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
@@ -105,44 +110,99 @@ Ctx g;
 // ---------------------------------------------------------------------------
 // small packing kernels
 
-__global__ void k_scan_counts(const ahfgpu_halo* halo, int64_t nh, int which, uint64_t* out) {
-  // single block: exclusive scan of npart (which=0) or nbins (which=1)
-  __shared__ unsigned long long part[1024];
+// exclusive scans of the kept counts (block 0, into moff) and of the bin
+// counts (block 1, into poff); four consecutive haloes per thread
+__global__ void k_scan_counts(const ahfgpu_halo* halo, int64_t nh, uint64_t* moff, uint64_t* poff) {
+  const int which = blockIdx.x;
+  uint64_t* out = which ? poff : moff;
+  __shared__ unsigned long long wsum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned long long carry = 0;
-  for (int64_t base = 0; base < nh; base += blockDim.x) {
-    int64_t i = base + threadIdx.x;
-    unsigned long long v = 0;
-    if (i < nh) v = which == 0 ? halo[i].npart : (unsigned long long)halo[i].nbins;
-    part[threadIdx.x] = v;
-    __syncthreads();
-    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
-      unsigned long long t = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
-      __syncthreads();
-      part[threadIdx.x] += t;
-      __syncthreads();
+  for (int64_t base = 0; base < nh; base += 4 * (int64_t)blockDim.x) {
+    const int64_t i0 = base + 4 * (int64_t)threadIdx.x;
+    unsigned long long v[4], t = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      int64_t i = i0 + k;
+      v[k] = i < nh ? (which == 0 ? halo[i].npart : (unsigned long long)halo[i].nbins) : 0ull;
     }
-    if (i < nh) out[i + 1] = carry + part[threadIdx.x];
-    unsigned long long tot = part[blockDim.x - 1];
+#pragma unroll
+    for (int k = 0; k < 4; k++) t += v[k];
+    unsigned long long inc = t;            // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
+    }
+    if (lane == 31) wsum[wid] = inc;
     __syncthreads();
-    carry += tot;
+    if (wid == 0) {
+      unsigned long long w = lane < nw ? wsum[lane] : 0ull;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long u = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += u;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    unsigned long long run = carry + (wid ? wsum[wid - 1] : 0ull) + inc - t;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      run += v[k];
+      if (i0 + k < nh) out[i0 + k + 1] = run;
+    }
+    carry += wsum[nw - 1];
+    __syncthreads();
   }
   if (threadIdx.x == 0) out[0] = 0;
 }
 
-// kept ids into the packed CSR list, one output element per thread: the
-// halo of output j is the last h with moff[h] <= j (binary search; the lanes
-// of a warp mostly share it, so the probes are broadcasts)
-__global__ void k_pack_members(const uint64_t* off, const uint64_t* stage, const uint64_t* moff, uint64_t* member,
-                               int64_t nh) {
+// kept entries into the packed CSR list of ids (gidx[e], or e without gidx).
+// A block copies one chunk of kPackChunk
+// output slots: two binary searches over moff bound the haloes it touches;
+// when there are at most kPackHaloes of them their offsets are staged in
+// shared memory and each slot's halo (the last h with moff[h] <= j) is
+// searched there, else in global memory within the same bounds.
+constexpr int kPackChunk = 4096, kPackHaloes = 1024;
+
+__device__ __forceinline__ int64_t last_le(const uint64_t* a, int64_t lo, int64_t hi, uint64_t j) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi + 1) >> 1;
+    if (a[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_pack_members(const uint64_t* off, const uint64_t* stage, const uint64_t* moff,
+                               const uint64_t* gidx, uint64_t* member, int64_t nh) {
+  __shared__ uint64_t s_moff[kPackHaloes], s_off[kPackHaloes];
+  __shared__ int64_t s_h[2];
   const uint64_t total = moff[nh];
-  for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total;
-       j += (uint64_t)gridDim.x * blockDim.x) {
-    int64_t lo = 0, hi = nh - 1;
-    while (lo < hi) {
-      int64_t mid = (lo + hi + 1) >> 1;
-      if (moff[mid] <= j) lo = mid; else hi = mid - 1;
+  for (uint64_t c0 = (uint64_t)blockIdx.x * kPackChunk; c0 < total; c0 += (uint64_t)gridDim.x * kPackChunk) {
+    const uint64_t c1 = c0 + kPackChunk < total ? c0 + kPackChunk : total;
+    if (threadIdx.x < 2) s_h[threadIdx.x] = last_le(moff, 0, nh - 1, threadIdx.x ? c1 - 1 : c0);
+    __syncthreads();
+    const int64_t h0 = s_h[0], nc = s_h[1] - h0 + 1;
+    if (nc <= kPackHaloes) {
+      for (int64_t i = threadIdx.x; i < nc; i += blockDim.x) {
+        s_moff[i] = moff[h0 + i];
+        s_off[i] = off[h0 + i];
+      }
+      __syncthreads();
+      for (uint64_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+        int64_t i = last_le(s_moff, 0, nc - 1, j);
+        uint64_t e = stage[s_off[i] + (j - s_moff[i])];
+        member[j] = gidx ? gidx[e] : e;
+      }
+    } else {
+      for (uint64_t j = c0 + threadIdx.x; j < c1; j += blockDim.x) {
+        int64_t h = last_le(moff, h0, h0 + nc - 1, j);
+        uint64_t e = stage[off[h] + (j - moff[h])];
+        member[j] = gidx ? gidx[e] : e;
+      }
     }
-    member[j] = stage[off[lo] + (j - moff[lo])];
+    __syncthreads();
   }
 }
 
@@ -200,11 +260,15 @@ int nbins_cap(uint64_t n, int64_t minpart) {
   return std::min(nb, kMaxBins);
 }
 
+// batches below this many particles are copied in one piece
+constexpr uint64_t kSplitMinParticles = 1u << 22;
+
 struct Plan {
   int64_t nhalo = 0;
   uint64_t N = 0, maxn = 0, nbins_total = 0;
   std::vector<int32_t> queue;
   int cls_begin[4] = {0, 0, 0, 0};   // queue positions of the FP32C size classes (largest class first)
+  int split = 0;                     // FP32C: queue prefix [0, split) launched as a part of its own
   std::vector<uint64_t> prof_cap_off;
 };
 
@@ -232,13 +296,26 @@ int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, P
   }
   pl.N = off[nh];
   pl.nbins_total = pl.prof_cap_off[nh];
+  // largest first, ties by index: a stable radix sort (two 16-bit digits)
+  // of the complemented sizes, starting from the ascending indices
   pl.queue.resize(nh);
-  std::iota(pl.queue.begin(), pl.queue.end(), 0);
-  // largest first, ties by index (a deterministic total order)
-  std::sort(pl.queue.begin(), pl.queue.end(), [&](int32_t a, int32_t b) {
-    uint64_t na = off[a + 1] - off[a], nb = off[b + 1] - off[b];
-    return na > nb || (na == nb && a < b);
-  });
+  {
+    std::vector<int32_t> tmp(nh);
+    std::vector<uint32_t> cnt(65537);
+    std::iota(tmp.begin(), tmp.end(), 0);
+    int32_t* src = tmp.data();
+    int32_t* dst = pl.queue.data();
+    for (int shift = 0; shift < 32; shift += 16) {
+      std::fill(cnt.begin(), cnt.end(), 0u);
+      auto digit = [&](int32_t h) { return (~(uint32_t)(off[h + 1] - off[h]) >> shift) & 0xffffu; };
+      for (int64_t i = 0; i < nh; i++) cnt[digit(src[i]) + 1]++;
+      for (int d = 0; d < 65536; d++) cnt[d + 1] += cnt[d];
+      for (int64_t i = 0; i < nh; i++) dst[cnt[digit(src[i])]++] = src[i];
+      std::swap(src, dst);
+    }
+    // two passes: the sorted order is back in tmp
+    std::copy(tmp.begin(), tmp.end(), pl.queue.begin());
+  }
   // the queue is largest first: class 2 (largest) occupies the front
   int64_t qp = 0;
   pl.cls_begin[0] = 0;
@@ -281,13 +358,44 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   return AHFGPU_OK;
 }
 
-// Runs the stage on a device-resident batch.  Results stay in g.* buffers.
+// One FP32C launch: the queue range [q0, q1) of one size class within one
+// queue part (part 0 = [0, split)), with its grid.
+struct Seg {
+  int part, cls, q0, q1, grid;
+};
+
+std::vector<Seg> fp32c_segments(const Plan& pl) {
+  std::vector<Seg> v;
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < 3; k++) {                 // queue segment k holds class 2-k
+      int q0 = pl.cls_begin[k], q1 = pl.cls_begin[k + 1];
+      if (p == 0) q1 = std::min(q1, pl.split);
+      else q0 = std::max(q0, pl.split);
+      if (q1 <= q0) continue;
+      int cls = 2 - k;
+      v.push_back({p, cls, q0, q1, std::min(g.nsm * g.fp32c_bps[cls], q1 - q0)});
+    }
+  return v;
+}
+
+// Runs the stage on a device batch.  Results stay in g.* buffers.  With a
+// staging hook (host path) the hook issues the input copies on
+// g.copy_stream after the small set-up copies, recording g.ev_in[0] once the
+// particles of the queue prefix [0, split) are in and g.ev_in[1] once all
+// are; each part's launches wait for its event only.
 int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl, ahfgpu_mode mode,
-               cudaStream_t st, ahfgpu_stats* stats) {
+               cudaStream_t st, ahfgpu_stats* stats, const std::function<int()>* stage = nullptr) {
   int rc;
   if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64 && mode != AHFGPU_BATCHED_FP32C)
     return fail(AHFGPU_ERR_INVALID, "unknown mode %d", (int)mode);
-  const int grid = std::max(1, g.nsm * std::max(g.fp64_bps, g.fp32c_bps[2] + g.fp32c_bps[1]));
+  if (pl.split && mode != AHFGPU_BATCHED_FP32C) return fail(AHFGPU_ERR_STATE, "split queue outside FP32C");
+  const std::vector<Seg> segs = fp32c_segments(pl);
+  int grid = g.nsm * g.fp64_bps;
+  {
+    int sum = 0;
+    for (const Seg& sg : segs) sum += sg.grid;
+    grid = std::max(1, std::max(grid, sum));
+  }
   const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(pl.maxn / 512 + 64, 64), 1u << 20);
   if ((rc = ensure_work(pl, grid, stack_cap))) return rc;
   const int64_t nh = pl.nhalo;
@@ -304,6 +412,12 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   CK(cudaMemsetAsync(g.counters.p, 0, 64, st));
   CK(cudaMemsetAsync(g.err.p, 0, 64, st));
   CK(cudaMemsetAsync(g.halo.p, 0, nh * sizeof(ahfgpu_halo), st));
+  if (stage) {
+    if ((rc = (*stage)())) return rc;
+    // the set-up work on this stream (weight check, device timer) waits for
+    // the inputs that the first launches read: all of them without a split
+    CK(cudaStreamWaitEvent(st, g.ev_in[pl.split ? 0 : 1], 0));
+  }
 
   DevParams P{};
   P.VescTune = prm->VescTune;
@@ -347,7 +461,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   B.x = db->x; B.y = db->y; B.z = db->z;
   B.vx = db->vx; B.vy = db->vy; B.vz = db->vz;
   B.w = db->w;
-  B.gidx = db->gidx;
+  B.gidx = nullptr;   // the kernels stage entry indices; the pack maps them to ids
   B.cx = db->cx; B.cy = db->cy; B.cz = db->cz;
 
   Work W{};
@@ -377,8 +491,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   W.fdxl = g.fdxl.as<float>(); W.fdyl = g.fdyl.as<float>(); W.fdzl = g.fdzl.as<float>();
   W.fqh = g.fqh.as<float>(); W.fql = g.fql.as<float>();
 #ifdef AHFGPU_PHASE_TIMERS
-  // 16 phase counters, then per halo {start ns, end ns, SM cycles, SM id}
-  if ((rc = g.phase.ensure((16 + 4 * (size_t)nh) * 8))) return rc;
+  // kPhaseSlots phase counters, then per halo {start ns, end ns, SM cycles, SM id}
+  if ((rc = g.phase.ensure((kPhaseSlots + 4 * (size_t)nh) * 8))) return rc;
   W.phase = g.phase.as<unsigned long long>();
 #endif
 
@@ -393,26 +507,25 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
     launch_fp64(P, B, W, g.nsm * g.fp64_bps, -1, st);
     launches++;
   } else {
-    // size classes on their own streams, largest first; each class has its
-    // own queue, queue head and worklist region
+    // size classes on streams of their own (larger classes at higher
+    // priority), queue part 0 before part 1; each segment has its own queue
+    // range, queue head and worklist region.  A part-1 launch takes SMs as
+    // the part-0 CTAs of its class run out of work and exit.
     CK(cudaEventRecord(g.ev_fork, st));
-    int stack_base = 0;
-    for (int k = 0; k < 3; k++) {
-      int cls = 2 - k;                      // queue segment k holds class 2-k
-      int q0 = pl.cls_begin[k], q1 = pl.cls_begin[k + 1];
-      if (q1 <= q0) continue;
-      int gr = std::min(g.nsm * g.fp32c_bps[cls], q1 - q0);
+    int stack_base = 0, slot = 2;
+    for (const Seg& sg : segs) {
       Work Wc = W;
-      Wc.queue = g.queue.as<int32_t>() + q0;
-      Wc.nqueue = q1 - q0;
-      Wc.queue_head = g.qhead.as<unsigned int>() + 2 + k;
+      Wc.queue = g.queue.as<int32_t>() + sg.q0;
+      Wc.nqueue = sg.q1 - sg.q0;
+      Wc.queue_head = g.qhead.as<unsigned int>() + slot++;
       Wc.sort_stack = g.stack.as<uint4>() + (size_t)stack_base * stack_cap;
-      stack_base += gr;
-      cudaStream_t cs = g.cls_stream[cls];
+      stack_base += sg.grid;
+      cudaStream_t cs = g.seg_stream[sg.part][sg.cls];
       CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
-      launch_fp32c(cls, P, B, Wc, gr, cs);
-      CK(cudaEventRecord(g.ev_join[cls], cs));
-      CK(cudaStreamWaitEvent(st, g.ev_join[cls], 0));
+      if (stage) CK(cudaStreamWaitEvent(cs, g.ev_in[sg.part], 0));
+      launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
+      CK(cudaEventRecord(g.ev_join[sg.part][sg.cls], cs));
+      CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
       launches++;
     }
   }
@@ -421,15 +534,17 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   CK(cudaGetLastError());
   CK(cudaEventRecord(g.ev1, st));
   // pack
-  k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 0, g.member_off.as<uint64_t>());
-  k_scan_counts<<<1, 1024, 0, st>>>(W.halo, nh, 1, g.prof_off.as<uint64_t>());
+  k_scan_counts<<<2, 1024, 0, st>>>(W.halo, nh, g.member_off.as<uint64_t>(), g.prof_off.as<uint64_t>());
   int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
-  k_pack_members<<<g.nsm * 8, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(),
-                                             g.member.as<uint64_t>(), nh);
+  int mg = (int)std::max<uint64_t>(1, std::min<uint64_t>((pl.N + kPackChunk - 1) / kPackChunk, (uint64_t)g.nsm * 8));
+  if (stage) CK(cudaStreamWaitEvent(st, g.ev_in[2], 0));   // the ids come last
+  k_pack_members<<<mg, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(), db->gidx,
+                                      g.member.as<uint64_t>(), nh);
   k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
                                    g.prof.as<double>(), nh);
-  launches += 4;
+  launches += 3;
   CK(cudaGetLastError());
+  CK(cudaEventRecord(g.ev2, st));
   uint64_t tails[2];
   unsigned long long cnt[4];
   int derr = 0;
@@ -443,6 +558,14 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
   stats->ms_device = ms;
+  CK(cudaEventElapsedTime(&ms, g.ev1, g.ev2));
+  stats->ms_pack = ms;
+  if (stage) {
+    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_in[2]));
+    stats->ms_h2d = ms;
+    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_in[0]));
+    stats->ms_h2d_first = ms;
+  }
   stats->n_kept = tails[0];
   stats->n_retest = cnt[0];
   stats->n_replay_halos = cnt[1];
@@ -499,10 +622,16 @@ int ahfgpu_init(int device) {
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     int pr = k == 2 ? hi : (k == 1 ? (lo + hi) / 2 : lo);
-    CK(cudaStreamCreateWithPriority(&g.cls_stream[k], cudaStreamNonBlocking, pr));
-    CK(cudaEventCreateWithFlags(&g.ev_join[k], cudaEventDisableTiming));
+    for (int p = 0; p < 2; p++) {
+      CK(cudaStreamCreateWithPriority(&g.seg_stream[p][k], cudaStreamNonBlocking, pr));
+      CK(cudaEventCreateWithFlags(&g.ev_join[p][k], cudaEventDisableTiming));
+    }
   }
   CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
+  CK(cudaStreamCreateWithFlags(&g.copy_stream, cudaStreamNonBlocking));
+  for (int p = 0; p < 3; p++) CK(cudaEventCreate(&g.ev_in[p]));
+  CK(cudaEventCreate(&g.ev2));
+  CK(cudaEventCreate(&g.ev_cp0));
   CK(cudaGetLastError());
   g.init = true;
   g_err.clear();
@@ -522,13 +651,19 @@ int ahfgpu_shutdown(void) {
                   &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.rec, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
-  for (int k = 0; k < 3; k++) {
-    if (g.cls_stream[k]) cudaStreamDestroy(g.cls_stream[k]);
-    if (g.ev_join[k]) cudaEventDestroy(g.ev_join[k]);
-  }
+  for (int p = 0; p < 2; p++)
+    for (int k = 0; k < 3; k++) {
+      if (g.seg_stream[p][k]) cudaStreamDestroy(g.seg_stream[p][k]);
+      if (g.ev_join[p][k]) cudaEventDestroy(g.ev_join[p][k]);
+    }
+  if (g.copy_stream) cudaStreamDestroy(g.copy_stream);
+  for (int p = 0; p < 3; p++)
+    if (g.ev_in[p]) cudaEventDestroy(g.ev_in[p]);
   if (g.ev_fork) cudaEventDestroy(g.ev_fork);
   if (g.ev0) cudaEventDestroy(g.ev0);
   if (g.ev1) cudaEventDestroy(g.ev1);
+  if (g.ev2) cudaEventDestroy(g.ev2);
+  if (g.ev_cp0) cudaEventDestroy(g.ev_cp0);
   if (g.stream) cudaStreamDestroy(g.stream);
   g = Ctx();
   return AHFGPU_OK;
@@ -551,6 +686,7 @@ int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batc
   ahfgpu_stats s{};
   Plan pl;
   if ((rc = validate_and_plan(params, off.data(), nh, pl))) return rc;
+  s.ms_plan = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   rc = run_device(params, batch, pl, mode, st, &s);
   if (rc) return rc;
   s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -559,35 +695,83 @@ int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batc
   return AHFGPU_OK;
 }
 
-static int copy_in(const ahfgpu_batch* hb, ahfgpu_batch* db, cudaStream_t st) {
+// Host inputs -> device on stream cs, recording g.ev_in[0] once the
+// particles of the queue prefix [0, pl.split) are in, g.ev_in[1] once all
+// are and g.ev_in[2] after the ids (gidx), which only the final pack reads.
+// The prefix's particle ranges (merged where adjacent) go first, then the
+// gaps between them, so every particle crosses the link once.
+static int copy_in(const ahfgpu_batch* hb, ahfgpu_batch* db, const Plan& pl, cudaStream_t cs) {
   int64_t nh = hb->nhalo;
   uint64_t N = nh > 0 ? hb->off[nh] : 0;
   int rc;
   *db = *hb;
-  auto up = [&](DBuf& buf, const void* src, size_t bytes, const void** dst) -> int {
-    if (!src) { *dst = nullptr; return AHFGPU_OK; }
-    int r = buf.ensure(std::max<size_t>(bytes, 8));
-    if (r) return r;
-    cudaError_t e = cudaMemcpyAsync(buf.p, src, bytes, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return fail(AHFGPU_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
-    *dst = buf.p;
+  CK(cudaEventRecord(g.ev_cp0, cs));
+  if (nh == 0) {
+    for (int p = 0; p < 3; p++) CK(cudaEventRecord(g.ev_in[p], cs));
     return AHFGPU_OK;
-  };
-  if (nh == 0) return AHFGPU_OK;
+  }
   if (!hb->x || !hb->y || !hb->z || !hb->vx || !hb->vy || !hb->vz || !hb->cx || !hb->cy || !hb->cz)
     return fail(AHFGPU_ERR_INVALID, "a required batch array is NULL");
-  if ((rc = up(g.in_off, hb->off, (nh + 1) * 8, (const void**)&db->off))) return rc;
-  if ((rc = up(g.in_x, hb->x, N * 4, (const void**)&db->x))) return rc;
-  if ((rc = up(g.in_y, hb->y, N * 4, (const void**)&db->y))) return rc;
-  if ((rc = up(g.in_z, hb->z, N * 4, (const void**)&db->z))) return rc;
-  if ((rc = up(g.in_vx, hb->vx, N * 4, (const void**)&db->vx))) return rc;
-  if ((rc = up(g.in_vy, hb->vy, N * 4, (const void**)&db->vy))) return rc;
-  if ((rc = up(g.in_vz, hb->vz, N * 4, (const void**)&db->vz))) return rc;
-  if ((rc = up(g.in_w, hb->w, N * 4, (const void**)&db->w))) return rc;
-  if ((rc = up(g.in_gidx, hb->gidx, N * 8, (const void**)&db->gidx))) return rc;
-  if ((rc = up(g.in_cx, hb->cx, nh * 8, (const void**)&db->cx))) return rc;
-  if ((rc = up(g.in_cy, hb->cy, nh * 8, (const void**)&db->cy))) return rc;
-  if ((rc = up(g.in_cz, hb->cz, nh * 8, (const void**)&db->cz))) return rc;
+  struct Arr {
+    DBuf* buf;
+    const void* src;
+    size_t esize, count;
+    const void** dst;
+  };
+  Arr arr[12] = {{&g.in_off, hb->off, 8, (size_t)nh + 1, (const void**)&db->off},
+                 {&g.in_cx, hb->cx, 8, (size_t)nh, (const void**)&db->cx},
+                 {&g.in_cy, hb->cy, 8, (size_t)nh, (const void**)&db->cy},
+                 {&g.in_cz, hb->cz, 8, (size_t)nh, (const void**)&db->cz},
+                 {&g.in_x, hb->x, 4, N, (const void**)&db->x},
+                 {&g.in_y, hb->y, 4, N, (const void**)&db->y},
+                 {&g.in_z, hb->z, 4, N, (const void**)&db->z},
+                 {&g.in_vx, hb->vx, 4, N, (const void**)&db->vx},
+                 {&g.in_vy, hb->vy, 4, N, (const void**)&db->vy},
+                 {&g.in_vz, hb->vz, 4, N, (const void**)&db->vz},
+                 {&g.in_w, hb->w, 4, N, (const void**)&db->w},
+                 {&g.in_gidx, hb->gidx, 8, N, (const void**)&db->gidx}};
+  for (Arr& a : arr) {
+    if (!a.src) { *a.dst = nullptr; continue; }
+    if ((rc = a.buf->ensure(std::max<size_t>(a.esize * a.count, 8)))) return rc;
+    *a.dst = a.buf->p;
+  }
+  auto put = [&](const Arr& a, uint64_t lo, uint64_t hi) -> int {
+    if (!a.src || hi <= lo) return AHFGPU_OK;
+    cudaError_t e = cudaMemcpyAsync((char*)a.buf->p + lo * a.esize, (const char*)a.src + lo * a.esize,
+                                    (hi - lo) * a.esize, cudaMemcpyHostToDevice, cs);
+    if (e != cudaSuccess) return fail(AHFGPU_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
+    return AHFGPU_OK;
+  };
+  for (int i = 0; i < 4; i++)
+    if ((rc = put(arr[i], 0, arr[i].count))) return rc;
+  // particle ranges of the prefix, in memory order, adjacent ones merged
+  std::vector<std::pair<uint64_t, uint64_t>> head;
+  head.reserve(pl.split);
+  for (int q = 0; q < pl.split; q++) {
+    int32_t h = pl.queue[q];
+    if (hb->off[h + 1] > hb->off[h]) head.push_back({hb->off[h], hb->off[h + 1]});
+  }
+  std::sort(head.begin(), head.end());
+  std::vector<std::pair<uint64_t, uint64_t>> merged;
+  for (const auto& r : head) {
+    if (!merged.empty() && merged.back().second == r.first) merged.back().second = r.second;
+    else merged.push_back(r);
+  }
+  for (int i = 4; i < 11; i++)
+    for (const auto& r : merged)
+      if ((rc = put(arr[i], r.first, r.second))) return rc;
+  CK(cudaEventRecord(g.ev_in[0], cs));
+  for (int i = 4; i < 11; i++) {
+    uint64_t at = 0;
+    for (const auto& r : merged) {
+      if ((rc = put(arr[i], at, r.first))) return rc;
+      at = r.second;
+    }
+    if ((rc = put(arr[i], at, N))) return rc;
+  }
+  CK(cudaEventRecord(g.ev_in[1], cs));
+  if ((rc = put(arr[11], 0, N))) return rc;
+  CK(cudaEventRecord(g.ev_in[2], cs));
   return AHFGPU_OK;
 }
 
@@ -611,7 +795,10 @@ static void* host_block_get(size_t bytes) {
   if (g_spare.p) { cudaFreeHost(g_spare.p); g_spare = HostBlock{}; }
   void* p = nullptr;
   size_t cap = bytes + bytes / 8 + 4096;
-  if (cudaMallocHost(&p, cap) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  cudaError_t e = cudaMallocHost(&p, cap);
+  if (getenv("AHFGPU_LOG"))
+    fprintf(stderr, "ahfgpu: page-locked result block of %zu bytes: %s\n", cap, cudaGetErrorString(e));
+  if (e != cudaSuccess) { cudaGetLastError(); return nullptr; }
   g_lent.push_back(HostBlock{p, cap});
   return p;
 }
@@ -666,6 +853,7 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
   }
   cudaStream_t st = g.stream;
   CK(cudaStreamSynchronize(0));
+  auto t0 = std::chrono::steady_clock::now();
   if (nh > 0) CK(cudaMemcpyAsync(r->halo, g.halo.p, nh * sizeof(ahfgpu_halo), cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(r->member_off, g.member_off.p, (nh + 1) * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(r->prof_off, g.prof_off.p, (nh + 1) * 8, cudaMemcpyDeviceToHost, st));
@@ -673,6 +861,7 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
   if (g.last_nbins)
     CK(cudaMemcpyAsync(r->prof, g.prof.p, g.last_nbins * AHFGPU_PROF_NFIELDS * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
+  g.last_stats.ms_d2h = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   r->stats = g.last_stats;
   return AHFGPU_OK;
 }
@@ -687,13 +876,20 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
   cudaStream_t st = g.stream;
   Plan pl;
   if ((rc = validate_and_plan(params, batch->off, batch->nhalo, pl))) return rc;
+  // FP32C on unit weights: the largest lists (one per class-2 CTA) start as
+  // soon as their particles are in, while the rest of the batch crosses the
+  // link.  (A weighted batch is checked as a whole before any launch.)
+  if (mode == AHFGPU_BATCHED_FP32C && !batch->w && pl.N >= kSplitMinParticles)
+    pl.split = std::min(pl.cls_begin[1], g.nsm * g.fp32c_bps[2]);
   ahfgpu_batch db;
-  if ((rc = copy_in(batch, &db, st))) return rc;
+  std::function<int()> stage = [&]() { return copy_in(batch, &db, pl, g.copy_stream); };
   ahfgpu_stats s{};
-  rc = run_device(params, &db, pl, mode, st, &s);
+  s.ms_plan = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  rc = run_device(params, &db, pl, mode, st, &s, &stage);
   if (rc) return rc;
   g.last_stats = s;
   if ((rc = ahfgpu_fetch_result(result))) return rc;
+  s.ms_d2h = g.last_stats.ms_d2h;
   s.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   result->stats = s;
   g.last_stats = s;
@@ -728,15 +924,15 @@ const char* ahfgpu_version(void) { return "ahfgpu 1.0 (sm_103a)"; }
 AHFGPU_API int ahfgpu_debug_halo_times(unsigned long long* out, long long nh) {
   if (!g.phase.p) return AHFGPU_ERR_STATE;
   cudaDeviceSynchronize();
-  cudaMemcpy(out, g.phase.as<unsigned long long>() + 16, (size_t)nh * 4 * 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(out, g.phase.as<unsigned long long>() + kPhaseSlots, (size_t)nh * 4 * 8, cudaMemcpyDeviceToHost);
   return AHFGPU_OK;
 }
 
 AHFGPU_API int ahfgpu_debug_phase(unsigned long long* out, int reset) {
   if (!g.phase.p) return AHFGPU_ERR_STATE;
   cudaDeviceSynchronize();
-  cudaMemcpy(out, g.phase.p, 16 * 8, cudaMemcpyDeviceToHost);
-  if (reset) cudaMemset(g.phase.p, 0, 16 * 8);
+  cudaMemcpy(out, g.phase.p, kPhaseSlots * 8, cudaMemcpyDeviceToHost);
+  if (reset) cudaMemset(g.phase.p, 0, kPhaseSlots * 8);
   return AHFGPU_OK;
 }
 #endif

@@ -58,7 +58,7 @@ struct Work {
   float *fdx, *fdy, *fdz; // FP32C: offsets from the centre
   float *fdxl, *fdyl, *fdzl;  // FP32C: low parts of the offsets
   float *fqh, *fql;       // FP32C: 1/d^2 as float-float
-  float4* rec;            // FP32C: per entry {x, y, z, vx} {vy, vz, gidx lo, gidx hi} (two float4)
+  float4* rec;            // FP32C: per entry {x, y, z, vx} {vy, vz, id lo, id hi} (two float4)
   uint8_t* flag;          // member (1) / removed (0) per sorted slot
   uint8_t* nflag;         // fixpoint flags of the next round
   double *prof_a, *prof_b, *prof_c, *prof_d;  // per-member profile arrays
@@ -67,7 +67,7 @@ struct Work {
   int stack_cap;
   // per-halo outputs (staging, packed afterwards)
   ahfgpu_halo* halo;      // [nhalo]
-  uint64_t* mem_stage;    // [N] kept gidx, at the halo's input offset
+  uint64_t* mem_stage;    // [N] kept ids (gidx[e], or e where gidx is NULL), at the halo's input offset
   double* prof_stage;     // [nbins_cap_total * NFIELDS]
   const uint64_t* prof_cap_off;  // [nhalo+1] staging row offsets
   // work queue / diagnostics
@@ -87,7 +87,9 @@ __host__ __device__ __forceinline__ uint64_t slot_base(uint64_t off, int64_t h) 
   return (off + 3ull * (uint64_t)h + 3ull) & ~3ull;
 }
 
-// Optional per-phase cycle counters (build with -DAHFGPU_PHASE_TIMERS).
+// Optional per-phase cycle counters (build with -DAHFGPU_PHASE_TIMERS):
+// kPhaseSlots counters, then per halo {start ns, end ns, SM cycles, SM id}.
+constexpr int kPhaseSlots = 32;
 #ifdef AHFGPU_PHASE_TIMERS
 #define PT_BEGIN long long _pt = clock64();
 #define PT_MARK(W, k)                                              \

@@ -6,21 +6,25 @@
 #ifndef AHFGPU_CLASS0_T
 #define AHFGPU_CLASS0_T 64
 #endif
+#ifndef AHFGPU_CLASS0_MINB
+#define AHFGPU_CLASS0_MINB 1
+#endif
 
 namespace ahfgpu {
 
 constexpr int kT0 = AHFGPU_CLASS0_T;
+constexpr int kMinB0 = AHFGPU_CLASS0_MINB;
 using SS0 = SortSmemT<512, 16>;
 
 void launch_fp32c_class0(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
-  halo_fp32c_kernel<kT0, SS0><<<grid, kT0, sizeof(F32Smem<SS0, kT0>), st>>>(P, B, W);
+  halo_fp32c_kernel<kT0, SS0, kMinB0><<<grid, kT0, sizeof(F32Smem<SS0, kT0>), st>>>(P, B, W);
 }
 
 int fp32c_occupancy_class0() {
   int nb = 0;
-  cudaFuncSetAttribute(halo_fp32c_kernel<kT0, SS0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(halo_fp32c_kernel<kT0, SS0, kMinB0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(F32Smem<SS0, kT0>));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<kT0, SS0>, kT0, sizeof(F32Smem<SS0, kT0>));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, halo_fp32c_kernel<kT0, SS0, kMinB0>, kT0, sizeof(F32Smem<SS0, kT0>));
   return nb;
 }
 

@@ -2199,6 +2199,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   float* vc2 = reinterpret_cast<float*>(W.prof_c + o);     // Vcirc2 per rank
   float* dr2 = vc2 + n2;                                   // dens_r2 per rank
   uint32_t* ent = reinterpret_cast<uint32_t*>(W.prof_d + o);
+  PT_T0;
   // ranks -> distances (binning_parameter needs them)
   {
     int carry = 0;
@@ -2222,6 +2223,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     }
     __syncthreads();
   }
+  PT_T(W, 16);
   // binning_parameter, src/libutility/specific.c:259-322 (exact distances)
   if (threadIdx.x == 0) {
     int nb = (int)(6.2 * (log10((double)n2)) - 3.5);
@@ -2250,6 +2252,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     S.edn[b] = dn;
   }
   __syncthreads();
+  PT_T(W, 17);
   const int nbins = S.bi[0];
   const float Hrv = (float)(P.Hubble * P.r_fac / P.v_fac);
   const int has_w = P.has_w;
@@ -2348,6 +2351,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     long long ex[4], tot[4], ps, pbs;
     int excnt, tn;
     float dp4[4], blockLast[4];
+    PT_T(W, 18);
     scan_bound(a, nm, any, lastm, -1, cD, -1, ex, tot, excnt, tn, dp4, ps, blockLast, pbs, S, par);
     const int rank0 = cr + excnt;
     // per-particle terms, thread totals; bin ends of this tile
@@ -2402,6 +2406,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         r++;
       }
     }
+    PT_T(W, 19);
     // channels needed only at bin ends: full scans in tiles with a bin end,
     // block totals otherwise
     const bool tile_end = __syncthreads_or(has_end ? 1 : 0) != 0;
@@ -2426,6 +2431,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
 #pragma unroll
       for (int j = 0; j < 11; j++) { pacc[5 + j] = ff_add(pacc[5 + j], fff(tg[j])); tgt[j] = 0.f; eg[j] = 0.f; }
     }
+    PT_T(W, 20);
     // most bound particle: FP32 screen against the warp's running minimum
     // (this tile included), FP64 energy of each candidate; the best per
     // thread is reduced over the block once, after the last tile
@@ -2450,6 +2456,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         }
       }
     }
+    PT_T(W, 21);
     // bin records at bin ends (cumulative values over the members so far)
     if (tile_end && has_end) {
       ff dp = {dp4[0], dp4[1]};
@@ -2509,6 +2516,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     for (int j = 0; j < 4; j++) cD[j] = blockLast[j];
     cr += tn;
     __syncthreads();
+    PT_T(W, 22);
   }
   if constexpr (SM::kStage > 0) cp_async_wait<0>();
   {
@@ -2543,20 +2551,13 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     __syncthreads();
   }
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
-#ifdef AHFGPU_PHASE_TIMERS
-  long long _pp = clock64();
-#endif
+  PT_T(W, 23);
   write_bin_rows(S.bins, S.edge, nbins, rows, true);
   __syncthreads();
-#ifdef AHFGPU_PHASE_TIMERS
-  if (threadIdx.x == 0 && W.phase) { long long t = clock64(); atomicAdd(&W.phase[8], (unsigned long long)(t - _pp)); _pp = t; }
-#endif
+  PT_T(W, 24);
   uint64_t i_r2 = find_max32(c, B, W, S, 0, 3, n2, nret);
   uint64_t i_rm = find_max32(c, B, W, S, 1, 1, n2, nret);
-#ifdef AHFGPU_PHASE_TIMERS
-  __syncthreads();
-  if (threadIdx.x == 0 && W.phase) { long long t = clock64(); atomicAdd(&W.phase[9], (unsigned long long)(t - _pp)); }
-#endif
+  PT_T(W, 25);
   if (threadIdx.x == 0) {
     double r2 = rank_dist64(c, B, W, kNignore + i_r2);
     double x_max = rank_dist64(c, B, W, kNignore + i_rm);
@@ -2586,6 +2587,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     hout.nbins = nbins;
     hout.flags |= AHFGPU_HALO_RAN_PROFILE;
   }
+  PT_T(W, 26);
   __syncthreads();
 }
 
@@ -2788,10 +2790,10 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g1));
     unsigned smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    W.phase[16 + 4 * h] = _g0;
-    W.phase[16 + 4 * h + 1] = g1;
-    W.phase[16 + 4 * h + 2] = (unsigned long long)(clock64() - _c0);
-    W.phase[16 + 4 * h + 3] = smid;
+    W.phase[kPhaseSlots + 4 * h] = _g0;
+    W.phase[kPhaseSlots + 4 * h + 1] = g1;
+    W.phase[kPhaseSlots + 4 * h + 2] = (unsigned long long)(clock64() - _c0);
+    W.phase[kPhaseSlots + 4 * h + 3] = smid;
   }
 #endif
   if (threadIdx.x == 0) {
@@ -2804,8 +2806,8 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
 
 static_assert(sizeof(ahfgpu_halo) % 8 == 0, "the halo record is cleared in 8-byte words");
 
-template <int T, class SS>
-__global__ void __launch_bounds__(T) halo_fp32c_kernel(DevParams P, DevBatch B, Work W) {
+template <int T, class SS, int MinB = 1>
+__global__ void __launch_bounds__(T, MinB) halo_fp32c_kernel(DevParams P, DevBatch B, Work W) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using SM = F32Smem<SS, T>;
   SM& S = *reinterpret_cast<SM*>(smem_raw);

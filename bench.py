@@ -388,13 +388,14 @@ def ours_arm(args, ws, rank, local):
         e2e_steps = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
         d2h = 0
-        lib_total, lib_dev = [], []
+        lib_total, lib_dev, lib_parts = [], [], []
         for _ in range(e2e_steps):
             rr = lib.construct_halos_raw(params, hb, mode)
             nk = rr.stats.n_kept
             d2h = nk * 8 + len(n_in) * (C.sizeof(abi.Halo) + 16) + 8 * 25 * int(res.prof_off[-1])
             lib_total.append(rr.stats.ms_total)
             lib_dev.append(rr.stats.ms_device)
+            lib_parts.append([getattr(rr.stats, k) for k in ("ms_plan", "ms_h2d", "ms_h2d_first", "ms_pack", "ms_d2h")])
             lib.free_result(rr)
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / e2e_steps
@@ -403,6 +404,9 @@ def ours_arm(args, ws, rank, local):
         e2e = {"value": total_parts / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "ms_per_step": dt * 1e3, "ms_in_library": float(np.mean(lib_total)),
                "ms_device": float(np.mean(lib_dev))}
+        for k, v in zip(("ms_plan", "ms_h2d", "ms_h2d_first", "ms_pack", "ms_d2h"), np.mean(lib_parts, axis=0)):
+            e2e[k] = float(v)
+        e2e["ms_per_call"] = [round(float(v), 2) for v in lib_total]
 
     cpu = None
     if rank == 0 and not args.no_cpu:

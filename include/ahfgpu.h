@@ -153,6 +153,11 @@ typedef struct {
   uint64_t n_launches;       /* kernels launched by the call                  */
   double   ms_device;        /* device time of the compute kernels (ms)       */
   double   ms_total;         /* wall time of the whole call (ms)              */
+  double   ms_plan;          /* host: checks, halo queue and size classes     */
+  double   ms_h2d;           /* host calls: input copies, first to last byte  */
+  double   ms_h2d_first;     /* host calls: until the largest lists are in    */
+  double   ms_pack;          /* device: result packing after the compute      */
+  double   ms_d2h;           /* host calls: result copies to the host         */
 } ahfgpu_stats;
 
 /* Library-owned result; release with ahfgpu_result_free().                  */

@@ -95,6 +95,31 @@ def test_device_api_equals_host_api(gpu):
     assert np.array_equal(dev.prof, host.prof)
 
 
+def test_fp32c_staged_copies_equal_device_api(gpu):
+    """Host FP32C calls of at least 2^22 particles copy the particles of the
+    largest lists first and launch them before the rest has arrived; the
+    result must be the one the device-pointer call gives on the same batch,
+    byte for byte."""
+    import torch
+    from ahf_gb300 import lib
+    params, L = _synthetic("cfg3", scale=0.02)
+    assert L.n >= 1 << 22
+    host = gpu.construct_halos(params, L, "batched_fp32c")
+    t = {"off": torch.as_tensor(L.off.astype(np.int64)).cuda()}
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        t[k] = torch.as_tensor(getattr(L, k)).cuda()
+    t["gidx"] = torch.as_tensor(L.gidx.astype(np.int64)).cuda()
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(L, k)).cuda()
+    torch.cuda.synchronize()
+    lib.construct_halos_device(params, lib.device_batch(t), "batched_fp32c")
+    dev = lib.fetch_result()
+    assert np.array_equal(dev.member, host.member)
+    assert np.array_equal(dev.member_off, host.member_off)
+    assert np.array_equal(dev.halo.view(np.uint8), host.halo.view(np.uint8))
+    assert np.array_equal(dev.prof, host.prof)
+
+
 def test_repeat_calls_are_deterministic(gpu):
     params, L = _synthetic("cfg3", scale=0.001, max_particles=20000)
     a = gpu.construct_halos(params, L, "batched_fp64")
