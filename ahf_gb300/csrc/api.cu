@@ -78,6 +78,10 @@ struct DBuf {
   template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+constexpr int kMaxParts = 5;   // queue parts of a staged host call
+// queue heads: [0] the FP64 forms, [2 + s] FP32C launch segment s
+constexpr int kQueueHeads = 2 + 3 * kMaxParts;
+
 struct Ctx {
   bool init = false;
   int device = -1;
@@ -85,12 +89,13 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev_cp0 = nullptr;
   int fp64_bps = 1, fp32c_bps[3] = {1, 1, 1};
-  // FP32C launches: one stream per (queue part, size class); part 0 is the
-  // queue prefix whose inputs the host path copies first
-  cudaStream_t seg_stream[2][3] = {};
-  cudaEvent_t ev_fork = nullptr, ev_join[2][3] = {};
+  // FP32C launches: one stream per (queue part, size class); the host path
+  // copies the inputs part by part, the largest lists first
+  cudaStream_t seg_stream[kMaxParts][3] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kMaxParts][3] = {};
   cudaStream_t copy_stream = nullptr;       // host-to-device input copies
-  cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_part[kMaxParts] = {};      // inputs of queue part p are in
+  cudaEvent_t ev_ids = nullptr;             // the ids (gidx) are in
   // inputs copied from the host (host API)
   DBuf in_off, in_x, in_y, in_z, in_vx, in_vy, in_vz, in_w, in_gidx, in_cx, in_cy, in_cz;
   // work space
@@ -268,7 +273,9 @@ struct Plan {
   uint64_t N = 0, maxn = 0, nbins_total = 0;
   std::vector<int32_t> queue;
   int cls_begin[4] = {0, 0, 0, 0};   // queue positions of the FP32C size classes (largest class first)
-  int split = 0;                     // FP32C: queue prefix [0, split) launched as a part of its own
+  // FP32C: queue positions ending parts 0..P-2 (increasing); part p is
+  // launched as soon as its inputs are in.  Empty: one part.
+  std::vector<int> cuts;
   std::vector<uint64_t> prof_cap_off;
 };
 
@@ -346,7 +353,7 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.prof_stage, std::max<uint64_t>(pl.nbins_total, 1) * AHFGPU_PROF_NFIELDS * 8);
   EN(g.prof_cap_off, (pl.nhalo + 1) * 8);
   EN(g.queue, std::max<int64_t>(pl.nhalo, 1) * 4);
-  EN(g.qhead, 64);
+  EN(g.qhead, kQueueHeads * 4);
   EN(g.counters, 64);
   EN(g.err, 64);
   EN(g.wred, 64);
@@ -359,18 +366,20 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
 }
 
 // One FP32C launch: the queue range [q0, q1) of one size class within one
-// queue part (part 0 = [0, split)), with its grid.
+// queue part, with its grid.
 struct Seg {
   int part, cls, q0, q1, grid;
 };
 
+int part_begin(const Plan& pl, int p) { return p == 0 ? 0 : pl.cuts[p - 1]; }
+int part_end(const Plan& pl, int p) { return p < (int)pl.cuts.size() ? pl.cuts[p] : (int)pl.nhalo; }
+
 std::vector<Seg> fp32c_segments(const Plan& pl) {
   std::vector<Seg> v;
-  for (int p = 0; p < 2; p++)
+  for (int p = 0; p <= (int)pl.cuts.size(); p++)
     for (int k = 0; k < 3; k++) {                 // queue segment k holds class 2-k
-      int q0 = pl.cls_begin[k], q1 = pl.cls_begin[k + 1];
-      if (p == 0) q1 = std::min(q1, pl.split);
-      else q0 = std::max(q0, pl.split);
+      int q0 = std::max(pl.cls_begin[k], part_begin(pl, p));
+      int q1 = std::min(pl.cls_begin[k + 1], part_end(pl, p));
       if (q1 <= q0) continue;
       int cls = 2 - k;
       v.push_back({p, cls, q0, q1, std::min(g.nsm * g.fp32c_bps[cls], q1 - q0)});
@@ -379,16 +388,18 @@ std::vector<Seg> fp32c_segments(const Plan& pl) {
 }
 
 // Runs the stage on a device batch.  Results stay in g.* buffers.  With a
-// staging hook (host path) the hook issues the input copies on
-// g.copy_stream after the small set-up copies, recording g.ev_in[0] once the
-// particles of the queue prefix [0, split) are in and g.ev_in[1] once all
-// are; each part's launches wait for its event only.
+// staging hook (host path), stage(p) issues the input copies of queue part
+// p on g.copy_stream and records g.ev_part[p] (stage(P): the ids, g.ev_ids);
+// it is called after the small set-up copies for part 0 and right before
+// the first launch of each later part, and each part's launches wait for
+// its own event only.
 int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl, ahfgpu_mode mode,
-               cudaStream_t st, ahfgpu_stats* stats, const std::function<int()>* stage = nullptr) {
+               cudaStream_t st, ahfgpu_stats* stats, const std::function<int(int)>* stage = nullptr) {
   int rc;
   if (mode != AHFGPU_PLAIN_FP64 && mode != AHFGPU_BATCHED_FP64 && mode != AHFGPU_BATCHED_FP32C)
     return fail(AHFGPU_ERR_INVALID, "unknown mode %d", (int)mode);
-  if (pl.split && mode != AHFGPU_BATCHED_FP32C) return fail(AHFGPU_ERR_STATE, "split queue outside FP32C");
+  if (!pl.cuts.empty() && mode != AHFGPU_BATCHED_FP32C) return fail(AHFGPU_ERR_STATE, "split queue outside FP32C");
+  if ((int)pl.cuts.size() >= kMaxParts) return fail(AHFGPU_ERR_STATE, "too many queue parts");
   const std::vector<Seg> segs = fp32c_segments(pl);
   int grid = g.nsm * g.fp64_bps;
   {
@@ -408,15 +419,17 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   }
   CK(cudaMemcpyAsync(g.prof_cap_off.p, pl.prof_cap_off.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(g.queue.p, pl.queue.data(), nh * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemsetAsync(g.qhead.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.qhead.p, 0, kQueueHeads * 4, st));
   CK(cudaMemsetAsync(g.counters.p, 0, 64, st));
   CK(cudaMemsetAsync(g.err.p, 0, 64, st));
   CK(cudaMemsetAsync(g.halo.p, 0, nh * sizeof(ahfgpu_halo), st));
+  int staged = 0;   // parts whose copies are issued
+  const int nparts = (int)pl.cuts.size() + 1;
   if (stage) {
-    if ((rc = (*stage)())) return rc;
+    if ((rc = (*stage)(staged++))) return rc;
     // the set-up work on this stream (weight check, device timer) waits for
-    // the inputs that the first launches read: all of them without a split
-    CK(cudaStreamWaitEvent(st, g.ev_in[pl.split ? 0 : 1], 0));
+    // the inputs of the first part (all of them without a split)
+    CK(cudaStreamWaitEvent(st, g.ev_part[0], 0));
   }
 
   DevParams P{};
@@ -508,12 +521,14 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
     launches++;
   } else {
     // size classes on streams of their own (larger classes at higher
-    // priority), queue part 0 before part 1; each segment has its own queue
-    // range, queue head and worklist region.  A part-1 launch takes SMs as
-    // the part-0 CTAs of its class run out of work and exit.
+    // priority), queue parts in order; each segment has its own queue
+    // range, queue head and worklist region.  A later part's launch takes
+    // SMs as the CTAs of the earlier parts run out of work and exit.
     CK(cudaEventRecord(g.ev_fork, st));
     int stack_base = 0, slot = 2;
     for (const Seg& sg : segs) {
+      while (stage && staged <= sg.part)
+        if ((rc = (*stage)(staged++))) return rc;
       Work Wc = W;
       Wc.queue = g.queue.as<int32_t>() + sg.q0;
       Wc.nqueue = sg.q1 - sg.q0;
@@ -522,7 +537,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
       stack_base += sg.grid;
       cudaStream_t cs = g.seg_stream[sg.part][sg.cls];
       CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
-      if (stage) CK(cudaStreamWaitEvent(cs, g.ev_in[sg.part], 0));
+      if (stage) CK(cudaStreamWaitEvent(cs, g.ev_part[sg.part], 0));
       launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
       CK(cudaEventRecord(g.ev_join[sg.part][sg.cls], cs));
       CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
@@ -537,7 +552,11 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   k_scan_counts<<<2, 1024, 0, st>>>(W.halo, nh, g.member_off.as<uint64_t>(), g.prof_off.as<uint64_t>());
   int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
   int mg = (int)std::max<uint64_t>(1, std::min<uint64_t>((pl.N + kPackChunk - 1) / kPackChunk, (uint64_t)g.nsm * 8));
-  if (stage) CK(cudaStreamWaitEvent(st, g.ev_in[2], 0));   // the ids come last
+  if (stage) {
+    while (staged <= nparts)   // the parts without launches, then the ids
+      if ((rc = (*stage)(staged++))) return rc;
+    CK(cudaStreamWaitEvent(st, g.ev_ids, 0));   // the ids come last
+  }
   k_pack_members<<<mg, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(), db->gidx,
                                       g.member.as<uint64_t>(), nh);
   k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
@@ -554,6 +573,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   CK(cudaMemcpyAsync(&derr, g.err.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (derr == kErrWorklist) return fail(AHFGPU_ERR_CAPACITY, "radial sort worklist overflow");
+  if (derr == kErrSortState) return fail(AHFGPU_ERR_CUDA, "radial sort: inconsistent bucket run (self-check)");
   if (derr) return fail(AHFGPU_ERR_CUDA, "device error code %d", derr);
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, g.ev0, g.ev1));
@@ -561,9 +581,9 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   CK(cudaEventElapsedTime(&ms, g.ev1, g.ev2));
   stats->ms_pack = ms;
   if (stage) {
-    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_in[2]));
+    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_ids));
     stats->ms_h2d = ms;
-    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_in[0]));
+    CK(cudaEventElapsedTime(&ms, g.ev_cp0, g.ev_part[0]));
     stats->ms_h2d_first = ms;
   }
   stats->n_kept = tails[0];
@@ -617,19 +637,27 @@ int ahfgpu_init(int device) {
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
+    // AHFGPU_CLASS_BPS="a,b,c" caps the resident CTAs per SM of each class
+    // (tuning runs)
+    if (const char* e = getenv("AHFGPU_CLASS_BPS")) {
+      int cap[3] = {0, 0, 0};
+      if (sscanf(e, "%d,%d,%d", &cap[0], &cap[1], &cap[2]) == 3 && cap[k] >= 1)
+        g.fp32c_bps[k] = std::min(g.fp32c_bps[k], cap[k]);
+    }
     // larger classes get higher priority: their CTAs are scheduled first and
     // the small-halo classes fill SMs as they free up
     int lo = 0, hi = 0;
     CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     int pr = k == 2 ? hi : (k == 1 ? (lo + hi) / 2 : lo);
-    for (int p = 0; p < 2; p++) {
+    for (int p = 0; p < kMaxParts; p++) {
       CK(cudaStreamCreateWithPriority(&g.seg_stream[p][k], cudaStreamNonBlocking, pr));
       CK(cudaEventCreateWithFlags(&g.ev_join[p][k], cudaEventDisableTiming));
     }
   }
   CK(cudaEventCreateWithFlags(&g.ev_fork, cudaEventDisableTiming));
   CK(cudaStreamCreateWithFlags(&g.copy_stream, cudaStreamNonBlocking));
-  for (int p = 0; p < 3; p++) CK(cudaEventCreate(&g.ev_in[p]));
+  for (int p = 0; p < kMaxParts; p++) CK(cudaEventCreate(&g.ev_part[p]));
+  CK(cudaEventCreate(&g.ev_ids));
   CK(cudaEventCreate(&g.ev2));
   CK(cudaEventCreate(&g.ev_cp0));
   CK(cudaGetLastError());
@@ -651,14 +679,15 @@ int ahfgpu_shutdown(void) {
                   &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.rec, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
                   &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
   for (DBuf* b : bufs) b->release();
-  for (int p = 0; p < 2; p++)
+  for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
       if (g.seg_stream[p][k]) cudaStreamDestroy(g.seg_stream[p][k]);
       if (g.ev_join[p][k]) cudaEventDestroy(g.ev_join[p][k]);
     }
   if (g.copy_stream) cudaStreamDestroy(g.copy_stream);
-  for (int p = 0; p < 3; p++)
-    if (g.ev_in[p]) cudaEventDestroy(g.ev_in[p]);
+  for (int p = 0; p < kMaxParts; p++)
+    if (g.ev_part[p]) cudaEventDestroy(g.ev_part[p]);
+  if (g.ev_ids) cudaEventDestroy(g.ev_ids);
   if (g.ev_fork) cudaEventDestroy(g.ev_fork);
   if (g.ev0) cudaEventDestroy(g.ev0);
   if (g.ev1) cudaEventDestroy(g.ev1);
@@ -695,85 +724,114 @@ int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batc
   return AHFGPU_OK;
 }
 
-// Host inputs -> device on stream cs, recording g.ev_in[0] once the
-// particles of the queue prefix [0, pl.split) are in, g.ev_in[1] once all
-// are and g.ev_in[2] after the ids (gidx), which only the final pack reads.
-// The prefix's particle ranges (merged where adjacent) go first, then the
-// gaps between them, so every particle crosses the link once.
-static int copy_in(const ahfgpu_batch* hb, ahfgpu_batch* db, const Plan& pl, cudaStream_t cs) {
-  int64_t nh = hb->nhalo;
-  uint64_t N = nh > 0 ? hb->off[nh] : 0;
-  int rc;
-  *db = *hb;
-  CK(cudaEventRecord(g.ev_cp0, cs));
-  if (nh == 0) {
-    for (int p = 0; p < 3; p++) CK(cudaEventRecord(g.ev_in[p], cs));
-    return AHFGPU_OK;
-  }
-  if (!hb->x || !hb->y || !hb->z || !hb->vx || !hb->vy || !hb->vz || !hb->cx || !hb->cy || !hb->cz)
-    return fail(AHFGPU_ERR_INVALID, "a required batch array is NULL");
+// Host inputs -> device on stream cs, part by part, issued by run_device
+// between its launches (issue(p) right before the first launch of queue part
+// p), so a part's kernels are queued as soon as its copies are.
+// g.ev_part[p] is recorded once the particles of part p are in; issue(P)
+// copies the ids (gidx), which only the final pack reads, and records
+// g.ev_ids.  The particle ranges of parts 0..P-2 (merged where adjacent) go
+// first; the last part is the gaps between them, so every particle crosses
+// the link once.
+struct Stager {
+  using Range = std::pair<uint64_t, uint64_t>;
   struct Arr {
     DBuf* buf;
     const void* src;
     size_t esize, count;
     const void** dst;
   };
-  Arr arr[12] = {{&g.in_off, hb->off, 8, (size_t)nh + 1, (const void**)&db->off},
-                 {&g.in_cx, hb->cx, 8, (size_t)nh, (const void**)&db->cx},
-                 {&g.in_cy, hb->cy, 8, (size_t)nh, (const void**)&db->cy},
-                 {&g.in_cz, hb->cz, 8, (size_t)nh, (const void**)&db->cz},
-                 {&g.in_x, hb->x, 4, N, (const void**)&db->x},
-                 {&g.in_y, hb->y, 4, N, (const void**)&db->y},
-                 {&g.in_z, hb->z, 4, N, (const void**)&db->z},
-                 {&g.in_vx, hb->vx, 4, N, (const void**)&db->vx},
-                 {&g.in_vy, hb->vy, 4, N, (const void**)&db->vy},
-                 {&g.in_vz, hb->vz, 4, N, (const void**)&db->vz},
-                 {&g.in_w, hb->w, 4, N, (const void**)&db->w},
-                 {&g.in_gidx, hb->gidx, 8, N, (const void**)&db->gidx}};
-  for (Arr& a : arr) {
-    if (!a.src) { *a.dst = nullptr; continue; }
-    if ((rc = a.buf->ensure(std::max<size_t>(a.esize * a.count, 8)))) return rc;
-    *a.dst = a.buf->p;
-  }
-  auto put = [&](const Arr& a, uint64_t lo, uint64_t hi) -> int {
+  const ahfgpu_batch* hb;
+  ahfgpu_batch* db;
+  const Plan& pl;
+  cudaStream_t cs;
+  uint64_t N = 0;
+  int P = 1;
+  Arr arr[12];
+  std::vector<Range> taken;   // ranges of parts 0..P-2, sorted
+
+  Stager(const ahfgpu_batch* hb_, ahfgpu_batch* db_, const Plan& pl_, cudaStream_t cs_)
+      : hb(hb_), db(db_), pl(pl_), cs(cs_) {}
+
+  int put(const Arr& a, uint64_t lo, uint64_t hi) {
     if (!a.src || hi <= lo) return AHFGPU_OK;
     cudaError_t e = cudaMemcpyAsync((char*)a.buf->p + lo * a.esize, (const char*)a.src + lo * a.esize,
                                     (hi - lo) * a.esize, cudaMemcpyHostToDevice, cs);
     if (e != cudaSuccess) return fail(AHFGPU_ERR_CUDA, "H2D copy failed: %s", cudaGetErrorString(e));
     return AHFGPU_OK;
-  };
-  for (int i = 0; i < 4; i++)
-    if ((rc = put(arr[i], 0, arr[i].count))) return rc;
-  // particle ranges of the prefix, in memory order, adjacent ones merged
-  std::vector<std::pair<uint64_t, uint64_t>> head;
-  head.reserve(pl.split);
-  for (int q = 0; q < pl.split; q++) {
-    int32_t h = pl.queue[q];
-    if (hb->off[h + 1] > hb->off[h]) head.push_back({hb->off[h], hb->off[h + 1]});
   }
-  std::sort(head.begin(), head.end());
-  std::vector<std::pair<uint64_t, uint64_t>> merged;
-  for (const auto& r : head) {
-    if (!merged.empty() && merged.back().second == r.first) merged.back().second = r.second;
-    else merged.push_back(r);
-  }
-  for (int i = 4; i < 11; i++)
-    for (const auto& r : merged)
-      if ((rc = put(arr[i], r.first, r.second))) return rc;
-  CK(cudaEventRecord(g.ev_in[0], cs));
-  for (int i = 4; i < 11; i++) {
-    uint64_t at = 0;
-    for (const auto& r : merged) {
-      if ((rc = put(arr[i], at, r.first))) return rc;
-      at = r.second;
+
+  int issue(int p) {
+    const int64_t nh = hb->nhalo;
+    int rc;
+    if (p == 0) {
+      *db = *hb;
+      P = (int)pl.cuts.size() + 1;
+      CK(cudaEventRecord(g.ev_cp0, cs));
+      if (nh > 0 &&
+          (!hb->x || !hb->y || !hb->z || !hb->vx || !hb->vy || !hb->vz || !hb->cx || !hb->cy || !hb->cz))
+        return fail(AHFGPU_ERR_INVALID, "a required batch array is NULL");
+      N = nh > 0 ? hb->off[nh] : 0;
+      const Arr init[12] = {{&g.in_off, hb->off, 8, (size_t)nh + 1, (const void**)&db->off},
+                            {&g.in_cx, hb->cx, 8, (size_t)nh, (const void**)&db->cx},
+                            {&g.in_cy, hb->cy, 8, (size_t)nh, (const void**)&db->cy},
+                            {&g.in_cz, hb->cz, 8, (size_t)nh, (const void**)&db->cz},
+                            {&g.in_x, hb->x, 4, N, (const void**)&db->x},
+                            {&g.in_y, hb->y, 4, N, (const void**)&db->y},
+                            {&g.in_z, hb->z, 4, N, (const void**)&db->z},
+                            {&g.in_vx, hb->vx, 4, N, (const void**)&db->vx},
+                            {&g.in_vy, hb->vy, 4, N, (const void**)&db->vy},
+                            {&g.in_vz, hb->vz, 4, N, (const void**)&db->vz},
+                            {&g.in_w, hb->w, 4, N, (const void**)&db->w},
+                            {&g.in_gidx, hb->gidx, 8, N, (const void**)&db->gidx}};
+      for (int i = 0; i < 12; i++) {
+        arr[i] = init[i];
+        if (nh == 0 || !arr[i].src) { *arr[i].dst = nullptr; continue; }
+        if ((rc = arr[i].buf->ensure(std::max<size_t>(arr[i].esize * arr[i].count, 8)))) return rc;
+        *arr[i].dst = arr[i].buf->p;
+      }
+      if (nh > 0)
+        for (int i = 0; i < 4; i++)
+          if ((rc = put(arr[i], 0, arr[i].count))) return rc;
     }
-    if ((rc = put(arr[i], at, N))) return rc;
+    if (nh == 0) {
+      CK(cudaEventRecord(p < P ? g.ev_part[p] : g.ev_ids, cs));
+      return AHFGPU_OK;
+    }
+    if (p + 1 < P) {
+      std::vector<Range> head;
+      for (int q = part_begin(pl, p); q < part_end(pl, p); q++) {
+        int32_t h = pl.queue[q];
+        if (hb->off[h + 1] > hb->off[h]) head.push_back({hb->off[h], hb->off[h + 1]});
+      }
+      std::sort(head.begin(), head.end());
+      std::vector<Range> merged;
+      for (const Range& r : head) {
+        if (!merged.empty() && merged.back().second == r.first) merged.back().second = r.second;
+        else merged.push_back(r);
+      }
+      for (int i = 4; i < 11; i++)
+        for (const Range& r : merged)
+          if ((rc = put(arr[i], r.first, r.second))) return rc;
+      CK(cudaEventRecord(g.ev_part[p], cs));
+      taken.insert(taken.end(), merged.begin(), merged.end());
+    } else if (p + 1 == P) {
+      std::sort(taken.begin(), taken.end());
+      for (int i = 4; i < 11; i++) {
+        uint64_t at = 0;
+        for (const Range& r : taken) {
+          if ((rc = put(arr[i], at, r.first))) return rc;
+          at = r.second;
+        }
+        if ((rc = put(arr[i], at, N))) return rc;
+      }
+      CK(cudaEventRecord(g.ev_part[p], cs));
+    } else {
+      if ((rc = put(arr[11], 0, N))) return rc;
+      CK(cudaEventRecord(g.ev_ids, cs));
+    }
+    return AHFGPU_OK;
   }
-  CK(cudaEventRecord(g.ev_in[1], cs));
-  if ((rc = put(arr[11], 0, N))) return rc;
-  CK(cudaEventRecord(g.ev_in[2], cs));
-  return AHFGPU_OK;
-}
+};
 
 // Result arrays live in page-locked host blocks (device-to-host copies run
 // at link speed instead of through a bounce buffer).  A block handed out in
@@ -879,10 +937,16 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
   // FP32C on unit weights: the largest lists (one per class-2 CTA) start as
   // soon as their particles are in, while the rest of the batch crosses the
   // link.  (A weighted batch is checked as a whole before any launch.)
-  if (mode == AHFGPU_BATCHED_FP32C && !batch->w && pl.N >= kSplitMinParticles)
-    pl.split = std::min(pl.cls_begin[1], g.nsm * g.fp32c_bps[2]);
+  if (mode == AHFGPU_BATCHED_FP32C && !batch->w && pl.N >= kSplitMinParticles) {
+    // parts of 1/8, 1/8, 1/4 and 1/2 of the class-2 CTAs' first lists, then
+    // the rest: the first SMs start after a small fraction of the copy
+    const int K = std::min(pl.cls_begin[1], g.nsm * g.fp32c_bps[2]);
+    for (int c : {K / 8, K / 4, K / 2, K})
+      if (c > 0 && (pl.cuts.empty() || c > pl.cuts.back())) pl.cuts.push_back(c);
+  }
   ahfgpu_batch db;
-  std::function<int()> stage = [&]() { return copy_in(batch, &db, pl, g.copy_stream); };
+  Stager stager(batch, &db, pl, g.copy_stream);
+  std::function<int(int)> stage = [&](int p) { return stager.issue(p); };
   ahfgpu_stats s{};
   s.ms_plan = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   rc = run_device(params, &db, pl, mode, st, &s, &stage);

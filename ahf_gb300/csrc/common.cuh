@@ -20,7 +20,7 @@ constexpr int kMaxBins = 64;         // nbins = 6.2 log10(n) - 3.5 < 64 for n < 
 constexpr int kMaxFixRounds = 4096;  // cap of the bulk-velocity fixpoint
 
 // device-side error codes (written to Work::err, read by the host)
-enum : int { kErrNone = 0, kErrFixpoint = 1, kErrSortDepth = 2, kErrWorklist = 3 };
+enum : int { kErrNone = 0, kErrFixpoint = 1, kErrSortDepth = 2, kErrWorklist = 3, kErrSortState = 4 };
 
 struct DevParams {
   double VescTune;

@@ -2274,6 +2274,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   ff pacc[16];
 #pragma unroll
   for (int j = 0; j < 16; j++) pacc[j] = ffz();
+  bool pend = false;   // pacc holds tiles not folded yet (uniform)
   // most bound particle, per thread: the warp's running FP32 minimum as the
   // screen, FP64 energies of the candidates; one block reduction at the end
   float pEmin = 3.0e38f;
@@ -2414,15 +2415,18 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     float eg[11], tgt[11];
     if (tile_end) {
       // everything before this tile into the carries, then this tile's scans
-      ff ptot[16];
-      breduce_ff<16>(pacc, ptot, S.scan);
+      if (pend) {
+        ff ptot[16];
+        breduce_ff<16>(pacc, ptot, S.scan);
 #pragma unroll
-      for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], ptot[j]);
-      cU = ff_add(cU, ptot[4]);
+        for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], ptot[j]);
+        cU = ff_add(cU, ptot[4]);
 #pragma unroll
-      for (int j = 0; j < 11; j++) cgc[j] = ff_add(cgc[j], ptot[5 + j]);
+        for (int j = 0; j < 11; j++) cgc[j] = ff_add(cgc[j], ptot[5 + j]);
 #pragma unroll
-      for (int j = 0; j < 16; j++) pacc[j] = ffz();
+        for (int j = 0; j < 16; j++) pacc[j] = ffz();
+        pend = false;
+      }
       bscan_ff<5>(af5, ef5, tf5, S.scan);
       bscan_f<11>(tg, eg, tgt, S.scan);
     } else {
@@ -2430,6 +2434,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       for (int j = 0; j < 5; j++) { pacc[j] = ff_add(pacc[j], af5[j]); tf5[j] = ffz(); ef5[j] = ffz(); }
 #pragma unroll
       for (int j = 0; j < 11; j++) { pacc[5 + j] = ff_add(pacc[5 + j], fff(tg[j])); tgt[j] = 0.f; eg[j] = 0.f; }
+      pend = true;
     }
     PT_T(W, 20);
     // most bound particle: FP32 screen against the warp's running minimum
@@ -2519,7 +2524,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     PT_T(W, 22);
   }
   if constexpr (SM::kStage > 0) cp_async_wait<0>();
-  {
+  if (pend) {
     ff ptot[16];
     breduce_ff<16>(pacc, ptot, S.scan);
 #pragma unroll
@@ -2655,10 +2660,10 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
   float lim[3];
   keys32(c, B, W, P, S, lim);
   PT_MARK(W, 0);
-  bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.s, c.n, stack, W.stack_cap, S.sort);
+  const int src = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.s, c.n, stack, W.stack_cap, S.sort);
   PT_MARK(W, 1);
-  if (!ok) {
-    if (threadIdx.x == 0) { atomicExch(W.err, kErrWorklist); W.halo[h] = hout; }
+  if (src != kErrNone) {
+    if (threadIdx.x == 0) { atomicExch(W.err, src); W.halo[h] = hout; }
     __syncthreads();
     return;
   }

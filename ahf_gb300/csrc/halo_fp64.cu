@@ -977,10 +977,10 @@ __device__ void process_halo(int h, const DevParams& P, const DevBatch& B, const
     return;
   }
   compute_keys(c, B, W);
-  bool ok = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.o, c.n, stack, W.stack_cap, S.sort);
-  if (!ok) {
+  const int src = radial_sort(W.keyA, W.idxA, W.keyB, W.idxB, c.o, c.n, stack, W.stack_cap, S.sort);
+  if (src != kErrNone) {
     if (threadIdx.x == 0) {
-      atomicExch(W.err, kErrWorklist);
+      atomicExch(W.err, src);
       W.halo[h] = hout;   // npart 0: nothing is packed for this halo
     }
     __syncthreads();

@@ -40,7 +40,8 @@ struct SortSmemT {
   uint64_t red_u64[64];
   int sp;                 // worklist depth
   int seg_lo, seg_hi;     // current run of buckets
-  int flag;
+  uint32_t run_lo, run_hi;  // its slot range (written by thread 0 only)
+  int flag;               // 0, or the kErr* code that ended the sort
   int crowd;              // chunk: some bin too full for an insertion sort
 };
 using SortSmem = SortSmemT<kChunk, kSortBuckets>;
@@ -197,18 +198,19 @@ static __device__ void smem_sort_chunk(const uint64_t* ks, const uint32_t* is, u
 }
 
 // Sort (keyA, idxA)[o, o+n) in place by (key, slot).  Uses (keyB, idxB) and
-// the CTA's worklist `stack` (capacity cap) as scratch.  Returns false when
-// the worklist overflows (the caller reports kErrWorklist).
+// the CTA's worklist `stack` (capacity cap) as scratch.  Returns kErrNone, or
+// kErrWorklist when the worklist overflows, or kErrSortState when a bucket
+// run is inconsistent with its pass (the run is then skipped, not sorted).
 template <class SS>
-static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
+static __device__ int radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint64_t o,
                                    uint64_t n, uint4* stack, int cap, SS& S) {
   constexpr int kChunk = SS::kCh;
   constexpr int kHalfChunk = SS::kCh / 2;
   constexpr int kSortBuckets = SS::kNb;
-  if (n <= 1) return true;
+  if (n <= 1) return kErrNone;
   if (n <= (uint64_t)kChunk) {
     smem_sort_chunk(keyA, idxA, keyA, idxA, o, (int)n, S);
-    return true;
+    return kErrNone;
   }
   // worklist entry: x = lo(low 32), y = lo(high 32), z = count, w = src(bit0) | by_slot(bit1)
   if (threadIdx.x == 0) {
@@ -346,7 +348,7 @@ static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* key
         if (size0 > (uint32_t)kHalfChunk) {
           // big bucket: push (data now in the other buffer)
           if (S.sp >= cap) {
-            S.flag = 1;
+            S.flag = kErrWorklist;
           } else {
             uint64_t blo = lo + start;
             stack[S.sp] = make_uint4((uint32_t)blo, (uint32_t)(blo >> 32), size0,
@@ -366,24 +368,28 @@ static __device__ bool radial_sort(uint64_t* keyA, uint32_t* idxA, uint64_t* key
           S.seg_hi = b1;
         }
         S.seg_lo = b1;
-        // stash run bounds in red_u64
-        S.red_u64[0] = start;
-        S.red_u64[1] = S.hist[b1 - 1];
+        // the run's slots; fields of their own: the chunk sort below reuses
+        // every scratch array before all warps have read its bounds
+        const uint32_t end = S.hist[b1 - 1];
+        S.run_lo = start;
+        S.run_hi = end;
+        if (S.seg_hi >= 0 && (end < start || end > cnt || end - start > (uint32_t)kChunk))
+          S.flag = kErrSortState;
       }
       __syncthreads();
       if (S.flag) break;
       if (S.seg_hi >= 0) {
-        uint64_t s0 = S.red_u64[0], s1 = S.red_u64[1];
-        int c = (int)(s1 - s0);
+        const uint32_t s0 = S.run_lo, s1 = S.run_hi;
+        const int c = (int)(s1 - s0);
         if (c > 0) smem_sort_chunk(kd, id, keyA, idxA, lo + s0, c, S);
       }
       __syncthreads();
     }
     __syncthreads();
   }
-  bool ok = S.flag == 0;
+  const int rc = S.flag;
   __syncthreads();
-  return ok;
+  return rc;
 }
 
 }  // namespace ahfgpu

@@ -281,6 +281,18 @@ def ours_arm(args, ws, rank, local):
     t["gidx"] = lists.gidx
     for k in ("cx", "cy", "cz"):
         t[k] = torch.as_tensor(getattr(lists, k)).cuda()
+    # page-locked host copies of the inputs for the e2e leg, made first as a
+    # caller's particle arrays would be (they exist before the stage runs)
+    host = {}
+    if not args.no_e2e:
+        for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
+            v = getattr(lists, k)
+            if v is None:
+                host[k] = None
+                continue
+            hp = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+            hp.copy_(v)
+            host[k] = hp
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
     db = lib.device_batch(t)
@@ -360,15 +372,6 @@ def ours_arm(args, ws, rank, local):
     # e2e through the host API with pinned buffers
     e2e = None
     if not args.no_e2e:
-        host = {}
-        for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
-            v = getattr(lists, k)
-            if v is None:
-                host[k] = None
-                continue
-            hp = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
-            hp.copy_(v)
-            host[k] = hp
         hb = abi.Batch()
         off_np = np.ascontiguousarray(lists.off.astype(np.uint64))
         cen = {k: np.ascontiguousarray(getattr(lists, k)) for k in ("cx", "cy", "cz")}
