@@ -78,7 +78,7 @@ struct DBuf {
   template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
-constexpr int kMaxParts = 5;   // queue parts of a staged host call
+constexpr int kMaxParts = 16;  // queue parts of a staged host call
 // queue heads: [0] the FP64 forms, [2 + s] FP32C launch segment s
 constexpr int kQueueHeads = 2 + 3 * kMaxParts;
 
@@ -938,11 +938,17 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
   // soon as their particles are in, while the rest of the batch crosses the
   // link.  (A weighted batch is checked as a whole before any launch.)
   if (mode == AHFGPU_BATCHED_FP32C && !batch->w && pl.N >= kSplitMinParticles) {
-    // parts of 1/8, 1/8, 1/4 and 1/2 of the class-2 CTAs' first lists, then
-    // the rest: the first SMs start after a small fraction of the copy
-    const int K = std::min(pl.cls_begin[1], g.nsm * g.fp32c_bps[2]);
-    for (int c : {K / 8, K / 4, K / 2, K})
-      if (c > 0 && (pl.cuts.empty() || c > pl.cuts.back())) pl.cuts.push_back(c);
+    // the class-2 lists in parts that double in size (the first 1/8 of one
+    // list per class-2 CTA), then the small classes as the gaps between
+    // them: the particles cross the link in the order the SMs take them
+    const int n2 = pl.cls_begin[1];
+    const int K = g.nsm * g.fp32c_bps[2];
+    for (int c = std::max(1, K / 8); ; c *= 2) {
+      const int cut = std::min(c, n2);
+      if (cut > 0 && (pl.cuts.empty() || cut > pl.cuts.back())) pl.cuts.push_back(cut);
+      if (cut >= n2 || (int)pl.cuts.size() + 1 >= kMaxParts) break;
+    }
+    if (!pl.cuts.empty() && pl.cuts.back() < n2 && (int)pl.cuts.size() + 1 < kMaxParts) pl.cuts.push_back(n2);
   }
   ahfgpu_batch db;
   Stager stager(batch, &db, pl, g.copy_stream);
