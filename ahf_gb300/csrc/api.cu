@@ -15,6 +15,7 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include "common.cuh"
 
@@ -25,6 +26,7 @@ int fp64_max_blocks_per_sm();
 void launch_fp32c(int cls, const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st);
 int fp32c_max_blocks_per_sm(int cls);
 uint64_t fp32c_class_max(int cls);
+void fp32c_set_class_max(uint64_t a, uint64_t b);
 void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
 }  // namespace ahfgpu
 
@@ -89,6 +91,11 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev_cp0 = nullptr;
   int fp64_bps = 1, fp32c_bps[3] = {1, 1, 1};
+  // FP32C size-class tuning of this device (defaults, the per-GPU tuning
+  // cache written by ahf_gb300.autotune, then environment overrides)
+  std::string tune_key, tune_source = "default";
+  uint64_t tune_class_max[2] = {512, 16384};
+  int tune_bps_cap[3] = {0, 0, 0};
   // FP32C launches: one stream per (queue part, size class); the host path
   // copies the inputs part by part, the largest lists first
   cudaStream_t seg_stream[kMaxParts][3] = {};
@@ -598,6 +605,77 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   return AHFGPU_OK;
 }
 
+void library_anchor() {}
+
+// The tuning cache: a JSON object keyed by "<device name>|<SMs>|<cc>", each
+// value {"class_max": [a, b], "class_bps": [c0, c1, c2]} (written by
+// python -m ahf_gb300.autotune).  Path: AHFGPU_TUNE_CACHE, else
+// tune_cache.json beside this library.
+std::string tune_cache_path() {
+  if (const char* e = getenv("AHFGPU_TUNE_CACHE")) return e;
+  Dl_info info;
+  if (dladdr((void*)&library_anchor, &info) && info.dli_fname) {
+    std::string f = info.dli_fname;
+    size_t k = f.find_last_of('/');
+    return (k == std::string::npos ? std::string(".") : f.substr(0, k)) + "/tune_cache.json";
+  }
+  return "tune_cache.json";
+}
+
+void load_tuning(const cudaDeviceProp& prop) {
+  char key[320];
+  snprintf(key, sizeof key, "%s|%d|%d.%d", prop.name, prop.multiProcessorCount, prop.major, prop.minor);
+  g.tune_key = key;
+  g.tune_source = "default";
+  g.tune_class_max[0] = 512; g.tune_class_max[1] = 16384;
+  for (int k = 0; k < 3; k++) g.tune_bps_cap[k] = 0;
+  const std::string path = tune_cache_path();
+  if (FILE* f = fopen(path.c_str(), "rb")) {
+    std::string js;
+    char buf[4096];
+    size_t r;
+    while ((r = fread(buf, 1, sizeof buf, f)) > 0 && js.size() < (1u << 20)) js.append(buf, r);
+    fclose(f);
+    size_t at = js.find(std::string("\"") + key + "\"");
+    if (at != std::string::npos) {
+      size_t end = js.find('}', at);
+      std::string obj = js.substr(at, end == std::string::npos ? std::string::npos : end - at);
+      unsigned long long a = 0, b = 0;
+      int c0 = 0, c1 = 0, c2 = 0;
+      size_t m = obj.find("\"class_max\"");
+      size_t q = m == std::string::npos ? m : obj.find('[', m);
+      if (q != std::string::npos && sscanf(obj.c_str() + q, "[ %llu , %llu", &a, &b) == 2 && a >= 1 && b >= a) {
+        g.tune_class_max[0] = a; g.tune_class_max[1] = b;
+        g.tune_source = path;
+      }
+      m = obj.find("\"class_bps\"");
+      q = m == std::string::npos ? m : obj.find('[', m);
+      if (q != std::string::npos && sscanf(obj.c_str() + q, "[ %d , %d , %d", &c0, &c1, &c2) == 3) {
+        g.tune_bps_cap[0] = c0; g.tune_bps_cap[1] = c1; g.tune_bps_cap[2] = c2;
+        g.tune_source = path;
+      }
+    }
+  }
+  // environment overrides (tuning runs)
+  if (const char* e = getenv("AHFGPU_CLASS_MAX")) {
+    unsigned long long a = 0, b = 0;
+    if (sscanf(e, "%llu,%llu", &a, &b) == 2 && a >= 1 && b >= a) {
+      g.tune_class_max[0] = a; g.tune_class_max[1] = b;
+      g.tune_source = "environment";
+    }
+  }
+  if (const char* e = getenv("AHFGPU_CLASS_BPS")) {
+    int c[3] = {0, 0, 0};
+    if (sscanf(e, "%d,%d,%d", &c[0], &c[1], &c[2]) == 3) {
+      for (int k = 0; k < 3; k++) g.tune_bps_cap[k] = c[k];
+      g.tune_source = "environment";
+    }
+  }
+  fp32c_set_class_max(g.tune_class_max[0], g.tune_class_max[1]);
+  g.tune_class_max[0] = fp32c_class_max(0);
+  g.tune_class_max[1] = fp32c_class_max(1);
+}
+
 void fill_dres(ahfgpu_result* r) {
   memset(r, 0, sizeof(*r));
   r->nhalo = g.last_nhalo;
@@ -635,15 +713,10 @@ int ahfgpu_init(int device) {
   CK(cudaEventCreate(&g.ev0));
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
+  load_tuning(prop);
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
-    // AHFGPU_CLASS_BPS="a,b,c" caps the resident CTAs per SM of each class
-    // (tuning runs)
-    if (const char* e = getenv("AHFGPU_CLASS_BPS")) {
-      int cap[3] = {0, 0, 0};
-      if (sscanf(e, "%d,%d,%d", &cap[0], &cap[1], &cap[2]) == 3 && cap[k] >= 1)
-        g.fp32c_bps[k] = std::min(g.fp32c_bps[k], cap[k]);
-    }
+    if (g.tune_bps_cap[k] >= 1) g.fp32c_bps[k] = std::min(g.fp32c_bps[k], g.tune_bps_cap[k]);
     // larger classes get higher priority: their CTAs are scheduled first and
     // the small-halo classes fill SMs as they free up
     int lo = 0, hi = 0;
@@ -988,6 +1061,22 @@ int ahfgpu_last_error(char* buf, size_t len) {
 }
 
 const char* ahfgpu_version(void) { return "ahfgpu 1.0 (sm_103a)"; }
+
+int ahfgpu_tuning(char* buf, size_t len) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  char tmp[1024];
+  snprintf(tmp, sizeof tmp,
+           "{\"key\": \"%s\", \"source\": \"%s\", \"class_max\": [%llu, %llu], \"class_bps\": [%d, %d, %d]}",
+           g.tune_key.c_str(), g.tune_source.c_str(), (unsigned long long)g.tune_class_max[0],
+           (unsigned long long)g.tune_class_max[1], g.fp32c_bps[0], g.fp32c_bps[1], g.fp32c_bps[2]);
+  if (buf && len) {
+    size_t n = std::min(len - 1, strlen(tmp));
+    memcpy(buf, tmp, n);
+    buf[n] = 0;
+  }
+  return AHFGPU_OK;
+}
 
 #ifdef AHFGPU_PHASE_TIMERS
 // instrumented builds: per-phase SM cycles summed over the last call's CTAs

@@ -17,21 +17,17 @@ int fp32c_occupancy_class0();
 int fp32c_occupancy_class1();
 int fp32c_occupancy_class2();
 
-// Largest list of classes 0 and 1.  AHFGPU_CLASS_MAX="a,b" overrides them
-// (tuning runs); read once.
-uint64_t fp32c_class_max(int cls) {
-  static uint64_t lim[2] = {0, 0};
-  if (lim[0] == 0) {
-    uint64_t a = 512, b = 16384;
-    if (const char* e = getenv("AHFGPU_CLASS_MAX")) {
-      unsigned long long x = 0, y = 0;
-      if (sscanf(e, "%llu,%llu", &x, &y) == 2 && x >= 1 && x <= 512 && y >= x) { a = x; b = y; }
-    }
-    lim[1] = b;
-    lim[0] = a;
-  }
-  return cls == 0 ? lim[0] : cls == 1 ? lim[1] : ~0ull;
+// Largest list of classes 0 and 1 (class 0 is bounded by its 512-pair
+// shared-memory sort).  Set once per device by the tuning at ahfgpu_init.
+static uint64_t g_class_max[2] = {512, 16384};
+
+void fp32c_set_class_max(uint64_t a, uint64_t b) {
+  a = a < 1 ? 1 : (a > 512 ? 512 : a);
+  g_class_max[0] = a;
+  g_class_max[1] = b < a ? a : b;
 }
+
+uint64_t fp32c_class_max(int cls) { return cls == 0 ? g_class_max[0] : cls == 1 ? g_class_max[1] : ~0ull; }
 
 void launch_fp32c(int cls, const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {
   if (cls == 0) launch_fp32c_class0(P, B, W, grid, st);

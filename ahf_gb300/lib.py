@@ -21,7 +21,7 @@ LIB_PATH = os.environ.get("AHFGPU_LIB", os.path.join(HERE, "libahfgpu.so"))
 
 SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
-    "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version",
+    "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
 ]
 
 
@@ -60,6 +60,8 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_last_error.restype = C.c_int
     lib.ahfgpu_version.argtypes = []
     lib.ahfgpu_version.restype = C.c_char_p
+    lib.ahfgpu_tuning.argtypes = [C.c_char_p, C.c_size_t]
+    lib.ahfgpu_tuning.restype = C.c_int
     _lib = lib
     return lib
 
@@ -162,3 +164,12 @@ def fetch_result() -> HostResult:
 
 def version() -> str:
     return load().ahfgpu_version().decode()
+
+
+def tuning(device: int = 0) -> dict:
+    """The FP32C size-class tuning in effect on the device (see ahfgpu_tuning)."""
+    import json
+    init(device)
+    buf = C.create_string_buffer(1024)
+    check(load().ahfgpu_tuning(buf, len(buf)))
+    return json.loads(buf.value.decode())

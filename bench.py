@@ -327,6 +327,9 @@ def ours_arm(args, ws, rank, local):
     value = total_parts / (ms_max / 1e3)
     res = lib.fetch_result()
     stats = r.stats
+    tuning = {k: v for k, v in lib.tuning(local).items() if k in ("class_max", "class_bps", "source")}
+    if tuning.get("source", "").endswith(".json"):
+        tuning["source"] = os.path.basename(tuning["source"])
     headline_stats = {"replay_halos": int(stats.n_replay_halos), "key_ties": int(stats.n_key_ties),
                       "retests": int(stats.n_retest), "fp64_halos": int(stats.n_fp64_halos)}
     balg = alg_bytes(n_in, res.halo, lists.w is not None)
@@ -430,7 +433,8 @@ def ours_arm(args, ws, rank, local):
                                f"float32 pos/vel, 64-bit ids, equal masses" + (" (two species)" if args.multimass else ""),
                    "form": mode, "n_halos": int(len(n_in)), "n_particles": N, "n_kept": int(stats.n_kept),
                    "scale": args.scale, "l2": "inputs (%.1f GB) larger than L2 (129 MB): no flush" % (N * 32 / 1e9),
-                   "parallelism": f"{ws} independent replica(s), haloes sharded by rank"},
+                   "parallelism": f"{ws} independent replica(s), haloes sharded by rank",
+                   "tuning": tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kname,

@@ -212,6 +212,13 @@ AHFGPU_API int ahfgpu_last_error(char *buf, size_t len);
 
 AHFGPU_API const char *ahfgpu_version(void);
 
+/* The FP32C size-class tuning in effect on the initialised device, as JSON:
+ * {"key": "<name>|<SMs>|<cc>", "source": <cache path|"default"|"environment">,
+ *  "class_max": [a, b], "class_bps": [c0, c1, c2]}.  Tuning comes from the
+ * per-GPU cache written by `python -m ahf_gb300.autotune` (tune_cache.json
+ * beside the library, or AHFGPU_TUNE_CACHE).  Returns AHFGPU_OK.           */
+AHFGPU_API int ahfgpu_tuning(char *buf, size_t len);
+
 /* ---- no-allocation variant ----------------------------------------------
  * No counterpart in the reference (AHF has no GPU path).  For callers that
  * cannot allocate device memory (a CUDA-graph capture of a larger pipeline,

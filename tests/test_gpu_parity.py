@@ -210,3 +210,29 @@ def test_fp32c_exact_paths_match_oracle(gpu, oracle_built, monkeypatch, hook):
             # resolution confirms each, so no more iterations are replayed
             # whole than without the hook
             assert got.stats["n_fp64_halos"] == plain.stats["n_fp64_halos"]
+
+
+def test_tuning_cache_is_read(gpu, oracle_built, tmp_path, monkeypatch):
+    """ahfgpu_init applies the per-GPU tuning cache (class limits and CTAs per
+    SM of class 0); a tuned split keeps the reference's kept lists."""
+    import json
+    key = gpu.tuning()["key"]
+    path = tmp_path / "tune_cache.json"
+    path.write_text(json.dumps({key: {"class_max": [200, 6000], "class_bps": [2, 0, 0]}}))
+    monkeypatch.delenv("AHFGPU_CLASS_MAX", raising=False)
+    monkeypatch.delenv("AHFGPU_CLASS_BPS", raising=False)
+    monkeypatch.setenv("AHFGPU_TUNE_CACHE", str(path))
+    gpu.shutdown()
+    gpu.init(0)
+    try:
+        t = gpu.tuning()
+        assert t["class_max"] == [200, 6000] and t["source"] == str(path) and t["class_bps"][0] <= 2
+        params, L = _synthetic("cfg3", scale=0.002, max_particles=60000)
+        exp = oracle_built.run_oracle(params, L, 0)
+        got = gpu.construct_halos(params, L, "batched_fp32c")
+        bad = compare_fp32c(got, exp)
+        assert not bad, bad
+    finally:
+        monkeypatch.delenv("AHFGPU_TUNE_CACHE")
+        gpu.shutdown()
+        gpu.init(0)
