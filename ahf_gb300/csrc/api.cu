@@ -94,6 +94,12 @@ struct Ctx {
   // FP32C size-class tuning of this device (defaults, the per-GPU tuning
   // cache written by ahf_gb300.autotune, then environment overrides)
   std::string tune_key, tune_source = "default";
+  // device-resident calls: the launch sequence as a CUDA graph, re-launched
+  // while the launches (kernels, grids, arguments) stay the same
+  bool use_graph = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<unsigned char> graph_sig;
+  uint64_t graph_launches = 0, graph_replays = 0;
   uint64_t tune_class_max[2] = {512, 16384};
   int tune_bps_cap[3] = {0, 0, 0};
   // FP32C launches: one stream per (queue part, size class); the host path
@@ -439,7 +445,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
     CK(cudaStreamWaitEvent(st, g.ev_part[0], 0));
   }
 
-  DevParams P{};
+  DevParams P;
+  memset(&P, 0, sizeof P);   // padding too: the struct is part of the graph signature
   P.VescTune = prm->VescTune;
   P.v2_tune = prm->VescTune * prm->VescTune;
   P.MINPART = prm->MINPART;
@@ -475,7 +482,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
     if (!(bound < 4503599627370496.0)) P.force_serial = 1;   // 2^52
   }
 
-  DevBatch B{};
+  DevBatch B;
+  memset(&B, 0, sizeof B);
   B.nhalo = nh;
   B.off = db->off;
   B.x = db->x; B.y = db->y; B.z = db->z;
@@ -484,7 +492,8 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   B.gidx = nullptr;   // the kernels stage entry indices; the pack maps them to ids
   B.cx = db->cx; B.cy = db->cy; B.cz = db->cz;
 
-  Work W{};
+  Work W;
+  memset(&W, 0, sizeof W);
   W.keyA = g.keyA.as<uint64_t>(); W.keyB = g.keyB.as<uint64_t>();
   W.rec = g.rec.as<float4>();
   W.idxA = g.idxA.as<uint32_t>(); W.idxB = g.idxB.as<uint32_t>();
@@ -516,61 +525,125 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   W.phase = g.phase.as<unsigned long long>();
 #endif
 
-  CK(cudaEventRecord(g.ev0, st));
-  if (mode == AHFGPU_PLAIN_FP64) {
-    // one halo at a time, in batch order
-    for (int64_t h = 0; h < nh; h++) {
-      launch_fp64(P, B, W, 1, (int)h, st);
+  // the launch sequence, from the device timer's start to the end of the
+  // pack; issued directly, or captured once as a CUDA graph and re-launched
+  bool capturing = false;
+  auto rec_time = [&](cudaEvent_t ev, cudaStream_t s) {
+    return cudaEventRecordWithFlags(ev, s, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+  };
+  auto issue = [&]() -> int {
+    CK(rec_time(g.ev0, st));
+    if (mode == AHFGPU_PLAIN_FP64) {
+      // one halo at a time, in batch order
+      for (int64_t h = 0; h < nh; h++) {
+        launch_fp64(P, B, W, 1, (int)h, st);
+        launches++;
+      }
+    } else if (mode == AHFGPU_BATCHED_FP64) {
+      launch_fp64(P, B, W, g.nsm * g.fp64_bps, -1, st);
       launches++;
+    } else {
+      // size classes on streams of their own (larger classes at higher
+      // priority), queue parts in order; each segment has its own queue
+      // range, queue head and worklist region.  A later part's launch takes
+      // SMs as the CTAs of the earlier parts run out of work and exit.
+      CK(cudaEventRecord(g.ev_fork, st));
+      int stack_base = 0, slot = 2;
+      for (const Seg& sg : segs) {
+        while (stage && staged <= sg.part)
+          if ((rc = (*stage)(staged++))) return rc;
+        Work Wc = W;
+        Wc.queue = g.queue.as<int32_t>() + sg.q0;
+        Wc.nqueue = sg.q1 - sg.q0;
+        Wc.queue_head = g.qhead.as<unsigned int>() + slot++;
+        Wc.sort_stack = g.stack.as<uint4>() + (size_t)stack_base * stack_cap;
+        stack_base += sg.grid;
+        cudaStream_t cs = g.seg_stream[sg.part][sg.cls];
+        CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
+        if (stage) CK(cudaStreamWaitEvent(cs, g.ev_part[sg.part], 0));
+        launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
+        CK(cudaEventRecord(g.ev_join[sg.part][sg.cls], cs));
+        CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
+        launches++;
+      }
     }
-  } else if (mode == AHFGPU_BATCHED_FP64) {
-    launch_fp64(P, B, W, g.nsm * g.fp64_bps, -1, st);
+    launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
     launches++;
-  } else {
-    // size classes on streams of their own (larger classes at higher
-    // priority), queue parts in order; each segment has its own queue
-    // range, queue head and worklist region.  A later part's launch takes
-    // SMs as the CTAs of the earlier parts run out of work and exit.
-    CK(cudaEventRecord(g.ev_fork, st));
-    int stack_base = 0, slot = 2;
-    for (const Seg& sg : segs) {
-      while (stage && staged <= sg.part)
+    CK(cudaGetLastError());
+    CK(rec_time(g.ev1, st));
+    // pack
+    k_scan_counts<<<2, 1024, 0, st>>>(W.halo, nh, g.member_off.as<uint64_t>(), g.prof_off.as<uint64_t>());
+    int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
+    int mg = (int)std::max<uint64_t>(1, std::min<uint64_t>((pl.N + kPackChunk - 1) / kPackChunk, (uint64_t)g.nsm * 8));
+    if (stage) {
+      while (staged <= nparts)   // the parts without launches, then the ids
         if ((rc = (*stage)(staged++))) return rc;
-      Work Wc = W;
-      Wc.queue = g.queue.as<int32_t>() + sg.q0;
-      Wc.nqueue = sg.q1 - sg.q0;
-      Wc.queue_head = g.qhead.as<unsigned int>() + slot++;
-      Wc.sort_stack = g.stack.as<uint4>() + (size_t)stack_base * stack_cap;
-      stack_base += sg.grid;
-      cudaStream_t cs = g.seg_stream[sg.part][sg.cls];
-      CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
-      if (stage) CK(cudaStreamWaitEvent(cs, g.ev_part[sg.part], 0));
-      launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
-      CK(cudaEventRecord(g.ev_join[sg.part][sg.cls], cs));
-      CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
-      launches++;
+      CK(cudaStreamWaitEvent(st, g.ev_ids, 0));   // the ids come last
+    }
+    k_pack_members<<<mg, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(), db->gidx,
+                                        g.member.as<uint64_t>(), nh);
+    k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
+                                     g.prof.as<double>(), nh);
+    launches += 3;
+    CK(cudaGetLastError());
+    CK(rec_time(g.ev2, st));
+    return AHFGPU_OK;
+  };
+  const bool graphable = g.use_graph && !stage && mode != AHFGPU_PLAIN_FP64;
+  bool done = false;
+  if (graphable) {
+    // everything the sequence depends on: the kernels' arguments (params,
+    // batch, work-space pointers), the queue segments and grids, the outputs
+    std::vector<unsigned char> sig;
+    auto put = [&](const void* p, size_t n) {
+      const unsigned char* c = (const unsigned char*)p;
+      sig.insert(sig.end(), c, c + n);
+    };
+    put(&mode, sizeof mode);
+    put(&P, sizeof P);
+    put(&B, sizeof B);
+    put(&W, sizeof W);
+    put(&nh, sizeof nh);
+    put(&pl.N, sizeof pl.N);
+    put(&stack_cap, sizeof stack_cap);
+    put(&st, sizeof st);
+    for (const Seg& sg : segs) put(&sg, sizeof sg);
+    const void* outs[6] = {db->off, db->gidx, g.member_off.p, g.prof_off.p, g.member.p, g.prof.p};
+    put(outs, sizeof outs);
+    if (g.graph_exec && sig == g.graph_sig) {
+      CK(cudaGraphLaunch(g.graph_exec, st));
+      launches = g.graph_launches;
+      g.graph_replays++;
+      done = true;
+    } else if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      capturing = true;
+      const uint64_t l0 = launches;
+      rc = issue();
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamEndCapture(st, &graph);
+      capturing = false;
+      if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      cudaGraphExec_t ex = nullptr;
+      if (e == cudaSuccess && cudaGraphInstantiate(&ex, graph, 0) == cudaSuccess) {
+        if (g.graph_exec) cudaGraphExecDestroy(g.graph_exec);
+        g.graph_exec = ex;
+        g.graph_sig.swap(sig);
+        g.graph_launches = launches;
+        CK(cudaGraphLaunch(ex, st));
+        done = true;
+      } else {
+        launches = l0;   // capture refused: issue the launches directly
+      }
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+    } else {
+      cudaGetLastError();
     }
   }
-  launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
-  launches++;
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(g.ev1, st));
-  // pack
-  k_scan_counts<<<2, 1024, 0, st>>>(W.halo, nh, g.member_off.as<uint64_t>(), g.prof_off.as<uint64_t>());
-  int pg = (int)std::min<int64_t>((nh * 32 + 255) / 256, (int64_t)g.nsm * 16);
-  int mg = (int)std::max<uint64_t>(1, std::min<uint64_t>((pl.N + kPackChunk - 1) / kPackChunk, (uint64_t)g.nsm * 8));
-  if (stage) {
-    while (staged <= nparts)   // the parts without launches, then the ids
-      if ((rc = (*stage)(staged++))) return rc;
-    CK(cudaStreamWaitEvent(st, g.ev_ids, 0));   // the ids come last
-  }
-  k_pack_members<<<mg, 256, 0, st>>>(db->off, W.mem_stage, g.member_off.as<uint64_t>(), db->gidx,
-                                      g.member.as<uint64_t>(), nh);
-  k_pack_prof<<<pg, 256, 0, st>>>(W.halo, W.prof_cap_off, W.prof_stage, g.prof_off.as<uint64_t>(),
-                                   g.prof.as<double>(), nh);
-  launches += 3;
-  CK(cudaGetLastError());
-  CK(cudaEventRecord(g.ev2, st));
+  if (!done && (rc = issue())) return rc;
   uint64_t tails[2];
   unsigned long long cnt[4];
   int derr = 0;
@@ -714,6 +787,10 @@ int ahfgpu_init(int device) {
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
   load_tuning(prop);
+  {
+    const char* e = getenv("AHFGPU_GRAPH");   // "0": device-resident calls launch directly
+    g.use_graph = !(e && e[0] == '0');
+  }
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
     if (g.tune_bps_cap[k] >= 1) g.fp32c_bps[k] = std::min(g.fp32c_bps[k], g.tune_bps_cap[k]);
@@ -762,6 +839,7 @@ int ahfgpu_shutdown(void) {
     if (g.ev_part[p]) cudaEventDestroy(g.ev_part[p]);
   if (g.ev_ids) cudaEventDestroy(g.ev_ids);
   if (g.ev_fork) cudaEventDestroy(g.ev_fork);
+  if (g.graph_exec) cudaGraphExecDestroy(g.graph_exec);
   if (g.ev0) cudaEventDestroy(g.ev0);
   if (g.ev1) cudaEventDestroy(g.ev1);
   if (g.ev2) cudaEventDestroy(g.ev2);
@@ -1067,9 +1145,11 @@ int ahfgpu_tuning(char* buf, size_t len) {
   if (rc) return rc;
   char tmp[1024];
   snprintf(tmp, sizeof tmp,
-           "{\"key\": \"%s\", \"source\": \"%s\", \"class_max\": [%llu, %llu], \"class_bps\": [%d, %d, %d]}",
+           "{\"key\": \"%s\", \"source\": \"%s\", \"class_max\": [%llu, %llu], \"class_bps\": [%d, %d, %d], "
+           "\"graph\": %s, \"graph_replays\": %llu}",
            g.tune_key.c_str(), g.tune_source.c_str(), (unsigned long long)g.tune_class_max[0],
-           (unsigned long long)g.tune_class_max[1], g.fp32c_bps[0], g.fp32c_bps[1], g.fp32c_bps[2]);
+           (unsigned long long)g.tune_class_max[1], g.fp32c_bps[0], g.fp32c_bps[1], g.fp32c_bps[2],
+           g.use_graph ? "true" : "false", (unsigned long long)g.graph_replays);
   if (buf && len) {
     size_t n = std::min(len - 1, strlen(tmp));
     memcpy(buf, tmp, n);

@@ -120,6 +120,38 @@ def test_fp32c_staged_copies_equal_device_api(gpu):
     assert np.array_equal(dev.prof, host.prof)
 
 
+def test_device_calls_replay_a_graph(gpu):
+    """Device-resident calls capture their launch sequence once as a CUDA
+    graph and re-launch it while kernels and arguments stay the same; the
+    replays give the direct host-path result byte for byte."""
+    import torch
+    from ahf_gb300 import lib
+    params, L = _synthetic("cfg3", scale=0.004, max_particles=200000)
+    t = {"off": torch.as_tensor(L.off.astype(np.int64)).cuda()}
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        t[k] = torch.as_tensor(getattr(L, k)).cuda()
+    t["gidx"] = torch.as_tensor(L.gidx.astype(np.int64)).cuda()
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(L, k)).cuda()
+    torch.cuda.synchronize()
+    db = lib.device_batch(t)
+    for mode in ("batched_fp32c", "batched_fp64"):
+        r0 = gpu.tuning()["graph_replays"]
+        runs = []
+        for _ in range(3):
+            lib.construct_halos_device(params, db, mode)
+            runs.append(lib.fetch_result())
+        tun = gpu.tuning()
+        if tun["graph"]:
+            assert tun["graph_replays"] >= r0 + 2
+        host = gpu.construct_halos(params, L, mode)
+        for r in runs:
+            assert np.array_equal(r.member, host.member)
+            assert np.array_equal(r.member_off, host.member_off)
+            assert np.array_equal(r.halo.view(np.uint8), host.halo.view(np.uint8))
+            assert np.array_equal(r.prof, host.prof)
+
+
 def test_repeat_calls_are_deterministic(gpu):
     params, L = _synthetic("cfg3", scale=0.001, max_particles=20000)
     a = gpu.construct_halos(params, L, "batched_fp64")
