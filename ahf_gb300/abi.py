@@ -78,6 +78,24 @@ class Batch(C.Structure):
     ]
 
 
+class Particles(C.Structure):
+    """ahfgpu_particles: a snapshot's particles (device pointers)."""
+    _fields_ = [
+        ("n", C.c_uint64),
+        ("x", _fp), ("y", _fp), ("z", _fp),
+        ("vx", _fp), ("vy", _fp), ("vz", _fp),
+        ("w", _fp),
+    ]
+
+
+class Centres(C.Structure):
+    """ahfgpu_centres: halo centres and gather radii (device pointers)."""
+    _fields_ = [
+        ("nhalo", C.c_int64),
+        ("cx", _dp), ("cy", _dp), ("cz", _dp), ("rad", _dp),
+    ]
+
+
 class Halo(C.Structure):
     _fields_ = [
         ("npart", C.c_uint64),

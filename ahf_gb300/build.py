@@ -26,6 +26,7 @@ UNITS = {
     "fp32c_class2.cu": ["--fmad=false"],
     "fp32c_dispatch.cu": [],
     "noalloc.cu": [],
+    "gather.cu": [],
 }
 
 

@@ -28,6 +28,24 @@ int fp32c_max_blocks_per_sm(int cls);
 uint64_t fp32c_class_max(int cls);
 void fp32c_set_class_max(uint64_t a, uint64_t b);
 void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
+// the particle gather (gather.cu)
+void gather_cells(uint64_t n, const float* x, const float* y, const float* z, int G, uint32_t* cell,
+                  uint32_t* count, int grid, cudaStream_t st);
+void gather_scan_u32(const uint32_t* in, uint32_t* out, uint64_t m, uint32_t* sums, cudaStream_t st);
+void gather_scatter(uint64_t n, const float* x, const float* y, const float* z, const uint32_t* cell,
+                    const uint32_t* start, uint32_t* fill, float4* sorted, int grid, cudaStream_t st);
+void gather_halos(int pass, int G, const uint32_t* start, const float4* sorted, int64_t nhalo, const int32_t* queue,
+                  unsigned int* qhead, const double* cx, const double* cy, const double* cz, const double* rad,
+                  uint64_t* cnt, const uint64_t* off, unsigned int* hfill, uint64_t* out_idx, int grid,
+                  cudaStream_t st);
+void gather_offsets(const uint64_t* cnt, int64_t nhalo, uint64_t* off, cudaStream_t st);
+int gather_sort_setup();
+void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
+                 uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int* err, int grid,
+                 cudaStream_t st);
+void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
+                 const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
+                 float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st);
 }  // namespace ahfgpu
 
 using namespace ahfgpu;
@@ -117,6 +135,10 @@ struct Ctx {
   DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
   // packed results (device)
   DBuf member_off, member, prof_off, prof, phase;
+  // the particle gather: grid buckets, per-halo counts and lists, the
+  // gathered batch
+  DBuf ga_cell, ga_count, ga_start, ga_fill, ga_sums, ga_sorted, ga_queue, ga_qhead, ga_cnt, ga_off, ga_hfill;
+  DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -787,6 +809,7 @@ int ahfgpu_init(int device) {
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
   load_tuning(prop);
+  CK((cudaError_t)gather_sort_setup());
   {
     const char* e = getenv("AHFGPU_GRAPH");   // "0": device-resident calls launch directly
     g.use_graph = !(e && e[0] == '0');
@@ -827,7 +850,11 @@ int ahfgpu_shutdown(void) {
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
                   &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.rec, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
-                  &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof};
+                  &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof,
+                  &g.ga_cell, &g.ga_count, &g.ga_start, &g.ga_fill, &g.ga_sums, &g.ga_sorted, &g.ga_queue,
+                  &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
+                  &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
+                  &g.ga_id, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1072,6 +1099,116 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
   CK(cudaStreamSynchronize(st));
   g.last_stats.ms_d2h = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   r->stats = g.last_stats;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* cen, ahfgpu_batch* out,
+                         void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!parts || !cen || !out) return fail(AHFGPU_ERR_INVALID, "particles/centres/out is NULL");
+  const uint64_t n = parts->n;
+  const int64_t nh = cen->nhalo;
+  if (nh < 0 || nh > 0x7fffffff) return fail(AHFGPU_ERR_INVALID, "nhalo %lld out of range", (long long)nh);
+  if (n >= (1ull << 32)) return fail(AHFGPU_ERR_CAPACITY, "the gather takes fewer than 2^32 particles");
+  if (n > 0 && (!parts->x || !parts->y || !parts->z || !parts->vx || !parts->vy || !parts->vz))
+    return fail(AHFGPU_ERR_INVALID, "a particle array is NULL");
+  if (nh > 0 && (!cen->cx || !cen->cy || !cen->cz || !cen->rad)) return fail(AHFGPU_ERR_INVALID, "a centre array is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  memset(out, 0, sizeof(*out));
+  out->nhalo = nh;
+  // radii on the host: the grid resolution and the queue (largest first)
+  std::vector<double> rad((size_t)std::max<int64_t>(nh, 1));
+  if (nh > 0) {
+    CK(cudaMemcpyAsync(rad.data(), cen->rad, nh * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  for (int64_t h = 0; h < nh; h++)
+    if (!(rad[h] >= 0.0) || !(rad[h] <= 1.0)) return fail(AHFGPU_ERR_INVALID, "gather radius of halo %lld not in [0, 1]", (long long)h);
+  std::vector<int32_t> queue((size_t)std::max<int64_t>(nh, 1));
+  std::iota(queue.begin(), queue.begin() + nh, 0);
+  std::sort(queue.begin(), queue.begin() + nh, [&](int32_t a, int32_t b) { return rad[a] > rad[b] || (rad[a] == rad[b] && a < b); });
+  double rmed = nh > 0 ? rad[queue[nh / 2]] : 0.5;
+  // cells of about half the median radius, 8..256 per axis
+  int G = rmed > 0 ? (int)std::min(256.0, std::max(8.0, std::floor(2.0 / rmed))) : 8;
+  const uint64_t m = (uint64_t)G * G * G;
+#define EN(buf, bytes) if ((rc = (buf).ensure(std::max<size_t>((size_t)(bytes), 8))) != AHFGPU_OK) return rc
+  EN(g.ga_cell, n * 4);
+  EN(g.ga_count, m * 4);
+  EN(g.ga_fill, m * 4);
+  EN(g.ga_start, (m + 1) * 4);
+  EN(g.ga_sums, ((m + 2047) / 2048) * 4);
+  EN(g.ga_sorted, n * 16);
+  EN(g.ga_queue, nh * 4);
+  EN(g.ga_qhead, 64);
+  EN(g.ga_cnt, nh * 8);
+  EN(g.ga_off, (nh + 1) * 8);
+  EN(g.ga_hfill, nh * 4);
+  EN(g.ga_err, 64);
+  const int grid_p = std::max(1, std::min<int>(g.nsm * 8, (int)((n + 255) / 256)));
+  const int grid_h = std::max(1, std::min<int>(g.nsm * 4, (int)std::max<int64_t>(nh, 1)));
+  CK(cudaMemsetAsync(g.ga_count.p, 0, m * 4, st));
+  CK(cudaMemsetAsync(g.ga_fill.p, 0, m * 4, st));
+  CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.ga_err.p, 0, 64, st));
+  if (nh > 0) {
+    CK(cudaMemcpyAsync(g.ga_queue.p, queue.data(), nh * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(g.ga_hfill.p, 0, nh * 4, st));
+  }
+  if (n > 0) gather_cells(n, parts->x, parts->y, parts->z, G, g.ga_cell.as<uint32_t>(), g.ga_count.as<uint32_t>(), grid_p, st);
+  gather_scan_u32(g.ga_count.as<uint32_t>(), g.ga_start.as<uint32_t>(), m, g.ga_sums.as<uint32_t>(), st);
+  if (n > 0)
+    gather_scatter(n, parts->x, parts->y, parts->z, g.ga_cell.as<uint32_t>(), g.ga_start.as<uint32_t>(),
+                   g.ga_fill.as<uint32_t>(), g.ga_sorted.as<float4>(), grid_p, st);
+  if (nh > 0)
+    gather_halos(0, G, g.ga_start.as<uint32_t>(), g.ga_sorted.as<float4>(), nh, g.ga_queue.as<int32_t>(),
+                 g.ga_qhead.as<unsigned int>(), cen->cx, cen->cy, cen->cz, cen->rad, g.ga_cnt.as<uint64_t>(), nullptr,
+                 nullptr, nullptr, grid_h, st);
+  gather_offsets(g.ga_cnt.as<uint64_t>(), nh, g.ga_off.as<uint64_t>(), st);
+  CK(cudaGetLastError());
+  std::vector<uint64_t> cnt((size_t)std::max<int64_t>(nh, 1), 0);
+  if (nh > 0) CK(cudaMemcpyAsync(cnt.data(), g.ga_cnt.p, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  uint64_t ng = 0, maxn = 0;
+  for (int64_t h = 0; h < nh; h++) { ng += cnt[h]; maxn = std::max(maxn, cnt[h]); }
+  if (maxn >= (1ull << 32)) return fail(AHFGPU_ERR_CAPACITY, "a gathered list exceeds 2^32-1 particles");
+  const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(maxn / 512 + 64, 64), 1u << 20);
+  EN(g.ga_idx, ng * 8);
+  EN(g.ga_idxA, ng * 4);
+  EN(g.ga_keyB, ng * 8);
+  EN(g.ga_idxB, ng * 4);
+  EN(g.ga_stack, (size_t)grid_h * stack_cap * sizeof(uint4));
+  EN(g.ga_x, ng * 4); EN(g.ga_y, ng * 4); EN(g.ga_z, ng * 4);
+  EN(g.ga_vx, ng * 4); EN(g.ga_vy, ng * 4); EN(g.ga_vz, ng * 4);
+  if (parts->w) EN(g.ga_w, ng * 4);
+  EN(g.ga_id, ng * 8);
+#undef EN
+  if (nh > 0 && ng > 0) {
+    CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
+    gather_halos(1, G, g.ga_start.as<uint32_t>(), g.ga_sorted.as<float4>(), nh, g.ga_queue.as<int32_t>(),
+                 g.ga_qhead.as<unsigned int>(), cen->cx, cen->cy, cen->cz, cen->rad, g.ga_cnt.as<uint64_t>(),
+                 g.ga_off.as<uint64_t>(), g.ga_hfill.as<unsigned int>(), g.ga_idx.as<uint64_t>(), grid_h, st);
+    CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
+    gather_sort(nh, g.ga_queue.as<int32_t>(), g.ga_qhead.as<unsigned int>(), g.ga_off.as<uint64_t>(),
+                g.ga_idx.as<uint64_t>(), g.ga_idxA.as<uint32_t>(), g.ga_keyB.as<uint64_t>(), g.ga_idxB.as<uint32_t>(),
+                g.ga_stack.as<uint4>(), stack_cap, g.ga_err.as<int>(), grid_h, st);
+    gather_pack(ng, g.ga_idx.as<uint64_t>(), parts->x, parts->y, parts->z, parts->vx, parts->vy, parts->vz, parts->w,
+                g.ga_x.as<float>(), g.ga_y.as<float>(), g.ga_z.as<float>(), g.ga_vx.as<float>(), g.ga_vy.as<float>(),
+                g.ga_vz.as<float>(), parts->w ? g.ga_w.as<float>() : nullptr, g.ga_id.as<uint64_t>(),
+                std::max(1, std::min<int>(g.nsm * 8, (int)((ng + 255) / 256))), st);
+  }
+  CK(cudaGetLastError());
+  int derr = 0;
+  CK(cudaMemcpyAsync(&derr, g.ga_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr == kErrWorklist) return fail(AHFGPU_ERR_CAPACITY, "gather sort worklist overflow");
+  if (derr) return fail(AHFGPU_ERR_CUDA, "gather: device error code %d", derr);
+  out->off = g.ga_off.as<uint64_t>();
+  out->x = g.ga_x.as<float>(); out->y = g.ga_y.as<float>(); out->z = g.ga_z.as<float>();
+  out->vx = g.ga_vx.as<float>(); out->vy = g.ga_vy.as<float>(); out->vz = g.ga_vz.as<float>();
+  out->w = parts->w ? g.ga_w.as<float>() : nullptr;
+  out->gidx = g.ga_id.as<uint64_t>();
+  out->cx = cen->cx; out->cy = cen->cy; out->cz = cen->cz;
   return AHFGPU_OK;
 }
 

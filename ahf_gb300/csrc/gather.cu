@@ -1,0 +1,321 @@
+// gather.cu -- the particle gather on the GPU.  Replaces
+// ahf_halos_sfc_gatherParts (src/libahf/ahf_halos_sfc.c:171-412) for every
+// halo of a snapshot at once: the list of halo h is every particle i with
+// dist2(i, h) <= gatherRad_h^2, dist2 computed as the reference's
+// LOCAL_CAL_DXYZ (:69-78) on the float position promoted to double, the sum
+// and the comparison as local_checkAndAddParticles (:329-332) makes them.
+// The reference finds candidates through its Hilbert-key sorted particle
+// array and the 3x3x3 cells around the centre; here the particles are
+// bucketed once into a uniform G^3 grid (counting sort) and each halo scans
+// the grid cells its sphere can touch.  Lists come out in ascending particle
+// index (a per-halo sort of the matches), a deterministic order; the
+// reference's order follows its SFC cells.
+#include <cstdint>
+
+#include "common.cuh"
+#include "sort.cuh"
+
+namespace ahfgpu {
+
+using GatherSS = SortSmemT<2048, 4096>;
+
+__device__ __forceinline__ int cell_of(float x, int G) {
+  int c = (int)(x * (float)G);
+  return c < 0 ? 0 : (c >= G ? G - 1 : c);
+}
+
+// periodic squared distance of a float position from a double centre, in
+// the reference's operation order (no contraction)
+__device__ __forceinline__ double gather_d2(float px, float py, float pz, double cx, double cy, double cz) {
+  double dx = fabs(__dsub_rn((double)px, cx)), dy = fabs(__dsub_rn((double)py, cy)),
+         dz = fabs(__dsub_rn((double)pz, cz));
+  if (dx > 0.5) dx = __dsub_rn(1.0, dx);
+  if (dy > 0.5) dy = __dsub_rn(1.0, dy);
+  if (dz > 0.5) dz = __dsub_rn(1.0, dz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__global__ void k_gather_cells(uint64_t n, const float* __restrict__ x, const float* __restrict__ y,
+                               const float* __restrict__ z, int G, uint32_t* __restrict__ cell,
+                               uint32_t* __restrict__ count) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = ((uint32_t)cell_of(x[i], G) * (uint32_t)G + (uint32_t)cell_of(y[i], G)) * (uint32_t)G +
+                       (uint32_t)cell_of(z[i], G);
+    cell[i] = c;
+    atomicAdd(&count[c], 1u);
+  }
+}
+
+// exclusive scan of m u32 counts in tiles of 2048 (block sums to `sums`)
+__global__ void k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t m,
+                             uint32_t* __restrict__ sums) {
+  __shared__ uint32_t wsum[32];
+  const uint64_t base = (uint64_t)blockIdx.x * 2048;
+  const uint64_t i0 = base + 2 * (uint64_t)threadIdx.x;
+  const uint32_t a = i0 < m ? in[i0] : 0u, b = i0 + 1 < m ? in[i0 + 1] : 0u;
+  uint32_t v = a + b, inc = v;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = lane < nw ? wsum[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t ex = (wid ? wsum[wid - 1] : 0u) + inc - v;
+  if (i0 < m) out[i0] = ex;
+  if (i0 + 1 < m) out[i0 + 1] = ex + a;
+  if (threadIdx.x == blockDim.x - 1) sums[blockIdx.x] = wsum[nw - 1];
+}
+
+// exclusive scan of the tile sums in place (one block), total to *total
+__global__ void k_scan_sums(uint32_t* __restrict__ sums, uint64_t ns, uint32_t* __restrict__ total) {
+  __shared__ uint32_t wsum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t carry = 0;
+  for (uint64_t base = 0; base < ns; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    const uint32_t v = i < ns ? sums[i] : 0u;
+    uint32_t inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      uint32_t w = lane < nw ? wsum[lane] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    if (i < ns) sums[i] = carry + (wid ? wsum[wid - 1] : 0u) + inc - v;
+    carry += wsum[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, uint64_t m, const uint32_t* __restrict__ sums) {
+  const uint64_t i0 = (uint64_t)blockIdx.x * 2048;
+  const uint32_t s = sums[blockIdx.x];
+  for (uint64_t i = i0 + threadIdx.x; i < i0 + 2048 && i < m; i += blockDim.x) out[i] += s;
+}
+
+// particles in cell order: {x, y, z, index bits}
+__global__ void k_gather_scatter(uint64_t n, const float* __restrict__ x, const float* __restrict__ y,
+                                 const float* __restrict__ z, const uint32_t* __restrict__ cell,
+                                 const uint32_t* __restrict__ start, uint32_t* __restrict__ fill,
+                                 float4* __restrict__ sorted) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cell[i];
+    const uint32_t p = start[c] + atomicAdd(&fill[c], 1u);
+    sorted[p] = make_float4(x[i], y[i], z[i], __uint_as_float((uint32_t)i));
+  }
+}
+
+// One CTA per halo (persistent, queue largest radius first).  Pass 0 counts
+// the matches of each halo into cnt[h]; pass 1 writes their particle indices
+// at off[h] (unordered; k_gather_sort orders them).
+__global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uint32_t* __restrict__ start,
+                                                      const float4* __restrict__ sorted, int64_t nhalo,
+                                                      const int32_t* __restrict__ queue,
+                                                      unsigned int* __restrict__ qhead,
+                                                      const double* __restrict__ cx, const double* __restrict__ cy,
+                                                      const double* __restrict__ cz, const double* __restrict__ rad,
+                                                      uint64_t* __restrict__ cnt, const uint64_t* __restrict__ off,
+                                                      unsigned int* __restrict__ hfill,
+                                                      uint64_t* __restrict__ out_idx) {
+  __shared__ int s_h;
+  __shared__ unsigned long long s_cnt;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned q = atomicAdd(qhead, 1u);
+      s_h = q < (unsigned)nhalo ? queue[q] : -1;
+      s_cnt = 0;
+    }
+    __syncthreads();
+    const int h = s_h;
+    if (h < 0) break;
+    const double ccx = cx[h], ccy = cy[h], ccz = cz[h], r = rad[h];
+    const double r2 = __dmul_rn(r, r);
+    // cells the sphere can touch, one cell of margin for the float cell
+    // assignment; a span of G or more covers the whole periodic axis once
+    int lo[3], nd[3];
+    const double cc[3] = {ccx, ccy, ccz};
+    for (int d = 0; d < 3; d++) {
+      const long long a = (long long)floor((cc[d] - r) * (double)G) - 1;
+      const long long b = (long long)floor((cc[d] + r) * (double)G) + 1;
+      if (!(r >= 0.0) || b - a + 1 >= G) { lo[d] = 0; nd[d] = G; }
+      else { lo[d] = (int)(((a % G) + G) % G); nd[d] = (int)(b - a + 1); }
+    }
+    const long long ncell = (long long)nd[0] * nd[1] * nd[2];
+    unsigned long long mine = 0;
+    for (long long k = wid; k < ncell; k += nw) {
+      const int kz = (int)(k % nd[2]), ky = (int)((k / nd[2]) % nd[1]), kx = (int)(k / ((long long)nd[2] * nd[1]));
+      const int ix = (lo[0] + kx) % G, iy = (lo[1] + ky) % G, iz = (lo[2] + kz) % G;
+      const uint32_t c = ((uint32_t)ix * (uint32_t)G + (uint32_t)iy) * (uint32_t)G + (uint32_t)iz;
+      const uint32_t s0 = start[c], s1 = start[c + 1];
+      for (uint32_t j = s0 + lane; j < s1; j += 32) {
+        const float4 p = sorted[j];
+        if (gather_d2(p.x, p.y, p.z, ccx, ccy, ccz) <= r2) {
+          if (pass == 0) {
+            mine++;
+          } else {
+            const unsigned q = atomicAdd(&hfill[h], 1u);
+            out_idx[off[h] + q] = (uint64_t)__float_as_uint(p.w);
+          }
+        }
+      }
+    }
+    if (pass == 0) {
+      for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+      if (lane == 0 && mine) atomicAdd(&s_cnt, mine);
+      __syncthreads();
+      if (threadIdx.x == 0) cnt[h] = s_cnt;
+    }
+    __syncthreads();
+  }
+}
+
+// exclusive scan of nhalo u64 counts into off[0..nhalo] (one block)
+__global__ void k_gather_offsets(const uint64_t* __restrict__ cnt, int64_t nhalo, uint64_t* __restrict__ off) {
+  __shared__ unsigned long long wsum[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned long long carry = 0;
+  for (int64_t base = 0; base < nhalo; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const unsigned long long v = i < nhalo ? cnt[i] : 0ull;
+    unsigned long long inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+      unsigned long long w = lane < nw ? wsum[lane] : 0ull;
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    if (i < nhalo) off[i + 1] = carry + (wid ? wsum[wid - 1] : 0ull) + inc;
+    carry += wsum[nw - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) off[0] = 0;
+}
+
+// each halo's list in ascending particle index: the block radial sort on
+// (index, slot) over [off[h], off[h+1]) of keyA (indices) / idxA (scratch)
+__global__ void __launch_bounds__(256) k_gather_sort(int64_t nhalo, const int32_t* __restrict__ queue,
+                                                     unsigned int* __restrict__ qhead, const uint64_t* __restrict__ off,
+                                                     uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB,
+                                                     uint4* stack, int stack_cap, int* err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  GatherSS& S = *reinterpret_cast<GatherSS*>(smem_raw);
+  __shared__ int s_h;
+  uint4* my_stack = stack + (uint64_t)blockIdx.x * stack_cap;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned q = atomicAdd(qhead, 1u);
+      s_h = q < (unsigned)nhalo ? queue[q] : -1;
+    }
+    __syncthreads();
+    const int h = s_h;
+    if (h < 0) break;
+    const uint64_t o = off[h], n = off[h + 1] - o;
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) idxA[o + i] = (uint32_t)i;
+    __syncthreads();
+    const int rc = radial_sort(keyA, idxA, keyB, idxB, o, n, my_stack, stack_cap, S);
+    if (rc != kErrNone && threadIdx.x == 0) atomicExch(err, rc);
+    __syncthreads();
+  }
+}
+
+// the gathered lists as a stage batch: SoA particle data per entry, the
+// particle index as the entry's id
+__global__ void k_gather_pack(uint64_t ng, const uint64_t* __restrict__ idx, const float* __restrict__ x,
+                              const float* __restrict__ y, const float* __restrict__ z, const float* __restrict__ vx,
+                              const float* __restrict__ vy, const float* __restrict__ vz, const float* __restrict__ w,
+                              float* __restrict__ ox, float* __restrict__ oy, float* __restrict__ oz,
+                              float* __restrict__ ovx, float* __restrict__ ovy, float* __restrict__ ovz,
+                              float* __restrict__ ow, uint64_t* __restrict__ oid) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ng; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = idx[k];
+    ox[k] = x[i]; oy[k] = y[i]; oz[k] = z[i];
+    ovx[k] = vx[i]; ovy[k] = vy[i]; ovz[k] = vz[i];
+    if (w) ow[k] = w[i];
+    oid[k] = i;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers (host)
+
+void gather_cells(uint64_t n, const float* x, const float* y, const float* z, int G, uint32_t* cell,
+                  uint32_t* count, int grid, cudaStream_t st) {
+  k_gather_cells<<<grid, 256, 0, st>>>(n, x, y, z, G, cell, count);
+}
+
+// exclusive scan of m counts into out[0..m) with out[m] = total (out has m+1)
+void gather_scan_u32(const uint32_t* in, uint32_t* out, uint64_t m, uint32_t* sums, cudaStream_t st) {
+  const uint64_t nt = (m + 2047) / 2048;
+  k_scan_tiles<<<(unsigned)nt, 1024, 0, st>>>(in, out, m, sums);
+  k_scan_sums<<<1, 1024, 0, st>>>(sums, nt, out + m);
+  k_scan_add<<<(unsigned)nt, 256, 0, st>>>(out, m, sums);
+}
+
+void gather_scatter(uint64_t n, const float* x, const float* y, const float* z, const uint32_t* cell,
+                    const uint32_t* start, uint32_t* fill, float4* sorted, int grid, cudaStream_t st) {
+  k_gather_scatter<<<grid, 256, 0, st>>>(n, x, y, z, cell, start, fill, sorted);
+}
+
+void gather_halos(int pass, int G, const uint32_t* start, const float4* sorted, int64_t nhalo, const int32_t* queue,
+                  unsigned int* qhead, const double* cx, const double* cy, const double* cz, const double* rad,
+                  uint64_t* cnt, const uint64_t* off, unsigned int* hfill, uint64_t* out_idx, int grid,
+                  cudaStream_t st) {
+  k_gather_halos<<<grid, 256, 0, st>>>(pass, G, start, sorted, nhalo, queue, qhead, cx, cy, cz, rad, cnt, off, hfill,
+                                       out_idx);
+}
+
+void gather_offsets(const uint64_t* cnt, int64_t nhalo, uint64_t* off, cudaStream_t st) {
+  k_gather_offsets<<<1, 1024, 0, st>>>(cnt, nhalo, off);
+}
+
+size_t gather_sort_smem() { return sizeof(GatherSS); }
+
+int gather_sort_setup() {
+  return (int)cudaFuncSetAttribute(k_gather_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(GatherSS));
+}
+
+void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
+                 uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int* err, int grid,
+                 cudaStream_t st) {
+  k_gather_sort<<<grid, 256, sizeof(GatherSS), st>>>(nhalo, queue, qhead, off, keyA, idxA, keyB, idxB, stack, stack_cap,
+                                                      err);
+}
+
+void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
+                 const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
+                 float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st) {
+  k_gather_pack<<<grid, 256, 0, st>>>(ng, idx, x, y, z, vx, vy, vz, w, ox, oy, oz, ovx, ovy, ovz, ow, oid);
+}
+
+}  // namespace ahfgpu

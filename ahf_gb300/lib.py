@@ -22,6 +22,7 @@ LIB_PATH = os.environ.get("AHFGPU_LIB", os.path.join(HERE, "libahfgpu.so"))
 SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
+    "ahfgpu_gather_device",
 ]
 
 
@@ -62,6 +63,9 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_version.restype = C.c_char_p
     lib.ahfgpu_tuning.argtypes = [C.c_char_p, C.c_size_t]
     lib.ahfgpu_tuning.restype = C.c_int
+    lib.ahfgpu_gather_device.argtypes = [C.POINTER(abi.Particles), C.POINTER(abi.Centres), C.POINTER(Batch),
+                                         C.c_void_p]
+    lib.ahfgpu_gather_device.restype = C.c_int
     _lib = lib
     return lib
 
@@ -173,3 +177,46 @@ def tuning(device: int = 0) -> dict:
     buf = C.create_string_buffer(1024)
     check(load().ahfgpu_tuning(buf, len(buf)))
     return json.loads(buf.value.decode())
+
+
+def gather_device(parts: dict, centres: dict, stream: int | None = None) -> Batch:
+    """The GPU gather (ahfgpu_gather_device) on torch CUDA tensors:
+    parts {x, y, z, vx, vy, vz[, w]}, centres {cx, cy, cz, rad}.  Returns the
+    gathered batch (device pointers, library-owned until the next gather),
+    ready for construct_halos_device."""
+    init()
+    p = abi.Particles()
+    p.n = int(parts["x"].numel())
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+        v = parts.get(k)
+        setattr(p, k, C.cast(C.c_void_p(v.data_ptr() if v is not None else None), C.POINTER(C.c_float)))
+    c = abi.Centres()
+    c.nhalo = int(centres["cx"].numel())
+    for k in ("cx", "cy", "cz", "rad"):
+        setattr(c, k, C.cast(C.c_void_p(centres[k].data_ptr()), C.POINTER(C.c_double)))
+    b = Batch()
+    check(load().ahfgpu_gather_device(C.byref(p), C.byref(c), C.byref(b), C.c_void_p(stream) if stream else None))
+    return b
+
+
+def device_view(ptr: int, count: int, typestr: str):
+    """A torch CUDA tensor viewing `count` elements at a device address the
+    library owns (no copy)."""
+    import torch
+
+    class _Dev:
+        __cuda_array_interface__ = {"shape": (count,), "typestr": typestr, "data": (ptr, False), "version": 3}
+    return torch.as_tensor(_Dev(), device="cuda")
+
+
+def gathered_lists(b: Batch):
+    """(off, gidx) of a gathered batch, copied to host numpy arrays."""
+    import numpy as np
+    import torch
+    torch.cuda.synchronize()
+    nh = int(b.nhalo)
+    off = device_view(C.cast(b.off, C.c_void_p).value, nh + 1, "<u8").cpu().numpy().astype(np.uint64)
+    n = int(off[-1])
+    gid = (device_view(C.cast(b.gidx, C.c_void_p).value, n, "<u8").cpu().numpy().astype(np.uint64) if n
+           else np.zeros(0, np.uint64))
+    return off, gid

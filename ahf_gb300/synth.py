@@ -329,3 +329,88 @@ def generate(name: str, scale: float = 1.0, device: str = "cpu", multimass: bool
 
 def params_for(lists: HaloLists, **kw):
     return ahf_params(lists.boxsize, lists.pmass, **kw)
+
+
+@dataclass
+class Snapshot:
+    """Particles of a periodic box plus halo centres and gather radii (the
+    inputs of AHF's particle gather)."""
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    vx: np.ndarray
+    vy: np.ndarray
+    vz: np.ndarray
+    w: object
+    cx: np.ndarray
+    cy: np.ndarray
+    cz: np.ndarray
+    rad: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return len(self.x)
+
+    @property
+    def nhalo(self) -> int:
+        return len(self.cx)
+
+
+def snapshot_from_lists(lists: HaloLists, n_background: int, seed: int = 7) -> Snapshot:
+    """A snapshot made of every particle of the lists (each list is its own
+    NFW sphere plus background out to 1.5 R_vir) and `n_background` uniform
+    particles (sigma 100 km/s) over the whole box, in a seeded random order.
+    Each halo's gather radius is the largest periodic distance of its own
+    list's particles from its centre (<= 1.5 R_vir)."""
+    L = lists.to_numpy() if not isinstance(lists.x, np.ndarray) else lists
+    rng = np.random.default_rng(seed)
+    vsig = 100.0 / (L.boxsize * H0)
+    bx = rng.random((n_background, 3)).astype(np.float32)
+    bv = (rng.standard_normal((n_background, 3)) * vsig).astype(np.float32)
+    pos = np.concatenate([np.stack([L.x, L.y, L.z], 1).astype(np.float32), bx])
+    vel = np.concatenate([np.stack([L.vx, L.vy, L.vz], 1).astype(np.float32), bv])
+    w = None
+    if L.w is not None:
+        w = np.concatenate([np.asarray(L.w, np.float32), np.ones(n_background, np.float32)])
+    perm = rng.permutation(len(pos))
+    pos, vel = pos[perm], vel[perm]
+    if w is not None:
+        w = w[perm]
+    off = L.off.astype(np.int64)
+    rad = np.zeros(L.nhalo)
+    for h in range(L.nhalo):
+        s = slice(off[h], off[h + 1])
+        if off[h + 1] == off[h]:
+            continue
+        d2 = np.zeros(off[h + 1] - off[h])
+        for a, c in ((L.x, L.cx), (L.y, L.cy), (L.z, L.cz)):
+            d = np.abs(a[s].astype(np.float64) - c[h])
+            d = np.where(d > 0.5, 1.0 - d, d)
+            d2 += d * d
+        rad[h] = float(np.sqrt(d2.max()))
+    return Snapshot(np.ascontiguousarray(pos[:, 0]), np.ascontiguousarray(pos[:, 1]), np.ascontiguousarray(pos[:, 2]),
+                    np.ascontiguousarray(vel[:, 0]), np.ascontiguousarray(vel[:, 1]), np.ascontiguousarray(vel[:, 2]),
+                    w, np.asarray(L.cx, np.float64).copy(), np.asarray(L.cy, np.float64).copy(),
+                    np.asarray(L.cz, np.float64).copy(), rad)
+
+
+def gather_edge_snapshot(seed: int = 11) -> Snapshot:
+    """Hand-built gather cases: centres on box faces, edges and corners
+    (periodic wrap), a zero radius, a radius above 0.5 (the whole box along
+    every axis), two haloes with the same centre, a centre exactly on a
+    particle, particles exactly on the box's lower faces."""
+    rng = np.random.default_rng(seed)
+    n = 40000
+    pos = rng.random((n, 3)).astype(np.float32)
+    pos[:50, 0] = 0.0
+    pos[50:100, 1] = 0.0
+    pos[100:120] = 0.0
+    vel = (rng.standard_normal((n, 3)) * 0.01).astype(np.float32)
+    cen = np.array([[0.0, 0.5, 0.5], [0.999, 0.999, 0.999], [0.0, 0.0, 0.0], [0.5, 0.0, 0.999],
+                    [0.3, 0.3, 0.3], [0.3, 0.3, 0.3], [0.25, 0.75, 0.5], [0.6, 0.2, 0.9],
+                    [float(pos[500, 0]), float(pos[500, 1]), float(pos[500, 2])], [0.01, 0.99, 0.5]])
+    rad = np.array([0.05, 0.08, 0.03, 0.1, 0.0, 0.04, 0.6, 0.02, 0.015, 0.12])
+    return Snapshot(np.ascontiguousarray(pos[:, 0]), np.ascontiguousarray(pos[:, 1]), np.ascontiguousarray(pos[:, 2]),
+                    np.ascontiguousarray(vel[:, 0]), np.ascontiguousarray(vel[:, 1]), np.ascontiguousarray(vel[:, 2]),
+                    None, np.ascontiguousarray(cen[:, 0]), np.ascontiguousarray(cen[:, 1]),
+                    np.ascontiguousarray(cen[:, 2]), rad)

@@ -189,6 +189,36 @@ AHFGPU_API int ahfgpu_construct_halos(const ahfgpu_params *params,
                            ahfgpu_result       *result,
                            ahfgpu_mode          mode);
 
+/* ---- the particle gather (the stage's input) ------------------------------ */
+
+/* A snapshot's particles in device memory: positions in box units [0,1)
+ * (float), momenta (float), weights (float, NULL = 1).  n < 2^32.          */
+typedef struct {
+  uint64_t     n;
+  const float *x, *y, *z, *vx, *vy, *vz, *w;
+} ahfgpu_particles;
+
+/* Halo centres (box units) and gather radii (HALO.gatherRad), device memory */
+typedef struct {
+  int64_t       nhalo;
+  const double *cx, *cy, *cz, *rad;
+} ahfgpu_centres;
+
+/* Replaces ahf_halos_sfc_gatherParts (src/libahf/ahf_halos_sfc.c:171-412) for
+ * every halo at once: the list of halo h is every particle i whose periodic
+ * squared distance from the centre, computed as the reference computes it
+ * (LOCAL_CAL_DXYZ :69-78 on the float position promoted to double, compared
+ * by islessequal with gatherRad^2, :329-332), is within the radius; each
+ * list in ascending particle index (the reference lists its SFC cells in
+ * turn).  `gathered` is filled with device pointers to library-owned
+ * buffers (valid until the next gather or ahfgpu_shutdown) in the layout
+ * ahfgpu_construct_halos_device takes: off, the particles' x..vz (w when
+ * given), gidx = particle index, and the caller's centres.                 */
+AHFGPU_API int ahfgpu_gather_device(const ahfgpu_particles *parts,
+                                    const ahfgpu_centres   *centres,
+                                    ahfgpu_batch           *gathered,
+                                    void                   *stream);
+
 /* Same stage with every pointer of `batch` already in device memory; the
  * results stay on the device in library-owned buffers (valid until the next
  * call or ahfgpu_shutdown) and are described by `dres` (device pointers,

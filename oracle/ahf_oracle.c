@@ -790,3 +790,56 @@ void ahforacle_result_free(ahfgpu_result *r)
   free(r->halo); free(r->member_off); free(r->member); free(r->prof_off); free(r->prof);
   memset(r, 0, sizeof(*r));
 }
+
+
+/* ---------------------------------------------------------------------------
+ * Particle gather, src/libahf/ahf_halos_sfc.c:171-412.  The reference visits
+ * the 3x3x3 cells (at the coarsest level whose cells exceed 1.001 gatherRad,
+ * local_getSuitableBits :236-255) around the centre's cell, which contain
+ * the whole gather sphere, and keeps each particle with
+ * islessequal(dist2, gatherRad2) (:329-332), dist2 from LOCAL_CAL_DXYZ
+ * (:69-78) on the float position promoted to double.  The kept set is
+ * therefore every particle within the radius; this restatement lists it in
+ * ascending particle index (the reference's order follows its SFC cells).
+ */
+static double gather_d2(float px, float py, float pz, double cx, double cy, double cz)
+{
+  double dx = fabs((double)px - cx), dy = fabs((double)py - cy), dz = fabs((double)pz - cz);
+  if (dx > 0.5) dx = 1.0 - dx;
+  if (dy > 0.5) dy = 1.0 - dy;
+  if (dz > 0.5) dz = 1.0 - dz;
+  return dx * dx + dy * dy + dz * dz;
+}
+
+int ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z, int64_t nhalo,
+                     const double *cx, const double *cy, const double *cz, const double *rad,
+                     uint64_t *out_off, uint64_t **out_idx)
+{
+  uint64_t *cnt = (uint64_t *)calloc((size_t)(nhalo > 0 ? nhalo : 1), sizeof(uint64_t));
+  if (!cnt) return -1;
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t h = 0; h < nhalo; h++) {
+    const double r2 = rad[h] * rad[h];
+    uint64_t c = 0;
+    for (uint64_t i = 0; i < n; i++)
+      if (gather_d2(x[i], y[i], z[i], cx[h], cy[h], cz[h]) <= r2) c++;
+    cnt[h] = c;
+  }
+  out_off[0] = 0;
+  for (int64_t h = 0; h < nhalo; h++) out_off[h + 1] = out_off[h] + cnt[h];
+  free(cnt);
+  uint64_t tot = nhalo > 0 ? out_off[nhalo] : 0;
+  uint64_t *idx = (uint64_t *)malloc((size_t)(tot ? tot : 1) * sizeof(uint64_t));
+  if (!idx) return -1;
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t h = 0; h < nhalo; h++) {
+    const double r2 = rad[h] * rad[h];
+    uint64_t k = out_off[h];
+    for (uint64_t i = 0; i < n; i++)
+      if (gather_d2(x[i], y[i], z[i], cx[h], cy[h], cz[h]) <= r2) idx[k++] = i;
+  }
+  *out_idx = idx;
+  return 0;
+}
+
+void ahforacle_gather_free(uint64_t *idx) { free(idx); }

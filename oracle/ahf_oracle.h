@@ -27,6 +27,16 @@ int  ahforacle_construct_halos(const ahfgpu_params *params,
 void ahforacle_result_free(ahfgpu_result *result);
 int  ahforacle_max_threads(void);
 
+/* The particle gather (src/libahf/ahf_halos_sfc.c:171-412): the list of halo
+ * h is every particle i with dist2 <= rad[h]^2, dist2 computed as the
+ * reference's LOCAL_CAL_DXYZ (:69-78) and local_checkAndAddParticles
+ * (:329-332) do, in ascending particle index.  CSR out: out_off[nhalo+1],
+ * *out_idx malloc()ed (free with ahforacle_gather_free).                  */
+int  ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z, int64_t nhalo,
+                      const double *cx, const double *cy, const double *cz, const double *rad,
+                      uint64_t *out_off, uint64_t **out_idx);
+void ahforacle_gather_free(uint64_t *idx);
+
 #ifdef __cplusplus
 }
 #endif

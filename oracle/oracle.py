@@ -91,3 +91,39 @@ def max_threads() -> int:
     lib, _, _ = _load(oracle_path(), "ahforacle")
     lib.ahforacle_max_threads.restype = C.c_int
     return int(lib.ahforacle_max_threads())
+
+
+def _gather(path: str, prefix: str, x, y, z, cx, cy, cz, rad):
+    import numpy as np
+    lib = C.CDLL(path)
+    fn = getattr(lib, f"{prefix}_gather")
+    fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.POINTER(C.c_uint64))]
+    fn.restype = C.c_int
+    fr = getattr(lib, f"{prefix}_gather_free")
+    fr.argtypes = [C.POINTER(C.c_uint64)]
+    fr.restype = None
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z)]
+    cen = [np.ascontiguousarray(a, dtype=np.float64) for a in (cx, cy, cz, rad)]
+    nh = len(cen[0])
+    off = np.zeros(nh + 1, np.uint64)
+    pidx = C.POINTER(C.c_uint64)()
+    rc = fn(len(arrs[0]), *[a.ctypes.data for a in arrs], nh, *[a.ctypes.data for a in cen], off.ctypes.data,
+            C.byref(pidx))
+    if rc != 0:
+        raise RuntimeError(f"{prefix}_gather failed ({rc})")
+    tot = int(off[-1])
+    idx = np.ctypeslib.as_array(pidx, shape=(max(tot, 1),))[:tot].copy() if tot else np.zeros(0, np.uint64)
+    fr(pidx)
+    return off, idx
+
+
+def gather_oracle(x, y, z, cx, cy, cz, rad):
+    """CSR (off, idx) of the restated gather: every particle within each
+    halo's radius, ascending index."""
+    return _gather(oracle_path(), "ahforacle", x, y, z, cx, cy, cz, rad)
+
+
+def gather_reference(x, y, z, cx, cy, cz, rad):
+    """CSR (off, idx) of the reference's own SFC gather (its order)."""
+    return _gather(ref_path(False), "ahfref", x, y, z, cx, cy, cz, rad)

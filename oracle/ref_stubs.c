@@ -1,8 +1,8 @@
 /*
  * ref_stubs.c -- link-time stand-ins for reference symbols that
  * src/libahf/ahf_halos.c and src/libutility/*.c reference but that the
- * unbinding + property stage never calls (output writers, logging, the SFC
- * gather, grid freeing, MPI termination).  TEST INFRASTRUCTURE ONLY: part of
+ * unbinding + property stage and the gather never call (output writers,
+ * logging, grid freeing, MPI termination).  TEST INFRASTRUCTURE ONLY: part of
  * oracle/_ref/libahfref.so.  Each aborts loudly if ever reached.
  */
 #include <stdio.h>
@@ -15,13 +15,6 @@ STUB(ahf_io_WriteHalos)
 STUB(ahf_io_WriteParticles)
 STUB(ahf_io_WriteProfiles)
 STUB(ahf_io_WriteSubstructure)
-STUB(ahf_halos_sfc_constructHalo)
 STUB(common_terminate)
 STUB(io_logging_msg)
 STUB(timer_getTime)
-STUB(util_bsearch)
-STUB(sfc_curve_calcKey)
-STUB(sfc_curve_calcPos)
-STUB(sfc_curve_getShell)
-STUB(sfc_curve_prolongMax)
-STUB(sfc_curve_prolongMin)

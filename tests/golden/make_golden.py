@@ -13,6 +13,9 @@ lists, and hand-built edge cases (empty list, fewer than MINPART particles,
 haloes straddling the periodic boundary, a particle exactly at the centre,
 every particle unbound, the innermost particle unbound, a halo that falls
 below MINPART during unbinding, list sizes around warp/block boundaries).
+The gather fixtures (gather_*.npz) hold the reference's own particle gather
+(ahf_halos_sfc_gatherParts with its Hilbert-key setup) on a cfg1 snapshot and
+on hand-built periodic-boundary and radius edge cases.
 """
 from __future__ import annotations
 
@@ -180,5 +183,25 @@ def main() -> None:
               os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def gather_cases():
+    """Inputs of the particle-gather fixtures: a cfg1 snapshot (its lists
+    plus 60,000 uniform particles) and the hand-built edge cases."""
+    L = synth.generate("cfg1")
+    return [("gather_cfg1", synth.snapshot_from_lists(L, 60000)), ("gather_edges", synth.gather_edge_snapshot())]
+
+
+def make_gather() -> None:
+    """The reference's own SFC gather (ahf_halos_sfc_gatherParts) on each
+    case; lists stored in the reference's order."""
+    import oracle as O
+    O.build()
+    for name, S in gather_cases():
+        off, idx = O.gather_reference(S.x, S.y, S.z, S.cx, S.cy, S.cz, S.rad)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), x=S.x, y=S.y, z=S.z, cx=S.cx, cy=S.cy, cz=S.cz,
+                            rad=S.rad, off=off, idx=idx)
+        print(name, S.n, S.nhalo, "gathered", int(off[-1]), os.path.getsize(os.path.join(HERE, name + ".npz")))
+
+
 if __name__ == "__main__":
     main()
+    make_gather()
