@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--plain-particles", type=float, default=2e7, help="plain FP64 form sample size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-gather", action="store_true", help="skip the particle-gather leg")
+    ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
     ap.add_argument("--multimass", action="store_true")
     return ap.parse_args()
 
@@ -171,6 +173,69 @@ def alg_bytes(n_in: np.ndarray, res_halo, has_w: bool) -> float:
     nbins = res_halo["nbins"].astype(np.float64)
     per_p = 24.0 + (4.0 if has_w else 0.0)
     return float(per_p * n_in.sum() + 16.0 * nb.sum() + (24.0 + 256.0) * len(n_in) + 8.0 * 25.0 * nbins.sum())
+
+
+def gather_radii(lists, n_in: np.ndarray):
+    """Per halo: the farthest periodic distance of its own list's particles
+    from its centre (the lists were drawn out to 1.5 R_vir), on the GPU."""
+    import torch
+    dev = lists.x.device
+    hid = torch.repeat_interleave(torch.arange(len(n_in), device=dev), torch.as_tensor(n_in, device=dev))
+    d2 = torch.zeros(len(hid), dtype=torch.float64, device=dev)
+    for a, c in ((lists.x, lists.cx), (lists.y, lists.cy), (lists.z, lists.cz)):
+        d = (a.double() - torch.as_tensor(c, device=dev)[hid]).abs()
+        d = torch.where(d > 0.5, 1.0 - d, d)
+        d2 += d * d
+        del d
+    m = torch.zeros(len(n_in), dtype=torch.float64, device=dev).scatter_reduce(0, hid, d2, "amax")
+    return m.sqrt()
+
+
+def gather_leg(lists, n_in: np.ndarray, args, ws: int, rank: int) -> dict:
+    """The particle gather (ahfgpu_gather_device) on the workload's lists as
+    one snapshot: every list particle once, each halo's radius the farthest
+    of its own particles.  Timed like the stage (CUDA events, W warm-up
+    calls), with the restated gather's grid search on a bounded sample of the
+    haloes on the host cores beside it."""
+    import torch
+    from ahf_gb300 import lib
+    parts = {k: getattr(lists, k) for k in ("x", "y", "z", "vx", "vy", "vz", "w")}
+    rad = gather_radii(lists, n_in)
+    cen = {"cx": torch.as_tensor(lists.cx).cuda(), "cy": torch.as_tensor(lists.cy).cuda(),
+           "cz": torch.as_tensor(lists.cz).cuda(), "rad": rad}
+    torch.cuda.synchronize()
+    for _ in range(max(1, args.warmup)):
+        b = lib.gather_device(parts, cen)
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b = lib.gather_device(parts, cen)
+    torch.cuda.synchronize()
+    dt = allmax(ws, (time.perf_counter() - t0) / args.steps)
+    off, _ = lib.gathered_lists(b)
+    ng = int(off[-1])
+    out = {"metric": "particles gathered/s", "value": allsum(ws, float(ng)) / dt, "unit": "particles/s",
+           "ms_per_step": dt * 1e3, "n_particles": int(lists.x.numel()), "n_halos": int(len(n_in)),
+           "n_gathered": ng, "workload": f"{args.workload} lists as one snapshot, radius = farthest own particle",
+           "timing": "host wall clock around each synchronous call", "cpu_baseline": None}
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build(ref=False)
+        samp = cpu_sample(n_in, args.gather_cpu_particles, seed=17)
+        sub = _device_subset(lists, samp)
+        xs = {k: sub[k].cpu().numpy() for k in ("x", "y", "z")}
+        r = rad[torch.as_tensor(samp, device=rad.device)].cpu().numpy()
+        c = [np.asarray(getattr(lists, k))[samp] for k in ("cx", "cy", "cz")]
+        t1 = time.perf_counter()
+        coff, _ = O.gather_oracle(xs["x"], xs["y"], xs["z"], c[0], c[1], c[2], r)
+        cdt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": float(coff[-1]) / cdt, "unit": "particles/s", "cores": os.cpu_count() or 1,
+                               "kind": "port",
+                               "sample": f"the lists of {len(samp)} seeded random haloes ({int(coff[-1])} gathered) "
+                                         f"as their own snapshot, grid search, {cdt:.2f} s"}
+    return out
 
 
 def cpu_sample(n_in: np.ndarray, target: float, seed: int = 99) -> np.ndarray:
@@ -414,6 +479,10 @@ def ours_arm(args, ws, rank, local):
             e2e[k] = float(v)
         e2e["ms_per_call"] = [round(float(v), 2) for v in lib_total]
 
+    gather = None
+    if not args.no_gather:
+        gather = gather_leg(lists, n_in, args, ws, rank)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         lists_np = host_lists(lists)
@@ -444,6 +513,7 @@ def ours_arm(args, ws, rank, local):
         "clocks": ck,
         "gpu_launches": int(launches),
         "forms": forms,
+        "gather": gather,
         "diagnostics": headline_stats,
     }
     print(json.dumps(line), flush=True)

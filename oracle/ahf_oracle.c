@@ -801,6 +801,8 @@ void ahforacle_result_free(ahfgpu_result *r)
  * (:69-78) on the float position promoted to double.  The kept set is
  * therefore every particle within the radius; this restatement lists it in
  * ascending particle index (the reference's order follows its SFC cells).
+ * Candidate particles come from a uniform grid (below), a superset of the
+ * sphere; the kept set is decided by the reference's test alone.
  */
 static double gather_d2(float px, float py, float pz, double cx, double cy, double cz)
 {
@@ -811,33 +813,104 @@ static double gather_d2(float px, float py, float pz, double cx, double cy, doub
   return dx * dx + dy * dy + dz * dz;
 }
 
+/* Candidates come from a uniform grid of G^3 cells (about half the median
+ * radius, 8..256 per axis), scanned one cell beyond each sphere; the test
+ * itself is the reference's.  Lists in ascending particle index.          */
+static int gather_cell(float x, int G)
+{
+  int c = (int)((double)x * (double)G);
+  return c < 0 ? 0 : (c >= G ? G - 1 : c);
+}
+
+static int cmp_u64(const void *a, const void *b)
+{
+  uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+  return x < y ? -1 : x > y;
+}
+
+static double median_radius(const double *rad, int64_t nhalo)
+{
+  double *t = (double *)malloc((size_t)(nhalo > 0 ? nhalo : 1) * sizeof(double));
+  if (!t) return 0.5;
+  memcpy(t, rad, (size_t)nhalo * sizeof(double));
+  for (int64_t i = 1; i < nhalo; i++) {           /* insertion sort is enough here */
+    double v = t[i];
+    int64_t j = i;
+    while (j > 0 && t[j - 1] > v) { t[j] = t[j - 1]; j--; }
+    t[j] = v;
+  }
+  double m = nhalo > 0 ? t[nhalo / 2] : 0.5;
+  free(t);
+  return m;
+}
+
+/* one halo's matches, ascending; returns the count (buf NULL: count only) */
+static uint64_t gather_one(const float *x, const float *y, const float *z, const uint64_t *start,
+                           const uint64_t *order, int G, double cx, double cy, double cz, double r,
+                           uint64_t *buf)
+{
+  const double r2 = r * r, cc[3] = {cx, cy, cz};
+  int lo[3], nd[3];
+  for (int d = 0; d < 3; d++) {
+    long long a = (long long)floor((cc[d] - r) * G) - 1, b = (long long)floor((cc[d] + r) * G) + 1;
+    if (!(r >= 0.0) || b - a + 1 >= G) { lo[d] = 0; nd[d] = G; }
+    else { lo[d] = (int)(((a % G) + G) % G); nd[d] = (int)(b - a + 1); }
+  }
+  uint64_t k = 0;
+  for (int i = 0; i < nd[0]; i++)
+    for (int j = 0; j < nd[1]; j++)
+      for (int l = 0; l < nd[2]; l++) {
+        uint64_t c = ((uint64_t)((lo[0] + i) % G) * G + (uint64_t)((lo[1] + j) % G)) * G + (uint64_t)((lo[2] + l) % G);
+        for (uint64_t q = start[c]; q < start[c + 1]; q++) {
+          uint64_t p = order[q];
+          if (gather_d2(x[p], y[p], z[p], cx, cy, cz) <= r2) {
+            if (buf) buf[k] = p;
+            k++;
+          }
+        }
+      }
+  if (buf) qsort(buf, (size_t)k, sizeof(uint64_t), cmp_u64);
+  return k;
+}
+
 int ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z, int64_t nhalo,
                      const double *cx, const double *cy, const double *cz, const double *rad,
                      uint64_t *out_off, uint64_t **out_idx)
 {
+  const double rmed = median_radius(rad, nhalo);
+  int G = rmed > 0 ? (int)fmin(256.0, fmax(8.0, floor(2.0 / rmed))) : 8;
+  const uint64_t m = (uint64_t)G * G * G;
+  uint64_t *start = (uint64_t *)calloc(m + 1, sizeof(uint64_t));
+  uint64_t *order = (uint64_t *)malloc((size_t)(n ? n : 1) * sizeof(uint64_t));
   uint64_t *cnt = (uint64_t *)calloc((size_t)(nhalo > 0 ? nhalo : 1), sizeof(uint64_t));
-  if (!cnt) return -1;
-#pragma omp parallel for schedule(dynamic)
-  for (int64_t h = 0; h < nhalo; h++) {
-    const double r2 = rad[h] * rad[h];
-    uint64_t c = 0;
-    for (uint64_t i = 0; i < n; i++)
-      if (gather_d2(x[i], y[i], z[i], cx[h], cy[h], cz[h]) <= r2) c++;
-    cnt[h] = c;
+  if (!start || !order || !cnt) { free(start); free(order); free(cnt); return -1; }
+  /* counting sort of the particles by cell (particle order within a cell) */
+  for (uint64_t i = 0; i < n; i++) {
+    uint64_t c = ((uint64_t)gather_cell(x[i], G) * G + (uint64_t)gather_cell(y[i], G)) * G + (uint64_t)gather_cell(z[i], G);
+    start[c + 1]++;
   }
+  for (uint64_t c = 0; c < m; c++) start[c + 1] += start[c];
+  {
+    uint64_t *fill = (uint64_t *)malloc((size_t)m * sizeof(uint64_t));
+    if (!fill) { free(start); free(order); free(cnt); return -1; }
+    memcpy(fill, start, (size_t)m * sizeof(uint64_t));
+    for (uint64_t i = 0; i < n; i++) {
+      uint64_t c = ((uint64_t)gather_cell(x[i], G) * G + (uint64_t)gather_cell(y[i], G)) * G + (uint64_t)gather_cell(z[i], G);
+      order[fill[c]++] = i;
+    }
+    free(fill);
+  }
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t h = 0; h < nhalo; h++) cnt[h] = gather_one(x, y, z, start, order, G, cx[h], cy[h], cz[h], rad[h], NULL);
   out_off[0] = 0;
   for (int64_t h = 0; h < nhalo; h++) out_off[h + 1] = out_off[h] + cnt[h];
-  free(cnt);
   uint64_t tot = nhalo > 0 ? out_off[nhalo] : 0;
   uint64_t *idx = (uint64_t *)malloc((size_t)(tot ? tot : 1) * sizeof(uint64_t));
-  if (!idx) return -1;
+  if (!idx) { free(start); free(order); free(cnt); return -1; }
 #pragma omp parallel for schedule(dynamic)
-  for (int64_t h = 0; h < nhalo; h++) {
-    const double r2 = rad[h] * rad[h];
-    uint64_t k = out_off[h];
-    for (uint64_t i = 0; i < n; i++)
-      if (gather_d2(x[i], y[i], z[i], cx[h], cy[h], cz[h]) <= r2) idx[k++] = i;
-  }
+  for (int64_t h = 0; h < nhalo; h++)
+    gather_one(x, y, z, start, order, G, cx[h], cy[h], cz[h], rad[h], idx + out_off[h]);
+  free(start); free(order); free(cnt);
   *out_idx = idx;
   return 0;
 }
