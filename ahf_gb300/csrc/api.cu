@@ -36,7 +36,7 @@ void gather_scatter(uint64_t n, const float* x, const float* y, const float* z, 
                     const uint32_t* start, uint32_t* fill, float4* sorted, int grid, cudaStream_t st);
 void gather_halos(int pass, int G, const uint32_t* start, const float4* sorted, int64_t nhalo, const int32_t* queue,
                   unsigned int* qhead, const double* cx, const double* cy, const double* cz, const double* rad,
-                  uint64_t* cnt, const uint64_t* off, unsigned int* hfill, uint64_t* out_idx, int grid,
+                  uint64_t* cnt, const uint64_t* off, unsigned long long* hfill, uint64_t* out_idx, int grid,
                   cudaStream_t st);
 void gather_offsets(const uint64_t* cnt, int64_t nhalo, uint64_t* off, cudaStream_t st);
 int gather_sort_setup();
@@ -1143,7 +1143,7 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
   EN(g.ga_qhead, 64);
   EN(g.ga_cnt, nh * 8);
   EN(g.ga_off, (nh + 1) * 8);
-  EN(g.ga_hfill, nh * 4);
+  EN(g.ga_hfill, nh * 8);
   EN(g.ga_err, 64);
   const int grid_p = std::max(1, std::min<int>(g.nsm * 8, (int)((n + 255) / 256)));
   const int grid_h = std::max(1, std::min<int>(g.nsm * 4, (int)std::max<int64_t>(nh, 1)));
@@ -1153,7 +1153,8 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
   CK(cudaMemsetAsync(g.ga_err.p, 0, 64, st));
   if (nh > 0) {
     CK(cudaMemcpyAsync(g.ga_queue.p, queue.data(), nh * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(g.ga_hfill.p, 0, nh * 4, st));
+    CK(cudaMemsetAsync(g.ga_hfill.p, 0, nh * 8, st));
+    CK(cudaMemsetAsync(g.ga_cnt.p, 0, nh * 8, st));
   }
   if (n > 0) gather_cells(n, parts->x, parts->y, parts->z, G, g.ga_cell.as<uint32_t>(), g.ga_count.as<uint32_t>(), grid_p, st);
   gather_scan_u32(g.ga_count.as<uint32_t>(), g.ga_start.as<uint32_t>(), m, g.ga_sums.as<uint32_t>(), st);
@@ -1187,7 +1188,7 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
     CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
     gather_halos(1, G, g.ga_start.as<uint32_t>(), g.ga_sorted.as<float4>(), nh, g.ga_queue.as<int32_t>(),
                  g.ga_qhead.as<unsigned int>(), cen->cx, cen->cy, cen->cz, cen->rad, g.ga_cnt.as<uint64_t>(),
-                 g.ga_off.as<uint64_t>(), g.ga_hfill.as<unsigned int>(), g.ga_idx.as<uint64_t>(), grid_h, st);
+                 g.ga_off.as<uint64_t>(), g.ga_hfill.as<unsigned long long>(), g.ga_idx.as<uint64_t>(), grid_h, st);
     CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
     gather_sort(nh, g.ga_queue.as<int32_t>(), g.ga_qhead.as<unsigned int>(), g.ga_off.as<uint64_t>(),
                 g.ga_idx.as<uint64_t>(), g.ga_idxA.as<uint32_t>(), g.ga_keyB.as<uint64_t>(), g.ga_idxB.as<uint32_t>(),

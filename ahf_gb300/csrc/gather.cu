@@ -125,9 +125,35 @@ __global__ void k_gather_scatter(uint64_t n, const float* __restrict__ x, const 
   }
 }
 
-// One CTA per halo (persistent, queue largest radius first).  Pass 0 counts
-// the matches of each halo into cnt[h]; pass 1 writes their particle indices
-// at off[h] (unordered; k_gather_sort orders them).
+// FP32 screen of the sphere test: 1 = surely inside, 0 = surely outside,
+// -1 = too close to the surface to tell.  Per axis |dxf - dx| <= 4e-7
+// (positions < 1: the centre's rounding to float and the subtraction lose
+// 6e-8 each, and where float and double fold differently near 0.5 the two
+// values differ by twice that plus the fold's rounding), so
+// |d2f - d2| <= 8e-7 (dxf + dyf + dzf) + 1.8e-7 d2f, below the margin
+// 1e-6 (dxf + dyf + dzf + d2f) + 1e-12; lo and hi bracket r2 even after
+// r2's rounding to float.
+__device__ __forceinline__ int gather_screen(float px, float py, float pz, float fx, float fy, float fz, float r2f) {
+  float dx = fabsf(__fsub_rn(px, fx)), dy = fabsf(__fsub_rn(py, fy)), dz = fabsf(__fsub_rn(pz, fz));
+  if (dx > 0.5f) dx = __fsub_rn(1.0f, dx);
+  if (dy > 0.5f) dy = __fsub_rn(1.0f, dy);
+  if (dz > 0.5f) dz = __fsub_rn(1.0f, dz);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  const float err = __fmaf_rn(1e-6f, __fadd_rn(__fadd_rn(dx, dy), __fadd_rn(dz, d2)), 1e-12f);
+  const float lo = __fmaf_rn(-4e-7f, r2f, r2f), hi = __fmaf_rn(4e-7f, r2f, r2f);
+  if (__fadd_rn(d2, err) < lo) return 1;
+  if (__fsub_rn(d2, err) > hi) return 0;
+  return -1;
+}
+
+// One CTA per halo (persistent, queue largest radius first).  The CTA's
+// warps walk the grid cells the halo's sphere can touch together, cutting
+// each cell's particles into chunks of 32 x 8 and taking every eighth chunk
+// of the walk, so a halo of millions of particles is spread over all warps.
+// Pass 0 adds each warp's matches to cnt[h] (zeroed before); pass 1 writes
+// the particle indices at off[h] + a per-chunk reservation (k_gather_sort
+// orders them).  The FP32 screen decides all but the particles near the
+// surface, which take the reference's FP64 test.
 __global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uint32_t* __restrict__ start,
                                                       const float4* __restrict__ sorted, int64_t nhalo,
                                                       const int32_t* __restrict__ queue,
@@ -135,58 +161,90 @@ __global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uin
                                                       const double* __restrict__ cx, const double* __restrict__ cy,
                                                       const double* __restrict__ cz, const double* __restrict__ rad,
                                                       uint64_t* __restrict__ cnt, const uint64_t* __restrict__ off,
-                                                      unsigned int* __restrict__ hfill,
+                                                      unsigned long long* __restrict__ hfill,
                                                       uint64_t* __restrict__ out_idx) {
+  constexpr int U = 8;                 // particles in flight per lane
+  constexpr uint32_t CH = 32 * U;      // particles per chunk
   __shared__ int s_h;
-  __shared__ unsigned long long s_cnt;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned FULL = 0xffffffffu;
   while (true) {
     if (threadIdx.x == 0) {
       const unsigned q = atomicAdd(qhead, 1u);
       s_h = q < (unsigned)nhalo ? queue[q] : -1;
-      s_cnt = 0;
     }
     __syncthreads();
     const int h = s_h;
+    __syncthreads();
     if (h < 0) break;
     const double ccx = cx[h], ccy = cy[h], ccz = cz[h], r = rad[h];
     const double r2 = __dmul_rn(r, r);
+    const float fx = (float)ccx, fy = (float)ccy, fz = (float)ccz, r2f = (float)r2;
     // cells the sphere can touch, one cell of margin for the float cell
     // assignment; a span of G or more covers the whole periodic axis once
     int lo[3], nd[3];
     const double cc[3] = {ccx, ccy, ccz};
+#pragma unroll
     for (int d = 0; d < 3; d++) {
       const long long a = (long long)floor((cc[d] - r) * (double)G) - 1;
       const long long b = (long long)floor((cc[d] + r) * (double)G) + 1;
       if (!(r >= 0.0) || b - a + 1 >= G) { lo[d] = 0; nd[d] = G; }
       else { lo[d] = (int)(((a % G) + G) % G); nd[d] = (int)(b - a + 1); }
     }
-    const long long ncell = (long long)nd[0] * nd[1] * nd[2];
-    unsigned long long mine = 0;
-    for (long long k = wid; k < ncell; k += nw) {
-      const int kz = (int)(k % nd[2]), ky = (int)((k / nd[2]) % nd[1]), kx = (int)(k / ((long long)nd[2] * nd[1]));
-      const int ix = (lo[0] + kx) % G, iy = (lo[1] + ky) % G, iz = (lo[2] + kz) % G;
-      const uint32_t c = ((uint32_t)ix * (uint32_t)G + (uint32_t)iy) * (uint32_t)G + (uint32_t)iz;
-      const uint32_t s0 = start[c], s1 = start[c + 1];
-      for (uint32_t j = s0 + lane; j < s1; j += 32) {
-        const float4 p = sorted[j];
-        if (gather_d2(p.x, p.y, p.z, ccx, ccy, ccz) <= r2) {
-          if (pass == 0) {
-            mine++;
-          } else {
-            const unsigned q = atomicAdd(&hfill[h], 1u);
-            out_idx[off[h] + q] = (uint64_t)__float_as_uint(p.w);
+    unsigned long long found = 0;
+    uint64_t chunk = 0;                // chunks of the walk so far
+    for (int kx = 0; kx < nd[0]; kx++) {
+      const uint32_t ix = (uint32_t)((lo[0] + kx) % G);
+      for (int ky = 0; ky < nd[1]; ky++) {
+        const uint32_t iy = (uint32_t)((lo[1] + ky) % G);
+        for (int kz = 0; kz < nd[2]; kz++) {
+          const uint32_t c = (ix * (uint32_t)G + iy) * (uint32_t)G + (uint32_t)((lo[2] + kz) % G);
+          const uint32_t s0 = start[c], s1 = start[c + 1];
+          const uint64_t nch = (s1 - s0 + CH - 1) / CH;
+          // this warp's chunks of the cell: global chunk numbers = wid mod nw
+          uint64_t first = (uint64_t)((wid - (int)(chunk % (uint64_t)nw) + nw) % nw);
+          for (uint64_t k = first; k < nch; k += (uint64_t)nw) {
+            const uint32_t j0 = s0 + (uint32_t)(k * CH);
+            float4 p[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+              const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
+              p[u] = j < s1 ? sorted[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            unsigned m[U];
+            unsigned tot = 0;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+              const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
+              bool in = false;
+              if (j < s1) {
+                const int sc = gather_screen(p[u].x, p[u].y, p[u].z, fx, fy, fz, r2f);
+                in = sc > 0 || (sc < 0 && gather_d2(p[u].x, p[u].y, p[u].z, ccx, ccy, ccz) <= r2);
+              }
+              m[u] = __ballot_sync(FULL, in);
+              tot += (unsigned)__popc(m[u]);
+            }
+            if (pass == 0) {
+              found += tot;
+            } else if (tot) {
+              unsigned long long b = 0;
+              if (lane == 0) b = atomicAdd(&hfill[h], (unsigned long long)tot);
+              b = __shfl_sync(FULL, b, 0);
+              const uint64_t at = off[h] + b;
+              unsigned run = 0;
+#pragma unroll
+              for (int u = 0; u < U; u++) {
+                if ((m[u] >> lane) & 1u)
+                  out_idx[at + run + (unsigned)__popc(m[u] & ((1u << lane) - 1u))] = (uint64_t)__float_as_uint(p[u].w);
+                run += (unsigned)__popc(m[u]);
+              }
+            }
           }
+          chunk += nch;
         }
       }
     }
-    if (pass == 0) {
-      for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
-      if (lane == 0 && mine) atomicAdd(&s_cnt, mine);
-      __syncthreads();
-      if (threadIdx.x == 0) cnt[h] = s_cnt;
-    }
-    __syncthreads();
+    if (pass == 0 && lane == 0 && found) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[h]), found);
   }
 }
 
@@ -288,7 +346,7 @@ void gather_scatter(uint64_t n, const float* x, const float* y, const float* z, 
 
 void gather_halos(int pass, int G, const uint32_t* start, const float4* sorted, int64_t nhalo, const int32_t* queue,
                   unsigned int* qhead, const double* cx, const double* cy, const double* cz, const double* rad,
-                  uint64_t* cnt, const uint64_t* off, unsigned int* hfill, uint64_t* out_idx, int grid,
+                  uint64_t* cnt, const uint64_t* off, unsigned long long* hfill, uint64_t* out_idx, int grid,
                   cudaStream_t st) {
   k_gather_halos<<<grid, 256, 0, st>>>(pass, G, start, sorted, nhalo, queue, qhead, cx, cy, cz, rad, cnt, off, hfill,
                                        out_idx);

@@ -4,6 +4,7 @@
     python -m ahf_gb300.profcase medium [mode]  # 300 haloes of 2048..16384 particles
     python -m ahf_gb300.profcase big [mode]     # one halo of ~2e5 particles
     python -m ahf_gb300.profcase full [mode]    # the whole 1e5-halo workload
+    python -m ahf_gb300.profcase gather [scale] # the particle gather, the lists of 1e5*scale haloes as a snapshot
 
 Each runs the stage twice on a device-resident batch cut from the seeded
 1e5-halo workload (cfg3) and prints the device time and diagnostics.
@@ -33,9 +34,40 @@ def subset(lists, halos):
     return t
 
 
+def gather_case(scale: float = 0.05) -> None:
+    import time
+    import torch
+    from . import lib, synth
+    lib.init(0)
+    L = synth.generate("cfg3", scale=scale, device="cuda", as_numpy=False)
+    n = np.diff(L.off.astype(np.int64))
+    dev = L.x.device
+    hid = torch.repeat_interleave(torch.arange(len(n), device=dev), torch.as_tensor(n, device=dev))
+    d2 = torch.zeros(len(hid), dtype=torch.float64, device=dev)
+    for a, c in ((L.x, L.cx), (L.y, L.cy), (L.z, L.cz)):
+        d = (a.double() - torch.as_tensor(c, device=dev)[hid]).abs()
+        d2 += torch.where(d > 0.5, 1.0 - d, d) ** 2
+    rad = torch.zeros(len(n), dtype=torch.float64, device=dev).scatter_reduce(0, hid, d2, "amax").sqrt()
+    parts = {k: getattr(L, k) for k in ("x", "y", "z", "vx", "vy", "vz", "w")}
+    cen = {"cx": torch.as_tensor(L.cx).cuda(), "cy": torch.as_tensor(L.cy).cuda(), "cz": torch.as_tensor(L.cz).cuda(),
+           "rad": rad}
+    ms = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b = lib.gather_device(parts, cen)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    off, _ = lib.gathered_lists(b)
+    print(f"gather: haloes {len(n)} particles {int(L.x.numel())} gathered {int(off[-1])} "
+          f"ms per call {', '.join(f'{m:.1f}' for m in ms)}")
+
+
 def main(argv):
     from . import lib, synth
     which = argv[0] if argv else "small"
+    if which == "gather":
+        gather_case(float(argv[1]) if len(argv) > 1 else 0.05)
+        return
     mode = argv[1] if len(argv) > 1 else "batched_fp32c"
     lib.init(0)
     scale = 1.0 if which == "full" else 0.05
