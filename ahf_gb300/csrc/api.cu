@@ -43,6 +43,8 @@ int gather_sort_setup();
 void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
                  uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int* err, int grid,
                  cudaStream_t st);
+void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
+                  const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st);
 void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
                  const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
                  float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st);
@@ -139,6 +141,7 @@ struct Ctx {
   // gathered batch
   DBuf ga_cell, ga_count, ga_start, ga_fill, ga_sums, ga_sorted, ga_queue, ga_qhead, ga_cnt, ga_off, ga_hfill;
   DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
+  DBuf gr_pos, gr_lim, gr_orig;   // gather radii: sorted centres and R_vir, candidate counts, order
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -854,7 +857,7 @@ int ahfgpu_shutdown(void) {
                   &g.ga_cell, &g.ga_count, &g.ga_start, &g.ga_fill, &g.ga_sums, &g.ga_sorted, &g.ga_queue,
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
-                  &g.ga_id, &g.phase};
+                  &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1210,6 +1213,48 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
   out->w = parts->w ? g.ga_w.as<float>() : nullptr;
   out->gidx = g.ga_id.as<uint64_t>();
   out->cx = cen->cx; out->cy = cen->cy; out->cz = cen->cz;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_gather_radii_device(int64_t nh, const uint64_t* npart, const double* cx, const double* cy,
+                               const double* cz, const double* rvir, double max_gather_rad_box, double* rad,
+                               void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (nh < 0 || nh > 0x7fffffff) return fail(AHFGPU_ERR_INVALID, "nhalo %lld out of range", (long long)nh);
+  if (nh == 0) return AHFGPU_OK;
+  if (!npart || !cx || !cy || !cz || !rvir || !rad) return fail(AHFGPU_ERR_INVALID, "a gather-radius array is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  // counts, centres and R_vir to the host: the order by particle count
+  // (largest first) and each halo's number of strictly larger haloes
+  std::vector<uint64_t> np(nh);
+  std::vector<double> h4((size_t)nh * 4);
+  CK(cudaMemcpyAsync(np.data(), npart, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h4.data(), cx, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h4.data() + nh, cy, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h4.data() + 2 * nh, cz, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h4.data() + 3 * nh, rvir, nh * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  std::vector<int32_t> ord(nh);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return np[a] > np[b] || (np[a] == np[b] && a < b); });
+  std::vector<int64_t> lim(nh);
+  std::vector<double> sp((size_t)nh * 4);
+  for (int64_t s2 = 0; s2 < nh; s2++) {
+    lim[s2] = (s2 > 0 && np[ord[s2]] == np[ord[s2 - 1]]) ? lim[s2 - 1] : s2;
+    for (int k = 0; k < 4; k++) sp[(size_t)k * nh + s2] = h4[(size_t)k * nh + ord[s2]];
+  }
+  const double maxr = std::min(max_gather_rad_box, 0.25);
+  if ((rc = g.gr_pos.ensure(nh * 32))) return rc;
+  if ((rc = g.gr_lim.ensure(nh * 8))) return rc;
+  if ((rc = g.gr_orig.ensure(nh * 4))) return rc;
+  CK(cudaMemcpyAsync(g.gr_pos.p, sp.data(), nh * 32, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(g.gr_lim.p, lim.data(), nh * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(g.gr_orig.p, ord.data(), nh * 4, cudaMemcpyHostToDevice, st));
+  const double* d = g.gr_pos.as<double>();
+  gather_radii(nh, d, d + nh, d + 2 * nh, g.gr_lim.as<int64_t>(), d + 3 * nh, g.gr_orig.as<int32_t>(), maxr, rad, st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
   return AHFGPU_OK;
 }
 

@@ -324,6 +324,81 @@ __global__ void k_gather_pack(uint64_t ng, const uint64_t* __restrict__ idx, con
 }
 
 // ---------------------------------------------------------------------------
+// Gather radii: the loop of spatialRef2halos (src/libahf/ahf_halos.c:2987-3051).
+// Haloes come sorted by particle count, largest first (s = sorted position);
+// lim[s] = how many haloes have strictly more particles than halo s, i.e.
+// the candidates are sorted positions [0, lim[s]).  For each halo the
+// reference takes the smallest periodic squared distance (double, its
+// operation order) to a candidate; here pass A finds, in FP32, the smallest
+// upper bound m of any candidate's distance, and pass B evaluates in FP64 the
+// candidates whose lower bound is within m (they include every exact
+// minimiser).  Per-pair float error as in gather_screen: |d2f - d2| below
+// 1e-6 (dxf + dyf + dzf + d2f) + 1e-12.
+__device__ __forceinline__ float pair_d2f(float ax, float ay, float az, float bx, float by, float bz, float* err) {
+  float dx = fabsf(__fsub_rn(ax, bx)), dy = fabsf(__fsub_rn(ay, by)), dz = fabsf(__fsub_rn(az, bz));
+  if (dx > 0.5f) dx = __fsub_rn(1.0f, dx);
+  if (dy > 0.5f) dy = __fsub_rn(1.0f, dy);
+  if (dz > 0.5f) dz = __fsub_rn(1.0f, dz);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+  *err = __fmaf_rn(1e-6f, __fadd_rn(__fadd_rn(dx, dy), __fadd_rn(dz, d2)), 1e-12f);
+  return d2;
+}
+
+__device__ __forceinline__ double pair_d2(double ax, double ay, double az, double bx, double by, double bz) {
+  double dx = fabs(__dsub_rn(ax, bx)), dy = fabs(__dsub_rn(ay, by)), dz = fabs(__dsub_rn(az, bz));
+  if (dx > 0.5) dx = __dsub_rn(1.0, dx);
+  if (dy > 0.5) dy = __dsub_rn(1.0, dy);
+  if (dz > 0.5) dz = __dsub_rn(1.0, dz);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__global__ void __launch_bounds__(256) k_gather_radii(int64_t nh, const double* __restrict__ px,
+                                                      const double* __restrict__ py, const double* __restrict__ pz,
+                                                      const int64_t* __restrict__ lim, const double* __restrict__ rv,
+                                                      const int32_t* __restrict__ orig, double maxr,
+                                                      double* __restrict__ out) {
+  __shared__ double tx[256], ty[256], tz[256];
+  __shared__ float fx[256], fy[256], fz[256];
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = s < nh;
+  const int64_t my_lim = live ? lim[s] : 0;
+  const int64_t last = min((int64_t)(blockIdx.x + 1) * blockDim.x, nh) - 1;
+  const int64_t blim = lim[last];   // the block's largest candidate range (lim grows with s)
+  const double ax = live ? px[s] : 0.0, ay = live ? py[s] : 0.0, az = live ? pz[s] : 0.0;
+  const float afx = (float)ax, afy = (float)ay, afz = (float)az;
+  float m = 3.0e38f;
+  for (int pass = 0; pass < 2; pass++) {
+    double best = 100000000000.0;    // the reference's initial gatherRad
+    for (int64_t t0 = 0; t0 < blim; t0 += blockDim.x) {
+      const int64_t j = t0 + threadIdx.x;
+      if (j < blim) {
+        tx[threadIdx.x] = px[j]; ty[threadIdx.x] = py[j]; tz[threadIdx.x] = pz[j];
+        fx[threadIdx.x] = (float)px[j]; fy[threadIdx.x] = (float)py[j]; fz[threadIdx.x] = (float)pz[j];
+      }
+      __syncthreads();
+      const int64_t n = min((int64_t)blockDim.x, my_lim - t0);
+      for (int64_t k = 0; k < n; k++) {
+        float err;
+        const float d2f = pair_d2f(afx, afy, afz, fx[k], fy[k], fz[k], &err);
+        if (pass == 0) {
+          m = fminf(m, __fadd_rn(d2f, err));
+        } else if (__fsub_rn(d2f, err) <= m) {
+          const double d2 = pair_d2(ax, ay, az, tx[k], ty[k], tz[k]);
+          if (d2 < best) best = d2;
+        }
+      }
+      __syncthreads();
+    }
+    if (pass == 1 && live) {
+      double r = my_lim > 0 ? sqrt(best) * 0.5 : maxr;
+      r = fmax(r, rv[s]);
+      r = fmin(r, maxr);
+      out[orig[s]] = r;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // launchers (host)
 
 void gather_cells(uint64_t n, const float* x, const float* y, const float* z, int G, uint32_t* cell,
@@ -376,4 +451,12 @@ void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* 
   k_gather_pack<<<grid, 256, 0, st>>>(ng, idx, x, y, z, vx, vy, vz, w, ox, oy, oz, ovx, ovy, ovz, ow, oid);
 }
 
+}  // namespace ahfgpu
+
+namespace ahfgpu {
+void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
+                  const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st) {
+  const unsigned nb = (unsigned)((nh + 255) / 256);
+  if (nb) k_gather_radii<<<nb, 256, 0, st>>>(nh, px, py, pz, lim, rv, orig, maxr, out);
+}
 }  // namespace ahfgpu

@@ -22,7 +22,7 @@ LIB_PATH = os.environ.get("AHFGPU_LIB", os.path.join(HERE, "libahfgpu.so"))
 SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
-    "ahfgpu_gather_device",
+    "ahfgpu_gather_device", "ahfgpu_gather_radii_device",
 ]
 
 
@@ -66,6 +66,9 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_gather_device.argtypes = [C.POINTER(abi.Particles), C.POINTER(abi.Centres), C.POINTER(Batch),
                                          C.c_void_p]
     lib.ahfgpu_gather_device.restype = C.c_int
+    lib.ahfgpu_gather_radii_device.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
+    lib.ahfgpu_gather_radii_device.restype = C.c_int
     _lib = lib
     return lib
 
@@ -220,3 +223,15 @@ def gathered_lists(b: Batch):
     gid = (device_view(C.cast(b.gidx, C.c_void_p).value, n, "<u8").cpu().numpy().astype(np.uint64) if n
            else np.zeros(0, np.uint64))
     return off, gid
+
+
+def gather_radii_device(npart, cx, cy, cz, rvir, max_gather_rad_box: float, stream: int | None = None):
+    """ahfgpu_gather_radii_device on torch CUDA tensors; returns the radii
+    (float64 CUDA tensor)."""
+    import torch
+    init()
+    out = torch.empty(npart.numel(), dtype=torch.float64, device=npart.device)
+    check(load().ahfgpu_gather_radii_device(int(npart.numel()), npart.data_ptr(), cx.data_ptr(), cy.data_ptr(),
+                                           cz.data_ptr(), rvir.data_ptr(), float(max_gather_rad_box),
+                                           out.data_ptr(), C.c_void_p(stream) if stream else None))
+    return out

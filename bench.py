@@ -219,6 +219,39 @@ def gather_leg(lists, n_in: np.ndarray, args, ws: int, rank: int) -> dict:
            "ms_per_step": dt * 1e3, "n_particles": int(lists.x.numel()), "n_halos": int(len(n_in)),
            "n_gathered": ng, "workload": f"{args.workload} lists as one snapshot, radius = farthest own particle",
            "timing": "host wall clock around each synchronous call", "cpu_baseline": None}
+    # gather radii (spatialRef2halos' loop): every halo against every halo
+    # with more particles; R_vir stands in as 2/3 of the list radius, the cap
+    # is AHF's default MaxGatherRad = 3 Mpc/h over the box
+    npart = torch.as_tensor(n_in.astype(np.int64)).cuda()
+    rvir = rad / 1.5
+    maxg = 3.0 / float(lists.boxsize)
+    for _ in range(max(1, args.warmup)):
+        gr = lib.gather_radii_device(npart, cen["cx"], cen["cy"], cen["cz"], rvir, maxg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gr = lib.gather_radii_device(npart, cen["cx"], cen["cy"], cen["cz"], rvir, maxg)
+    torch.cuda.synchronize()
+    rdt = (time.perf_counter() - t0) / args.steps
+
+    def pairs(counts):
+        srt = np.sort(counts)
+        return float(np.sum(len(srt) - np.searchsorted(srt, counts, side="right")))
+    npairs = pairs(n_in)
+    out["radii"] = {"metric": "halo pairs/s", "value": npairs / rdt, "unit": "pairs/s", "ms_per_step": rdt * 1e3,
+                    "n_halos": int(len(n_in)), "n_pairs": npairs, "cpu_baseline": None}
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build(ref=False)
+        rs = np.random.default_rng(23).choice(len(n_in), size=min(len(n_in), 20000), replace=False)
+        cxyz = [np.asarray(getattr(lists, k))[rs] for k in ("cx", "cy", "cz")]
+        t1 = time.perf_counter()
+        O.gather_radii_oracle(n_in[rs].astype(np.uint64), cxyz[0], cxyz[1], cxyz[2], rvir.cpu().numpy()[rs], maxg)
+        rcdt = time.perf_counter() - t1
+        out["radii"]["cpu_baseline"] = {"value": pairs(n_in[rs]) / rcdt, "unit": "pairs/s", "cores": os.cpu_count() or 1,
+                                        "kind": "port", "sample": f"{len(rs)} seeded random haloes as their own "
+                                                                  f"catalogue, {rcdt:.2f} s"}
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O

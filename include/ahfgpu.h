@@ -219,6 +219,18 @@ AHFGPU_API int ahfgpu_gather_device(const ahfgpu_particles *parts,
                                     ahfgpu_batch           *gathered,
                                     void                   *stream);
 
+/* Replaces the gather-radius loop of spatialRef2halos
+ * (src/libahf/ahf_halos.c:2987-3051): for each halo, half the periodic
+ * distance (double, the reference's operation order) to the closest halo
+ * with strictly more particles, or max_rad without one; then raised to
+ * rvir[h] (the halo's R_vir at that stage) and capped at max_rad, where
+ * max_rad = min(MaxGatherRad / boxsize, 1/4) (:2987).  Device pointers:
+ * npart[nhalo], centres, rvir in; rad[nhalo] out.                          */
+AHFGPU_API int ahfgpu_gather_radii_device(int64_t nhalo, const uint64_t *npart,
+                                          const double *cx, const double *cy, const double *cz,
+                                          const double *rvir, double max_gather_rad_box,
+                                          double *rad, void *stream);
+
 /* Same stage with every pointer of `batch` already in device memory; the
  * results stay on the device in library-owned buffers (valid until the next
  * call or ahfgpu_shutdown) and are described by `dres` (device pointers,

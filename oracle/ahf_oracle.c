@@ -916,3 +916,39 @@ int ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z,
 }
 
 void ahforacle_gather_free(uint64_t *idx) { free(idx); }
+
+
+/* ---------------------------------------------------------------------------
+ * Gather radii, src/libahf/ahf_halos.c:2987-3051.  The reference walks the
+ * haloes in order of decreasing particle count and, for each, every halo
+ * before it with strictly more particles: the smallest periodic squared
+ * distance (LOCAL-style fold at 0.5, dx*dx + dy*dy + dz*dz) starting from
+ * 1e11 (:2535), then sqrt(.) * 0.5, max_rad when there is no such halo, then
+ * MAX with R_vir and MIN with max_rad = MIN(MaxGatherRad / boxsize, 1/4).
+ * The set of candidates does not depend on how ties in the count are
+ * ordered, so a plain scan over all haloes restates it.                    */
+void ahforacle_gather_radii(int64_t nhalo, const uint64_t *npart, const double *cx, const double *cy,
+                            const double *cz, const double *rvir, double max_gather_rad_box, double *rad)
+{
+  const double maxr = max_gather_rad_box < 0.25 ? max_gather_rad_box : 0.25;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < nhalo; i++) {
+    double best = 100000000000.0;
+    int64_t count = 0;
+    for (int64_t j = 0; j < nhalo; j++) {
+      if (j == i || !(npart[j] > npart[i])) continue;
+      double dx = fabs(cx[i] - cx[j]), dy = fabs(cy[i] - cy[j]), dz = fabs(cz[i] - cz[j]);
+      if (dx > 0.5) dx = 1.0 - dx;
+      if (dy > 0.5) dy = 1.0 - dy;
+      if (dz > 0.5) dz = 1.0 - dz;
+      double d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 < best) best = d2;
+      count++;
+    }
+    double r = sqrt(best) * 0.5;
+    if (count == 0) r = maxr;
+    r = r > rvir[i] ? r : rvir[i];
+    r = r < maxr ? r : maxr;
+    rad[i] = r;
+  }
+}

@@ -37,6 +37,13 @@ int  ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z
                       uint64_t *out_off, uint64_t **out_idx);
 void ahforacle_gather_free(uint64_t *idx);
 
+/* The gather radii, the loop of spatialRef2halos (src/libahf/ahf_halos.c:
+ * 2987-3051): half the distance to the closest halo with strictly more
+ * particles (or max_rad without one), raised to rvir, capped at max_rad =
+ * min(max_gather_rad_box, 1/4).                                            */
+void ahforacle_gather_radii(int64_t nhalo, const uint64_t *npart, const double *cx, const double *cy,
+                            const double *cz, const double *rvir, double max_gather_rad_box, double *rad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -127,3 +127,17 @@ def gather_oracle(x, y, z, cx, cy, cz, rad):
 def gather_reference(x, y, z, cx, cy, cz, rad):
     """CSR (off, idx) of the reference's own SFC gather (its order)."""
     return _gather(ref_path(False), "ahfref", x, y, z, cx, cy, cz, rad)
+
+
+def gather_radii_oracle(npart, cx, cy, cz, rvir, max_gather_rad_box: float):
+    """The restated gather-radius loop (spatialRef2halos)."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_gather_radii
+    fn.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+    fn.restype = None
+    a = [np.ascontiguousarray(npart, dtype=np.uint64)] + [np.ascontiguousarray(v, dtype=np.float64)
+                                                          for v in (cx, cy, cz, rvir)]
+    out = np.zeros(len(a[0]))
+    fn(len(a[0]), *[v.ctypes.data for v in a], float(max_gather_rad_box), out.ctypes.data)
+    return out
