@@ -27,6 +27,7 @@ UNITS = {
     "fp32c_dispatch.cu": [],
     "noalloc.cu": [],
     "gather.cu": [],
+    "writer.cu": [],
 }
 
 

@@ -45,6 +45,14 @@ void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const
                  cudaStream_t st);
 void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
                   const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st);
+void writer_count(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                  const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
+                  uint64_t* blk, unsigned long long* good, int grid, cudaStream_t st);
+void writer_offsets(const uint64_t* blk, int64_t nh, uint64_t* boff, cudaStream_t st);
+void writer_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                  const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
+                  const uint64_t* boff, const unsigned long long* good, unsigned char* out, int grid,
+                  cudaStream_t st);
 void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
                  const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
                  float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st);
@@ -142,6 +150,7 @@ struct Ctx {
   DBuf ga_cell, ga_count, ga_start, ga_fill, ga_sums, ga_sorted, ga_queue, ga_qhead, ga_cnt, ga_off, ga_hfill;
   DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
   DBuf gr_pos, gr_lim, gr_orig;   // gather radii: sorted centres and R_vir, candidate counts, order
+  DBuf wp_blk, wp_boff, wp_good, wp_qhead, wp_out;   // the AHF_particles bytes
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -857,7 +866,8 @@ int ahfgpu_shutdown(void) {
                   &g.ga_cell, &g.ga_count, &g.ga_start, &g.ga_fill, &g.ga_sums, &g.ga_sorted, &g.ga_queue,
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
-                  &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.phase};
+                  &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
+                  &g.wp_out, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1213,6 +1223,44 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
   out->w = parts->w ? g.ga_w.as<float>() : nullptr;
   out->gidx = g.ga_id.as<uint64_t>();
   out->cx = cen->cx; out->cy = cen->cy; out->cz = cen->cz;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int64_t* order, int64_t minpart,
+                                  const unsigned char** out, uint64_t* nbytes, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!out || !nbytes) return fail(AHFGPU_ERR_INVALID, "out/nbytes is NULL");
+  if (g.last_nhalo < 0) return fail(AHFGPU_ERR_STATE, "no device result to write");
+  const int64_t nh = g.last_nhalo;
+  if (nh > 0 && (!ids || !order)) return fail(AHFGPU_ERR_INVALID, "ids/order is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  if ((rc = g.wp_blk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
+  if ((rc = g.wp_boff.ensure((nh + 1) * 8))) return rc;
+  if ((rc = g.wp_good.ensure(64))) return rc;
+  if ((rc = g.wp_qhead.ensure(64))) return rc;
+  const int grid = std::max(1, std::min<int>(g.nsm * 4, (int)std::max<int64_t>(nh, 1)));
+  CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.wp_good.p, 0, 64, st));
+  if (nh > 0)
+    writer_count(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids, w,
+                 minpart, g.wp_qhead.as<unsigned int>(), g.wp_blk.as<uint64_t>(),
+                 g.wp_good.as<unsigned long long>(), grid, st);
+  writer_offsets(g.wp_blk.as<uint64_t>(), nh, g.wp_boff.as<uint64_t>(), st);
+  CK(cudaGetLastError());
+  uint64_t body = 0;
+  CK(cudaMemcpyAsync(&body, g.wp_boff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const uint64_t total = 16 + body;
+  if ((rc = g.wp_out.ensure(total))) return rc;
+  CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
+  writer_write(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids, w,
+               minpart, g.wp_qhead.as<unsigned int>(), g.wp_boff.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
+               g.wp_out.as<unsigned char>(), grid, st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  *out = g.wp_out.as<unsigned char>();
+  *nbytes = total;
   return AHFGPU_OK;
 }
 

@@ -22,7 +22,7 @@ LIB_PATH = os.environ.get("AHFGPU_LIB", os.path.join(HERE, "libahfgpu.so"))
 SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
-    "ahfgpu_gather_device", "ahfgpu_gather_radii_device",
+    "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
 ]
 
 
@@ -69,6 +69,9 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_gather_radii_device.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_double, C.c_void_p, C.c_void_p]
     lib.ahfgpu_gather_radii_device.restype = C.c_int
+    lib.ahfgpu_write_particles_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                                  C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]
+    lib.ahfgpu_write_particles_device.restype = C.c_int
     _lib = lib
     return lib
 
@@ -235,3 +238,16 @@ def gather_radii_device(npart, cx, cy, cz, rvir, max_gather_rad_box: float, stre
                                            cz.data_ptr(), rvir.data_ptr(), float(max_gather_rad_box),
                                            out.data_ptr(), C.c_void_p(stream) if stream else None))
     return out
+
+
+def write_particles_device(ids, w, order, minpart: int, stream: int | None = None):
+    """ahfgpu_write_particles_device for the last device result; ids, w
+    (or None), order are torch CUDA tensors.  Returns (device address,
+    nbytes) of the AHF_particles bytes."""
+    init()
+    out = C.c_void_p()
+    nb = C.c_uint64()
+    check(load().ahfgpu_write_particles_device(ids.data_ptr(), w.data_ptr() if w is not None else None,
+                                              order.data_ptr(), int(minpart), C.byref(out), C.byref(nb),
+                                              C.c_void_p(stream) if stream else None))
+    return out.value, nb.value

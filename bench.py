@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-gather", action="store_true", help="skip the particle-gather leg")
+    ap.add_argument("--no-writer", action="store_true", help="skip the AHF_particles writer leg")
     ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
     ap.add_argument("--multimass", action="store_true")
     return ap.parse_args()
@@ -173,6 +174,51 @@ def alg_bytes(n_in: np.ndarray, res_halo, has_w: bool) -> float:
     nbins = res_halo["nbins"].astype(np.float64)
     per_p = 24.0 + (4.0 if has_w else 0.0)
     return float(per_p * n_in.sum() + 16.0 * nb.sum() + (24.0 + 256.0) * len(n_in) + 8.0 * 25.0 * nbins.sum())
+
+
+def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
+    """The AHF_particles file of the last result on the GPU (ids = entry
+    index, haloes by decreasing kept count), timed like the stage; the
+    restated writer (snprintf per line, as the reference's fprintf) on a
+    bounded sample of the haloes on one host core beside it."""
+    import torch
+    from ahf_gb300 import lib
+    N = int(lists.x.numel())
+    ids = torch.arange(N, dtype=torch.int64, device="cuda")
+    npk = res.halo["npart"].astype(np.int64)
+    order_np = np.argsort(-npk, kind="stable").astype(np.int64)
+    order = torch.as_tensor(order_np).cuda()
+    for _ in range(max(1, args.warmup)):
+        addr, nb = lib.write_particles_device(ids, lists.w, order, 20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        addr, nb = lib.write_particles_device(ids, lists.w, order, 20)
+    torch.cuda.synchronize()
+    dt = allmax(ws, (time.perf_counter() - t0) / args.steps)
+    lines = int(npk[npk >= 20].sum() + (npk >= 20).sum() + 1)
+    out = {"metric": "AHF_particles bytes/s", "value": nb / dt, "unit": "bytes/s", "ms_per_step": dt * 1e3,
+           "bytes": int(nb), "lines": lines, "lines_per_s": lines / dt, "cpu_baseline": None}
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build(ref=False)
+        sel = np.random.default_rng(29).permutation(len(npk))
+        cum = np.cumsum(npk[sel])
+        sel = np.sort(sel[:int(np.searchsorted(cum, 1e7)) + 1])
+        moff = np.zeros(len(sel) + 1, np.uint64)
+        moff[1:] = np.cumsum(npk[sel])
+        mem = np.concatenate([res.member[int(res.member_off[h]):int(res.member_off[h + 1])] for h in sel])
+        sub_order = np.argsort(-npk[sel], kind="stable").astype(np.int64)
+        wn = lists.w.cpu().numpy() if lists.w is not None else None
+        t1 = time.perf_counter()
+        data = O.write_particles_oracle(np.arange(N, dtype=np.uint64), wn, moff, mem, npk[sel].astype(np.uint64),
+                                        sub_order, 20)
+        cdt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": len(data) / cdt, "unit": "bytes/s", "cores": 1, "kind": "port",
+                               "sample": f"the kept lists of {len(sel)} seeded random haloes ({len(data)} bytes), "
+                                         f"snprintf per line, {cdt:.2f} s"}
+    return out
 
 
 def gather_radii(lists, n_in: np.ndarray):
@@ -438,6 +484,11 @@ def ours_arm(args, ws, rank, local):
     tpp = ncu_traffic(args.workload, kname)
     traffic = tpp * N if tpp is not None else None
 
+    # the AHF_particles bytes of this result (ahfgpu_write_particles_device)
+    writer = None
+    if not args.no_writer:
+        writer = writer_leg(lists, res, args, ws, rank)
+
     # other forms, once each (same workload)
     forms = {}
     if args.forms != "none":
@@ -547,6 +598,7 @@ def ours_arm(args, ws, rank, local):
         "gpu_launches": int(launches),
         "forms": forms,
         "gather": gather,
+        "writer": writer,
         "diagnostics": headline_stats,
     }
     print(json.dumps(line), flush=True)

@@ -231,6 +231,18 @@ AHFGPU_API int ahfgpu_gather_radii_device(int64_t nhalo, const uint64_t *npart,
                                           const double *rvir, double max_gather_rad_box,
                                           double *rad, void *stream);
 
+/* Replaces WriteParticlesLegacy (src/libahf/ahf_io.c:1095-1175, default
+ * build; the AHF_particles file) for the last device-resident result: the
+ * file's exact bytes in a library-owned device buffer (*out, *nbytes; valid
+ * until the next call or ahfgpu_shutdown).  The kept entries of the result
+ * index ids[] (and w[], NULL without weights) -- the particle index when the
+ * batch's gidx held HALO.ipart; order[nhalo] (device) is the reference's idx
+ * (the output order); haloes below minpart are left out as the reference
+ * does.                                                                    */
+AHFGPU_API int ahfgpu_write_particles_device(const uint64_t *ids, const float *w, const int64_t *order,
+                                             int64_t minpart, const unsigned char **out, uint64_t *nbytes,
+                                             void *stream);
+
 /* Same stage with every pointer of `batch` already in device memory; the
  * results stay on the device in library-owned buffers (valid until the next
  * call or ahfgpu_shutdown) and are described by `dres` (device pointers,

@@ -952,3 +952,51 @@ void ahforacle_gather_radii(int64_t nhalo, const uint64_t *npart, const double *
     rad[i] = r;
   }
 }
+
+
+/* ---------------------------------------------------------------------------
+ * AHF_particles, WriteParticlesLegacy (src/libahf/ahf_io.c:1095-1175), default
+ * build (no GAS_PARTICLES, SUSSING2013 or AHFnewHaloIDs): the header holds
+ * the good-halo count (written as 0, rewritten with "%15lu" after the rewind
+ * :1167-1170, so the first line is that count and the original newline).   */
+#include <inttypes.h>
+#include <stdio.h>
+
+int ahforacle_write_particles(const uint64_t *ids, const float *w, int64_t nhalo, const uint64_t *member_off,
+                              const uint64_t *member, const uint64_t *halo_npart, const int64_t *order,
+                              int64_t minpart, unsigned char **out, uint64_t *nbytes)
+{
+  uint64_t cap = 1 << 20, used = 0;
+  char *buf = (char *)malloc(cap);
+  if (!buf) return -1;
+  unsigned long good = 0;
+  for (int64_t j = 0; j < nhalo; j++)
+    if ((int64_t)halo_npart[order[j]] >= minpart) good++;
+  char line[96];
+#define PUT(...)                                                             \
+  do {                                                                       \
+    int n_ = snprintf(line, sizeof line, __VA_ARGS__);                       \
+    if (used + (uint64_t)n_ > cap) {                                         \
+      while (used + (uint64_t)n_ > cap) cap *= 2;                            \
+      char *t_ = (char *)realloc(buf, cap);                                  \
+      if (!t_) { free(buf); return -1; }                                     \
+      buf = t_;                                                              \
+    }                                                                        \
+    memcpy(buf + used, line, (size_t)n_);                                    \
+    used += (uint64_t)n_;                                                    \
+  } while (0)
+  PUT("%15lu\n", good);
+  for (int64_t j = 0; j < nhalo; j++) {
+    const int64_t i = order[j];
+    if (!((int64_t)halo_npart[i] >= minpart)) continue;
+    PUT("%lu %10ld\n", (unsigned long)halo_npart[i], (long)j);
+    for (uint64_t k = member_off[i]; k < member_off[i] + halo_npart[i]; k++) {
+      const uint64_t e = member[k];
+      PUT("%" PRIu64 "\t%d\n", ids[e], w ? (int)w[e] : (int)(-(-1.0)));
+    }
+  }
+#undef PUT
+  *out = (unsigned char *)buf;
+  *nbytes = used;
+  return 0;
+}

@@ -37,6 +37,15 @@ int  ahforacle_gather(uint64_t n, const float *x, const float *y, const float *z
                       uint64_t *out_off, uint64_t **out_idx);
 void ahforacle_gather_free(uint64_t *idx);
 
+/* The AHF_particles file (WriteParticlesLegacy, src/libahf/ahf_io.c:1095-1175,
+ * default build): "%15lu\n" with the number of haloes of at least minpart
+ * particles, then per such halo in `order`: "%lu %10ld\n" (npart, its
+ * position j in `order`) and per kept particle "%" PRIu64 "\t%d\n" (id,
+ * (int)weight with weights, else (int)(-PDM) = 1).  *out malloc()ed.      */
+int  ahforacle_write_particles(const uint64_t *ids, const float *w, int64_t nhalo, const uint64_t *member_off,
+                               const uint64_t *member, const uint64_t *halo_npart, const int64_t *order,
+                               int64_t minpart, unsigned char **out, uint64_t *nbytes);
+
 /* The gather radii, the loop of spatialRef2halos (src/libahf/ahf_halos.c:
  * 2987-3051): half the distance to the closest halo with strictly more
  * particles (or max_rad without one), raised to rvir, capped at max_rad =

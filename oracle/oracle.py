@@ -141,3 +141,54 @@ def gather_radii_oracle(npart, cx, cy, cz, rvir, max_gather_rad_box: float):
     out = np.zeros(len(a[0]))
     fn(len(a[0]), *[v.ctypes.data for v in a], float(max_gather_rad_box), out.ctypes.data)
     return out
+
+
+def _writer(path: str, prefix: str, ids, w, member_off, member, halo_npart, order, minpart: int, ref: bool):
+    import tempfile
+    import numpy as np
+    lib = C.CDLL(path)
+    fr = getattr(lib, f"{prefix}_write_free" if ref else "ahforacle_gather_free")
+    a = dict(ids=np.ascontiguousarray(ids, dtype=np.uint64), off=np.ascontiguousarray(member_off, dtype=np.uint64),
+             mem=np.ascontiguousarray(member, dtype=np.uint64), np_=np.ascontiguousarray(halo_npart, dtype=np.uint64),
+             order=np.ascontiguousarray(order, dtype=np.int64))
+    wa = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+    out = C.POINTER(C.c_ubyte)()
+    nb = C.c_uint64()
+    nh = len(a["np_"])
+    if ref:
+        fn = getattr(lib, f"{prefix}_write_particles")
+        fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                       C.c_int64, C.c_char_p, C.POINTER(C.POINTER(C.c_ubyte)), C.POINTER(C.c_uint64)]
+        fn.restype = C.c_int
+        with tempfile.TemporaryDirectory() as d:
+            rc = fn(len(a["ids"]), a["ids"].ctypes.data, wa.ctypes.data if wa is not None else None, nh,
+                    a["off"].ctypes.data, a["mem"].ctypes.data, a["np_"].ctypes.data, a["order"].ctypes.data,
+                    int(minpart), os.path.join(d, "ref").encode(), C.byref(out), C.byref(nb))
+    else:
+        fn = lib.ahforacle_write_particles
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                       C.POINTER(C.POINTER(C.c_ubyte)), C.POINTER(C.c_uint64)]
+        fn.restype = C.c_int
+        rc = fn(a["ids"].ctypes.data, wa.ctypes.data if wa is not None else None, nh, a["off"].ctypes.data,
+                a["mem"].ctypes.data, a["np_"].ctypes.data, a["order"].ctypes.data, int(minpart), C.byref(out),
+                C.byref(nb))
+    if rc != 0:
+        raise RuntimeError(f"writer failed ({rc})")
+    data = bytes(np.ctypeslib.as_array(out, shape=(max(nb.value, 1),))[:nb.value])
+    if ref:
+        fr.argtypes = [C.c_void_p]
+        fr(C.cast(out, C.c_void_p))
+    else:
+        C.CDLL(None).free.argtypes = [C.c_void_p]
+        C.CDLL(None).free(C.cast(out, C.c_void_p))
+    return data
+
+
+def write_particles_oracle(ids, w, member_off, member, halo_npart, order, minpart: int) -> bytes:
+    """The restated AHF_particles bytes."""
+    return _writer(oracle_path(), "ahforacle", ids, w, member_off, member, halo_npart, order, minpart, False)
+
+
+def write_particles_reference(ids, w, member_off, member, halo_npart, order, minpart: int) -> bytes:
+    """The reference's own writer (ahf_io_WriteParticles), file read back."""
+    return _writer(ref_path(w is not None), "ahfref", ids, w, member_off, member, halo_npart, order, minpart, True)

@@ -15,7 +15,8 @@ every particle unbound, the innermost particle unbound, a halo that falls
 below MINPART during unbinding, list sizes around warp/block boundaries).
 The gather fixtures (gather_*.npz) hold the reference's own particle gather
 (ahf_halos_sfc_gatherParts with its Hilbert-key setup) on a cfg1 snapshot and
-on hand-built periodic-boundary and radius edge cases.
+on hand-built periodic-boundary and radius edge cases; writer_cfg1.npz the
+reference's AHF_particles bytes for the cfg1 haloes.
 """
 from __future__ import annotations
 
@@ -202,6 +203,25 @@ def make_gather() -> None:
         print(name, S.n, S.nhalo, "gathered", int(off[-1]), os.path.getsize(os.path.join(HERE, name + ".npz")))
 
 
+def make_writer() -> None:
+    """The reference's own AHF_particles writer (ahf_io_WriteParticles) on the
+    reference stage's kept lists of the cfg1 slice: inputs and the file's
+    bytes."""
+    import oracle as O
+    O.build()
+    L = synth.generate("cfg1")
+    p = synth.params_for(L)
+    res = O.run_reference(p, L)
+    ids = (np.arange(L.n, dtype=np.uint64) * np.uint64(7919)) + np.uint64(10**12)
+    order = np.argsort(-res.halo["npart"].astype(np.int64), kind="stable").astype(np.int64)
+    data = O.write_particles_reference(ids, None, res.member_off, res.member, res.halo["npart"], order, 20)
+    np.savez_compressed(os.path.join(HERE, "writer_cfg1.npz"), ids=ids, member_off=res.member_off,
+                        member=res.member, npart=res.halo["npart"], order=order, minpart=20,
+                        data=np.frombuffer(data, np.uint8))
+    print("writer_cfg1", len(data), os.path.getsize(os.path.join(HERE, "writer_cfg1.npz")))
+
+
 if __name__ == "__main__":
     main()
     make_gather()
+    make_writer()
