@@ -28,6 +28,8 @@ int fp32c_max_blocks_per_sm(int cls);
 uint64_t fp32c_class_max(int cls);
 void fp32c_set_class_max(uint64_t a, uint64_t b);
 void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
+void launch_fp32c_finish(const DevParams& P, const DevBatch& B, ahfgpu_halo* halo, const uint64_t* prof_cap_off,
+                         double* prof_stage, const double* fin, int64_t nh, int grid, cudaStream_t st);
 // the particle gather (gather.cu)
 void gather_cells(uint64_t n, const float* x, const float* y, const float* z, int G, uint32_t* cell,
                   uint32_t* count, int grid, cudaStream_t st);
@@ -142,7 +144,7 @@ struct Ctx {
   // work space
   DBuf keyA, keyB, idxA, idxB, sdx, sdy, sdz, sd, svx, svy, svz, sw, seid, phi, flag, nflag;
   DBuf fdh, fdl, fdx, fdy, fdz, fdxl, fdyl, fdzl, fqh, fql, rec;
-  DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred;
+  DBuf pa, pb, pc, pd, stack, halo, mem_stage, prof_stage, prof_cap_off, queue, qhead, counters, err, wred, fin;
   // packed results (device)
   DBuf member_off, member, prof_off, prof, phase;
   // the particle gather: grid buckets, per-halo counts and lists, the
@@ -399,6 +401,7 @@ int ensure_work(const Plan& pl, int nblocks, int stack_cap) {
   EN(g.mem_stage, N * 8);
   EN(g.prof_stage, std::max<uint64_t>(pl.nbins_total, 1) * AHFGPU_PROF_NFIELDS * 8);
   EN(g.prof_cap_off, (pl.nhalo + 1) * 8);
+  EN(g.fin, std::max<int64_t>(pl.nhalo, 1) * kFinStride * 8);
   EN(g.queue, std::max<int64_t>(pl.nhalo, 1) * 4);
   EN(g.qhead, kQueueHeads * 4);
   EN(g.counters, 64);
@@ -543,6 +546,7 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   W.halo = g.halo.as<ahfgpu_halo>();
   W.mem_stage = g.mem_stage.as<uint64_t>();
   W.prof_stage = g.prof_stage.as<double>();
+  W.fin = g.fin.as<double>();
   W.prof_cap_off = g.prof_cap_off.as<uint64_t>();
   W.queue_head = g.qhead.as<unsigned int>();
   W.queue = g.queue.as<int32_t>();
@@ -600,6 +604,11 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
         CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
         launches++;
       }
+    }
+    if (mode == AHFGPU_BATCHED_FP32C) {
+      launch_fp32c_finish(P, B, W.halo, W.prof_cap_off, W.prof_stage, W.fin, nh,
+                          std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
+      launches++;
     }
     launch_concentration(W.halo, nh, std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 127) / 128))), st);
     launches++;
@@ -862,7 +871,7 @@ int ahfgpu_shutdown(void) {
                   &g.in_cx, &g.in_cy, &g.in_cz, &g.keyA, &g.keyB, &g.idxA, &g.idxB, &g.sdx, &g.sdy, &g.sdz,
                   &g.sd, &g.svx, &g.svy, &g.svz, &g.sw, &g.seid, &g.phi, &g.flag, &g.nflag, &g.pa, &g.pb,
                   &g.pc, &g.pd, &g.fdh, &g.fdl, &g.fdx, &g.fdy, &g.fdz, &g.fdxl, &g.fdyl, &g.fdzl, &g.fqh, &g.fql, &g.rec, &g.stack, &g.halo, &g.mem_stage, &g.prof_stage, &g.prof_cap_off, &g.queue,
-                  &g.qhead, &g.counters, &g.err, &g.wred, &g.member_off, &g.member, &g.prof_off, &g.prof,
+                  &g.qhead, &g.counters, &g.err, &g.wred, &g.fin, &g.member_off, &g.member, &g.prof_off, &g.prof,
                   &g.ga_cell, &g.ga_count, &g.ga_start, &g.ga_fill, &g.ga_sums, &g.ga_sorted, &g.ga_queue,
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,

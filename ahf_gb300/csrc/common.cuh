@@ -20,6 +20,9 @@ constexpr int kMaxBins = 64;         // nbins = 6.2 log10(n) - 3.5 < 64 for n < 
 constexpr int kMaxFixRounds = 4096;  // cap of the bulk-velocity fixpoint
 
 // device-side error codes (written to Work::err, read by the host)
+// doubles per halo of the FP32C post-pass inputs (Work::fin)
+constexpr int kFinStride = 16;
+
 enum : int { kErrNone = 0, kErrFixpoint = 1, kErrSortDepth = 2, kErrWorklist = 3, kErrSortState = 4 };
 
 struct DevParams {
@@ -69,6 +72,7 @@ struct Work {
   ahfgpu_halo* halo;      // [nhalo]
   uint64_t* mem_stage;    // [N] kept ids (gidx[e], or e where gidx is NULL), at the halo's input offset
   double* prof_stage;     // [nbins_cap_total * NFIELDS]
+  double* fin;            // FP32C: [nhalo * kFinStride] inputs of the integral properties (post-pass)
   const uint64_t* prof_cap_off;  // [nhalo+1] staging row offsets
   // work queue / diagnostics
   unsigned int* queue_head;

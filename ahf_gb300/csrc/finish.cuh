@@ -153,58 +153,82 @@ static __device__ double calc_cR1(double R1) {
 }
 
 
-// Profile rows of HaloProfiles' per-bin block (ahf_halos.c:4632-4868) from
-// the cumulative bin records; one thread per bin.
+// One profile row of HaloProfiles' per-bin block (ahf_halos.c:4632-4868)
+// from bin b's cumulative record R, its outer edge, and the previous bin's
+// mass and edge (has_prev false for the first bin).
 // f32eig: FP32 eigen-solver (FP32-compensated form)
+static __device__ __forceinline__ void bin_row(const Bin& R, double cur_rad, bool has_prev, double Mprev_in,
+                                               double edge_prev, double* row, bool f32eig) {
+  const double FPT = 4. * kPi / 3.;
+  double Volume = FPT * (cur_rad * cur_rad * cur_rad);
+  double Mprev = has_prev ? Mprev_in : 0.0;
+  double Vprev = has_prev ? FPT * (edge_prev * edge_prev * edge_prev) : 0.0;
+  double dM = R.M - Mprev;
+  double dV = Volume - Vprev;
+  double it[3][3], ax1, ax2, ax3;
+  if (R.npart > 10) {
+    it[0][0] = R.a11; it[1][1] = R.a22; it[2][2] = R.a33;
+    it[0][1] = R.a12; it[1][0] = R.a12;
+    it[0][2] = R.a13; it[2][0] = R.a13;
+    it[1][2] = R.a23; it[2][1] = R.a23;
+    get_axes(it, &ax1, &ax2, &ax3, f32eig);
+  } else {
+    for (int x = 0; x < 3; x++)
+      for (int y = 0; y < 3; y++) it[x][y] = 0.0;
+    ax1 = 1; ax2 = 0; ax3 = 0;
+  }
+  row[AHFGPU_PROF_R] = cur_rad;
+  row[AHFGPU_PROF_NPART] = R.npart;
+  row[AHFGPU_PROF_NVPART] = R.M;
+  row[AHFGPU_PROF_OVDENS] = R.M / Volume;
+  row[AHFGPU_PROF_DENS] = dV > 0 ? dM / dV : 0.0;
+  row[AHFGPU_PROF_V2_CIRC] = R.M / cur_rad;
+  row[AHFGPU_PROF_V_ESC2] = R.vesc2;
+  row[AHFGPU_PROF_SIG_V] = sqrt(R.T / R.M);
+  row[AHFGPU_PROF_EKIN] = 0.5 * R.T;
+  row[AHFGPU_PROF_EPOT] = 0.5 * R.U;
+  row[AHFGPU_PROF_LX] = R.Lx;
+  row[AHFGPU_PROF_LY] = R.Ly;
+  row[AHFGPU_PROF_LZ] = R.Lz;
+  row[AHFGPU_PROF_E1X] = it[0][0]; row[AHFGPU_PROF_E1Y] = it[1][0]; row[AHFGPU_PROF_E1Z] = it[2][0];
+  row[AHFGPU_PROF_E2X] = it[0][1]; row[AHFGPU_PROF_E2Y] = it[1][1]; row[AHFGPU_PROF_E2Z] = it[2][1];
+  row[AHFGPU_PROF_E3X] = it[0][2]; row[AHFGPU_PROF_E3Y] = it[1][2]; row[AHFGPU_PROF_E3Z] = it[2][2];
+  row[AHFGPU_PROF_AXIS1] = 1.0;
+  if (ax1 > 0.) {
+    row[AHFGPU_PROF_AXIS2] = sqrt(ax2 / ax1);
+    row[AHFGPU_PROF_AXIS3] = sqrt(ax3 / ax1);
+  } else {
+    row[AHFGPU_PROF_AXIS2] = 0.0;
+    row[AHFGPU_PROF_AXIS3] = 0.0;
+  }
+}
+
+// FP32C hands the bin records and the integral properties' inputs to a
+// post-pass over all haloes (fp32c_finish_kernel): each bin's record and
+// outer edge wait in the bin's own profile row (the row is then computed in
+// place), the per-halo inputs in W.fin.
+enum : int { kFinM = 0, kFinVX, kFinVY, kFinVZ, kFinCX, kFinCY, kFinCZ, kFinMhi, kFinMlo, kFinMbe, kFinR2, kFinRmax,
+             kFinVmax };
+
+__device__ __forceinline__ void stash_bin(double* row, const Bin& R, double edge) {
+  row[0] = R.npart; row[1] = R.M; row[2] = R.Lx; row[3] = R.Ly; row[4] = R.Lz; row[5] = R.T; row[6] = R.U;
+  row[7] = R.a11; row[8] = R.a22; row[9] = R.a33; row[10] = R.a12; row[11] = R.a13; row[12] = R.a23;
+  row[13] = R.vesc2; row[14] = edge;
+}
+
+__device__ __forceinline__ void load_bin(const double* row, Bin& R, double& edge) {
+  R.npart = row[0]; R.M = row[1]; R.Lx = row[2]; R.Ly = row[3]; R.Lz = row[4]; R.T = row[5]; R.U = row[6];
+  R.a11 = row[7]; R.a22 = row[8]; R.a33 = row[9]; R.a12 = row[10]; R.a13 = row[11]; R.a23 = row[12];
+  R.vesc2 = row[13]; edge = row[14];
+}
+
+// Profile rows of HaloProfiles' per-bin block from the cumulative bin
+// records; one thread per bin.
 static __device__ void write_bin_rows(const Bin* bins, const double* edge, int nbins, double* rows,
                                       bool f32eig = false) {
-  const double FPT = 4. * kPi / 3.;
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) {
-    const Bin& R = bins[b];
-    double cur_rad = edge[b];
-    double Volume = FPT * (cur_rad * cur_rad * cur_rad);
-    double Mprev = b > 0 ? bins[b - 1].M : 0.0;
-    double Vprev = b > 0 ? FPT * (edge[b - 1] * edge[b - 1] * edge[b - 1]) : 0.0;
-    double dM = R.M - Mprev;
-    double dV = Volume - Vprev;
-    double it[3][3], ax1, ax2, ax3;
-    if (R.npart > 10) {
-      it[0][0] = R.a11; it[1][1] = R.a22; it[2][2] = R.a33;
-      it[0][1] = R.a12; it[1][0] = R.a12;
-      it[0][2] = R.a13; it[2][0] = R.a13;
-      it[1][2] = R.a23; it[2][1] = R.a23;
-      get_axes(it, &ax1, &ax2, &ax3, f32eig);
-    } else {
-      for (int x = 0; x < 3; x++)
-        for (int y = 0; y < 3; y++) it[x][y] = 0.0;
-      ax1 = 1; ax2 = 0; ax3 = 0;
-    }
-    double* row = rows + (uint64_t)b * AHFGPU_PROF_NFIELDS;
-    row[AHFGPU_PROF_R] = cur_rad;
-    row[AHFGPU_PROF_NPART] = R.npart;
-    row[AHFGPU_PROF_NVPART] = R.M;
-    row[AHFGPU_PROF_OVDENS] = R.M / Volume;
-    row[AHFGPU_PROF_DENS] = dV > 0 ? dM / dV : 0.0;
-    row[AHFGPU_PROF_V2_CIRC] = R.M / cur_rad;
-    row[AHFGPU_PROF_V_ESC2] = R.vesc2;
-    row[AHFGPU_PROF_SIG_V] = sqrt(R.T / R.M);
-    row[AHFGPU_PROF_EKIN] = 0.5 * R.T;
-    row[AHFGPU_PROF_EPOT] = 0.5 * R.U;
-    row[AHFGPU_PROF_LX] = R.Lx;
-    row[AHFGPU_PROF_LY] = R.Ly;
-    row[AHFGPU_PROF_LZ] = R.Lz;
-    row[AHFGPU_PROF_E1X] = it[0][0]; row[AHFGPU_PROF_E1Y] = it[1][0]; row[AHFGPU_PROF_E1Z] = it[2][0];
-    row[AHFGPU_PROF_E2X] = it[0][1]; row[AHFGPU_PROF_E2Y] = it[1][1]; row[AHFGPU_PROF_E2Z] = it[2][1];
-    row[AHFGPU_PROF_E3X] = it[0][2]; row[AHFGPU_PROF_E3Y] = it[1][2]; row[AHFGPU_PROF_E3Z] = it[2][2];
-    row[AHFGPU_PROF_AXIS1] = 1.0;
-    if (ax1 > 0.) {
-      row[AHFGPU_PROF_AXIS2] = sqrt(ax2 / ax1);
-      row[AHFGPU_PROF_AXIS3] = sqrt(ax3 / ax1);
-    } else {
-      row[AHFGPU_PROF_AXIS2] = 0.0;
-      row[AHFGPU_PROF_AXIS3] = 0.0;
-    }
-  }
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    bin_row(bins[b], edge[b], b > 0, b > 0 ? bins[b - 1].M : 0.0, b > 0 ? edge[b - 1] : 0.0,
+            rows + (uint64_t)b * AHFGPU_PROF_NFIELDS, f32eig);
 }
 
 // Integral properties at the end of HaloProfiles (ahf_halos.c:4870-5018),

@@ -2557,7 +2557,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
   }
   double* rows = W.prof_stage + W.prof_cap_off[c.h] * AHFGPU_PROF_NFIELDS;
   PT_T(W, 23);
-  write_bin_rows(S.bins, S.edge, nbins, rows, true);
+  // the bin records (rows and integral properties: fp32c_finish_kernel)
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    stash_bin(rows + (uint64_t)b * AHFGPU_PROF_NFIELDS, S.bins[b], S.edge[b]);
   __syncthreads();
   PT_T(W, 24);
   uint64_t i_r2 = find_max32(c, B, W, S, 0, 3, n2, nret);
@@ -2586,9 +2588,13 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     double V_max = M_max / R_max;
     long long mbe = Eslot >= 0 ? (long long)(c.o + W.seid[o + Eslot]) : -1;
     double Mt = (double)cM * F.dm;
-    finish_scalars(rows, nbins, Mt, (double)cX * F.dv, (double)cY * F.dv, (double)cZ * F.dv, Mt * c.cx + ff_d(cf[1]),
-                   Mt * c.cy + ff_d(cf[2]), Mt * c.cz + ff_d(cf[3]), ff_d(cgc[9]), ff_d(cgc[10]), mbe, r2, R_max,
-                   V_max, P, B, c.cx, c.cy, c.cz, hout);
+    double* fin = W.fin + (uint64_t)c.h * kFinStride;
+    fin[kFinM] = Mt;
+    fin[kFinVX] = (double)cX * F.dv; fin[kFinVY] = (double)cY * F.dv; fin[kFinVZ] = (double)cZ * F.dv;
+    fin[kFinCX] = Mt * c.cx + ff_d(cf[1]); fin[kFinCY] = Mt * c.cy + ff_d(cf[2]); fin[kFinCZ] = Mt * c.cz + ff_d(cf[3]);
+    fin[kFinMhi] = ff_d(cgc[9]); fin[kFinMlo] = ff_d(cgc[10]);
+    fin[kFinMbe] = __longlong_as_double(mbe);
+    fin[kFinR2] = r2; fin[kFinRmax] = R_max; fin[kFinVmax] = V_max;
     hout.nbins = nbins;
     hout.flags |= AHFGPU_HALO_RAN_PROFILE;
   }
@@ -2828,3 +2834,4 @@ __global__ void __launch_bounds__(T, MinB) halo_fp32c_kernel(DevParams P, DevBat
 }
 
 }  // namespace ahfgpu
+
