@@ -2100,8 +2100,20 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
 // T stays accurate where Ekin + Epot cancels (lambdaE).
 struct PTerms {
   ff T, cx, cy, cz;        // kinetic term, w dX, w dY, w dZ
-  float g[11];             // Lx, Ly, Lz, a11, a22, a33, a12, a13, a23, Mhi, Mlo
+  ff L[3];                 // w (dX x dV): Lx, Ly, Lz
+  float g[11];             // 3..10: a11, a22, a33, a12, a13, a23, Mhi, Mlo (0..2 unused)
 };
+
+// (a + al) gb - (b + bl) ga in float-float.  The angular-momentum terms of
+// a slowly rotating halo cancel to |L| ~ 1e-4 of sum |w dX x dV|, so FP32
+// products would leave L (and lambda) a relative error ~1e-3 / sqrt(N).
+__device__ __forceinline__ ff cross_term(float a, float al, ff gb, float b, float bl, ff ga) {
+  ff p = two_prod(a, gb.hi);
+  p = ff_quick(p.hi, __fmaf_rn(a, gb.lo, __fmaf_rn(al, gb.hi, p.lo)));
+  ff q = two_prod(b, ga.hi);
+  q = ff_quick(q.hi, __fmaf_rn(b, ga.lo, __fmaf_rn(bl, ga.hi, q.lo)));
+  return ff_sub(p, q);
+}
 
 __device__ __forceinline__ ff rel_vel(float v, ff V, ff M, float rM) {
   float b = __fmul_rn(V.hi, rM);
@@ -2115,10 +2127,9 @@ __device__ __forceinline__ void pterms(float w, float vx, float vy, float vz, fl
                                        int has_w, PTerms& t) {
   const float rM = __frcp_rn(M.hi);
   ff gx = rel_vel(vx, VX, M, rM), gy = rel_vel(vy, VY, M, rM), gz = rel_vel(vz, VZ, M, rM);
-  float gxf = ff_f(gx), gyf = ff_f(gy), gzf = ff_f(gz);
-  t.g[0] = __fmul_rn(w, __fsub_rn(__fmul_rn(dy, gzf), __fmul_rn(dz, gyf)));
-  t.g[1] = __fmul_rn(w, __fsub_rn(__fmul_rn(dz, gxf), __fmul_rn(dx, gzf)));
-  t.g[2] = __fmul_rn(w, __fsub_rn(__fmul_rn(dx, gyf), __fmul_rn(dy, gxf)));
+  t.L[0] = ff_mulf(cross_term(dy, dyl, gz, dz, dzl, gy), w);
+  t.L[1] = ff_mulf(cross_term(dz, dzl, gx, dx, dxl, gz), w);
+  t.L[2] = ff_mulf(cross_term(dx, dxl, gy, dy, dyl, gx), w);
   gx = ff_add(gx, ff_mulf(two_sum(dx, dxl), Hrv));
   gy = ff_add(gy, ff_mulf(two_sum(dy, dyl), Hrv));
   gz = ff_add(gz, ff_mulf(two_sum(dz, dzl), Hrv));
@@ -2357,9 +2368,10 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     const int rank0 = cr + excnt;
     // per-particle terms, thread totals; bin ends of this tile
     ff tf[4] = {ffz(), ffz(), ffz(), ffz()}, tU = ffz();
-    float tg[11];
+    float tg[11];                 // channels 3..10 (0..2 stay zero: tL)
 #pragma unroll
     for (int j = 0; j < 11; j++) tg[j] = 0.f;
+    ff tL[3] = {ffz(), ffz(), ffz()};   // Lx, Ly, Lz in float-float (lambda cancels them)
     float Ef[kItems];
     ff Mk[kItems];
     bool has_end = false;
@@ -2385,7 +2397,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         tf[2] = ff_add(tf[2], t.cy);
         tf[3] = ff_add(tf[3], t.cz);
 #pragma unroll
-        for (int j = 0; j < 11; j++) tg[j] = __fadd_rn(tg[j], t.g[j]);
+        for (int j = 0; j < 3; j++) tL[j] = ff_add(tL[j], t.L[j]);
+#pragma unroll
+        for (int j = 3; j < 11; j++) tg[j] = __fadd_rn(tg[j], t.g[j]);
         ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
         tU = ff_add(tU, U);
         Ef[k] = __fadd_rn(__fmul_rn(0.5f, Tp), ff_f(U));
@@ -2413,6 +2427,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     const bool tile_end = __syncthreads_or(has_end ? 1 : 0) != 0;
     ff ef5[5], tf5[5], af5[5] = {tf[0], tf[1], tf[2], tf[3], tU};
     float eg[11], tgt[11];
+    ff eL[3], tLt[3];
     if (tile_end) {
       // everything before this tile into the carries, then this tile's scans
       if (pend) {
@@ -2428,12 +2443,15 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         pend = false;
       }
       bscan_ff<5>(af5, ef5, tf5, S.scan);
+      bscan_ff<3>(tL, eL, tLt, S.scan);
       bscan_f<11>(tg, eg, tgt, S.scan);
     } else {
 #pragma unroll
       for (int j = 0; j < 5; j++) { pacc[j] = ff_add(pacc[j], af5[j]); tf5[j] = ffz(); ef5[j] = ffz(); }
 #pragma unroll
-      for (int j = 0; j < 11; j++) { pacc[5 + j] = ff_add(pacc[5 + j], fff(tg[j])); tgt[j] = 0.f; eg[j] = 0.f; }
+      for (int j = 0; j < 3; j++) { pacc[5 + j] = ff_add(pacc[5 + j], tL[j]); tLt[j] = ffz(); eL[j] = ffz(); }
+#pragma unroll
+      for (int j = 3; j < 11; j++) { pacc[5 + j] = ff_add(pacc[5 + j], fff(tg[j])); tgt[j] = 0.f; eg[j] = 0.f; }
       pend = true;
     }
     PT_T(W, 20);
@@ -2468,6 +2486,7 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
       int r = rank0;
       ff runf[5];
       float rung[11];
+      ff runL[3] = {eL[0], eL[1], eL[2]};
 #pragma unroll
       for (int j = 0; j < 5; j++) runf[j] = ff_add(j < 4 ? cf[j] : cU, ef5[j]);
 #pragma unroll
@@ -2483,7 +2502,8 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
         pterms_ool(w[k], vx[k], vy[k], vz[k], dx[k], dy[k], dz[k], dxl[k], dyl[k], dzl[k], M, i2ff(rX, F.iv),
                    i2ff(rY, F.iv), i2ff(rZ, F.iv), Hrv, has_w, t);
         runf[0] = ff_add(runf[0], t.T);
-        for (int j = 0; j < 11; j++) rung[j] = __fadd_rn(rung[j], t.g[j]);
+        for (int j = 0; j < 3; j++) runL[j] = ff_add(runL[j], t.L[j]);
+        for (int j = 3; j < 11; j++) rung[j] = __fadd_rn(rung[j], t.g[j]);
         ff U = ff_mulf(ff_sub(phi[k], Phi0), w[k]);
         runU = ff_add(runU, U);
         int bnext = edges_le(S, nbins, d[k], bcur);
@@ -2493,9 +2513,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
           Bin& R = S.bins[bb];
           R.npart = (double)(r + 1);
           R.M = ff_d(M);
-          R.Lx = ff_d(ff_add(cgc[0], fff(rung[0])));
-          R.Ly = ff_d(ff_add(cgc[1], fff(rung[1])));
-          R.Lz = ff_d(ff_add(cgc[2], fff(rung[2])));
+          R.Lx = ff_d(ff_add(cgc[0], runL[0]));
+          R.Ly = ff_d(ff_add(cgc[1], runL[1]));
+          R.Lz = ff_d(ff_add(cgc[2], runL[2]));
           R.T = ff_d(runf[0]);
           R.U = ff_d(runU);
           R.a11 = ff_d(ff_add(cgc[3], fff(rung[3])));
@@ -2516,7 +2536,9 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     for (int j = 0; j < 4; j++) cf[j] = ff_add(cf[j], tf5[j]);
     cU = ff_add(cU, tf5[4]);
 #pragma unroll
-    for (int j = 0; j < 11; j++) { cgc[j] = ff_add(cgc[j], fff(tgt[j])); cg[j] = 0.f; }
+    for (int j = 0; j < 3; j++) cgc[j] = ff_add(cgc[j], tLt[j]);
+#pragma unroll
+    for (int j = 3; j < 11; j++) { cgc[j] = ff_add(cgc[j], fff(tgt[j])); cg[j] = 0.f; }
 #pragma unroll
     for (int j = 0; j < 4; j++) cD[j] = blockLast[j];
     cr += tn;

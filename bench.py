@@ -176,6 +176,39 @@ def alg_bytes(n_in: np.ndarray, res_halo, has_w: bool) -> float:
     return float(per_p * n_in.sum() + 16.0 * nb.sum() + (24.0 + 256.0) * len(n_in) + 8.0 * 25.0 * nbins.sum())
 
 
+def precision_report(r32, r64, retests: int) -> dict:
+    """The FP32-compensated result against the FP64 form on the same batch:
+    haloes whose kept lists differ (must be 0), the largest relative
+    differences of Phi0, M_vir, V_max = sqrt(V2_max) and the spin lambda, and
+    the particles routed to the FP64 re-test."""
+    n = len(r32.halo)
+    diff = 0
+    m32, m64, o32, o64 = r32.member, r64.member, r32.member_off, r64.member_off
+    if not np.array_equal(o32, o64):
+        diff = int(np.count_nonzero(np.diff(o32.astype(np.int64)) != np.diff(o64.astype(np.int64))))
+    elif not np.array_equal(m32, m64):
+        bad = np.nonzero(m32 != m64)[0]
+        diff = int(len(np.unique(np.searchsorted(o32.astype(np.int64), bad, side="right") - 1)))
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+        ok = np.isfinite(a) & np.isfinite(b) & (b != 0)
+        return float(np.max(np.abs(a[ok] - b[ok]) / np.abs(b[ok]))) if ok.any() else 0.0
+    h32, h64 = r32.halo, r64.halo
+    prof = (h64["flags"] & 0x20) != 0   # AHFGPU_HALO_RAN_PROFILE
+    l32, l64 = h32["lambda_"][prof].astype(np.float64), h64["lambda_"][prof].astype(np.float64)
+    le = np.abs(l32 - l64) / np.maximum(np.abs(l64), 1e-300)
+    iw = int(np.argmax(le)) if le.size else 0
+    worst = ({"npart": int(h64["npart"][prof][iw]), "lambda": float(l64[iw]), "rel_err": float(le[iw]),
+              "median_lambda": float(np.median(np.abs(l64))), "haloes_above_1e-6": int(np.sum(le > 1e-6))}
+             if le.size else None)
+    return {"haloes": n, "kept_list_mismatches": diff, "lambda_worst": worst, "max_rel_err": {
+        "Phi0": rel(h32["Phi0"], h64["Phi0"]), "M_vir": rel(h32["M_vir"], h64["M_vir"]),
+        "V_max": rel(np.sqrt(np.abs(h32["V2_max"][prof])), np.sqrt(np.abs(h64["V2_max"][prof]))),
+        "lambda": rel(h32["lambda_"][prof], h64["lambda_"][prof])},
+        "fp64_retests": retests, "against": "the batched FP64 form (bit-exact to the reference) on the same batch"}
+
+
 def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
     """The AHF_particles file of the last result on the GPU (ids = entry
     index, haloes by decreasing kept count), timed like the stage; the
@@ -491,6 +524,7 @@ def ours_arm(args, ws, rank, local):
 
     # other forms, once each (same workload)
     forms = {}
+    precision = None
     if args.forms != "none":
         want = ["batched_fp32c", "batched_fp64", "plain_fp64"] if args.forms == "all" else args.forms.split(",")
         for f in want:
@@ -515,6 +549,8 @@ def ours_arm(args, ws, rank, local):
                 fms = a.elapsed_time(b)
                 forms[f] = {"value": nf / (fms / 1e3), "ms_per_step": fms, "sample": desc,
                             "replay_halos": int(rr.stats.n_replay_halos)}
+                if f == "batched_fp64" and mode == "batched_fp32c":
+                    precision = precision_report(res, lib.fetch_result(), int(stats.n_retest))
             except lib.AhfGpuError as e:
                 forms[f] = {"unavailable": str(e)}
         # leave the last result of the headline form in place for fetch_result()
@@ -599,6 +635,7 @@ def ours_arm(args, ws, rank, local):
         "forms": forms,
         "gather": gather,
         "writer": writer,
+        "precision": precision,
         "diagnostics": headline_stats,
     }
     print(json.dumps(line), flush=True)
