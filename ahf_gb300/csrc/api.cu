@@ -51,6 +51,11 @@ void writer_count(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, con
                   const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
                   uint64_t* blk, unsigned long long* good, int grid, cudaStream_t st);
 void writer_offsets(const uint64_t* blk, int64_t nh, uint64_t* boff, cudaStream_t st);
+void writer_bin_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
+                      uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st);
+void writer_bin_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                      const uint64_t* member, const uint64_t* ids, const uint64_t* boff, const uint64_t* coff,
+                      const unsigned long long* good, unsigned int* qhead, uint32_t* out, int grid, cudaStream_t st);
 void writer_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
                   const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
                   const uint64_t* boff, const unsigned long long* good, unsigned char* out, int grid,
@@ -153,6 +158,7 @@ struct Ctx {
   DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
   DBuf gr_pos, gr_lim, gr_orig;   // gather radii: sorted centres and R_vir, candidate counts, order
   DBuf wp_blk, wp_boff, wp_good, wp_qhead, wp_out;   // the AHF_particles bytes
+  DBuf wb_chunk, wb_coff;                            // AHF_particles_bin: chunks per block, their scan
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -876,7 +882,7 @@ int ahfgpu_shutdown(void) {
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
                   &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
-                  &g.wp_out, &g.phase};
+                  &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1266,6 +1272,48 @@ int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int
   writer_write(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids, w,
                minpart, g.wp_qhead.as<unsigned int>(), g.wp_boff.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
                g.wp_out.as<unsigned char>(), grid, st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
+  *out = g.wp_out.as<unsigned char>();
+  *nbytes = total;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order, int64_t minpart,
+                                      const unsigned char** out, uint64_t* nbytes, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!out || !nbytes) return fail(AHFGPU_ERR_INVALID, "out/nbytes is NULL");
+  if (g.last_nhalo < 0) return fail(AHFGPU_ERR_STATE, "no device result to write");
+  const int64_t nh = g.last_nhalo;
+  if (nh > 0 && (!ids || !order)) return fail(AHFGPU_ERR_INVALID, "ids/order is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  if ((rc = g.wp_blk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
+  if ((rc = g.wp_boff.ensure((nh + 1) * 8))) return rc;
+  if ((rc = g.wb_chunk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
+  if ((rc = g.wb_coff.ensure((nh + 1) * 8))) return rc;
+  if ((rc = g.wp_good.ensure(64))) return rc;
+  if ((rc = g.wp_qhead.ensure(64))) return rc;
+  CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
+  CK(cudaMemsetAsync(g.wp_good.p, 0, 64, st));
+  if (nh > 0)
+    writer_bin_sizes(nh, order, g.halo.as<ahfgpu_halo>(), minpart, g.wp_blk.as<uint64_t>(), g.wb_chunk.as<uint64_t>(),
+                     g.wp_good.as<unsigned long long>(), std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 255) / 256))),
+                     st);
+  writer_offsets(g.wp_blk.as<uint64_t>(), nh, g.wp_boff.as<uint64_t>(), st);
+  writer_offsets(g.wb_chunk.as<uint64_t>(), nh, g.wb_coff.as<uint64_t>(), st);
+  CK(cudaGetLastError());
+  uint64_t tail[2] = {0, 0};
+  CK(cudaMemcpyAsync(&tail[0], g.wp_boff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&tail[1], g.wb_coff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (tail[1] >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "binary writer: %llu chunks", (unsigned long long)tail[1]);
+  const uint64_t total = 16 + tail[0];
+  if ((rc = g.wp_out.ensure(total))) return rc;
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, tail[1]));
+  writer_bin_write(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids,
+                   g.wp_boff.as<uint64_t>(), g.wb_coff.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
+                   g.wp_qhead.as<unsigned int>(), g.wp_out.as<uint32_t>(), grid, st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   *out = g.wp_out.as<unsigned char>();

@@ -194,6 +194,132 @@ __global__ void __launch_bounds__(256) k_wp_write(int64_t nh, const int64_t* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// AHF_particles_bin: ahf_binwrite_particles (src/libahf/ahf_io.c:1733-1855,
+// AHFbinary build without GAS_PARTICLES or AHFnewHaloIDs).  Bytes: int32 1,
+// uint64 haloes written, uint32 2 (columns); per halo j of the output order
+// with at least MINPART particles, uint64 npart and uint64 j, then per kept
+// particle uint64 id and int32 1 (the type is (int32)(-u) only with
+// GAS_PARTICLES).  Native byte order, no padding: a halo block is 16 + 12 n
+// bytes, so every block and every field starts on a 4-byte boundary and the
+// file is written as 32-bit words.  Block sizes need no particle pass; the
+// work is cut into chunks of kWbChunk particles so the largest lists spread
+// over many CTAs.
+constexpr int kWbChunk = 4096;
+constexpr int kWbUnroll = 4;
+
+__global__ void __launch_bounds__(256) k_wb_sizes(int64_t nh, const int64_t* __restrict__ order,
+                                                  const ahfgpu_halo* __restrict__ halo, int64_t minpart,
+                                                  uint64_t* __restrict__ blk, uint64_t* __restrict__ nchunk,
+                                                  unsigned long long* __restrict__ good) {
+  unsigned long long mine = 0;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < nh; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t np = halo[order[j]].npart;
+    const bool ok = (int64_t)np >= minpart;
+    blk[j] = ok ? 16 + 12 * np : 0;
+    nchunk[j] = ok ? (np > 0 ? (np + kWbChunk - 1) / kWbChunk : 1) : 0;   // chunk 0 writes the block header
+    mine += ok;
+  }
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(good, mine);
+}
+
+// one 32-particle group of a warp: 96 words, lane l stores words l, l+32,
+// l+64 (word w is field w % 3 of particle w / 3: id low, id high, type 1)
+__device__ __forceinline__ void wb_group(uint32_t* __restrict__ rec, uint64_t id, int cnt, int lane) {
+  const uint32_t lo = (uint32_t)id, hi = (uint32_t)(id >> 32);
+#pragma unroll
+  for (int r = 0; r < 3; r++) {
+    const int w = lane + 32 * r;
+    const int src = w / 3, f = w - 3 * src;
+    const uint32_t a = __shfl_sync(0xffffffffu, lo, src), b = __shfl_sync(0xffffffffu, hi, src);
+    if (src < cnt) rec[w] = f == 0 ? a : (f == 1 ? b : 1u);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_wb_write(int64_t nh, const int64_t* __restrict__ order,
+                                                  const ahfgpu_halo* __restrict__ halo,
+                                                  const uint64_t* __restrict__ moff, const uint64_t* __restrict__ member,
+                                                  const uint64_t* __restrict__ ids, const uint64_t* __restrict__ boff,
+                                                  const uint64_t* __restrict__ coff,
+                                                  const unsigned long long* __restrict__ good,
+                                                  unsigned int* __restrict__ qhead, uint32_t* __restrict__ out) {
+  __shared__ long long s_j;
+  __shared__ unsigned long long s_c;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long gc = *good;
+    out[0] = 1u;
+    out[1] = (uint32_t)gc;
+    out[2] = (uint32_t)(gc >> 32);
+    out[3] = 2u;
+  }
+  const uint64_t nchunks = coff[nh];
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned q = atomicAdd(qhead, 1u);
+      if ((uint64_t)q >= nchunks) {
+        s_j = -1;
+      } else {
+        int64_t lo = 0, hi = nh;   // coff[lo] <= q < coff[hi]
+        while (hi - lo > 1) {
+          const int64_t mid = (lo + hi) >> 1;
+          if (coff[mid] <= q) lo = mid; else hi = mid;
+        }
+        s_j = lo;
+        s_c = q - coff[lo];
+      }
+    }
+    __syncthreads();
+    const long long j = s_j;
+    const uint64_t c = s_c;
+    __syncthreads();
+    if (j < 0) break;
+    const int64_t i = order[j];
+    const uint64_t np = halo[i].npart;
+    uint32_t* blkw = out + (16 + boff[j]) / 4;
+    if (c == 0 && threadIdx.x < 4) {
+      const uint64_t v = threadIdx.x < 2 ? np : (uint64_t)j;
+      blkw[threadIdx.x] = (threadIdx.x & 1) ? (uint32_t)(v >> 32) : (uint32_t)v;
+    }
+    const uint64_t k0 = c * kWbChunk, k1 = np < k0 + kWbChunk ? np : k0 + kWbChunk;
+    const uint64_t* mem = member + moff[i];
+    uint32_t* rec = blkw + 4;
+    for (uint64_t base = k0 + (uint64_t)wid * 32 * kWbUnroll; base < k1; base += (uint64_t)blockDim.x * kWbUnroll) {
+      uint64_t e[kWbUnroll], id[kWbUnroll];
+#pragma unroll
+      for (int u = 0; u < kWbUnroll; u++) {
+        const uint64_t k = base + 32 * u + lane;
+        e[u] = k < k1 ? mem[k] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kWbUnroll; u++) {
+        const uint64_t k = base + 32 * u + lane;
+        id[u] = k < k1 ? ids[e[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kWbUnroll; u++) {
+        const uint64_t g0 = base + 32 * u;
+        if (g0 < k1) {
+          const int cnt = k1 - g0 < 32 ? (int)(k1 - g0) : 32;
+          wb_group(rec + 3 * g0, id[u], cnt, lane);
+        }
+      }
+    }
+  }
+}
+
+void writer_bin_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
+                      uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st) {
+  k_wb_sizes<<<grid, 256, 0, st>>>(nh, order, halo, minpart, blk, nchunk, good);
+}
+
+void writer_bin_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                      const uint64_t* member, const uint64_t* ids, const uint64_t* boff, const uint64_t* coff,
+                      const unsigned long long* good, unsigned int* qhead, uint32_t* out, int grid, cudaStream_t st) {
+  k_wb_write<<<grid, 256, 0, st>>>(nh, order, halo, moff, member, ids, boff, coff, good, qhead, out);
+}
+
 void writer_count(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
                   const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
                   uint64_t* blk, unsigned long long* good, int grid, cudaStream_t st) {

@@ -23,6 +23,7 @@ SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
     "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
+    "ahfgpu_write_particles_bin_device",
 ]
 
 
@@ -72,6 +73,9 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_write_particles_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                                   C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_void_p]
     lib.ahfgpu_write_particles_device.restype = C.c_int
+    lib.ahfgpu_write_particles_bin_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
+                                                      C.POINTER(C.c_uint64), C.c_void_p]
+    lib.ahfgpu_write_particles_bin_device.restype = C.c_int
     _lib = lib
     return lib
 
@@ -250,4 +254,16 @@ def write_particles_device(ids, w, order, minpart: int, stream: int | None = Non
     check(load().ahfgpu_write_particles_device(ids.data_ptr(), w.data_ptr() if w is not None else None,
                                               order.data_ptr(), int(minpart), C.byref(out), C.byref(nb),
                                               C.c_void_p(stream) if stream else None))
+    return out.value, nb.value
+
+
+def write_particles_bin_device(ids, order, minpart: int, stream: int | None = None):
+    """ahfgpu_write_particles_bin_device for the last device result; ids and
+    order are torch CUDA tensors.  Returns (device address, nbytes) of the
+    AHF_particles_bin bytes."""
+    init()
+    out = C.c_void_p()
+    nb = C.c_uint64()
+    check(load().ahfgpu_write_particles_bin_device(ids.data_ptr(), order.data_ptr(), int(minpart), C.byref(out),
+                                                  C.byref(nb), C.c_void_p(stream) if stream else None))
     return out.value, nb.value

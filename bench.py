@@ -232,6 +232,21 @@ def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
     lines = int(npk[npk >= 20].sum() + (npk >= 20).sum() + 1)
     out = {"metric": "AHF_particles bytes/s", "value": nb / dt, "unit": "bytes/s", "ms_per_step": dt * 1e3,
            "bytes": int(nb), "lines": lines, "lines_per_s": lines / dt, "cpu_baseline": None}
+    # AHF_particles_bin (the AHFbinary build's file): 12 B per kept particle
+    for _ in range(max(1, args.warmup)):
+        addr, nbb = lib.write_particles_bin_device(ids, order, 20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        addr, nbb = lib.write_particles_bin_device(ids, order, 20)
+    torch.cuda.synchronize()
+    dtb = allmax(ws, (time.perf_counter() - t0) / args.steps)
+    kept = int(npk[npk >= 20].sum())
+    # algorithmic bytes: the kept entry (8 B) and its id (8 B) read, 12 B written
+    alg = 28 * kept + 16 * int((npk >= 20).sum()) + 16
+    out["binary"] = {"metric": "AHF_particles_bin bytes/s", "value": nbb / dtb, "unit": "bytes/s",
+                     "ms_per_step": dtb * 1e3, "bytes": int(nbb), "particles": kept,
+                     "algorithmic_bytes": alg, "achieved_gbs": alg / dtb / 1e9, "cpu_baseline": None}
     if rank == 0 and not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
@@ -251,6 +266,13 @@ def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
         out["cpu_baseline"] = {"value": len(data) / cdt, "unit": "bytes/s", "cores": 1, "kind": "port",
                                "sample": f"the kept lists of {len(sel)} seeded random haloes ({len(data)} bytes), "
                                          f"snprintf per line, {cdt:.2f} s"}
+        t1 = time.perf_counter()
+        data = O.write_particles_bin_oracle(np.arange(N, dtype=np.uint64), moff, mem, npk[sel].astype(np.uint64),
+                                            sub_order, 20)
+        cdt = time.perf_counter() - t1
+        out["binary"]["cpu_baseline"] = {"value": len(data) / cdt, "unit": "bytes/s", "cores": 1, "kind": "port",
+                                         "sample": f"the same {len(sel)} haloes ({len(data)} bytes), a copy per "
+                                                   f"field as the reference's fwrite calls, {cdt:.2f} s"}
     return out
 
 

@@ -243,6 +243,17 @@ AHFGPU_API int ahfgpu_write_particles_device(const uint64_t *ids, const float *w
                                              int64_t minpart, const unsigned char **out, uint64_t *nbytes,
                                              void *stream);
 
+/* Replaces ahf_binwrite_particles (src/libahf/ahf_io.c:1733-1855, the
+ * AHFbinary build; the AHF_particles_bin file) for the last device-resident
+ * result, arguments as ahfgpu_write_particles_device (the binary file has no
+ * weight column: every particle's type is 1).  Bytes: int32 1, uint64
+ * haloes written, uint32 2; per halo uint64 npart, uint64 j, then per kept
+ * particle uint64 id, int32 1 -- native byte order, no padding.  The text
+ * companion <prefix>.AHF_particles_info (ahf_io.c:1766-1774, constant) stays
+ * with the caller.                                                          */
+AHFGPU_API int ahfgpu_write_particles_bin_device(const uint64_t *ids, const int64_t *order, int64_t minpart,
+                                                 const unsigned char **out, uint64_t *nbytes, void *stream);
+
 /* Same stage with every pointer of `batch` already in device memory; the
  * results stay on the device in library-owned buffers (valid until the next
  * call or ahfgpu_shutdown) and are described by `dres` (device pointers,

@@ -1000,3 +1000,52 @@ int ahforacle_write_particles(const uint64_t *ids, const float *w, int64_t nhalo
   *nbytes = used;
   return 0;
 }
+
+
+/* ---------------------------------------------------------------------------
+ * AHF_particles_bin, ahf_binwrite_particles (src/libahf/ahf_io.c:1733-1855,
+ * AHFbinary build, no GAS_PARTICLES or AHFnewHaloIDs): int32 1, uint64 the
+ * number of haloes written (written as 0, put back after the rewind
+ * :1842-1844), uint32 2 (columns); per halo j of the output order with at
+ * least minpart particles, uint64 npart and uint64 j, then per kept particle
+ * uint64 id and int32 1.  Native byte order, fwrite of each field: no
+ * padding, 16 + 12 npart bytes per halo.                                    */
+static void put_bytes(unsigned char *buf, uint64_t *used, const void *v, size_t n)
+{
+  memcpy(buf + *used, v, n);
+  *used += n;
+}
+
+int ahforacle_write_particles_bin(const uint64_t *ids, int64_t nhalo, const uint64_t *member_off,
+                                  const uint64_t *member, const uint64_t *halo_npart, const int64_t *order,
+                                  int64_t minpart, unsigned char **out, uint64_t *nbytes)
+{
+  uint64_t total = 16, good = 0;
+  for (int64_t j = 0; j < nhalo; j++)
+    if ((int64_t)halo_npart[order[j]] >= minpart) {
+      good++;
+      total += 16 + 12 * halo_npart[order[j]];
+    }
+  unsigned char *buf = (unsigned char *)malloc(total);
+  if (!buf) return -1;
+  uint64_t used = 0;
+  const int32_t one = 1;
+  const uint32_t ncol = 2;
+  put_bytes(buf, &used, &one, 4);
+  put_bytes(buf, &used, &good, 8);
+  put_bytes(buf, &used, &ncol, 4);
+  for (int64_t j = 0; j < nhalo; j++) {
+    const int64_t i = order[j];
+    if (!((int64_t)halo_npart[i] >= minpart)) continue;
+    const uint64_t np = halo_npart[i], hj = (uint64_t)j;
+    put_bytes(buf, &used, &np, 8);
+    put_bytes(buf, &used, &hj, 8);
+    for (uint64_t k = member_off[i]; k < member_off[i] + np; k++) {
+      put_bytes(buf, &used, &ids[member[k]], 8);
+      put_bytes(buf, &used, &one, 4);
+    }
+  }
+  *out = buf;
+  *nbytes = used;
+  return 0;
+}

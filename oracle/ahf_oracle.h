@@ -45,6 +45,9 @@ void ahforacle_gather_free(uint64_t *idx);
 int  ahforacle_write_particles(const uint64_t *ids, const float *w, int64_t nhalo, const uint64_t *member_off,
                                const uint64_t *member, const uint64_t *halo_npart, const int64_t *order,
                                int64_t minpart, unsigned char **out, uint64_t *nbytes);
+int  ahforacle_write_particles_bin(const uint64_t *ids, int64_t nhalo, const uint64_t *member_off,
+                                   const uint64_t *member, const uint64_t *halo_npart, const int64_t *order,
+                                   int64_t minpart, unsigned char **out, uint64_t *nbytes);
 
 /* The gather radii, the loop of spatialRef2halos (src/libahf/ahf_halos.c:
  * 2987-3051): half the distance to the closest halo with strictly more

@@ -5,7 +5,8 @@ baseline leg import this module.  It loads
 
   oracle/_build/libahforacle.so   the C restatement (ahf_oracle.c), and
   oracle/_ref/libahfref[_mm].so   the reference's own routines driven by
-                                  ref_harness.c (only where they were built)
+                                  ref_harness.c (only where they were built;
+                                  libahfref_bin.so: the -DAHFbinary build)
 
 and returns ahf_gb300.abi.HostResult objects, the same shape the GPU library
 returns.
@@ -52,6 +53,10 @@ def oracle_path() -> str:
 
 def ref_path(multimass: bool) -> str:
     return os.path.join(HERE, "_ref", "libahfref_mm.so" if multimass else "libahfref.so")
+
+
+def ref_bin_path() -> str:
+    return os.path.join(HERE, "_ref", "libahfref_bin.so")
 
 
 def have_ref(multimass: bool = False) -> bool:
@@ -192,3 +197,30 @@ def write_particles_oracle(ids, w, member_off, member, halo_npart, order, minpar
 def write_particles_reference(ids, w, member_off, member, halo_npart, order, minpart: int) -> bytes:
     """The reference's own writer (ahf_io_WriteParticles), file read back."""
     return _writer(ref_path(w is not None), "ahfref", ids, w, member_off, member, halo_npart, order, minpart, True)
+
+
+def write_particles_bin_oracle(ids, member_off, member, halo_npart, order, minpart: int) -> bytes:
+    """The restated AHF_particles_bin bytes (ahf_binwrite_particles)."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_write_particles_bin
+    fn.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                   C.POINTER(C.POINTER(C.c_ubyte)), C.POINTER(C.c_uint64)]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(v, dtype=np.uint64) for v in (ids, member_off, member, halo_npart)]
+    o = np.ascontiguousarray(order, dtype=np.int64)
+    out = C.POINTER(C.c_ubyte)()
+    nb = C.c_uint64()
+    if fn(a[0].ctypes.data, len(a[3]), a[1].ctypes.data, a[2].ctypes.data, a[3].ctypes.data, o.ctypes.data,
+          int(minpart), C.byref(out), C.byref(nb)) != 0:
+        raise RuntimeError("binary writer failed")
+    data = bytes(np.ctypeslib.as_array(out, shape=(max(nb.value, 1),))[:nb.value])
+    C.CDLL(None).free.argtypes = [C.c_void_p]
+    C.CDLL(None).free(C.cast(out, C.c_void_p))
+    return data
+
+
+def write_particles_bin_reference(ids, member_off, member, halo_npart, order, minpart: int) -> bytes:
+    """The reference's own binary writer (ahf_io_WriteParticles of the
+    -DAHFbinary build), the AHF_particles_bin file read back."""
+    return _writer(ref_bin_path(), "ahfref", ids, None, member_off, member, halo_npart, order, minpart, True)

@@ -4,8 +4,11 @@
  * (src/libahf/ahf_io.c:178-212, WriteParticlesLegacy :1095-1175, compiled
  * unchanged), on haloes given as kept particle lists: global.fst_part holds
  * the particles (their ids), each HALO its npart and ipart, idx the output
- * order, simu.AHF_MINPART the cut.  The file it writes (<prefix>.AHF_particles)
- * is read back into a malloc()ed buffer.
+ * order, simu.AHF_MINPART the cut.  The file it writes is read back into a
+ * malloc()ed buffer: <prefix>.AHF_particles, or in the -DAHFbinary build
+ * (libahfref_bin.so) <prefix>.AHF_particles_bin, written by
+ * ahf_binwrite_particles (ahf_io.c:1733-1855); its text companion
+ * <prefix>.AHF_particles_info is removed.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -51,7 +54,13 @@ int ahfref_write_particles(uint64_t npart_total, const uint64_t *ids, const floa
   global.fst_part = NULL;
   global.no_part = 0;
   char fn[4096];
+#ifdef AHFbinary
+  snprintf(fn, sizeof fn, "%s.AHF_particles_info", prefix);
+  remove(fn);
+  snprintf(fn, sizeof fn, "%s.AHF_particles_bin", prefix);
+#else
   snprintf(fn, sizeof fn, "%s.AHF_particles", prefix);
+#endif
   FILE *f = fopen(fn, "rb");
   if (!f) return -2;
   fseek(f, 0, SEEK_END);

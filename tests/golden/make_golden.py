@@ -206,7 +206,9 @@ def make_gather() -> None:
 def make_writer() -> None:
     """The reference's own AHF_particles writer (ahf_io_WriteParticles) on the
     reference stage's kept lists of the cfg1 slice: inputs and the file's
-    bytes."""
+    bytes (`data`), and the AHF_particles_bin bytes of the reference's
+    -DAHFbinary build (ahf_binwrite_particles) on the same inputs
+    (`data_bin`)."""
     import oracle as O
     O.build()
     L = synth.generate("cfg1")
@@ -215,9 +217,10 @@ def make_writer() -> None:
     ids = (np.arange(L.n, dtype=np.uint64) * np.uint64(7919)) + np.uint64(10**12)
     order = np.argsort(-res.halo["npart"].astype(np.int64), kind="stable").astype(np.int64)
     data = O.write_particles_reference(ids, None, res.member_off, res.member, res.halo["npart"], order, 20)
+    data_bin = O.write_particles_bin_reference(ids, res.member_off, res.member, res.halo["npart"], order, 20)
     np.savez_compressed(os.path.join(HERE, "writer_cfg1.npz"), ids=ids, member_off=res.member_off,
                         member=res.member, npart=res.halo["npart"], order=order, minpart=20,
-                        data=np.frombuffer(data, np.uint8))
+                        data=np.frombuffer(data, np.uint8), data_bin=np.frombuffer(data_bin, np.uint8))
     print("writer_cfg1", len(data), os.path.getsize(os.path.join(HERE, "writer_cfg1.npz")))
 
 
