@@ -47,19 +47,19 @@ void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const
                  cudaStream_t st);
 void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
                   const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st);
-void writer_count(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
-                  const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
-                  uint64_t* blk, unsigned long long* good, int grid, cudaStream_t st);
+void writer_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
+                  uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st);
 void writer_offsets(const uint64_t* blk, int64_t nh, uint64_t* boff, cudaStream_t st);
-void writer_bin_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
-                      uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st);
+void writer_count(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                  const uint64_t* member, const uint64_t* ids, const float* w, const uint64_t* coff,
+                  unsigned int* qhead, uint64_t* cbytes, int grid, cudaStream_t st);
+void writer_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
+                  const uint64_t* member, const uint64_t* ids, const float* w, const uint64_t* coff,
+                  unsigned int* qhead, const uint64_t* cboff, const unsigned long long* good, unsigned char* out,
+                  int grid, cudaStream_t st);
 void writer_bin_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
                       const uint64_t* member, const uint64_t* ids, const uint64_t* boff, const uint64_t* coff,
                       const unsigned long long* good, unsigned int* qhead, uint32_t* out, int grid, cudaStream_t st);
-void writer_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
-                  const uint64_t* member, const uint64_t* ids, const float* w, int64_t minpart, unsigned int* qhead,
-                  const uint64_t* boff, const unsigned long long* good, unsigned char* out, int grid,
-                  cudaStream_t st);
 void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
                  const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
                  float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st);
@@ -158,7 +158,8 @@ struct Ctx {
   DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
   DBuf gr_pos, gr_lim, gr_orig;   // gather radii: sorted centres and R_vir, candidate counts, order
   DBuf wp_blk, wp_boff, wp_good, wp_qhead, wp_out;   // the AHF_particles bytes
-  DBuf wb_chunk, wb_coff;                            // AHF_particles_bin: chunks per block, their scan
+  DBuf wb_chunk, wb_coff;                            // both writers: chunks per block, their scan
+  DBuf wp_cbytes, wp_cboff;                          // ASCII: bytes per chunk, their scan
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -882,7 +883,8 @@ int ahfgpu_shutdown(void) {
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
                   &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
-                  &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.phase};
+                  &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.wp_cbytes,
+                  &g.wp_cboff, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1241,6 +1243,38 @@ int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* ce
   return AHFGPU_OK;
 }
 
+// The chunk plan shared by both writers: per output position j the chunks
+// of its block (wb_chunk) and their exclusive scan (wb_coff), the written
+// block count (wp_good), optionally the binary block bytes (wp_blk) and
+// their scan (wp_boff).  Returns the chunk total in *nchunks.
+static int writer_plan(const int64_t* order, int64_t minpart, bool bin_blocks, cudaStream_t st, uint64_t* nchunks,
+                       uint64_t* bin_total) {
+  const int64_t nh = g.last_nhalo;
+  int rc;
+  if ((rc = g.wp_blk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
+  if ((rc = g.wp_boff.ensure((nh + 1) * 8))) return rc;
+  if ((rc = g.wb_chunk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
+  if ((rc = g.wb_coff.ensure((nh + 1) * 8))) return rc;
+  if ((rc = g.wp_good.ensure(64))) return rc;
+  if ((rc = g.wp_qhead.ensure(64))) return rc;
+  CK(cudaMemsetAsync(g.wp_good.p, 0, 64, st));
+  if (nh > 0)
+    writer_sizes(nh, order, g.halo.as<ahfgpu_halo>(), minpart, bin_blocks ? g.wp_blk.as<uint64_t>() : nullptr,
+                 g.wb_chunk.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
+                 std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 255) / 256))), st);
+  if (bin_blocks) writer_offsets(g.wp_blk.as<uint64_t>(), nh, g.wp_boff.as<uint64_t>(), st);
+  writer_offsets(g.wb_chunk.as<uint64_t>(), nh, g.wb_coff.as<uint64_t>(), st);
+  CK(cudaGetLastError());
+  uint64_t tail[2] = {0, 0};
+  CK(cudaMemcpyAsync(&tail[0], g.wb_coff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  if (bin_blocks) CK(cudaMemcpyAsync(&tail[1], g.wp_boff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (tail[0] >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "writer: %llu chunks", (unsigned long long)tail[0]);
+  *nchunks = tail[0];
+  if (bin_total) *bin_total = tail[1];
+  return AHFGPU_OK;
+}
+
 int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int64_t* order, int64_t minpart,
                                   const unsigned char** out, uint64_t* nbytes, void* stream) {
   int rc = ensure_init();
@@ -1250,28 +1284,26 @@ int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int
   const int64_t nh = g.last_nhalo;
   if (nh > 0 && (!ids || !order)) return fail(AHFGPU_ERR_INVALID, "ids/order is NULL");
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
-  if ((rc = g.wp_blk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
-  if ((rc = g.wp_boff.ensure((nh + 1) * 8))) return rc;
-  if ((rc = g.wp_good.ensure(64))) return rc;
-  if ((rc = g.wp_qhead.ensure(64))) return rc;
-  const int grid = std::max(1, std::min<int>(g.nsm * 4, (int)std::max<int64_t>(nh, 1)));
+  uint64_t nch = 0;
+  if ((rc = writer_plan(order, minpart, false, st, &nch, nullptr))) return rc;
+  if ((rc = g.wp_cbytes.ensure(std::max<uint64_t>(nch * 8, 8)))) return rc;
+  if ((rc = g.wp_cboff.ensure((nch + 1) * 8))) return rc;
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, nch));
   CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
-  CK(cudaMemsetAsync(g.wp_good.p, 0, 64, st));
-  if (nh > 0)
+  if (nch > 0)
     writer_count(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids, w,
-                 minpart, g.wp_qhead.as<unsigned int>(), g.wp_blk.as<uint64_t>(),
-                 g.wp_good.as<unsigned long long>(), grid, st);
-  writer_offsets(g.wp_blk.as<uint64_t>(), nh, g.wp_boff.as<uint64_t>(), st);
+                 g.wb_coff.as<uint64_t>(), g.wp_qhead.as<unsigned int>(), g.wp_cbytes.as<uint64_t>(), grid, st);
+  writer_offsets(g.wp_cbytes.as<uint64_t>(), (int64_t)nch, g.wp_cboff.as<uint64_t>(), st);
   CK(cudaGetLastError());
   uint64_t body = 0;
-  CK(cudaMemcpyAsync(&body, g.wp_boff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&body, g.wp_cboff.as<uint64_t>() + nch, 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   const uint64_t total = 16 + body;
   if ((rc = g.wp_out.ensure(total))) return rc;
   CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
   writer_write(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids, w,
-               minpart, g.wp_qhead.as<unsigned int>(), g.wp_boff.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
-               g.wp_out.as<unsigned char>(), grid, st);
+               g.wb_coff.as<uint64_t>(), g.wp_qhead.as<unsigned int>(), g.wp_cboff.as<uint64_t>(),
+               g.wp_good.as<unsigned long long>(), g.wp_out.as<unsigned char>(), grid, st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));
   *out = g.wp_out.as<unsigned char>();
@@ -1288,29 +1320,12 @@ int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order,
   const int64_t nh = g.last_nhalo;
   if (nh > 0 && (!ids || !order)) return fail(AHFGPU_ERR_INVALID, "ids/order is NULL");
   cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
-  if ((rc = g.wp_blk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
-  if ((rc = g.wp_boff.ensure((nh + 1) * 8))) return rc;
-  if ((rc = g.wb_chunk.ensure(std::max<size_t>(nh * 8, 8)))) return rc;
-  if ((rc = g.wb_coff.ensure((nh + 1) * 8))) return rc;
-  if ((rc = g.wp_good.ensure(64))) return rc;
-  if ((rc = g.wp_qhead.ensure(64))) return rc;
-  CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
-  CK(cudaMemsetAsync(g.wp_good.p, 0, 64, st));
-  if (nh > 0)
-    writer_bin_sizes(nh, order, g.halo.as<ahfgpu_halo>(), minpart, g.wp_blk.as<uint64_t>(), g.wb_chunk.as<uint64_t>(),
-                     g.wp_good.as<unsigned long long>(), std::max(1, std::min<int>(g.nsm * 4, (int)((nh + 255) / 256))),
-                     st);
-  writer_offsets(g.wp_blk.as<uint64_t>(), nh, g.wp_boff.as<uint64_t>(), st);
-  writer_offsets(g.wb_chunk.as<uint64_t>(), nh, g.wb_coff.as<uint64_t>(), st);
-  CK(cudaGetLastError());
-  uint64_t tail[2] = {0, 0};
-  CK(cudaMemcpyAsync(&tail[0], g.wp_boff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(&tail[1], g.wb_coff.as<uint64_t>() + nh, 8, cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  if (tail[1] >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "binary writer: %llu chunks", (unsigned long long)tail[1]);
-  const uint64_t total = 16 + tail[0];
+  uint64_t nch = 0, body = 0;
+  if ((rc = writer_plan(order, minpart, true, st, &nch, &body))) return rc;
+  const uint64_t total = 16 + body;
   if ((rc = g.wp_out.ensure(total))) return rc;
-  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, tail[1]));
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, nch));
+  CK(cudaMemsetAsync(g.wp_qhead.p, 0, 64, st));
   writer_bin_write(nh, order, g.halo.as<ahfgpu_halo>(), g.member_off.as<uint64_t>(), g.member.as<uint64_t>(), ids,
                    g.wp_boff.as<uint64_t>(), g.wb_coff.as<uint64_t>(), g.wp_good.as<unsigned long long>(),
                    g.wp_qhead.as<unsigned int>(), g.wp_out.as<uint32_t>(), grid, st);

@@ -124,22 +124,25 @@ def _gpu_bytes(lib, ids, w, order, minpart):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["cfg4", "multimass"])
+@pytest.mark.parametrize("case", ["cfg4", "multimass", "large"])
 def test_gpu_writer_matches_restatement(gpu, case):
+    """Blocks of one and of several 4096-line chunks, MINPART 20 and 0."""
     import torch
     from ahf_gb300 import synth
     O = _oracle()
     L = (synth.generate("cfg3", scale=0.002, max_particles=20000, multimass=True) if case == "multimass"
+         else synth.generate("cfg3", scale=0.0003, max_particles=300000) if case == "large"
          else synth.generate("cfg4", scale=0.01))
     t = _device_lists(L)
     gpu.construct_halos_device(synth.params_for(L), gpu.device_batch(t), "batched_fp32c")
     res = gpu.fetch_result()
     ids = np.arange(L.n, dtype=np.uint64) * np.uint64(977) + np.uint64(123456789)
     order = np.argsort(-res.halo["npart"].astype(np.int64), kind="stable").astype(np.int64)
-    exp = O.write_particles_oracle(ids, L.w, res.member_off, res.member, res.halo["npart"], order, 20)
-    got = _gpu_bytes(gpu, torch.as_tensor(ids.astype(np.int64)).cuda(), t["w"],
-                     torch.as_tensor(order).cuda(), 20)
-    assert got == exp
+    ids_d = torch.as_tensor(ids.astype(np.int64)).cuda()
+    order_d = torch.as_tensor(order).cuda()
+    for minpart in (20, 0):
+        exp = O.write_particles_oracle(ids, L.w, res.member_off, res.member, res.halo["npart"], order, minpart)
+        assert _gpu_bytes(gpu, ids_d, t["w"], order_d, minpart) == exp
 
 
 @pytest.mark.gpu
