@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--mode", default=None, help="form timed for `value` (default: fastest built)")
     ap.add_argument("--forms", default="all", help="comma list of extra forms to time once, or none")
     ap.add_argument("--cpu-particles", type=float, default=6e7, help="CPU baseline sample size")
+    ap.add_argument("--cpu-serial-particles", type=float, default=5e6,
+                    help="sample size of the one-thread CPU rate (0: skip)")
     ap.add_argument("--plain-particles", type=float, default=2e7, help="plain FP64 form sample size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -634,6 +636,13 @@ def ours_arm(args, ws, rank, local):
         cpu = {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": kind,
                "sample": f"seeded random subset of {len(samp)} haloes / {n} particles of the workload, "
                          f"{nthreads} OpenMP threads, {dt:.2f} s"}
+        if args.cpu_serial_particles > 0:
+            # the serial build's rate (one host core), beside the threaded one
+            samp1 = cpu_sample(n_in, args.cpu_serial_particles, seed=23)
+            n1, dt1, kind1 = run_cpu(params, lists_np, samp1, 1)
+            cpu["serial"] = {"value": n1 / dt1, "unit": UNIT, "cores": 1, "kind": kind1,
+                             "sample": f"seeded random subset of {len(samp1)} haloes / {n1} particles, "
+                                       f"one thread, {dt1:.2f} s"}
     if rank != 0:
         return
     line = {
