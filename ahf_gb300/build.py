@@ -29,6 +29,7 @@ UNITS = {
     "noalloc.cu": [],
     "gather.cu": [],
     "writer.cu": [],
+    "sfc.cu": [],
 }
 
 

@@ -47,6 +47,13 @@ void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const
                  cudaStream_t st);
 void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
                   const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st);
+uint32_t sfc_ntiles(uint32_t n);
+uint32_t sfc_scan_blocks(uint32_t m);
+void sfc_keys(uint32_t n, const float* x, const float* y, const float* z, int bits, uint64_t* keys, uint32_t* idx,
+              int grid, cudaStream_t st);
+void sfc_pass(uint32_t n, const uint64_t* kin, const uint32_t* iin, int shift, uint32_t* gh, uint32_t* goff,
+              uint32_t* part, uint64_t* kout, uint32_t* iout, int* err, cudaStream_t st);
+void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaStream_t st);
 void writer_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
                   uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st);
 void writer_offsets(const uint64_t* blk, int64_t nh, uint64_t* boff, cudaStream_t st);
@@ -160,6 +167,7 @@ struct Ctx {
   DBuf wp_blk, wp_boff, wp_good, wp_qhead, wp_out;   // the AHF_particles bytes
   DBuf wb_chunk, wb_coff;                            // both writers: chunks per block, their scan
   DBuf wp_cbytes, wp_cboff;                          // ASCII: bytes per chunk, their scan
+  DBuf sfc_kb, sfc_ia, sfc_ib, sfc_gh, sfc_goff, sfc_part, sfc_err;   // the SFC key sort
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -884,7 +892,8 @@ int ahfgpu_shutdown(void) {
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
                   &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
                   &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.wp_cbytes,
-                  &g.wp_cboff, &g.phase};
+                  &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
+                  &g.sfc_err, &g.phase};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1333,6 +1342,45 @@ int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order,
   CK(cudaStreamSynchronize(st));
   *out = g.wp_out.as<unsigned char>();
   *nbytes = total;
+  return AHFGPU_OK;
+}
+
+int ahfgpu_sfc_sort_device(uint64_t n, const float* x, const float* y, const float* z, int bits, uint64_t* keys,
+                           uint64_t* order, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (n == 0) return AHFGPU_OK;
+  if (n >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "sfc sort: %llu particles (limit 2^31 - 1)",
+                                     (unsigned long long)n);
+  if (bits < 1 || bits > 21) return fail(AHFGPU_ERR_INVALID, "sfc sort: bits %d outside 1..21", bits);
+  if (!x || !y || !z || !keys || !order) return fail(AHFGPU_ERR_INVALID, "sfc sort: a pointer is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  const uint32_t nn = (uint32_t)n, nt = sfc_ntiles(nn), m = 256u * nt, nb = sfc_scan_blocks(m);
+  if ((rc = g.sfc_kb.ensure(n * 8))) return rc;
+  if ((rc = g.sfc_ia.ensure(n * 4))) return rc;
+  if ((rc = g.sfc_ib.ensure(n * 4))) return rc;
+  if ((rc = g.sfc_gh.ensure((size_t)m * 4))) return rc;
+  if ((rc = g.sfc_goff.ensure((size_t)m * 4))) return rc;
+  if ((rc = g.sfc_part.ensure((size_t)nb * 4))) return rc;
+  if ((rc = g.sfc_err.ensure(64))) return rc;
+  CK(cudaMemsetAsync(g.sfc_err.p, 0, 64, st));
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
+  sfc_keys(nn, x, y, z, bits, keys, g.sfc_ia.as<uint32_t>(), grid, st);
+  uint64_t *kin = keys, *kout = g.sfc_kb.as<uint64_t>();
+  uint32_t *iin = g.sfc_ia.as<uint32_t>(), *iout = g.sfc_ib.as<uint32_t>();
+  for (int shift = 0; shift < 3 * bits; shift += 8) {
+    sfc_pass(nn, kin, iin, shift, g.sfc_gh.as<uint32_t>(), g.sfc_goff.as<uint32_t>(), g.sfc_part.as<uint32_t>(),
+             kout, iout, g.sfc_err.as<int>(), st);
+    std::swap(kin, kout);
+    std::swap(iin, iout);
+  }
+  if (kin != keys) CK(cudaMemcpyAsync(keys, kin, n * 8, cudaMemcpyDeviceToDevice, st));
+  sfc_order(nn, iin, order, grid, st);
+  CK(cudaGetLastError());
+  int derr = 0;
+  CK(cudaMemcpyAsync(&derr, g.sfc_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr) return fail(AHFGPU_ERR_CUDA, "sfc sort: a scatter index left the array");
   return AHFGPU_OK;
 }
 

@@ -23,7 +23,7 @@ SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
     "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
-    "ahfgpu_write_particles_bin_device",
+    "ahfgpu_write_particles_bin_device", "ahfgpu_sfc_sort_device",
 ]
 
 
@@ -76,6 +76,9 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_write_particles_bin_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
     lib.ahfgpu_write_particles_bin_device.restype = C.c_int
+    lib.ahfgpu_sfc_sort_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]
+    lib.ahfgpu_sfc_sort_device.restype = C.c_int
     _lib = lib
     return lib
 
@@ -267,3 +270,16 @@ def write_particles_bin_device(ids, order, minpart: int, stream: int | None = No
     check(load().ahfgpu_write_particles_bin_device(ids.data_ptr(), order.data_ptr(), int(minpart), C.byref(out),
                                                   C.byref(nb), C.c_void_p(stream) if stream else None))
     return out.value, nb.value
+
+
+def sfc_sort_device(x, y, z, bits: int = 21, stream: int | None = None):
+    """ahfgpu_sfc_sort_device on float32 CUDA tensors x, y, z: (keys, order)
+    as int64 CUDA tensors (keys hold the uint64 Hilbert keys bit for bit)."""
+    import torch
+    init()
+    n = int(x.numel())
+    keys = torch.empty(n, dtype=torch.int64, device=x.device)
+    order = torch.empty(n, dtype=torch.int64, device=x.device)
+    check(load().ahfgpu_sfc_sort_device(n, x.data_ptr(), y.data_ptr(), z.data_ptr(), int(bits), keys.data_ptr(),
+                                        order.data_ptr(), C.c_void_p(stream) if stream else None))
+    return keys, order

@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-gather", action="store_true", help="skip the particle-gather leg")
     ap.add_argument("--no-writer", action="store_true", help="skip the AHF_particles writer leg")
     ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
+    ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
     ap.add_argument("--multimass", action="store_true")
     return ap.parse_args()
 
@@ -275,6 +276,47 @@ def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
         out["binary"]["cpu_baseline"] = {"value": len(data) / cdt, "unit": "bytes/s", "cores": 1, "kind": "port",
                                          "sample": f"the same {len(sel)} haloes ({len(data)} bytes), a copy per "
                                                    f"field as the reference's fwrite calls, {cdt:.2f} s"}
+    return out
+
+
+def sfc_leg(lists, args, ws: int, rank: int) -> dict:
+    """Hilbert keys and the particle order by key for the workload's
+    particles as one snapshot (the keying loop and qsort of main.c:342-356),
+    timed like the other legs; the restated keying and sort (C, one host
+    core) on a bounded sample beside it."""
+    import torch
+    from ahf_gb300 import lib
+    try:
+        n = int(lists.x.numel())
+        for _ in range(max(1, args.warmup)):
+            keys, order = lib.sfc_sort_device(lists.x, lists.y, lists.z)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            keys, order = lib.sfc_sort_device(lists.x, lists.y, lists.z)
+        torch.cuda.synchronize()
+        dt = allmax(ws, (time.perf_counter() - t0) / args.steps)
+        ok = bool((keys[1:] >= keys[:-1]).all().item())
+        del keys, order
+        torch.cuda.empty_cache()
+        # algorithmic bytes: positions read (12 B), keys and order written (16 B)
+        out = {"metric": "particles keyed and sorted/s", "value": n / dt, "unit": "particles/s",
+               "ms_per_step": dt * 1e3, "n_particles": n, "keys_ascending": ok,
+               "algorithmic_bytes": 28 * n, "achieved_gbs": 28 * n / dt / 1e9, "cpu_baseline": None}
+    except Exception as e:   # noqa: BLE001 -- reported in the line, the other legs stand
+        return {"error": str(e)[:300]}
+    if rank == 0 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build(ref=False)
+        m = min(n, 5_000_000)
+        sel = slice(0, m)
+        xs = [v[sel].cpu().numpy() for v in (lists.x, lists.y, lists.z)]
+        t1 = time.perf_counter()
+        O.sfc_sort_oracle(*xs)
+        cdt = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": m / cdt, "unit": "particles/s", "cores": 1, "kind": "port",
+                               "sample": f"the first {m} particles, keys and qsort, {cdt:.2f} s"}
     return out
 
 
@@ -643,6 +685,9 @@ def ours_arm(args, ws, rank, local):
             cpu["serial"] = {"value": n1 / dt1, "unit": UNIT, "cores": 1, "kind": kind1,
                              "sample": f"seeded random subset of {len(samp1)} haloes / {n1} particles, "
                                        f"one thread, {dt1:.2f} s"}
+    # the Hilbert keying and particle sort (ahfgpu_sfc_sort_device), last:
+    # a failure here is reported in its key and costs no other number
+    sfc = None if args.no_sfc else sfc_leg(lists, args, ws, rank)
     if rank != 0:
         return
     line = {
@@ -666,6 +711,7 @@ def ours_arm(args, ws, rank, local):
         "forms": forms,
         "gather": gather,
         "writer": writer,
+        "sfc_sort": sfc,
         "precision": precision,
         "diagnostics": headline_stats,
     }

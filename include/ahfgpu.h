@@ -219,6 +219,15 @@ AHFGPU_API int ahfgpu_gather_device(const ahfgpu_particles *parts,
                                     ahfgpu_batch           *gathered,
                                     void                   *stream);
 
+/* Replaces the keying loop and the particle sort of src/main.c:342-356
+ * (sfc_curve_calcKey(SFC_CURVE_HILBERT, pos, BITS_PER_DIMENSION) for every
+ * particle, then qsort by cmp_sfckey_part, src/libutility/specific.c:1117):
+ * keys[k] the k-th smallest Hilbert key at `bits` levels (1..21; AHF uses
+ * 21), order[k] the input index of that particle; equal keys keep their
+ * input order.  Device pointers; positions in [0, 1]; n < 2^31.           */
+AHFGPU_API int ahfgpu_sfc_sort_device(uint64_t n, const float *x, const float *y, const float *z, int bits,
+                                      uint64_t *keys, uint64_t *order, void *stream);
+
 /* Replaces the gather-radius loop of spatialRef2halos
  * (src/libahf/ahf_halos.c:2987-3051): for each halo, half the periodic
  * distance (double, the reference's operation order) to the closest halo

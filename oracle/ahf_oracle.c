@@ -1049,3 +1049,75 @@ int ahforacle_write_particles_bin(const uint64_t *ids, int64_t nhalo, const uint
   *nbytes = used;
   return 0;
 }
+
+
+/* ---------------------------------------------------------------------------
+ * Hilbert keys and the particle sort (src/main.c:342-356).
+ * sfc_curve_calcKey(SFC_CURVE_HILBERT, ...) (libsfc/sfc_curve.c:79-91) maps
+ * a position in [0,1]^3 to grid coordinates c_d = trunc(x_d 2^bits), capped
+ * at 2^bits - 1 (libsfc/hilbert_util.c:69-92), and those to the index of the
+ * cell on the Hilbert curve of libsfc/hilbert.c (hilbert_c2i, :197-240).
+ * That curve, restated per level from the most significant bit: with g_b the
+ * 3-bit group (bit b of c_0, c_1, c_2 as bits 0, 1, 2) and G_b = g_b ^
+ * g_{b+1} (g_bits = 0), each level emits r_b = rotr3(G_b ^ flip, rot); then
+ * flip = 1 << rot, and rot advances by 1, plus 1 or 2 when the lowest set
+ * bit of r_b is bit 0 or bit 1 (mod 3); rot and flip start at 0.  The
+ * emitted index has bit 2 of every level but the top one inverted and is
+ * then Gray-decoded (prefix XOR from the top).  The sort: ascending key; the
+ * reference's qsort leaves equal keys in its C library's order, the
+ * restatement by original index.                                          */
+uint64_t ahforacle_sfc_key(double x, double y, double z, unsigned bits)
+{
+  const uint64_t max = (uint64_t)1 << bits;
+  const double v[3] = {x, y, z};
+  uint64_t c[3];
+  for (int d = 0; d < 3; d++) {
+    c[d] = (uint64_t)trunc(v[d] * (double)max);
+    if (c[d] == max) c[d] = max - 1;
+  }
+  uint64_t key = 0;
+  unsigned rot = 0, flip = 0, gup = 0;
+  for (int b = (int)bits - 1; b >= 0; b--) {
+    const unsigned g = (unsigned)(((c[0] >> b) & 1u) | (((c[1] >> b) & 1u) << 1) | (((c[2] >> b) & 1u) << 2));
+    const unsigned t = (g ^ gup ^ flip) & 7u;
+    const unsigned r = ((t >> rot) | (t << (3u - rot))) & 7u;
+    key = (key << 3) | r;
+    flip = 1u << rot;
+    const unsigned low = r & (0u - r) & 3u;
+    rot += 1u + (low == 1u ? 1u : 0u) + (low == 2u ? 2u : 0u);
+    if (rot >= 3u) rot -= 3u;
+    gup = g;
+  }
+  for (unsigned b = 0; b + 1 < bits; b++) key ^= (uint64_t)4 << (3 * b);
+  for (unsigned s = 1; s < 3 * bits; s *= 2) key ^= key >> s;
+  return key;
+}
+
+typedef struct {
+  uint64_t key, idx;
+} keyidx_t;
+
+static int cmp_keyidx(const void *a, const void *b)
+{
+  const keyidx_t *p = (const keyidx_t *)a, *q = (const keyidx_t *)b;
+  if (p->key != q->key) return p->key < q->key ? -1 : 1;
+  return p->idx < q->idx ? -1 : (p->idx > q->idx);
+}
+
+int ahforacle_sfc_sort(uint64_t n, const float *x, const float *y, const float *z, unsigned bits, uint64_t *keys,
+                       uint64_t *order)
+{
+  keyidx_t *a = (keyidx_t *)malloc((n ? n : 1) * sizeof(keyidx_t));
+  if (!a) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    a[i].key = ahforacle_sfc_key((double)x[i], (double)y[i], (double)z[i], bits);
+    a[i].idx = i;
+  }
+  qsort(a, (size_t)n, sizeof(keyidx_t), cmp_keyidx);
+  for (uint64_t k = 0; k < n; k++) {
+    keys[k] = a[k].key;
+    order[k] = a[k].idx;
+  }
+  free(a);
+  return 0;
+}

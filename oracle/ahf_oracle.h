@@ -56,6 +56,12 @@ int  ahforacle_write_particles_bin(const uint64_t *ids, int64_t nhalo, const uin
 void ahforacle_gather_radii(int64_t nhalo, const uint64_t *npart, const double *cx, const double *cy,
                             const double *cz, const double *rvir, double max_gather_rad_box, double *rad);
 
+/* Hilbert keys (sfc_curve_calcKey, SFC_CURVE_HILBERT) and the particle sort
+ * by key (src/main.c:342-356; equal keys by original index).              */
+uint64_t ahforacle_sfc_key(double x, double y, double z, unsigned bits);
+int  ahforacle_sfc_sort(uint64_t n, const float *x, const float *y, const float *z, unsigned bits, uint64_t *keys,
+                        uint64_t *order);
+
 #ifdef __cplusplus
 }
 #endif

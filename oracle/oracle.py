@@ -224,3 +224,46 @@ def write_particles_bin_reference(ids, member_off, member, halo_npart, order, mi
     """The reference's own binary writer (ahf_io_WriteParticles of the
     -DAHFbinary build), the AHF_particles_bin file read back."""
     return _writer(ref_bin_path(), "ahfref", ids, None, member_off, member, halo_npart, order, minpart, True)
+
+
+def sfc_keys_oracle(x, y, z, bits: int = 21):
+    """Restated Hilbert keys of float positions (sfc_curve_calcKey)."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_sfc_key
+    fn.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint]
+    fn.restype = C.c_uint64
+    return np.array([fn(float(a), float(b), float(c), bits) for a, b, c in zip(x, y, z)], dtype=np.uint64)
+
+
+def _sfc_sort(lib, name, x, y, z, extra):
+    import numpy as np
+    fn = getattr(lib, name)
+    fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p] + [C.c_uint] * len(extra) + [C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    keys = np.zeros(len(a[0]), np.uint64)
+    order = np.zeros(len(a[0]), np.uint64)
+    if fn(len(a[0]), *[v.ctypes.data for v in a], *extra, keys.ctypes.data, order.ctypes.data) != 0:
+        raise RuntimeError(f"{name} failed")
+    return keys, order
+
+
+def sfc_sort_oracle(x, y, z, bits: int = 21):
+    """(keys ascending, original index of each): the restated keying and
+    sort of main.c:342-356, equal keys by original index."""
+    return _sfc_sort(C.CDLL(oracle_path()), "ahforacle_sfc_sort", x, y, z, [bits])
+
+
+def sfc_sort_reference(x, y, z):
+    """The reference's own keying (sfc_curve_calcKey, BITS_PER_DIMENSION) and
+    qsort by cmp_sfckey_part."""
+    return _sfc_sort(C.CDLL(ref_path(False)), "ahfref_sfc_sort", x, y, z, [])
+
+
+def sfc_key_reference(x: float, y: float, z: float, bits: int) -> int:
+    lib = C.CDLL(ref_path(False))
+    fn = lib.ahfref_sfc_key
+    fn.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint]
+    fn.restype = C.c_uint64
+    return int(fn(x, y, z, bits))

@@ -73,3 +73,34 @@ int ahfref_gather(uint64_t n, const float *x, const float *y, const float *z, in
 }
 
 void ahfref_gather_free(uint64_t *idx) { free(idx); }
+
+/* The reference's keying and sort alone (main.c:342-356): keys[k] and
+ * order[k] = original index of the k-th particle after the qsort by
+ * cmp_sfckey_part.  Equal keys come out in the order the C library's qsort
+ * leaves them. */
+int ahfref_sfc_sort(uint64_t n, const float *x, const float *y, const float *z, uint64_t *keys, uint64_t *order)
+{
+  partptr p = (partptr)calloc(n ? n : 1, sizeof(part));
+  if (!p) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    p[i].pos[0] = x[i];
+    p[i].pos[1] = y[i];
+    p[i].pos[2] = z[i];
+    p[i].sfckey = sfc_curve_calcKey(SFC_CURVE_HILBERT, (double)p[i].pos[0], (double)p[i].pos[1],
+                                    (double)p[i].pos[2], BITS_PER_DIMENSION);
+    p[i].id = (part_id_t)i;
+  }
+  qsort(p, (size_t)n, sizeof(part), &cmp_sfckey_part);
+  for (uint64_t k = 0; k < n; k++) {
+    keys[k] = (uint64_t)p[k].sfckey;
+    order[k] = (uint64_t)p[k].id;
+  }
+  free(p);
+  return 0;
+}
+
+/* One key: sfc_curve_calcKey(SFC_CURVE_HILBERT, x, y, z, bits). */
+uint64_t ahfref_sfc_key(double x, double y, double z, unsigned bits)
+{
+  return (uint64_t)sfc_curve_calcKey(SFC_CURVE_HILBERT, x, y, z, bits);
+}
