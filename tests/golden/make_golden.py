@@ -224,7 +224,26 @@ def make_writer() -> None:
     print("writer_cfg1", len(data), os.path.getsize(os.path.join(HERE, "writer_cfg1.npz")))
 
 
+def make_sfc() -> None:
+    """The reference's own keying and particle sort (sfc_curve_calcKey at
+    BITS_PER_DIMENSION, qsort by cmp_sfckey_part; main.c:342-356) on the cfg1
+    snapshot of the gather fixture (its first 6000 particles) plus edge positions (0, 1 - 2^-24, 1.0)
+    and repeated positions: inputs, sorted keys and the original index of
+    each."""
+    import oracle as O
+    O.build()
+    L = synth.generate("cfg1")
+    S = synth.snapshot_from_lists(L, 20000, seed=9)
+    x, y, z = (np.asarray(v, dtype=np.float32)[:6000].copy() for v in (S.x, S.y, S.z))
+    x[:8], y[:8], z[:8] = 0.0, np.float32(1 - 2 ** -24), 1.0
+    x[8:40], y[8:40], z[8:40] = x[100:132], y[100:132], z[100:132]
+    keys, order = O.sfc_sort_reference(x, y, z)
+    np.savez_compressed(os.path.join(HERE, "sfc_cfg1.npz"), x=x, y=y, z=z, keys=keys, order=order)
+    print("sfc_cfg1", len(keys), os.path.getsize(os.path.join(HERE, "sfc_cfg1.npz")))
+
+
 if __name__ == "__main__":
     main()
     make_gather()
     make_writer()
+    make_sfc()

@@ -5,7 +5,8 @@ reference's own sfc_curve_calcKey (compiled unchanged into oracle/_ref) for
 every level count 1..21 and at the box edges; hand-worked first-level order;
 the Hilbert property (consecutive keys are face-adjacent cells) over every
 cell at 2 and 3 levels; the sort equal to the reference's qsort (keys, and
-each run of equal keys as a set).  GPU: ahfgpu_sfc_sort_device equal to the
+each run of equal keys as a set; live and the committed fixture
+tests/golden/sfc_cfg1.npz).  GPU: ahfgpu_sfc_sort_device equal to the
 restatement, keys and order (equal keys by original index).
 Bar: identical integers.
 """
@@ -103,6 +104,21 @@ def test_sort_matches_reference(ties):
         else:
             assert o1[s] == o2[s]
     assert np.all(np.diff(o1.astype(np.int64))[k1[1:] == k1[:-1]] > 0)   # equal keys by original index
+
+
+def test_sort_matches_reference_fixture():
+    """tests/golden/sfc_cfg1.npz: the reference's own keys and qsort order on
+    a cfg1 snapshot with edge and repeated positions (make_golden.py)."""
+    O = _oracle()
+    d = np.load(os.path.join(HERE, "golden", "sfc_cfg1.npz"))
+    k, o = O.sfc_sort_oracle(d["x"], d["y"], d["z"])
+    assert np.array_equal(k, d["keys"])
+    same = np.r_[False, k[1:] == k[:-1]]
+    assert same.any()                                   # the fixture holds equal keys
+    assert np.array_equal(o[~same & ~np.r_[same[1:], False]], d["order"][~same & ~np.r_[same[1:], False]])
+    starts = np.flatnonzero(~same)
+    for s_, e_ in zip(starts, np.r_[starts[1:], len(k)]):
+        assert sorted(o[s_:e_]) == sorted(d["order"][s_:e_])
 
 
 HARNESS = r"""
