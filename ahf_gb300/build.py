@@ -2,8 +2,10 @@
 
 Each translation unit is compiled by nvcc in parallel and linked into one
 shared library with the CUDA runtime linked statically, so the library only
-needs the driver at run time.  halo_*.cu kernels that must round like the
-reference's FP64 C build are compiled with --fmad=false.
+needs the CUDA driver at run time.  The stage's units (halo_fp64.cu,
+fp32c_*.cu) are compiled with --fmad=false: their FP64 paths must round like
+the reference's C build, and the float-float arithmetic needs its products
+and sums unfused.
 """
 from __future__ import annotations
 
