@@ -267,3 +267,28 @@ def sfc_key_reference(x: float, y: float, z: float, bits: int) -> int:
     fn.argtypes = [C.c_double, C.c_double, C.c_double, C.c_uint]
     fn.restype = C.c_uint64
     return int(fn(x, y, z, bits))
+
+
+def ref_radii_path() -> str:
+    return os.path.join(HERE, "_ref", "libahfref_radii.so")
+
+
+def gather_radii_reference(npart, cx, cy, cz, rvir, max_gather_rad_box: float):
+    """The reference's own gather-radius loop, run through spatialRef2halos
+    on a two-level refinement tree (oracle/ref_radii.c).  Halo 0 is the
+    tree's host, whose R_vir the reference leaves at -1: returns (radii,
+    R_vir each halo carried)."""
+    import numpy as np
+    lib = C.CDLL(ref_radii_path())
+    fn = lib.ahfref_gather_radii
+    fn.argtypes = [C.c_int64] + [C.c_void_p] * 5 + [C.c_double, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(npart, dtype=np.uint64)] + [np.ascontiguousarray(v, dtype=np.float64)
+                                                          for v in (cx, cy, cz, rvir)]
+    n = len(a[0])
+    rad = np.zeros(n)
+    rv = np.zeros(n)
+    rc = fn(n, *[v.ctypes.data for v in a], float(max_gather_rad_box), rad.ctypes.data, rv.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ahfref_gather_radii failed ({rc})")
+    return rad, rv

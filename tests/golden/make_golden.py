@@ -242,8 +242,31 @@ def make_sfc() -> None:
     print("sfc_cfg1", len(keys), os.path.getsize(os.path.join(HERE, "sfc_cfg1.npz")))
 
 
+def make_radii() -> None:
+    """The reference's own gather-radius loop (spatialRef2halos run on a
+    two-level refinement tree, oracle/ref_radii.c) on 2500 haloes: counts
+    with many ties, coincident and grid-aligned centres, R_vir above and
+    below the radii; inputs, radii and the R_vir each halo carried."""
+    import oracle as O
+    O.build()
+    rng = np.random.default_rng(21)
+    n = 2500
+    npart = np.floor(20 * rng.random(n) ** -1.3).astype(np.uint64)
+    c = rng.random((3, n))
+    c[:, :60] = np.round(c[:, :60], 2)
+    c[:, 60:70] = c[:, 70:80]
+    rvir = rng.random(n) * 0.004
+    rvir[100:110] = 0.3
+    maxg = 0.02
+    rad, rv = O.gather_radii_reference(npart, c[0], c[1], c[2], rvir, maxg)
+    np.savez_compressed(os.path.join(HERE, "radii_ref.npz"), npart=npart, cx=c[0], cy=c[1], cz=c[2], rvir=rv,
+                        max_gather_rad_box=maxg, rad=rad)
+    print("radii_ref", n, os.path.getsize(os.path.join(HERE, "radii_ref.npz")))
+
+
 if __name__ == "__main__":
     main()
     make_gather()
     make_writer()
     make_sfc()
+    make_radii()

@@ -1,9 +1,12 @@
 """Gather radii: the loop of spatialRef2halos (src/libahf/ahf_halos.c:2987-3051).
 
-The loop sits inside spatialRef2halos after AHF's AMR refinement walk and
-cannot be called alone, so the oracle is a restatement of it
-(oracle/ahf_oracle.c), checked here against hand-worked cases and against a
-second, vectorised numpy statement of the same rule.  GPU: the C ABI
+The loop sits at the end of spatialRef2halos, after the refinement tree has
+been turned into haloes.  The restatement (oracle/ahf_oracle.c) is checked
+against hand-worked cases, a second, vectorised numpy statement of the same
+rule, and the reference itself: oracle/ref_radii.c runs the reference's
+spatialRef2halos (compiled unchanged) on a two-level refinement tree that
+yields the given haloes (live where the reference is compiled, and the
+committed fixture tests/golden/radii_ref.npz).  GPU: the C ABI
 (ahfgpu_gather_radii_device) equal to the oracle, bit for bit.
 """
 import os
@@ -80,6 +83,30 @@ def test_gather_radii_restatement_matches_numpy():
     rvir = rng.random(n) * 0.002
     got = O.gather_radii_oracle(npart, c[0], c[1], c[2], rvir, 0.3)
     assert np.array_equal(got, numpy_radii(npart, c[0], c[1], c[2], rvir, 0.3))
+
+
+def test_gather_radii_restatement_matches_reference_live():
+    O = _oracle()
+    if not os.path.isfile(O.ref_radii_path()):
+        pytest.skip("reference not compiled here")
+    cases = [hand_case()]
+    rng = np.random.default_rng(31)
+    for n, maxg in ((1, 0.1), (2, 0.1), (4000, 0.3)):
+        npart = np.floor(20 * rng.random(n) ** -1.2).astype(np.uint64)
+        c = rng.random((3, n))
+        c[:, : n // 10] = np.round(c[:, : n // 10], 1)          # coincident and grid-aligned centres
+        cases.append((npart, c[0], c[1], c[2], rng.random(n) * 0.01, maxg))
+    for npart, cx, cy, cz, rvir, maxg in cases:
+        rad, rv = O.gather_radii_reference(npart, cx, cy, cz, rvir, maxg)
+        assert rv[0] == -1.0 and np.array_equal(rv[1:], np.asarray(rvir, dtype=np.float64)[1:])
+        assert np.array_equal(O.gather_radii_oracle(npart, cx, cy, cz, rv, maxg), rad)
+
+
+def test_gather_radii_restatement_matches_reference_fixture():
+    O = _oracle()
+    d = np.load(os.path.join(HERE, "golden", "radii_ref.npz"))
+    got = O.gather_radii_oracle(d["npart"], d["cx"], d["cy"], d["cz"], d["rvir"], float(d["max_gather_rad_box"]))
+    assert np.array_equal(got, d["rad"])
 
 
 @pytest.mark.gpu
