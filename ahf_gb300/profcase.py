@@ -5,6 +5,7 @@
     python -m ahf_gb300.profcase big [mode]     # one halo of ~2e5 particles
     python -m ahf_gb300.profcase full [mode]    # the whole 1e5-halo workload
     python -m ahf_gb300.profcase gather [scale] # the particle gather, the lists of 1e5*scale haloes as a snapshot
+    python -m ahf_gb300.profcase sfc [n]        # Hilbert keys and sort of n seeded uniform points (5e7)
 
 Each runs the stage twice on a device-resident batch cut from the seeded
 1e5-halo workload (cfg3) and prints the device time and diagnostics.
@@ -62,11 +63,33 @@ def gather_case(scale: float = 0.05) -> None:
           f"ms per call {', '.join(f'{m:.1f}' for m in ms)}")
 
 
+def sfc_case(n: int = 50_000_000) -> None:
+    import torch
+    from . import lib
+    lib.init(0)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    x, y, z = (torch.rand(n, device="cuda", generator=g) for _ in range(3))
+    ms = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        keys, order = lib.sfc_sort_device(x, y, z)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    ok = bool((keys[1:] >= keys[:-1]).all().item())
+    print(f"sfc: points {n} ascending {ok} ms per call {', '.join(f'{m:.2f}' for m in ms)}")
+
+
 def main(argv):
     from . import lib, synth
     which = argv[0] if argv else "small"
     if which == "gather":
         gather_case(float(argv[1]) if len(argv) > 1 else 0.05)
+        return
+    if which == "sfc":
+        sfc_case(int(float(argv[1])) if len(argv) > 1 else 50_000_000)
         return
     mode = argv[1] if len(argv) > 1 else "batched_fp32c"
     lib.init(0)
