@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--mode", default=None, help="form timed for `value` (default: fastest built)")
     ap.add_argument("--forms", default="all", help="comma list of extra forms to time once, or none")
     ap.add_argument("--cpu-particles", type=float, default=6e7, help="CPU baseline sample size")
+    ap.add_argument("--cpu-repeats", type=int, default=3, help="CPU baseline: best of this many runs")
     ap.add_argument("--cpu-serial-particles", type=float, default=5e6,
                     help="sample size of the one-thread CPU rate (0: skip)")
     ap.add_argument("--plain-particles", type=float, default=2e7, help="plain FP64 form sample size")
@@ -673,10 +674,11 @@ def ours_arm(args, ws, rank, local):
         lists_np = host_lists(lists)
         samp = cpu_sample(n_in, args.cpu_particles)
         nthreads = os.cpu_count() or 1
-        n, dt, kind = run_cpu(params, lists_np, samp, nthreads)
+        runs = [run_cpu(params, lists_np, samp, nthreads) for _ in range(max(1, args.cpu_repeats))]
+        n, dt, kind = min(runs, key=lambda r: r[1])
         cpu = {"value": n / dt, "unit": UNIT, "cores": nthreads, "kind": kind,
                "sample": f"seeded random subset of {len(samp)} haloes / {n} particles of the workload, "
-                         f"{nthreads} OpenMP threads, {dt:.2f} s"}
+                         f"{nthreads} OpenMP threads, best of {len(runs)}: {dt:.2f} s"}
         if args.cpu_serial_particles > 0:
             # the serial build's rate (one host core), beside the threaded one
             samp1 = cpu_sample(n_in, args.cpu_serial_particles, seed=23)
@@ -697,7 +699,8 @@ def ours_arm(args, ws, rank, local):
                                f"float32 pos/vel, 64-bit ids, equal masses" + (" (two species)" if args.multimass else ""),
                    "form": mode, "n_halos": int(len(n_in)), "n_particles": N, "n_kept": int(stats.n_kept),
                    "scale": args.scale, "l2": "inputs (%.1f GB) larger than L2 (129 MB): no flush" % (N * 32 / 1e9),
-                   "parallelism": f"{ws} independent replica(s), haloes sharded by rank",
+                   "parallelism": f"{ws} rank(s), each its own full-size batch (seed + rank): haloes "
+                                  f"sharded by rank, no data-path collective",
                    "tuning": tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
