@@ -292,3 +292,44 @@ def gather_radii_reference(npart, cx, cy, cz, rvir, max_gather_rad_box: float):
     if rc != 0:
         raise RuntimeError(f"ahfref_gather_radii failed ({rc})")
     return rad, rv
+
+
+def ref_amr_path() -> str:
+    return os.path.join(HERE, "_ref", "libahfref_amr.so")
+
+
+_AMR_CHILD = r"""
+import ctypes as C, json, sys
+import numpy as np
+a = np.load(sys.argv[1])
+lib = C.CDLL(sys.argv[2])
+f = lib.ahfref_amr_levels
+f.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int]
+f.restype = C.c_int
+x, y, z = (np.ascontiguousarray(a[k], dtype=np.float32) for k in ("x", "y", "z"))
+lv = np.zeros(3 * 64, np.int64)
+ng = f(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, int(a["ngrid_dom"]), int(a["ngrid_max"]),
+       float(a["nth_dom"]), float(a["nth_ref"]), lv.ctypes.data, 64)
+print(json.dumps({"ngrids": int(ng), "levels": lv[:3 * max(ng, 0)].tolist()}))
+"""
+
+
+def amr_levels_reference(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float, nth_ref: float):
+    """The reference's own AMR hierarchy (gen_domgrids, ll, assign_npart,
+    gen_AMRhierarchy; oracle/ref_amr.c) on float positions: an (ngrids, 3)
+    int64 array of (l1dim, nodes, particles) per grid.  Runs in a child
+    process: the hierarchy lives in the reference's globals until exit."""
+    import json
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "in.npz")
+        np.savez(path, x=np.asarray(x, np.float32), y=np.asarray(y, np.float32), z=np.asarray(z, np.float32),
+                 ngrid_dom=ngrid_dom, ngrid_max=ngrid_max, nth_dom=nth_dom, nth_ref=nth_ref)
+        r = subprocess.run([sys.executable, "-c", _AMR_CHILD, path, ref_amr_path()], capture_output=True, text=True,
+                           check=True)
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    if out["ngrids"] < 1:
+        raise RuntimeError(f"ahfref_amr_levels failed ({out['ngrids']})")
+    return np.array(out["levels"], dtype=np.int64).reshape(-1, 3)

@@ -1,0 +1,91 @@
+/*
+ * ref_amr.c -- TEST INFRASTRUCTURE ONLY (oracle/_ref/libahfref_amr.so).
+ *
+ * Runs the reference's own AMR hierarchy on a snapshot given as float
+ * positions, the way src/main.c:614-648 sets it up: the domain grids
+ * (gen_domgrids, libamr_serial/generate_grids.c:24), the particles linked to
+ * the domain grid (ll, libamr_serial/lltools.c:32), their number density on
+ * it (zero_dens / assign_npart, libamr_serial/density.c), then the recursive
+ * refinement (gen_AMRhierarchy, generate_grids.c:278) under the NperDomCell /
+ * NperRefCell criteria.  All reference sources are compiled unchanged.
+ *
+ * Result per grid of the hierarchy: its nodes per dimension (l1dim), the
+ * number of nodes it holds and the number of particles assigned to it
+ * (gridls.size.no_nodes / no_part, as assign_npart leaves them).  This is the
+ * oracle of the AMR-hierarchy row; the haloes built from the hierarchy come
+ * after ahf_gridinfo and are not reported here.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "common.h"
+#include "libamr_serial/amr_serial.h"
+
+/* globals normally defined in src/common.c and src/main.c */
+info_timing   timing;
+info_global   global;
+info_io       io;
+info_ahf      ahf;
+info_energy   energy;
+info_Pk       PkSpectrum;
+info_gadget   gadget;
+param_simu    simu;
+global_io_t   global_io;
+global_info_t global_info;
+SRINDEX      *spatialRefIndex;
+int          *numIsoRef;
+int           totnumIsoRef;
+
+/* levels[3 * g + 0..2] = l1dim, no_nodes, no_part of grid g; returns the
+ * number of grids (at most max_levels reported) or a negative error */
+int ahfref_amr_levels(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom, int ngrid_max,
+                      double nth_dom, double nth_ref, int64_t *levels, int max_levels)
+{
+  FILE *log = fopen("/dev/null", "w");
+  io.logfile = log ? log : stderr;
+  partptr p = (partptr)calloc(n ? n : 1, sizeof(part));
+  if (!p) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    p[i].pos[0] = x[i];
+    p[i].pos[1] = y[i];
+    p[i].pos[2] = z[i];
+    p[i].id = (part_id_t)i;
+  }
+  simu.no_part = n;
+  simu.no_vpart = (double)n;
+  simu.NGRID_DOM = ngrid_dom;
+  simu.NGRID_MIN = ngrid_dom;
+  simu.NGRID_MAX = ngrid_max;
+  simu.Nth_dom = nth_dom;
+  simu.Nth_ref = nth_ref;
+  simu.boxsize = 1.0;
+  simu.mean_dens = 1.0;
+  global.super_t = 1.0;
+  global.fst_part = p;
+  global.no_part = n;
+  global_info.fst_part = p;
+  global_info.no_part = n;
+
+  int no_grids = 0;
+  gridls *grid_list = gen_domgrids(&no_grids);
+  ll(n, p, global.dom_grid);
+  zero_dens(global.dom_grid);
+  assign_npart(global.dom_grid);
+  global.fst_cycle = TRUE;
+  gen_AMRhierarchy(&grid_list, &no_grids);
+
+  for (int g = 0; g < no_grids && g < max_levels; g++) {
+    levels[3 * g + 0] = (int64_t)grid_list[g].l1dim;
+    levels[3 * g + 1] = (int64_t)grid_list[g].size.no_nodes;
+    levels[3 * g + 2] = (int64_t)grid_list[g].size.no_part;
+  }
+  /* the grids' quads are left to process exit: this harness runs once per
+   * process (the reference frees them only at the end of a run) */
+  free(p);
+  global.fst_part = NULL;
+  if (log) fclose(log);
+  io.logfile = NULL;
+  return no_grids;
+}

@@ -264,9 +264,28 @@ def make_radii() -> None:
     print("radii_ref", n, os.path.getsize(os.path.join(HERE, "radii_ref.npz")))
 
 
+def make_amr() -> None:
+    """The reference's own AMR hierarchy (oracle/ref_amr.c: gen_domgrids, ll,
+    assign_npart, gen_AMRhierarchy) on the cfg1 snapshot of the gather
+    fixture, for two domain grids: positions and (l1dim, nodes, particles)
+    per grid."""
+    import oracle as O
+    O.build()
+    L = synth.generate("cfg1")
+    S = synth.snapshot_from_lists(L, 20000, seed=9)
+    x, y, z = (np.asarray(v, dtype=np.float32) for v in (S.x, S.y, S.z))
+    out = {"x": x, "y": y, "z": z}
+    for tag, dom, mx in (("d16", 16, 4096), ("d32", 32, 256)):
+        out[f"levels_{tag}"] = O.amr_levels_reference(x, y, z, dom, mx, 5.0, 5.0)
+        out[f"params_{tag}"] = np.array([dom, mx, 5.0, 5.0])
+    np.savez_compressed(os.path.join(HERE, "amr_cfg1.npz"), **out)
+    print("amr_cfg1", os.path.getsize(os.path.join(HERE, "amr_cfg1.npz")))
+
+
 if __name__ == "__main__":
     main()
     make_gather()
     make_writer()
     make_sfc()
     make_radii()
+    make_amr()

@@ -1,0 +1,57 @@
+"""The AMR hierarchy (src/main.c:614-648, libamr_serial): oracle groundwork.
+
+oracle/ref_amr.c runs the reference's own gen_domgrids, ll, assign_npart
+and gen_AMRhierarchy (compiled unchanged) on float positions and reports
+each grid's nodes per dimension, node count and particle count.  The
+committed fixture tests/golden/amr_cfg1.npz holds its output on the cfg1
+snapshot for two domain grids; the live reference must reproduce it where it
+is compiled.  No GPU path of this row exists yet: these are the numbers it
+will have to meet.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIXTURE = os.path.join(HERE, "golden", "amr_cfg1.npz")
+
+
+def _oracle():
+    sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+    import oracle
+    oracle.build()
+    return oracle
+
+
+def test_fixture_levels_are_a_hierarchy():
+    d = np.load(FIXTURE)
+    n = len(d["x"])
+    for tag in ("d16", "d32"):
+        lv = d[f"levels_{tag}"]
+        dom, mx = int(d[f"params_{tag}"][0]), int(d[f"params_{tag}"][1])
+        assert lv[0, 0] == dom and lv[0, 1] == dom ** 3 and lv[0, 2] == n   # full domain grid, every particle
+        assert np.all(lv[1:, 0] == 2 * lv[:-1, 0]) and lv[-1, 0] <= mx
+        assert np.all(lv[1:, 2] <= n)
+
+
+def test_refined_levels_do_not_depend_on_the_domain_grid():
+    d = np.load(FIXTURE)
+    a, b = d["levels_d16"], d["levels_d32"]
+    common = np.intersect1d(a[1:, 0], b[1:, 0])
+    common = common[common <= 256]
+    assert len(common) >= 2
+    for l1 in common:
+        assert np.array_equal(a[a[:, 0] == l1], b[b[:, 0] == l1])
+
+
+@pytest.mark.parametrize("tag", ["d16", "d32"])
+def test_reference_reproduces_fixture(tag):
+    O = _oracle()
+    if not os.path.isfile(O.ref_amr_path()):
+        pytest.skip("reference not compiled here")
+    d = np.load(FIXTURE)
+    dom, mx, nd, nr = d[f"params_{tag}"]
+    got = O.amr_levels_reference(d["x"], d["y"], d["z"], int(dom), int(mx), float(nd), float(nr))
+    assert np.array_equal(got, d[f"levels_{tag}"])

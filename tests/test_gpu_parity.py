@@ -19,7 +19,7 @@ from make_golden import load_case
 pytestmark = pytest.mark.gpu
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith(("gather_", "writer_", "sfc_", "radii_")))   # stage cases only
+                if not os.path.basename(p).startswith(("gather_", "writer_", "sfc_", "radii_", "amr_")))   # stage cases only
 FP64_MODES = ["batched_fp64", "plain_fp64"]
 
 

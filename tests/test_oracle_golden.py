@@ -16,7 +16,7 @@ from compare import compare
 from make_golden import load_case
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz"))
-                if not os.path.basename(p).startswith(("gather_", "writer_", "sfc_", "radii_")))   # stage cases only
+                if not os.path.basename(p).startswith(("gather_", "writer_", "sfc_", "radii_", "amr_")))   # stage cases only
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
