@@ -50,6 +50,8 @@ def test_ctypes_layout_matches_c(tmp_path):
         "ahfgpu_halo": [("lambda" if f[0] == "lambda_" else f[0]) for f in abi.Halo._fields_],
         "ahfgpu_stats": [f[0] for f in abi.Stats._fields_],
         "ahfgpu_result": [f[0] for f in abi.Result._fields_],
+        "ahfgpu_particles": [f[0] for f in abi.Particles._fields_],
+        "ahfgpu_centres": [f[0] for f in abi.Centres._fields_],
     }
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for st, fields in checks.items():
@@ -62,7 +64,8 @@ def test_ctypes_layout_matches_c(tmp_path):
     subprocess.run(["gcc", "-std=c99", "-o", str(exe), str(src)], check=True)
     got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
     types = {"ahfgpu_params": abi.Params, "ahfgpu_batch": abi.Batch, "ahfgpu_halo": abi.Halo,
-             "ahfgpu_stats": abi.Stats, "ahfgpu_result": abi.Result}
+             "ahfgpu_stats": abi.Stats, "ahfgpu_result": abi.Result, "ahfgpu_particles": abi.Particles,
+             "ahfgpu_centres": abi.Centres}
     for st, ty in types.items():
         assert int(got[st]) == C.sizeof(ty), st
         for f in ty._fields_:
@@ -70,6 +73,21 @@ def test_ctypes_layout_matches_c(tmp_path):
             assert int(got[f"{st}.{cname}"]) == getattr(ty, f[0]).offset, (st, f[0])
     assert int(got["NFIELDS"]) == abi.PROF_NFIELDS
     assert abi.HALO_DTYPE.itemsize == C.sizeof(abi.Halo)
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "c99"), ("g++", "c++11")])
+def test_header_compiles_strictly(tmp_path, compiler, std):
+    """AHF is built with gcc -std=c99: the header must compile there (and in
+    C++) without a warning."""
+    import shutil
+    if not shutil.which(compiler):
+        pytest.skip(f"no {compiler}")
+    src = tmp_path / "h.c"
+    src.write_text('#include "ahfgpu.h"\nint main(void) { ahfgpu_params p; ahfgpu_batch b; ahfgpu_result r; '
+                   '(void)p; (void)b; (void)r; return ahfgpu_version() ? 0 : 1; }\n')
+    lang = ["-x", "c++"] if compiler == "g++" else []
+    subprocess.run([compiler, f"-std={std}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.dirname(HEADER), *lang, "-c", str(src), "-o", str(tmp_path / "h.o")], check=True)
 
 
 def test_calls_fail_cleanly_without_init(libpath):
