@@ -103,6 +103,34 @@ def test_calls_fail_cleanly_without_init(libpath):
     assert l.ahfgpu_version().decode().startswith("ahfgpu")
 
 
+def test_device_entry_points_refuse_before_init(libpath):
+    """Every device entry point returns AHFGPU_ERR_STATE, touching none of
+    its arguments, until ahfgpu_init has succeeded."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the library may be initialised)")
+    from ahf_gb300 import lib
+    l = lib.load()
+    out, nb = C.c_void_p(), C.c_uint64()
+    calls = {
+        "ahfgpu_construct_halos_device": lambda: l.ahfgpu_construct_halos_device(None, None, None, 2, None),
+        "ahfgpu_fetch_result": lambda: l.ahfgpu_fetch_result(None),
+        "ahfgpu_gather_device": lambda: l.ahfgpu_gather_device(None, None, None, None),
+        "ahfgpu_gather_radii_device": lambda: l.ahfgpu_gather_radii_device(5, None, None, None, None, None, 0.1,
+                                                                           None, None),
+        "ahfgpu_write_particles_device": lambda: l.ahfgpu_write_particles_device(None, None, None, 20,
+                                                                                 C.byref(out), C.byref(nb), None),
+        "ahfgpu_write_particles_bin_device": lambda: l.ahfgpu_write_particles_bin_device(None, None, 20,
+                                                                                         C.byref(out), C.byref(nb),
+                                                                                         None),
+        "ahfgpu_sfc_sort_device": lambda: l.ahfgpu_sfc_sort_device(10, None, None, None, 21, None, None, None),
+        "ahfgpu_tuning": lambda: l.ahfgpu_tuning(None, 0),
+    }
+    for name, call in calls.items():
+        assert call() == abi.AHFGPU_ERR_STATE, name
+        assert "init" in lib.last_error(), name
+
+
 def test_init_without_device_reports_no_device(libpath):
     import torch
     if torch.cuda.is_available():
