@@ -1121,3 +1121,85 @@ int ahforacle_sfc_sort(uint64_t n, const float *x, const float *y, const float *
   free(a);
   return 0;
 }
+
+
+/* ---------------------------------------------------------------------------
+ * The domain grid's TSC number density (assign_npart,
+ * src/libamr_serial/density.c:238-420, default TSC build, periodic, float
+ * node densities), the first step of the AMR hierarchy: every node starts
+ * at -mean_dens = -1 (zero_dens); the nodes are visited in z, y, x order
+ * and, within a node, its particles in linked-list order (ll() prepends, so
+ * descending input index); each particle adds masstodens w_z w_y w_x to the
+ * 27 nodes around its own (periodic), with separations d measured from the
+ * node centre (x + 1/2)/l1 in cells, wrapped through f1mod when |d| > l1/2,
+ * and TSC weights 0.75 - d^2, (1/2 - d)^2 / 2, (1/2 + d)^2 / 2.  Each
+ * addition is the reference's float += double.                            */
+static double f1mod_ref(double x) { return x >= 2.0 ? x - 2.0 : (x >= 1.0 ? x - 1.0 : x); }
+
+int ahforacle_domain_dens(uint64_t n, const float *x, const float *y, const float *z, int l1, double *dens_out)
+{
+  const size_t nn = (size_t)l1 * (size_t)l1 * (size_t)l1;
+  float *dens = (float *)malloc(nn * sizeof(float));
+  uint64_t *start = (uint64_t *)calloc(nn + 1, sizeof(uint64_t));
+  uint64_t *cell = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  uint64_t *list = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  if (!dens || !start || !cell || !list) return -1;
+  const float *pos[3] = {x, y, z};
+  for (uint64_t i = 0; i < n; i++) {
+    unsigned long c[3];
+    for (int d = 0; d < 3; d++) {
+      c[d] = (unsigned long)((double)l1 * (double)pos[d][i]);
+      if (c[d] > (unsigned long)(l1 - 1)) c[d] = 0;
+    }
+    cell[i] = ((uint64_t)c[2] * (uint64_t)l1 + c[1]) * (uint64_t)l1 + c[0];
+    start[cell[i] + 1]++;
+  }
+  for (size_t k = 0; k < nn; k++) start[k + 1] += start[k];
+  {
+    uint64_t *fill = (uint64_t *)malloc((nn ? nn : 1) * sizeof(uint64_t));
+    if (!fill) return -1;
+    memcpy(fill, start, nn * sizeof(uint64_t));
+    for (uint64_t i = n; i-- > 0;) list[fill[cell[i]]++] = i;   /* descending index within a node */
+    free(fill);
+  }
+  for (size_t k = 0; k < nn; k++) dens[k] = (float)(-1.0);
+  const double dl1 = (double)l1;
+  const double m2d = (dl1 * dl1 * dl1) / (double)n;
+  const double shift = 0.5 / dl1;
+  for (long zz = 0; zz < l1; zz++)
+    for (long yy = 0; yy < l1; yy++)
+      for (long xx = 0; xx < l1; xx++) {
+        const size_t node = ((size_t)zz * l1 + yy) * l1 + xx;
+        const long cc[3] = {xx, yy, zz};
+        double centre[3];
+        for (int d = 0; d < 3; d++) centre[d] = f1mod_ref(((double)cc[d] / dl1 + shift) + 1.0);
+        for (uint64_t s = start[node]; s < start[node + 1]; s++) {
+          const uint64_t i = list[s];
+          double w[3][3];   /* w[d][0..2]: weights of the nodes below, at, above along axis d */
+          for (int d = 0; d < 3; d++) {
+            double sep = ((double)pos[d][i] - centre[d]) * dl1;
+            if (fabs(sep) > 0.5 * dl1) {
+              const double a = f1mod_ref(((double)pos[d][i] + 0.5) + 1.0);
+              const double b = f1mod_ref((centre[d] + 0.5) + 1.0);
+              sep = (a - b) * dl1;
+            }
+            w[d][1] = 0.75 - sep * sep;
+            w[d][0] = ((0.5 - sep) * (0.5 - sep)) / 2;
+            w[d][2] = ((0.5 + sep) * (0.5 + sep)) / 2;
+          }
+          for (int k = 0; k < 3; k++)
+            for (int j = 0; j < 3; j++)
+              for (int q = 0; q < 3; q++) {
+                const size_t t = ((size_t)((zz + k - 1 + l1) % l1) * l1 + (size_t)((yy + j - 1 + l1) % l1)) * l1 +
+                                 (size_t)((xx + q - 1 + l1) % l1);
+                dens[t] += m2d * w[2][k] * w[1][j] * w[0][q];
+              }
+        }
+      }
+  for (size_t k = 0; k < nn; k++) dens_out[k] = (double)dens[k];
+  free(dens);
+  free(start);
+  free(cell);
+  free(list);
+  return 0;
+}

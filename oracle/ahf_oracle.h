@@ -62,6 +62,9 @@ uint64_t ahforacle_sfc_key(double x, double y, double z, unsigned bits);
 int  ahforacle_sfc_sort(uint64_t n, const float *x, const float *y, const float *z, unsigned bits, uint64_t *keys,
                         uint64_t *order);
 
+/* The domain grid's TSC number density (assign_npart), l1^3 nodes. */
+int  ahforacle_domain_dens(uint64_t n, const float *x, const float *y, const float *z, int l1, double *dens_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -333,3 +333,50 @@ def amr_levels_reference(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float
     if out["ngrids"] < 1:
         raise RuntimeError(f"ahfref_amr_levels failed ({out['ngrids']})")
     return np.array(out["levels"], dtype=np.int64).reshape(-1, 3)
+
+
+def domain_dens_oracle(x, y, z, l1: int):
+    """Restated TSC densities of the l1^3 domain grid (assign_npart), as an
+    (l1, l1, l1) array indexed [z, y, x]."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_domain_dens
+    fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    out = np.zeros(l1 ** 3)
+    if fn(len(a[0]), *[v.ctypes.data for v in a], int(l1), out.ctypes.data) != 0:
+        raise RuntimeError("ahforacle_domain_dens failed")
+    return out.reshape(l1, l1, l1)
+
+
+_DENS_CHILD = r"""
+import ctypes as C, sys
+import numpy as np
+a = np.load(sys.argv[1])
+lib = C.CDLL(sys.argv[2])
+f = lib.ahfref_domain_dens
+f.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_void_p]
+f.restype = C.c_int64
+x, y, z = (np.ascontiguousarray(a[k], dtype=np.float32) for k in ("x", "y", "z"))
+l1 = int(a["l1"])
+out = np.zeros(l1 ** 3)
+n = f(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, l1, out.ctypes.data)
+if n != l1 ** 3:
+    sys.exit(3)
+np.save(sys.argv[3], out)
+"""
+
+
+def domain_dens_reference(x, y, z, l1: int):
+    """The reference's own domain-grid densities after assign_npart
+    (oracle/ref_amr.c), [z, y, x]; in a child process."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "in.npz")
+        np.savez(path, x=np.asarray(x, np.float32), y=np.asarray(y, np.float32), z=np.asarray(z, np.float32), l1=l1)
+        subprocess.run([sys.executable, "-c", _DENS_CHILD, path, ref_amr_path(), os.path.join(d, "out.npy")],
+                       check=True, capture_output=True)
+        return np.load(os.path.join(d, "out.npy")).reshape(l1, l1, l1)

@@ -89,3 +89,61 @@ int ahfref_amr_levels(uint64_t n, const float *x, const float *y, const float *z
   io.logfile = NULL;
   return no_grids;
 }
+
+/* The domain grid's node densities straight after assign_npart (TSC
+ * assignment, libamr_serial/density.c:238-420), before any refinement:
+ * dens[(z * l1 + y) * l1 + x] for the ngrid_dom^3 nodes, read from the
+ * grid's quads.  Returns the number of nodes written, or a negative error. */
+int64_t ahfref_domain_dens(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom,
+                           double *dens)
+{
+  FILE *log = fopen("/dev/null", "w");
+  io.logfile = log ? log : stderr;
+  partptr p = (partptr)calloc(n ? n : 1, sizeof(part));
+  if (!p) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    p[i].pos[0] = x[i];
+    p[i].pos[1] = y[i];
+    p[i].pos[2] = z[i];
+    p[i].id = (part_id_t)i;
+  }
+  simu.no_part = n;
+  simu.no_vpart = (double)n;
+  simu.NGRID_DOM = ngrid_dom;
+  simu.NGRID_MIN = ngrid_dom;
+  simu.NGRID_MAX = ngrid_dom;
+  simu.Nth_dom = 5.0;
+  simu.Nth_ref = 5.0;
+  simu.boxsize = 1.0;
+  simu.mean_dens = 1.0;
+  global.super_t = 1.0;
+  int no_grids = 0;
+  gridls *grid_list = gen_domgrids(&no_grids);
+  gridls *g = global.dom_grid;
+  ll(n, p, g);
+  zero_dens(g);
+  assign_npart(g);
+  const long l1 = (long)g->l1dim;
+  int64_t count = 0;
+  for (pqptr pq = g->pquad; pq != NULL; pq = pq->next) {
+    long zz = pq->z;
+    for (cqptr cq = pq->loc; cq < pq->loc + pq->length; cq++, zz++)
+      for (cqptr icq = cq; icq != NULL; icq = icq->next) {
+        long yy = icq->y;
+        for (nqptr nq = icq->loc; nq < icq->loc + icq->length; nq++, yy++)
+          for (nqptr inq = nq; inq != NULL; inq = inq->next) {
+            long xx = inq->x;
+            for (nptr nd = inq->loc; nd < inq->loc + inq->length; nd++, xx++) {
+              if (zz < 0 || zz >= l1 || yy < 0 || yy >= l1 || xx < 0 || xx >= l1) return -2;
+              dens[(zz * l1 + yy) * l1 + xx] = (double)nd->dens;
+              count++;
+            }
+          }
+      }
+  }
+  (void)grid_list;
+  free(p);
+  if (log) fclose(log);
+  io.logfile = NULL;
+  return count;
+}

@@ -2,11 +2,13 @@
 
 oracle/ref_amr.c runs the reference's own gen_domgrids, ll, assign_npart
 and gen_AMRhierarchy (compiled unchanged) on float positions and reports
-each grid's nodes per dimension, node count and particle count.  The
-committed fixture tests/golden/amr_cfg1.npz holds its output on the cfg1
-snapshot for two domain grids; the live reference must reproduce it where it
-is compiled.  No GPU path of this row exists yet: these are the numbers it
-will have to meet.
+each grid's nodes per dimension, node count and particle count, and the
+domain grid's TSC densities.  The committed fixture tests/golden/amr_cfg1.npz
+holds its output on the cfg1 snapshot; the live reference must reproduce it
+where it is compiled.  The first step, the domain grid's TSC density
+(assign_npart), is restated in oracle/ahf_oracle.c and equal to the
+reference bit for bit.  No GPU path of this row exists yet: these are the
+numbers it will have to meet.
 """
 import os
 import sys
@@ -55,3 +57,32 @@ def test_reference_reproduces_fixture(tag):
     dom, mx, nd, nr = d[f"params_{tag}"]
     got = O.amr_levels_reference(d["x"], d["y"], d["z"], int(dom), int(mx), float(nd), float(nr))
     assert np.array_equal(got, d[f"levels_{tag}"])
+
+
+def test_domain_density_restatement_matches_fixture():
+    O = _oracle()
+    d = np.load(FIXTURE)
+    got = O.domain_dens_oracle(d["x"], d["y"], d["z"], 16)
+    assert np.array_equal(got, d["dens_d16"])
+    # every particle is spread over 27 nodes with weights summing to one:
+    # the grid's mean density contrast is zero up to the float sums
+    assert abs(got.mean()) < 1e-4
+
+
+@pytest.mark.parametrize("l1", [8, 32, 64])
+def test_domain_density_restatement_matches_reference_live(l1):
+    O = _oracle()
+    if not os.path.isfile(O.ref_amr_path()):
+        pytest.skip("reference not compiled here")
+    rng = np.random.default_rng(l1)
+    n = 20000
+    p = rng.random((3, n)).astype(np.float32)
+    p[:, :10] = 0.0
+    p[0, 10:20] = np.float32(1 - 2 ** -24)
+    p[1, 20:30] = 1.0                                   # folded into cell 0, as the reference does
+    p[:, 30:40] = np.float32(0.5) / l1                  # exactly on node centres
+    p[:, 40:50] = np.float32(1.0) / l1                  # exactly on cell faces
+    p[:, 1000:3000] = (0.3 + 0.02 * rng.standard_normal((3, 2000))).astype(np.float32) % np.float32(1.0)
+    a = O.domain_dens_oracle(p[0], p[1], p[2], l1)
+    b = O.domain_dens_reference(p[0], p[1], p[2], l1)
+    assert np.array_equal(a, b)
