@@ -1203,3 +1203,60 @@ int ahforacle_domain_dens(uint64_t n, const float *x, const float *y, const floa
   free(list);
   return 0;
 }
+
+
+/* The first refinement of the domain grid (gen_refgrid -> refine_grid,
+ * src/libamr_serial/generate_grids.c:126 and refine_grid.c:113-609, default
+ * build, periodic), restated as a rule on the full l1^3 domain grid: a coarse
+ * node is flagged (test_node, :113-137) when any node at dz, dy in {-1,0,1}
+ * and dx in {0,1} has density >= critdens - mean_dens, critdens = NperDomCell
+ * l1^3 / n; along x, ref_nquad's runs also cover the node after a flagged
+ * one (x - 1 flagged), wrapping at x = 0 but not at x = l1 - 1; every
+ * covered coarse node becomes 2x2x2 fine nodes (ref_cquad/ref_pquad mirror
+ * each refined row and plane); the grid is kept only with at least
+ * MIN_NNODES = 125 fine nodes (assign_npart, density.c:215).  Output: the
+ * fine nodes' (z, y, x) in ascending order; returns their number (0 when no
+ * grid is kept), -1 on allocation failure, -2 when more than max_nodes.    */
+int64_t ahforacle_first_refinement(uint64_t n, const float *x, const float *y, const float *z, int l1,
+                                   double nth_dom, int64_t *zyx, int64_t max_nodes)
+{
+  const size_t nn = (size_t)l1 * l1 * l1;
+  double *dens = (double *)malloc(nn * sizeof(double));
+  unsigned char *hit = (unsigned char *)calloc(nn, 1), *flag = (unsigned char *)calloc(nn, 1);
+  if (!dens || !hit || !flag) return -1;
+  if (ahforacle_domain_dens(n, x, y, z, l1, dens) != 0) return -1;
+  const double dl1 = (double)l1;
+  const double crit = nth_dom * ((dl1 * dl1 * dl1) / (double)n);
+  for (size_t k = 0; k < nn; k++) hit[k] = dens[k] >= crit - 1.0;
+#define NODE(zz, yy, xx) ((((size_t)(((zz) + l1) % l1)) * l1 + (size_t)(((yy) + l1) % l1)) * l1 + (size_t)(((xx) + l1) % l1))
+  for (long zz = 0; zz < l1; zz++)
+    for (long yy = 0; yy < l1; yy++)
+      for (long xx = 0; xx < l1; xx++) {
+        unsigned char f = 0;
+        for (int dz = -1; dz <= 1 && !f; dz++)
+          for (int dy = -1; dy <= 1 && !f; dy++)
+            for (int dx = 0; dx <= 1 && !f; dx++) f = hit[NODE(zz + dz, yy + dy, xx + dx)];
+        flag[NODE(zz, yy, xx)] = f;
+      }
+  int64_t count = 0;
+  for (long zz = 0; zz < l1; zz++)
+    for (int a = 0; a < 2; a++)
+      for (long yy = 0; yy < l1; yy++)
+        for (int b = 0; b < 2; b++)
+          for (long xx = 0; xx < l1; xx++) {
+            const int cov = flag[NODE(zz, yy, xx)] || (xx != l1 - 1 && flag[NODE(zz, yy, xx - 1)]);
+            if (!cov) continue;
+            for (int c = 0; c < 2; c++) {
+              if (count >= max_nodes) return -2;
+              zyx[3 * count + 0] = 2 * zz + a;
+              zyx[3 * count + 1] = 2 * yy + b;
+              zyx[3 * count + 2] = 2 * xx + c;
+              count++;
+            }
+          }
+#undef NODE
+  free(dens);
+  free(hit);
+  free(flag);
+  return count >= 125 ? count : 0;
+}

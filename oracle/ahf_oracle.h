@@ -65,6 +65,10 @@ int  ahforacle_sfc_sort(uint64_t n, const float *x, const float *y, const float 
 /* The domain grid's TSC number density (assign_npart), l1^3 nodes. */
 int  ahforacle_domain_dens(uint64_t n, const float *x, const float *y, const float *z, int l1, double *dens_out);
 
+/* The first refinement of the l1^3 domain grid: its fine nodes (z, y, x). */
+int64_t ahforacle_first_refinement(uint64_t n, const float *x, const float *y, const float *z, int l1,
+                                   double nth_dom, int64_t *zyx, int64_t max_nodes);
+
 #ifdef __cplusplus
 }
 #endif

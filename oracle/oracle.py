@@ -380,3 +380,55 @@ def domain_dens_reference(x, y, z, l1: int):
         subprocess.run([sys.executable, "-c", _DENS_CHILD, path, ref_amr_path(), os.path.join(d, "out.npy")],
                        check=True, capture_output=True)
         return np.load(os.path.join(d, "out.npy")).reshape(l1, l1, l1)
+
+
+_REF1_CHILD = r"""
+import ctypes as C, sys
+import numpy as np
+a = np.load(sys.argv[1])
+lib = C.CDLL(sys.argv[2])
+f = lib.ahfref_first_refinement
+f.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_double, C.c_double, C.c_void_p, C.c_int64]
+f.restype = C.c_int64
+x, y, z = (np.ascontiguousarray(a[k], dtype=np.float32) for k in ("x", "y", "z"))
+mx = 8 * int(a["dom"]) ** 3
+out = np.zeros(3 * mx, np.int64)
+k = f(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, int(a["dom"]), float(a["nd"]), float(a["nr"]),
+      out.ctypes.data, mx)
+if k < 0:
+    sys.exit(3)
+np.save(sys.argv[3], out[:3 * k].reshape(-1, 3))
+"""
+
+
+def first_refinement_reference(x, y, z, ngrid_dom: int, nth_dom: float, nth_ref: float):
+    """The nodes (z, y, x in fine-grid units, quad order) of the first grid
+    the reference refines from the ngrid_dom^3 domain grid (oracle/ref_amr.c);
+    in a child process."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "in.npz")
+        np.savez(path, x=np.asarray(x, np.float32), y=np.asarray(y, np.float32), z=np.asarray(z, np.float32),
+                 dom=ngrid_dom, nd=nth_dom, nr=nth_ref)
+        subprocess.run([sys.executable, "-c", _REF1_CHILD, path, ref_amr_path(), os.path.join(d, "out.npy")],
+                       check=True, capture_output=True)
+        return np.load(os.path.join(d, "out.npy"))
+
+
+def first_refinement_oracle(x, y, z, l1: int, nth_dom: float):
+    """Restated first refinement of the l1^3 domain grid: its fine nodes
+    (z, y, x), ascending; empty when no grid is kept."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_first_refinement
+    fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p, C.c_int64]
+    fn.restype = C.c_int64
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    mx = 8 * l1 ** 3
+    out = np.zeros(3 * mx, np.int64)
+    k = fn(len(a[0]), *[v.ctypes.data for v in a], int(l1), float(nth_dom), out.ctypes.data, mx)
+    if k < 0:
+        raise RuntimeError(f"ahforacle_first_refinement failed ({k})")
+    return out[:3 * k].reshape(-1, 3)

@@ -268,7 +268,8 @@ def make_amr() -> None:
     """The reference's own AMR hierarchy (oracle/ref_amr.c: gen_domgrids, ll,
     assign_npart, gen_AMRhierarchy) on the cfg1 snapshot of the gather
     fixture, for two domain grids: positions and (l1dim, nodes, particles)
-    per grid; and the 16^3 domain grid's TSC densities after assign_npart."""
+    per grid; the 16^3 domain grid's TSC densities after assign_npart; and
+    the nodes (z, y, x) of the first grid refined from the 32^3 domain grid."""
     import oracle as O
     O.build()
     L = synth.generate("cfg1")
@@ -279,6 +280,7 @@ def make_amr() -> None:
         out[f"levels_{tag}"] = O.amr_levels_reference(x, y, z, dom, mx, 5.0, 5.0)
         out[f"params_{tag}"] = np.array([dom, mx, 5.0, 5.0])
     out["dens_d16"] = O.domain_dens_reference(x, y, z, 16)   # the 16^3 domain grid after assign_npart
+    out["first_ref_d32"] = O.first_refinement_reference(x, y, z, 32, 5.0, 5.0).astype(np.int16)
     np.savez_compressed(os.path.join(HERE, "amr_cfg1.npz"), **out)
     print("amr_cfg1", os.path.getsize(os.path.join(HERE, "amr_cfg1.npz")))
 

@@ -5,9 +5,10 @@ and gen_AMRhierarchy (compiled unchanged) on float positions and reports
 each grid's nodes per dimension, node count and particle count, and the
 domain grid's TSC densities.  The committed fixture tests/golden/amr_cfg1.npz
 holds its output on the cfg1 snapshot; the live reference must reproduce it
-where it is compiled.  The first step, the domain grid's TSC density
-(assign_npart), is restated in oracle/ahf_oracle.c and equal to the
-reference bit for bit.  No GPU path of this row exists yet: these are the
+where it is compiled.  The first steps are restated in oracle/ahf_oracle.c
+and equal to the reference: the domain grid's TSC density (assign_npart),
+bit for bit, and the first refinement (gen_refgrid -> refine_grid), node
+for node and in the reference's node order.  No GPU path of this row exists yet: these are the
 numbers it will have to meet.
 """
 import os
@@ -86,3 +87,34 @@ def test_domain_density_restatement_matches_reference_live(l1):
     a = O.domain_dens_oracle(p[0], p[1], p[2], l1)
     b = O.domain_dens_reference(p[0], p[1], p[2], l1)
     assert np.array_equal(a, b)
+
+
+def test_first_refinement_restatement_matches_fixture():
+    O = _oracle()
+    d = np.load(FIXTURE)
+    got = O.first_refinement_oracle(d["x"], d["y"], d["z"], 32, 5.0)
+    assert np.array_equal(got, d["first_ref_d32"].astype(np.int64))
+    assert len(got) % 8 == 0                            # whole 2x2x2 blocks of fine nodes
+
+
+def _first_ref_cases():
+    rng = np.random.default_rng(5)
+    p = rng.random((3, 30000)).astype(np.float32)
+    p[:, :15000] = (0.97 + 0.03 * rng.standard_normal((3, 15000))).astype(np.float32) % np.float32(1.0)
+    yield "cluster across the periodic corner", p, 32
+    p = rng.random((3, 30000)).astype(np.float32)
+    yield "dense: the whole grid refines", p, 16
+    p = rng.random((3, 3000)).astype(np.float32)
+    p[:, :60] = (0.5 + 0.001 * rng.standard_normal((3, 60))).astype(np.float32)
+    yield "one small clump", p, 32
+    yield "nothing refines", rng.random((3, 3000)).astype(np.float32), 32
+
+
+def test_first_refinement_restatement_matches_reference_live():
+    O = _oracle()
+    if not os.path.isfile(O.ref_amr_path()):
+        pytest.skip("reference not compiled here")
+    for name, p, l1 in _first_ref_cases():
+        ref = O.first_refinement_reference(p[0], p[1], p[2], l1, 5.0, 5.0)
+        got = O.first_refinement_oracle(p[0], p[1], p[2], l1, 5.0)
+        assert np.array_equal(got, ref), name
