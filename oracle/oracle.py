@@ -432,3 +432,73 @@ def first_refinement_oracle(x, y, z, l1: int, nth_dom: float):
     if k < 0:
         raise RuntimeError(f"ahforacle_first_refinement failed ({k})")
     return out[:3 * k].reshape(-1, 3)
+
+
+def amr_levels_oracle(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float, nth_ref: float):
+    """Restated AMR hierarchy (oracle_amr.c): (ngrids, 3) int64 array of
+    (l1dim, nodes, particles) per grid."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_amr_levels
+    fn.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                   C.c_void_p, C.c_int]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    lv = np.zeros(3 * 40, np.int64)
+    ng = fn(len(a[0]), *[v.ctypes.data for v in a], int(ngrid_dom), int(ngrid_max), float(nth_dom), float(nth_ref),
+            lv.ctypes.data, 40)
+    if ng < 1:
+        raise RuntimeError(f"ahforacle_amr_levels failed ({ng})")
+    return lv[:3 * ng].reshape(-1, 3)
+
+
+def _amr_nodes_call(lib, name, x, y, z, dom, mx, nd, nr, level):
+    import numpy as np
+    fn = getattr(lib, name)
+    fn.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                                      C.c_void_p, C.c_void_p, C.c_int64]
+    fn.restype = C.c_int64
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    mxn = 1 << 24
+    zyx = np.zeros(3 * mxn, np.int64)
+    dens = np.zeros(mxn)
+    k = fn(len(a[0]), *[v.ctypes.data for v in a], int(dom), int(mx), float(nd), float(nr), int(level),
+           zyx.ctypes.data, dens.ctypes.data, mxn)
+    if k < 0:
+        raise RuntimeError(f"{name} failed ({k})")
+    return zyx[:3 * k].reshape(-1, 3), dens[:k]
+
+
+def amr_nodes_oracle(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, level: int):
+    """Grid `level` of the restated hierarchy: (nodes (z, y, x), densities)."""
+    return _amr_nodes_call(C.CDLL(oracle_path()), "ahforacle_amr_nodes", x, y, z, ngrid_dom, ngrid_max, nth_dom,
+                           nth_ref, level)
+
+
+_NODES_CHILD = r"""
+import ctypes as C, sys
+import numpy as np
+sys.path.insert(0, sys.argv[4])
+import oracle as O
+a = np.load(sys.argv[1])
+zyx, dens = O._amr_nodes_call(C.CDLL(sys.argv[2]), "ahfref_amr_nodes", a["x"], a["y"], a["z"], int(a["dom"]),
+                              int(a["mx"]), float(a["nd"]), float(a["nr"]), int(a["level"]))
+np.savez(sys.argv[3], zyx=zyx, dens=dens)
+"""
+
+
+def amr_nodes_reference(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, level: int):
+    """Grid `level` of the reference's own hierarchy (oracle/ref_amr.c):
+    (nodes (z, y, x) in quad order, densities); in a child process."""
+    import sys
+    import tempfile
+    import numpy as np
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "in.npz")
+        np.savez(path, x=np.asarray(x, np.float32), y=np.asarray(y, np.float32), z=np.asarray(z, np.float32),
+                 dom=ngrid_dom, mx=ngrid_max, nd=nth_dom, nr=nth_ref, level=level)
+        out = os.path.join(d, "out.npz")
+        subprocess.run([sys.executable, "-c", _NODES_CHILD, path, ref_amr_path(), out, HERE], check=True,
+                       capture_output=True)
+        r = np.load(out)
+        return r["zyx"], r["dens"]

@@ -213,3 +213,66 @@ int64_t ahfref_first_refinement(uint64_t n, const float *x, const float *y, cons
   io.logfile = NULL;
   return count;
 }
+
+/* Grid `level` of the hierarchy ahfref_amr_levels builds: its nodes in the
+ * order of its quads, zyx[3 k + 0..2], and their densities as the last
+ * assign_npart left them.  Returns the number of nodes, -3 when more than
+ * max_nodes, -4 when the hierarchy has no such grid. */
+int64_t ahfref_amr_nodes(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom, int ngrid_max,
+                         double nth_dom, double nth_ref, int level, int64_t *zyx, double *dens, int64_t max_nodes)
+{
+  FILE *log = fopen("/dev/null", "w");
+  io.logfile = log ? log : stderr;
+  partptr p = (partptr)calloc(n ? n : 1, sizeof(part));
+  if (!p) return -1;
+  for (uint64_t i = 0; i < n; i++) {
+    p[i].pos[0] = x[i];
+    p[i].pos[1] = y[i];
+    p[i].pos[2] = z[i];
+    p[i].id = (part_id_t)i;
+  }
+  simu.no_part = n;
+  simu.no_vpart = (double)n;
+  simu.NGRID_DOM = ngrid_dom;
+  simu.NGRID_MIN = ngrid_dom;
+  simu.NGRID_MAX = ngrid_max;
+  simu.Nth_dom = nth_dom;
+  simu.Nth_ref = nth_ref;
+  simu.boxsize = 1.0;
+  simu.mean_dens = 1.0;
+  global.super_t = 1.0;
+  global.fst_part = p;
+  global.no_part = n;
+  int no_grids = 0;
+  gridls *grid_list = gen_domgrids(&no_grids);
+  ll(n, p, global.dom_grid);
+  zero_dens(global.dom_grid);
+  assign_npart(global.dom_grid);
+  global.fst_cycle = TRUE;
+  gen_AMRhierarchy(&grid_list, &no_grids);
+  if (level >= no_grids) return -4;
+  gridls *g = grid_list + level;
+  int64_t count = 0;
+  for (pqptr pq = g->pquad; pq != NULL; pq = pq->next) {
+    long zz = pq->z;
+    for (cqptr cq = pq->loc; cq < pq->loc + pq->length; cq++, zz++)
+      for (cqptr icq = cq; icq != NULL; icq = icq->next) {
+        long yy = icq->y;
+        for (nqptr nq = icq->loc; nq < icq->loc + icq->length; nq++, yy++)
+          for (nqptr inq = nq; inq != NULL; inq = inq->next) {
+            long xx = inq->x;
+            for (nptr nd = inq->loc; nd < inq->loc + inq->length; nd++, xx++) {
+              if (count >= max_nodes) return -3;
+              zyx[3 * count + 0] = zz;
+              zyx[3 * count + 1] = yy;
+              zyx[3 * count + 2] = xx;
+              dens[count] = (double)nd->dens;
+              count++;
+            }
+          }
+      }
+  }
+  if (log) fclose(log);
+  io.logfile = NULL;
+  return count;
+}

@@ -264,6 +264,14 @@ def make_radii() -> None:
     print("radii_ref", n, os.path.getsize(os.path.join(HERE, "radii_ref.npz")))
 
 
+def amr_digest(zyx, dens) -> int:
+    """First 8 bytes of the SHA-256 of a grid's nodes (int64 z, y, x) and
+    densities (float64 of the float values)."""
+    import hashlib
+    h = hashlib.sha256(np.ascontiguousarray(zyx, np.int64).tobytes() + np.ascontiguousarray(dens, np.float64).tobytes())
+    return int.from_bytes(h.digest()[:8], "little")
+
+
 def make_amr() -> None:
     """The reference's own AMR hierarchy (oracle/ref_amr.c: gen_domgrids, ll,
     assign_npart, gen_AMRhierarchy) on the cfg1 snapshot of the gather
@@ -281,6 +289,10 @@ def make_amr() -> None:
         out[f"params_{tag}"] = np.array([dom, mx, 5.0, 5.0])
     out["dens_d16"] = O.domain_dens_reference(x, y, z, 16)   # the 16^3 domain grid after assign_npart
     out["first_ref_d32"] = O.first_refinement_reference(x, y, z, 32, 5.0, 5.0).astype(np.int16)
+    # every grid of the 16^3-domain hierarchy: a digest of its nodes (quad
+    # order) and float densities
+    out["level_digest_d16"] = np.array([amr_digest(*O.amr_nodes_reference(x, y, z, 16, 4096, 5.0, 5.0, lev))
+                                        for lev in range(len(out["levels_d16"]))], dtype=np.uint64)
     np.savez_compressed(os.path.join(HERE, "amr_cfg1.npz"), **out)
     print("amr_cfg1", os.path.getsize(os.path.join(HERE, "amr_cfg1.npz")))
 

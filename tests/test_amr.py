@@ -5,10 +5,12 @@ and gen_AMRhierarchy (compiled unchanged) on float positions and reports
 each grid's nodes per dimension, node count and particle count, and the
 domain grid's TSC densities.  The committed fixture tests/golden/amr_cfg1.npz
 holds its output on the cfg1 snapshot; the live reference must reproduce it
-where it is compiled.  The first steps are restated in oracle/ahf_oracle.c
-and equal to the reference: the domain grid's TSC density (assign_npart),
-bit for bit, and the first refinement (gen_refgrid -> refine_grid), node
-for node and in the reference's node order.  No GPU path of this row exists yet: these are the
+where it is compiled.  The hierarchy is restated in oracle/oracle_amr.c
+(runs, segment-local neighbours, the refinement state machines, relink and
+assign_npart in the reference's list order) and equal to the reference on
+every grid: nodes in the reference's order and float densities bit for bit.
+The domain grid's TSC density and the first refinement are also restated on
+their own in oracle/ahf_oracle.c (a direct density sum and a stencil rule).  No GPU path of this row exists yet: these are the
 numbers it will have to meet.
 """
 import os
@@ -118,3 +120,48 @@ def test_first_refinement_restatement_matches_reference_live():
         ref = O.first_refinement_reference(p[0], p[1], p[2], l1, 5.0, 5.0)
         got = O.first_refinement_oracle(p[0], p[1], p[2], l1, 5.0)
         assert np.array_equal(got, ref), name
+
+
+def _digest(zyx, dens):
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import amr_digest
+    return amr_digest(zyx, dens)
+
+
+@pytest.mark.parametrize("tag", ["d16", "d32"])
+def test_hierarchy_restatement_matches_fixture_counts(tag):
+    O = _oracle()
+    d = np.load(FIXTURE)
+    dom, mx, nd, nr = d[f"params_{tag}"]
+    got = O.amr_levels_oracle(d["x"], d["y"], d["z"], int(dom), int(mx), float(nd), float(nr))
+    assert np.array_equal(got, d[f"levels_{tag}"])
+
+
+def test_hierarchy_restatement_matches_fixture_every_grid():
+    """Nodes (in order) and float densities of all nine grids, 16^3 to 4096^3."""
+    O = _oracle()
+    d = np.load(FIXTURE)
+    want = d["level_digest_d16"]
+    for lev in range(len(want)):
+        assert _digest(*O.amr_nodes_oracle(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0, lev)) == int(want[lev]), lev
+
+
+def test_hierarchy_restatement_matches_reference_live():
+    """Three clusters, two across periodic faces: every grid equal."""
+    O = _oracle()
+    if not os.path.isfile(O.ref_amr_path()):
+        pytest.skip("reference not compiled here")
+    rng = np.random.default_rng(11)
+    n = 40000
+    p = rng.random((3, n)).astype(np.float32)
+    for k, c in enumerate([(0.98, 0.01, 0.5), (0.5, 0.99, 0.02), (0.3, 0.3, 0.3)]):
+        m = slice(k * 8000, (k + 1) * 8000)
+        p[:, m] = ((np.array(c)[:, None] + 0.01 * rng.standard_normal((3, 8000)) * (1 + rng.random(8000)))
+                   % 1.0).astype(np.float32)
+    lv = O.amr_levels_reference(p[0], p[1], p[2], 32, 2048, 5.0, 5.0)
+    assert len(lv) >= 4
+    assert np.array_equal(O.amr_levels_oracle(p[0], p[1], p[2], 32, 2048, 5.0, 5.0), lv)
+    for lev in range(len(lv)):
+        a = O.amr_nodes_oracle(p[0], p[1], p[2], 32, 2048, 5.0, 5.0, lev)
+        b = O.amr_nodes_reference(p[0], p[1], p[2], 32, 2048, 5.0, 5.0, lev)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), lev
