@@ -502,3 +502,16 @@ def amr_nodes_reference(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, level: 
                        capture_output=True)
         r = np.load(out)
         return r["zyx"], r["dens"]
+
+
+def amr_list_order_violations(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref) -> int:
+    """Out-of-order pairs in the restated hierarchy's particle lists against
+    index order, descending on even grids and ascending on odd ones."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_amr_list_order_violations
+    fn.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.c_double]
+    fn.restype = C.c_int64
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    return int(fn(len(a[0]), *[v.ctypes.data for v in a], int(ngrid_dom), int(ngrid_max), float(nth_dom),
+                  float(nth_ref)))

@@ -553,7 +553,8 @@ static int64_t assign_npart(grid_t *g, const float *pos[3], const int64_t *next,
 #define MAX_GRIDS 40
 
 static int build_hierarchy(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom, int ngrid_max,
-                           double nth_dom, double nth_ref, grid_t *grids, int64_t *levels, int max_levels)
+                           double nth_dom, double nth_ref, grid_t *grids, int64_t *levels, int max_levels,
+                           int64_t **next_out)
 {
   const float *pos[3] = {x, y, z};
   const int64_t L = ngrid_dom;
@@ -613,7 +614,8 @@ static int build_hierarchy(uint64_t n, const float *x, const float *y, const flo
     m2d = m2f;
     thr = nth_ref * m2d - 1.0;
   }
-  free(next);
+  if (next_out) *next_out = next;
+  else free(next);
   return ng;
 }
 
@@ -621,7 +623,7 @@ int ahforacle_amr_levels(uint64_t n, const float *x, const float *y, const float
                          int ngrid_max, double nth_dom, double nth_ref, int64_t *levels, int max_levels)
 {
   grid_t grids[MAX_GRIDS];
-  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, levels, max_levels);
+  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, levels, max_levels, NULL);
   for (int g = 0; g < ng; g++) grid_free(&grids[g]);
   return ng;
 }
@@ -635,7 +637,7 @@ int64_t ahforacle_amr_nodes(uint64_t n, const float *x, const float *y, const fl
 {
   grid_t grids[MAX_GRIDS];
   int64_t lv[3 * MAX_GRIDS];
-  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, lv, MAX_GRIDS);
+  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, lv, MAX_GRIDS, NULL);
   int64_t count = level < ng ? 0 : -4;
   if (level < ng) {
     const grid_t *g = &grids[level];
@@ -650,4 +652,33 @@ int64_t ahforacle_amr_nodes(uint64_t n, const float *x, const float *y, const fl
   }
   for (int g = 0; g < ng; g++) grid_free(&grids[g]);
   return count;
+}
+
+
+/* Checks a property of the hierarchy a GPU version can build on: each
+ * node's particle list is in input-index order, descending on grids 0, 2,
+ * 4, ... and ascending on grids 1, 3, ... (ll prepends in index order;
+ * relink reverses the matches it moves).  Each grid is checked as the finest
+ * of a hierarchy stopped there, before another relink takes particles from
+ * it.  Returns the number of out-of-order pairs over all grids, or -1. */
+int64_t ahforacle_amr_list_order_violations(uint64_t n, const float *x, const float *y, const float *z,
+                                            int ngrid_dom, int ngrid_max, double nth_dom, double nth_ref)
+{
+  grid_t grids[MAX_GRIDS];
+  int64_t lv[3 * MAX_GRIDS], bad = 0;
+  for (int level = 0; level < MAX_GRIDS && ((int64_t)ngrid_dom << level) <= ngrid_max; level++) {
+    int64_t *next = NULL;
+    const int ng = build_hierarchy(n, x, y, z, ngrid_dom, (int)((int64_t)ngrid_dom << level), nth_dom, nth_ref,
+                                   grids, lv, MAX_GRIDS, &next);
+    if (ng < 0) return -1;
+    const grid_t *g = &grids[ng - 1];
+    const int desc = ((ng - 1) % 2) == 0;
+    for (int64_t i = 0; i < g->nnodes; i++)
+      for (int64_t p = g->head[i]; p >= 0 && next[p] >= 0; p = next[p])
+        if (desc ? !(p > next[p]) : !(p < next[p])) bad++;
+    for (int k = 0; k < ng; k++) grid_free(&grids[k]);
+    free(next);
+    if (ng - 1 < level) break;   /* the hierarchy stopped earlier */
+  }
+  return bad;
 }

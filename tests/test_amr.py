@@ -165,3 +165,14 @@ def test_hierarchy_restatement_matches_reference_live():
         a = O.amr_nodes_oracle(p[0], p[1], p[2], 32, 2048, 5.0, 5.0, lev)
         b = O.amr_nodes_reference(p[0], p[1], p[2], 32, 2048, 5.0, 5.0, lev)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), lev
+
+
+def test_particle_lists_are_in_index_order_by_level():
+    """ll prepends in index order and relink reverses the particles it
+    moves, so on every grid each node's list is in index order, descending
+    on even grids and ascending on odd ones: a node's density is then a sum
+    over its source nodes in node order, each in index order, which a GPU
+    gather can reproduce exactly."""
+    O = _oracle()
+    d = np.load(FIXTURE)
+    assert O.amr_list_order_violations(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0) == 0
