@@ -143,7 +143,10 @@ def test_hierarchy_restatement_matches_fixture_every_grid():
     d = np.load(FIXTURE)
     want = d["level_digest_d16"]
     for lev in range(len(want)):
-        assert _digest(*O.amr_nodes_oracle(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0, lev)) == int(want[lev]), lev
+        zyx, dens = O.amr_nodes_oracle(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0, lev)
+        assert _digest(zyx, dens) == int(want[lev]), lev
+        key = (zyx[:, 0] * 8192 + zyx[:, 1]) * 8192 + zyx[:, 2]
+        assert np.all(np.diff(key) > 0), lev            # the reference's node order is ascending (z, y, x)
 
 
 def test_hierarchy_restatement_matches_reference_live():
