@@ -74,6 +74,8 @@ int  ahforacle_amr_levels(uint64_t n, const float *x, const float *y, const floa
                           int ngrid_max, double nth_dom, double nth_ref, int64_t *levels, int max_levels);
 int64_t ahforacle_amr_list_order_violations(uint64_t n, const float *x, const float *y, const float *z,
                                             int ngrid_dom, int ngrid_max, double nth_dom, double nth_ref);
+int64_t ahforacle_amr_gather_mismatches(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom,
+                                        int ngrid_max, double nth_dom, double nth_ref);
 int64_t ahforacle_amr_nodes(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom,
                             int ngrid_max, double nth_dom, double nth_ref, int level, int64_t *zyx, double *dens,
                             int64_t max_nodes);

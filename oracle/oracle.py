@@ -515,3 +515,17 @@ def amr_list_order_violations(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref) -
     a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
     return int(fn(len(a[0]), *[v.ctypes.data for v in a], int(ngrid_dom), int(ngrid_max), float(nth_dom),
                   float(nth_ref)))
+
+
+def amr_gather_mismatches(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref) -> int:
+    """Nodes, over all grids of the restated hierarchy, whose density
+    computed as a gather (targets in order, sources in node order, particles
+    in list order) differs from the reference-ordered scatter."""
+    import numpy as np
+    lib = C.CDLL(oracle_path())
+    fn = lib.ahforacle_amr_gather_mismatches
+    fn.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.c_double]
+    fn.restype = C.c_int64
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    return int(fn(len(a[0]), *[v.ctypes.data for v in a], int(ngrid_dom), int(ngrid_max), float(nth_dom),
+                  float(nth_ref)))

@@ -540,6 +540,68 @@ static int64_t assign_npart(grid_t *g, const float *pos[3], const int64_t *next,
   return np;
 }
 
+/* The same densities as a gather (the formulation a GPU kernel can use
+ * without atomics): the (target, source, stencil slot) pairs of every
+ * source's TSC nodes, ordered by target and then source (stable in slot);
+ * each target starts at -mean_dens and adds, source by source in node
+ * order, each source particle's weight in list order.  Float additions in
+ * the same order as assign_npart's scatter, so the result is identical;
+ * returns the number of nodes whose density differs from g->dens. */
+typedef struct { int64_t t, s; int slot; } tpair_t;
+
+static int cmp_tpair(const void *a, const void *b)
+{
+  const tpair_t *p = a, *q = b;
+  if (p->t != q->t) return p->t < q->t ? -1 : 1;
+  if (p->s != q->s) return p->s < q->s ? -1 : 1;
+  return p->slot - q->slot;
+}
+
+static int64_t gather_mismatch(const grid_t *g, const float *pos[3], const int64_t *next, double m2d)
+{
+  const double l1 = (double)g->l1, shift = 0.5 / l1;
+  tpair_t *pr = malloc((size_t)(g->nnodes ? g->nnodes : 1) * 27 * sizeof(tpair_t));
+  float *out = malloc((size_t)(g->nnodes ? g->nnodes : 1) * sizeof(float));
+  if (!pr || !out) return -1;
+  int64_t np = 0;
+  for (int64_t s = 0; s < g->nnodes; s++) {
+    if (g->head[s] < 0) continue;
+    int64_t t[3][3][3];
+    tsc_nodes(g, s, t);
+    for (int k = 0; k < 27; k++)
+      if (t[k / 9][(k / 3) % 3][k % 3] >= 0) { pr[np].t = t[k / 9][(k / 3) % 3][k % 3]; pr[np].s = s; pr[np].slot = k; np++; }
+  }
+  qsort(pr, (size_t)np, sizeof(tpair_t), cmp_tpair);
+  for (int64_t i = 0; i < g->nnodes; i++) out[i] = (float)(-1.0);
+  for (int64_t e = 0; e < np; e++) {
+    const int64_t s = pr[e].s, tt = pr[e].t;
+    const int k = pr[e].slot / 9, j = (pr[e].slot / 3) % 3, q = pr[e].slot % 3;
+    const int64_t cc[3] = {g->nx[s], g->ny[s], g->nz[s]};
+    double centre[3];
+    for (int d = 0; d < 3; d++) centre[d] = f1mod_amr(((double)cc[d] / l1 + shift) + 1.0);
+    for (int64_t p = g->head[s]; p >= 0; p = next[p]) {
+      double w[3][3];
+      for (int d = 0; d < 3; d++) {
+        double sep = ((double)pos[d][p] - centre[d]) * l1;
+        if (fabs(sep) > 0.5 * l1) {
+          const double a = f1mod_amr(((double)pos[d][p] + 0.5) + 1.0);
+          const double b = f1mod_amr((centre[d] + 0.5) + 1.0);
+          sep = (a - b) * l1;
+        }
+        w[d][1] = 0.75 - sep * sep;
+        w[d][0] = ((0.5 - sep) * (0.5 - sep)) / 2;
+        w[d][2] = ((0.5 + sep) * (0.5 + sep)) / 2;
+      }
+      out[tt] += m2d * w[2][k] * w[1][j] * w[0][q];
+    }
+  }
+  int64_t bad = 0;
+  for (int64_t i = 0; i < g->nnodes; i++) bad += memcmp(&out[i], &g->dens[i], sizeof(float)) != 0;
+  free(pr);
+  free(out);
+  return bad;
+}
+
 /* The hierarchy (main.c:614-648, gen_AMRhierarchy): the ngrid_dom^3 domain
  * grid (one run per plane, row and node line), particles linked to it by ll
  * (cell trunc(l1 x), a cell index above l1 - 1 folded to 0; each particle
@@ -551,6 +613,8 @@ static int64_t assign_npart(grid_t *g, const float *pos[3], const int64_t *next,
  * levels[3 g + 0..2] = nodes per dimension, nodes, particles assigned of
  * grid g; returns the number of grids (at most max_levels reported), or -1. */
 #define MAX_GRIDS 40
+
+static int64_t *g_gather_check;   /* when set: gather-vs-scatter mismatches, summed over grids */
 
 static int build_hierarchy(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom, int ngrid_max,
                            double nth_dom, double nth_ref, grid_t *grids, int64_t *levels, int max_levels,
@@ -596,6 +660,7 @@ static int build_hierarchy(uint64_t n, const float *x, const float *y, const flo
   const double dl = (double)L;
   double m2d = (dl * dl * dl) / (double)n;
   int64_t np = assign_npart(d, pos, next, m2d);
+  if (g_gather_check) *g_gather_check += gather_mismatch(d, pos, next, m2d);
   int ng = 1;
   if (max_levels > 0) { levels[0] = L; levels[1] = d->nnodes; levels[2] = np; }
   double thr = nth_dom * m2d - 1.0;
@@ -608,6 +673,7 @@ static int build_hierarchy(uint64_t n, const float *x, const float *y, const flo
     relink(c, f, pos, next);
     const double m2f = m2d * 8.0;
     np = assign_npart(f, pos, next, m2f);
+    if (g_gather_check) *g_gather_check += gather_mismatch(f, pos, next, m2f);
     if (f->nnodes < 125) { grid_free(f); break; }
     if (ng < max_levels) { levels[3 * ng] = f->l1; levels[3 * ng + 1] = f->nnodes; levels[3 * ng + 2] = np; }
     ng++;
@@ -681,4 +747,20 @@ int64_t ahforacle_amr_list_order_violations(uint64_t n, const float *x, const fl
     if (ng - 1 < level) break;   /* the hierarchy stopped earlier */
   }
   return bad;
+}
+
+
+/* Builds the hierarchy and recomputes every grid's densities in the gather
+ * formulation (gather_mismatch); returns the number of nodes, over all
+ * grids, whose gathered density differs from the scattered one, or -1. */
+int64_t ahforacle_amr_gather_mismatches(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom,
+                                        int ngrid_max, double nth_dom, double nth_ref)
+{
+  grid_t grids[MAX_GRIDS];
+  int64_t lv[3 * MAX_GRIDS], bad = 0;
+  g_gather_check = &bad;
+  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, lv, MAX_GRIDS, NULL);
+  g_gather_check = NULL;
+  for (int k = 0; k < ng; k++) grid_free(&grids[k]);
+  return ng < 0 ? -1 : bad;
 }

@@ -179,3 +179,12 @@ def test_particle_lists_are_in_index_order_by_level():
     O = _oracle()
     d = np.load(FIXTURE)
     assert O.amr_list_order_violations(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0) == 0
+
+
+def test_densities_as_a_gather_equal_the_scatter():
+    """The formulation a GPU kernel can use without atomics — each node sums
+    its source nodes in node order, each source's particles in list order —
+    gives every grid's float densities bit for bit."""
+    O = _oracle()
+    d = np.load(FIXTURE)
+    assert O.amr_gather_mismatches(d["x"], d["y"], d["z"], 16, 4096, 5.0, 5.0) == 0
