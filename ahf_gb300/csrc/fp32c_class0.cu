@@ -3,17 +3,11 @@
 // translation unit per class so the classes compile in parallel.
 #include "halo_fp32c.cuh"
 
-#ifndef AHFGPU_CLASS0_T
-#define AHFGPU_CLASS0_T 64
-#endif
-#ifndef AHFGPU_CLASS0_MINB
-#define AHFGPU_CLASS0_MINB 1
-#endif
-
 namespace ahfgpu {
 
-constexpr int kT0 = AHFGPU_CLASS0_T;
-constexpr int kMinB0 = AHFGPU_CLASS0_MINB;
+// the only CTA shape built for class 0: 64 threads, no register cap
+constexpr int kT0 = 64;
+constexpr int kMinB0 = 1;
 using SS0 = SortSmemT<512, 16>;
 
 void launch_fp32c_class0(const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st) {

@@ -2,13 +2,12 @@
 // every byte of work space taken from one file-scope device array, for
 // callers that must not allocate device memory.
 //
-// Who cannot allocate: code that runs where cudaMalloc is unavailable or
-// forbidden -- inside a CUDA-graph capture of a larger pipeline, under a
-// memory pool that the host application owns and partitions up front, or in
-// an embedding (e.g. a plugin loaded into a running simulation) whose device
-// memory budget is fixed before AHF's analysis starts.  They pass device
-// pointers for the inputs and the outputs; this entry point allocates
-// nothing (no cudaMalloc/cudaFree, no allocating library call).
+// Who cannot allocate: an application that hands AHF's analysis a fixed
+// device-memory budget and partitions the GPU's memory itself up front (a
+// memory pool that the host owns), or a plugin loaded into a running
+// simulation that may not call cudaMalloc/cudaFree behind its host's back.
+// They pass device pointers for the inputs and the outputs; this entry point
+// allocates nothing (no cudaMalloc/cudaFree, no allocating library call).
 //
 // Limits (compile-time): at most AHFGPU_NOALLOC_MAX_PARTICLES list entries
 // and AHFGPU_NOALLOC_MAX_HALOS haloes per call, profile rows at a fixed
@@ -17,13 +16,17 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and fills its constant
-// parts (identity work queue, profile row offsets).  That first call must
+// parts (identity work queue, profile row offsets).  That first call should
 // come before any stream capture.  Every later call on the device reuses the
 // array, which keeps the previous call's contents; the per-call counters,
-// queue head and error word are cleared at the start of each call.  Calls
-// that overlap on the GPU (different streams or host threads) share the
-// array and race: serialise them.
+// queue head, weight range and error word are cleared at the start of each
+// call.  Calls that overlap on the GPU (different streams or host threads)
+// share the array and race: serialise them.  Each call waits for its stream
+// three times: it reads the entry count off[nhalo], the batch checks and the
+// device error word back to the host.
+#include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -103,12 +106,18 @@ __global__ void na_init_constants(int32_t* queue, uint64_t* prof_off) {
 }
 
 // batch checks on the device: offsets monotone from 0, weights positive and
-// finite, and the weight range (exactness of FP64 mass prefixes)
-__global__ void na_check(const uint64_t* off, int64_t nh, const float* w, uint64_t n, int* err, float* wred) {
+// finite, the weight range and the largest list (exactness of FP64 mass
+// prefixes)
+__global__ void na_check(const uint64_t* off, int64_t nh, const float* w, uint64_t n, int* err, float* wred,
+                         unsigned long long* maxn) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t h = t; h < nh; h += stride)
+  unsigned long long longest = 0;
+  for (int64_t h = t; h < nh; h += stride) {
     if (off[h + 1] < off[h]) atomicExch(&err[1], 1);
+    else if (off[h + 1] - off[h] > longest) longest = off[h + 1] - off[h];
+  }
+  if (longest) atomicMax(maxn, longest);
   if (t == 0 && off[0] != 0) atomicExch(&err[1], 1);
   if (!w) return;
   float mn = INFINITY, mx = 0.f;
@@ -123,11 +132,12 @@ __global__ void na_check(const uint64_t* off, int64_t nh, const float* w, uint64
   if (bad) atomicExch(&err[2], 1);
 }
 
-__global__ void na_clear(int* err, unsigned* qhead, unsigned long long* counters, float* wred) {
+__global__ void na_clear(int* err, unsigned* qhead, unsigned long long* counters, float* wred,
+                         unsigned long long* maxn) {
   int t = threadIdx.x;
   if (t < 16) { err[t] = 0; qhead[t] = 0; }
   if (t < 8) counters[t] = 0;
-  if (t == 0) { wred[0] = INFINITY; wred[1] = 0.f; }
+  if (t == 0) { wred[0] = INFINITY; wred[1] = 0.f; *maxn = 0; }
 }
 
 // set-up of the current device (once): symbol address + constant parts
@@ -186,18 +196,21 @@ extern "C" AHFGPU_API int ahfgpu_construct_halos_noalloc(const ahfgpu_params* pr
   float* wred = (float*)(b + oWred);
   unsigned* qhead = (unsigned*)(b + oQhead);
   unsigned long long* counters = (unsigned long long*)(b + oCounters);
+  unsigned long long* maxn = (unsigned long long*)(b + oWred + 8);
   // entry count, then the batch checks
   uint64_t N = 0;
   if (cudaMemcpyAsync(&N, db->off + nh, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return na_fail(AHFGPU_ERR_CUDA, "reading off[nhalo] failed");
   if (N > kNaN) return na_fail(AHFGPU_ERR_CAPACITY, "off[nhalo] exceeds AHFGPU_NOALLOC_MAX_PARTICLES");
-  na_clear<<<1, 32, 0, st>>>(err, qhead, counters, wred);
-  na_check<<<s->nsm, 256, 0, st>>>(db->off, nh, db->w, N, err, wred);
+  na_clear<<<1, 32, 0, st>>>(err, qhead, counters, wred, maxn);
+  na_check<<<s->nsm, 256, 0, st>>>(db->off, nh, db->w, N, err, wred, maxn);
   int herr[3] = {0, 0, 0};
   float hw[2] = {0.f, 0.f};
+  unsigned long long hmaxn = 0;
   if (cudaMemcpyAsync(herr, err, 12, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaMemcpyAsync(hw, wred, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&hmaxn, maxn, 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return na_fail(AHFGPU_ERR_CUDA, "batch check failed");
   if (herr[1]) return na_fail(AHFGPU_ERR_INVALID, "off must start at 0 and be monotone");
@@ -215,14 +228,11 @@ extern "C" AHFGPU_API int ahfgpu_construct_halos_noalloc(const ahfgpu_params* pr
   P.f_ovlim = (float)prm->ovlim;
   P.f_rvrf = (float)(prm->rho_vir / prm->rho_fac);
   if (db->w) {
-    // FP64 mass prefixes are exact when all partial sums stay below 2^52
-    // quanta of the lightest weight; otherwise every halo is replayed
-    // serially in the reference's order
-    int e = 0;
-    double wmin = (double)hw[0];
-    frexp(wmin, &e);
-    double q = ldexp(1.0, e - 24);
-    if (!((double)N * (double)hw[1] / q < 4503599627370496.0)) P.force_serial = 1;
+    // FP64 mass prefixes are exact when every partial sum of the longest
+    // list stays below 2^52 quanta of the lightest weight; otherwise every
+    // halo is replayed serially in the reference's order
+    double q = ldexp(1.0, ilogb((double)hw[0]) - 23);
+    if (!((double)hmaxn * (double)hw[1] / q < 4503599627370496.0)) P.force_serial = 1;
   }
   DevBatch B{};
   B.nhalo = nh;
@@ -263,7 +273,13 @@ extern "C" AHFGPU_API int ahfgpu_construct_halos_noalloc(const ahfgpu_params* pr
   if (cudaMemcpyAsync(&derr, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return na_fail(AHFGPU_ERR_CUDA, "device error after the halo kernel");
-  if (derr) return na_fail(AHFGPU_ERR_CAPACITY, "radial sort worklist overflow");
+  if (derr == kErrWorklist) return na_fail(AHFGPU_ERR_CAPACITY, "radial sort worklist overflow");
+  if (derr == kErrSortState) return na_fail(AHFGPU_ERR_CUDA, "radial sort: inconsistent bucket run (self-check)");
+  if (derr) {
+    char msg[64];
+    snprintf(msg, sizeof msg, "device error code %d", derr);
+    return na_fail(AHFGPU_ERR_CUDA, msg);
+  }
   return AHFGPU_OK;
 }
 

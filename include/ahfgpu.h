@@ -91,8 +91,9 @@ typedef struct {
  * in [0,1), velocities are AHF internal momenta (struct particle .pos/.mom,
  * src/tdef.h:36-77).  w is the MULTIMASS weight (NULL = all 1.0, the default
  * build).  gidx is the particle's index in global.fst_part and is what the
- * kept list returns (NULL = return the entry index inside the batch).  id is
- * optional and only carried through.  cx/cy/cz are HALO.pos.               */
+ * kept list returns (NULL = return the entry index inside the batch); the
+ * particle ids stay with the caller, who maps the returned indices to them
+ * (AHF writes fst_part[ipart].id).  cx/cy/cz are HALO.pos.                 */
 typedef struct {
   int64_t         nhalo;
   const uint64_t *off;                    /* [nhalo+1], off[0] == 0        */
@@ -295,19 +296,23 @@ AHFGPU_API int ahfgpu_tuning(char *buf, size_t len);
 
 /* ---- no-allocation variant ----------------------------------------------
  * No counterpart in the reference (AHF has no GPU path).  For callers that
- * cannot allocate device memory (a CUDA-graph capture of a larger pipeline,
- * a host-owned pre-partitioned memory pool, a plugin with a fixed device
- * budget): the batched FP64 stage with every byte of work space taken from
- * one static device array of about 16 MB that each GPU loading the library
- * holds until exit.  All pointers are device pointers; the batch is as for
+ * cannot allocate device memory: an application that gives AHF's analysis a
+ * fixed device budget and partitions the GPU's memory itself, or a plugin
+ * inside a running simulation that may not call cudaMalloc/cudaFree.  The
+ * batched FP64 stage with every byte of work space taken from one static
+ * device array of about 16 MB that each GPU loading the library holds until
+ * exit.  All pointers are device pointers; the batch is as for
  * ahfgpu_construct_halos_device; nothing is allocated.
  * Outputs (caller-owned): out_halo[nhalo]; halo h's kept list in radial order
  * at out_member[off[h] .. off[h] + out_halo[h].npart) (out_member has
  * off[nhalo] entries); profile rows of halo h at
  * out_prof[(h * AHFGPU_NOALLOC_MAX_BINS + b) * AHFGPU_PROF_NFIELDS + f].
  * Larger batches return AHFGPU_ERR_CAPACITY.  The first call on a device
- * sets the array up and must precede any stream capture; calls that overlap
- * on the GPU share the array and race.  stream: cudaStream_t or NULL. */
+ * sets the array up (cudaGetSymbolAddress, with that device current) and
+ * should come before any stream capture.  Each call waits for `stream` (it
+ * reads the entry count, the batch checks and the error word back).  Calls
+ * that overlap on the GPU share the array and race: serialise them.
+ * stream: cudaStream_t or NULL. */
 #define AHFGPU_NOALLOC_MAX_PARTICLES 131072
 #define AHFGPU_NOALLOC_MAX_HALOS     8192
 #define AHFGPU_NOALLOC_MAX_BINS      64

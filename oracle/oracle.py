@@ -23,14 +23,52 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _LIBS: dict = {}
 
 
+REPO = os.path.dirname(HERE)
+# The reference's sources as a build input for machines without the AHF tree:
+# a git-ignored mirror of its src/ directory, refreshed whenever the tree is
+# present.  Nothing of it is committed; it only lets the same recipe compile
+# the reference's own routines where the tree itself is absent.
+REF_MIRROR = os.path.join(REPO, "baseline", "_ref")
+
+
+def _mirror_reference(refdir: str) -> None:
+    import shutil
+    src = os.path.join(refdir, "src")
+    dst = os.path.join(REF_MIRROR, "src")
+    for root, _dirs, files in os.walk(src):
+        rel = os.path.relpath(root, src)
+        os.makedirs(os.path.join(dst, rel), exist_ok=True)
+        for f in files:
+            if not f.endswith((".c", ".h")):
+                continue
+            a, b = os.path.join(root, f), os.path.join(dst, rel, f)
+            if not os.path.exists(b) or os.path.getmtime(b) < os.path.getmtime(a):
+                shutil.copy2(a, b)
+
+
+def reference_tree() -> str | None:
+    """The AHF source tree to compile the reference from: $AHF_REFERENCE, the
+    reference checkout, or the git-ignored mirror of it (refreshed from the
+    checkout when that is present)."""
+    env = os.environ.get("AHF_REFERENCE")
+    if env:
+        return env if os.path.isfile(os.path.join(env, "src/libahf/ahf_halos.c")) else None
+    if os.path.isfile("/root/reference/src/libahf/ahf_halos.c"):
+        _mirror_reference("/root/reference")
+    if os.path.isfile(os.path.join(REF_MIRROR, "src/libahf/ahf_halos.c")):
+        return REF_MIRROR
+    return None
+
+
 def build(ref: bool | None = None) -> None:
     """Compile the restatement (and the reference harness when the reference
-    tree is present and `ref` is not False)."""
+    tree, or its mirror, is present and `ref` is not False)."""
     targets = ["oracle"]
-    refdir = os.environ.get("AHF_REFERENCE", "/root/reference")
-    if ref is not False and os.path.isfile(os.path.join(refdir, "src/libahf/ahf_halos.c")):
+    refdir = reference_tree() if ref is not False else None
+    if refdir:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, f"REF={refdir}", *targets], check=True)
+    jobs = str(min(8, os.cpu_count() or 1))
+    subprocess.run(["make", "-s", "-j", jobs, "-C", HERE, f"REF={refdir or '/nonexistent'}", *targets], check=True)
 
 
 def _load(path: str, prefix: str):

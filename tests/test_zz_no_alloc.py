@@ -1,13 +1,14 @@
 """ahfgpu_construct_halos_noalloc against the allocating entry point.
 
 The no-allocation entry point serves callers that cannot allocate device
-memory (inside a CUDA-graph capture of a larger pipeline, under a host-owned
-pre-partitioned memory pool, or as a plugin with a fixed device budget): its
-work space is one static device array, and the caller passes device buffers
-for every input and output.  This test calls it through the C ABI twice in a
+memory (an application that partitions the GPU's memory itself and gives the
+analysis a fixed budget, or a plugin inside a running simulation that may not
+call cudaMalloc): its work space is one static device array, and the caller
+passes device buffers for every input and output.  This test calls it through the C ABI twice in a
 row on the same batch and checks both results against ahfgpu_construct_halos
 in the batched FP64 form: identical kept lists, properties within 1e-10
-relative, eigenvectors up to sign.  It also checks the size limits.  The
+relative, eigenvectors up to sign, with and without MULTIMASS weights.  It
+also checks the size limits.  The
 file is named to be collected last.
 """
 import ctypes as C
@@ -71,11 +72,12 @@ def _pack(halo, mem, prof, off):
     return d
 
 
-def test_noalloc_matches_allocating_entry_point_twice():
+@pytest.mark.parametrize("multimass", [False, True])
+def test_noalloc_matches_allocating_entry_point_twice(multimass):
     import torch
     from ahf_gb300 import synth
     lib, l = _lib()
-    L = synth.generate("cfg3", scale=0.002, max_particles=12000)
+    L = synth.generate("cfg3", scale=0.002, max_particles=12000, multimass=multimass)
     # keep the batch within the static work space
     n = np.diff(L.off.astype(np.int64))
     keep = np.nonzero(np.cumsum(n) <= 120000)[0]
@@ -85,6 +87,8 @@ def test_noalloc_matches_allocating_entry_point_twice():
     t = {"off": torch.as_tensor(L.off.astype(np.int64)).cuda()}
     for k in ("x", "y", "z", "vx", "vy", "vz"):
         t[k] = torch.as_tensor(getattr(L, k)).cuda()
+    if L.w is not None:
+        t["w"] = torch.as_tensor(L.w).cuda()
     t["gidx"] = torch.as_tensor(L.gidx.astype(np.int64)).cuda()
     for k in ("cx", "cy", "cz"):
         t[k] = torch.as_tensor(getattr(L, k)).cuda()
