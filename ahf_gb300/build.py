@@ -32,6 +32,7 @@ UNITS = {
     "gather.cu": [],
     "writer.cu": [],
     "sfc.cu": [],
+    "shard.cu": [],
 }
 
 

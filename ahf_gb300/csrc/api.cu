@@ -10,6 +10,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <new>
+#include <stdexcept>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -88,6 +90,31 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+// Host-side fault injection for tests: AHFGPU_INJECT_OOM names one
+// allocation site whose next allocation fails as a real one would --
+// "device_work" (a cudaMalloc of the work space), "host_result" (the result's
+// page-locked block and its malloc fallback), "host_plan" (a host container
+// of the call's plan: std::bad_alloc).  Unset in normal use.
+static bool inject_oom(const char* site) {
+  const char* e = getenv("AHFGPU_INJECT_OOM");
+  return e && strcmp(e, site) == 0;
+}
+
+// Every exported call runs inside this guard: a C++ exception (a failed host
+// allocation in a std::vector, for one) must not cross the C ABI.
+template <class F>
+static int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    return fail(AHFGPU_ERR_OOM, "host allocation failed (std::bad_alloc)");
+  } catch (const std::exception& ex) {
+    return fail(AHFGPU_ERR_STATE, "unexpected C++ exception: %s", ex.what());
+  } catch (...) {
+    return fail(AHFGPU_ERR_STATE, "unexpected C++ exception");
+  }
+}
+
 #define CK(call)                                                                         \
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \
@@ -106,7 +133,7 @@ struct DBuf {
     p = nullptr;
     cap = 0;
     size_t want = std::max<size_t>(bytes + bytes / 8, 256);
-    cudaError_t e = cudaMalloc(&p, want);
+    cudaError_t e = inject_oom("device_work") ? cudaErrorMemoryAllocation : cudaMalloc(&p, want);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return fail(AHFGPU_ERR_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
@@ -344,6 +371,7 @@ struct Plan {
 };
 
 int validate_and_plan(const ahfgpu_params* p, const uint64_t* off, int64_t nh, Plan& pl) {
+  if (inject_oom("host_plan")) throw std::bad_alloc();
   if (!p) return fail(AHFGPU_ERR_INVALID, "params is NULL");
   if (p->MINPART < 4) return fail(AHFGPU_ERR_INVALID, "MINPART must be >= 4 (got %lld)", (long long)p->MINPART);
   if (p->MINPART > 128)
@@ -822,7 +850,7 @@ void fill_dres(ahfgpu_result* r) {
 
 extern "C" {
 
-int ahfgpu_init(int device) {
+static int init_impl(int device) {
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
   if (e != cudaSuccess || n == 0) {
@@ -915,7 +943,7 @@ int ahfgpu_shutdown(void) {
   return AHFGPU_OK;
 }
 
-int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* dres,
+static int construct_halos_device_impl(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* dres,
                                   ahfgpu_mode mode, void* stream) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1061,6 +1089,7 @@ static HostBlock g_spare;                    // one cached block
 static std::vector<HostBlock> g_lent;        // blocks held by results
 
 static void* host_block_get(size_t bytes) {
+  if (inject_oom("host_result")) return nullptr;
   if (g_spare.p && g_spare.cap >= bytes) {
     g_lent.push_back(g_spare);
     void* p = g_spare.p;
@@ -1096,7 +1125,7 @@ static bool host_block_put(void* p) {
   return false;
 }
 
-int ahfgpu_fetch_result(ahfgpu_result* r) {
+static int fetch_result_impl(ahfgpu_result* r) {
   int rc = ensure_init();
   if (rc) return rc;
   if (!r) return fail(AHFGPU_ERR_INVALID, "result is NULL");
@@ -1116,7 +1145,8 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
     r->member = (uint64_t*)(blk + b_halo + 2 * b_off);
     r->prof = (double*)(blk + b_halo + 2 * b_off + b_mem);
   } else {
-    r->halo = (ahfgpu_halo*)malloc(b_halo);
+    const bool fail_all = inject_oom("host_result");
+    r->halo = fail_all ? nullptr : (ahfgpu_halo*)malloc(b_halo);
     r->member_off = (uint64_t*)malloc(b_off);
     r->member = (uint64_t*)malloc(b_mem);
     r->prof_off = (uint64_t*)malloc(b_off);
@@ -1141,7 +1171,7 @@ int ahfgpu_fetch_result(ahfgpu_result* r) {
   return AHFGPU_OK;
 }
 
-int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* cen, ahfgpu_batch* out,
+static int gather_device_impl(const ahfgpu_particles* parts, const ahfgpu_centres* cen, ahfgpu_batch* out,
                          void* stream) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1284,7 +1314,7 @@ static int writer_plan(const int64_t* order, int64_t minpart, bool bin_blocks, c
   return AHFGPU_OK;
 }
 
-int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int64_t* order, int64_t minpart,
+static int write_particles_device_impl(const uint64_t* ids, const float* w, const int64_t* order, int64_t minpart,
                                   const unsigned char** out, uint64_t* nbytes, void* stream) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1320,7 +1350,7 @@ int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int
   return AHFGPU_OK;
 }
 
-int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order, int64_t minpart,
+static int write_particles_bin_device_impl(const uint64_t* ids, const int64_t* order, int64_t minpart,
                                       const unsigned char** out, uint64_t* nbytes, void* stream) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1345,7 +1375,7 @@ int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order,
   return AHFGPU_OK;
 }
 
-int ahfgpu_sfc_sort_device(uint64_t n, const float* x, const float* y, const float* z, int bits, uint64_t* keys,
+static int sfc_sort_device_impl(uint64_t n, const float* x, const float* y, const float* z, int bits, uint64_t* keys,
                            uint64_t* order, void* stream) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1384,7 +1414,7 @@ int ahfgpu_sfc_sort_device(uint64_t n, const float* x, const float* y, const flo
   return AHFGPU_OK;
 }
 
-int ahfgpu_gather_radii_device(int64_t nh, const uint64_t* npart, const double* cx, const double* cy,
+static int gather_radii_device_impl(int64_t nh, const uint64_t* npart, const double* cx, const double* cy,
                                const double* cz, const double* rvir, double max_gather_rad_box, double* rad,
                                void* stream) {
   int rc = ensure_init();
@@ -1426,7 +1456,7 @@ int ahfgpu_gather_radii_device(int64_t nh, const uint64_t* npart, const double* 
   return AHFGPU_OK;
 }
 
-int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,
+static int construct_halos_impl(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,
                            ahfgpu_mode mode) {
   int rc = ensure_init();
   if (rc) return rc;
@@ -1466,6 +1496,51 @@ int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batc
   result->stats = s;
   g.last_stats = s;
   return AHFGPU_OK;
+}
+
+// the exported calls: each body above, inside the exception guard
+int ahfgpu_init(int device) {
+  return guarded([&] { return init_impl(device); });
+}
+
+int ahfgpu_construct_halos_device(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* dres,
+                                  ahfgpu_mode mode, void* stream) {
+  return guarded([&] { return construct_halos_device_impl(params, batch, dres, mode, stream); });
+}
+
+int ahfgpu_fetch_result(ahfgpu_result* r) {
+  return guarded([&] { return fetch_result_impl(r); });
+}
+
+int ahfgpu_gather_device(const ahfgpu_particles* parts, const ahfgpu_centres* cen, ahfgpu_batch* out,
+                         void* stream) {
+  return guarded([&] { return gather_device_impl(parts, cen, out, stream); });
+}
+
+int ahfgpu_write_particles_device(const uint64_t* ids, const float* w, const int64_t* order, int64_t minpart,
+                                  const unsigned char** out, uint64_t* nbytes, void* stream) {
+  return guarded([&] { return write_particles_device_impl(ids, w, order, minpart, out, nbytes, stream); });
+}
+
+int ahfgpu_write_particles_bin_device(const uint64_t* ids, const int64_t* order, int64_t minpart,
+                                      const unsigned char** out, uint64_t* nbytes, void* stream) {
+  return guarded([&] { return write_particles_bin_device_impl(ids, order, minpart, out, nbytes, stream); });
+}
+
+int ahfgpu_sfc_sort_device(uint64_t n, const float* x, const float* y, const float* z, int bits, uint64_t* keys,
+                           uint64_t* order, void* stream) {
+  return guarded([&] { return sfc_sort_device_impl(n, x, y, z, bits, keys, order, stream); });
+}
+
+int ahfgpu_gather_radii_device(int64_t nh, const uint64_t* npart, const double* cx, const double* cy,
+                               const double* cz, const double* rvir, double max_gather_rad_box, double* rad,
+                               void* stream) {
+  return guarded([&] { return gather_radii_device_impl(nh, npart, cx, cy, cz, rvir, max_gather_rad_box, rad, stream); });
+}
+
+int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,
+                           ahfgpu_mode mode) {
+  return guarded([&] { return construct_halos_impl(params, batch, result, mode); });
 }
 
 void ahfgpu_result_free(ahfgpu_result* r) {

@@ -23,7 +23,7 @@ SYMBOLS = [
     "ahfgpu_init", "ahfgpu_shutdown", "ahfgpu_construct_halos", "ahfgpu_construct_halos_device",
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
     "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
-    "ahfgpu_write_particles_bin_device", "ahfgpu_sfc_sort_device",
+    "ahfgpu_write_particles_bin_device", "ahfgpu_sfc_sort_device", "ahfgpu_shard_halos",
 ]
 
 
@@ -76,6 +76,8 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_write_particles_bin_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
     lib.ahfgpu_write_particles_bin_device.restype = C.c_int
+    lib.ahfgpu_shard_halos.argtypes = [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.ahfgpu_shard_halos.restype = C.c_int
     lib.ahfgpu_sfc_sort_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                            C.c_void_p, C.c_void_p]
     lib.ahfgpu_sfc_sort_device.restype = C.c_int

@@ -8,24 +8,20 @@ results back into batch order.  Only the merge crosses ranks.
 """
 from __future__ import annotations
 
-import heapq
-
 import numpy as np
 
 
 def lpt_assign(sizes, nranks: int) -> np.ndarray:
-    """Rank of every halo: LPT on cost n*log2(n+2), ties to the lowest rank."""
-    sizes = np.asarray(sizes, dtype=np.float64)
-    cost = sizes * np.log2(sizes + 2.0)
-    order = np.argsort(-cost, kind="stable")
-    heap = [(0.0, r) for r in range(nranks)]
-    heapq.heapify(heap)
-    rank = np.zeros(len(sizes), dtype=np.int64)
-    for h in order:
-        load, r = heapq.heappop(heap)
-        rank[h] = r
-        heapq.heappush(heap, (load + cost[h], r))
-    return rank
+    """Rank of every halo: LPT on cost n*log2(n+2), ties to the lower halo
+    index and the lower rank (ahfgpu_shard_halos, the library's split)."""
+    import ctypes as C
+    from . import lib
+    sizes = np.asarray(sizes, dtype=np.int64)
+    off = np.zeros(len(sizes) + 1, np.uint64)
+    off[1:] = np.cumsum(sizes)
+    rank = np.zeros(len(sizes), np.int32)
+    lib.check(lib.load().ahfgpu_shard_halos(len(sizes), off.ctypes.data, int(nranks), rank.ctypes.data))
+    return rank.astype(np.int64)
 
 
 def shard(lists, rank: int, nranks: int):

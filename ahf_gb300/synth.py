@@ -26,6 +26,12 @@ Workloads (the names used by bench.py and the tests):
   cfg5  1024^3 / 800 Mpc/h, 5e5 haloes, N^-1.9 on [20, 1e6], subhaloes
 The generator runs on torch (CPU for tests, CUDA for the large workloads) and
 returns numpy or torch arrays.
+
+`box_snapshot` builds the whole periodic box of a snapshot workload (cfg1,
+cfg2, cfg4, cfg5: ngrid^3 equal-mass particles, the haloes' NFW particles
+and a uniform background for the rest) and `write_gadget1` writes it as a
+GADGET-1 file (AHF ic_filetype 60) with an AHF.input beside it, for runs of
+the whole AHF program.
 """
 from __future__ import annotations
 
@@ -83,13 +89,16 @@ class HaloLists:
                          self.boxsize, self.pmass, self.name, dict(self.meta))
 
     def select(self, halos) -> "HaloLists":
-        """Sub-batch of the given halo indices (numpy arrays only)."""
+        """Sub-batch of the given halo indices (numpy or torch arrays; the
+        sub-batch keeps the array kind and device)."""
         halos = np.asarray(halos, dtype=np.int64)
         counts = (self.off[halos + 1] - self.off[halos]).astype(np.int64)
         off = np.zeros(len(halos) + 1, np.uint64)
         off[1:] = np.cumsum(counts)
         idx = np.concatenate([np.arange(self.off[h], self.off[h + 1], dtype=np.int64) for h in halos]) \
             if len(halos) else np.zeros(0, np.int64)
+        if isinstance(self.x, torch.Tensor):
+            idx = torch.as_tensor(idx, device=self.x.device)
         g = lambda a: None if a is None else a[idx]
         return HaloLists(off, g(self.x), g(self.y), g(self.z), g(self.vx), g(self.vy), g(self.vz),
                          g(self.w), g(self.gidx), self.cx[halos].copy(), self.cy[halos].copy(),
@@ -327,6 +336,20 @@ def generate(name: str, scale: float = 1.0, device: str = "cpu", multimass: bool
     return out.to_numpy() if as_numpy else out
 
 
+def parity_halos(n_in: np.ndarray, largest: int = 20, sample_particles: float = 2e7, seed: int = 31) -> np.ndarray:
+    """Haloes for a full-size parity check, ascending: the `largest` longest
+    lists plus a seeded random choice of the others holding about
+    `sample_particles` entries (drawn uniformly over haloes, so the sample
+    follows the batch's size mix)."""
+    n_in = np.asarray(n_in, np.int64)
+    top = np.argsort(-n_in, kind="stable")[:largest]
+    rest = np.setdiff1d(np.arange(len(n_in)), top)
+    rng = np.random.default_rng(seed)
+    perm = rest[rng.permutation(len(rest))]
+    k = int(np.searchsorted(np.cumsum(n_in[perm]), sample_particles)) + 1 if len(perm) else 0
+    return np.sort(np.concatenate([top, perm[:k]]))
+
+
 def params_for(lists: HaloLists, **kw):
     return ahf_params(lists.boxsize, lists.pmass, **kw)
 
@@ -414,3 +437,96 @@ def gather_edge_snapshot(seed: int = 11) -> Snapshot:
                     np.ascontiguousarray(vel[:, 0]), np.ascontiguousarray(vel[:, 1]), np.ascontiguousarray(vel[:, 2]),
                     None, np.ascontiguousarray(cen[:, 0]), np.ascontiguousarray(cen[:, 1]),
                     np.ascontiguousarray(cen[:, 2]), rad)
+
+
+@dataclass
+class BoxSnapshot:
+    """A whole periodic box: positions in Mpc/h in [0, box), peculiar
+    velocities in km/s, 32-bit ids, equal particle masses (Msun/h)."""
+    pos: np.ndarray
+    vel: np.ndarray
+    ids: np.ndarray
+    box: float
+    pmass: float
+    nhalo: int
+
+
+def box_snapshot(name: str, scale: float = 1.0, seed: int | None = None) -> BoxSnapshot:
+    """ngrid^3 particles: the NFW particles of the workload's haloes (and
+    subhaloes), truncated at R_vir, 10 % interlopers with v x 3, then a
+    uniform background (sigma = 100 km/s per axis) for the rest of the box;
+    ids are a seeded permutation of 1..N, the file order a seeded shuffle.
+    `scale` multiplies the number of haloes."""
+    cfg = dict(CONFIGS[name])
+    rng = np.random.default_rng(cfg["seed"] if seed is None else seed)
+    nhalo = max(1, int(round(cfg["nhalo"] * scale)))
+    box = cfg["box"]
+    tab = _halo_table(cfg, nhalo, rng, PMASS)
+    if cfg["subs"]:
+        tab = _add_subhalos(tab, rng)
+    nh = len(tab["npart"])
+    gen = torch.Generator(device="cpu")
+    gen.manual_seed(int(rng.integers(1 << 62)))
+    pos, vel, counts = _sample_spheres(tab, np.arange(nh), tab["npart"], np.zeros(nh, np.int64), gen, "cpu")
+    ntot = int(cfg["ngrid"]) ** 3
+    nbg = ntot - int(counts.sum())
+    if nbg < 0:
+        raise ValueError(f"{name}: the haloes hold more than ngrid^3 particles")
+    bpos = rng.random((nbg, 3)) * box
+    bvel = rng.standard_normal((nbg, 3)) * 100.0
+    P = np.concatenate([np.mod(pos.numpy(), box), bpos]).astype(np.float32)
+    P[P >= box] = 0.0
+    V = np.concatenate([vel.numpy().astype(np.float64), bvel]).astype(np.float32)
+    perm = rng.permutation(ntot)
+    ids = (rng.permutation(ntot) + 1).astype(np.uint32)
+    return BoxSnapshot(np.ascontiguousarray(P[perm]), np.ascontiguousarray(V[perm]), ids, box, PMASS, nh)
+
+
+def write_gadget1(path: str, snap: BoxSnapshot, outfile_prefix: str, input_path: str,
+                  omega0: float = OMEGA_M, lambda0: float = OMEGA_L, write_snapshot: bool = True) -> None:
+    """The snapshot as a single GADGET-1 file (Fortran-record blocks: the
+    256-byte header, POS, VEL, ID; one particle type, its mass in the header;
+    lengths in Mpc/h, masses in 1e10 Msun/h, a = 1; skipped when not
+    `write_snapshot`) and an AHF.input for it
+    (ic_filetype 60, LgridDomain 64, NperDomCell = NperRefCell = 5,
+    VescTune 1.5, NminPerHalo 20, RhoVir 0, Dvir 200, MaxGatherRad 3)."""
+    import struct
+    n = len(snap.ids)
+    hdr = struct.pack("<6i", 0, n, 0, 0, 0, 0)
+    hdr += struct.pack("<6d", 0.0, snap.pmass / 1e10, 0.0, 0.0, 0.0, 0.0)
+    hdr += struct.pack("<dd", 1.0, 0.0)              # expansion, redshift
+    hdr += struct.pack("<ii", 0, 0)                  # flag_sfr, flag_feedback
+    hdr += struct.pack("<6I", 0, n, 0, 0, 0, 0)      # npartTotal
+    hdr += struct.pack("<ii", 0, 1)                  # flag_cooling, num_files
+    hdr += struct.pack("<4d", snap.box, omega0, lambda0, 0.7)
+    hdr += b"\0" * (256 - len(hdr))
+
+    def block(f, data: bytes):
+        f.write(struct.pack("<i", len(data)))
+        f.write(data)
+        f.write(struct.pack("<i", len(data)))
+    if write_snapshot:
+        with open(path, "wb") as f:
+            block(f, hdr)
+            block(f, np.ascontiguousarray(snap.pos, "<f4").tobytes())
+            block(f, np.ascontiguousarray(snap.vel, "<f4").tobytes())
+            block(f, np.ascontiguousarray(snap.ids, "<u4").tobytes())
+    with open(input_path, "w") as f:
+        f.write("[AHF]\n"
+                f"ic_filename       = {path}\n"
+                "ic_filetype       = 60\n"
+                f"outfile_prefix    = {outfile_prefix}\n"
+                "LgridDomain       = 64\n"
+                "LgridMax          = 16777216\n"
+                "NperDomCell       = 5.0\n"
+                "NperRefCell       = 5.0\n"
+                "VescTune          = 1.5\n"
+                "NminPerHalo       = 20\n"
+                "RhoVir            = 0\n"
+                "Dvir              = 200\n"
+                "MaxGatherRad      = 3.0\n"
+                "LevelDomainDecomp = 6\n"
+                "NcpuReading       = 1\n"
+                "\n[GADGET]\n"
+                "GADGET_LUNIT      = 1.0\n"
+                "GADGET_MUNIT      = 1e10\n")

@@ -16,9 +16,18 @@ data).  A step is one call of the stage over the whole batch.
           reference's own code where it was built) on all host cores, on a
           bounded sample of the same haloes
 
-`--impl reference` times that CPU implementation alone on the same workload
-(rank 0; other ranks exit).  Under torchrun every rank processes its own
-full-size batch (seed + rank): weak scaling, no collective on the data path.
+`--impl reference` times the reference's own routines (compiled from its
+sources on the host; the C restatement where they could not be built) on all
+host cores, its K timed steps together covering the whole workload (rank 0;
+other ranks exit).  Under torchrun every rank builds the same batch and runs
+its share of the haloes (the library's LPT split, ahfgpu_shard_halos): strong
+scaling, no collective on the data path.
+
+`--case small|medium|big|gather|sfc` runs one small device-resident case
+twice and prints its device time (the cases the profiles/ summaries were
+captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, one of ~2e5,
+the gather on the lists of 5e3 haloes as a snapshot, the Hilbert sort of
+5e7 uniform points.
 """
 from __future__ import annotations
 
@@ -60,6 +69,9 @@ def parse():
     ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
     ap.add_argument("--multimass", action="store_true")
+    ap.add_argument("--case", default=None, choices=["small", "medium", "big", "gather", "sfc"],
+                    help="run one small profiling case instead of the benchmark")
+    ap.add_argument("--case-arg", type=float, default=None, help="gather: halo scale; sfc: points")
     return ap.parse_args()
 
 
@@ -180,11 +192,12 @@ def alg_bytes(n_in: np.ndarray, res_halo, has_w: bool) -> float:
     return float(per_p * n_in.sum() + 16.0 * nb.sum() + (24.0 + 256.0) * len(n_in) + 8.0 * 25.0 * nbins.sum())
 
 
-def precision_report(r32, r64, retests: int) -> dict:
-    """The FP32-compensated result against the FP64 form on the same batch:
-    haloes whose kept lists differ (must be 0), the largest relative
-    differences of Phi0, M_vir, V_max = sqrt(V2_max) and the spin lambda, and
-    the particles routed to the FP64 re-test."""
+def precision_report(r32, r64, retests, against: str) -> dict:
+    """The FP32-compensated result `r32` against `r64` (the FP64 oracle or the
+    batched FP64 form) on the same haloes: haloes whose kept lists differ
+    (must be 0), the largest relative differences of Phi0, M_vir, R_vir,
+    V_max = sqrt(V2_max), sigV and the spin lambda, and the particles routed
+    to the FP64 re-test."""
     n = len(r32.halo)
     diff = 0
     m32, m64, o32, o64 = r32.member, r64.member, r32.member_off, r64.member_off
@@ -206,11 +219,59 @@ def precision_report(r32, r64, retests: int) -> dict:
     worst = ({"npart": int(h64["npart"][prof][iw]), "lambda": float(l64[iw]), "rel_err": float(le[iw]),
               "median_lambda": float(np.median(np.abs(l64))), "haloes_above_1e-6": int(np.sum(le > 1e-6))}
              if le.size else None)
-    return {"haloes": n, "kept_list_mismatches": diff, "lambda_worst": worst, "max_rel_err": {
-        "Phi0": rel(h32["Phi0"], h64["Phi0"]), "M_vir": rel(h32["M_vir"], h64["M_vir"]),
-        "V_max": rel(np.sqrt(np.abs(h32["V2_max"][prof])), np.sqrt(np.abs(h64["V2_max"][prof]))),
-        "lambda": rel(h32["lambda_"][prof], h64["lambda_"][prof])},
-        "fp64_retests": retests, "against": "the batched FP64 form (bit-exact to the reference) on the same batch"}
+    return {"haloes": n, "particles": int(o64[-1]) if len(o64) else 0, "kept_list_mismatches": diff,
+            "lambda_worst": worst, "max_rel_err": {
+                "Phi0": rel(h32["Phi0"], h64["Phi0"]), "M_vir": rel(h32["M_vir"], h64["M_vir"]),
+                "R_vir": rel(h32["R_vir"], h64["R_vir"]),
+                "V_max": rel(np.sqrt(np.abs(h32["V2_max"][prof])), np.sqrt(np.abs(h64["V2_max"][prof]))),
+                "sigV": rel(h32["sigV"][prof], h64["sigV"][prof]),
+                "lambda": rel(h32["lambda_"][prof], h64["lambda_"][prof])},
+            "fp64_retests": retests, "against": against}
+
+
+def oracle_precision(lists, params, n_in: np.ndarray, args) -> dict:
+    """FP32C and batched FP64 against the oracle (the reference's algorithm
+    restated in C, all host threads) on the same haloes: the whole batch when
+    it holds at most 6e7 entries, else its 20 longest lists plus a seeded
+    random choice of ~2e7 entries of the others."""
+    import torch
+    from ahf_gb300 import lib, synth
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+    from compare import compare, compare_fp32c
+    O.build(ref=False)
+    N = int(n_in.sum())
+    if N <= 6e7:
+        sel, what = np.arange(len(n_in)), "every halo of the batch"
+    else:
+        sel = synth.parity_halos(n_in, largest=20, sample_particles=2e7, seed=31)
+        what = "the 20 longest lists and a seeded random choice of ~2e7 entries of the others"
+    sub = lists.select(sel)
+    t = {k: getattr(sub, k) for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx")}
+    t["off"] = torch.as_tensor(sub.off.astype(np.int64)).cuda()
+    for k in ("cx", "cy", "cz"):
+        t[k] = torch.as_tensor(getattr(sub, k)).cuda()
+    db = lib.device_batch(t)   # raw pointers into `t`, which stays alive below
+    r = lib.construct_halos_device(params, db, "batched_fp32c")
+    retests = int(r.stats.n_retest)
+    r32 = lib.fetch_result()
+    lib.construct_halos_device(params, db, "batched_fp64")
+    r64 = lib.fetch_result()
+    host = sub.to_numpy()
+    del db, t, sub
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    exp = O.run_oracle(params, host, 0)
+    odt = time.perf_counter() - t0
+    out = precision_report(r32, exp, retests, "the oracle (FP64, the reference's operation order) on " + what)
+    out["batched_fp64_vs_oracle"] = {"kept_lists_identical": bool(np.array_equal(r64.member_off, exp.member_off)
+                                                                   and np.array_equal(r64.member, exp.member)),
+                                     "failures_at_1e-10": compare(r64, exp, rtol=1e-10, etol=1e-8)[:5]}
+    out["fp32c_failures_at_bar"] = compare_fp32c(r32, exp)[:5]
+    out["longest_list"] = int(n_in[sel].max())
+    out["oracle_s"] = round(odt, 2)
+    return out
 
 
 def writer_leg(lists, res, args, ws: int, rank: int) -> dict:
@@ -449,10 +510,11 @@ def host_lists(lists):
     return lists.to_numpy()
 
 
-def run_cpu(params, lists_np, sample, nthreads):
+def run_cpu(params, lists_np, sample, nthreads, keep_order: bool = False):
+    """One CPU run over the haloes `sample` (ascending, unless keep_order)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    sub = lists_np.select(sample)
+    sub = lists_np.select(sample if keep_order else np.sort(sample))
     kind = "port"
     fn = O.run_oracle
     if O.have_ref(sub.w is not None):
@@ -465,7 +527,29 @@ def run_cpu(params, lists_np, sample, nthreads):
 
 # ---------------------------------------------------------------- arms
 
+def workload_config(args, n_in: np.ndarray, ws: int) -> dict:
+    """The `config` of both arms' lines (the same dict for the same workload)."""
+    N = int(n_in.sum())
+    desc = {"cfg1": "cfg1: 20 NFW haloes of 25-2,500 particles in 50 Mpc/h, lists to 1.5 R_vir",
+            "cfg2": "cfg2: 2,000 haloes, N_p ~ N^-1.9 on [20,1e6], 3 subhaloes per host above 1e4",
+            "cfg3": "cfg3: 1e5 halo particle lists, N_p ~ N^-1.56 on [20,2e6], float32 pos/vel, 64-bit ids",
+            "cfg4": "cfg4: 40,000 NFW haloes of 25-2,500 particles in 400 Mpc/h, lists to 1.5 R_vir",
+            "cfg5": "cfg5: 5e5 haloes, N_p ~ N^-1.9 on [20,1e6], 3 subhaloes per host above 1e4"}
+    return {"workload": desc.get(args.workload, args.workload) +
+            (", two species 5:1 (15% heavy)" if args.multimass else ", equal masses"),
+            "n_halos": int(len(n_in)), "n_particles": N, "scale": args.scale, "multimass": bool(args.multimass),
+            "l2": "inputs (%.1f GB) larger than L2 (129 MB): no flush" % (N * 32 / 1e9),
+            "parallelism": f"{ws} rank(s); the batch's haloes split over the ranks (LPT on n log n), "
+                           f"no data-path collective"}
+
+
 def reference_arm(args, ws, rank):
+    """The reference's own routines (compiled from its sources; the C
+    restatement where they could not be built) on all host threads.  The K
+    timed steps together process the whole workload once: halo i of the
+    batch sorted by decreasing list length goes to step i mod K, and each
+    step runs its haloes largest first under OpenMP's dynamic schedule, as
+    the reference's loop does.  Warm-up steps run small seeded samples."""
     if rank != 0:
         return
     import torch
@@ -478,24 +562,32 @@ def reference_arm(args, ws, rank):
     params = synth.params_for(lists)
     n_in = np.diff(lists.off.astype(np.int64))
     nthreads = os.cpu_count() or 1
-    per_step = min(args.cpu_particles, float(n_in.sum()))
+    order = np.argsort(-n_in, kind="stable")
+    K = max(1, args.steps)
+    for s in range(args.warmup):
+        run_cpu(params, lists, cpu_sample(n_in, min(2e6, float(n_in.sum())), seed=1000 + s), nthreads)
     times, parts, kind = [], [], "port"
-    for s in range(args.warmup + args.steps):
-        samp = cpu_sample(n_in, per_step, seed=1000 + s)
-        n, dt, kind = run_cpu(params, lists, samp, nthreads)
-        if s >= args.warmup:
-            times.append(dt)
-            parts.append(n)
+    for k in range(K):
+        n, dt, kind = run_cpu(params, lists, order[k::K], nthreads, keep_order=True)
+        times.append(dt)
+        parts.append(n)
     value = float(np.sum(parts) / np.sum(times))
+    serial = None
+    if args.cpu_serial_particles > 0:
+        samp1 = cpu_sample(n_in, args.cpu_serial_particles, seed=23)
+        n1, dt1, kind1 = run_cpu(params, lists, samp1, 1)
+        serial = {"value": n1 / dt1, "unit": UNIT, "cores": 1, "kind": kind1,
+                  "sample": f"seeded random subset of {len(samp1)} haloes / {n1} particles, one thread, {dt1:.2f} s"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: 1e5 halo particle lists, N_p ~ N^-1.56 on [20,2e6]",
-                   "n_halos": int(len(n_in)), "n_particles": int(n_in.sum()), "scale": args.scale,
-                   "multimass": args.multimass},
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, n_in, args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": f"per step a seeded random subset of ~{per_step:.3g} particles of the workload"},
+                         "sample": f"the whole workload ({int(np.sum(parts))} particles) over the {K} timed steps: "
+                                   f"haloes dealt round-robin by decreasing length, {nthreads} OpenMP threads, "
+                                   f"{np.sum(times):.1f} s in all",
+                         "serial": serial},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -512,10 +604,17 @@ def ours_arm(args, ws, rank, local):
     torch.cuda.set_device(local)
     lib.init(local)
     mode = args.mode or "batched_fp32c"
-    seed = synth.CONFIGS[args.workload]["seed"] + rank
+    # every rank builds the same seeded batch and keeps its share of the
+    # haloes (the library's LPT split, ahfgpu_shard_halos)
     lists = synth.generate(args.workload, scale=args.scale, device="cuda", multimass=args.multimass,
-                           seed=seed, as_numpy=False)
+                           as_numpy=False)
     params = synth.params_for(lists)
+    n_full = np.diff(lists.off.astype(np.int64))
+    if ws > 1:
+        from ahf_gb300.shard import lpt_assign
+        mine = np.nonzero(lpt_assign(n_full, ws) == rank)[0]
+        lists = lists.select(mine)
+        torch.cuda.empty_cache()
     n_in = np.diff(lists.off.astype(np.int64))
     N = int(n_in.sum())
     t = {"off": torch.as_tensor(lists.off.astype(np.int64)).cuda()}
@@ -616,9 +715,17 @@ def ours_arm(args, ws, rank, local):
                 forms[f] = {"value": nf / (fms / 1e3), "ms_per_step": fms, "sample": desc,
                             "replay_halos": int(rr.stats.n_replay_halos)}
                 if f == "batched_fp64" and mode == "batched_fp32c":
-                    precision = precision_report(res, lib.fetch_result(), int(stats.n_retest))
+                    precision = {"vs_fp64": precision_report(
+                        res, lib.fetch_result(), int(stats.n_retest),
+                        "the batched FP64 form (bit-exact to the reference) on the whole batch")}
             except lib.AhfGpuError as e:
                 forms[f] = {"unavailable": str(e)}
+        if mode == "batched_fp32c" and rank == 0 and not args.no_cpu:
+            try:
+                precision = dict(precision or {})
+                precision["vs_oracle"] = oracle_precision(lists, params, n_in, args)
+            except Exception as e:   # noqa: BLE001 -- reported in the line, the other legs stand
+                precision["vs_oracle"] = {"error": str(e)[:300]}
         # leave the last result of the headline form in place for fetch_result()
         step(mode)
         torch.cuda.synchronize()
@@ -664,6 +771,34 @@ def ours_arm(args, ws, rank, local):
         for k, v in zip(("ms_plan", "ms_h2d", "ms_h2d_first", "ms_pack", "ms_d2h"), np.mean(lib_parts, axis=0)):
             e2e[k] = float(v)
         e2e["ms_per_call"] = [round(float(v), 2) for v in lib_total]
+        e2e["host_buffers"] = "page-locked (torch pin_memory)"
+        # the same call from pageable host arrays, as a C caller's malloc'd
+        # arrays are: the input copies then go through the driver's staging
+        pg = {k: (np.ascontiguousarray(host[k].numpy()).copy() if host[k] is not None else None)
+              for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx")}
+        hp = abi.Batch()
+        hp.nhalo, hp.off = hb.nhalo, hb.off
+        for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+            setattr(hp, k, C.cast(C.c_void_p(pg[k].ctypes.data if pg[k] is not None else None),
+                                  C.POINTER(C.c_float)))
+        hp.gidx = C.cast(C.c_void_p(pg["gidx"].ctypes.data), C.POINTER(C.c_uint64))
+        for k in ("cx", "cy", "cz"):
+            setattr(hp, k, getattr(hb, k))
+        rr = lib.construct_halos_raw(params, hp, mode)
+        lib.free_result(rr)
+        barrier(ws)
+        t0 = time.perf_counter()
+        pg_parts = []
+        for _ in range(e2e_steps):
+            rr = lib.construct_halos_raw(params, hp, mode)
+            pg_parts.append([rr.stats.ms_total, rr.stats.ms_h2d, rr.stats.ms_device])
+            lib.free_result(rr)
+        pdt = allmax(ws, (time.perf_counter() - t0) / e2e_steps)
+        m = np.mean(pg_parts, axis=0)
+        e2e["pageable"] = {"value": total_parts / pdt, "unit": UNIT, "ms_per_step": pdt * 1e3,
+                           "ms_in_library": float(m[0]), "ms_h2d": float(m[1]), "ms_device": float(m[2]),
+                           "host_buffers": "pageable (numpy arrays)"}
+        del pg
 
     gather = None
     if not args.no_gather:
@@ -693,15 +828,10 @@ def ours_arm(args, ws, rank, local):
         return
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": ms_max, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
         "dtype": "f64" if "fp64" in mode else "f32+f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: 1e5 halo particle lists, N_p ~ N^-1.56 on [20,2e6], "
-                               f"float32 pos/vel, 64-bit ids, equal masses" + (" (two species)" if args.multimass else ""),
-                   "form": mode, "n_halos": int(len(n_in)), "n_particles": N, "n_kept": int(stats.n_kept),
-                   "scale": args.scale, "l2": "inputs (%.1f GB) larger than L2 (129 MB): no flush" % (N * 32 / 1e9),
-                   "parallelism": f"{ws} rank(s), each its own full-size batch (seed + rank): haloes "
-                                  f"sharded by rank, no data-path collective",
-                   "tuning": tuning},
+        "config": workload_config(args, n_full, ws),
+        "run": {"form": mode, "n_kept": int(stats.n_kept), "tuning": tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": kname,
@@ -720,8 +850,74 @@ def ours_arm(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def profile_case(args) -> None:
+    """One small device-resident case, run twice, for a profiler: the stage on
+    lists cut from the seeded 1e5-halo batch (small: 3000 lists of <= 512
+    entries, medium: 300 of 2048-16384, big: the one nearest 2e5), the gather
+    on the lists of 1e5 * scale haloes as a snapshot, or the Hilbert key sort
+    of n seeded uniform points."""
+    import torch
+    from ahf_gb300 import build as B
+    from ahf_gb300 import lib, synth
+    B.build()
+    lib.init(0)
+    mode = args.mode or "batched_fp32c"
+    if args.case == "sfc":
+        n = int(args.case_arg or 5e7)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(5)
+        x, y, z = (torch.rand(n, device="cuda", generator=g) for _ in range(3))
+        ms = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            keys, _order = lib.sfc_sort_device(x, y, z)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        ok = bool((keys[1:] >= keys[:-1]).all().item())
+        print(f"sfc: points {n} ascending {ok} ms per call {', '.join(f'{m:.2f}' for m in ms)}")
+        return
+    scale = (args.case_arg or 0.05) if args.case == "gather" else 0.05
+    L = synth.generate("cfg3", scale=scale, device="cuda", as_numpy=False)
+    n = np.diff(L.off.astype(np.int64))
+    if args.case == "gather":
+        rad = gather_radii(L, n)
+        parts = {k: getattr(L, k) for k in ("x", "y", "z", "vx", "vy", "vz", "w")}
+        cen = {"cx": torch.as_tensor(L.cx).cuda(), "cy": torch.as_tensor(L.cy).cuda(),
+               "cz": torch.as_tensor(L.cz).cuda(), "rad": rad}
+        ms = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b = lib.gather_device(parts, cen)
+            ms.append((time.perf_counter() - t0) * 1e3)
+        off, _ = lib.gathered_lists(b)
+        print(f"gather: haloes {len(n)} particles {int(L.x.numel())} gathered {int(off[-1])} "
+              f"ms per call {', '.join(f'{m:.1f}' for m in ms)}")
+        return
+    if args.case == "small":
+        sel = np.nonzero(n <= 512)[0][:3000]
+    elif args.case == "medium":
+        sel = np.nonzero((n > 2048) & (n <= 16384))[0][:300]
+    else:
+        sel = np.array([int(np.argmin(np.abs(n - 200000)))])
+    p = synth.params_for(L)
+    t = _device_subset(L, sel)
+    db = lib.device_batch(t)   # raw pointers into `t`, kept alive to the end
+    for _ in range(2):
+        r = lib.construct_halos_device(p, db, mode)
+    res = lib.fetch_result()
+    print(f"{args.case} {mode}: haloes {len(sel)} particles {int(n[sel].sum())} ms {r.stats.ms_device:.3f} "
+          f"fix_rounds max {res.halo['fix_rounds'].max()} niter mean {res.halo['niter'].mean():.2f} "
+          f"retests {r.stats.n_retest} exact_iterations {r.stats.n_replay_halos}")
+
+
 def main():
     args = parse()
+    if args.case:
+        profile_case(args)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, ws, rank)

@@ -294,6 +294,18 @@ AHFGPU_API const char *ahfgpu_version(void);
  * beside the library, or AHFGPU_TUNE_CACHE).  Returns AHFGPU_OK.           */
 AHFGPU_API int ahfgpu_tuning(char *buf, size_t len);
 
+/* ---- the split across GPUs ------------------------------------------------
+ * Replaces nothing in one process: AHF's haloes are independent
+ * (src/libahf/ahf_halos.c:504-510 runs them in any order), so a caller with
+ * several GPUs splits one snapshot's batch by halo and makes one
+ * ahfgpu_construct_halos call per GPU on its share -- no data exchange.
+ * rank_of_halo[h] (out, [nhalo]) is the rank of halo h: longest processing
+ * time first on the cost n log2(n + 2), n = off[h+1] - off[h], haloes by
+ * decreasing cost (ties: lower index), each to the least-loaded rank so far
+ * (ties: lower rank).  Host pointers; needs no device.                    */
+AHFGPU_API int ahfgpu_shard_halos(int64_t nhalo, const uint64_t *off, int32_t nranks,
+                                  int32_t *rank_of_halo);
+
 /* ---- no-allocation variant ----------------------------------------------
  * No counterpart in the reference (AHF has no GPU path).  For callers that
  * cannot allocate device memory: an application that gives AHF's analysis a

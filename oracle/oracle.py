@@ -71,6 +71,18 @@ def build(ref: bool | None = None) -> None:
     subprocess.run(["make", "-s", "-j", jobs, "-C", HERE, f"REF={refdir or '/nonexistent'}", *targets], check=True)
 
 
+def build_ahf() -> tuple[str, str]:
+    """The whole AHF program from the reference tree (or its mirror): the
+    stock serial build and the build with the stage swapped for the GPU
+    library (oracle/Makefile target `ahf`).  Returns their paths."""
+    refdir = reference_tree()
+    if not refdir:
+        raise FileNotFoundError("no AHF source tree (reference checkout or its mirror)")
+    jobs = str(min(16, os.cpu_count() or 1))
+    subprocess.run(["make", "-s", "-j", jobs, "-C", HERE, f"REF={refdir}", "ahf"], check=True)
+    return os.path.join(HERE, "_ref", "ahf", "AHF"), os.path.join(HERE, "_ref", "ahf", "AHF-gpu")
+
+
 def _load(path: str, prefix: str):
     if path in _LIBS:
         return _LIBS[path]

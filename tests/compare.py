@@ -4,7 +4,10 @@ Policy (the bar each test states):
   * kept particle lists (member_off, member): identical, in order;
   * npart, nbins and the stage flags: identical;
   * scalar properties: relative tolerance `rtol` (1e-10 for the FP64 forms,
-    1e-6 for the FP32-compensated form), absolute floor `atol`;
+    1e-6 for the FP32-compensated form), absolute floor `atol`; a profile
+    bin's angular momentum components relative to that bin's |L| (a
+    component near zero is the difference of large terms, and carries the
+    rounding of the whole vector in the reference's own sums too);
   * eigenvectors (E1..E3, per bin too): compared up to sign through
     |e_a . e_b| >= 1 - etol, skipped where two eigenvalues are within 1e-6
     relative of each other (the eigenvector is then not defined);
@@ -92,11 +95,21 @@ def compare(got, exp, rtol=1e-10, atol=1e-300, etol=1e-8, check_eig=True, skip_o
     if pg.shape != pe.shape:
         bad.append(f"profile shape {pg.shape} vs {pe.shape}")
     elif pg.size:
-        cols = [i for i, f in enumerate(PROF_FIELDS) if not f.startswith("E")]
+        cols = [i for i, f in enumerate(PROF_FIELDS)
+                if (not f.startswith("E") or f in ("Ekin", "Epot")) and f not in ("Lx", "Ly", "Lz")]
         e = rel_err(pg[:, cols], pe[:, cols], atol)
         if np.max(e) > rtol:
             c = cols[int(np.argmax(e.max(0)))]
             bad.append(f"profile {PROF_FIELDS[c]}: max rel err {np.max(e):.3e}")
+        # a bin's angular momentum components against the bin's |L|: a
+        # component that cancels to near zero carries the rounding of the
+        # whole vector, in the reference's own sequential sums as in ours
+        li = [PROF_FIELDS.index(f) for f in ("Lx", "Ly", "Lz")]
+        norm = np.linalg.norm(pe[:, li], axis=1, keepdims=True)
+        d = np.abs(pg[:, li] - pe[:, li])
+        eL = np.where(d == 0, 0.0, d / np.maximum(norm, 1e-300))
+        if np.max(eL) > rtol:
+            bad.append(f"profile L: max err / |L_bin| {np.max(eL):.3e}")
         if check_eig:
             ax = pe[:, [PROF_FIELDS.index("axis1"), PROF_FIELDS.index("axis2"), PROF_FIELDS.index("axis3")]]
             for j, nm in enumerate(("E1", "E2", "E3")):
