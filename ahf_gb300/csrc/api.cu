@@ -56,6 +56,14 @@ void sfc_keys(uint32_t n, const float* x, const float* y, const float* z, int bi
 void sfc_pass(uint32_t n, const uint64_t* kin, const uint32_t* iin, int shift, uint32_t* gh, uint32_t* goff,
               uint32_t* part, uint64_t* kout, uint32_t* iout, int* err, cudaStream_t st);
 void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaStream_t st);
+// the AMR hierarchy's first levels (amr.cu)
+void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l1, uint64_t* key, uint32_t* idx,
+               uint32_t* count, int grid, cudaStream_t st);
+void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
+              const uint32_t* ord, float* dens, cudaStream_t st);
+void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st);
+void amr_emit(int l1, const uint8_t* flag, const uint32_t* rowcnt, const uint32_t* rowoff, int64_t cap, int32_t* zyx,
+              int* err, cudaStream_t st);
 void writer_sizes(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, int64_t minpart, uint64_t* blk,
                   uint64_t* nchunk, unsigned long long* good, int grid, cudaStream_t st);
 void writer_offsets(const uint64_t* blk, int64_t nh, uint64_t* boff, cudaStream_t st);
@@ -195,6 +203,8 @@ struct Ctx {
   DBuf wb_chunk, wb_coff;                            // both writers: chunks per block, their scan
   DBuf wp_cbytes, wp_cboff;                          // ASCII: bytes per chunk, their scan
   DBuf sfc_kb, sfc_ia, sfc_ib, sfc_gh, sfc_goff, sfc_part, sfc_err;   // the SFC key sort
+  DBuf am_key, am_keyb, am_idx, am_idxb, am_cnt, am_start, am_sums;    // AMR: particles by domain node
+  DBuf am_gh, am_goff, am_part, am_err, am_flag, am_rowcnt, am_rowoff, am_rsums;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -921,7 +931,9 @@ int ahfgpu_shutdown(void) {
                   &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
                   &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.wp_cbytes,
                   &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
-                  &g.sfc_err, &g.phase};
+                  &g.sfc_err, &g.phase, &g.am_key, &g.am_keyb, &g.am_idx, &g.am_idxb, &g.am_cnt,
+                  &g.am_start, &g.am_sums, &g.am_gh, &g.am_goff, &g.am_part, &g.am_err, &g.am_flag,
+                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1414,6 +1426,88 @@ static int sfc_sort_device_impl(uint64_t n, const float* x, const float* y, cons
   return AHFGPU_OK;
 }
 
+static int amr_domain_density_device_impl(uint64_t n, const float* x, const float* y, const float* z, int l1,
+                                          float* dens, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (n == 0) return fail(AHFGPU_ERR_INVALID, "amr: no particles");
+  if (n >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "amr: %llu particles (limit 2^31 - 1)",
+                                     (unsigned long long)n);
+  if (l1 < 3 || l1 > 1024) return fail(AHFGPU_ERR_INVALID, "amr: domain grid %d outside 3..1024", l1);
+  if (!x || !y || !z || !dens) return fail(AHFGPU_ERR_INVALID, "amr: a pointer is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  const uint64_t nn = (uint64_t)l1 * l1 * l1;
+  const uint32_t n32 = (uint32_t)n, nt = sfc_ntiles(n32), m = 256u * nt, nb = sfc_scan_blocks(m);
+  if ((rc = g.am_key.ensure(n * 8)) || (rc = g.am_keyb.ensure(n * 8)) || (rc = g.am_idx.ensure(n * 4)) ||
+      (rc = g.am_idxb.ensure(n * 4)) || (rc = g.am_cnt.ensure(nn * 4)) || (rc = g.am_start.ensure((nn + 1) * 4)) ||
+      (rc = g.am_sums.ensure(((nn + 2047) / 2048) * 4)) || (rc = g.am_gh.ensure((size_t)m * 4)) ||
+      (rc = g.am_goff.ensure((size_t)m * 4)) || (rc = g.am_part.ensure((size_t)nb * 4)) ||
+      (rc = g.am_err.ensure(64)))
+    return rc;
+  CK(cudaMemsetAsync(g.am_cnt.p, 0, nn * 4, st));
+  CK(cudaMemsetAsync(g.am_err.p, 0, 64, st));
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
+  amr_cells(n32, x, y, z, l1, g.am_key.as<uint64_t>(), g.am_idx.as<uint32_t>(), g.am_cnt.as<uint32_t>(), grid, st);
+  gather_scan_u32(g.am_cnt.as<uint32_t>(), g.am_start.as<uint32_t>(), nn, g.am_sums.as<uint32_t>(), st);
+  // particles by node, ascending index within a node (stable radix sort)
+  int bits = 1;
+  while ((1ull << bits) < nn) bits++;
+  uint64_t *kin = g.am_key.as<uint64_t>(), *kout = g.am_keyb.as<uint64_t>();
+  uint32_t *iin = g.am_idx.as<uint32_t>(), *iout = g.am_idxb.as<uint32_t>();
+  for (int shift = 0; shift < bits; shift += 8) {
+    sfc_pass(n32, kin, iin, shift, g.am_gh.as<uint32_t>(), g.am_goff.as<uint32_t>(), g.am_part.as<uint32_t>(), kout,
+             iout, g.am_err.as<int>(), st);
+    std::swap(kin, kout);
+    std::swap(iin, iout);
+  }
+  amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), iin, dens, st);
+  CK(cudaGetLastError());
+  int derr = 0;
+  CK(cudaMemcpyAsync(&derr, g.am_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr) return fail(AHFGPU_ERR_CUDA, "amr: a scatter index left the array");
+  return AHFGPU_OK;
+}
+
+static int amr_first_refinement_device_impl(int l1, const float* dens, uint64_t n, double nth_dom, int32_t* zyx,
+                                            int64_t max_nodes, int64_t* nnodes, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!nnodes || !dens) return fail(AHFGPU_ERR_INVALID, "amr: a pointer is NULL");
+  *nnodes = 0;
+  if (n == 0) return fail(AHFGPU_ERR_INVALID, "amr: no particles");
+  if (l1 < 3 || l1 > 1024) return fail(AHFGPU_ERR_INVALID, "amr: domain grid %d outside 3..1024", l1);
+  if (max_nodes < 0 || (max_nodes > 0 && !zyx)) return fail(AHFGPU_ERR_INVALID, "amr: bad output buffer");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  const uint64_t nn = (uint64_t)l1 * l1 * l1, nr = (uint64_t)l1 * l1;
+  if ((rc = g.am_flag.ensure(nn)) || (rc = g.am_rowcnt.ensure(nr * 4)) || (rc = g.am_rowoff.ensure((nr + 1) * 4)) ||
+      (rc = g.am_rsums.ensure(((nr + 2047) / 2048) * 4)) || (rc = g.am_err.ensure(64)))
+    return rc;
+  // critdens - mean_dens, as refine_grid.c:120 and generate_grids.c:82 form it
+  const double dl1 = (double)l1;
+  const double thr = nth_dom * ((dl1 * dl1 * dl1) / (double)n) - 1.0;
+  CK(cudaMemsetAsync(g.am_err.p, 0, 64, st));
+  amr_flags(l1, dens, thr, g.am_flag.as<uint8_t>(), g.am_rowcnt.as<uint32_t>(), st);
+  gather_scan_u32(g.am_rowcnt.as<uint32_t>(), g.am_rowoff.as<uint32_t>(), nr, g.am_rsums.as<uint32_t>(), st);
+  uint32_t covered = 0;
+  CK(cudaMemcpyAsync(&covered, g.am_rowoff.as<uint32_t>() + nr, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const int64_t count = 8 * (int64_t)covered;
+  if (count < 125) return AHFGPU_OK;   // MIN_NNODES: no fine grid
+  *nnodes = count;
+  if (count > max_nodes)
+    return fail(AHFGPU_ERR_CAPACITY, "amr: the first refinement has %lld nodes, the buffer %lld", (long long)count,
+                (long long)max_nodes);
+  amr_emit(l1, g.am_flag.as<uint8_t>(), g.am_rowcnt.as<uint32_t>(), g.am_rowoff.as<uint32_t>(), max_nodes, zyx,
+           g.am_err.as<int>(), st);
+  CK(cudaGetLastError());
+  int derr = 0;
+  CK(cudaMemcpyAsync(&derr, g.am_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr) return fail(AHFGPU_ERR_CUDA, "amr: a fine node left the output buffer");
+  return AHFGPU_OK;
+}
+
 static int gather_radii_device_impl(int64_t nh, const uint64_t* npart, const double* cx, const double* cy,
                                const double* cz, const double* rvir, double max_gather_rad_box, double* rad,
                                void* stream) {
@@ -1536,6 +1630,16 @@ int ahfgpu_gather_radii_device(int64_t nh, const uint64_t* npart, const double* 
                                const double* cz, const double* rvir, double max_gather_rad_box, double* rad,
                                void* stream) {
   return guarded([&] { return gather_radii_device_impl(nh, npart, cx, cy, cz, rvir, max_gather_rad_box, rad, stream); });
+}
+
+int ahfgpu_amr_domain_density_device(uint64_t n, const float* x, const float* y, const float* z, int l1,
+                                     float* dens, void* stream) {
+  return guarded([&] { return amr_domain_density_device_impl(n, x, y, z, l1, dens, stream); });
+}
+
+int ahfgpu_amr_first_refinement_device(int l1, const float* dens, uint64_t n, double nth_dom, int32_t* zyx,
+                                       int64_t max_nodes, int64_t* nnodes, void* stream) {
+  return guarded([&] { return amr_first_refinement_device_impl(l1, dens, n, nth_dom, zyx, max_nodes, nnodes, stream); });
 }
 
 int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,

@@ -24,6 +24,7 @@ SYMBOLS = [
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
     "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
     "ahfgpu_write_particles_bin_device", "ahfgpu_sfc_sort_device", "ahfgpu_shard_halos",
+    "ahfgpu_amr_domain_density_device", "ahfgpu_amr_first_refinement_device",
 ]
 
 
@@ -76,6 +77,12 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_write_particles_bin_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_void_p),
                                                       C.POINTER(C.c_uint64), C.c_void_p]
     lib.ahfgpu_write_particles_bin_device.restype = C.c_int
+    lib.ahfgpu_amr_domain_density_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                                     C.c_void_p, C.c_void_p]
+    lib.ahfgpu_amr_domain_density_device.restype = C.c_int
+    lib.ahfgpu_amr_first_refinement_device.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p,
+                                                       C.c_int64, C.POINTER(C.c_int64), C.c_void_p]
+    lib.ahfgpu_amr_first_refinement_device.restype = C.c_int
     lib.ahfgpu_shard_halos.argtypes = [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p]
     lib.ahfgpu_shard_halos.restype = C.c_int
     lib.ahfgpu_sfc_sort_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
@@ -285,3 +292,27 @@ def sfc_sort_device(x, y, z, bits: int = 21, stream: int | None = None):
     check(load().ahfgpu_sfc_sort_device(n, x.data_ptr(), y.data_ptr(), z.data_ptr(), int(bits), keys.data_ptr(),
                                         order.data_ptr(), C.c_void_p(stream) if stream else None))
     return keys, order
+
+
+def amr_domain_density_device(x, y, z, l1: int, stream: int | None = None):
+    """TSC density minus the mean of the l1^3 domain grid (float, z-major)
+    from device float positions (torch tensors)."""
+    import torch
+    lib = load()
+    dens = torch.empty(l1 * l1 * l1, dtype=torch.float32, device=x.device)
+    check(lib.ahfgpu_amr_domain_density_device(int(x.numel()), x.data_ptr(), y.data_ptr(), z.data_ptr(), int(l1),
+                                               dens.data_ptr(), C.c_void_p(stream) if stream else None))
+    return dens
+
+
+def amr_first_refinement_device(dens, l1: int, n: int, nth_dom: float, stream: int | None = None):
+    """(z, y, x) of the first refined grid's nodes (int32 [k, 3] on the
+    device, ascending; empty below MIN_NNODES)."""
+    import torch
+    lib = load()
+    cap = 8 * l1 * l1 * l1
+    out = torch.empty((cap, 3), dtype=torch.int32, device=dens.device)
+    nn = C.c_int64(0)
+    check(lib.ahfgpu_amr_first_refinement_device(int(l1), dens.data_ptr(), int(n), float(nth_dom), out.data_ptr(),
+                                                 cap, C.byref(nn), C.c_void_p(stream) if stream else None))
+    return out[:nn.value]

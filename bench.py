@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--no-writer", action="store_true", help="skip the AHF_particles writer leg")
     ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
+    ap.add_argument("--no-amr", action="store_true", help="skip the AMR first-levels leg")
     ap.add_argument("--multimass", action="store_true")
     ap.add_argument("--case", default=None, choices=["small", "medium", "big", "gather", "sfc"],
                     help="run one small profiling case instead of the benchmark")
@@ -378,6 +379,55 @@ def sfc_leg(lists, args, ws: int, rank: int) -> dict:
                                    "sample": f"the first {m} particles, keys and qsort, {cdt:.2f} s"}
     except Exception as e:   # noqa: BLE001 -- reported in the line, the other legs stand
         return {"error": str(e)[:300]}
+    return out
+
+
+def amr_leg(args, rank: int) -> dict:
+    """The AMR hierarchy's first two levels on the GPU for the cfg1 and cfg2
+    boxes (64^3 and 256^3 particles, LgridDomain 64, NperDomCell 5): the
+    domain grid's TSC density (ahfgpu_amr_domain_density_device) and its
+    first refinement (ahfgpu_amr_first_refinement_device), timed together
+    with CUDA events over W warm-up and K timed calls; beside it the
+    reference's own gen_domgrids + ll + assign_npart (compiled from its
+    sources; one host core, timed inside a child process around those calls)
+    on the same particles."""
+    import torch
+    from ahf_gb300 import lib, synth
+    out = {}
+    try:
+        for name in ("cfg1", "cfg2"):
+            S = synth.box_snapshot(name)
+            p = (S.pos / np.float32(S.box)).astype(np.float32)
+            x, y, z = (torch.as_tensor(np.ascontiguousarray(p[:, k])).cuda() for k in range(3))
+            n = len(S.ids)
+            for _ in range(max(1, args.warmup)):
+                dens = lib.amr_domain_density_device(x, y, z, 64)
+                fine = lib.amr_first_refinement_device(dens, 64, n, 5.0)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                dens = lib.amr_domain_density_device(x, y, z, 64)
+                fine = lib.amr_first_refinement_device(dens, 64, n, 5.0)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            leg = {"metric": "particles assigned/s (domain grid + first refinement)", "value": n / (ms / 1e3),
+                   "unit": "particles/s", "ms_per_step": ms, "n_particles": n, "l1": 64,
+                   "fine_nodes": int(fine.shape[0]), "cpu_baseline": None}
+            if rank == 0 and not args.no_cpu:
+                sys.path.insert(0, os.path.join(ROOT, "oracle"))
+                import oracle as O
+                O.build()
+                if os.path.isfile(O.ref_amr_path()):
+                    _, sec = O.domain_dens_reference(p[:, 0], p[:, 1], p[:, 2], 64, timed=True)
+                    leg["cpu_baseline"] = {"value": n / sec, "unit": "particles/s", "cores": 1, "kind": "reference",
+                                           "sample": f"the whole box, gen_domgrids + ll + assign_npart only "
+                                                     f"(no refinement), {sec:.3f} s"}
+            out[name] = leg
+            del x, y, z, dens, fine
+    except Exception as e:   # noqa: BLE001 -- reported in the line, the other legs stand
+        out["error"] = str(e)[:300]
     return out
 
 
@@ -824,6 +874,7 @@ def ours_arm(args, ws, rank, local):
     # the Hilbert keying and particle sort (ahfgpu_sfc_sort_device), last:
     # a failure here is reported in its key and costs no other number
     sfc = None if args.no_sfc else sfc_leg(lists, args, ws, rank)
+    amr = None if args.no_amr else amr_leg(args, rank)
     if rank != 0:
         return
     line = {
@@ -844,6 +895,7 @@ def ours_arm(args, ws, rank, local):
         "gather": gather,
         "writer": writer,
         "sfc_sort": sfc,
+        "amr": amr,
         "precision": precision,
         "diagnostics": headline_stats,
     }

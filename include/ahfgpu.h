@@ -294,6 +294,33 @@ AHFGPU_API const char *ahfgpu_version(void);
  * beside the library, or AHFGPU_TUNE_CACHE).  Returns AHFGPU_OK.           */
 AHFGPU_API int ahfgpu_tuning(char *buf, size_t len);
 
+/* ---- the AMR hierarchy, first levels ---------------------------------------
+ * Replaces, for the domain grid, gen_domgrids + ll + assign_npart
+ * (src/libamr_serial/generate_grids.c:24, lltools.c, density.c:238; default
+ * TSC build, periodic): dens[(z*l1 + y)*l1 + x] (device, float, l1^3) is the
+ * node's TSC number density minus the mean, the float the reference's
+ * assign_npart leaves there bit for bit (each node's sum in its visiting
+ * order: source nodes ascending, each node's particles by descending input
+ * index).  Positions in [0, 1] (device floats; a coordinate of exactly 1.0
+ * falls in node 0 as ll() folds it); 3 <= l1 <= 1024; n < 2^31.            */
+AHFGPU_API int ahfgpu_amr_domain_density_device(uint64_t n, const float *x, const float *y, const float *z,
+                                                int l1, float *dens, void *stream);
+
+/* Replaces the first refine_grid call on the domain grid (gen_refgrid ->
+ * refine_grid, src/libamr_serial/generate_grids.c:126, refine_grid.c:899):
+ * the fine grid's nodes, 2 per dimension inside each coarse node that
+ * test_node (refine_grid.c:113-137) flags -- a node any of whose 18 nodes at
+ * dz, dy in {-1,0,1}, dx in {0,1} has dens >= NperDomCell l1^3 / n - 1 --
+ * or that follows a flagged node along x (wrapping at x = 0, not at
+ * x = l1 - 1).  zyx[3k .. 3k+2] (device int32) = (z, y, x) of fine node k on
+ * the 2 l1 grid, ascending; *nnodes their number, 0 when below MIN_NNODES
+ * (125, no fine grid).  A buffer of fewer than *nnodes nodes returns
+ * AHFGPU_ERR_CAPACITY with *nnodes set.  dens as returned by
+ * ahfgpu_amr_domain_density_device for the same n particles.               */
+AHFGPU_API int ahfgpu_amr_first_refinement_device(int l1, const float *dens, uint64_t n, double nth_dom,
+                                                  int32_t *zyx, int64_t max_nodes, int64_t *nnodes,
+                                                  void *stream);
+
 /* ---- the split across GPUs ------------------------------------------------
  * Replaces nothing in one process: AHF's haloes are independent
  * (src/libahf/ahf_halos.c:504-510 runs them in any order), so a caller with

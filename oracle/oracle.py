@@ -411,16 +411,22 @@ f.restype = C.c_int64
 x, y, z = (np.ascontiguousarray(a[k], dtype=np.float32) for k in ("x", "y", "z"))
 l1 = int(a["l1"])
 out = np.zeros(l1 ** 3)
+import time
+t0 = time.perf_counter()
 n = f(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, l1, out.ctypes.data)
+dt = time.perf_counter() - t0
 if n != l1 ** 3:
     sys.exit(3)
 np.save(sys.argv[3], out)
+open(sys.argv[3] + ".time", "w").write(repr(dt))
 """
 
 
-def domain_dens_reference(x, y, z, l1: int):
+def domain_dens_reference(x, y, z, l1: int, timed: bool = False):
     """The reference's own domain-grid densities after assign_npart
-    (oracle/ref_amr.c), [z, y, x]; in a child process."""
+    (oracle/ref_amr.c), [z, y, x]; in a child process.  With `timed`, also
+    the seconds the reference's calls took (gen_domgrids, ll, assign_npart,
+    measured inside the child)."""
     import sys
     import tempfile
     import numpy as np
@@ -429,7 +435,10 @@ def domain_dens_reference(x, y, z, l1: int):
         np.savez(path, x=np.asarray(x, np.float32), y=np.asarray(y, np.float32), z=np.asarray(z, np.float32), l1=l1)
         subprocess.run([sys.executable, "-c", _DENS_CHILD, path, ref_amr_path(), os.path.join(d, "out.npy")],
                        check=True, capture_output=True)
-        return np.load(os.path.join(d, "out.npy")).reshape(l1, l1, l1)
+        dens = np.load(os.path.join(d, "out.npy")).reshape(l1, l1, l1)
+        if timed:
+            return dens, float(open(os.path.join(d, "out.npy.time")).read())
+        return dens
 
 
 _REF1_CHILD = r"""

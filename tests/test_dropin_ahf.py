@@ -12,9 +12,13 @@ NFW haloes plus a uniform background) and the output files are compared:
   plain and batched FP64 forms: AHF_particles, AHF_halos, AHF_profiles and
     AHF_substructure byte for byte (bound id sets bit-exact, and every
     printed property equal);
-  FP32C form: AHF_particles and AHF_substructure byte for byte; AHF_halos
-    and AHF_profiles field by field, integers equal, every printed number
-    within 1e-6 relative or one unit of its last printed digit.
+  FP32C form: AHF_particles and AHF_substructure byte for byte (membership
+    identical); AHF_halos and AHF_profiles field by field, integers equal,
+    the spec properties (Mhalo, centre, bulk velocity, Rhalo, Rmax,
+    Vmax, sigV, lambda, lambdaE) within 1e-6 relative, the other numbers
+    within 1e-4 (or one unit of their last printed digit), unit vectors
+    within 1e-4 absolute up to sign, a bin's angular momentum within 1e-4
+    of its halo's largest |L|.
 cfg1: 64^3 particles in 50 Mpc/h, 20 haloes; cfg2: 256^3 in 200 Mpc/h,
 2,000 haloes with subhaloes (slow).
 """
@@ -54,39 +58,70 @@ def _run(binary, tmp, tag, snap_path, snap, env=None):
     return out
 
 
-def _close_text(a: bytes, b: bytes, rtol: float):
-    """Field-by-field comparison of two AHF text tables: integer fields
-    equal, numbers within rtol relative or one unit of the last printed
-    digit of the expected value.  Returns a list of differences."""
-    la, lb = a.decode().splitlines(), b.decode().splitlines()
-    if len(la) != len(lb):
-        return [f"{len(la)} lines vs {len(lb)}"]
+def _num_close(u: str, v: str, rtol: float, atol: float = 0.0) -> bool:
+    """u equals v, or is within rtol relative / atol absolute, or within one
+    unit of the last printed digit of v (the file's own precision)."""
+    if u == v:
+        return True
+    fu, fv = float(u), float(v)
+    mant = v.lower().split("e")[0]
+    dec = len(mant.split(".")[1]) if "." in mant else 0
+    exp = int(v.lower().split("e")[1]) if "e" in v.lower() else 0
+    ulp = 10.0 ** (exp - dec)
+    return abs(fu - fv) <= max(rtol * abs(fv), atol, 1.0001 * ulp)
+
+
+def _rows(a: bytes):
+    return [l.split() for l in a.decode().splitlines() if not l.startswith("#")]
+
+
+def _close_text(a: bytes, b: bytes, rtol: float, cols=None, vec_cols=(), atol_vec: float = 0.0):
+    """Field-by-field comparison of two AHF text tables (a got, b expected):
+    integer fields equal; numbers per `cols` (0-based column -> rtol, others
+    `rtol`) within that relative tolerance or one unit of the last printed
+    digit; each triple of `vec_cols` (unit-vector components) within
+    `atol_vec` absolute, up to a common sign.  Returns a list of
+    differences."""
+    ra, rb = _rows(a), _rows(b)
+    ha = [l for l in a.decode().splitlines() if l.startswith("#")]
+    hb = [l for l in b.decode().splitlines() if l.startswith("#")]
+    if ha != hb:
+        return ["headers differ"]
+    if len(ra) != len(rb):
+        return [f"{len(ra)} rows vs {len(rb)}"]
+    in_vec = {c for t in vec_cols for c in t}
     bad = []
-    for i, (x, y) in enumerate(zip(la, lb)):
-        if x.startswith("#") or y.startswith("#"):
-            if x != y:
-                bad.append(f"line {i}: header differs")
-            continue
-        fx, fy = x.split(), y.split()
+    for i, (fx, fy) in enumerate(zip(ra, rb)):
         if len(fx) != len(fy):
-            bad.append(f"line {i}: {len(fx)} fields vs {len(fy)}")
+            bad.append(f"row {i}: {len(fx)} fields vs {len(fy)}")
             continue
         for j, (u, v) in enumerate(zip(fx, fy)):
-            if u == v:
+            if u == v or j in in_vec:
                 continue
             if "." not in v and "e" not in v.lower():
-                bad.append(f"line {i} field {j}: {u} vs {v}")
+                bad.append(f"row {i} field {j + 1}: {u} vs {v}")
+            elif not _num_close(u, v, (cols or {}).get(j, rtol)):
+                bad.append(f"row {i} field {j + 1}: {u} vs {v}")
+        for t in vec_cols:
+            if t[-1] >= len(fy):
                 continue
-            fu, fv = float(u), float(v)
-            mant = v.lower().split("e")[0]
-            dec = len(mant.split(".")[1]) if "." in mant else 0
-            exp = int(v.lower().split("e")[1]) if "e" in v.lower() else 0
-            ulp = 10.0 ** (exp - dec)
-            if abs(fu - fv) > max(rtol * abs(fv), 1.0001 * ulp):
-                bad.append(f"line {i} field {j}: {u} vs {v}")
+            ga = np.array([float(fx[c]) for c in t])
+            gb = np.array([float(fy[c]) for c in t])
+            if not (np.all(np.abs(ga - gb) <= atol_vec) or np.all(np.abs(ga + gb) <= atol_vec)):
+                bad.append(f"row {i} vector {[c + 1 for c in t]}: {ga} vs {gb}")
         if len(bad) > 10:
             break
     return bad
+
+
+# AHF_halos columns (0-based) of the properties under the 1e-6 bar: Mhalo,
+# Xc, Yc, Zc, VXc, VYc, VZc, Rhalo, Rmax, Vmax, sigV, lambda, lambdaE; the
+# unit vectors L, Ea, Eb, Ec
+HALO_NS = {3: 1e-6, 5: 1e-6, 6: 1e-6, 7: 1e-6, 8: 1e-6, 9: 1e-6, 10: 1e-6, 11: 1e-6, 12: 1e-6, 16: 1e-6,
+           18: 1e-6, 19: 1e-6, 20: 1e-6}
+HALO_VEC = ((21, 22, 23), (26, 27, 28), (29, 30, 31), (32, 33, 34))
+# AHF_profiles: the axis vectors Ea, Eb, Ec of each bin
+PROF_VEC = ((13, 14, 15), (16, 17, 18), (19, 20, 21))
 
 
 def _case(name, tmp_path, ahf_bins, modes):
@@ -106,9 +141,31 @@ def _case(name, tmp_path, ahf_bins, modes):
                 assert got[suf] == want[suf], f"{name} {mode}: {suf} differ: " \
                     f"{_close_text(got[suf], want[suf], 0.0)[:5]}"
         else:
-            for suf in ("AHF_halos", "AHF_profiles"):
-                bad = _close_text(got[suf], want[suf], 1e-6)
-                assert not bad, (name, mode, suf, bad[:5])
+            # FP32C bar: the spec properties within 1e-6, the others
+            # within 1e-4, unit vectors within 1e-4 absolute up to sign; a
+            # bin's angular momentum within 1e-4 of the halo's largest |L_i|
+            bad = _close_text(got["AHF_halos"], want["AHF_halos"], 1e-4, HALO_NS, HALO_VEC, 1e-4)
+            assert not bad, (name, mode, "AHF_halos", bad[:5])
+            bad = _close_text(got["AHF_profiles"], want["AHF_profiles"], 1e-4, {8: 1e9, 9: 1e9, 10: 1e9},
+                              PROF_VEC, 1e-4)
+            assert not bad, (name, mode, "AHF_profiles", bad[:5])
+            bad = _profile_L(got["AHF_profiles"], want["AHF_profiles"], want["AHF_halos"], 1e-4)
+            assert not bad, (name, mode, "AHF_profiles L", bad[:5])
+
+
+def _profile_L(a: bytes, b: bytes, halos: bytes, atol_rel: float):
+    """Each bin's (Lx, Ly, Lz) within atol_rel of the largest |L| among its
+    halo's bins (the halo's nbins, AHF_halos column 37, split the rows)."""
+    ra, rb = _rows(a), _rows(b)
+    nb = [int(r[36]) for r in _rows(halos)]
+    bad, k = [], 0
+    for h, n in enumerate(nb):
+        A = np.array([[float(r[c]) for c in (8, 9, 10)] for r in ra[k:k + n]]).reshape(-1, 3)
+        B = np.array([[float(r[c]) for c in (8, 9, 10)] for r in rb[k:k + n]]).reshape(-1, 3)
+        k += n
+        if n and np.max(np.abs(A - B)) > atol_rel * max(np.max(np.linalg.norm(B, axis=1)), 1e-300):
+            bad.append(f"halo {h}: max |dL| {np.max(np.abs(A - B)):.3e}")
+    return bad
 
 
 @pytest.mark.gpu
@@ -123,9 +180,11 @@ def test_dropin_cfg2_plain_equals_stock_ahf(tmp_path, ahf_bins):
 
 
 def test_close_text_rules():
-    a = b"#h\n 1  2.50  3.1e+05\n"
+    a = b"#h\n 1  2.50  3.1e+05  0.6 0.8 0.0\n"
     assert _close_text(a, a, 0.0) == []
-    assert _close_text(b"#h\n 1  2.51  3.1e+05\n", a, 0.0) == []          # one unit of the last digit
-    assert _close_text(b"#h\n 1  2.52  3.1e+05\n", a, 0.0) != []
-    assert _close_text(b"#h\n 2  2.50  3.1e+05\n", a, 0.0) != []          # integers exact
-    assert np.isfinite(float("3.1e+05"))
+    assert _close_text(b"#h\n 1  2.51  3.1e+05  0.6 0.8 0.0\n", a, 0.0) == []   # one unit of the last digit
+    assert _close_text(b"#h\n 1  2.52  3.1e+05  0.6 0.8 0.0\n", a, 0.0) != []
+    assert _close_text(b"#h\n 2  2.50  3.1e+05  0.6 0.8 0.0\n", a, 0.0) != []   # integers exact
+    assert _close_text(b"#h\n 1  2.50  3.1e+05  -0.6 -0.8 -0.0\n", a, 0.0, None, ((3, 4, 5),), 1e-4) == []
+    assert _close_text(b"#h\n 1  2.50  3.1e+05  -0.6 0.8 0.0\n", a, 0.0, None, ((3, 4, 5),), 1e-4) != []
+    assert _close_text(b"#g\n" + a[3:], a, 0.0) != []                            # headers must agree
