@@ -19,7 +19,9 @@
 // adding the same double term to a float in the same order -- the floats
 // equal the reference's bit for bit.  The particles are grouped by node by a
 // stable radix sort of their node index (ascending index within a node; the
-// list order is that read backwards).
+// list order is that read backwards), and each particle's three separations
+// from its node's centre are computed once, in that order, so a target's
+// loop reads them contiguously and only forms its own weights and product.
 //
 // First refinement (refine_grid, refine_grid.c:899, test_node :113-137 on the
 // domain grid): a node is flagged when any node at dz, dy in {-1,0,1} and
@@ -87,10 +89,30 @@ __device__ __forceinline__ double amr_sep(float p, double centre, double dl1) {
   return sep;
 }
 
-__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, uint64_t n, const float* __restrict__ x,
+// each particle's separations (cells) from its own node's centre, in node
+// order (the order of the sorted node keys): computed once here, read by
+// the 27 targets around the node
+__global__ void __launch_bounds__(kAmrT) k_amr_seps(int l1, uint32_t n, const uint64_t* __restrict__ skey,
+                                                    const uint32_t* __restrict__ ord, const float* __restrict__ x,
                                                     const float* __restrict__ y, const float* __restrict__ z,
-                                                    const uint32_t* __restrict__ start,
-                                                    const uint32_t* __restrict__ ord, float* __restrict__ dens) {
+                                                    double* __restrict__ sx, double* __restrict__ sy,
+                                                    double* __restrict__ sz) {
+  const double dl1 = (double)l1;
+  const double shift = 0.5 / dl1;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const uint64_t node = skey[k];
+    const uint32_t i = ord[k];
+    const int cx = (int)(node % (uint64_t)l1), cy = (int)((node / (uint64_t)l1) % (uint64_t)l1),
+              cz = (int)(node / ((uint64_t)l1 * l1));
+    sx[k] = amr_sep(x[i], amr_fold(((double)cx / dl1 + shift) + 1.0), dl1);
+    sy[k] = amr_sep(y[i], amr_fold(((double)cy / dl1 + shift) + 1.0), dl1);
+    sz[k] = amr_sep(z[i], amr_fold(((double)cz / dl1 + shift) + 1.0), dl1);
+  }
+}
+
+__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, uint64_t n, const uint32_t* __restrict__ start,
+                                                    const double* __restrict__ sx, const double* __restrict__ sy,
+                                                    const double* __restrict__ sz, float* __restrict__ dens) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nn) return;
@@ -98,29 +120,25 @@ __global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, uint64_t n, const fl
             tz = (int)(t / ((uint64_t)l1 * l1));
   const double dl1 = (double)l1;
   const double m2d = (dl1 * dl1 * dl1) / (double)n;
-  const double shift = 0.5 / dl1;
-  int sz[3], sy[3], sx[3];
-  amr_three(tz, l1, sz);
-  amr_three(ty, l1, sy);
-  amr_three(tx, l1, sx);
+  int sz3[3], sy3[3], sx3[3];
+  amr_three(tz, l1, sz3);
+  amr_three(ty, l1, sy3);
+  amr_three(tx, l1, sx3);
   float acc = (float)(-1.0);
   for (int a = 0; a < 3; a++) {
     // offset of the target from the source along z, in {-1, 0, 1}
-    const int oz = ((tz - sz[a] + l1 + 1) % l1) - 1;
-    const double cz = amr_fold(((double)sz[a] / dl1 + shift) + 1.0);
+    const int oz = ((tz - sz3[a] + l1 + 1) % l1) - 1;
     for (int b = 0; b < 3; b++) {
-      const int oy = ((ty - sy[b] + l1 + 1) % l1) - 1;
-      const double cy = amr_fold(((double)sy[b] / dl1 + shift) + 1.0);
+      const int oy = ((ty - sy3[b] + l1 + 1) % l1) - 1;
       for (int c = 0; c < 3; c++) {
-        const int ox = ((tx - sx[c] + l1 + 1) % l1) - 1;
-        const double cx = amr_fold(((double)sx[c] / dl1 + shift) + 1.0);
-        const uint64_t s = ((uint64_t)sz[a] * l1 + (uint64_t)sy[b]) * l1 + (uint64_t)sx[c];
+        const int ox = ((tx - sx3[c] + l1 + 1) % l1) - 1;
+        const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
         const uint32_t s0 = start[s], s1 = start[s + 1];
-        for (uint32_t k = s1; k-- > s0;) {   // list order: descending input index
-          const uint32_t i = ord[k];
-          const double wz = amr_w(amr_sep(z[i], cz, dl1), oz);
-          const double wy = amr_w(amr_sep(y[i], cy, dl1), oy);
-          const double wx = amr_w(amr_sep(x[i], cx, dl1), ox);
+#pragma unroll 4
+        for (uint32_t k = s1; k > s0; k--) {   // list order: descending input index
+          const double wz = amr_w(__ldg(sz + k - 1), oz);
+          const double wy = amr_w(__ldg(sy + k - 1), oy);
+          const double wx = amr_w(__ldg(sx + k - 1), ox);
           acc = (float)((double)acc + m2d * wz * wy * wx);
         }
       }
@@ -205,9 +223,11 @@ void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l
 }
 
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint32_t* ord, float* dens, cudaStream_t st) {
+              const uint64_t* skey, const uint32_t* ord, double* seps, float* dens, int grid, cudaStream_t st) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
-  k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, n, x, y, z, start, ord, dens);
+  double *sx = seps, *sy = seps + n, *sz = seps + 2 * n;
+  k_amr_seps<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, sx, sy, sz);
+  k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, n, start, sx, sy, sz, dens);
 }
 
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st) {

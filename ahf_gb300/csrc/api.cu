@@ -60,7 +60,7 @@ void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaS
 void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l1, uint64_t* key, uint32_t* idx,
                uint32_t* count, int grid, cudaStream_t st);
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint32_t* ord, float* dens, cudaStream_t st);
+              const uint64_t* skey, const uint32_t* ord, double* seps, float* dens, int grid, cudaStream_t st);
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st);
 void amr_emit(int l1, const uint8_t* flag, const uint32_t* rowcnt, const uint32_t* rowoff, int64_t cap, int32_t* zyx,
               int* err, cudaStream_t st);
@@ -204,7 +204,7 @@ struct Ctx {
   DBuf wp_cbytes, wp_cboff;                          // ASCII: bytes per chunk, their scan
   DBuf sfc_kb, sfc_ia, sfc_ib, sfc_gh, sfc_goff, sfc_part, sfc_err;   // the SFC key sort
   DBuf am_key, am_keyb, am_idx, am_idxb, am_cnt, am_start, am_sums;    // AMR: particles by domain node
-  DBuf am_gh, am_goff, am_part, am_err, am_flag, am_rowcnt, am_rowoff, am_rsums;
+  DBuf am_gh, am_goff, am_part, am_err, am_flag, am_rowcnt, am_rowoff, am_rsums, am_seps;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -933,7 +933,7 @@ int ahfgpu_shutdown(void) {
                   &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
                   &g.sfc_err, &g.phase, &g.am_key, &g.am_keyb, &g.am_idx, &g.am_idxb, &g.am_cnt,
                   &g.am_start, &g.am_sums, &g.am_gh, &g.am_goff, &g.am_part, &g.am_err, &g.am_flag,
-                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums};
+                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums, &g.am_seps};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
@@ -1442,7 +1442,7 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
       (rc = g.am_idxb.ensure(n * 4)) || (rc = g.am_cnt.ensure(nn * 4)) || (rc = g.am_start.ensure((nn + 1) * 4)) ||
       (rc = g.am_sums.ensure(((nn + 2047) / 2048) * 4)) || (rc = g.am_gh.ensure((size_t)m * 4)) ||
       (rc = g.am_goff.ensure((size_t)m * 4)) || (rc = g.am_part.ensure((size_t)nb * 4)) ||
-      (rc = g.am_err.ensure(64)))
+      (rc = g.am_err.ensure(64)) || (rc = g.am_seps.ensure(n * 24)))
     return rc;
   CK(cudaMemsetAsync(g.am_cnt.p, 0, nn * 4, st));
   CK(cudaMemsetAsync(g.am_err.p, 0, 64, st));
@@ -1460,7 +1460,7 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
     std::swap(kin, kout);
     std::swap(iin, iout);
   }
-  amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), iin, dens, st);
+  amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), dens, grid, st);
   CK(cudaGetLastError());
   int derr = 0;
   CK(cudaMemcpyAsync(&derr, g.am_err.p, 4, cudaMemcpyDeviceToHost, st));

@@ -15,11 +15,14 @@
 //
 // Sort: least-significant-digit radix sort with 8-bit digits over the 3 bits
 // key bits (8 passes at 21 bits), stable, so equal keys keep their original
-// index order.  Per pass: a digit histogram of every 4096-key tile (one warp
-// per tile), an exclusive scan of the digit-major histogram (three kernels),
-// and a stable scatter in which each warp walks its tile 32 keys at a time,
-// ranking equal digits with __match_any_sync.  Every store index is checked
-// against n; a violation sets the error flag instead of writing.
+// index order.  Per pass: a digit histogram of every 4096-key tile (one
+// block per tile), an exclusive scan of the digit-major histogram (three
+// kernels), and a stable scatter per tile: each warp ranks its 512 keys 32
+// at a time with __match_any_sync, the tile is reordered by digit in shared
+// memory, and the keys are written out in that order, so each digit's run
+// of the tile (16 keys on average) lands as one contiguous, coalesced piece.
+// Every store index is checked against n; a violation sets the error flag
+// instead of writing.
 #include <cstdint>
 
 #include "common.cuh"
@@ -27,9 +30,20 @@
 
 namespace ahfgpu {
 
-constexpr int kSfcTile = 4096;          // keys per warp tile
-constexpr int kSfcWarps = 4;            // warps (tiles) per block
+constexpr int kSfcTile = 4096;          // keys per tile (one block)
+constexpr int kSfcT = 256;              // threads per tile block
+constexpr int kSfcWarps = kSfcT / 32;   // 8 warps, 512 keys each
+constexpr int kSfcPer = kSfcTile / kSfcT;
 constexpr int kScanChunk = 4096;        // values per block of the generic scan
+
+struct SfcTileSmem {
+  uint64_t key[kSfcTile];               // the tile, reordered by digit
+  uint32_t idx[kSfcTile];
+  uint32_t wcnt[kSfcWarps][256];        // per-warp digit counts, then offsets
+  uint32_t dstart[256];                 // tile-local start of each digit
+  uint32_t gbase[256];                  // where the tile's digit-d keys go
+  uint32_t wsum[kSfcWarps];
+};
 
 __global__ void __launch_bounds__(256) k_sfc_keys(uint32_t n, const float* __restrict__ x,
                                                   const float* __restrict__ y, const float* __restrict__ z, int bits,
@@ -41,59 +55,96 @@ __global__ void __launch_bounds__(256) k_sfc_keys(uint32_t n, const float* __res
 }
 
 // digit counts of every tile, digit-major: gh[d * ntiles + t]
-__global__ void __launch_bounds__(32 * kSfcWarps) k_sfc_hist(uint32_t n, uint32_t ntiles,
-                                                             const uint64_t* __restrict__ keys, int shift,
-                                                             uint32_t* __restrict__ gh) {
-  __shared__ uint32_t cnt[kSfcWarps][256];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t tile = blockIdx.x * kSfcWarps + w;
-  for (int d = lane; d < 256; d += 32) cnt[w][d] = 0;
-  __syncwarp();
-  if (tile < ntiles) {
-    const uint64_t base = (uint64_t)tile * kSfcTile;
-    for (int r = 0; r < kSfcTile / 32; r++) {
-      const uint64_t i = base + (uint64_t)r * 32 + lane;
-      if (i < n) atomicAdd(&cnt[w][(uint32_t)(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncwarp();
-    for (int d = lane; d < 256; d += 32) gh[(uint64_t)d * ntiles + tile] = cnt[w][d];
+__global__ void __launch_bounds__(kSfcT) k_sfc_hist(uint32_t n, uint32_t ntiles, const uint64_t* __restrict__ keys,
+                                                    int shift, uint32_t* __restrict__ gh) {
+  __shared__ uint32_t cnt[256];
+  const uint32_t tile = blockIdx.x;
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t base = (uint64_t)tile * kSfcTile;
+  for (int r = 0; r < kSfcPer; r++) {
+    const uint64_t i = base + (uint64_t)r * kSfcT + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[(uint32_t)(keys[i] >> shift) & 255u], 1u);
   }
+  __syncthreads();
+  gh[(uint64_t)threadIdx.x * ntiles + tile] = cnt[threadIdx.x];
 }
 
-// stable scatter of one tile per warp; goff[d * ntiles + t] is where tile
+// stable scatter of one tile per block; goff[d * ntiles + t] is where tile
 // t's first key of digit d goes
-__global__ void __launch_bounds__(32 * kSfcWarps) k_sfc_scatter(uint32_t n, uint32_t ntiles,
-                                                                const uint64_t* __restrict__ kin,
-                                                                const uint32_t* __restrict__ iin, int shift,
-                                                                const uint32_t* __restrict__ goff,
-                                                                uint64_t* __restrict__ kout,
-                                                                uint32_t* __restrict__ iout, int* __restrict__ err) {
-  __shared__ uint32_t cnt[kSfcWarps][256];
+__global__ void __launch_bounds__(kSfcT) k_sfc_scatter(uint32_t n, uint32_t ntiles, const uint64_t* __restrict__ kin,
+                                                       const uint32_t* __restrict__ iin, int shift,
+                                                       const uint32_t* __restrict__ goff,
+                                                       uint64_t* __restrict__ kout, uint32_t* __restrict__ iout,
+                                                       int* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char sfc_smem[];
+  SfcTileSmem& S = *reinterpret_cast<SfcTileSmem*>(sfc_smem);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const uint32_t tile = blockIdx.x * kSfcWarps + w;
-  if (tile >= ntiles) return;           // whole warp
-  for (int d = lane; d < 256; d += 32) cnt[w][d] = goff[(uint64_t)d * ntiles + tile];
-  __syncwarp();
-  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t tile = blockIdx.x;
   const uint64_t base = (uint64_t)tile * kSfcTile;
-  for (int r = 0; r < kSfcTile / 32; r++) {
-    const uint64_t i = base + (uint64_t)r * 32 + lane;
+  for (int d = lane; d < 256; d += 32) S.wcnt[w][d] = 0;
+  S.gbase[threadIdx.x] = goff[(uint64_t)threadIdx.x * ntiles + tile];
+  __syncwarp();
+  // 1. ranks within each warp's 512 consecutive keys, in order
+  const uint32_t lt = (1u << lane) - 1u;
+  uint64_t k[kSfcPer];
+  uint32_t v[kSfcPer], rank[kSfcPer], dig[kSfcPer];
+#pragma unroll
+  for (int r = 0; r < kSfcPer; r++) {
+    const uint64_t i = base + (uint64_t)w * (kSfcTile / kSfcWarps) + (uint64_t)r * 32 + lane;
     const bool valid = i < n;
-    const uint64_t k = valid ? kin[i] : 0ull;
-    const uint32_t v = valid ? iin[i] : 0u;
-    const uint32_t d = valid ? ((uint32_t)(k >> shift) & 255u) : 256u + (uint32_t)lane;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t pos = valid ? cnt[w][d] + __popc(peers & lt) : 0u;
+    k[r] = valid ? kin[i] : 0ull;
+    v[r] = valid ? iin[i] : 0u;
+    dig[r] = valid ? ((uint32_t)(k[r] >> shift) & 255u) : 256u + (uint32_t)lane;
+    const uint32_t peers = __match_any_sync(0xffffffffu, dig[r]);
+    rank[r] = valid ? S.wcnt[w][dig[r]] + __popc(peers & lt) : 0u;
     __syncwarp();
-    if (valid && lane == __ffs(peers) - 1) cnt[w][d] += __popc(peers);
+    if (valid && lane == __ffs(peers) - 1) S.wcnt[w][dig[r]] += __popc(peers);
     __syncwarp();
-    if (valid) {
-      if (pos < n) {
-        kout[pos] = k;
-        iout[pos] = v;
-      } else {
-        atomicExch(err, 1);
-      }
+  }
+  __syncthreads();
+  // 2. per digit (thread = digit): the warps' offsets within the digit, the
+  //    digit's total; then the digits' starts in the tile (a block scan)
+  uint32_t tot = 0;
+#pragma unroll
+  for (int q = 0; q < kSfcWarps; q++) {
+    const uint32_t c = S.wcnt[q][threadIdx.x];
+    S.wcnt[q][threadIdx.x] = tot;
+    tot += c;
+  }
+  uint32_t inc = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) S.wsum[w] = inc;
+  __syncthreads();
+  uint32_t before = 0;
+  for (int q = 0; q < w; q++) before += S.wsum[q];
+  S.dstart[threadIdx.x] = before + inc - tot;
+  __syncthreads();
+  // 3. the tile reordered by digit in shared memory
+#pragma unroll
+  for (int r = 0; r < kSfcPer; r++) {
+    if (dig[r] < 256u) {
+      const uint32_t p = S.dstart[dig[r]] + S.wcnt[w][dig[r]] + rank[r];
+      S.key[p] = k[r];
+      S.idx[p] = v[r];
+    }
+  }
+  __syncthreads();
+  // 4. out in that order: each digit's run contiguous in the output
+  const uint64_t left = (uint64_t)n - base;
+  const uint32_t valid_n = left < (uint64_t)kSfcTile ? (uint32_t)left : (uint32_t)kSfcTile;
+  for (uint32_t p = threadIdx.x; p < valid_n; p += kSfcT) {
+    const uint64_t key = S.key[p];
+    const uint32_t d = (uint32_t)(key >> shift) & 255u;
+    const uint64_t pos = (uint64_t)S.gbase[d] + (p - S.dstart[d]);
+    if (pos < n) {
+      kout[pos] = key;
+      iout[pos] = S.idx[p];
+    } else {
+      atomicExch(err, 1);
     }
   }
 }
@@ -193,14 +244,14 @@ void sfc_keys(uint32_t n, const float* x, const float* y, const float* z, int bi
 void sfc_pass(uint32_t n, const uint64_t* kin, const uint32_t* iin, int shift, uint32_t* gh, uint32_t* goff,
               uint32_t* part, uint64_t* kout, uint32_t* iout, int* err, cudaStream_t st) {
   const uint32_t nt = sfc_ntiles(n);
-  const uint32_t blocks = (nt + kSfcWarps - 1) / kSfcWarps;
   const uint32_t m = 256u * nt;
   const uint32_t nb = sfc_scan_blocks(m);
-  k_sfc_hist<<<blocks, 32 * kSfcWarps, 0, st>>>(n, nt, kin, shift, gh);
+  cudaFuncSetAttribute(k_sfc_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SfcTileSmem));
+  k_sfc_hist<<<nt, kSfcT, 0, st>>>(n, nt, kin, shift, gh);
   k_scan_sums<<<nb, 256, 0, st>>>(gh, m, part);
   k_scan_parts<<<1, 1024, 0, st>>>(part, nb);
   k_scan_apply<<<nb, 256, 0, st>>>(gh, m, part, goff);
-  k_sfc_scatter<<<blocks, 32 * kSfcWarps, 0, st>>>(n, nt, kin, iin, shift, goff, kout, iout, err);
+  k_sfc_scatter<<<nt, kSfcT, sizeof(SfcTileSmem), st>>>(n, nt, kin, iin, shift, goff, kout, iout, err);
 }
 
 void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaStream_t st) {

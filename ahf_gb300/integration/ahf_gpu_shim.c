@@ -207,6 +207,12 @@ int ahfgpu_shim_construct_halos(HALO *halos, int numHalos)
   rc = ahfgpu_construct_halos(&prm, &b, &res, shim_mode());
   free(buf); free(gidx); free(cen); free(off);
   if (rc != AHFGPU_OK) { free(which); return shim_fail(rc, "ahfgpu_construct_halos"); }
+  if (getenv("AHFGPU_LOG"))
+    fprintf(stderr, "ahfgpu: %lld haloes, %llu particles in, %llu kept, %llu equal radial keys, "
+            "%llu replayed haloes, %.3f ms on the device\n", (long long)nb,
+            (unsigned long long)res.stats.n_particles_in, (unsigned long long)res.stats.n_kept,
+            (unsigned long long)res.stats.n_key_ties, (unsigned long long)res.stats.n_replay_halos,
+            res.stats.ms_device);
 
   /* 3. write back where the five functions write */
   for (k = 0; k < nb; k++) {

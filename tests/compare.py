@@ -4,8 +4,9 @@ Policy (the bar each test states):
   * kept particle lists (member_off, member): identical, in order;
   * npart, nbins and the stage flags: identical;
   * scalar properties: relative tolerance `rtol` (1e-10 for the FP64 forms,
-    1e-6 for the FP32-compensated form), absolute floor `atol`; a profile
-    bin's angular momentum components relative to that bin's |L| (a
+    1e-6 for the FP32-compensated form), absolute floor `atol`; the halo's
+    AngMom components and a profile bin's angular momentum components
+    relative to that vector's norm (a
     component near zero is the difference of large terms, and carries the
     rounding of the whole vector in the reference's own sums too);
   * eigenvectors (E1..E3, per bin too): compared up to sign through
@@ -77,6 +78,11 @@ def compare(got, exp, rtol=1e-10, atol=1e-300, etol=1e-8, check_eig=True, skip_o
         e = rel_err(a, b, atol)
         if k == "R_vir":
             e = e[~nob] if e.ndim == 1 else e[~nob]
+        if k == "AngMom":
+            # components against the vector's norm (see the profile L below)
+            nrm = np.linalg.norm(np.asarray(b, np.float64).reshape(-1, 3), axis=1, keepdims=True)
+            d = np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)).reshape(-1, 3)
+            e = np.where(d == 0, 0.0, d / np.maximum(nrm, 1e-300))
         if e.size and np.max(e) > rtol:
             i = int(np.argmax(e.reshape(len(e), -1).max(1)))
             bad.append(f"{k}: max rel err {np.max(e):.3e} (halo {i})")
