@@ -19,9 +19,10 @@
 // adding the same double term to a float in the same order -- the floats
 // equal the reference's bit for bit.  The particles are grouped by node by a
 // stable radix sort of their node index (ascending index within a node; the
-// list order is that read backwards), and each particle's three separations
-// from its node's centre are computed once, in that order, so a target's
-// loop reads them contiguously and only forms its own weights and product.
+// list order is that read backwards), and each particle's nine TSC factors
+// (m2d w_z, w_y, w_x for the three offsets per axis) are computed once, in
+// that order, so a target's loop reads three of them contiguously and forms
+// the rest of the product (two multiplications) and the float sum.
 //
 // First refinement (refine_grid, refine_grid.c:899, test_node :113-137 on the
 // domain grid): a node is flagged when any node at dz, dy in {-1,0,1} and
@@ -89,37 +90,47 @@ __device__ __forceinline__ double amr_sep(float p, double centre, double dl1) {
   return sep;
 }
 
-// each particle's separations (cells) from its own node's centre, in node
-// order (the order of the sorted node keys): computed once here, read by
-// the 27 targets around the node
-__global__ void __launch_bounds__(kAmrT) k_amr_seps(int l1, uint32_t n, const uint64_t* __restrict__ skey,
-                                                    const uint32_t* __restrict__ ord, const float* __restrict__ x,
-                                                    const float* __restrict__ y, const float* __restrict__ z,
-                                                    double* __restrict__ sx, double* __restrict__ sy,
-                                                    double* __restrict__ sz) {
+// each particle's TSC weights, in node order (the order of the sorted node
+// keys), computed once and read by the 27 targets around the node:
+// az[o] = m2d * w_z(o) (the first product of the reference's left-to-right
+// m2d * w_z * w_y * w_x), wy[o], wx[o], o = offset + 1 of the target
+struct AmrW {
+  double* az[3];
+  double* wy[3];
+  double* wx[3];
+};
+
+__global__ void __launch_bounds__(kAmrT) k_amr_weights(int l1, uint32_t n, const uint64_t* __restrict__ skey,
+                                                       const uint32_t* __restrict__ ord, const float* __restrict__ x,
+                                                       const float* __restrict__ y, const float* __restrict__ z,
+                                                       AmrW W) {
   const double dl1 = (double)l1;
   const double shift = 0.5 / dl1;
+  const double m2d = (dl1 * dl1 * dl1) / (double)n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint64_t node = skey[k];
     const uint32_t i = ord[k];
     const int cx = (int)(node % (uint64_t)l1), cy = (int)((node / (uint64_t)l1) % (uint64_t)l1),
               cz = (int)(node / ((uint64_t)l1 * l1));
-    sx[k] = amr_sep(x[i], amr_fold(((double)cx / dl1 + shift) + 1.0), dl1);
-    sy[k] = amr_sep(y[i], amr_fold(((double)cy / dl1 + shift) + 1.0), dl1);
-    sz[k] = amr_sep(z[i], amr_fold(((double)cz / dl1 + shift) + 1.0), dl1);
+    const double sx = amr_sep(x[i], amr_fold(((double)cx / dl1 + shift) + 1.0), dl1);
+    const double sy = amr_sep(y[i], amr_fold(((double)cy / dl1 + shift) + 1.0), dl1);
+    const double sz = amr_sep(z[i], amr_fold(((double)cz / dl1 + shift) + 1.0), dl1);
+#pragma unroll
+    for (int o = 0; o < 3; o++) {
+      W.az[o][k] = m2d * amr_w(sz, o - 1);
+      W.wy[o][k] = amr_w(sy, o - 1);
+      W.wx[o][k] = amr_w(sx, o - 1);
+    }
   }
 }
 
-__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, uint64_t n, const uint32_t* __restrict__ start,
-                                                    const double* __restrict__ sx, const double* __restrict__ sy,
-                                                    const double* __restrict__ sz, float* __restrict__ dens) {
+__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, const uint32_t* __restrict__ start, AmrW W,
+                                                    float* __restrict__ dens) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nn) return;
   const int tx = (int)(t % (uint64_t)l1), ty = (int)((t / (uint64_t)l1) % (uint64_t)l1),
             tz = (int)(t / ((uint64_t)l1 * l1));
-  const double dl1 = (double)l1;
-  const double m2d = (dl1 * dl1 * dl1) / (double)n;
   int sz3[3], sy3[3], sx3[3];
   amr_three(tz, l1, sz3);
   amr_three(ty, l1, sy3);
@@ -128,18 +139,27 @@ __global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, uint64_t n, const ui
   for (int a = 0; a < 3; a++) {
     // offset of the target from the source along z, in {-1, 0, 1}
     const int oz = ((tz - sz3[a] + l1 + 1) % l1) - 1;
+    const double* __restrict__ az = W.az[oz + 1];
     for (int b = 0; b < 3; b++) {
       const int oy = ((ty - sy3[b] + l1 + 1) % l1) - 1;
+      const double* __restrict__ wy = W.wy[oy + 1];
       for (int c = 0; c < 3; c++) {
         const int ox = ((tx - sx3[c] + l1 + 1) % l1) - 1;
+        const double* __restrict__ wx = W.wx[ox + 1];
         const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
         const uint32_t s0 = start[s], s1 = start[s + 1];
-#pragma unroll 4
-        for (uint32_t k = s1; k > s0; k--) {   // list order: descending input index
-          const double wz = amr_w(__ldg(sz + k - 1), oz);
-          const double wy = amr_w(__ldg(sy + k - 1), oy);
-          const double wx = amr_w(__ldg(sx + k - 1), ox);
-          acc = (float)((double)acc + m2d * wz * wy * wx);
+        // list order: descending input index.  Eight terms at a time: their
+        // loads and products are independent, only the float sums chain
+        for (uint32_t k = s1; k > s0;) {
+          const uint32_t m = k - s0 < 8u ? k - s0 : 8u;
+          double tv[8];
+#pragma unroll
+          for (uint32_t j = 0; j < 8; j++)
+            if (j < m) tv[j] = __ldg(az + k - 1 - j) * __ldg(wy + k - 1 - j) * __ldg(wx + k - 1 - j);
+#pragma unroll
+          for (uint32_t j = 0; j < 8; j++)
+            if (j < m) acc = (float)((double)acc + tv[j]);
+          k -= m;
         }
       }
     }
@@ -223,11 +243,16 @@ void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l
 }
 
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint64_t* skey, const uint32_t* ord, double* seps, float* dens, int grid, cudaStream_t st) {
+              const uint64_t* skey, const uint32_t* ord, double* wts, float* dens, int grid, cudaStream_t st) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
-  double *sx = seps, *sy = seps + n, *sz = seps + 2 * n;
-  k_amr_seps<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, sx, sy, sz);
-  k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, n, start, sx, sy, sz, dens);
+  AmrW W;
+  for (int o = 0; o < 3; o++) {
+    W.az[o] = wts + (uint64_t)o * n;
+    W.wy[o] = wts + (uint64_t)(3 + o) * n;
+    W.wx[o] = wts + (uint64_t)(6 + o) * n;
+  }
+  k_amr_weights<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, W);
+  k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, start, W, dens);
 }
 
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st) {

@@ -60,7 +60,7 @@ void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaS
 void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l1, uint64_t* key, uint32_t* idx,
                uint32_t* count, int grid, cudaStream_t st);
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint64_t* skey, const uint32_t* ord, double* seps, float* dens, int grid, cudaStream_t st);
+              const uint64_t* skey, const uint32_t* ord, double* wts, float* dens, int grid, cudaStream_t st);
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st);
 void amr_emit(int l1, const uint8_t* flag, const uint32_t* rowcnt, const uint32_t* rowoff, int64_t cap, int32_t* zyx,
               int* err, cudaStream_t st);
@@ -1442,7 +1442,7 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
       (rc = g.am_idxb.ensure(n * 4)) || (rc = g.am_cnt.ensure(nn * 4)) || (rc = g.am_start.ensure((nn + 1) * 4)) ||
       (rc = g.am_sums.ensure(((nn + 2047) / 2048) * 4)) || (rc = g.am_gh.ensure((size_t)m * 4)) ||
       (rc = g.am_goff.ensure((size_t)m * 4)) || (rc = g.am_part.ensure((size_t)nb * 4)) ||
-      (rc = g.am_err.ensure(64)) || (rc = g.am_seps.ensure(n * 24)))
+      (rc = g.am_err.ensure(64)) || (rc = g.am_seps.ensure(n * 72)))
     return rc;
   CK(cudaMemsetAsync(g.am_cnt.p, 0, nn * 4, st));
   CK(cudaMemsetAsync(g.am_err.p, 0, 64, st));

@@ -27,7 +27,7 @@ scaling, no collective on the data path.
 twice and prints its device time (the cases the profiles/ summaries were
 captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, one of ~2e5,
 the gather on the lists of 5e3 haloes as a snapshot, the Hilbert sort of
-5e7 uniform points.
+5e7 uniform points, the AMR first levels of the 256^3-particle cfg2 box.
 """
 from __future__ import annotations
 
@@ -70,7 +70,7 @@ def parse():
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
     ap.add_argument("--no-amr", action="store_true", help="skip the AMR first-levels leg")
     ap.add_argument("--multimass", action="store_true")
-    ap.add_argument("--case", default=None, choices=["small", "medium", "big", "gather", "sfc"],
+    ap.add_argument("--case", default=None, choices=["small", "medium", "big", "gather", "sfc", "amr"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--case-arg", type=float, default=None, help="gather: halo scale; sfc: points")
     return ap.parse_args()
@@ -929,6 +929,22 @@ def profile_case(args) -> None:
             ms.append(e0.elapsed_time(e1))
         ok = bool((keys[1:] >= keys[:-1]).all().item())
         print(f"sfc: points {n} ascending {ok} ms per call {', '.join(f'{m:.2f}' for m in ms)}")
+        return
+    if args.case == "amr":
+        S = synth.box_snapshot("cfg2")
+        p = (S.pos / np.float32(S.box)).astype(np.float32)
+        x, y, z = (torch.as_tensor(np.ascontiguousarray(p[:, k])).cuda() for k in range(3))
+        ms = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dens = lib.amr_domain_density_device(x, y, z, 64)
+            fine = lib.amr_first_refinement_device(dens, 64, len(S.ids), 5.0)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        print(f"amr: particles {len(S.ids)} l1 64 fine nodes {int(fine.shape[0])} "
+              f"ms per call {', '.join(f'{m:.2f}' for m in ms)}")
         return
     scale = (args.case_arg or 0.05) if args.case == "gather" else 0.05
     L = synth.generate("cfg3", scale=scale, device="cuda", as_numpy=False)
