@@ -27,6 +27,7 @@ UNITS = {
     "fp32c_class1.cu": ["--fmad=false"],
     "fp32c_class2.cu": ["--fmad=false"],
     "fp32c_finish.cu": ["--fmad=false"],
+    "fp32c_small.cu": ["--fmad=false"],
     "fp32c_dispatch.cu": [],
     "noalloc.cu": [],
     "gather.cu": [],

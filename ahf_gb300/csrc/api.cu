@@ -27,6 +27,11 @@ void launch_fp64(const DevParams& P, const DevBatch& B, const Work& W, int grid,
 int fp64_max_blocks_per_sm();
 void launch_fp32c(int cls, const DevParams& P, const DevBatch& B, const Work& W, int grid, cudaStream_t st);
 int fp32c_max_blocks_per_sm(int cls);
+// the small lists of the FP32C form, one per thread (fp32c_small.cu)
+void launch_fp32c_small(const DevParams& P, const DevBatch& B, const Work& W, unsigned char* scratch, uint32_t nmax,
+                        int grid, cudaStream_t st);
+size_t fp32c_small_bytes_per_warp(uint64_t nmax);
+int fp32c_small_occupancy();
 uint64_t fp32c_class_max(int cls);
 void fp32c_set_class_max(uint64_t a, uint64_t b);
 void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
@@ -174,6 +179,9 @@ struct Ctx {
   // device-resident calls: the launch sequence as a CUDA graph, re-launched
   // while the launches (kernels, grids, arguments) stay the same
   bool use_graph = true;
+  bool small_on = true;        // FP32C class 0 by the one-list-per-thread kernel
+  int small_bps = 1;           // its blocks (128 threads) per SM
+  DBuf small_scr;              // its work space
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<unsigned char> graph_sig;
   uint64_t graph_launches = 0, graph_replays = 0;
@@ -485,7 +493,10 @@ std::vector<Seg> fp32c_segments(const Plan& pl) {
       int q1 = std::min(pl.cls_begin[k + 1], part_end(pl, p));
       if (q1 <= q0) continue;
       int cls = 2 - k;
-      v.push_back({p, cls, q0, q1, std::min(g.nsm * g.fp32c_bps[cls], q1 - q0)});
+      if (cls == 0 && g.small_on)   // blocks of 128 threads, one list per thread
+        v.push_back({p, cls, q0, q1, std::min(g.nsm * g.small_bps, (q1 - q0 + 127) / 128)});
+      else
+        v.push_back({p, cls, q0, q1, std::min(g.nsm * g.fp32c_bps[cls], q1 - q0)});
     }
   return v;
 }
@@ -512,6 +523,17 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
   }
   const int stack_cap = (int)std::min<uint64_t>(std::max<uint64_t>(pl.maxn / 512 + 64, 64), 1u << 20);
   if ((rc = ensure_work(pl, grid, stack_cap))) return rc;
+  // the small-list kernel's work space: per class-0 segment, per warp
+  const uint32_t small_nmax = (uint32_t)std::min<uint64_t>(fp32c_class_max(0), std::max<uint64_t>(pl.maxn, 1));
+  std::vector<size_t> small_off;
+  if (mode == AHFGPU_BATCHED_FP32C && g.small_on) {
+    size_t tot = 0;
+    for (const Seg& sg : segs) {
+      small_off.push_back(tot);
+      if (sg.cls == 0) tot += (size_t)sg.grid * 4 * fp32c_small_bytes_per_warp(small_nmax);
+    }
+    if (tot && (rc = g.small_scr.ensure(tot))) return rc;
+  }
   const int64_t nh = pl.nhalo;
   stats->n_particles_in = pl.N;
   if (nh == 0) {
@@ -652,7 +674,11 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
         cudaStream_t cs = g.seg_stream[sg.part][sg.cls];
         CK(cudaStreamWaitEvent(cs, g.ev_fork, 0));
         if (stage) CK(cudaStreamWaitEvent(cs, g.ev_part[sg.part], 0));
-        launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
+        if (sg.cls == 0 && g.small_on)
+          launch_fp32c_small(P, B, Wc, g.small_scr.as<unsigned char>() + small_off[&sg - segs.data()], small_nmax,
+                             sg.grid, cs);
+        else
+          launch_fp32c(sg.cls, P, B, Wc, sg.grid, cs);
         CK(cudaEventRecord(g.ev_join[sg.part][sg.cls], cs));
         CK(cudaStreamWaitEvent(st, g.ev_join[sg.part][sg.cls], 0));
         launches++;
@@ -704,6 +730,9 @@ int run_device(const ahfgpu_params* prm, const ahfgpu_batch* db, const Plan& pl,
     put(&stack_cap, sizeof stack_cap);
     put(&st, sizeof st);
     for (const Seg& sg : segs) put(&sg, sizeof sg);
+    put(&g.small_on, sizeof g.small_on);
+    put(&g.small_scr.p, sizeof g.small_scr.p);
+    put(&small_nmax, sizeof small_nmax);
     const void* outs[6] = {db->off, db->gidx, g.member_off.p, g.prof_off.p, g.member.p, g.prof.p};
     put(outs, sizeof outs);
     if (g.graph_exec && sig == g.graph_sig) {
@@ -887,6 +916,9 @@ static int init_impl(int device) {
   {
     const char* e = getenv("AHFGPU_GRAPH");   // "0": device-resident calls launch directly
     g.use_graph = !(e && e[0] == '0');
+    const char* sm = getenv("AHFGPU_SMALL");  // "0": the small lists on 64-thread CTAs instead
+    g.small_on = !(sm && sm[0] == '0');
+    g.small_bps = std::max(1, fp32c_small_occupancy());
   }
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
@@ -933,7 +965,7 @@ int ahfgpu_shutdown(void) {
                   &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
                   &g.sfc_err, &g.phase, &g.am_key, &g.am_keyb, &g.am_idx, &g.am_idxb, &g.am_cnt,
                   &g.am_start, &g.am_sums, &g.am_gh, &g.am_goff, &g.am_part, &g.am_err, &g.am_flag,
-                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums, &g.am_seps};
+                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums, &g.am_seps, &g.small_scr};
   for (DBuf* b : bufs) b->release();
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
