@@ -33,7 +33,7 @@ void launch_fp32c_small(const DevParams& P, const DevBatch& B, const Work& W, un
 size_t fp32c_small_bytes_per_warp(uint64_t nmax);
 int fp32c_small_occupancy();
 uint64_t fp32c_class_max(int cls);
-void fp32c_set_class_max(uint64_t a, uint64_t b);
+void fp32c_set_class_max(uint64_t a, uint64_t b, uint64_t cap0);
 void launch_concentration(ahfgpu_halo* halo, int64_t nh, int grid, cudaStream_t st);
 void launch_fp32c_finish(const DevParams& P, const DevBatch& B, ahfgpu_halo* halo, const uint64_t* prof_cap_off,
                          double* prof_stage, const double* fin, int64_t nh, int grid, cudaStream_t st);
@@ -373,6 +373,9 @@ int nbins_cap(uint64_t n, int64_t minpart) {
   nb = std::max(2, nb) + 1;            // +1: device log10 may differ by an ulp
   return std::min(nb, kMaxBins);
 }
+
+// the longest list the one-list-per-thread kernel may be given (class 0)
+constexpr uint64_t kSmallMaxList = 1024;
 
 // batches below this many particles are copied in one piece
 constexpr uint64_t kSplitMinParticles = 1u << 22;
@@ -869,7 +872,7 @@ void load_tuning(const cudaDeviceProp& prop) {
       g.tune_source = "environment";
     }
   }
-  fp32c_set_class_max(g.tune_class_max[0], g.tune_class_max[1]);
+  fp32c_set_class_max(g.tune_class_max[0], g.tune_class_max[1], g.small_on ? kSmallMaxList : 512);
   g.tune_class_max[0] = fp32c_class_max(0);
   g.tune_class_max[1] = fp32c_class_max(1);
 }
@@ -911,8 +914,6 @@ static int init_impl(int device) {
   CK(cudaEventCreate(&g.ev0));
   CK(cudaEventCreate(&g.ev1));
   g.fp64_bps = std::max(1, fp64_max_blocks_per_sm());
-  load_tuning(prop);
-  CK((cudaError_t)gather_sort_setup());
   {
     const char* e = getenv("AHFGPU_GRAPH");   // "0": device-resident calls launch directly
     g.use_graph = !(e && e[0] == '0');
@@ -920,6 +921,8 @@ static int init_impl(int device) {
     g.small_on = !(sm && sm[0] == '0');
     g.small_bps = std::max(1, fp32c_small_occupancy());
   }
+  load_tuning(prop);
+  CK((cudaError_t)gather_sort_setup());
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
     if (g.tune_bps_cap[k] >= 1) g.fp32c_bps[k] = std::min(g.fp32c_bps[k], g.tune_bps_cap[k]);

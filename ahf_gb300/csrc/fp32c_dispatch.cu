@@ -17,12 +17,15 @@ int fp32c_occupancy_class0();
 int fp32c_occupancy_class1();
 int fp32c_occupancy_class2();
 
-// Largest list of classes 0 and 1 (class 0 is bounded by its 512-pair
-// shared-memory sort).  Set once per device by the tuning at ahfgpu_init.
+// Largest list of classes 0 and 1.  Set once per device by the tuning at
+// ahfgpu_init.
 static uint64_t g_class_max[2] = {512, 16384};
 
-void fp32c_set_class_max(uint64_t a, uint64_t b) {
-  a = a < 1 ? 1 : (a > 512 ? 512 : a);
+// cap0: the largest class-0 list the class-0 kernel takes (512 for the
+// 64-thread CTAs, whose shared-memory sort holds 512 pairs; more for the
+// one-list-per-thread kernel, whose work space is sized per call)
+void fp32c_set_class_max(uint64_t a, uint64_t b, uint64_t cap0) {
+  a = a < 1 ? 1 : (a > cap0 ? cap0 : a);
   g_class_max[0] = a;
   g_class_max[1] = b < a ? a : b;
 }
