@@ -25,7 +25,9 @@ scaling, no collective on the data path.
 
 `--case small|medium|big|gather|sfc` runs one small device-resident case
 twice and prints its device time (the cases the profiles/ summaries were
-captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, one of ~2e5,
+captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, the 160
+lists nearest 1e5 entries of a 1.5e4-halo batch (about one per SM, as at full
+load), one of ~2e5,
 the gather on the lists of 5e3 haloes as a snapshot, the Hilbert sort of
 5e7 uniform points, the AMR first levels of the 256^3-particle cfg2 box.
 """
@@ -70,7 +72,7 @@ def parse():
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
     ap.add_argument("--no-amr", action="store_true", help="skip the AMR first-levels leg")
     ap.add_argument("--multimass", action="store_true")
-    ap.add_argument("--case", default=None, choices=["small", "medium", "big", "gather", "sfc", "amr"],
+    ap.add_argument("--case", default=None, choices=["small", "medium", "large", "big", "gather", "sfc", "amr"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--case-arg", type=float, default=None, help="gather: halo scale; sfc: points")
     return ap.parse_args()
@@ -947,7 +949,7 @@ def profile_case(args) -> None:
               f"ms per call {', '.join(f'{m:.2f}' for m in ms)}")
         return
     scale = (args.case_arg or 0.05) if args.case == "gather" else 0.05
-    L = synth.generate("cfg3", scale=scale, device="cuda", as_numpy=False)
+    L = synth.generate("cfg3", scale=0.15 if args.case == "large" else scale, device="cuda", as_numpy=False)
     n = np.diff(L.off.astype(np.int64))
     if args.case == "gather":
         rad = gather_radii(L, n)
@@ -968,6 +970,8 @@ def profile_case(args) -> None:
         sel = np.nonzero(n <= 512)[0][:3000]
     elif args.case == "medium":
         sel = np.nonzero((n > 2048) & (n <= 16384))[0][:300]
+    elif args.case == "large":
+        sel = np.sort(np.argsort(np.abs(n - 100000), kind="stable")[:160])
     else:
         sel = np.array([int(np.argmin(np.abs(n - 200000)))])
     p = synth.params_for(L)
