@@ -23,7 +23,7 @@ other ranks exit).  Under torchrun every rank builds the same batch and runs
 its share of the haloes (the library's LPT split, ahfgpu_shard_halos): strong
 scaling, no collective on the data path.
 
-`--case small|medium|big|gather|sfc` runs one small device-resident case
+`--case small|medium|large|big|gather|sfc|amr` runs one small device-resident case
 twice and prints its device time (the cases the profiles/ summaries were
 captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, the 160
 lists nearest 1e5 entries of a 1.5e4-halo batch (about one per SM, as at full
