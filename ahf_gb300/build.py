@@ -3,7 +3,7 @@
 Each translation unit is compiled by nvcc in parallel and linked into one
 shared library with the CUDA runtime linked statically, so the library only
 needs the CUDA driver at run time.  The stage's units (halo_fp64.cu,
-fp32c_*.cu, amr.cu) are compiled with --fmad=false: their FP64 paths must round like
+fp32c_*.cu, amr*.cu) are compiled with --fmad=false: their FP64 paths must round like
 the reference's C build, and the float-float arithmetic needs its products
 and sums unfused.
 """
@@ -35,6 +35,7 @@ UNITS = {
     "sfc.cu": [],
     "shard.cu": [],
     "amr.cu": ["--fmad=false"],
+    "amr_tree.cu": ["--fmad=false"],
 }
 
 

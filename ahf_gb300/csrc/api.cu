@@ -20,6 +20,7 @@
 #include <dlfcn.h>
 
 #include "common.cuh"
+#include "amr_tree.cuh"
 
 namespace ahfgpu {
 size_t fp64_smem_bytes();
@@ -213,6 +214,22 @@ struct Ctx {
   DBuf sfc_kb, sfc_ia, sfc_ib, sfc_gh, sfc_goff, sfc_part, sfc_err;   // the SFC key sort
   DBuf am_key, am_keyb, am_idx, am_idxb, am_cnt, am_start, am_sums;    // AMR: particles by domain node
   DBuf am_gh, am_goff, am_part, am_err, am_flag, am_rowcnt, am_rowoff, am_rsums, am_seps;
+  // the AMR hierarchy: every kept grid's run tables, nodes, TSC table,
+  // flags, densities and particle lists (slot k: particle ord[k] of node
+  // node[k]; node s's slots start[s] .. start[s + 1] - 1)
+  struct AmrLevel {
+    int l1 = 0, nP = 0, npl = 0, nC = 0, nR = 0, nN = 0, nn = 0;
+    uint32_t np = 0;
+    DBuf P, pl, C, R, N, key, nseg, tsc, flag, dens, start, ord, node;
+  };
+  static constexpr int kAmrMaxGrids = 40;
+  AmrLevel amr_lv[kAmrMaxGrids + 1];
+  int amr_nlev = 0;
+  // ... and its scratch: row and plane state machines, fine planes, relink,
+  // the radix passes, the density pairs
+  DBuf at_rrun, at_rnode, at_rref, at_runoff, at_runs, at_pref, at_po, at_pnc, at_pnsel, at_rroff, at_seloff;
+  DBuf at_rr, at_sel, at_fpl, at_tot, at_dest, at_moved, at_moff, at_cnt, at_kA, at_kB, at_iA, at_iB;
+  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt, at_tstart;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -968,8 +985,16 @@ int ahfgpu_shutdown(void) {
                   &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
                   &g.sfc_err, &g.phase, &g.am_key, &g.am_keyb, &g.am_idx, &g.am_idxb, &g.am_cnt,
                   &g.am_start, &g.am_sums, &g.am_gh, &g.am_goff, &g.am_part, &g.am_err, &g.am_flag,
-                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums, &g.am_seps, &g.small_scr};
+                  &g.am_rowcnt, &g.am_rowoff, &g.am_rsums, &g.am_seps, &g.small_scr, &g.at_rrun, &g.at_rnode,
+                  &g.at_rref, &g.at_runoff, &g.at_runs, &g.at_pref, &g.at_po, &g.at_pnc, &g.at_pnsel, &g.at_rroff,
+                  &g.at_seloff, &g.at_rr, &g.at_sel, &g.at_fpl, &g.at_tot, &g.at_dest, &g.at_moved, &g.at_moff,
+                  &g.at_cnt, &g.at_kA, &g.at_kB, &g.at_iA, &g.at_iB, &g.at_gh, &g.at_goff, &g.at_part, &g.at_err,
+                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt, &g.at_tstart};
   for (DBuf* b : bufs) b->release();
+  for (Ctx::AmrLevel& L : g.amr_lv)
+    for (DBuf* b : {&L.P, &L.pl, &L.C, &L.R, &L.N, &L.key, &L.nseg, &L.tsc, &L.flag, &L.dens, &L.start, &L.ord, &L.node})
+      b->release();
+  g.amr_nlev = 0;
   for (int p = 0; p < kMaxParts; p++)
     for (int k = 0; k < 3; k++) {
       if (g.seg_stream[p][k]) cudaStreamDestroy(g.seg_stream[p][k]);
@@ -1461,16 +1486,13 @@ static int sfc_sort_device_impl(uint64_t n, const float* x, const float* y, cons
   return AHFGPU_OK;
 }
 
-static int amr_domain_density_device_impl(uint64_t n, const float* x, const float* y, const float* z, int l1,
-                                          float* dens, void* stream) {
-  int rc = ensure_init();
-  if (rc) return rc;
-  if (n == 0) return fail(AHFGPU_ERR_INVALID, "amr: no particles");
-  if (n >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "amr: %llu particles (limit 2^31 - 1)",
-                                     (unsigned long long)n);
-  if (l1 < 3 || l1 > 1024) return fail(AHFGPU_ERR_INVALID, "amr: domain grid %d outside 3..1024", l1);
-  if (!x || !y || !z || !dens) return fail(AHFGPU_ERR_INVALID, "amr: a pointer is NULL");
-  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+// the particles of the domain grid's lists (ll, lltools.c): node of every
+// particle (floor(l1 x) per axis, an index past l1 - 1 folded to node 0),
+// list starts in g.am_start, and the particles by node with ascending index
+// within a node (stable radix sort) in *key / *idx
+static int amr_domain_lists(uint64_t n, const float* x, const float* y, const float* z, int l1, cudaStream_t st,
+                            uint64_t** key, uint32_t** idx) {
+  int rc;
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
   const uint32_t n32 = (uint32_t)n, nt = sfc_ntiles(n32), m = 256u * nt, nb = sfc_scan_blocks(m);
   if ((rc = g.am_key.ensure(n * 8)) || (rc = g.am_keyb.ensure(n * 8)) || (rc = g.am_idx.ensure(n * 4)) ||
@@ -1484,7 +1506,6 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
   amr_cells(n32, x, y, z, l1, g.am_key.as<uint64_t>(), g.am_idx.as<uint32_t>(), g.am_cnt.as<uint32_t>(), grid, st);
   gather_scan_u32(g.am_cnt.as<uint32_t>(), g.am_start.as<uint32_t>(), nn, g.am_sums.as<uint32_t>(), st);
-  // particles by node, ascending index within a node (stable radix sort)
   int bits = 1;
   while ((1ull << bits) < nn) bits++;
   uint64_t *kin = g.am_key.as<uint64_t>(), *kout = g.am_keyb.as<uint64_t>();
@@ -1495,6 +1516,30 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
     std::swap(kin, kout);
     std::swap(iin, iout);
   }
+  *key = kin;
+  *idx = iin;
+  return AHFGPU_OK;
+}
+
+static int amr_domain_check(uint64_t n, int l1) {
+  if (n == 0) return fail(AHFGPU_ERR_INVALID, "amr: no particles");
+  if (n >= (1ull << 31)) return fail(AHFGPU_ERR_CAPACITY, "amr: %llu particles (limit 2^31 - 1)",
+                                     (unsigned long long)n);
+  if (l1 < 3 || l1 > 1024) return fail(AHFGPU_ERR_INVALID, "amr: domain grid %d outside 3..1024", l1);
+  return AHFGPU_OK;
+}
+
+static int amr_domain_density_device_impl(uint64_t n, const float* x, const float* y, const float* z, int l1,
+                                          float* dens, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if ((rc = amr_domain_check(n, l1))) return rc;
+  if (!x || !y || !z || !dens) return fail(AHFGPU_ERR_INVALID, "amr: a pointer is NULL");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  uint64_t* kin;
+  uint32_t* iin;
+  if ((rc = amr_domain_lists(n, x, y, z, l1, st, &kin, &iin))) return rc;
+  const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
   amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), dens, grid, st);
   CK(cudaGetLastError());
   int derr = 0;
@@ -1540,6 +1585,259 @@ static int amr_first_refinement_device_impl(int l1, const float* dens, uint64_t 
   CK(cudaMemcpyAsync(&derr, g.am_err.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (derr) return fail(AHFGPU_ERR_CUDA, "amr: a fine node left the output buffer");
+  return AHFGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// the AMR hierarchy (gen_AMRhierarchy, src/libamr_serial/generate_grids.c:278,
+// called from src/main.c:614-648): the domain grid as above, then, while the
+// finest grid is below ngrid_max, refine it (threshold critdens - mean_dens,
+// critdens = NperDomCell m2d on the domain grid and NperRefCell m2d below,
+// m2d = ngrid_dom^3 / n times 8 per level), relink the particles and assign
+// the refined grid's densities; a refined grid of fewer than MIN_NNODES =
+// 125 nodes is dropped and ends the hierarchy.  The run tables and the state
+// machines are in amr_tree.cu.
+
+static AGrid agrid_of(const Ctx::AmrLevel& L) {
+  AGrid a;
+  a.l1 = L.l1; a.nP = L.nP; a.npl = L.npl; a.nC = L.nC; a.nR = L.nR; a.nN = L.nN; a.nn = L.nn;
+  a.P = L.P.as<APRun>(); a.pl = L.pl.as<APlane>(); a.C = L.C.as<ACRun>(); a.R = L.R.as<ARow>();
+  a.N = L.N.as<ANRun>(); a.key = L.key.as<uint64_t>(); a.nseg = L.nseg.as<int>();
+  return a;
+}
+
+// exclusive scan of m counts, the total at out[m]
+static int amr_scan(const uint32_t* in, uint32_t* out, uint64_t m, cudaStream_t st) {
+  int rc;
+  if (m == 0) {
+    CK(cudaMemsetAsync(out, 0, 4, st));
+    return AHFGPU_OK;
+  }
+  if ((rc = g.at_sums.ensure(((m + 2047) / 2048) * 4))) return rc;
+  gather_scan_u32(in, out, m, g.at_sums.as<uint32_t>(), st);
+  return AHFGPU_OK;
+}
+
+// stable radix sort of n (key, value) pairs on the low `bits` bits of the
+// keys; the result is in (*k, *v), the other pair of buffers is scratch
+static int amr_radix(uint32_t n, int bits, uint64_t** k, uint32_t** v, uint64_t** kb, uint32_t** vb,
+                     cudaStream_t st) {
+  int rc;
+  if (n == 0) return AHFGPU_OK;
+  const uint32_t nt = sfc_ntiles(n), m = 256u * nt, nb = sfc_scan_blocks(m);
+  if ((rc = g.at_gh.ensure((size_t)m * 4)) || (rc = g.at_goff.ensure((size_t)m * 4)) ||
+      (rc = g.at_part.ensure((size_t)nb * 4)))
+    return rc;
+  for (int shift = 0; shift < bits; shift += 8) {
+    sfc_pass(n, *k, *v, shift, g.at_gh.as<uint32_t>(), g.at_goff.as<uint32_t>(), g.at_part.as<uint32_t>(), *kb, *vb,
+             g.at_err.as<int>(), st);
+    std::swap(*k, *kb);
+    std::swap(*v, *vb);
+  }
+  return AHFGPU_OK;
+}
+
+static int amr_bits(uint64_t m) {
+  int b = 1;
+  while ((1ull << b) < m) b++;
+  return b;
+}
+
+static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y, const float* z, int ngrid_dom,
+                                     int ngrid_max, double nth_dom, double nth_ref, int64_t* levels, int max_levels,
+                                     int* ngrids, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!ngrids) return fail(AHFGPU_ERR_INVALID, "amr: ngrids is NULL");
+  *ngrids = 0;
+  g.amr_nlev = 0;
+  if ((rc = amr_domain_check(n, ngrid_dom))) return rc;
+  if (ngrid_max < ngrid_dom || ngrid_max > (1 << 20))
+    return fail(AHFGPU_ERR_INVALID, "amr: ngrid_max %d outside %d..2^20", ngrid_max, ngrid_dom);
+  if (!x || !y || !z) return fail(AHFGPU_ERR_INVALID, "amr: a pointer is NULL");
+  if (max_levels < 0 || (max_levels > 0 && !levels)) return fail(AHFGPU_ERR_INVALID, "amr: bad levels buffer");
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  const int L = ngrid_dom;
+  const uint64_t nn0 = (uint64_t)L * L * L;
+  if ((rc = g.at_err.ensure(64)) || (rc = g.at_tot.ensure(sizeof(AFineTotals)))) return rc;
+  CK(cudaMemsetAsync(g.at_err.p, 0, 64, st));
+
+  // the domain grid: lists, densities, run tables, TSC table
+  uint64_t* kin;
+  uint32_t* iin;
+  if ((rc = amr_domain_lists(n, x, y, z, L, st, &kin, &iin))) return rc;
+  Ctx::AmrLevel& d = g.amr_lv[0];
+  if ((rc = d.P.ensure(sizeof(APRun))) || (rc = d.pl.ensure(sizeof(APlane) * L)) ||
+      (rc = d.C.ensure(sizeof(ACRun) * L)) || (rc = d.R.ensure(sizeof(ARow) * (size_t)L * L)) ||
+      (rc = d.N.ensure(sizeof(ANRun) * (size_t)L * L)) || (rc = d.key.ensure(nn0 * 8)) ||
+      (rc = d.nseg.ensure(nn0 * 4)) || (rc = d.tsc.ensure(nn0 * 108)) || (rc = d.flag.ensure(nn0)) ||
+      (rc = d.dens.ensure(nn0 * 4)) || (rc = d.start.ensure((nn0 + 1) * 4)) || (rc = d.ord.ensure(n * 4)) ||
+      (rc = d.node.ensure(n * 8)))
+    return rc;
+  d.l1 = L; d.nP = 1; d.npl = L; d.nC = L; d.nR = L * L; d.nN = L * L; d.nn = (int)nn0; d.np = (uint32_t)n;
+  const int pgrid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
+  amr_dens(L, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), d.dens.as<float>(), pgrid, st);
+  CK(cudaMemcpyAsync(d.ord.p, iin, n * 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.node.p, kin, n * 8, cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(d.start.p, g.am_start.p, (nn0 + 1) * 4, cudaMemcpyDeviceToDevice, st));
+  ag_domain(L, d.P.as<APRun>(), d.pl.as<APlane>(), d.C.as<ACRun>(), d.R.as<ARow>(), d.N.as<ANRun>(),
+            d.key.as<uint64_t>(), d.nseg.as<int>(), st);
+  ag_tsc(agrid_of(d), d.tsc.as<int>(), d.flag.as<uint8_t>(), st);
+  CK(cudaGetLastError());
+  if (max_levels > 0) { levels[0] = L; levels[1] = (int64_t)nn0; levels[2] = (int64_t)n; }
+  int ng = 1;
+  const double dl = (double)L;
+  double m2d = (dl * dl * dl) / (double)n;
+  double thr = nth_dom * m2d - 1.0;
+
+  while (ng < Ctx::kAmrMaxGrids) {
+    Ctx::AmrLevel& c = g.amr_lv[ng - 1];
+    Ctx::AmrLevel& f = g.amr_lv[ng];
+    if (c.l1 >= ngrid_max) break;
+    const AGrid gc = agrid_of(c);
+    // refine: test_node, rows, planes, plane runs
+    ag_test(c.nn, c.tsc.as<int>(), c.dens.as<float>(), thr, c.flag.as<uint8_t>(), st);
+    const uint64_t runs_cap = (uint64_t)c.nn + 2ull * c.nN + 1;
+    if ((rc = g.at_rrun.ensure((size_t)c.nR * 4 + 4)) || (rc = g.at_rnode.ensure((size_t)c.nR * 4 + 4)) ||
+        (rc = g.at_rref.ensure((size_t)c.nR + 1)) || (rc = g.at_runoff.ensure(((size_t)c.nR + 1) * 4)) ||
+        (rc = g.at_runs.ensure(runs_cap * 8)) || (rc = g.at_pref.ensure((size_t)c.npl + 1)) ||
+        (rc = g.at_po.ensure(sizeof(APlaneOut) * ((size_t)c.npl + 1))) ||
+        (rc = g.at_pnc.ensure((size_t)c.npl * 4 + 4)) || (rc = g.at_pnsel.ensure((size_t)c.npl * 4 + 4)) ||
+        (rc = g.at_rroff.ensure(((size_t)c.npl + 1) * 4)) || (rc = g.at_seloff.ensure(((size_t)c.npl + 1) * 4)) ||
+        (rc = g.at_rr.ensure(((size_t)c.nR + 1) * 8)) || (rc = g.at_sel.ensure(((size_t)c.nR + 1) * 4)) ||
+        (rc = g.at_fpl.ensure(sizeof(AFPlane) * (2 * (size_t)c.npl + 2))) ||
+        (rc = f.P.ensure(sizeof(APRun) * ((size_t)c.npl + 1))))
+      return rc;
+    ag_rows(gc, c.flag.as<uint8_t>(), g.at_rrun.as<uint32_t>(), g.at_rnode.as<uint32_t>(), g.at_rref.as<uint8_t>(), st);
+    if ((rc = amr_scan(g.at_rrun.as<uint32_t>(), g.at_runoff.as<uint32_t>(), c.nR, st))) return rc;
+    ag_rows_emit(gc, c.flag.as<uint8_t>(), g.at_runoff.as<uint32_t>(), g.at_runs.as<int2>(), st);
+    ag_planes(gc, g.at_rref.as<uint8_t>(), g.at_rrun.as<uint32_t>(), g.at_rnode.as<uint32_t>(),
+              g.at_pref.as<uint8_t>(), g.at_po.as<APlaneOut>(), g.at_pnc.as<uint32_t>(), g.at_pnsel.as<uint32_t>(), st);
+    if ((rc = amr_scan(g.at_pnc.as<uint32_t>(), g.at_rroff.as<uint32_t>(), c.npl, st)) ||
+        (rc = amr_scan(g.at_pnsel.as<uint32_t>(), g.at_seloff.as<uint32_t>(), c.npl, st)))
+      return rc;
+    ag_planes_emit(gc, g.at_rref.as<uint8_t>(), g.at_rrun.as<uint32_t>(), g.at_rnode.as<uint32_t>(),
+                   g.at_rroff.as<uint32_t>(), g.at_seloff.as<uint32_t>(), g.at_rr.as<int2>(), g.at_sel.as<int>(), st);
+    ag_pquad(gc, g.at_pref.as<uint8_t>(), g.at_po.as<APlaneOut>(), f.P.as<APRun>(), g.at_fpl.as<AFPlane>(),
+             g.at_tot.as<AFineTotals>(), st);
+    CK(cudaGetLastError());
+    AFineTotals T;
+    uint32_t nruns = 0;
+    CK(cudaMemcpyAsync(&T, g.at_tot.p, sizeof T, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&nruns, g.at_runoff.as<uint32_t>() + c.nR, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if ((uint64_t)nruns > runs_cap) return fail(AHFGPU_ERR_STATE, "amr: %u fine node runs past the bound", nruns);
+    if (!T.refined) break;
+    if (T.err) return fail(AHFGPU_ERR_CAPACITY, "amr: the refined grid of %d^3 exceeds 2^31 - 1 entries", 2 * c.l1);
+    f.l1 = 2 * c.l1; f.nP = T.nP; f.npl = T.npl; f.nC = T.nC; f.nR = T.nR; f.nN = T.nN; f.nn = T.nn;
+    const size_t fnn = (size_t)f.nn;
+    if ((rc = f.pl.ensure(sizeof(APlane) * ((size_t)f.npl + 1))) || (rc = f.C.ensure(sizeof(ACRun) * ((size_t)f.nC + 1))) ||
+        (rc = f.R.ensure(sizeof(ARow) * ((size_t)f.nR + 1))) || (rc = f.N.ensure(sizeof(ANRun) * ((size_t)f.nN + 1))) ||
+        (rc = f.key.ensure(fnn * 8 + 8)) || (rc = f.nseg.ensure(fnn * 4 + 4)) || (rc = f.tsc.ensure(fnn * 108 + 108)) ||
+        (rc = f.flag.ensure(fnn + 1)) || (rc = f.dens.ensure(fnn * 4 + 4)) || (rc = f.start.ensure((fnn + 1) * 4)))
+      return rc;
+    ag_fplanes(f.npl, g.at_fpl.as<AFPlane>(), g.at_rroff.as<uint32_t>(), g.at_seloff.as<uint32_t>(),
+               g.at_po.as<APlaneOut>(), g.at_rr.as<int2>(), g.at_sel.as<int>(), gc, g.at_runoff.as<uint32_t>(),
+               g.at_runs.as<int2>(), f.pl.as<APlane>(), f.C.as<ACRun>(), f.R.as<ARow>(), f.N.as<ANRun>(), st);
+    ag_fnodes(f.nN, f.l1, f.N.as<ANRun>(), f.R.as<ARow>(), f.pl.as<APlane>(), f.key.as<uint64_t>(), f.nseg.as<int>(),
+              st);
+    ag_tsc(agrid_of(f), f.tsc.as<int>(), f.flag.as<uint8_t>(), st);
+
+    // relink: the coarse grid's listed particles to the fine nodes
+    const uint32_t npc = c.np;
+    if ((rc = g.at_dest.ensure((size_t)npc * 4 + 4)) || (rc = g.at_moved.ensure((size_t)npc * 4 + 4)) ||
+        (rc = g.at_moff.ensure(((size_t)npc + 1) * 4)) || (rc = g.at_cnt.ensure((fnn + 1) * 4)) ||
+        (rc = g.at_kA.ensure((size_t)npc * 8 + 8)) || (rc = g.at_kB.ensure((size_t)npc * 8 + 8)) ||
+        (rc = g.at_iA.ensure((size_t)npc * 4 + 4)) || (rc = g.at_iB.ensure((size_t)npc * 4 + 4)))
+      return rc;
+    CK(cudaMemsetAsync(g.at_cnt.p, 0, (fnn + 1) * 4, st));
+    ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, f.key.as<uint64_t>(),
+              f.nn, f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(), st);
+    if ((rc = amr_scan(g.at_moved.as<uint32_t>(), g.at_moff.as<uint32_t>(), npc, st))) return rc;
+    ag_compact(npc, g.at_dest.as<int>(), g.at_moff.as<uint32_t>(), c.ord.as<uint32_t>(), g.at_kA.as<uint64_t>(),
+               g.at_iA.as<uint32_t>(), g.at_cnt.as<uint32_t>(), st);
+    if ((rc = amr_scan(g.at_cnt.as<uint32_t>(), f.start.as<uint32_t>(), fnn, st))) return rc;
+    uint32_t nm = 0;
+    CK(cudaMemcpyAsync(&nm, g.at_moff.as<uint32_t>() + npc, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    uint64_t *k = g.at_kA.as<uint64_t>(), *kb = g.at_kB.as<uint64_t>();
+    uint32_t *v = g.at_iA.as<uint32_t>(), *vb = g.at_iB.as<uint32_t>();
+    if ((rc = amr_radix(nm, amr_bits(fnn), &k, &v, &kb, &vb, st))) return rc;
+    if ((rc = f.ord.ensure((size_t)nm * 4 + 4)) || (rc = f.node.ensure((size_t)nm * 8 + 8))) return rc;
+    if (nm) {
+      CK(cudaMemcpyAsync(f.ord.p, v, (size_t)nm * 4, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemcpyAsync(f.node.p, k, (size_t)nm * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    f.np = nm;
+
+    // densities: the (target, source, slot) pairs by target, then the gather
+    const double m2f = m2d * 8.0;
+    if ((rc = g.at_w.ensure((size_t)nm * 72 + 72)) || (rc = g.at_ne.ensure(fnn * 4 + 4)) ||
+        (rc = g.at_srcoff.ensure((fnn + 1) * 4)) || (rc = g.at_tcnt.ensure((fnn + 1) * 4)) ||
+        (rc = g.at_tstart.ensure((fnn + 1) * 4)))
+      return rc;
+    ag_weights(f.l1, m2f, nm, f.node.as<uint64_t>(), f.key.as<uint64_t>(), f.ord.as<uint32_t>(), x, y, z,
+               g.at_w.as<double>(), st);
+    ag_nonempty(f.nn, f.start.as<uint32_t>(), g.at_ne.as<uint32_t>(), st);
+    if ((rc = amr_scan(g.at_ne.as<uint32_t>(), g.at_srcoff.as<uint32_t>(), fnn, st))) return rc;
+    uint32_t nsrc = 0;
+    CK(cudaMemcpyAsync(&nsrc, g.at_srcoff.as<uint32_t>() + fnn, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const uint64_t npairs = 27ull * nsrc;
+    if (npairs >= (1ull << 32)) return fail(AHFGPU_ERR_CAPACITY, "amr: %llu density pairs", (unsigned long long)npairs);
+    if ((rc = g.at_kA.ensure(npairs * 8 + 8)) || (rc = g.at_kB.ensure(npairs * 8 + 8)) ||
+        (rc = g.at_iA.ensure(npairs * 4 + 4)) || (rc = g.at_iB.ensure(npairs * 4 + 4)))
+      return rc;
+    CK(cudaMemsetAsync(g.at_tcnt.p, 0, (fnn + 1) * 4, st));
+    ag_pairs(f.nn, f.start.as<uint32_t>(), g.at_srcoff.as<uint32_t>(), f.tsc.as<int>(), g.at_kA.as<uint64_t>(),
+             g.at_iA.as<uint32_t>(), g.at_tcnt.as<uint32_t>(), st);
+    k = g.at_kA.as<uint64_t>(); kb = g.at_kB.as<uint64_t>();
+    v = g.at_iA.as<uint32_t>(); vb = g.at_iB.as<uint32_t>();
+    if ((rc = amr_radix((uint32_t)npairs, amr_bits(fnn + 1), &k, &v, &kb, &vb, st))) return rc;
+    if ((rc = amr_scan(g.at_tcnt.as<uint32_t>(), g.at_tstart.as<uint32_t>(), fnn, st))) return rc;
+    ag_dens(f.nn, g.at_tstart.as<uint32_t>(), v, f.start.as<uint32_t>(), g.at_w.as<double>(), nm, ng % 2 == 0,
+            f.dens.as<float>(), st);
+    CK(cudaGetLastError());
+    if (f.nn < 125) break;   // MIN_NNODES: the refined grid is dropped
+    if (ng < max_levels) {
+      levels[3 * ng] = f.l1;
+      levels[3 * ng + 1] = f.nn;
+      levels[3 * ng + 2] = nm;
+    }
+    ng++;
+    m2d = m2f;
+    thr = nth_ref * m2d - 1.0;
+  }
+  int derr[2] = {0, 0};
+  CK(cudaMemcpyAsync(&derr[0], g.am_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&derr[1], g.at_err.p, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr[0] || derr[1]) return fail(AHFGPU_ERR_CUDA, "amr: a scatter index left the array");
+  *ngrids = ng;
+  g.amr_nlev = ng;
+  return AHFGPU_OK;
+}
+
+// grid `level` of the last hierarchy: node (z, y, x) and density
+static int amr_grid_device_impl(int level, int32_t* zyx, float* dens, int64_t max_nodes, int64_t* nnodes,
+                                void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!nnodes) return fail(AHFGPU_ERR_INVALID, "amr: nnodes is NULL");
+  *nnodes = 0;
+  if (level < 0 || level >= g.amr_nlev)
+    return fail(AHFGPU_ERR_INVALID, "amr: no grid %d in the last hierarchy (%d grids)", level, g.amr_nlev);
+  const Ctx::AmrLevel& L = g.amr_lv[level];
+  *nnodes = L.nn;
+  if (max_nodes == 0) return AHFGPU_OK;
+  if (max_nodes < 0 || (!zyx && !dens)) return fail(AHFGPU_ERR_INVALID, "amr: bad output buffer");
+  if (L.nn > max_nodes)
+    return fail(AHFGPU_ERR_CAPACITY, "amr: grid %d has %d nodes, the buffer %lld", level, L.nn, (long long)max_nodes);
+  cudaStream_t st = stream ? (cudaStream_t)stream : g.stream;
+  if (zyx) ag_zyx(L.nn, L.l1, L.key.as<uint64_t>(), zyx, st);
+  if (dens && L.nn) CK(cudaMemcpyAsync(dens, L.dens.p, (size_t)L.nn * 4, cudaMemcpyDeviceToDevice, st));
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));
   return AHFGPU_OK;
 }
 
@@ -1675,6 +1973,19 @@ int ahfgpu_amr_domain_density_device(uint64_t n, const float* x, const float* y,
 int ahfgpu_amr_first_refinement_device(int l1, const float* dens, uint64_t n, double nth_dom, int32_t* zyx,
                                        int64_t max_nodes, int64_t* nnodes, void* stream) {
   return guarded([&] { return amr_first_refinement_device_impl(l1, dens, n, nth_dom, zyx, max_nodes, nnodes, stream); });
+}
+
+int ahfgpu_amr_hierarchy_device(uint64_t n, const float* x, const float* y, const float* z, int ngrid_dom,
+                                int ngrid_max, double nth_dom, double nth_ref, int64_t* levels, int max_levels,
+                                int* ngrids, void* stream) {
+  return guarded([&] {
+    return amr_hierarchy_device_impl(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, levels, max_levels, ngrids,
+                                     stream);
+  });
+}
+
+int ahfgpu_amr_grid_device(int level, int32_t* zyx, float* dens, int64_t max_nodes, int64_t* nnodes, void* stream) {
+  return guarded([&] { return amr_grid_device_impl(level, zyx, dens, max_nodes, nnodes, stream); });
 }
 
 int ahfgpu_construct_halos(const ahfgpu_params* params, const ahfgpu_batch* batch, ahfgpu_result* result,

@@ -24,7 +24,8 @@ SYMBOLS = [
     "ahfgpu_fetch_result", "ahfgpu_result_free", "ahfgpu_last_error", "ahfgpu_version", "ahfgpu_tuning",
     "ahfgpu_gather_device", "ahfgpu_gather_radii_device", "ahfgpu_write_particles_device",
     "ahfgpu_write_particles_bin_device", "ahfgpu_sfc_sort_device", "ahfgpu_shard_halos",
-    "ahfgpu_amr_domain_density_device", "ahfgpu_amr_first_refinement_device",
+    "ahfgpu_amr_domain_density_device", "ahfgpu_amr_first_refinement_device", "ahfgpu_amr_hierarchy_device",
+    "ahfgpu_amr_grid_device",
 ]
 
 
@@ -83,6 +84,13 @@ def load(path: str = LIB_PATH):
     lib.ahfgpu_amr_first_refinement_device.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_double, C.c_void_p,
                                                        C.c_int64, C.POINTER(C.c_int64), C.c_void_p]
     lib.ahfgpu_amr_first_refinement_device.restype = C.c_int
+    lib.ahfgpu_amr_hierarchy_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                                C.c_double, C.c_double, C.c_void_p, C.c_int, C.POINTER(C.c_int),
+                                                C.c_void_p]
+    lib.ahfgpu_amr_hierarchy_device.restype = C.c_int
+    lib.ahfgpu_amr_grid_device.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                           C.c_void_p]
+    lib.ahfgpu_amr_grid_device.restype = C.c_int
     lib.ahfgpu_shard_halos.argtypes = [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p]
     lib.ahfgpu_shard_halos.restype = C.c_int
     lib.ahfgpu_sfc_sort_device.argtypes = [C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
@@ -316,3 +324,35 @@ def amr_first_refinement_device(dens, l1: int, n: int, nth_dom: float, stream: i
     check(lib.ahfgpu_amr_first_refinement_device(int(l1), dens.data_ptr(), int(n), float(nth_dom), out.data_ptr(),
                                                  cap, C.byref(nn), C.c_void_p(stream) if stream else None))
     return out[:nn.value]
+
+
+def amr_hierarchy_device(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float, nth_ref: float,
+                         stream: int | None = None) -> np.ndarray:
+    """The whole AMR hierarchy from device float positions (torch tensors):
+    an (ngrids, 3) int64 array of nodes per dimension, nodes and listed
+    particles per grid.  The grids stay in the library for amr_grid_device."""
+    lib = load()
+    cap = 64
+    lv = np.zeros(3 * cap, np.int64)
+    ng = C.c_int(0)
+    check(lib.ahfgpu_amr_hierarchy_device(int(x.numel()), x.data_ptr(), y.data_ptr(), z.data_ptr(), int(ngrid_dom),
+                                          int(ngrid_max), float(nth_dom), float(nth_ref),
+                                          lv.ctypes.data_as(C.c_void_p), cap, C.byref(ng),
+                                          C.c_void_p(stream) if stream else None))
+    return lv[:3 * ng.value].reshape(-1, 3)
+
+
+def amr_grid_device(level: int, device="cuda", stream: int | None = None):
+    """Grid `level` of the last hierarchy: (zyx int32 [k, 3], dens float32
+    [k]) torch tensors on the device, in the reference's node order."""
+    import torch
+    lib = load()
+    nn = C.c_int64(0)
+    check(lib.ahfgpu_amr_grid_device(int(level), None, None, 0, C.byref(nn), None))
+    k = nn.value
+    zyx = torch.empty((max(k, 1), 3), dtype=torch.int32, device=device)
+    dens = torch.empty(max(k, 1), dtype=torch.float32, device=device)
+    if k:
+        check(lib.ahfgpu_amr_grid_device(int(level), zyx.data_ptr(), dens.data_ptr(), k, C.byref(nn),
+                                         C.c_void_p(stream) if stream else None))
+    return zyx[:k], dens[:k]

@@ -321,6 +321,35 @@ AHFGPU_API int ahfgpu_amr_first_refinement_device(int l1, const float *dens, uin
                                                   int32_t *zyx, int64_t max_nodes, int64_t *nnodes,
                                                   void *stream);
 
+/* ---- the AMR hierarchy, every level ---------------------------------------
+ * Replaces the grid generation of src/main.c:614-648 (gen_domgrids + ll +
+ * assign_npart on the ngrid_dom^3 domain grid, then gen_AMRhierarchy,
+ * src/libamr_serial/generate_grids.c:278: refine_grid, relink, assign_npart
+ * per level; default TSC build, periodic, no NP_LIMIT, non-MULTIMASS).
+ * While the finest grid has fewer than ngrid_max nodes per dimension it is
+ * refined with threshold critdens - mean_dens (critdens = nth_dom m2d on the
+ * domain grid, nth_ref m2d below, i.e. NperDomCell and NperRefCell; m2d =
+ * ngrid_dom^3 / n, times 8 per level); a refined grid of fewer than
+ * MIN_NNODES = 125 nodes is dropped and ends the hierarchy.  Every grid keeps
+ * the reference's run structure, node order, particle lists and float
+ * densities bit for bit.  levels[3g .. 3g+2] (host, max_levels entries) =
+ * nodes per dimension, nodes, particles in the lists of grid g; *ngrids the
+ * number of grids.  The grids stay in the library (until the next call or
+ * ahfgpu_shutdown) for ahfgpu_amr_grid_device.  Positions in [0, 1]
+ * (device floats); 3 <= ngrid_dom <= 1024; ngrid_dom <= ngrid_max <= 2^20;
+ * n < 2^31.                                                                */
+AHFGPU_API int ahfgpu_amr_hierarchy_device(uint64_t n, const float *x, const float *y, const float *z,
+                                           int ngrid_dom, int ngrid_max, double nth_dom, double nth_ref,
+                                           int64_t *levels, int max_levels, int *ngrids, void *stream);
+
+/* Grid `level` of the last ahfgpu_amr_hierarchy_device call: *nnodes its
+ * node count; with max_nodes > 0, zyx[3k .. 3k+2] (device int32, may be
+ * NULL) = (z, y, x) of node k in the reference's node order (ascending) and
+ * dens[k] (device float, may be NULL) its density.  max_nodes = 0 only
+ * reports *nnodes; fewer than *nnodes returns AHFGPU_ERR_CAPACITY.          */
+AHFGPU_API int ahfgpu_amr_grid_device(int level, int32_t *zyx, float *dens, int64_t max_nodes, int64_t *nnodes,
+                                      void *stream);
+
 /* ---- the split across GPUs ------------------------------------------------
  * Replaces nothing in one process: AHF's haloes are independent
  * (src/libahf/ahf_halos.c:504-510 runs them in any order), so a caller with

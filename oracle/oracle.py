@@ -534,6 +534,30 @@ def amr_nodes_oracle(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, level: int
                            nth_ref, level)
 
 
+def amr_all_nodes_oracle(x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, max_total: int = 1 << 26):
+    """Every grid of the restated hierarchy from one build: a list of
+    (nodes (z, y, x), densities) per grid."""
+    import numpy as np
+    fn = C.CDLL(oracle_path()).ahforacle_amr_all_nodes
+    fn.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.c_double, C.c_void_p,
+                                                      C.c_void_p, C.c_int64, C.c_void_p, C.c_int]
+    fn.restype = C.c_int
+    a = [np.ascontiguousarray(v, dtype=np.float32) for v in (x, y, z)]
+    zyx = np.zeros(3 * max_total, np.int64)
+    dens = np.zeros(max_total)
+    counts = np.zeros(40, np.int64)
+    ng = fn(len(a[0]), *[v.ctypes.data for v in a], int(ngrid_dom), int(ngrid_max), float(nth_dom), float(nth_ref),
+            zyx.ctypes.data, dens.ctypes.data, max_total, counts.ctypes.data, 40)
+    if ng < 1:
+        raise RuntimeError(f"ahforacle_amr_all_nodes failed ({ng})")
+    out, at = [], 0
+    for g in range(ng):
+        k = int(counts[g])
+        out.append((zyx[3 * at:3 * (at + k)].reshape(-1, 3), dens[at:at + k]))
+        at += k
+    return out
+
+
 _NODES_CHILD = r"""
 import ctypes as C, sys
 import numpy as np

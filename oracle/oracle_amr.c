@@ -721,6 +721,31 @@ int64_t ahforacle_amr_nodes(uint64_t n, const float *x, const float *y, const fl
 }
 
 
+/* Every grid of that hierarchy at once: grid g's nodes and densities at
+ * offsets counts[0] + ... + counts[g - 1] of zyx (3 per node) and dens;
+ * counts[g] its node count.  Returns the number of grids, -3 when more than
+ * max_total nodes or max_grids grids. */
+int ahforacle_amr_all_nodes(uint64_t n, const float *x, const float *y, const float *z, int ngrid_dom,
+                            int ngrid_max, double nth_dom, double nth_ref, int64_t *zyx, double *dens,
+                            int64_t max_total, int64_t *counts, int max_grids)
+{
+  grid_t grids[MAX_GRIDS];
+  int64_t lv[3 * MAX_GRIDS];
+  const int ng = build_hierarchy(n, x, y, z, ngrid_dom, ngrid_max, nth_dom, nth_ref, grids, lv, MAX_GRIDS, NULL);
+  int rc = ng;
+  int64_t at = 0;
+  for (int g = 0; g < ng && rc >= 0; g++) {
+    if (g >= max_grids || at + grids[g].nnodes > max_total) { rc = -3; break; }
+    for (int64_t i = 0; i < grids[g].nnodes; i++, at++) {
+      zyx[3 * at] = grids[g].nz[i]; zyx[3 * at + 1] = grids[g].ny[i]; zyx[3 * at + 2] = grids[g].nx[i];
+      dens[at] = (double)grids[g].dens[i];
+    }
+    counts[g] = grids[g].nnodes;
+  }
+  for (int g = 0; g < ng; g++) grid_free(&grids[g]);
+  return rc;
+}
+
 /* Checks a property of the hierarchy a GPU version can build on: each
  * node's particle list is in input-index order, descending on grids 0, 2,
  * 4, ... and ascending on grids 1, 3, ... (ll prepends in index order;
