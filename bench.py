@@ -29,7 +29,7 @@ captured on): 3000 lists of <= 512 entries, 300 of 2048-16384, the 160
 lists nearest 1e5 entries of a 1.5e4-halo batch (about one per SM, as at full
 load), one of ~2e5,
 the gather on the lists of 5e3 haloes as a snapshot, the Hilbert sort of
-5e7 uniform points, the AMR first levels of the 256^3-particle cfg2 box.
+5e7 uniform points, the AMR hierarchy of the 256^3-particle cfg2 box.
 """
 from __future__ import annotations
 
@@ -70,7 +70,7 @@ def parse():
     ap.add_argument("--no-writer", action="store_true", help="skip the AHF_particles writer leg")
     ap.add_argument("--gather-cpu-particles", type=float, default=2e7, help="CPU gather baseline sample size")
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
-    ap.add_argument("--no-amr", action="store_true", help="skip the AMR first-levels leg")
+    ap.add_argument("--no-amr", action="store_true", help="skip the AMR hierarchy leg")
     ap.add_argument("--multimass", action="store_true")
     ap.add_argument("--case", default=None, choices=["small", "medium", "large", "big", "gather", "sfc", "amr"],
                     help="run one small profiling case instead of the benchmark")
@@ -385,14 +385,15 @@ def sfc_leg(lists, args, ws: int, rank: int) -> dict:
 
 
 def amr_leg(args, rank: int) -> dict:
-    """The AMR hierarchy's first two levels on the GPU for the cfg1 and cfg2
-    boxes (64^3 and 256^3 particles, LgridDomain 64, NperDomCell 5): the
-    domain grid's TSC density (ahfgpu_amr_domain_density_device) and its
-    first refinement (ahfgpu_amr_first_refinement_device), timed together
-    with CUDA events over W warm-up and K timed calls; beside it the
-    reference's own gen_domgrids + ll + assign_npart (compiled from its
-    sources; one host core, timed inside a child process around those calls)
-    on the same particles."""
+    """AHF's AMR hierarchy on the GPU for the cfg1 and cfg2 boxes (64^3 and
+    256^3 particles; LgridDomain 64, LgridMax 16384, NperDomCell =
+    NperRefCell = 5): the domain grid and every refinement with its relink
+    and TSC densities (ahfgpu_amr_hierarchy_device), timed with CUDA events
+    over W warm-up and K timed calls; beside it the reference's own
+    gen_domgrids + ll + assign_npart + gen_AMRhierarchy (compiled from its
+    sources, libamr_serial: one host core, timed inside a child process
+    around the call) on the same particles, with its grid counts checked
+    against the GPU's."""
     import torch
     from ahf_gb300 import lib, synth
     out = {}
@@ -403,31 +404,31 @@ def amr_leg(args, rank: int) -> dict:
             x, y, z = (torch.as_tensor(np.ascontiguousarray(p[:, k])).cuda() for k in range(3))
             n = len(S.ids)
             for _ in range(max(1, args.warmup)):
-                dens = lib.amr_domain_density_device(x, y, z, 64)
-                fine = lib.amr_first_refinement_device(dens, 64, n, 5.0)
+                lv = lib.amr_hierarchy_device(x, y, z, 64, 16384, 5.0, 5.0)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(args.steps):
-                dens = lib.amr_domain_density_device(x, y, z, 64)
-                fine = lib.amr_first_refinement_device(dens, 64, n, 5.0)
+                lv = lib.amr_hierarchy_device(x, y, z, 64, 16384, 5.0, 5.0)
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / args.steps
-            leg = {"metric": "particles assigned/s (domain grid + first refinement)", "value": n / (ms / 1e3),
-                   "unit": "particles/s", "ms_per_step": ms, "n_particles": n, "l1": 64,
-                   "fine_nodes": int(fine.shape[0]), "cpu_baseline": None}
+            leg = {"metric": "particles through the AMR hierarchy/s", "value": n / (ms / 1e3),
+                   "unit": "particles/s", "ms_per_step": ms, "n_particles": n, "ngrid_dom": 64,
+                   "grids": lv.tolist(), "timing": "CUDA events around the call (it synchronises per level)",
+                   "cpu_baseline": None}
             if rank == 0 and not args.no_cpu:
                 sys.path.insert(0, os.path.join(ROOT, "oracle"))
                 import oracle as O
                 O.build()
                 if os.path.isfile(O.ref_amr_path()):
-                    _, sec = O.domain_dens_reference(p[:, 0], p[:, 1], p[:, 2], 64, timed=True)
+                    ref, sec = O.amr_levels_reference(p[:, 0], p[:, 1], p[:, 2], 64, 16384, 5.0, 5.0, timed=True)
                     leg["cpu_baseline"] = {"value": n / sec, "unit": "particles/s", "cores": 1, "kind": "reference",
-                                           "sample": f"the whole box, gen_domgrids + ll + assign_npart only "
-                                                     f"(no refinement), {sec:.3f} s"}
+                                           "sample": f"the whole box, gen_domgrids + ll + assign_npart + "
+                                                     f"gen_AMRhierarchy, {sec:.3f} s",
+                                           "same_grids": bool(np.array_equal(ref, lv))}
             out[name] = leg
-            del x, y, z, dens, fine
+            del x, y, z
     except Exception as e:   # noqa: BLE001 -- reported in the line, the other legs stand
         out["error"] = str(e)[:300]
     return out
@@ -940,12 +941,11 @@ def profile_case(args) -> None:
         for _ in range(3):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            dens = lib.amr_domain_density_device(x, y, z, 64)
-            fine = lib.amr_first_refinement_device(dens, 64, len(S.ids), 5.0)
+            lv = lib.amr_hierarchy_device(x, y, z, 64, 16384, 5.0, 5.0)
             e1.record()
             torch.cuda.synchronize()
             ms.append(e0.elapsed_time(e1))
-        print(f"amr: particles {len(S.ids)} l1 64 fine nodes {int(fine.shape[0])} "
+        print(f"amr: particles {len(S.ids)} grids {lv.tolist()} "
               f"ms per call {', '.join(f'{m:.2f}' for m in ms)}")
         return
     scale = (args.case_arg or 0.05) if args.case == "gather" else 0.05

@@ -358,16 +358,21 @@ f.argtypes = [C.c_uint64] + [C.c_void_p] * 3 + [C.c_int, C.c_int, C.c_double, C.
 f.restype = C.c_int
 x, y, z = (np.ascontiguousarray(a[k], dtype=np.float32) for k in ("x", "y", "z"))
 lv = np.zeros(3 * 64, np.int64)
+import time
+t0 = time.perf_counter()
 ng = f(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, int(a["ngrid_dom"]), int(a["ngrid_max"]),
        float(a["nth_dom"]), float(a["nth_ref"]), lv.ctypes.data, 64)
-print(json.dumps({"ngrids": int(ng), "levels": lv[:3 * max(ng, 0)].tolist()}))
+dt = time.perf_counter() - t0
+print(json.dumps({"ngrids": int(ng), "levels": lv[:3 * max(ng, 0)].tolist(), "seconds": dt}))
 """
 
 
-def amr_levels_reference(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float, nth_ref: float):
+def amr_levels_reference(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float, nth_ref: float,
+                         timed: bool = False):
     """The reference's own AMR hierarchy (gen_domgrids, ll, assign_npart,
     gen_AMRhierarchy; oracle/ref_amr.c) on float positions: an (ngrids, 3)
-    int64 array of (l1dim, nodes, particles) per grid.  Runs in a child
+    int64 array of (l1dim, nodes, particles) per grid, and with `timed` also
+    the seconds the call took (measured inside the child).  Runs in a child
     process: the hierarchy lives in the reference's globals until exit."""
     import json
     import sys
@@ -382,7 +387,8 @@ def amr_levels_reference(x, y, z, ngrid_dom: int, ngrid_max: int, nth_dom: float
     out = json.loads(r.stdout.strip().splitlines()[-1])
     if out["ngrids"] < 1:
         raise RuntimeError(f"ahfref_amr_levels failed ({out['ngrids']})")
-    return np.array(out["levels"], dtype=np.int64).reshape(-1, 3)
+    lv = np.array(out["levels"], dtype=np.int64).reshape(-1, 3)
+    return (lv, float(out["seconds"])) if timed else lv
 
 
 def domain_dens_oracle(x, y, z, l1: int):
