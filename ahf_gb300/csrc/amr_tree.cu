@@ -44,10 +44,11 @@
 // Densities (assign_npart, density.c:238): every node starts at -1 (minus
 // the mean density); the reference visits the nodes in order and adds each
 // listed particle's m2d w_z w_y w_x (double) to the float density of its 27
-// TSC nodes.  Here as a gather: the (target, source, stencil slot) pairs are
-// sorted by target (stable, so sources stay in node order) and one thread
-// per target adds its sources' particles in list order -- the same float
-// additions in the same order, so the floats are identical.
+// TSC nodes.  Here as a gather: one thread per target finds its sources
+// through its own stencil (and the few one-sided pairs the runs make, listed
+// beforehand), orders them by node index and adds their particles in list
+// order -- the same float additions in the same order, so the floats are
+// identical.
 #include <cstdint>
 
 #include "common.cuh"
@@ -642,42 +643,59 @@ __global__ void __launch_bounds__(kAgT) k_ag_weights(int l1, double m2d, uint32_
   }
 }
 
-// the (target, source, slot) pairs of every node with a list, generated in
-// (source, slot) order at the source's scanned place
-__global__ void __launch_bounds__(kAgT) k_ag_pairs(int nn, const uint32_t* __restrict__ start,
-                                                   const uint32_t* __restrict__ src_off,
-                                                   const int* __restrict__ tsc, uint64_t* __restrict__ pkey,
-                                                   uint32_t* __restrict__ pval, uint32_t* __restrict__ tcount) {
+// The sources of a target.  Source s adds to the 27 nodes of its stencil;
+// a target t reads the same relation back through its own stencil: the
+// node s at t's slot j reaches t at s's mirrored slot 26 - j when
+// tsc[s][26 - j] == t.  Where the run segmentation makes the relation
+// one-sided (s finds t, t does not find s at the mirrored slot), the pair is
+// an "extra" of t, listed per target here: pass 0 counts them per target,
+// pass 1 writes (s, slot) at the target's scanned place (in any order; the
+// density kernel orders every target's sources by node index).
+__global__ void __launch_bounds__(kAgT) k_ag_extras(int nn, const uint32_t* __restrict__ start,
+                                                    const int* __restrict__ tsc, int pass,
+                                                    uint32_t* __restrict__ ecount, const uint32_t* __restrict__ eoff,
+                                                    uint32_t* __restrict__ efill, uint64_t* __restrict__ extra) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nn || start[s + 1] == start[s]) return;
-  const uint64_t o = (uint64_t)src_off[s] * 27;
   for (int k = 0; k < 27; k++) {
     const int t = tsc[(int64_t)s * 27 + k];
-    pkey[o + k] = t >= 0 ? (uint64_t)t : (uint64_t)nn;   // a missing node sorts past every target
-    pval[o + k] = (uint32_t)s * 27u + (uint32_t)k;
-    if (t >= 0) atomicAdd(&tcount[t], 1u);
+    if (t < 0 || tsc[(int64_t)t * 27 + (26 - k)] == s) continue;
+    if (pass == 0) atomicAdd(&ecount[t], 1u);
+    else extra[eoff[t] + atomicAdd(&efill[t], 1u)] = (uint64_t)s * 32u + (uint64_t)k;
   }
 }
 
-__global__ void __launch_bounds__(kAgT) k_ag_nonempty(int nn, const uint32_t* __restrict__ start,
-                                                      uint32_t* __restrict__ ne) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < nn) ne[s] = start[s + 1] > start[s] ? 1u : 0u;
-}
-
 // one thread per target: -1, then its sources in node order, each source's
-// particles in list order (descending slots when `desc`)
-__global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const uint32_t* __restrict__ tstart,
-                                                  const uint32_t* __restrict__ pval, const uint32_t* __restrict__ start,
-                                                  const double* __restrict__ w, uint32_t np, int desc,
-                                                  float* __restrict__ dens) {
+// particles in list order (descending slots when `desc`).  A target has at
+// most 27 sources (one per stencil position).
+__global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict__ tsc,
+                                                  const uint32_t* __restrict__ eoff,
+                                                  const uint64_t* __restrict__ extra,
+                                                  const uint32_t* __restrict__ start, const double* __restrict__ w,
+                                                  uint32_t np, int desc, float* __restrict__ dens,
+                                                  int* __restrict__ err) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nn) return;
+  int cs[27], ck[27];
+  int nc = 0;
+  bool over = false;
+  auto add = [&](int s, int k) {
+    if (nc == 27) { over = true; return; }
+    int i = nc++;
+    while (i > 0 && cs[i - 1] > s) { cs[i] = cs[i - 1]; ck[i] = ck[i - 1]; i--; }
+    cs[i] = s;
+    ck[i] = k;
+  };
+  for (int j = 0; j < 27; j++) {
+    const int s = tsc[(int64_t)t * 27 + j];
+    if (s >= 0 && start[s + 1] > start[s] && tsc[(int64_t)s * 27 + (26 - j)] == t) add(s, 26 - j);
+  }
+  for (uint32_t e = eoff[t]; e < eoff[t + 1]; e++) add((int)(extra[e] >> 5), (int)(extra[e] & 31u));
+  if (over) atomicExch(err, 1);
   float acc = (float)(-1.0);
   const uint64_t n = np;
-  for (uint32_t e = tstart[t]; e < tstart[t + 1]; e++) {
-    const uint32_t v = pval[e];
-    const uint32_t s = v / 27u, slot = v % 27u;
+  for (int c = 0; c < nc; c++) {
+    const uint32_t s = (uint32_t)cs[c], slot = (uint32_t)ck[c];
     const double* __restrict__ az = w + (uint64_t)(slot / 9u) * n;
     const double* __restrict__ wy = w + (uint64_t)(3u + (slot / 3u) % 3u) * n;
     const double* __restrict__ wx = w + (uint64_t)(6u + slot % 3u) * n;
@@ -794,18 +812,14 @@ void ag_weights(int l1, double m2d, uint32_t np, const uint64_t* node, const uin
   if (np > 0) k_ag_weights<<<ag_blocks(np), kAgT, 0, st>>>(l1, m2d, np, node, nkey, ord, x, y, z, w);
 }
 
-void ag_nonempty(int nn, const uint32_t* start, uint32_t* ne, cudaStream_t st) {
-  if (nn > 0) k_ag_nonempty<<<ag_blocks(nn), kAgT, 0, st>>>(nn, start, ne);
+void ag_extras(int nn, const uint32_t* start, const int* tsc, int pass, uint32_t* ecount, const uint32_t* eoff,
+               uint32_t* efill, uint64_t* extra, cudaStream_t st) {
+  if (nn > 0) k_ag_extras<<<ag_blocks(nn), kAgT, 0, st>>>(nn, start, tsc, pass, ecount, eoff, efill, extra);
 }
 
-void ag_pairs(int nn, const uint32_t* start, const uint32_t* src_off, const int* tsc, uint64_t* pkey, uint32_t* pval,
-              uint32_t* tcount, cudaStream_t st) {
-  if (nn > 0) k_ag_pairs<<<ag_blocks(nn), kAgT, 0, st>>>(nn, start, src_off, tsc, pkey, pval, tcount);
-}
-
-void ag_dens(int nn, const uint32_t* tstart, const uint32_t* pval, const uint32_t* start, const double* w,
-             uint32_t np, int desc, float* dens, cudaStream_t st) {
-  if (nn > 0) k_ag_dens<<<ag_blocks(nn), kAgT, 0, st>>>(nn, tstart, pval, start, w, np, desc, dens);
+void ag_dens(int nn, const int* tsc, const uint32_t* eoff, const uint64_t* extra, const uint32_t* start,
+             const double* w, uint32_t np, int desc, float* dens, int* err, cudaStream_t st) {
+  if (nn > 0) k_ag_dens<<<ag_blocks(nn), kAgT, 0, st>>>(nn, tsc, eoff, extra, start, w, np, desc, dens, err);
 }
 
 void ag_zyx(int nn, int l1, const uint64_t* key, int32_t* zyx, cudaStream_t st) {

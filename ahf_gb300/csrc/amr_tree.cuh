@@ -71,11 +71,10 @@ void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_
                 uint32_t* fidx_out, uint32_t* count, cudaStream_t st);
 void ag_weights(int l1, double m2d, uint32_t np, const uint64_t* node, const uint64_t* nkey, const uint32_t* ord,
                 const float* x, const float* y, const float* z, double* w, cudaStream_t st);
-void ag_nonempty(int nn, const uint32_t* start, uint32_t* ne, cudaStream_t st);
-void ag_pairs(int nn, const uint32_t* start, const uint32_t* src_off, const int* tsc, uint64_t* pkey, uint32_t* pval,
-              uint32_t* tcount, cudaStream_t st);
-void ag_dens(int nn, const uint32_t* tstart, const uint32_t* pval, const uint32_t* start, const double* w,
-             uint32_t np, int desc, float* dens, cudaStream_t st);
+void ag_extras(int nn, const uint32_t* start, const int* tsc, int pass, uint32_t* ecount, const uint32_t* eoff,
+               uint32_t* efill, uint64_t* extra, cudaStream_t st);
+void ag_dens(int nn, const int* tsc, const uint32_t* eoff, const uint64_t* extra, const uint32_t* start,
+             const double* w, uint32_t np, int desc, float* dens, int* err, cudaStream_t st);
 void ag_zyx(int nn, int l1, const uint64_t* key, int32_t* zyx, cudaStream_t st);
 
 }  // namespace ahfgpu

@@ -229,7 +229,7 @@ struct Ctx {
   // the radix passes, the density pairs
   DBuf at_rrun, at_rnode, at_rref, at_runoff, at_runs, at_pref, at_po, at_pnc, at_pnsel, at_rroff, at_seloff;
   DBuf at_rr, at_sel, at_fpl, at_tot, at_dest, at_moved, at_moff, at_cnt, at_kA, at_kB, at_iA, at_iB;
-  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt, at_tstart;
+  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -989,7 +989,7 @@ int ahfgpu_shutdown(void) {
                   &g.at_rref, &g.at_runoff, &g.at_runs, &g.at_pref, &g.at_po, &g.at_pnc, &g.at_pnsel, &g.at_rroff,
                   &g.at_seloff, &g.at_rr, &g.at_sel, &g.at_fpl, &g.at_tot, &g.at_dest, &g.at_moved, &g.at_moff,
                   &g.at_cnt, &g.at_kA, &g.at_kB, &g.at_iA, &g.at_iB, &g.at_gh, &g.at_goff, &g.at_part, &g.at_err,
-                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt, &g.at_tstart};
+                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt};
   for (DBuf* b : bufs) b->release();
   for (Ctx::AmrLevel& L : g.amr_lv)
     for (DBuf* b : {&L.P, &L.pl, &L.C, &L.R, &L.N, &L.key, &L.nseg, &L.tsc, &L.flag, &L.dens, &L.start, &L.ord, &L.node})
@@ -1770,33 +1770,29 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
     }
     f.np = nm;
 
-    // densities: the (target, source, slot) pairs by target, then the gather
+    // densities: the one-sided (source, target) pairs per target, then the
+    // gather
     const double m2f = m2d * 8.0;
     if ((rc = g.at_w.ensure((size_t)nm * 72 + 72)) || (rc = g.at_ne.ensure(fnn * 4 + 4)) ||
-        (rc = g.at_srcoff.ensure((fnn + 1) * 4)) || (rc = g.at_tcnt.ensure((fnn + 1) * 4)) ||
-        (rc = g.at_tstart.ensure((fnn + 1) * 4)))
+        (rc = g.at_srcoff.ensure((fnn + 1) * 4)) || (rc = g.at_tcnt.ensure(fnn * 4 + 4)))
       return rc;
     ag_weights(f.l1, m2f, nm, f.node.as<uint64_t>(), f.key.as<uint64_t>(), f.ord.as<uint32_t>(), x, y, z,
                g.at_w.as<double>(), st);
-    ag_nonempty(f.nn, f.start.as<uint32_t>(), g.at_ne.as<uint32_t>(), st);
+    CK(cudaMemsetAsync(g.at_ne.p, 0, fnn * 4 + 4, st));
+    ag_extras(f.nn, f.start.as<uint32_t>(), f.tsc.as<int>(), 0, g.at_ne.as<uint32_t>(), nullptr, nullptr, nullptr,
+              st);
     if ((rc = amr_scan(g.at_ne.as<uint32_t>(), g.at_srcoff.as<uint32_t>(), fnn, st))) return rc;
-    uint32_t nsrc = 0;
-    CK(cudaMemcpyAsync(&nsrc, g.at_srcoff.as<uint32_t>() + fnn, 4, cudaMemcpyDeviceToHost, st));
+    uint32_t nextra = 0;
+    CK(cudaMemcpyAsync(&nextra, g.at_srcoff.as<uint32_t>() + fnn, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    const uint64_t npairs = 27ull * nsrc;
-    if (npairs >= (1ull << 32)) return fail(AHFGPU_ERR_CAPACITY, "amr: %llu density pairs", (unsigned long long)npairs);
-    if ((rc = g.at_kA.ensure(npairs * 8 + 8)) || (rc = g.at_kB.ensure(npairs * 8 + 8)) ||
-        (rc = g.at_iA.ensure(npairs * 4 + 4)) || (rc = g.at_iB.ensure(npairs * 4 + 4)))
-      return rc;
-    CK(cudaMemsetAsync(g.at_tcnt.p, 0, (fnn + 1) * 4, st));
-    ag_pairs(f.nn, f.start.as<uint32_t>(), g.at_srcoff.as<uint32_t>(), f.tsc.as<int>(), g.at_kA.as<uint64_t>(),
-             g.at_iA.as<uint32_t>(), g.at_tcnt.as<uint32_t>(), st);
-    k = g.at_kA.as<uint64_t>(); kb = g.at_kB.as<uint64_t>();
-    v = g.at_iA.as<uint32_t>(); vb = g.at_iB.as<uint32_t>();
-    if ((rc = amr_radix((uint32_t)npairs, amr_bits(fnn + 1), &k, &v, &kb, &vb, st))) return rc;
-    if ((rc = amr_scan(g.at_tcnt.as<uint32_t>(), g.at_tstart.as<uint32_t>(), fnn, st))) return rc;
-    ag_dens(f.nn, g.at_tstart.as<uint32_t>(), v, f.start.as<uint32_t>(), g.at_w.as<double>(), nm, ng % 2 == 0,
-            f.dens.as<float>(), st);
+    if ((rc = g.at_kB.ensure((size_t)nextra * 8 + 8))) return rc;
+    if (nextra) {
+      CK(cudaMemsetAsync(g.at_tcnt.p, 0, fnn * 4 + 4, st));
+      ag_extras(f.nn, f.start.as<uint32_t>(), f.tsc.as<int>(), 1, nullptr, g.at_srcoff.as<uint32_t>(),
+                g.at_tcnt.as<uint32_t>(), g.at_kB.as<uint64_t>(), st);
+    }
+    ag_dens(f.nn, f.tsc.as<int>(), g.at_srcoff.as<uint32_t>(), g.at_kB.as<uint64_t>(), f.start.as<uint32_t>(),
+            g.at_w.as<double>(), nm, ng % 2 == 0, f.dens.as<float>(), g.at_err.as<int>() + 1, st);
     CK(cudaGetLastError());
     if (f.nn < 125) break;   // MIN_NNODES: the refined grid is dropped
     if (ng < max_levels) {
@@ -1813,6 +1809,9 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
   CK(cudaMemcpyAsync(&derr[1], g.at_err.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (derr[0] || derr[1]) return fail(AHFGPU_ERR_CUDA, "amr: a scatter index left the array");
+  CK(cudaMemcpyAsync(&derr[1], g.at_err.as<int>() + 1, 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (derr[1]) return fail(AHFGPU_ERR_STATE, "amr: a node with more than 27 TSC sources");
   *ngrids = ng;
   g.amr_nlev = ng;
   return AHFGPU_OK;
