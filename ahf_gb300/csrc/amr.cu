@@ -19,10 +19,12 @@
 // adding the same double term to a float in the same order -- the floats
 // equal the reference's bit for bit.  The particles are grouped by node by a
 // stable radix sort of their node index (ascending index within a node; the
-// list order is that read backwards), and each particle's nine TSC factors
-// (m2d w_z, w_y, w_x for the three offsets per axis) are computed once, in
-// that order, so a target's loop reads three of them contiguously and forms
-// the rest of the product (two multiplications) and the float sum.
+// list order is that read backwards), and each particle's TSC factors are
+// formed once, in that order: the nine (m2d w_z) w_y and the three w_x, so a
+// target's loop reads two of them per particle, forms the last product and
+// the sum.  The sums are FP64-pipe bound on this GPU, so the rounding of
+// each sum to float is done by integer arithmetic (amr_round_f32), leaving
+// two FP64 operations per term.
 //
 // First refinement (refine_grid, refine_grid.c:899, test_node :113-137 on the
 // domain grid): a node is flagged when any node at dz, dy in {-1,0,1} and
@@ -35,6 +37,7 @@
 #include <cstdint>
 
 #include "common.cuh"
+#include "amr_tree.cuh"
 
 namespace ahfgpu {
 
@@ -90,14 +93,14 @@ __device__ __forceinline__ double amr_sep(float p, double centre, double dl1) {
   return sep;
 }
 
-// each particle's TSC weights, in node order (the order of the sorted node
-// keys), computed once and read by the 27 targets around the node:
-// az[o] = m2d * w_z(o) (the first product of the reference's left-to-right
-// m2d * w_z * w_y * w_x), wy[o], wx[o], o = offset + 1 of the target
+// each particle's TSC factors, in node order (the order of the sorted node
+// keys), computed once and read by the 27 targets around the node: the
+// reference forms m2d * w_z * w_y * w_x left to right, so the first two
+// products are kept, b[3 oz + oy] = (m2d * w_z(oz - 1)) * w_y(oy - 1), and
+// x[ox] = w_x(ox - 1); o = offset + 1 of the target from the source
 struct AmrW {
-  double* az[3];
-  double* wy[3];
-  double* wx[3];
+  double* b[9];
+  double* x[3];
 };
 
 __global__ void __launch_bounds__(kAmrT) k_amr_weights(int l1, uint32_t n, const uint64_t* __restrict__ skey,
@@ -116,11 +119,13 @@ __global__ void __launch_bounds__(kAmrT) k_amr_weights(int l1, uint32_t n, const
     const double sy = amr_sep(y[i], amr_fold(((double)cy / dl1 + shift) + 1.0), dl1);
     const double sz = amr_sep(z[i], amr_fold(((double)cz / dl1 + shift) + 1.0), dl1);
 #pragma unroll
-    for (int o = 0; o < 3; o++) {
-      W.az[o][k] = m2d * amr_w(sz, o - 1);
-      W.wy[o][k] = amr_w(sy, o - 1);
-      W.wx[o][k] = amr_w(sx, o - 1);
+    for (int oz = 0; oz < 3; oz++) {
+      const double az = m2d * amr_w(sz, oz - 1);
+#pragma unroll
+      for (int oy = 0; oy < 3; oy++) W.b[3 * oz + oy][k] = az * amr_w(sy, oy - 1);
     }
+#pragma unroll
+    for (int o = 0; o < 3; o++) W.x[o][k] = amr_w(sx, o - 1);
   }
 }
 
@@ -135,36 +140,37 @@ __global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, const uint32_t* __re
   amr_three(tz, l1, sz3);
   amr_three(ty, l1, sy3);
   amr_three(tx, l1, sx3);
-  float acc = (float)(-1.0);
+  // the float density as a double holding a float: each double addition is
+  // rounded to float (amr_round_f32), as the reference's += on a float does
+  double acc = -1.0;
   for (int a = 0; a < 3; a++) {
     // offset of the target from the source along z, in {-1, 0, 1}
     const int oz = ((tz - sz3[a] + l1 + 1) % l1) - 1;
-    const double* __restrict__ az = W.az[oz + 1];
     for (int b = 0; b < 3; b++) {
       const int oy = ((ty - sy3[b] + l1 + 1) % l1) - 1;
-      const double* __restrict__ wy = W.wy[oy + 1];
+      const double* __restrict__ bz = W.b[3 * (oz + 1) + (oy + 1)];
       for (int c = 0; c < 3; c++) {
         const int ox = ((tx - sx3[c] + l1 + 1) % l1) - 1;
-        const double* __restrict__ wx = W.wx[ox + 1];
+        const double* __restrict__ wx = W.x[ox + 1];
         const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
         const uint32_t s0 = start[s], s1 = start[s + 1];
         // list order: descending input index.  Eight terms at a time: their
-        // loads and products are independent, only the float sums chain
+        // loads and products are independent, only the sums chain
         for (uint32_t k = s1; k > s0;) {
           const uint32_t m = k - s0 < 8u ? k - s0 : 8u;
           double tv[8];
 #pragma unroll
           for (uint32_t j = 0; j < 8; j++)
-            if (j < m) tv[j] = __ldg(az + k - 1 - j) * __ldg(wy + k - 1 - j) * __ldg(wx + k - 1 - j);
+            if (j < m) tv[j] = __ldg(bz + k - 1 - j) * __ldg(wx + k - 1 - j);
 #pragma unroll
           for (uint32_t j = 0; j < 8; j++)
-            if (j < m) acc = (float)((double)acc + tv[j]);
+            if (j < m) acc = amr_round_f32(acc + tv[j]);
           k -= m;
         }
       }
     }
   }
-  dens[t] = acc;
+  dens[t] = (float)acc;
 }
 
 // refinement flag of every coarse node: any of its 18 nodes at dz, dy in
@@ -246,11 +252,8 @@ void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z
               const uint64_t* skey, const uint32_t* ord, double* wts, float* dens, int grid, cudaStream_t st) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
   AmrW W;
-  for (int o = 0; o < 3; o++) {
-    W.az[o] = wts + (uint64_t)o * n;
-    W.wy[o] = wts + (uint64_t)(3 + o) * n;
-    W.wx[o] = wts + (uint64_t)(6 + o) * n;
-  }
+  for (int o = 0; o < 9; o++) W.b[o] = wts + (uint64_t)o * n;
+  for (int o = 0; o < 3; o++) W.x[o] = wts + (uint64_t)(9 + o) * n;
   k_amr_weights<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, W);
   k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, start, W, dens);
 }

@@ -615,9 +615,9 @@ __device__ __forceinline__ double ag_sep(float p, double centre, double dl1) {
   return sep;
 }
 
-// each listed particle's nine TSC factors in list-slot order: w[o] =
-// m2d * w_z(o - 1), w[3 + o] = w_y(o - 1), w[6 + o] = w_x(o - 1) at column
-// o * np + k (the first product of the reference's left-to-right
+// each listed particle's TSC factors in list-slot order: w[3 oz + oy] =
+// (m2d * w_z(oz - 1)) * w_y(oy - 1) and w[9 + ox] = w_x(ox - 1) at column
+// o * np + k (the first two products of the reference's left-to-right
 // m2d * w_z * w_y * w_x formed once)
 __global__ void __launch_bounds__(kAgT) k_ag_weights(int l1, double m2d, uint32_t np, const uint64_t* __restrict__ node,
                                                      const uint64_t* __restrict__ nkey,
@@ -636,11 +636,13 @@ __global__ void __launch_bounds__(kAgT) k_ag_weights(int l1, double m2d, uint32_
   const double sz = ag_sep(z[i], ag_fold(((double)cz / dl1 + shift) + 1.0), dl1);
   const uint64_t n = np;
 #pragma unroll
-  for (int o = 0; o < 3; o++) {
-    w[(uint64_t)o * n + k] = m2d * ag_w(sz, o - 1);
-    w[(uint64_t)(3 + o) * n + k] = ag_w(sy, o - 1);
-    w[(uint64_t)(6 + o) * n + k] = ag_w(sx, o - 1);
+  for (int oz = 0; oz < 3; oz++) {
+    const double az = m2d * ag_w(sz, oz - 1);
+#pragma unroll
+    for (int oy = 0; oy < 3; oy++) w[(uint64_t)(3 * oz + oy) * n + k] = az * ag_w(sy, oy - 1);
   }
+#pragma unroll
+  for (int o = 0; o < 3; o++) w[(uint64_t)(9 + o) * n + k] = ag_w(sx, o - 1);
 }
 
 // The sources of a target.  Source s adds to the 27 nodes of its stencil;
@@ -692,13 +694,14 @@ __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict_
   }
   for (uint32_t e = eoff[t]; e < eoff[t + 1]; e++) add((int)(extra[e] >> 5), (int)(extra[e] & 31u));
   if (over) atomicExch(err, 1);
-  float acc = (float)(-1.0);
+  // the float density as a double holding a float (amr_round_f32 after
+  // every addition, as the reference's += on a float rounds)
+  double acc = -1.0;
   const uint64_t n = np;
   for (int c = 0; c < nc; c++) {
     const uint32_t s = (uint32_t)cs[c], slot = (uint32_t)ck[c];
-    const double* __restrict__ az = w + (uint64_t)(slot / 9u) * n;
-    const double* __restrict__ wy = w + (uint64_t)(3u + (slot / 3u) % 3u) * n;
-    const double* __restrict__ wx = w + (uint64_t)(6u + slot % 3u) * n;
+    const double* __restrict__ bz = w + (uint64_t)(slot / 3u) * n;
+    const double* __restrict__ wx = w + (uint64_t)(9u + slot % 3u) * n;
     const uint32_t s0 = start[s], s1 = start[s + 1];
     if (desc) {
       for (uint32_t k = s1; k > s0;) {
@@ -706,10 +709,10 @@ __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict_
         double tv[8];
 #pragma unroll
         for (uint32_t j = 0; j < 8; j++)
-          if (j < m) tv[j] = __ldg(az + k - 1 - j) * __ldg(wy + k - 1 - j) * __ldg(wx + k - 1 - j);
+          if (j < m) tv[j] = __ldg(bz + k - 1 - j) * __ldg(wx + k - 1 - j);
 #pragma unroll
         for (uint32_t j = 0; j < 8; j++)
-          if (j < m) acc = (float)((double)acc + tv[j]);
+          if (j < m) acc = amr_round_f32(acc + tv[j]);
         k -= m;
       }
     } else {
@@ -718,15 +721,15 @@ __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict_
         double tv[8];
 #pragma unroll
         for (uint32_t j = 0; j < 8; j++)
-          if (j < m) tv[j] = __ldg(az + k + j) * __ldg(wy + k + j) * __ldg(wx + k + j);
+          if (j < m) tv[j] = __ldg(bz + k + j) * __ldg(wx + k + j);
 #pragma unroll
         for (uint32_t j = 0; j < 8; j++)
-          if (j < m) acc = (float)((double)acc + tv[j]);
+          if (j < m) acc = amr_round_f32(acc + tv[j]);
         k += m;
       }
     }
   }
-  dens[t] = acc;
+  dens[t] = (float)acc;
 }
 
 // node coordinates (z, y, x) from the keys

@@ -8,6 +8,25 @@
 
 namespace ahfgpu {
 
+// (double)(float)s: for s whose float rounding is a normal float below the
+// largest binade, the double's significand rounded to 24 bits (to nearest,
+// ties to even) by integer arithmetic -- the same value the conversion
+// instructions give, without their FP64-pipe issue slots; every other s
+// (zero, subnormal float results, the top binade, inf, NaN) through the
+// conversions.  The TSC density sums round to float after every double
+// addition, so this runs once per term.
+__device__ __forceinline__ double amr_round_f32(double s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if (e - 897u <= 252u) {   // biased exponent 897 .. 1149: float exponent 1 .. 253
+    unsigned long long m = b & 0x7fffffffffffffffull;
+    m += 0x0fffffffull + ((m >> 29) & 1ull);
+    m &= ~0x1fffffffull;
+    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | m));
+  }
+  return (double)(float)s;
+}
+
 struct APRun { int z0, len, pl0, pad; };
 struct APlane { int z, pq, c0, nc; };
 struct ACRun { int y0, len, r0, pl; };

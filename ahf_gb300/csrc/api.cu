@@ -1499,7 +1499,7 @@ static int amr_domain_lists(uint64_t n, const float* x, const float* y, const fl
       (rc = g.am_idxb.ensure(n * 4)) || (rc = g.am_cnt.ensure(nn * 4)) || (rc = g.am_start.ensure((nn + 1) * 4)) ||
       (rc = g.am_sums.ensure(((nn + 2047) / 2048) * 4)) || (rc = g.am_gh.ensure((size_t)m * 4)) ||
       (rc = g.am_goff.ensure((size_t)m * 4)) || (rc = g.am_part.ensure((size_t)nb * 4)) ||
-      (rc = g.am_err.ensure(64)) || (rc = g.am_seps.ensure(n * 72)))
+      (rc = g.am_err.ensure(64)) || (rc = g.am_seps.ensure(n * 96)))
     return rc;
   CK(cudaMemsetAsync(g.am_cnt.p, 0, nn * 4, st));
   CK(cudaMemsetAsync(g.am_err.p, 0, 64, st));
@@ -1773,7 +1773,7 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
     // densities: the one-sided (source, target) pairs per target, then the
     // gather
     const double m2f = m2d * 8.0;
-    if ((rc = g.at_w.ensure((size_t)nm * 72 + 72)) || (rc = g.at_ne.ensure(fnn * 4 + 4)) ||
+    if ((rc = g.at_w.ensure((size_t)nm * 96 + 96)) || (rc = g.at_ne.ensure(fnn * 4 + 4)) ||
         (rc = g.at_srcoff.ensure((fnn + 1) * 4)) || (rc = g.at_tcnt.ensure(fnn * 4 + 4)))
       return rc;
     ag_weights(f.l1, m2f, nm, f.node.as<uint64_t>(), f.key.as<uint64_t>(), f.ord.as<uint32_t>(), x, y, z,
