@@ -348,8 +348,28 @@ struct Fix {
 
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
 
+// A float rounded to the nearest 64-bit integer (ties to even), |x| < 2^62,
+// by integer arithmetic: the 64-bit conversion instructions issue on the
+// FP64 pipe, which this GPU runs at a small fraction of the FP32 rate, and
+// this runs once per list entry and array.
+__device__ __forceinline__ long long f2ll_rn(float x) {
+  const unsigned u = __float_as_uint(x);
+  const int e = (int)((u >> 23) & 0xffu);
+  if (e < 126) return 0;   // |x| < 1/2 (zero and subnormals included)
+  const unsigned long long m = (u & 0x7fffffu) | 0x800000u;
+  unsigned long long r;
+  if (e >= 150) {
+    r = m << (e - 150);   // an integer already
+  } else {
+    const int k = 150 - e;   // 1 .. 24 fraction bits
+    const unsigned long long q = m >> k, rem = m & ((1ull << k) - 1ull), half = 1ull << (k - 1);
+    r = q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+  }
+  return (u >> 31) ? -(long long)r : (long long)r;
+}
+
 // round(x 2^s) for |x 2^s| < 2^62 (the scaling by 2^s is exact)
-__device__ __forceinline__ long long f2fix(float x, float scale) { return __float2ll_rn(__fmul_rn(x, scale)); }
+__device__ __forceinline__ long long f2fix(float x, float scale) { return f2ll_rn(__fmul_rn(x, scale)); }
 
 // w v in fixed point: the exact product (two floats) rounded to the grid
 __device__ __forceinline__ long long wv2fix(float w, float v, float scale, int has_w) {
@@ -383,7 +403,7 @@ __device__ __forceinline__ float i2f(long long v, float iscale) { return __fmul_
 // mass prefix as float-float: with unit weights it is the particle count
 // (exact in one float below 2^24), else the fixed-point sum
 __device__ __forceinline__ ff mass_ff(long long fixsum, long long count, int has_w, float iscale) {
-  if (!has_w && count < (1ll << 24)) return ff{(float)count, 0.f};
+  if (!has_w && count < (1ll << 24)) return ff{__int2float_rn((int)count), 0.f};   // exact: a 32-bit conversion
   return i2ff(fixsum, iscale);
 }
 
@@ -1067,7 +1087,8 @@ static __device__ uint64_t rvir0_phi(const Ctx32& c, const DevBatch& B, const Wo
       ff prevq = k == 0 ? qp : q[k - 1];
       if (i < c.n) {
         const bool cnt_mass = !P.has_w && i + 1 < (1ull << 24);
-        accT = ff_add(accT, cnt_mass ? phi_termq_c((float)(i + 1), (float)i, d[k], q[k], prevd, prevq)
+        accT = ff_add(accT, cnt_mass ? phi_termq_c(__uint2float_rn((unsigned)(i + 1)), __uint2float_rn((unsigned)i),
+                                                   d[k], q[k], prevd, prevq)
                                      : phi_termq(Mk[k], w[k], d[k], q[k], prevd, prevq));
       }
       term[k] = accT;     // thread-local inclusive
@@ -1402,7 +1423,8 @@ static __device__ void unbind_pass(const Ctx32& c, const DevBatch& B, const Work
         rC++;
         ff Mb = mass_ff(rMb, rC, has_w, F.im);
         const bool cnt_mass = !has_w && rC < (1ll << 24);
-        accN = ff_add(accN, cnt_mass ? phi_termq_c((float)rC, (float)(rC - 1), d[k], q[k], dp, qp)
+        accN = ff_add(accN, cnt_mass ? phi_termq_c(__int2float_rn((int)rC), __int2float_rn((int)(rC - 1)), d[k], q[k],
+                                                   dp, qp)
                                      : phi_termq(Mb, w[k], d[k], q[k], dp, qp));
         pn[k] = accN;
         dp = d[k];

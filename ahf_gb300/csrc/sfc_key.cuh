@@ -21,7 +21,9 @@ AHFGPU_HD uint32_t sfc_coord(float x, int bits) {
   const float scale = (float)(1u << bits);
   const uint32_t top = (1u << bits) - 1u;
 #ifdef __CUDA_ARCH__
-  const uint32_t q = (uint32_t)__float2ull_rz(__fmul_rn(x, scale));
+  // a 32-bit conversion (saturating: negative and NaN give 0, past 2^32 - 1
+  // the maximum, then the cap); the 64-bit one would issue on the FP64 pipe
+  const uint32_t q = __float2uint_rz(__fmul_rn(x, scale));
 #else
   const float p = x * scale;
   const uint32_t q = p > 0.f ? (p < 4194304.f ? (uint32_t)p : top) : 0u;
