@@ -154,19 +154,20 @@ __global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, const uint32_t* __re
         const double* __restrict__ wx = W.x[ox + 1];
         const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
         const uint32_t s0 = start[s], s1 = start[s + 1];
-        // list order: descending input index.  Eight terms at a time: their
-        // loads and products are independent, only the sums chain
-        for (uint32_t k = s1; k > s0;) {
-          const uint32_t m = k - s0 < 8u ? k - s0 : 8u;
-          double tv[8];
-#pragma unroll
-          for (uint32_t j = 0; j < 8; j++)
-            if (j < m) tv[j] = __ldg(bz + k - 1 - j) * __ldg(wx + k - 1 - j);
-#pragma unroll
-          for (uint32_t j = 0; j < 8; j++)
-            if (j < m) acc = amr_round_f32(acc + tv[j]);
-          k -= m;
+        // list order: descending input index.  Four terms at a time (their
+        // loads and products are independent, only the sums chain), then one
+        // at a time: no predicated-off FP64 instructions, which would still
+        // take FP64 issue slots
+        uint32_t k = s1;
+        for (; k >= s0 + 4; k -= 4) {
+          const double t0 = __ldg(bz + k - 1) * __ldg(wx + k - 1), t1 = __ldg(bz + k - 2) * __ldg(wx + k - 2);
+          const double t2 = __ldg(bz + k - 3) * __ldg(wx + k - 3), t3 = __ldg(bz + k - 4) * __ldg(wx + k - 4);
+          acc = amr_round_f32(acc + t0);
+          acc = amr_round_f32(acc + t1);
+          acc = amr_round_f32(acc + t2);
+          acc = amr_round_f32(acc + t3);
         }
+        for (; k > s0; k--) acc = amr_round_f32(acc + __ldg(bz + k - 1) * __ldg(wx + k - 1));
       }
     }
   }

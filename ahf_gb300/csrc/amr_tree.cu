@@ -703,30 +703,31 @@ __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict_
     const double* __restrict__ bz = w + (uint64_t)(slot / 3u) * n;
     const double* __restrict__ wx = w + (uint64_t)(9u + slot % 3u) * n;
     const uint32_t s0 = start[s], s1 = start[s + 1];
+    // four terms at a time (independent loads and products, only the sums
+    // chain), then one at a time: no predicated-off FP64 instructions, which
+    // would still take FP64 issue slots
     if (desc) {
-      for (uint32_t k = s1; k > s0;) {
-        const uint32_t m = k - s0 < 8u ? k - s0 : 8u;
-        double tv[8];
-#pragma unroll
-        for (uint32_t j = 0; j < 8; j++)
-          if (j < m) tv[j] = __ldg(bz + k - 1 - j) * __ldg(wx + k - 1 - j);
-#pragma unroll
-        for (uint32_t j = 0; j < 8; j++)
-          if (j < m) acc = amr_round_f32(acc + tv[j]);
-        k -= m;
+      uint32_t k = s1;
+      for (; k >= s0 + 4; k -= 4) {
+        const double t0 = __ldg(bz + k - 1) * __ldg(wx + k - 1), t1 = __ldg(bz + k - 2) * __ldg(wx + k - 2);
+        const double t2 = __ldg(bz + k - 3) * __ldg(wx + k - 3), t3 = __ldg(bz + k - 4) * __ldg(wx + k - 4);
+        acc = amr_round_f32(acc + t0);
+        acc = amr_round_f32(acc + t1);
+        acc = amr_round_f32(acc + t2);
+        acc = amr_round_f32(acc + t3);
       }
+      for (; k > s0; k--) acc = amr_round_f32(acc + __ldg(bz + k - 1) * __ldg(wx + k - 1));
     } else {
-      for (uint32_t k = s0; k < s1;) {
-        const uint32_t m = s1 - k < 8u ? s1 - k : 8u;
-        double tv[8];
-#pragma unroll
-        for (uint32_t j = 0; j < 8; j++)
-          if (j < m) tv[j] = __ldg(bz + k + j) * __ldg(wx + k + j);
-#pragma unroll
-        for (uint32_t j = 0; j < 8; j++)
-          if (j < m) acc = amr_round_f32(acc + tv[j]);
-        k += m;
+      uint32_t k = s0;
+      for (; k + 4 <= s1; k += 4) {
+        const double t0 = __ldg(bz + k) * __ldg(wx + k), t1 = __ldg(bz + k + 1) * __ldg(wx + k + 1);
+        const double t2 = __ldg(bz + k + 2) * __ldg(wx + k + 2), t3 = __ldg(bz + k + 3) * __ldg(wx + k + 3);
+        acc = amr_round_f32(acc + t0);
+        acc = amr_round_f32(acc + t1);
+        acc = amr_round_f32(acc + t2);
+        acc = amr_round_f32(acc + t3);
       }
+      for (; k < s1; k++) acc = amr_round_f32(acc + __ldg(bz + k) * __ldg(wx + k));
     }
   }
   dens[t] = (float)acc;
