@@ -677,7 +677,8 @@ def ours_arm(args, ws, rank, local):
     for k in ("cx", "cy", "cz"):
         t[k] = torch.as_tensor(getattr(lists, k)).cuda()
     # page-locked host copies of the inputs for the e2e leg, made first as a
-    # caller's particle arrays would be (they exist before the stage runs)
+    # caller's particle arrays would be (they exist before the stage runs,
+    # written by the host: AHF reads them from the snapshot files)
     host = {}
     if not args.no_e2e:
         for k in ("x", "y", "z", "vx", "vy", "vz", "w", "gidx"):
@@ -686,7 +687,7 @@ def ours_arm(args, ws, rank, local):
                 host[k] = None
                 continue
             hp = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
-            hp.copy_(v)
+            hp.copy_(v.cpu())   # through pageable memory: the host writes the pinned pages
             host[k] = hp
     torch.cuda.synchronize()
     torch.cuda.empty_cache()
