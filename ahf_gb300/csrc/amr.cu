@@ -38,6 +38,7 @@
 
 #include "common.cuh"
 #include "amr_tree.cuh"
+#include "amr_sum.cuh"
 
 namespace ahfgpu {
 
@@ -129,49 +130,48 @@ __global__ void __launch_bounds__(kAmrT) k_amr_weights(int l1, uint32_t n, const
   }
 }
 
-__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, const uint32_t* __restrict__ start, AmrW W,
+// one warp per target node: its 27 source nodes (ascending node index, the
+// reference's visiting order; with l1 >= 3 distinct), those with particles
+// compacted with their stencil slots and term offsets into shared memory,
+// then the float sum over their particles in list order (amr_warp_sum)
+__global__ void __launch_bounds__(kAmrT) k_amr_dens(int l1, const uint32_t* __restrict__ start,
+                                                    const double* __restrict__ wts, uint64_t n,
                                                     float* __restrict__ dens) {
+  __shared__ AmrSrc sh[kAmrT / 32][32];
+  const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
-  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nn) return;
+  const uint64_t t = (uint64_t)blockIdx.x * (kAmrT / 32) + wid;
+  if (t >= nn) return;   // uniform over the warp
   const int tx = (int)(t % (uint64_t)l1), ty = (int)((t / (uint64_t)l1) % (uint64_t)l1),
             tz = (int)(t / ((uint64_t)l1 * l1));
   int sz3[3], sy3[3], sx3[3];
   amr_three(tz, l1, sz3);
   amr_three(ty, l1, sy3);
   amr_three(tx, l1, sx3);
-  // the float density as a double holding a float: each double addition is
-  // rounded to float (amr_round_f32), as the reference's += on a float does
-  double acc = -1.0;
-  for (int a = 0; a < 3; a++) {
-    // offset of the target from the source along z, in {-1, 0, 1}
+  uint32_t s0 = 0, cnt = 0, slot = 0;
+  if (lane < 27u) {
+    const int a = (int)lane / 9, b = ((int)lane / 3) % 3, c = (int)lane % 3;
+    // offset of the target from the source per axis, in {-1, 0, 1}
     const int oz = ((tz - sz3[a] + l1 + 1) % l1) - 1;
-    for (int b = 0; b < 3; b++) {
-      const int oy = ((ty - sy3[b] + l1 + 1) % l1) - 1;
-      const double* __restrict__ bz = W.b[3 * (oz + 1) + (oy + 1)];
-      for (int c = 0; c < 3; c++) {
-        const int ox = ((tx - sx3[c] + l1 + 1) % l1) - 1;
-        const double* __restrict__ wx = W.x[ox + 1];
-        const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
-        const uint32_t s0 = start[s], s1 = start[s + 1];
-        // list order: descending input index.  Four terms at a time (their
-        // loads and products are independent, only the sums chain), then one
-        // at a time: no predicated-off FP64 instructions, which would still
-        // take FP64 issue slots
-        uint32_t k = s1;
-        for (; k >= s0 + 4; k -= 4) {
-          const double t0 = __ldg(bz + k - 1) * __ldg(wx + k - 1), t1 = __ldg(bz + k - 2) * __ldg(wx + k - 2);
-          const double t2 = __ldg(bz + k - 3) * __ldg(wx + k - 3), t3 = __ldg(bz + k - 4) * __ldg(wx + k - 4);
-          acc = amr_round_f32(acc + t0);
-          acc = amr_round_f32(acc + t1);
-          acc = amr_round_f32(acc + t2);
-          acc = amr_round_f32(acc + t3);
-        }
-        for (; k > s0; k--) acc = amr_round_f32(acc + __ldg(bz + k - 1) * __ldg(wx + k - 1));
-      }
-    }
+    const int oy = ((ty - sy3[b] + l1 + 1) % l1) - 1;
+    const int ox = ((tx - sx3[c] + l1 + 1) % l1) - 1;
+    const uint64_t s = ((uint64_t)sz3[a] * l1 + (uint64_t)sy3[b]) * l1 + (uint64_t)sx3[c];
+    s0 = start[s];
+    cnt = start[s + 1] - s0;
+    slot = (uint32_t)(9 * (oz + 1) + 3 * (oy + 1) + (ox + 1));
   }
-  dens[t] = (float)acc;
+  uint32_t inc = cnt;   // inclusive scan of the counts
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t v = __shfl_up_sync(FULL, inc, off);
+    if ((int)lane >= off) inc += v;
+  }
+  const unsigned nz = __ballot_sync(FULL, cnt > 0u);
+  if (cnt > 0u) sh[wid][__popc(nz & ((1u << lane) - 1u))] = AmrSrc{s0, cnt, slot, inc - cnt};
+  __syncwarp();
+  const uint32_t nterm = __shfl_sync(FULL, inc, 31);
+  const float d = nterm ? amr_warp_sum<true>(sh[wid], __popc(nz), nterm, wts, n) : (float)(-1.0);
+  if (lane == 0u) dens[t] = d;
 }
 
 // refinement flag of every coarse node: any of its 18 nodes at dz, dy in
@@ -256,7 +256,7 @@ void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z
   for (int o = 0; o < 9; o++) W.b[o] = wts + (uint64_t)o * n;
   for (int o = 0; o < 3; o++) W.x[o] = wts + (uint64_t)(9 + o) * n;
   k_amr_weights<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, W);
-  k_amr_dens<<<(unsigned)((nn + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, start, W, dens);
+  k_amr_dens<<<(unsigned)((nn + kAmrT / 32 - 1) / (kAmrT / 32)), kAmrT, 0, st>>>(l1, start, wts, n, dens);
 }
 
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st) {

@@ -53,6 +53,7 @@
 
 #include "common.cuh"
 #include "amr_tree.cuh"
+#include "amr_sum.cuh"
 
 namespace ahfgpu {
 
@@ -543,12 +544,27 @@ __global__ void __launch_bounds__(kAgT) k_ag_domain(int l1, APRun* __restrict__ 
 // ---------------------------------------------------------------------------
 // relink
 
+// the node of key `want` (keys ascend with the node index), or -1
+__device__ __forceinline__ int ag_find_key(const uint64_t* __restrict__ key, int nn, uint64_t want) {
+  int lo = 0, hi = nn;   // first key >= want
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (key[mid] < want) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < nn && key[lo] == want) ? lo : -1;
+}
+
 // the fine node each listed particle of the coarse grid moves to, or -1.
 // Slot k of the coarse lists holds particle ord[k] of coarse node cnode[k].
+// The children of a refined node are a 2 x 2 x 2 block (fine node runs
+// start and end on even x, fine rows and planes come in identical pairs), so
+// child (a, b, c) is i0 + a P + b R + c, i0 the first child, R and P the
+// nodes of its fine row and plane; each child is checked against its key and
+// searched for where that layout would not give it.
 __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t* __restrict__ ord,
                                                     const uint64_t* __restrict__ cnode,
-                                                    const uint64_t* __restrict__ ckey, int l1c,
-                                                    const uint64_t* __restrict__ fkey, int nnf,
+                                                    const uint64_t* __restrict__ ckey, int l1c, AGrid gf,
                                                     const uint8_t* __restrict__ fflag, const float* __restrict__ x,
                                                     const float* __restrict__ y, const float* __restrict__ z,
                                                     int* __restrict__ dest, uint32_t* __restrict__ moved) {
@@ -558,25 +574,34 @@ __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t*
   const uint64_t L = (uint64_t)l1c;
   const int cx = (int)(ck % L), cy = (int)((ck / L) % L), cz = (int)(ck / (L * L));
   const int l1f = 2 * l1c;
+  const uint64_t Lf = (uint64_t)l1f;
   const double dl = (double)l1f, shift = 0.5 / dl;
-  const uint32_t p = ord[k];
-  const double px = (double)x[p], py = (double)y[p], pz = (double)z[p];
+  const uint64_t base = ((uint64_t)(2 * cz) * Lf + (uint64_t)(2 * cy)) * Lf + (uint64_t)(2 * cx);
   int to = -1;
-  for (int a = 0; a < 2 && to < 0; a++)
-    for (int b = 0; b < 2 && to < 0; b++)
-      for (int c = 0; c < 2 && to < 0; c++) {
-        const int fz = 2 * cz + a, fy = 2 * cy + b, fx = 2 * cx + c;
-        const uint64_t want = ((uint64_t)fz * (uint64_t)l1f + (uint64_t)fy) * (uint64_t)l1f + (uint64_t)fx;
-        int lo = 0, hi = nnf;   // first key >= want
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (fkey[mid] < want) lo = mid + 1;
-          else hi = mid;
+  const int i0 = ag_find_key(gf.key, gf.nn, base);
+  if (i0 >= 0) {
+    const ARow Rw = gf.R[gf.N[gf.nseg[i0]].row];
+    const ANRun Rl = gf.N[Rw.s0 + Rw.ns - 1];
+    const int rlen = Rl.n0 + Rl.len - gf.N[Rw.s0].n0;
+    const APlane Pl = gf.pl[Rw.pl];
+    const ACRun C0 = gf.C[Pl.c0], C1 = gf.C[Pl.c0 + Pl.nc - 1];
+    const ARow Rf = gf.R[C0.r0], Rz = gf.R[C1.r0 + C1.len - 1];
+    const ANRun Pz = gf.N[Rz.s0 + Rz.ns - 1];
+    const int plen = Pz.n0 + Pz.len - gf.N[Rf.s0].n0;
+    const uint32_t p = ord[k];
+    const double px = (double)x[p], py = (double)y[p], pz = (double)z[p];
+    for (int a = 0; a < 2 && to < 0; a++)
+      for (int b = 0; b < 2 && to < 0; b++)
+        for (int c = 0; c < 2 && to < 0; c++) {
+          const uint64_t want = base + ((uint64_t)a * Lf + (uint64_t)b) * Lf + (uint64_t)c;
+          int i = i0 + a * plen + b * rlen + c;
+          if (i >= gf.nn || gf.key[i] != want) i = ag_find_key(gf.key, gf.nn, want);
+          if (i < 0 || !(fflag[i] & kAgAll)) continue;
+          const int fz = 2 * cz + a, fy = 2 * cy + b, fx = 2 * cx + c;
+          const double ccx = (double)fx / dl + shift, ccy = (double)fy / dl + shift, ccz = (double)fz / dl + shift;
+          if (fabs(px - ccx) <= shift && fabs(py - ccy) <= shift && fabs(pz - ccz) <= shift) to = i;
         }
-        if (lo >= nnf || fkey[lo] != want || !(fflag[lo] & kAgAll)) continue;
-        const double ccx = (double)fx / dl + shift, ccy = (double)fy / dl + shift, ccz = (double)fz / dl + shift;
-        if (fabs(px - ccx) <= shift && fabs(py - ccy) <= shift && fabs(pz - ccz) <= shift) to = lo;
-      }
+  }
   dest[k] = to;
   moved[k] = to >= 0 ? 1u : 0u;
 }
@@ -667,70 +692,86 @@ __global__ void __launch_bounds__(kAgT) k_ag_extras(int nn, const uint32_t* __re
   }
 }
 
-// one thread per target: -1, then its sources in node order, each source's
-// particles in list order (descending slots when `desc`).  A target has at
-// most 27 sources (one per stencil position).
+// One warp per target: -1, then its sources in node order, each source's
+// particles in list order (descending slots when `desc`).  Lane j < 27 takes
+// the node at the target's stencil slot j when it has particles: such a node
+// has all 27 of its TSC nodes (relink moves particles only into those), so
+// its own slot 26 - j is the node at the target's coordinates, the target.
+// The listed one-sided sources follow; the candidates are ranked by node
+// index (a target has at most 27 sources, one per stencil position), laid
+// out in shared memory with their term offsets, and summed by amr_warp_sum.
 __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict__ tsc,
                                                   const uint32_t* __restrict__ eoff,
                                                   const uint64_t* __restrict__ extra,
                                                   const uint32_t* __restrict__ start, const double* __restrict__ w,
                                                   uint32_t np, int desc, float* __restrict__ dens,
                                                   int* __restrict__ err) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nn) return;
-  int cs[27], ck[27];
-  int nc = 0;
-  bool over = false;
-  auto add = [&](int s, int k) {
-    if (nc == 27) { over = true; return; }
-    int i = nc++;
-    while (i > 0 && cs[i - 1] > s) { cs[i] = cs[i - 1]; ck[i] = ck[i - 1]; i--; }
-    cs[i] = s;
-    ck[i] = k;
-  };
-  for (int j = 0; j < 27; j++) {
-    const int s = tsc[(int64_t)t * 27 + j];
-    if (s >= 0 && start[s + 1] > start[s] && tsc[(int64_t)s * 27 + (26 - j)] == t) add(s, 26 - j);
-  }
-  for (uint32_t e = eoff[t]; e < eoff[t + 1]; e++) add((int)(extra[e] >> 5), (int)(extra[e] & 31u));
-  if (over) atomicExch(err, 1);
-  // the float density as a double holding a float (amr_round_f32 after
-  // every addition, as the reference's += on a float rounds)
-  double acc = -1.0;
-  const uint64_t n = np;
-  for (int c = 0; c < nc; c++) {
-    const uint32_t s = (uint32_t)cs[c], slot = (uint32_t)ck[c];
-    const double* __restrict__ bz = w + (uint64_t)(slot / 3u) * n;
-    const double* __restrict__ wx = w + (uint64_t)(9u + slot % 3u) * n;
-    const uint32_t s0 = start[s], s1 = start[s + 1];
-    // four terms at a time (independent loads and products, only the sums
-    // chain), then one at a time: no predicated-off FP64 instructions, which
-    // would still take FP64 issue slots
-    if (desc) {
-      uint32_t k = s1;
-      for (; k >= s0 + 4; k -= 4) {
-        const double t0 = __ldg(bz + k - 1) * __ldg(wx + k - 1), t1 = __ldg(bz + k - 2) * __ldg(wx + k - 2);
-        const double t2 = __ldg(bz + k - 3) * __ldg(wx + k - 3), t3 = __ldg(bz + k - 4) * __ldg(wx + k - 4);
-        acc = amr_round_f32(acc + t0);
-        acc = amr_round_f32(acc + t1);
-        acc = amr_round_f32(acc + t2);
-        acc = amr_round_f32(acc + t3);
-      }
-      for (; k > s0; k--) acc = amr_round_f32(acc + __ldg(bz + k - 1) * __ldg(wx + k - 1));
-    } else {
-      uint32_t k = s0;
-      for (; k + 4 <= s1; k += 4) {
-        const double t0 = __ldg(bz + k) * __ldg(wx + k), t1 = __ldg(bz + k + 1) * __ldg(wx + k + 1);
-        const double t2 = __ldg(bz + k + 2) * __ldg(wx + k + 2), t3 = __ldg(bz + k + 3) * __ldg(wx + k + 3);
-        acc = amr_round_f32(acc + t0);
-        acc = amr_round_f32(acc + t1);
-        acc = amr_round_f32(acc + t2);
-        acc = amr_round_f32(acc + t3);
-      }
-      for (; k < s1; k++) acc = amr_round_f32(acc + __ldg(bz + k) * __ldg(wx + k));
+  __shared__ AmrSrc sh[kAgT / 32][32];
+  __shared__ int cs[kAgT / 32][32];
+  __shared__ uint32_t ck[kAgT / 32][32];
+  const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  const int t = (int)(blockIdx.x * (kAgT / 32) + wid);
+  if (t >= nn) return;   // uniform over the warp
+  int s = -1;
+  uint32_t slot = 0;
+  if (lane < 27u) {
+    const int c = tsc[(int64_t)t * 27 + lane];
+    if (c >= 0 && start[c + 1] > start[c]) {
+      s = c;
+      slot = 26u - lane;
     }
   }
-  dens[t] = (float)acc;
+  const unsigned reg = __ballot_sync(FULL, s >= 0);
+  const int nreg = __popc(reg);
+  if (s >= 0) {
+    const int at = __popc(reg & ((1u << lane) - 1u));
+    cs[wid][at] = s;
+    ck[wid][at] = slot;
+  }
+  const uint32_t e0 = eoff[t], ne = eoff[t + 1] - e0;
+  int total = nreg + (int)ne;
+  if (total > 27) {
+    if (lane == 0u) atomicExch(err, 1);
+    total = 27;
+  }
+  if ((int)lane < total - nreg) {
+    const uint64_t e = extra[e0 + lane];
+    cs[wid][nreg + (int)lane] = (int)(e >> 5);
+    ck[wid][nreg + (int)lane] = (uint32_t)(e & 31u);
+  }
+  __syncwarp();
+  // rank by node index (distinct), the source's slots, then term offsets
+  uint32_t s0 = 0, cnt = 0;
+  int rank = 0, my = -1;
+  uint32_t myslot = 0;
+  if ((int)lane < total) {
+    my = cs[wid][lane];
+    myslot = ck[wid][lane];
+    for (int k = 0; k < total; k++) rank += cs[wid][k] < my ? 1 : 0;
+    s0 = start[my];
+    cnt = start[my + 1] - s0;
+  }
+  // counts in rank order: each lane reads the count of the rank-th source
+  __syncwarp();
+  if ((int)lane < total) ck[wid][rank] = cnt;
+  __syncwarp();
+  uint32_t rc = (int)lane < total ? ck[wid][lane] : 0u;
+  uint32_t inc = rc;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t v = __shfl_up_sync(FULL, inc, off);
+    if ((int)lane >= off) inc += v;
+  }
+  const uint32_t cum_rank = inc - rc;   // term offset of the source of rank `lane`
+  const uint32_t nterm = __shfl_sync(FULL, inc, 31);
+  // each source's entry at its rank, with the offset of that rank
+  const uint32_t mycum = __shfl_sync(FULL, cum_rank, rank & 31);
+  if ((int)lane < total) sh[wid][rank] = AmrSrc{s0, cnt, myslot, mycum};
+  __syncwarp();
+  float d = (float)(-1.0);
+  if (nterm) d = desc ? amr_warp_sum<true>(sh[wid], total, nterm, w, np)
+                      : amr_warp_sum<false>(sh[wid], total, nterm, w, np);
+  if (lane == 0u) dens[t] = d;
 }
 
 // node coordinates (z, y, x) from the keys
@@ -800,10 +841,10 @@ void ag_fnodes(int nN, int l1, const ANRun* N, const ARow* R, const APlane* pl, 
 }
 
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const uint64_t* fkey, int nnf, const uint8_t* fflag, const float* x, const float* y, const float* z,
-               int* dest, uint32_t* moved, cudaStream_t st) {
+               const AGrid& gf, const uint8_t* fflag, const float* x, const float* y, const float* z, int* dest,
+               uint32_t* moved, cudaStream_t st) {
   if (np > 0)
-    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, fkey, nnf, fflag, x, y, z, dest, moved);
+    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, fflag, x, y, z, dest, moved);
 }
 
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,
@@ -823,7 +864,9 @@ void ag_extras(int nn, const uint32_t* start, const int* tsc, int pass, uint32_t
 
 void ag_dens(int nn, const int* tsc, const uint32_t* eoff, const uint64_t* extra, const uint32_t* start,
              const double* w, uint32_t np, int desc, float* dens, int* err, cudaStream_t st) {
-  if (nn > 0) k_ag_dens<<<ag_blocks(nn), kAgT, 0, st>>>(nn, tsc, eoff, extra, start, w, np, desc, dens, err);
+  if (nn > 0)
+    k_ag_dens<<<(unsigned)(((int64_t)nn + kAgT / 32 - 1) / (kAgT / 32)), kAgT, 0, st>>>(nn, tsc, eoff, extra, start, w,
+                                                                                       np, desc, dens, err);
 }
 
 void ag_zyx(int nn, int l1, const uint64_t* key, int32_t* zyx, cudaStream_t st) {

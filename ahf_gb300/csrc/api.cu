@@ -1751,8 +1751,8 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
         (rc = g.at_iA.ensure((size_t)npc * 4 + 4)) || (rc = g.at_iB.ensure((size_t)npc * 4 + 4)))
       return rc;
     CK(cudaMemsetAsync(g.at_cnt.p, 0, (fnn + 1) * 4, st));
-    ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, f.key.as<uint64_t>(),
-              f.nn, f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(), st);
+    ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, agrid_of(f),
+              f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(), st);
     if ((rc = amr_scan(g.at_moved.as<uint32_t>(), g.at_moff.as<uint32_t>(), npc, st))) return rc;
     ag_compact(npc, g.at_dest.as<int>(), g.at_moff.as<uint32_t>(), c.ord.as<uint32_t>(), g.at_kA.as<uint64_t>(),
                g.at_iA.as<uint32_t>(), g.at_cnt.as<uint32_t>(), st);
