@@ -45,7 +45,7 @@ struct AmrTr {
 
 constexpr int kAmrSat = 1 << 25;
 
-__device__ __forceinline__ AmrTr amr_compose(const AmrTr& L, const AmrTr& R) {
+__host__ __device__ __forceinline__ AmrTr amr_compose(const AmrTr& L, const AmrTr& R) {
   const unsigned q0 = L.pb & 1u, q1 = (L.pb >> 1) & 1u;
   AmrTr o;
   const int a0 = L.r0 + (q0 ? R.r1 : R.r0), a1 = L.r1 + (q1 ? R.r1 : R.r0);
@@ -56,8 +56,8 @@ __device__ __forceinline__ AmrTr amr_compose(const AmrTr& L, const AmrTr& R) {
 }
 
 // the map of one term t >= 0 in the binade of float exponent ef
-__device__ __forceinline__ AmrTr amr_term_map(double t, int ef) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+__host__ __device__ __forceinline__ AmrTr amr_term_map(double t, int ef) {
+  const unsigned long long b = amr_bits(t);
   unsigned long long Q = 0;
   bool big = false;
   if (b != 0ull) {
@@ -150,7 +150,7 @@ __device__ float amr_warp_sum(const AmrSrc* __restrict__ src, int nsrc, uint32_t
     const int Ak = neg ? A - R : A + R;
     const bool leave = lane < m && (neg ? Ak <= (1 << 23) : Ak >= (1 << 24));
     const unsigned ex = __ballot_sync(FULL, leave);
-    const double u = __longlong_as_double((long long)((unsigned long long)(ef - 23 + 1023) << 52));
+    const double u = amr_from_bits((unsigned long long)(ef - 23 + 1023) << 52);
     if (ex == 0u) {
       const int An = __shfl_sync(FULL, Ak, (int)m - 1);
       acc = (neg ? -(double)An : (double)An) * u;

@@ -3,6 +3,7 @@
 // wrappers of amr_tree.cu.
 #pragma once
 #include <cstdint>
+#include <cstring>
 
 #include <cuda_runtime.h>
 
@@ -15,14 +16,36 @@ namespace ahfgpu {
 // (zero, subnormal float results, the top binade, inf, NaN) through the
 // conversions.  The TSC density sums round to float after every double
 // addition, so this runs once per term.
-__device__ __forceinline__ double amr_round_f32(double s) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(s);
+// the bits of a double and back (host code too: the host checks of the
+// summation rules compile these helpers)
+__host__ __device__ __forceinline__ unsigned long long amr_bits(double d) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long b;
+  memcpy(&b, &d, 8);
+  return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ double amr_from_bits(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ double amr_round_f32(double s) {
+  const unsigned long long b = amr_bits(s);
   const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
   if (e - 897u <= 252u) {   // biased exponent 897 .. 1149: float exponent 1 .. 253
     unsigned long long m = b & 0x7fffffffffffffffull;
     m += 0x0fffffffull + ((m >> 29) & 1ull);
     m &= ~0x1fffffffull;
-    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | m));
+    return amr_from_bits((b & 0x8000000000000000ull) | m);
   }
   return (double)(float)s;
 }
