@@ -555,16 +555,34 @@ __device__ __forceinline__ int ag_find_key(const uint64_t* __restrict__ key, int
   return (lo < nn && key[lo] == want) ? lo : -1;
 }
 
+// the first child of every refined coarse node: a fine node with even
+// (z, y, x) is child (0, 0, 0) of the coarse node at half its coordinates
+__global__ void __launch_bounds__(kAgT) k_ag_child0(int nnf, const uint64_t* __restrict__ fkey, int l1f,
+                                                    const uint64_t* __restrict__ ckey, int nnc,
+                                                    int* __restrict__ child0) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nnf) return;
+  const uint64_t k = fkey[i], L = (uint64_t)l1f;
+  const uint64_t x = k % L, y = (k / L) % L, z = k / (L * L);
+  if ((x | y | z) & 1ull) return;
+  const uint64_t Lc = L / 2;
+  const uint64_t want = ((z / 2) * Lc + y / 2) * Lc + x / 2;
+  const int c = ag_find_key(ckey, nnc, want);
+  if (c >= 0) child0[c] = i;
+}
+
 // the fine node each listed particle of the coarse grid moves to, or -1.
 // Slot k of the coarse lists holds particle ord[k] of coarse node cnode[k].
 // The children of a refined node are a 2 x 2 x 2 block (fine node runs
 // start and end on even x, fine rows and planes come in identical pairs), so
 // child (a, b, c) is i0 + a P + b R + c, i0 the first child, R and P the
 // nodes of its fine row and plane; each child is checked against its key and
-// searched for where that layout would not give it.
+// searched for where that layout would not give it.  i0 comes from the
+// first-child table of the coarse nodes (k_ag_child0).
 __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t* __restrict__ ord,
                                                     const uint64_t* __restrict__ cnode,
                                                     const uint64_t* __restrict__ ckey, int l1c, AGrid gf,
+                                                    const int* __restrict__ child0,
                                                     const uint8_t* __restrict__ fflag, const float* __restrict__ x,
                                                     const float* __restrict__ y, const float* __restrict__ z,
                                                     int* __restrict__ dest, uint32_t* __restrict__ moved) {
@@ -578,7 +596,7 @@ __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t*
   const double dl = (double)l1f, shift = 0.5 / dl;
   const uint64_t base = ((uint64_t)(2 * cz) * Lf + (uint64_t)(2 * cy)) * Lf + (uint64_t)(2 * cx);
   int to = -1;
-  const int i0 = ag_find_key(gf.key, gf.nn, base);
+  const int i0 = child0[cnode[k]];
   if (i0 >= 0) {
     const ARow Rw = gf.R[gf.N[gf.nseg[i0]].row];
     const ANRun Rl = gf.N[Rw.s0 + Rw.ns - 1];
@@ -840,11 +858,15 @@ void ag_fnodes(int nN, int l1, const ANRun* N, const ARow* R, const APlane* pl, 
   if (nN > 0) k_ag_fnodes<<<ag_blocks(nN), kAgT, 0, st>>>(nN, l1, N, R, pl, key, nseg);
 }
 
+void ag_child0(int nnf, const uint64_t* fkey, int l1f, const uint64_t* ckey, int nnc, int* child0, cudaStream_t st) {
+  if (nnf > 0) k_ag_child0<<<ag_blocks(nnf), kAgT, 0, st>>>(nnf, fkey, l1f, ckey, nnc, child0);
+}
+
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const AGrid& gf, const uint8_t* fflag, const float* x, const float* y, const float* z, int* dest,
-               uint32_t* moved, cudaStream_t st) {
+               const AGrid& gf, const int* child0, const uint8_t* fflag, const float* x, const float* y,
+               const float* z, int* dest, uint32_t* moved, cudaStream_t st) {
   if (np > 0)
-    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, fflag, x, y, z, dest, moved);
+    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, child0, fflag, x, y, z, dest, moved);
 }
 
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,

@@ -229,7 +229,7 @@ struct Ctx {
   // the radix passes, the density pairs
   DBuf at_rrun, at_rnode, at_rref, at_runoff, at_runs, at_pref, at_po, at_pnc, at_pnsel, at_rroff, at_seloff;
   DBuf at_rr, at_sel, at_fpl, at_tot, at_dest, at_moved, at_moff, at_cnt, at_kA, at_kB, at_iA, at_iB;
-  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt;
+  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt, at_child;
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -989,7 +989,7 @@ int ahfgpu_shutdown(void) {
                   &g.at_rref, &g.at_runoff, &g.at_runs, &g.at_pref, &g.at_po, &g.at_pnc, &g.at_pnsel, &g.at_rroff,
                   &g.at_seloff, &g.at_rr, &g.at_sel, &g.at_fpl, &g.at_tot, &g.at_dest, &g.at_moved, &g.at_moff,
                   &g.at_cnt, &g.at_kA, &g.at_kB, &g.at_iA, &g.at_iB, &g.at_gh, &g.at_goff, &g.at_part, &g.at_err,
-                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt};
+                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt, &g.at_child};
   for (DBuf* b : bufs) b->release();
   for (Ctx::AmrLevel& L : g.amr_lv)
     for (DBuf* b : {&L.P, &L.pl, &L.C, &L.R, &L.N, &L.key, &L.nseg, &L.tsc, &L.flag, &L.dens, &L.start, &L.ord, &L.node})
@@ -1751,8 +1751,12 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
         (rc = g.at_iA.ensure((size_t)npc * 4 + 4)) || (rc = g.at_iB.ensure((size_t)npc * 4 + 4)))
       return rc;
     CK(cudaMemsetAsync(g.at_cnt.p, 0, (fnn + 1) * 4, st));
+    if ((rc = g.at_child.ensure((size_t)c.nn * 4 + 4))) return rc;
+    CK(cudaMemsetAsync(g.at_child.p, 0xff, (size_t)c.nn * 4, st));   // -1: not refined
+    ag_child0(f.nn, f.key.as<uint64_t>(), f.l1, c.key.as<uint64_t>(), c.nn, g.at_child.as<int>(), st);
     ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, agrid_of(f),
-              f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(), st);
+              g.at_child.as<int>(), f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(),
+              st);
     if ((rc = amr_scan(g.at_moved.as<uint32_t>(), g.at_moff.as<uint32_t>(), npc, st))) return rc;
     ag_compact(npc, g.at_dest.as<int>(), g.at_moff.as<uint32_t>(), c.ord.as<uint32_t>(), g.at_kA.as<uint64_t>(),
                g.at_iA.as<uint32_t>(), g.at_cnt.as<uint32_t>(), st);
