@@ -555,20 +555,30 @@ __device__ __forceinline__ int ag_find_key(const uint64_t* __restrict__ key, int
   return (lo < nn && key[lo] == want) ? lo : -1;
 }
 
-// the first child of every refined coarse node: a fine node with even
-// (z, y, x) is child (0, 0, 0) of the coarse node at half its coordinates
-__global__ void __launch_bounds__(kAgT) k_ag_child0(int nnf, const uint64_t* __restrict__ fkey, int l1f,
-                                                    const uint64_t* __restrict__ ckey, int nnc,
-                                                    int* __restrict__ child0) {
+// the first child of every refined coarse node, with the nodes of its fine
+// row and plane: a fine node with even (z, y, x) is child (0, 0, 0) of the
+// coarse node at half its coordinates.  child[c] = {i0, R, P, 0}; i0 = -1
+// where the coarse node is not refined (set before the launch).
+__global__ void __launch_bounds__(kAgT) k_ag_child0(AGrid gf, const uint64_t* __restrict__ ckey, int nnc,
+                                                    int4* __restrict__ child) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nnf) return;
-  const uint64_t k = fkey[i], L = (uint64_t)l1f;
+  if (i >= gf.nn) return;
+  const uint64_t k = gf.key[i], L = (uint64_t)gf.l1;
   const uint64_t x = k % L, y = (k / L) % L, z = k / (L * L);
   if ((x | y | z) & 1ull) return;
   const uint64_t Lc = L / 2;
   const uint64_t want = ((z / 2) * Lc + y / 2) * Lc + x / 2;
   const int c = ag_find_key(ckey, nnc, want);
-  if (c >= 0) child0[c] = i;
+  if (c < 0) return;
+  const ARow Rw = gf.R[gf.N[gf.nseg[i]].row];
+  const ANRun Rl = gf.N[Rw.s0 + Rw.ns - 1];
+  const int rlen = Rl.n0 + Rl.len - gf.N[Rw.s0].n0;
+  const APlane Pl = gf.pl[Rw.pl];
+  const ACRun C0 = gf.C[Pl.c0], C1 = gf.C[Pl.c0 + Pl.nc - 1];
+  const ARow Rf = gf.R[C0.r0], Rz = gf.R[C1.r0 + C1.len - 1];
+  const ANRun Pz = gf.N[Rz.s0 + Rz.ns - 1];
+  const int plen = Pz.n0 + Pz.len - gf.N[Rf.s0].n0;
+  child[c] = make_int4(i, rlen, plen, 0);
 }
 
 // the fine node each listed particle of the coarse grid moves to, or -1.
@@ -577,12 +587,13 @@ __global__ void __launch_bounds__(kAgT) k_ag_child0(int nnf, const uint64_t* __r
 // start and end on even x, fine rows and planes come in identical pairs), so
 // child (a, b, c) is i0 + a P + b R + c, i0 the first child, R and P the
 // nodes of its fine row and plane; each child is checked against its key and
-// searched for where that layout would not give it.  i0 comes from the
-// first-child table of the coarse nodes (k_ag_child0).
+// searched for where that layout would not give it.  i0, R and P come from
+// the coarse nodes' child table (k_ag_child0): the particles are in coarse
+// node order, so neighbouring threads read the same entries.
 __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t* __restrict__ ord,
                                                     const uint64_t* __restrict__ cnode,
                                                     const uint64_t* __restrict__ ckey, int l1c, AGrid gf,
-                                                    const int* __restrict__ child0,
+                                                    const int4* __restrict__ child,
                                                     const uint8_t* __restrict__ fflag, const float* __restrict__ x,
                                                     const float* __restrict__ y, const float* __restrict__ z,
                                                     int* __restrict__ dest, uint32_t* __restrict__ moved) {
@@ -596,16 +607,10 @@ __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t*
   const double dl = (double)l1f, shift = 0.5 / dl;
   const uint64_t base = ((uint64_t)(2 * cz) * Lf + (uint64_t)(2 * cy)) * Lf + (uint64_t)(2 * cx);
   int to = -1;
-  const int i0 = child0[cnode[k]];
+  const int4 ch = child[cnode[k]];
+  const int i0 = ch.x;
   if (i0 >= 0) {
-    const ARow Rw = gf.R[gf.N[gf.nseg[i0]].row];
-    const ANRun Rl = gf.N[Rw.s0 + Rw.ns - 1];
-    const int rlen = Rl.n0 + Rl.len - gf.N[Rw.s0].n0;
-    const APlane Pl = gf.pl[Rw.pl];
-    const ACRun C0 = gf.C[Pl.c0], C1 = gf.C[Pl.c0 + Pl.nc - 1];
-    const ARow Rf = gf.R[C0.r0], Rz = gf.R[C1.r0 + C1.len - 1];
-    const ANRun Pz = gf.N[Rz.s0 + Rz.ns - 1];
-    const int plen = Pz.n0 + Pz.len - gf.N[Rf.s0].n0;
+    const int rlen = ch.y, plen = ch.z;
     const uint32_t p = ord[k];
     const double px = (double)x[p], py = (double)y[p], pz = (double)z[p];
     for (int a = 0; a < 2 && to < 0; a++)
@@ -762,10 +767,16 @@ __global__ void __launch_bounds__(kAgT) k_ag_dens(int nn, const int* __restrict_
   uint32_t s0 = 0, cnt = 0;
   int rank = 0, my = -1;
   uint32_t myslot = 0;
+  // the stencil slots give ascending node indices unless the stencil
+  // crosses a periodic face (or extras were appended): rank only then
+  const bool inorder = (int)lane + 1 >= total || cs[wid][lane] < cs[wid][lane + 1];
+  const bool sorted = __all_sync(FULL, inorder);
   if ((int)lane < total) {
     my = cs[wid][lane];
     myslot = ck[wid][lane];
-    for (int k = 0; k < total; k++) rank += cs[wid][k] < my ? 1 : 0;
+    if (sorted) rank = (int)lane;
+    else
+      for (int k = 0; k < total; k++) rank += cs[wid][k] < my ? 1 : 0;
     s0 = start[my];
     cnt = start[my + 1] - s0;
   }
@@ -858,15 +869,15 @@ void ag_fnodes(int nN, int l1, const ANRun* N, const ARow* R, const APlane* pl, 
   if (nN > 0) k_ag_fnodes<<<ag_blocks(nN), kAgT, 0, st>>>(nN, l1, N, R, pl, key, nseg);
 }
 
-void ag_child0(int nnf, const uint64_t* fkey, int l1f, const uint64_t* ckey, int nnc, int* child0, cudaStream_t st) {
-  if (nnf > 0) k_ag_child0<<<ag_blocks(nnf), kAgT, 0, st>>>(nnf, fkey, l1f, ckey, nnc, child0);
+void ag_child0(const AGrid& gf, const uint64_t* ckey, int nnc, int4* child, cudaStream_t st) {
+  if (gf.nn > 0) k_ag_child0<<<ag_blocks(gf.nn), kAgT, 0, st>>>(gf, ckey, nnc, child);
 }
 
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const AGrid& gf, const int* child0, const uint8_t* fflag, const float* x, const float* y,
+               const AGrid& gf, const int4* child, const uint8_t* fflag, const float* x, const float* y,
                const float* z, int* dest, uint32_t* moved, cudaStream_t st) {
   if (np > 0)
-    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, child0, fflag, x, y, z, dest, moved);
+    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, child, fflag, x, y, z, dest, moved);
 }
 
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,

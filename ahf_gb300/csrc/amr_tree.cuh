@@ -106,9 +106,9 @@ void ag_fplanes(int npl_f, const AFPlane* fpl, const uint32_t* rr_off, const uin
                 APlane* pl, ACRun* C, ARow* R, ANRun* N, cudaStream_t st);
 void ag_fnodes(int nN, int l1, const ANRun* N, const ARow* R, const APlane* pl, uint64_t* key, int* nseg,
                cudaStream_t st);
-void ag_child0(int nnf, const uint64_t* fkey, int l1f, const uint64_t* ckey, int nnc, int* child0, cudaStream_t st);
+void ag_child0(const AGrid& gf, const uint64_t* ckey, int nnc, int4* child, cudaStream_t st);
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const AGrid& gf, const int* child0, const uint8_t* fflag, const float* x, const float* y,
+               const AGrid& gf, const int4* child, const uint8_t* fflag, const float* x, const float* y,
                const float* z, int* dest, uint32_t* moved, cudaStream_t st);
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,
                 uint32_t* fidx_out, uint32_t* count, cudaStream_t st);

@@ -1751,11 +1751,11 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
         (rc = g.at_iA.ensure((size_t)npc * 4 + 4)) || (rc = g.at_iB.ensure((size_t)npc * 4 + 4)))
       return rc;
     CK(cudaMemsetAsync(g.at_cnt.p, 0, (fnn + 1) * 4, st));
-    if ((rc = g.at_child.ensure((size_t)c.nn * 4 + 4))) return rc;
-    CK(cudaMemsetAsync(g.at_child.p, 0xff, (size_t)c.nn * 4, st));   // -1: not refined
-    ag_child0(f.nn, f.key.as<uint64_t>(), f.l1, c.key.as<uint64_t>(), c.nn, g.at_child.as<int>(), st);
+    if ((rc = g.at_child.ensure((size_t)c.nn * 16 + 16))) return rc;
+    CK(cudaMemsetAsync(g.at_child.p, 0xff, (size_t)c.nn * 16, st));   // i0 = -1: not refined
+    ag_child0(agrid_of(f), c.key.as<uint64_t>(), c.nn, g.at_child.as<int4>(), st);
     ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, agrid_of(f),
-              g.at_child.as<int>(), f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(),
+              g.at_child.as<int4>(), f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(),
               st);
     if ((rc = amr_scan(g.at_moved.as<uint32_t>(), g.at_moff.as<uint32_t>(), npc, st))) return rc;
     ag_compact(npc, g.at_dest.as<int>(), g.at_moff.as<uint32_t>(), c.ord.as<uint32_t>(), g.at_kA.as<uint64_t>(),
