@@ -104,21 +104,30 @@ struct AmrW {
   double* x[3];
 };
 
+// a node's folded centre coordinate per grid index c, as the reference forms
+// it: fold((c / l1 + 1 / (2 l1)) + 1) -- one FP64 division per index here
+// instead of three per particle in the weights (FP64 is slow on this GPU)
+__global__ void __launch_bounds__(kAmrT) k_amr_cfold(int l1, double* __restrict__ cfold) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= l1) return;
+  const double dl1 = (double)l1, shift = 0.5 / dl1;
+  cfold[c] = amr_fold(((double)c / dl1 + shift) + 1.0);
+}
+
 __global__ void __launch_bounds__(kAmrT) k_amr_weights(int l1, uint32_t n, const uint64_t* __restrict__ skey,
                                                        const uint32_t* __restrict__ ord, const float* __restrict__ x,
                                                        const float* __restrict__ y, const float* __restrict__ z,
-                                                       AmrW W) {
+                                                       const double* __restrict__ cfold, AmrW W) {
   const double dl1 = (double)l1;
-  const double shift = 0.5 / dl1;
   const double m2d = (dl1 * dl1 * dl1) / (double)n;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint64_t node = skey[k];
     const uint32_t i = ord[k];
     const int cx = (int)(node % (uint64_t)l1), cy = (int)((node / (uint64_t)l1) % (uint64_t)l1),
               cz = (int)(node / ((uint64_t)l1 * l1));
-    const double sx = amr_sep(x[i], amr_fold(((double)cx / dl1 + shift) + 1.0), dl1);
-    const double sy = amr_sep(y[i], amr_fold(((double)cy / dl1 + shift) + 1.0), dl1);
-    const double sz = amr_sep(z[i], amr_fold(((double)cz / dl1 + shift) + 1.0), dl1);
+    const double sx = amr_sep(x[i], cfold[cx], dl1);
+    const double sy = amr_sep(y[i], cfold[cy], dl1);
+    const double sz = amr_sep(z[i], cfold[cz], dl1);
 #pragma unroll
     for (int oz = 0; oz < 3; oz++) {
       const double az = m2d * amr_w(sz, oz - 1);
@@ -250,12 +259,14 @@ void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l
 }
 
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint64_t* skey, const uint32_t* ord, double* wts, float* dens, int grid, cudaStream_t st) {
+              const uint64_t* skey, const uint32_t* ord, double* wts, double* cfold, float* dens, int grid,
+              cudaStream_t st) {
   const uint64_t nn = (uint64_t)l1 * l1 * l1;
   AmrW W;
   for (int o = 0; o < 9; o++) W.b[o] = wts + (uint64_t)o * n;
   for (int o = 0; o < 3; o++) W.x[o] = wts + (uint64_t)(9 + o) * n;
-  k_amr_weights<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, W);
+  k_amr_cfold<<<(unsigned)((l1 + kAmrT - 1) / kAmrT), kAmrT, 0, st>>>(l1, cfold);
+  k_amr_weights<<<grid, kAmrT, 0, st>>>(l1, (uint32_t)n, skey, ord, x, y, z, cfold, W);
   k_amr_dens<<<(unsigned)((nn + kAmrT / 32 - 1) / (kAmrT / 32)), kAmrT, 0, st>>>(l1, start, wts, n, dens);
 }
 

@@ -593,7 +593,7 @@ __global__ void __launch_bounds__(kAgT) k_ag_child0(AGrid gf, const uint64_t* __
 __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t* __restrict__ ord,
                                                     const uint64_t* __restrict__ cnode,
                                                     const uint64_t* __restrict__ ckey, int l1c, AGrid gf,
-                                                    const int4* __restrict__ child,
+                                                    const int4* __restrict__ child, const double* __restrict__ cen,
                                                     const uint8_t* __restrict__ fflag, const float* __restrict__ x,
                                                     const float* __restrict__ y, const float* __restrict__ z,
                                                     int* __restrict__ dest, uint32_t* __restrict__ moved) {
@@ -621,8 +621,7 @@ __global__ void __launch_bounds__(kAgT) k_ag_relink(uint32_t np, const uint32_t*
           if (i >= gf.nn || gf.key[i] != want) i = ag_find_key(gf.key, gf.nn, want);
           if (i < 0 || !(fflag[i] & kAgAll)) continue;
           const int fz = 2 * cz + a, fy = 2 * cy + b, fx = 2 * cx + c;
-          const double ccx = (double)fx / dl + shift, ccy = (double)fy / dl + shift, ccz = (double)fz / dl + shift;
-          if (fabs(px - ccx) <= shift && fabs(py - ccy) <= shift && fabs(pz - ccz) <= shift) to = i;
+          if (fabs(px - cen[fx]) <= shift && fabs(py - cen[fy]) <= shift && fabs(pz - cen[fz]) <= shift) to = i;
         }
   }
   dest[k] = to;
@@ -663,6 +662,19 @@ __device__ __forceinline__ double ag_sep(float p, double centre, double dl1) {
   return sep;
 }
 
+// per grid index c of a level: the node centre c / l1 + 1 / (2 l1) (relink's
+// half-cell test) and its fold((...) + 1) (the weights), formed as the
+// reference forms them -- one FP64 division per index instead of several per
+// particle
+__global__ void __launch_bounds__(kAgT) k_ag_centres(int l1, double* __restrict__ cen, double* __restrict__ cfold) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= l1) return;
+  const double dl = (double)l1, shift = 0.5 / dl;
+  const double v = (double)c / dl + shift;
+  cen[c] = v;
+  cfold[c] = ag_fold(v + 1.0);
+}
+
 // each listed particle's TSC factors in list-slot order: w[3 oz + oy] =
 // (m2d * w_z(oz - 1)) * w_y(oy - 1) and w[9 + ox] = w_x(ox - 1) at column
 // o * np + k (the first two products of the reference's left-to-right
@@ -671,17 +683,17 @@ __global__ void __launch_bounds__(kAgT) k_ag_weights(int l1, double m2d, uint32_
                                                      const uint64_t* __restrict__ nkey,
                                                      const uint32_t* __restrict__ ord, const float* __restrict__ x,
                                                      const float* __restrict__ y, const float* __restrict__ z,
-                                                     double* __restrict__ w) {
+                                                     const double* __restrict__ cfold, double* __restrict__ w) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= np) return;
-  const double dl1 = (double)l1, shift = 0.5 / dl1;
+  const double dl1 = (double)l1;
   const uint64_t key = nkey[node[k]];
   const uint64_t L = (uint64_t)l1;
   const int cx = (int)(key % L), cy = (int)((key / L) % L), cz = (int)(key / (L * L));
   const uint32_t i = ord[k];
-  const double sx = ag_sep(x[i], ag_fold(((double)cx / dl1 + shift) + 1.0), dl1);
-  const double sy = ag_sep(y[i], ag_fold(((double)cy / dl1 + shift) + 1.0), dl1);
-  const double sz = ag_sep(z[i], ag_fold(((double)cz / dl1 + shift) + 1.0), dl1);
+  const double sx = ag_sep(x[i], cfold[cx], dl1);
+  const double sy = ag_sep(y[i], cfold[cy], dl1);
+  const double sz = ag_sep(z[i], cfold[cz], dl1);
   const uint64_t n = np;
 #pragma unroll
   for (int oz = 0; oz < 3; oz++) {
@@ -874,10 +886,11 @@ void ag_child0(const AGrid& gf, const uint64_t* ckey, int nnc, int4* child, cuda
 }
 
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const AGrid& gf, const int4* child, const uint8_t* fflag, const float* x, const float* y,
-               const float* z, int* dest, uint32_t* moved, cudaStream_t st) {
+               const AGrid& gf, const int4* child, const double* cen, const uint8_t* fflag, const float* x,
+               const float* y, const float* z, int* dest, uint32_t* moved, cudaStream_t st) {
   if (np > 0)
-    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, child, fflag, x, y, z, dest, moved);
+    k_ag_relink<<<ag_blocks(np), kAgT, 0, st>>>(np, ord, cnode, ckey, l1c, gf, child, cen, fflag, x, y, z, dest,
+                                                 moved);
 }
 
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,
@@ -885,9 +898,13 @@ void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_
   if (np > 0) k_ag_compact<<<ag_blocks(np), kAgT, 0, st>>>(np, dest, off, ord, fkey_out, fidx_out, count);
 }
 
+void ag_centres(int l1, double* cen, double* cfold, cudaStream_t st) {
+  if (l1 > 0) k_ag_centres<<<ag_blocks(l1), kAgT, 0, st>>>(l1, cen, cfold);
+}
+
 void ag_weights(int l1, double m2d, uint32_t np, const uint64_t* node, const uint64_t* nkey, const uint32_t* ord,
-                const float* x, const float* y, const float* z, double* w, cudaStream_t st) {
-  if (np > 0) k_ag_weights<<<ag_blocks(np), kAgT, 0, st>>>(l1, m2d, np, node, nkey, ord, x, y, z, w);
+                const float* x, const float* y, const float* z, const double* cfold, double* w, cudaStream_t st) {
+  if (np > 0) k_ag_weights<<<ag_blocks(np), kAgT, 0, st>>>(l1, m2d, np, node, nkey, ord, x, y, z, cfold, w);
 }
 
 void ag_extras(int nn, const uint32_t* start, const int* tsc, int pass, uint32_t* ecount, const uint32_t* eoff,

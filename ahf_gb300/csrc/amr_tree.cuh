@@ -108,12 +108,13 @@ void ag_fnodes(int nN, int l1, const ANRun* N, const ARow* R, const APlane* pl, 
                cudaStream_t st);
 void ag_child0(const AGrid& gf, const uint64_t* ckey, int nnc, int4* child, cudaStream_t st);
 void ag_relink(uint32_t np, const uint32_t* ord, const uint64_t* cnode, const uint64_t* ckey, int l1c,
-               const AGrid& gf, const int4* child, const uint8_t* fflag, const float* x, const float* y,
-               const float* z, int* dest, uint32_t* moved, cudaStream_t st);
+               const AGrid& gf, const int4* child, const double* cen, const uint8_t* fflag, const float* x,
+               const float* y, const float* z, int* dest, uint32_t* moved, cudaStream_t st);
+void ag_centres(int l1, double* cen, double* cfold, cudaStream_t st);
 void ag_compact(uint32_t np, const int* dest, const uint32_t* off, const uint32_t* ord, uint64_t* fkey_out,
                 uint32_t* fidx_out, uint32_t* count, cudaStream_t st);
 void ag_weights(int l1, double m2d, uint32_t np, const uint64_t* node, const uint64_t* nkey, const uint32_t* ord,
-                const float* x, const float* y, const float* z, double* w, cudaStream_t st);
+                const float* x, const float* y, const float* z, const double* cfold, double* w, cudaStream_t st);
 void ag_extras(int nn, const uint32_t* start, const int* tsc, int pass, uint32_t* ecount, const uint32_t* eoff,
                uint32_t* efill, uint64_t* extra, cudaStream_t st);
 void ag_dens(int nn, const int* tsc, const uint32_t* eoff, const uint64_t* extra, const uint32_t* start,

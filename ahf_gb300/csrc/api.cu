@@ -66,7 +66,8 @@ void sfc_order(uint32_t n, const uint32_t* idx, uint64_t* order, int grid, cudaS
 void amr_cells(uint32_t n, const float* x, const float* y, const float* z, int l1, uint64_t* key, uint32_t* idx,
                uint32_t* count, int grid, cudaStream_t st);
 void amr_dens(int l1, uint64_t n, const float* x, const float* y, const float* z, const uint32_t* start,
-              const uint64_t* skey, const uint32_t* ord, double* wts, float* dens, int grid, cudaStream_t st);
+              const uint64_t* skey, const uint32_t* ord, double* wts, double* cfold, float* dens, int grid,
+              cudaStream_t st);
 void amr_flags(int l1, const float* dens, double thr, uint8_t* flag, uint32_t* rowcnt, cudaStream_t st);
 void amr_emit(int l1, const uint8_t* flag, const uint32_t* rowcnt, const uint32_t* rowoff, int64_t cap, int32_t* zyx,
               int* err, cudaStream_t st);
@@ -229,7 +230,8 @@ struct Ctx {
   // the radix passes, the density pairs
   DBuf at_rrun, at_rnode, at_rref, at_runoff, at_runs, at_pref, at_po, at_pnc, at_pnsel, at_rroff, at_seloff;
   DBuf at_rr, at_sel, at_fpl, at_tot, at_dest, at_moved, at_moff, at_cnt, at_kA, at_kB, at_iA, at_iB;
-  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt, at_child;
+  DBuf at_gh, at_goff, at_part, at_err, at_sums, at_w, at_ne, at_srcoff, at_tcnt, at_child, at_cen, at_cfold;
+  DBuf am_cfold;   // the domain grid's folded node centres
   // last device result description
   int64_t last_nhalo = -1;
   uint64_t last_nkept = 0, last_nbins = 0;
@@ -989,7 +991,8 @@ int ahfgpu_shutdown(void) {
                   &g.at_rref, &g.at_runoff, &g.at_runs, &g.at_pref, &g.at_po, &g.at_pnc, &g.at_pnsel, &g.at_rroff,
                   &g.at_seloff, &g.at_rr, &g.at_sel, &g.at_fpl, &g.at_tot, &g.at_dest, &g.at_moved, &g.at_moff,
                   &g.at_cnt, &g.at_kA, &g.at_kB, &g.at_iA, &g.at_iB, &g.at_gh, &g.at_goff, &g.at_part, &g.at_err,
-                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt, &g.at_child};
+                  &g.at_sums, &g.at_w, &g.at_ne, &g.at_srcoff, &g.at_tcnt, &g.at_child,
+                  &g.at_cen, &g.at_cfold, &g.am_cfold};
   for (DBuf* b : bufs) b->release();
   for (Ctx::AmrLevel& L : g.amr_lv)
     for (DBuf* b : {&L.P, &L.pl, &L.C, &L.R, &L.N, &L.key, &L.nseg, &L.tsc, &L.flag, &L.dens, &L.start, &L.ord, &L.node})
@@ -1540,7 +1543,9 @@ static int amr_domain_density_device_impl(uint64_t n, const float* x, const floa
   uint32_t* iin;
   if ((rc = amr_domain_lists(n, x, y, z, l1, st, &kin, &iin))) return rc;
   const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
-  amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), dens, grid, st);
+  if ((rc = g.am_cfold.ensure((size_t)l1 * 8 + 8))) return rc;
+  amr_dens(l1, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), g.am_cfold.as<double>(), dens,
+           grid, st);
   CK(cudaGetLastError());
   int derr = 0;
   CK(cudaMemcpyAsync(&derr, g.am_err.p, 4, cudaMemcpyDeviceToHost, st));
@@ -1676,7 +1681,9 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
     return rc;
   d.l1 = L; d.nP = 1; d.npl = L; d.nC = L; d.nR = L * L; d.nN = L * L; d.nn = (int)nn0; d.np = (uint32_t)n;
   const int pgrid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)g.nsm * 8, (n + 255) / 256));
-  amr_dens(L, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), d.dens.as<float>(), pgrid, st);
+  if ((rc = g.am_cfold.ensure((size_t)L * 8 + 8))) return rc;
+  amr_dens(L, n, x, y, z, g.am_start.as<uint32_t>(), kin, iin, g.am_seps.as<double>(), g.am_cfold.as<double>(),
+           d.dens.as<float>(), pgrid, st);
   CK(cudaMemcpyAsync(d.ord.p, iin, n * 4, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(d.node.p, kin, n * 8, cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(d.start.p, g.am_start.p, (nn0 + 1) * 4, cudaMemcpyDeviceToDevice, st));
@@ -1751,12 +1758,15 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
         (rc = g.at_iA.ensure((size_t)npc * 4 + 4)) || (rc = g.at_iB.ensure((size_t)npc * 4 + 4)))
       return rc;
     CK(cudaMemsetAsync(g.at_cnt.p, 0, (fnn + 1) * 4, st));
-    if ((rc = g.at_child.ensure((size_t)c.nn * 16 + 16))) return rc;
+    if ((rc = g.at_child.ensure((size_t)c.nn * 16 + 16)) || (rc = g.at_cen.ensure((size_t)f.l1 * 8 + 8)) ||
+        (rc = g.at_cfold.ensure((size_t)f.l1 * 8 + 8)))
+      return rc;
+    ag_centres(f.l1, g.at_cen.as<double>(), g.at_cfold.as<double>(), st);
     CK(cudaMemsetAsync(g.at_child.p, 0xff, (size_t)c.nn * 16, st));   // i0 = -1: not refined
     ag_child0(agrid_of(f), c.key.as<uint64_t>(), c.nn, g.at_child.as<int4>(), st);
     ag_relink(npc, c.ord.as<uint32_t>(), c.node.as<uint64_t>(), c.key.as<uint64_t>(), c.l1, agrid_of(f),
-              g.at_child.as<int4>(), f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(), g.at_moved.as<uint32_t>(),
-              st);
+              g.at_child.as<int4>(), g.at_cen.as<double>(), f.flag.as<uint8_t>(), x, y, z, g.at_dest.as<int>(),
+              g.at_moved.as<uint32_t>(), st);
     if ((rc = amr_scan(g.at_moved.as<uint32_t>(), g.at_moff.as<uint32_t>(), npc, st))) return rc;
     ag_compact(npc, g.at_dest.as<int>(), g.at_moff.as<uint32_t>(), c.ord.as<uint32_t>(), g.at_kA.as<uint64_t>(),
                g.at_iA.as<uint32_t>(), g.at_cnt.as<uint32_t>(), st);
@@ -1781,7 +1791,7 @@ static int amr_hierarchy_device_impl(uint64_t n, const float* x, const float* y,
         (rc = g.at_srcoff.ensure((fnn + 1) * 4)) || (rc = g.at_tcnt.ensure(fnn * 4 + 4)))
       return rc;
     ag_weights(f.l1, m2f, nm, f.node.as<uint64_t>(), f.key.as<uint64_t>(), f.ord.as<uint32_t>(), x, y, z,
-               g.at_w.as<double>(), st);
+               g.at_cfold.as<double>(), g.at_w.as<double>(), st);
     CK(cudaMemsetAsync(g.at_ne.p, 0, fnn * 4 + 4, st));
     ag_extras(f.nn, f.start.as<uint32_t>(), f.tsc.as<int>(), 0, g.at_ne.as<uint32_t>(), nullptr, nullptr, nullptr,
               st);
