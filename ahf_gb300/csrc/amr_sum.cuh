@@ -112,32 +112,43 @@ __device__ __forceinline__ double amr_term(const AmrSrc* __restrict__ src, int n
 }
 
 // -1 plus the node's terms in order, as the reference's float sum; every
-// lane of the warp calls it and gets the same value
+// lane of the warp calls it and gets the same value.  The accumulator is kept
+// as a double holding a float; its float fields are read from, and written
+// back into, the double's bits with integer arithmetic (the FP64 pipe of
+// this GPU is the bottleneck: it keeps only the terms' products and the
+// exact steps' additions).  A window's terms stay in the lanes: after an
+// exit at lane j the next window shifts them down by j + 1 lanes and forms
+// only the new ones.
 template <bool DESC>
 __device__ float amr_warp_sum(const AmrSrc* __restrict__ src, int nsrc, uint32_t nterm,
                               const double* __restrict__ w, uint64_t np) {
   const unsigned FULL = 0xffffffffu, lane = threadIdx.x & 31u;
   double acc = -1.0;
   uint32_t i = 0;
+  double t = 0.0;          // this lane's term, index i + lane, when have > lane
+  unsigned have = 0;       // terms of the window already formed
   while (i < nterm) {
-    const unsigned fb = __float_as_uint((float)acc);
-    const int E = (int)((fb >> 23) & 0xffu);
-    if (E == 0 || E >= 254) {
-      acc = amr_round_f32(acc + amr_term<DESC>(src, nsrc, i, w, np));
+    const unsigned m = nterm - i < 32u ? nterm - i : 32u;
+    if (lane < m && lane >= have) t = amr_term<DESC>(src, nsrc, i + lane, w, np);
+    have = m;
+    // the float fields of acc (exactly a float): exponent, magnitude in units of its ulp
+    const unsigned long long db = amr_bits(acc);
+    const int de = (int)((db >> 52) & 0x7ffu);
+    const int E = de == 0 ? 0 : de - 896;   // the float's biased exponent
+    if (E <= 0 || E >= 254) {
+      const double t0 = __shfl_sync(FULL, t, 0);
+      acc = amr_round_f32(acc + t0);
       i++;
+      t = __shfl_down_sync(FULL, t, 1);
+      have = have > 0u ? have - 1u : 0u;
       continue;
     }
     const int ef = E - 127;
-    const bool neg = (fb >> 31) != 0u;
-    const int A = (int)((fb & 0x7fffffu) | 0x800000u);
-    const unsigned m = nterm - i < 32u ? nterm - i : 32u;
-    double t = 0.0;
+    const bool neg = (db >> 63) != 0ull;
+    const int A = (int)(((db >> 29) & 0x7fffffull) | 0x800000ull);
     AmrTr T;
     T.r0 = 0; T.r1 = 0; T.pb = 2u;   // identity
-    if (lane < m) {
-      t = amr_term<DESC>(src, nsrc, i + lane, w, np);
-      T = amr_term_map(t, ef);
-    }
+    if (lane < m) T = amr_term_map(t, ef);
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
       AmrTr P;
@@ -150,19 +161,24 @@ __device__ float amr_warp_sum(const AmrSrc* __restrict__ src, int nsrc, uint32_t
     const int Ak = neg ? A - R : A + R;
     const bool leave = lane < m && (neg ? Ak <= (1 << 23) : Ak >= (1 << 24));
     const unsigned ex = __ballot_sync(FULL, leave);
-    const double u = amr_from_bits((unsigned long long)(ef - 23 + 1023) << 52);
+    // the float of magnitude An ulps in this binade, as the bits of a double
+    const unsigned long long hi = (db & 0x8000000000000000ull) | ((unsigned long long)(ef + 1023) << 52);
     if (ex == 0u) {
       const int An = __shfl_sync(FULL, Ak, (int)m - 1);
-      acc = (neg ? -(double)An : (double)An) * u;
+      acc = amr_from_bits(hi | ((unsigned long long)(An & 0x7fffff) << 29));
       i += m;
+      have = 0;
     } else {
       const int j = __ffs((int)ex) - 1;
       const int Ap = __shfl_sync(FULL, Ak, j > 0 ? j - 1 : 0);
       const double tj = __shfl_sync(FULL, t, j);
       const int Ab = j > 0 ? Ap : A;
-      acc = (neg ? -(double)Ab : (double)Ab) * u;
+      acc = amr_from_bits(hi | ((unsigned long long)(Ab & 0x7fffff) << 29));
       acc = amr_round_f32(acc + tj);
       i += (uint32_t)j + 1u;
+      // the window's later terms move down to their new lanes
+      t = __shfl_down_sync(FULL, t, (unsigned)j + 1u);
+      have = m - (unsigned)j - 1u;
     }
   }
   return (float)acc;
