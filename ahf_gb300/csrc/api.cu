@@ -50,9 +50,14 @@ void gather_halos(int pass, int G, const uint32_t* start, const float4* sorted, 
                   cudaStream_t st);
 void gather_offsets(const uint64_t* cnt, int64_t nhalo, uint64_t* off, cudaStream_t st);
 int gather_sort_setup();
-void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
-                 uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int* err, int grid,
-                 cudaStream_t st);
+int gather_window_shift_max();
+size_t gather_item_bytes();
+void gather_order_pack(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
+                       uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int wshift,
+                       int mode, void* items, uint64_t icap, int32_t* fbq, unsigned int* fbn, uint64_t ng,
+                       const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                       const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx, float* ovy,
+                       float* ovz, float* ow, uint64_t* oid, int* err, int grid, int grid_p, cudaStream_t st);
 void gather_radii(int64_t nh, const double* px, const double* py, const double* pz, const int64_t* lim,
                   const double* rv, const int32_t* orig, double maxr, double* out, cudaStream_t st);
 uint32_t sfc_ntiles(uint32_t n);
@@ -84,9 +89,6 @@ void writer_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, con
 void writer_bin_write(int64_t nh, const int64_t* order, const ahfgpu_halo* halo, const uint64_t* moff,
                       const uint64_t* member, const uint64_t* ids, const uint64_t* boff, const uint64_t* coff,
                       const unsigned long long* good, unsigned int* qhead, uint32_t* out, int grid, cudaStream_t st);
-void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
-                 const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
-                 float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st);
 }  // namespace ahfgpu
 
 using namespace ahfgpu;
@@ -207,7 +209,8 @@ struct Ctx {
   // the particle gather: grid buckets, per-halo counts and lists, the
   // gathered batch
   DBuf ga_cell, ga_count, ga_start, ga_fill, ga_sums, ga_sorted, ga_queue, ga_qhead, ga_cnt, ga_off, ga_hfill;
-  DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id;
+  DBuf ga_idx, ga_idxA, ga_keyB, ga_idxB, ga_stack, ga_err, ga_x, ga_y, ga_z, ga_vx, ga_vy, ga_vz, ga_w, ga_id,
+       ga_fbq, ga_fbn, ga_items;
   DBuf gr_pos, gr_lim, gr_orig;   // gather radii: sorted centres and R_vir, candidate counts, order
   DBuf wp_blk, wp_boff, wp_good, wp_qhead, wp_out;   // the AHF_particles bytes
   DBuf wb_chunk, wb_coff;                            // both writers: chunks per block, their scan
@@ -982,7 +985,7 @@ int ahfgpu_shutdown(void) {
                   &g.ga_cell, &g.ga_count, &g.ga_start, &g.ga_fill, &g.ga_sums, &g.ga_sorted, &g.ga_queue,
                   &g.ga_qhead, &g.ga_cnt, &g.ga_off, &g.ga_hfill, &g.ga_idx, &g.ga_idxA, &g.ga_keyB, &g.ga_idxB,
                   &g.ga_stack, &g.ga_err, &g.ga_x, &g.ga_y, &g.ga_z, &g.ga_vx, &g.ga_vy, &g.ga_vz, &g.ga_w,
-                  &g.ga_id, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
+                  &g.ga_id, &g.ga_fbq, &g.ga_fbn, &g.ga_items, &g.gr_pos, &g.gr_lim, &g.gr_orig, &g.wp_blk, &g.wp_boff, &g.wp_good, &g.wp_qhead,
                   &g.wp_out, &g.wb_chunk, &g.wb_coff, &g.wp_cbytes,
                   &g.wp_cboff, &g.sfc_kb, &g.sfc_ia, &g.sfc_ib, &g.sfc_gh, &g.sfc_goff, &g.sfc_part,
                   &g.sfc_err, &g.phase, &g.am_key, &g.am_keyb, &g.am_idx, &g.am_idxb, &g.am_cnt,
@@ -1246,6 +1249,31 @@ static int fetch_result_impl(ahfgpu_result* r) {
   return AHFGPU_OK;
 }
 
+// The gather's work queue: haloes by descending radius rounded to float,
+// ties in index order (two stable counting passes over 16-bit digits of the
+// float's bits, which order like the values for radii >= 0).  The order only
+// balances the work (largest first); the lists do not depend on it.
+static void gather_queue(const std::vector<double>& rad, int64_t nh, std::vector<int32_t>& queue) {
+  std::vector<uint32_t> key((size_t)std::max<int64_t>(nh, 1));
+  std::vector<int32_t> tmp((size_t)std::max<int64_t>(nh, 1));
+  for (int64_t h = 0; h < nh; h++) {
+    const float f = (float)rad[h];
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    key[h] = ~b;
+    queue[h] = (int32_t)h;
+  }
+  std::vector<uint32_t> pos(65536);
+  for (int shift = 0; shift < 32; shift += 16) {
+    std::fill(pos.begin(), pos.end(), 0u);
+    for (int64_t i = 0; i < nh; i++) pos[(key[queue[i]] >> shift) & 0xffffu]++;
+    uint32_t run = 0;
+    for (auto& p : pos) { const uint32_t c = p; p = run; run += c; }
+    for (int64_t i = 0; i < nh; i++) tmp[pos[(key[queue[i]] >> shift) & 0xffffu]++] = queue[i];
+    std::copy(tmp.begin(), tmp.begin() + nh, queue.begin());
+  }
+}
+
 static int gather_device_impl(const ahfgpu_particles* parts, const ahfgpu_centres* cen, ahfgpu_batch* out,
                          void* stream) {
   int rc = ensure_init();
@@ -1270,8 +1298,7 @@ static int gather_device_impl(const ahfgpu_particles* parts, const ahfgpu_centre
   for (int64_t h = 0; h < nh; h++)
     if (!(rad[h] >= 0.0) || !(rad[h] <= 1.0)) return fail(AHFGPU_ERR_INVALID, "gather radius of halo %lld not in [0, 1]", (long long)h);
   std::vector<int32_t> queue((size_t)std::max<int64_t>(nh, 1));
-  std::iota(queue.begin(), queue.begin() + nh, 0);
-  std::sort(queue.begin(), queue.begin() + nh, [&](int32_t a, int32_t b) { return rad[a] > rad[b] || (rad[a] == rad[b] && a < b); });
+  gather_queue(rad, nh, queue);
   double rmed = nh > 0 ? rad[queue[nh / 2]] : 0.5;
   // cells of about half the median radius, 8..256 per axis
   int G = rmed > 0 ? (int)std::min(256.0, std::max(8.0, std::floor(2.0 / rmed))) : 8;
@@ -1327,26 +1354,48 @@ static int gather_device_impl(const ahfgpu_particles* parts, const ahfgpu_centre
   EN(g.ga_vx, ng * 4); EN(g.ga_vy, ng * 4); EN(g.ga_vz, ng * 4);
   if (parts->w) EN(g.ga_w, ng * 4);
   EN(g.ga_id, ng * 8);
+  EN(g.ga_fbq, nh * 4);
+  EN(g.ga_fbn, 64);
+  // window items of the lists that span several windows (lists whose items
+  // do not fit take the radial sort)
+  const uint64_t icap = (uint64_t)nh * 16 + 65536;
+  EN(g.ga_items, icap * gather_item_bytes());
 #undef EN
   if (nh > 0 && ng > 0) {
     CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
     gather_halos(1, G, g.ga_start.as<uint32_t>(), g.ga_sorted.as<float4>(), nh, g.ga_queue.as<int32_t>(),
                  g.ga_qhead.as<unsigned int>(), cen->cx, cen->cy, cen->cz, cen->rad, g.ga_cnt.as<uint64_t>(),
                  g.ga_off.as<uint64_t>(), g.ga_hfill.as<unsigned long long>(), g.ga_idx.as<uint64_t>(), grid_h, st);
-    CK(cudaMemsetAsync(g.ga_qhead.p, 0, 64, st));
-    gather_sort(nh, g.ga_queue.as<int32_t>(), g.ga_qhead.as<unsigned int>(), g.ga_off.as<uint64_t>(),
-                g.ga_idx.as<uint64_t>(), g.ga_idxA.as<uint32_t>(), g.ga_keyB.as<uint64_t>(), g.ga_idxB.as<uint32_t>(),
-                g.ga_stack.as<uint4>(), stack_cap, g.ga_err.as<int>(), grid_h, st);
-    gather_pack(ng, g.ga_idx.as<uint64_t>(), parts->x, parts->y, parts->z, parts->vx, parts->vy, parts->vz, parts->w,
-                g.ga_x.as<float>(), g.ga_y.as<float>(), g.ga_z.as<float>(), g.ga_vx.as<float>(), g.ga_vy.as<float>(),
-                g.ga_vz.as<float>(), parts->w ? g.ga_w.as<float>() : nullptr, g.ga_id.as<uint64_t>(),
-                std::max(1, std::min<int>(g.nsm * 8, (int)((ng + 255) / 256))), st);
+    // the lists in ascending index and packed.  Test hooks: AHFGPU_GATHER_BITMAP
+    // "0" every list through the radial sort, "2" every window through the
+    // bitmap, "3" every window that fits through the bitonic network;
+    // AHFGPU_GATHER_WBITS a narrower window (a power of two, >= 32).
+    int mode = 1, wshift = gather_window_shift_max();
+    if (const char* e = getenv("AHFGPU_GATHER_BITMAP")) {
+      const int v = atoi(e);
+      mode = (v >= 0 && v <= 3) ? v : 1;
+    }
+    if (const char* e = getenv("AHFGPU_GATHER_WBITS")) {
+      const long v = atol(e);
+      int sh = 5;
+      while (sh < wshift && (2l << sh) <= v) sh++;
+      if (v >= 32) wshift = sh;
+    }
+    gather_order_pack(nh, g.ga_queue.as<int32_t>(), g.ga_qhead.as<unsigned int>(), g.ga_off.as<uint64_t>(),
+                      g.ga_idx.as<uint64_t>(), g.ga_idxA.as<uint32_t>(), g.ga_keyB.as<uint64_t>(),
+                      g.ga_idxB.as<uint32_t>(), g.ga_stack.as<uint4>(), stack_cap, wshift, mode, g.ga_items.p, icap,
+                      g.ga_fbq.as<int32_t>(), g.ga_fbn.as<unsigned int>(), ng, parts->x, parts->y, parts->z,
+                      parts->vx, parts->vy, parts->vz, parts->w, g.ga_x.as<float>(), g.ga_y.as<float>(),
+                      g.ga_z.as<float>(), g.ga_vx.as<float>(), g.ga_vy.as<float>(), g.ga_vz.as<float>(),
+                      parts->w ? g.ga_w.as<float>() : nullptr, g.ga_id.as<uint64_t>(), g.ga_err.as<int>(), grid_h,
+                      std::max(1, std::min<int>(g.nsm * 8, (int)((ng + 255) / 256))), st);
   }
   CK(cudaGetLastError());
   int derr = 0;
   CK(cudaMemcpyAsync(&derr, g.ga_err.p, 4, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (derr == kErrWorklist) return fail(AHFGPU_ERR_CAPACITY, "gather sort worklist overflow");
+  if (derr == kErrGatherDup) return fail(AHFGPU_ERR_CUDA, "gather: a list holds a particle twice (self-check)");
   if (derr) return fail(AHFGPU_ERR_CUDA, "gather: device error code %d", derr);
   out->off = g.ga_off.as<uint64_t>();
   out->x = g.ga_x.as<float>(); out->y = g.ga_y.as<float>(); out->z = g.ga_z.as<float>();

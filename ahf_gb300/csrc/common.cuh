@@ -23,7 +23,7 @@ constexpr int kMaxFixRounds = 4096;  // cap of the bulk-velocity fixpoint
 // doubles per halo of the FP32C post-pass inputs (Work::fin)
 constexpr int kFinStride = 16;
 
-enum : int { kErrNone = 0, kErrFixpoint = 1, kErrSortDepth = 2, kErrWorklist = 3, kErrSortState = 4 };
+enum : int { kErrNone = 0, kErrFixpoint = 1, kErrSortDepth = 2, kErrWorklist = 3, kErrSortState = 4, kErrGatherDup = 5 };
 
 struct DevParams {
   double VescTune;

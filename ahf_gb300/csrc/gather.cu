@@ -8,7 +8,7 @@
 // array and the 3x3x3 cells around the centre; here the particles are
 // bucketed once into a uniform G^3 grid (counting sort) and each halo scans
 // the grid cells its sphere can touch.  Lists come out in ascending particle
-// index (a per-halo sort of the matches), a deterministic order; the
+// index (a bitmap of the matches, or a per-halo sort of them), a deterministic order; the
 // reference's order follows its SFC cells.
 #include <cstdint>
 
@@ -42,7 +42,10 @@ __global__ void k_gather_cells(uint64_t n, const float* __restrict__ x, const fl
     const uint32_t c = ((uint32_t)cell_of(x[i], G) * (uint32_t)G + (uint32_t)cell_of(y[i], G)) * (uint32_t)G +
                        (uint32_t)cell_of(z[i], G);
     cell[i] = c;
-    atomicAdd(&count[c], 1u);
+    // one atomic per cell among the warp's active lanes (consecutive
+    // particles of a snapshot often share cells)
+    const unsigned act = __activemask(), grp = __match_any_sync(act, c);
+    if ((int)(threadIdx.x & 31) == __ffs((int)grp) - 1) atomicAdd(&count[c], (unsigned)__popc(grp));
   }
 }
 
@@ -120,7 +123,13 @@ __global__ void k_gather_scatter(uint64_t n, const float* __restrict__ x, const 
                                  float4* __restrict__ sorted) {
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t c = cell[i];
-    const uint32_t p = start[c] + atomicAdd(&fill[c], 1u);
+    // one reservation per cell among the warp's active lanes, in lane order
+    const unsigned act = __activemask(), grp = __match_any_sync(act, c);
+    const int lane = (int)(threadIdx.x & 31), lead = __ffs((int)grp) - 1;
+    uint32_t b = 0;
+    if (lane == lead) b = atomicAdd(&fill[c], (unsigned)__popc(grp));
+    b = __shfl_sync(act, b, lead);
+    const uint32_t p = start[c] + b + (uint32_t)__popc(grp & ((1u << lane) - 1u));
     sorted[p] = make_float4(x[i], y[i], z[i], __uint_as_float((uint32_t)i));
   }
 }
@@ -193,55 +202,65 @@ __global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uin
     }
     unsigned long long found = 0;
     uint64_t chunk = 0;                // chunks of the walk so far
-    for (int kx = 0; kx < nd[0]; kx++) {
-      const uint32_t ix = (uint32_t)((lo[0] + kx) % G);
-      for (int ky = 0; ky < nd[1]; ky++) {
-        const uint32_t iy = (uint32_t)((lo[1] + ky) % G);
-        for (int kz = 0; kz < nd[2]; kz++) {
-          const uint32_t c = (ix * (uint32_t)G + iy) * (uint32_t)G + (uint32_t)((lo[2] + kz) % G);
-          const uint32_t s0 = start[c], s1 = start[c + 1];
-          const uint64_t nch = (s1 - s0 + CH - 1) / CH;
-          // this warp's chunks of the cell: global chunk numbers = wid mod nw
-          uint64_t first = (uint64_t)((wid - (int)(chunk % (uint64_t)nw) + nw) % nw);
-          for (uint64_t k = first; k < nch; k += (uint64_t)nw) {
-            const uint32_t j0 = s0 + (uint32_t)(k * CH);
-            float4 p[U];
+    // the cells in (x, y, z) order, 32 at a time: lane j loads the particle
+    // range of cell t0 + j, so the warp waits once per 32 cells
+    const uint32_t ncell = (uint32_t)nd[0] * (uint32_t)nd[1] * (uint32_t)nd[2];
+    for (uint32_t t0 = 0; t0 < ncell; t0 += 32) {
+      uint32_t cs0 = 0, cs1 = 0;
+      const uint32_t t = t0 + (uint32_t)lane;
+      if (t < ncell) {
+        const uint32_t kz = t % (uint32_t)nd[2], ky = (t / (uint32_t)nd[2]) % (uint32_t)nd[1],
+                       kx = t / ((uint32_t)nd[2] * (uint32_t)nd[1]);
+        const uint32_t c = (((uint32_t)lo[0] + kx) % (uint32_t)G * (uint32_t)G + ((uint32_t)lo[1] + ky) % (uint32_t)G) *
+                               (uint32_t)G +
+                           ((uint32_t)lo[2] + kz) % (uint32_t)G;
+        cs0 = start[c];
+        cs1 = start[c + 1];
+      }
+      const uint32_t mc = ncell - t0 < 32u ? ncell - t0 : 32u;
+      for (uint32_t jc = 0; jc < mc; jc++) {
+        const uint32_t s0 = __shfl_sync(FULL, cs0, (int)jc), s1 = __shfl_sync(FULL, cs1, (int)jc);
+        const uint64_t nch = (s1 - s0 + CH - 1) / CH;
+        // this warp's chunks of the cell: global chunk numbers = wid mod nw
+        uint64_t first = (uint64_t)((wid - (int)(chunk % (uint64_t)nw) + nw) % nw);
+        for (uint64_t k = first; k < nch; k += (uint64_t)nw) {
+          const uint32_t j0 = s0 + (uint32_t)(k * CH);
+          float4 p[U];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
+            p[u] = j < s1 ? sorted[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          unsigned m[U];
+          unsigned tot = 0;
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
+            bool in = false;
+            if (j < s1) {
+              const int sc = gather_screen(p[u].x, p[u].y, p[u].z, fx, fy, fz, r2f);
+              in = sc > 0 || (sc < 0 && gather_d2(p[u].x, p[u].y, p[u].z, ccx, ccy, ccz) <= r2);
+            }
+            m[u] = __ballot_sync(FULL, in);
+            tot += (unsigned)__popc(m[u]);
+          }
+          if (pass == 0) {
+            found += tot;
+          } else if (tot) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&hfill[h], (unsigned long long)tot);
+            b = __shfl_sync(FULL, b, 0);
+            const uint64_t at = off[h] + b;
+            unsigned run = 0;
 #pragma unroll
             for (int u = 0; u < U; u++) {
-              const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
-              p[u] = j < s1 ? sorted[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            unsigned m[U];
-            unsigned tot = 0;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-              const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
-              bool in = false;
-              if (j < s1) {
-                const int sc = gather_screen(p[u].x, p[u].y, p[u].z, fx, fy, fz, r2f);
-                in = sc > 0 || (sc < 0 && gather_d2(p[u].x, p[u].y, p[u].z, ccx, ccy, ccz) <= r2);
-              }
-              m[u] = __ballot_sync(FULL, in);
-              tot += (unsigned)__popc(m[u]);
-            }
-            if (pass == 0) {
-              found += tot;
-            } else if (tot) {
-              unsigned long long b = 0;
-              if (lane == 0) b = atomicAdd(&hfill[h], (unsigned long long)tot);
-              b = __shfl_sync(FULL, b, 0);
-              const uint64_t at = off[h] + b;
-              unsigned run = 0;
-#pragma unroll
-              for (int u = 0; u < U; u++) {
-                if ((m[u] >> lane) & 1u)
-                  out_idx[at + run + (unsigned)__popc(m[u] & ((1u << lane) - 1u))] = (uint64_t)__float_as_uint(p[u].w);
-                run += (unsigned)__popc(m[u]);
-              }
+              if ((m[u] >> lane) & 1u)
+                out_idx[at + run + (unsigned)__popc(m[u] & ((1u << lane) - 1u))] = (uint64_t)__float_as_uint(p[u].w);
+              run += (unsigned)__popc(m[u]);
             }
           }
-          chunk += nch;
         }
+        chunk += nch;
       }
     }
     if (pass == 0 && lane == 0 && found) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[h]), found);
@@ -279,20 +298,359 @@ __global__ void k_gather_offsets(const uint64_t* __restrict__ cnt, int64_t nhalo
   if (threadIdx.x == 0) off[0] = 0;
 }
 
-// each halo's list in ascending particle index: the block radial sort on
-// (index, slot) over [off[h], off[h+1]) of keyA (indices) / idxA (scratch)
-__global__ void __launch_bounds__(256) k_gather_sort(int64_t nhalo, const int32_t* __restrict__ queue,
+// The lists in ascending particle index.  A halo's matches are distinct
+// particle indices.  Each list's index range [mn, mx] is cut into windows of
+// 2^wshift indices, and a window's keys are ordered in shared memory: marked
+// in a bitmap and read back in ascending order where they are dense enough
+// (span / 32 <= 4 cnt + 1024 words), else by a bitonic network (a sparse
+// window holds fewer than kGbSortMax keys).  k_gather_prep takes the lists
+// from the largest-first queue: a list of one window is ordered at once; a
+// list of several is counted per window, scattered by window into keyB and
+// queued as one work item per non-empty window for k_gather_windows, so that
+// the windows of a long list run on many CTAs.  The bitmap read-back: each
+// warp owns a contiguous run of the window's words (counted first, so that
+// every warp knows where its output starts), and per group of 32 words a
+// warp scan of the popcounts gives each word's first output position; output
+// element e of the group is found by a binary search over the lanes'
+// inclusive counts and a select of the bit inside its word, so consecutive
+// lanes write consecutive positions.  Lists of more windows than the count
+// table holds (only with a narrowed window), lists whose items do not fit the
+// item table and, under the test hook, every list take the block radial sort
+// instead (k_gather_sort).  mode: 1 = as above, 0 = every list to the radial
+// sort, 2 = every window through the bitmap, 3 = every window of at most
+// kGbSortMax keys through the bitonic network.
+constexpr int kGbT = 256;
+constexpr uint32_t kGbWords = 16384;           // shared words: a window's bitmap or a list's window counts
+constexpr uint32_t kGbSortMax = kGbWords / 2;  // u64 keys of the bitonic network
+constexpr int kGbU = 8;                        // keys in flight per thread
+constexpr unsigned long long kGbNone = ~0ull;  // no key (indices are below 2^32)
+
+struct GbItem {
+  unsigned long long kb;    // the window's first index
+  unsigned long long at;    // its first output position (in keyB and in the output)
+  unsigned long long cnt;   // its keys
+  unsigned long long pad;
+};
+
+struct GbShared {
+  long long q;
+  unsigned long long mn[kGbT / 32], mx[kGbT / 32];
+  unsigned wa[kGbT / 32], wb[kGbT / 32];
+  unsigned long long ibase;
+  int ok;
+};
+
+// position of the set bit of rank r (0-based) in w (r < popc(w))
+__device__ __forceinline__ unsigned select_bit(unsigned w, unsigned r) {
+  unsigned pos = 0;
+#pragma unroll
+  for (int half = 16; half > 0; half >>= 1) {
+    const unsigned lo = (unsigned)__popc(w & ((1u << half) - 1u));
+    if (r >= lo) { r -= lo; w >>= half; pos += (unsigned)half; }
+  }
+  return pos;
+}
+
+// kGbU keys of src[0, n) per thread: i0 + u kGbT + thread (kGbNone past n)
+__device__ __forceinline__ void gb_load(const uint64_t* __restrict__ src, uint64_t n, uint64_t i0,
+                                        unsigned long long (&k)[kGbU]) {
+#pragma unroll
+  for (int u = 0; u < kGbU; u++) {
+    const uint64_t i = i0 + (uint64_t)u * kGbT + threadIdx.x;
+    k[u] = i < n ? src[i] : kGbNone;
+  }
+}
+
+// block minimum and maximum of src[0, n) (n > 0)
+__device__ void gb_minmax(const uint64_t* __restrict__ src, uint64_t n, unsigned long long& mn,
+                          unsigned long long& mx, GbShared& S) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  mn = kGbNone;
+  mx = 0ull;
+  for (uint64_t i0 = 0; i0 < n; i0 += (uint64_t)kGbT * kGbU) {
+    unsigned long long k[kGbU];
+    gb_load(src, n, i0, k);
+#pragma unroll
+    for (int u = 0; u < kGbU; u++)
+      if (k[u] != kGbNone) {
+        mn = k[u] < mn ? k[u] : mn;
+        mx = k[u] > mx ? k[u] : mx;
+      }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const unsigned long long a = __shfl_xor_sync(FULL, mn, d), b = __shfl_xor_sync(FULL, mx, d);
+    mn = a < mn ? a : mn;
+    mx = b > mx ? b : mx;
+  }
+  if (lane == 0) { S.mn[wid] = mn; S.mx[wid] = mx; }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < kGbT / 32; v++) {
+    mn = S.mn[v] < mn ? S.mn[v] : mn;
+    mx = S.mx[v] > mx ? S.mx[v] : mx;
+  }
+  __syncthreads();
+}
+
+// block exclusive scan of two u32 values (ea, eb) and the totals (ta, tb)
+__device__ void gb_scan2(unsigned a, unsigned b, unsigned& ea, unsigned& eb, unsigned& ta, unsigned& tb, GbShared& S) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned ia = a, ib = b;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const unsigned x = __shfl_up_sync(FULL, ia, d), y = __shfl_up_sync(FULL, ib, d);
+    if (lane >= d) { ia += x; ib += y; }
+  }
+  if (lane == 31) { S.wa[wid] = ia; S.wb[wid] = ib; }
+  __syncthreads();
+  ea = ia - a;
+  eb = ib - b;
+  ta = 0;
+  tb = 0;
+#pragma unroll
+  for (int v = 0; v < kGbT / 32; v++) {
+    if (v < wid) { ea += S.wa[v]; eb += S.wb[v]; }
+    ta += S.wa[v];
+    tb += S.wb[v];
+  }
+  __syncthreads();
+}
+
+// Orders the distinct keys src[0, cnt), all in [lo, hi] (hi - lo < 32
+// kGbWords), into dst[0, cnt); every thread of the CTA calls it.  Returns the
+// keys written: cnt unless a key repeats.
+__device__ uint64_t gb_order(const uint64_t* __restrict__ src, uint64_t cnt, unsigned long long lo,
+                             unsigned long long hi, uint64_t* __restrict__ dst, int mode, unsigned* bm,
+                             GbShared& S) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int NW = kGbT / 32;
+  const uint64_t span = hi - lo + 1;
+  const uint32_t nwd = (uint32_t)((span + 31u) / 32u);
+  const bool net = cnt <= kGbSortMax && (mode == 3 || (mode != 2 && (uint64_t)nwd > 4u * cnt + 1024u));
+  if (net) {
+    unsigned long long* sk = reinterpret_cast<unsigned long long*>(bm);
+    uint32_t P = 1;
+    while (P < cnt) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += kGbT) sk[i] = i < cnt ? src[i] : kGbNone;
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1)
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t i = threadIdx.x; i < P; i += kGbT) {
+          const uint32_t l = i ^ j;
+          if (l > i) {
+            const unsigned long long a = sk[i], b = sk[l];
+            if ((a > b) == ((i & k) == 0u)) { sk[i] = b; sk[l] = a; }
+          }
+        }
+        __syncthreads();
+      }
+    int rep = 0;
+    for (uint32_t i = threadIdx.x; i < cnt; i += kGbT) {
+      dst[i] = sk[i];
+      if (i + 1u < cnt && sk[i + 1u] == sk[i]) rep = 1;
+    }
+    return __syncthreads_or(rep) ? cnt - 1u : cnt;
+  }
+  for (uint32_t j = threadIdx.x; j < nwd; j += kGbT) bm[j] = 0u;
+  __syncthreads();
+  for (uint64_t i0 = 0; i0 < cnt; i0 += (uint64_t)kGbT * kGbU) {
+    unsigned long long k[kGbU];
+    gb_load(src, cnt, i0, k);
+#pragma unroll
+    for (int u = 0; u < kGbU; u++) {
+      const uint64_t d = k[u] - lo;
+      if (k[u] != kGbNone && d < span) atomicOr(&bm[d >> 5], 1u << (d & 31u));
+    }
+  }
+  __syncthreads();
+  // this warp's words [w0, w1)
+  const uint32_t per = ((nwd + NW - 1) / NW + 31u) & ~31u;
+  const uint32_t w0 = min((uint32_t)wid * per, nwd), w1 = min(w0 + per, nwd);
+  unsigned c0 = 0;
+  for (uint32_t j = w0 + lane; j < w1; j += 32) c0 += (unsigned)__popc(bm[j]);
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) c0 += __shfl_xor_sync(FULL, c0, d);
+  if (lane == 0) S.wa[wid] = c0;
+  __syncthreads();
+  uint64_t base = 0, tot = 0;
+#pragma unroll
+  for (int v = 0; v < NW; v++) {
+    if (v < wid) base += S.wa[v];
+    tot += S.wa[v];
+  }
+  for (uint32_t g = w0; g < w1; g += 32) {
+    const uint32_t j = g + (uint32_t)lane;
+    const unsigned word = j < w1 ? bm[j] : 0u;
+    const unsigned c = (unsigned)__popc(word);
+    unsigned incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const unsigned t = __shfl_up_sync(FULL, incl, d);
+      if (lane >= d) incl += t;
+    }
+    const unsigned total = __shfl_sync(FULL, incl, 31);
+    for (unsigned e0 = 0; e0 < total; e0 += 32) {
+      const unsigned e = e0 + (unsigned)lane;
+      // s = the number of lanes whose inclusive count is <= e
+      int s = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const unsigned v = __shfl_sync(FULL, incl, s + step - 1);
+        if (v <= e) s += step;
+      }
+      const unsigned ws = __shfl_sync(FULL, word, s & 31), cs = __shfl_sync(FULL, c, s & 31),
+                     is = __shfl_sync(FULL, incl, s & 31);
+      if (e < total) dst[base + e] = lo + ((uint64_t)(g + (uint32_t)s) << 5) + select_bit(ws, e - (is - cs));
+    }
+    base += total;
+  }
+  __syncthreads();   // the bitmap is rewritten by the caller's next window
+  return tot;
+}
+
+__global__ void __launch_bounds__(kGbT) k_gather_prep(int64_t nhalo, const int32_t* __restrict__ queue,
+                                                      unsigned int* __restrict__ qhead,
+                                                      const uint64_t* __restrict__ off,
+                                                      const uint64_t* __restrict__ idx, uint64_t* __restrict__ keyB,
+                                                      uint64_t* __restrict__ dst, int wshift, int mode,
+                                                      GbItem* __restrict__ items,
+                                                      unsigned long long* __restrict__ nitems,
+                                                      unsigned long long icap, int32_t* __restrict__ fbq,
+                                                      unsigned int* __restrict__ fbn, int* __restrict__ err) {
+  extern __shared__ unsigned bm[];
+  __shared__ GbShared S;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned q = atomicAdd(qhead, 1u);
+      S.q = q < (unsigned)nhalo ? queue[q] : -1;
+    }
+    __syncthreads();
+    const int h = (int)S.q;
+    __syncthreads();
+    if (h < 0) break;
+    const uint64_t o = off[h], n = off[h + 1] - o;
+    if (n == 0) continue;
+    if (mode == 0) {
+      if (threadIdx.x == 0) fbq[atomicAdd(fbn, 1u)] = h;
+      continue;
+    }
+    unsigned long long mn, mx;
+    gb_minmax(idx + o, n, mn, mx, S);
+    const uint64_t nwin = ((mx - mn) >> wshift) + 1;
+    if (nwin == 1) {
+      const uint64_t got = gb_order(idx + o, n, mn, mx, dst + o, mode, bm, S);
+      if (threadIdx.x == 0 && got != n) atomicExch(err, kErrGatherDup);
+      continue;
+    }
+    if (nwin > kGbWords) {
+      if (threadIdx.x == 0) fbq[atomicAdd(fbn, 1u)] = h;
+      continue;
+    }
+    // keys per window
+    for (uint32_t j = threadIdx.x; j < (uint32_t)nwin; j += kGbT) bm[j] = 0u;
+    __syncthreads();
+    for (uint64_t i0 = 0; i0 < n; i0 += (uint64_t)kGbT * kGbU) {
+      unsigned long long k[kGbU];
+      gb_load(idx + o, n, i0, k);
+#pragma unroll
+      for (int u = 0; u < kGbU; u++)
+        if (k[u] != kGbNone) atomicAdd(&bm[(k[u] - mn) >> wshift], 1u);
+    }
+    __syncthreads();
+    // each thread's run of windows [c0, c1): keys and non-empty windows, scanned
+    const uint32_t per = (uint32_t)((nwin + kGbT - 1) / kGbT);
+    const uint32_t c0 = min((uint32_t)threadIdx.x * per, (uint32_t)nwin), c1 = min(c0 + per, (uint32_t)nwin);
+    unsigned sk = 0, sn = 0;
+    for (uint32_t j = c0; j < c1; j++) { sk += bm[j]; sn += bm[j] ? 1u : 0u; }
+    unsigned ek, en, tk, tn;
+    gb_scan2(sk, sn, ek, en, tk, tn, S);
+    if (threadIdx.x == 0) {
+      // reserve tn items if they fit the table
+      unsigned long long cur = *nitems;
+      S.ok = 0;
+      while (cur + tn <= icap) {
+        const unsigned long long prev = atomicCAS(nitems, cur, cur + tn);
+        if (prev == cur) { S.ok = 1; S.ibase = cur; break; }
+        cur = prev;
+      }
+      if (!S.ok) fbq[atomicAdd(fbn, 1u)] = h;
+    }
+    __syncthreads();
+    if (!S.ok) continue;
+    unsigned run = ek;
+    unsigned long long it = S.ibase + en;
+    for (uint32_t j = c0; j < c1; j++) {
+      const unsigned c = bm[j];
+      if (c) {
+        GbItem I;
+        I.kb = mn + ((unsigned long long)j << wshift);
+        I.at = o + run;
+        I.cnt = c;
+        I.pad = 0;
+        items[it++] = I;
+      }
+      bm[j] = run;   // the window's cursor
+      run += c;
+    }
+    __syncthreads();
+    for (uint64_t i0 = 0; i0 < n; i0 += (uint64_t)kGbT * kGbU) {
+      unsigned long long k[kGbU];
+      gb_load(idx + o, n, i0, k);
+#pragma unroll
+      for (int u = 0; u < kGbU; u++)
+        if (k[u] != kGbNone) keyB[o + atomicAdd(&bm[(k[u] - mn) >> wshift], 1u)] = k[u];
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kGbT) k_gather_windows(const GbItem* __restrict__ items,
+                                                         const unsigned long long* __restrict__ nitems,
+                                                         unsigned int* __restrict__ qhead,
+                                                         const uint64_t* __restrict__ keyB,
+                                                         uint64_t* __restrict__ dst, int mode, int* __restrict__ err) {
+  extern __shared__ unsigned bm[];
+  __shared__ GbShared S;
+  const unsigned long long ni = *nitems;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned long long q = atomicAdd(qhead, 1u);
+      S.q = q < ni ? (long long)q : -1;
+    }
+    __syncthreads();
+    const long long q = S.q;
+    __syncthreads();
+    if (q < 0) break;
+    const GbItem I = items[q];
+    unsigned long long lo, hi;
+    gb_minmax(keyB + I.at, I.cnt, lo, hi, S);
+    const uint64_t got = gb_order(keyB + I.at, I.cnt, lo, hi, dst + I.at, mode, bm, S);
+    if (threadIdx.x == 0 && got != I.cnt) atomicExch(err, kErrGatherDup);
+  }
+}
+
+// The radial-sort path: each queued halo's list in ascending particle index
+// by the block radial sort on (index, slot) over [off[h], off[h+1]) of keyA
+// (indices) / idxA (scratch), copied to dst.  The queue length is read on
+// the device (*nq).
+__global__ void __launch_bounds__(256) k_gather_sort(const unsigned int* __restrict__ nq,
+                                                     const int32_t* __restrict__ queue,
                                                      unsigned int* __restrict__ qhead, const uint64_t* __restrict__ off,
                                                      uint64_t* keyA, uint32_t* idxA, uint64_t* keyB, uint32_t* idxB,
-                                                     uint4* stack, int stack_cap, int* err) {
+                                                     uint4* stack, int stack_cap, uint64_t* __restrict__ dst, int* err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   GatherSS& S = *reinterpret_cast<GatherSS*>(smem_raw);
   __shared__ int s_h;
   uint4* my_stack = stack + (uint64_t)blockIdx.x * stack_cap;
+  const unsigned nhalo = *nq;
   while (true) {
     if (threadIdx.x == 0) {
       const unsigned q = atomicAdd(qhead, 1u);
-      s_h = q < (unsigned)nhalo ? queue[q] : -1;
+      s_h = q < nhalo ? queue[q] : -1;
     }
     __syncthreads();
     const int h = s_h;
@@ -303,23 +661,24 @@ __global__ void __launch_bounds__(256) k_gather_sort(int64_t nhalo, const int32_
     const int rc = radial_sort(keyA, idxA, keyB, idxB, o, n, my_stack, stack_cap, S);
     if (rc != kErrNone && threadIdx.x == 0) atomicExch(err, rc);
     __syncthreads();
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) dst[o + i] = keyA[o + i];
+    __syncthreads();
   }
 }
 
-// the gathered lists as a stage batch: SoA particle data per entry, the
-// particle index as the entry's id
+// the gathered lists as a stage batch: SoA particle data per entry (the
+// entry's particle index already in idx)
 __global__ void k_gather_pack(uint64_t ng, const uint64_t* __restrict__ idx, const float* __restrict__ x,
                               const float* __restrict__ y, const float* __restrict__ z, const float* __restrict__ vx,
                               const float* __restrict__ vy, const float* __restrict__ vz, const float* __restrict__ w,
                               float* __restrict__ ox, float* __restrict__ oy, float* __restrict__ oz,
                               float* __restrict__ ovx, float* __restrict__ ovy, float* __restrict__ ovz,
-                              float* __restrict__ ow, uint64_t* __restrict__ oid) {
+                              float* __restrict__ ow) {
   for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ng; k += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t i = idx[k];
     ox[k] = x[i]; oy[k] = y[i]; oz[k] = z[i];
     ovx[k] = vx[i]; ovy[k] = vy[i]; ovz[k] = vz[i];
     if (w) ow[k] = w[i];
-    oid[k] = i;
   }
 }
 
@@ -434,21 +793,37 @@ void gather_offsets(const uint64_t* cnt, int64_t nhalo, uint64_t* off, cudaStrea
 size_t gather_sort_smem() { return sizeof(GatherSS); }
 
 int gather_sort_setup() {
-  return (int)cudaFuncSetAttribute(k_gather_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(GatherSS));
+  cudaError_t e = cudaFuncSetAttribute(k_gather_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GatherSS));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_gather_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kGbWords * 4));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_gather_windows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kGbWords * 4));
+  return (int)e;
 }
 
-void gather_sort(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
-                 uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int* err, int grid,
-                 cudaStream_t st) {
-  k_gather_sort<<<grid, 256, sizeof(GatherSS), st>>>(nhalo, queue, qhead, off, keyA, idxA, keyB, idxB, stack, stack_cap,
-                                                      err);
-}
+int gather_window_shift_max() { return 19; }   // 2^19 = 32 kGbWords indices
+size_t gather_item_bytes() { return sizeof(GbItem); }
 
-void gather_pack(uint64_t ng, const uint64_t* idx, const float* x, const float* y, const float* z, const float* vx,
-                 const float* vy, const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx,
-                 float* ovy, float* ovz, float* ow, uint64_t* oid, int grid, cudaStream_t st) {
-  k_gather_pack<<<grid, 256, 0, st>>>(ng, idx, x, y, z, vx, vy, vz, w, ox, oy, oz, ovx, ovy, ovz, ow, oid);
+// The lists in ascending index (into oid), then packed: the per-list pass,
+// the windows it queued, the radial sort of the lists it left, the pack.
+// qhead: 3 queue heads; fbn: the radial-sort queue length (u32 at byte 0) and
+// the item count (u64 at byte 8).
+void gather_order_pack(int64_t nhalo, const int32_t* queue, unsigned int* qhead, const uint64_t* off, uint64_t* keyA,
+                       uint32_t* idxA, uint64_t* keyB, uint32_t* idxB, uint4* stack, int stack_cap, int wshift,
+                       int mode, void* items, uint64_t icap, int32_t* fbq, unsigned int* fbn, uint64_t ng,
+                       const float* x, const float* y, const float* z, const float* vx, const float* vy,
+                       const float* vz, const float* w, float* ox, float* oy, float* oz, float* ovx, float* ovy,
+                       float* ovz, float* ow, uint64_t* oid, int* err, int grid, int grid_p, cudaStream_t st) {
+  unsigned long long* nitems = reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(fbn) + 8);
+  cudaMemsetAsync(qhead, 0, 16, st);
+  cudaMemsetAsync(fbn, 0, 16, st);
+  GbItem* it = reinterpret_cast<GbItem*>(items);
+  k_gather_prep<<<grid, kGbT, kGbWords * 4, st>>>(nhalo, queue, qhead, off, keyA, keyB, oid, wshift, mode, it, nitems,
+                                                   (unsigned long long)icap, fbq, fbn, err);
+  k_gather_windows<<<grid, kGbT, kGbWords * 4, st>>>(it, nitems, qhead + 2, keyB, oid, mode, err);
+  k_gather_sort<<<grid, 256, sizeof(GatherSS), st>>>(fbn, fbq, qhead + 1, off, keyA, idxA, keyB, idxB, stack,
+                                                      stack_cap, oid, err);
+  k_gather_pack<<<grid_p, 256, 0, st>>>(ng, oid, x, y, z, vx, vy, vz, w, ox, oy, oz, ovx, ovy, ovz, w ? ow : nullptr);
 }
 
 }  // namespace ahfgpu

@@ -379,10 +379,11 @@ class Snapshot:
         return len(self.cx)
 
 
-def snapshot_from_lists(lists: HaloLists, n_background: int, seed: int = 7) -> Snapshot:
+def snapshot_from_lists(lists: HaloLists, n_background: int, seed: int = 7, shuffle: bool = True) -> Snapshot:
     """A snapshot made of every particle of the lists (each list is its own
     NFW sphere plus background out to 1.5 R_vir) and `n_background` uniform
-    particles (sigma 100 km/s) over the whole box, in a seeded random order.
+    particles (sigma 100 km/s) over the whole box, in a seeded random order
+    (shuffle=False: the lists' particles in list order, then the uniform ones).
     Each halo's gather radius is the largest periodic distance of its own
     list's particles from its centre (<= 1.5 R_vir)."""
     L = lists.to_numpy() if not isinstance(lists.x, np.ndarray) else lists
@@ -395,7 +396,7 @@ def snapshot_from_lists(lists: HaloLists, n_background: int, seed: int = 7) -> S
     w = None
     if L.w is not None:
         w = np.concatenate([np.asarray(L.w, np.float32), np.ones(n_background, np.float32)])
-    perm = rng.permutation(len(pos))
+    perm = rng.permutation(len(pos)) if shuffle else np.arange(len(pos))
     pos, vel = pos[perm], vel[perm]
     if w is not None:
         w = w[perm]

@@ -102,6 +102,52 @@ def test_gpu_gather_matches_restatement(gpu):
     assert np.array_equal(gid, oidx)
 
 
+def _packed(b, n):
+    """The gathered batch's particle arrays (device) as host numpy arrays."""
+    import ctypes as C
+    from ahf_gb300 import lib
+    out = {}
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+        ptr = C.cast(getattr(b, k), C.c_void_p).value
+        out[k] = lib.device_view(ptr, n, "<f4").cpu().numpy() if ptr and n else None
+    return out
+
+
+# The lists' order: per window of each list's index range, a bitmap where the
+# window's keys are dense (lists of a snapshot in list order), a bitonic
+# network where they are sparse (a shuffled snapshot), the block radial sort
+# for lists the windows do not cover; the hooks force each path and narrow
+# the window so that lists span many windows (queued as window items).
+ORDER_CASES = [
+    ("list_order", False, {}),
+    ("shuffled", True, {}),
+    ("list_order_fallback_only", False, {"AHFGPU_GATHER_BITMAP": "0"}),
+    ("shuffled_bitmap_only_64bit_windows", True, {"AHFGPU_GATHER_BITMAP": "2", "AHFGPU_GATHER_WBITS": "64"}),
+    ("list_order_256bit_windows", False, {"AHFGPU_GATHER_WBITS": "256"}),
+    ("list_order_network_only", False, {"AHFGPU_GATHER_BITMAP": "3"}),
+    ("shuffled_network_256bit_windows", True, {"AHFGPU_GATHER_BITMAP": "3", "AHFGPU_GATHER_WBITS": "256"}),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,shuffle,env", ORDER_CASES, ids=[c[0] for c in ORDER_CASES])
+def test_gpu_gather_order_paths(gpu, name, shuffle, env, monkeypatch):
+    from ahf_gb300 import synth
+    O = _oracle()
+    L = synth.generate("cfg4", scale=0.01, multimass=True)   # with a mass array, so that it is packed too
+    S = synth.snapshot_from_lists(L, 200000, seed=13, shuffle=shuffle)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    b, _, off, gid = _gpu_gather(S)
+    ooff, oidx = O.gather_oracle(S.x, S.y, S.z, S.cx, S.cy, S.cz, S.rad)
+    assert np.array_equal(off, ooff)
+    assert np.array_equal(gid, oidx)
+    got = _packed(b, len(gid))
+    sel = gid.astype(np.int64)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "w"):
+        assert np.array_equal(got[k], np.asarray(getattr(S, k))[sel]), k
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["batched_fp64", "batched_fp32c"])
 def test_gather_then_stage_matches_oracle(gpu, mode):
