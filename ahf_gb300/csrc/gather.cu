@@ -157,11 +157,12 @@ __device__ __forceinline__ int gather_screen(float px, float py, float pz, float
 
 // One CTA per halo (persistent, queue largest radius first).  The CTA's
 // warps walk the grid cells the halo's sphere can touch together, cutting
-// each cell's particles into chunks of 32 x 8 and taking every eighth chunk
-// of the walk, so a halo of millions of particles is spread over all warps.
+// the particles of each batch of cell runs into chunks of 32 x 8 and taking
+// every eighth chunk of the walk, so a halo of millions of particles is
+// spread over all warps.
 // Pass 0 adds each warp's matches to cnt[h] (zeroed before); pass 1 writes
-// the particle indices at off[h] + a per-chunk reservation (k_gather_sort
-// orders them).  The FP32 screen decides all but the particles near the
+// the particle indices at off[h] + a per-chunk reservation (k_gather_prep
+// and the kernels after it order them).  The FP32 screen decides all but the particles near the
 // surface, which take the reference's FP64 test.
 __global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uint32_t* __restrict__ start,
                                                       const float4* __restrict__ sorted, int64_t nhalo,
@@ -202,66 +203,84 @@ __global__ void __launch_bounds__(256) k_gather_halos(int pass, int G, const uin
     }
     unsigned long long found = 0;
     uint64_t chunk = 0;                // chunks of the walk so far
-    // the cells in (x, y, z) order, 32 at a time: lane j loads the particle
-    // range of cell t0 + j, so the warp waits once per 32 cells
-    const uint32_t ncell = (uint32_t)nd[0] * (uint32_t)nd[1] * (uint32_t)nd[2];
-    for (uint32_t t0 = 0; t0 < ncell; t0 += 32) {
-      uint32_t cs0 = 0, cs1 = 0;
+    // The sphere's cells as runs along z: cells (ix, iy, z) of consecutive z
+    // are consecutive in `sorted`, so each (x, y) column of the walk is one
+    // run of particles, or two where it wraps the periodic boundary.  Runs
+    // are taken 32 at a time (lane j loads the range of run t0 + j), their
+    // particles form one stream, and the warps take its chunks of CH
+    // particles in turn; a particle's run is found by a binary search over
+    // the lanes' inclusive run lengths.
+    const bool wrap = lo[2] + nd[2] > G;
+    const uint32_t nrun = (uint32_t)nd[0] * (uint32_t)nd[1] * (wrap ? 2u : 1u);
+    for (uint32_t t0 = 0; t0 < nrun; t0 += 32) {
+      uint32_t rs0 = 0, rlen = 0;
       const uint32_t t = t0 + (uint32_t)lane;
-      if (t < ncell) {
-        const uint32_t kz = t % (uint32_t)nd[2], ky = (t / (uint32_t)nd[2]) % (uint32_t)nd[1],
-                       kx = t / ((uint32_t)nd[2] * (uint32_t)nd[1]);
-        const uint32_t c = (((uint32_t)lo[0] + kx) % (uint32_t)G * (uint32_t)G + ((uint32_t)lo[1] + ky) % (uint32_t)G) *
-                               (uint32_t)G +
-                           ((uint32_t)lo[2] + kz) % (uint32_t)G;
-        cs0 = start[c];
-        cs1 = start[c + 1];
+      if (t < nrun) {
+        const uint32_t col = wrap ? t >> 1 : t, part = wrap ? (t & 1u) : 0u;
+        const uint32_t ky = col % (uint32_t)nd[1], kx = col / (uint32_t)nd[1];
+        const uint32_t ix = ((uint32_t)lo[0] + kx) % (uint32_t)G, iy = ((uint32_t)lo[1] + ky) % (uint32_t)G;
+        const uint32_t za = part ? 0u : (uint32_t)lo[2];
+        const uint32_t zb = wrap ? (part ? (uint32_t)(lo[2] + nd[2] - G) : (uint32_t)G) : (uint32_t)(lo[2] + nd[2]);
+        const uint32_t cb = (ix * (uint32_t)G + iy) * (uint32_t)G;
+        rs0 = start[cb + za];
+        rlen = start[cb + zb] - rs0;
       }
-      const uint32_t mc = ncell - t0 < 32u ? ncell - t0 : 32u;
-      for (uint32_t jc = 0; jc < mc; jc++) {
-        const uint32_t s0 = __shfl_sync(FULL, cs0, (int)jc), s1 = __shfl_sync(FULL, cs1, (int)jc);
-        const uint64_t nch = (s1 - s0 + CH - 1) / CH;
-        // this warp's chunks of the cell: global chunk numbers = wid mod nw
-        uint64_t first = (uint64_t)((wid - (int)(chunk % (uint64_t)nw) + nw) % nw);
-        for (uint64_t k = first; k < nch; k += (uint64_t)nw) {
-          const uint32_t j0 = s0 + (uint32_t)(k * CH);
-          float4 p[U];
+      uint32_t incl = rlen;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(FULL, incl, d);
+        if (lane >= d) incl += x;
+      }
+      const uint32_t total = __shfl_sync(FULL, incl, 31);
+      const uint64_t nch = (total + CH - 1) / CH;
+      // this warp's chunks of the stream: global chunk numbers = wid mod nw
+      const uint64_t first = (uint64_t)((wid - (int)(chunk % (uint64_t)nw) + nw) % nw);
+      for (uint64_t k = first; k < nch; k += (uint64_t)nw) {
+        const uint32_t v0 = (uint32_t)(k * CH);
+        float4 p[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const uint32_t vi = v0 + (uint32_t)(u * 32 + lane);
+          int r = 0;   // runs whose inclusive length is <= vi
+#pragma unroll
+          for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t x = __shfl_sync(FULL, incl, r + step - 1);
+            if (x <= vi) r += step;
+          }
+          const uint32_t rs = __shfl_sync(FULL, rs0, r & 31), ri = __shfl_sync(FULL, incl, r & 31),
+                         rl = __shfl_sync(FULL, rlen, r & 31);
+          p[u] = vi < total ? sorted[rs + vi - (ri - rl)] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        unsigned m[U];
+        unsigned tot = 0;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const uint32_t vi = v0 + (uint32_t)(u * 32 + lane);
+          bool in = false;
+          if (vi < total) {
+            const int sc = gather_screen(p[u].x, p[u].y, p[u].z, fx, fy, fz, r2f);
+            in = sc > 0 || (sc < 0 && gather_d2(p[u].x, p[u].y, p[u].z, ccx, ccy, ccz) <= r2);
+          }
+          m[u] = __ballot_sync(FULL, in);
+          tot += (unsigned)__popc(m[u]);
+        }
+        if (pass == 0) {
+          found += tot;
+        } else if (tot) {
+          unsigned long long b = 0;
+          if (lane == 0) b = atomicAdd(&hfill[h], (unsigned long long)tot);
+          b = __shfl_sync(FULL, b, 0);
+          const uint64_t at = off[h] + b;
+          unsigned run = 0;
 #pragma unroll
           for (int u = 0; u < U; u++) {
-            const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
-            p[u] = j < s1 ? sorted[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-          unsigned m[U];
-          unsigned tot = 0;
-#pragma unroll
-          for (int u = 0; u < U; u++) {
-            const uint32_t j = j0 + (uint32_t)(u * 32 + lane);
-            bool in = false;
-            if (j < s1) {
-              const int sc = gather_screen(p[u].x, p[u].y, p[u].z, fx, fy, fz, r2f);
-              in = sc > 0 || (sc < 0 && gather_d2(p[u].x, p[u].y, p[u].z, ccx, ccy, ccz) <= r2);
-            }
-            m[u] = __ballot_sync(FULL, in);
-            tot += (unsigned)__popc(m[u]);
-          }
-          if (pass == 0) {
-            found += tot;
-          } else if (tot) {
-            unsigned long long b = 0;
-            if (lane == 0) b = atomicAdd(&hfill[h], (unsigned long long)tot);
-            b = __shfl_sync(FULL, b, 0);
-            const uint64_t at = off[h] + b;
-            unsigned run = 0;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-              if ((m[u] >> lane) & 1u)
-                out_idx[at + run + (unsigned)__popc(m[u] & ((1u << lane) - 1u))] = (uint64_t)__float_as_uint(p[u].w);
-              run += (unsigned)__popc(m[u]);
-            }
+            if ((m[u] >> lane) & 1u)
+              out_idx[at + run + (unsigned)__popc(m[u] & ((1u << lane) - 1u))] = (uint64_t)__float_as_uint(p[u].w);
+            run += (unsigned)__popc(m[u]);
           }
         }
-        chunk += nch;
       }
+      chunk += nch;
     }
     if (pass == 0 && lane == 0 && found) atomicAdd(reinterpret_cast<unsigned long long*>(&cnt[h]), found);
   }
