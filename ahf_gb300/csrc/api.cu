@@ -944,6 +944,8 @@ static int init_impl(int device) {
     g.small_bps = std::max(1, fp32c_small_occupancy());
   }
   load_tuning(prop);
+  // the class-0 cap also bounds the one-list-per-thread kernel's CTAs per SM
+  if (g.tune_bps_cap[0] >= 1) g.small_bps = std::min(g.small_bps, g.tune_bps_cap[0]);
   CK((cudaError_t)gather_sort_setup());
   for (int k = 0; k < 3; k++) {
     g.fp32c_bps[k] = std::max(1, fp32c_max_blocks_per_sm(k));
