@@ -2030,37 +2030,79 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   const uint64_t m = n2 - kNignore;
   const float* y = reinterpret_cast<const float*>(W.prof_c + c.s) + (which ? 0 : n2) + kNignore;
   float* sv = reinterpret_cast<float*>(W.phi + c.s);
-  // smoothed FP32 values and their maximum over [0, m-2]
-  float best = -10.f;
-  for (uint64_t base = 0; base < m; base += (uint64_t)blockDim.x * 4) {
+#ifdef AHFGPU_PHASE_TIMERS
+  // slots 27..31: FP64 path cycles, FP64 candidates, calls taking it, FP32 screen cycles, candidate scan cycles
+  long long _f0 = clock64();
+#endif
+  // smoothed FP32 values (kept in sv) and, per thread, the two largest valid
+  // values over [0, m-2] with their indices: the block's maximum is the
+  // largest of them, and the candidates are counted from them without a
+  // second pass.  The ends (within ns of either end) go through
+  // smooth_edge32 first; the interior is one stencil with its loads batched.
+  float b1 = -10.f, b2 = -10.f;
+  long long i1 = -1, i2 = -1;
+  const bool direct = ns == 0 || m < 3;
+  const uint64_t ilo = direct ? 0 : (uint64_t)ns;
+  const uint64_t ihi = direct ? m : (m > 2 * (uint64_t)ns ? m - (uint64_t)ns : (uint64_t)ns);
+  if (!direct)
+    for (int e = threadIdx.x; e < 2 * ns; e += blockDim.x) {
+      const long long i = e < ns ? (long long)e : (long long)m - 2 * ns + e;
+      if (i < 0 || i >= (long long)m || (e >= ns && i < ns)) continue;
+      const float v = smooth_edge32(y, m, ns, (uint64_t)i);
+      sv[i] = v;
+      if ((uint64_t)i + 1 < m && !isnan(v)) {
+        if (i1 < 0 || v > b1) { b2 = b1; i2 = i1; b1 = v; i1 = i; }
+        else if (i2 < 0 || v > b2) { b2 = v; i2 = i; }
+      }
+    }
+  for (uint64_t base = ilo; base < ihi; base += (uint64_t)blockDim.x * 4) {
     float v[4];
+    if (direct) {
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      v[k] = -10.f;
-      if (i >= m) continue;
-      if (ns == 0 || m < 3) {
-        v[k] = y[i];
-      } else if (i < (uint64_t)ns || i + ns > m - 1) {
-        v[k] = smooth_edge32(y, m, ns, i);
-      } else if (ns == 1) {
-        v[k] = __fmul_rn(__fadd_rn(__fadd_rn(y[i - 1], y[i]), y[i + 1]), 0.33333334f);
-      } else {
-        float a = __fadd_rn(y[i - 3], y[i + 3]);
-        float b3 = __fadd_rn(y[i - 2], y[i + 2]);
-        float c6 = __fadd_rn(y[i - 1], y[i + 1]);
-        v[k] = __fmul_rn(__fadd_rn(__fadd_rn(a, __fmul_rn(3.f, b3)), __fadd_rn(__fmul_rn(6.f, c6), __fmul_rn(7.f, y[i]))),
+      for (int k = 0; k < 4; k++) {
+        const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+        v[k] = i < ihi ? y[i] : 0.f;
+      }
+    } else if (ns == 1) {
+      float t[4][3];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+#pragma unroll
+        for (int q = 0; q < 3; q++) t[k][q] = i < ihi ? y[i - 1 + q] : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) v[k] = __fmul_rn(__fadd_rn(__fadd_rn(t[k][0], t[k][1]), t[k][2]), 0.33333334f);
+    } else {
+      // ns == 3 (the only other smoothing the profiles ask for)
+      float t[4][7];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+#pragma unroll
+        for (int q = 0; q < 7; q++) t[k][q] = i < ihi ? y[i - 3 + q] : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        float a = __fadd_rn(t[k][0], t[k][6]);
+        float b3 = __fadd_rn(t[k][1], t[k][5]);
+        float c6 = __fadd_rn(t[k][2], t[k][4]);
+        v[k] = __fmul_rn(__fadd_rn(__fadd_rn(a, __fmul_rn(3.f, b3)), __fadd_rn(__fmul_rn(6.f, c6), __fmul_rn(7.f, t[k][3]))),
                          0.037037037f);
       }
     }
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-      uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
-      if (i >= m) continue;
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i >= ihi) continue;
       sv[i] = v[k];
-      if (i + 1 < m) best = fmaxf(best, isnan(v[k]) ? -10.f : v[k]);
+      if (i + 1 < m && !isnan(v[k])) {
+        if (i1 < 0 || v[k] > b1) { b2 = b1; i2 = i1; b1 = v[k]; i1 = (long long)i; }
+        else if (i2 < 0 || v[k] > b2) { b2 = v[k]; i2 = (long long)i; }
+      }
     }
   }
+  float best = i1 >= 0 ? fmaxf(-10.f, b1) : -10.f;
   for (int off = 16; off > 0; off >>= 1) best = fmaxf(best, __shfl_xor_sync(0xffffffffu, best, off));
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (lane == 0) S.bf[wid] = best;
@@ -2068,32 +2110,45 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
   float B32 = -10.f;
   for (int w = 0; w < nw; w++) B32 = fmaxf(B32, S.bf[w]);
   __syncthreads();
+#ifdef AHFGPU_PHASE_TIMERS
+  if (threadIdx.x == 0 && W.phase) { long long _t = clock64(); atomicAdd(&W.phase[30], (unsigned long long)(_t - _f0)); _f0 = _t; }
+#endif
   // candidates: within 2e-5 of the FP32 maximum (the FP32 values are within
   // ~1e-6 of the FP64 ones).  A single candidate is the maximum; several
   // are decided on their FP64 smoothed values.
   float thr = isinf(B32) ? B32 : B32 - 2e-5f * fabsf(B32) - 1e-30f;
-  int ncand = 0;
-  long long first = -1;
-  for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
-    if (sv[i] >= thr) {
-      if (first < 0) first = (long long)i;
-      ncand++;
-    }
+  const bool c1 = i1 >= 0 && b1 >= thr, c2 = i2 >= 0 && b2 >= thr;
+  const int multi = __syncthreads_or(c2 ? 1 : 0);
+  const int nthr = __syncthreads_count(c1 ? 1 : 0);
+#ifdef AHFGPU_PHASE_TIMERS
+  if (threadIdx.x == 0 && W.phase) { long long _t = clock64(); atomicAdd(&W.phase[31], (unsigned long long)(_t - _f0)); _f0 = _t; }
+  if (W.phase && (multi || nthr > 1)) {
+    if (c1) atomicAdd(&W.phase[28], c2 ? 2ull : 1ull);
+    if (threadIdx.x == 0) atomicAdd(&W.phase[29], 1ull);
   }
-  const int multi = __syncthreads_or(ncand > 1 ? 1 : 0);
-  const int nthr = __syncthreads_count(ncand > 0 ? 1 : 0);
+#endif
   if (!multi && nthr <= 1) {
-    long long f = -bmin_ll(-first, S);
+    long long f = -bmin_ll(-(c1 ? i1 : -1ll), S);
     return f < 0 ? m - 1 : (uint64_t)f;
   }
   double bv = -10.0;
   long long bi = -1;
-  for (uint64_t i = threadIdx.x; i + 1 < m; i += blockDim.x) {
-    float v = sv[i];
-    if (!(v >= thr)) continue;
-    (*nret)++;
-    double v64 = smooth_at64(c, B, W, which, m, ns, i);
-    if (bi < 0 || v64 > bv) { bv = v64; bi = (long long)i; }
+  // each thread's indices in ascending order, eight loads at a time
+  for (uint64_t base = 0; base + 1 < m; base += (uint64_t)blockDim.x * 8) {
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      v[k] = i + 1 < m ? sv[i] : 0.f;
+    }
+#pragma unroll 1
+    for (int k = 0; k < 8; k++) {
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (!(i + 1 < m) || !(v[k] >= thr)) continue;
+      (*nret)++;
+      double v64 = smooth_at64(c, B, W, which, m, ns, i);
+      if (bi < 0 || v64 > bv) { bv = v64; bi = (long long)i; }
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     double ov = __shfl_xor_sync(0xffffffffu, bv, off);
@@ -2112,6 +2167,9 @@ static __device__ uint64_t find_max32(const Ctx32& c, const DevBatch& B, const W
     if (take) { BV = ov; BI = oi; }
   }
   __syncthreads();
+#ifdef AHFGPU_PHASE_TIMERS
+  if (threadIdx.x == 0 && W.phase) atomicAdd(&W.phase[27], (unsigned long long)(clock64() - _f0));
+#endif
   return BI < 0 || !(BV > -10.0) ? m - 1 : (uint64_t)BI;
 }
 
