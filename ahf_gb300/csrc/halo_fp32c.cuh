@@ -863,36 +863,63 @@ static __device__ void keys32(const Ctx32& c, const DevBatch& B, const Work& W, 
 static __device__ __noinline__ unsigned long long fix_near_ties(const Ctx32& c, const DevBatch& B, const Work& W) {
   unsigned long long ties = 0;
   const uint64_t o = c.s;
+  constexpr int G = 8;   // slots in flight per thread
   // mark ambiguous adjacent pairs first (flag is free until gather32)
-  for (uint64_t i = threadIdx.x; i < c.n; i += blockDim.x)
-    W.flag[o + i] = (i + 1 < c.n && W.keyA[o + i + 1] - W.keyA[o + i] <= 512ull) ? 1 : 0;
-  __syncthreads();
-  for (uint64_t i = threadIdx.x; i + 1 < c.n; i += blockDim.x) {
-    if (!W.flag[o + i] || (i > 0 && W.flag[o + i - 1])) continue;
-    // run [i, j] of mutually ambiguous neighbours, owned by this thread
-    uint64_t j = i + 1;
-    while (j + 1 < c.n && W.flag[o + j]) j++;
-    // insertion sort of the run by (reference key, slot)
-    for (uint64_t a = i + 1; a <= j; a++) {
-      uint32_t sa = W.idxA[o + a];
-      uint64_t ka = W.keyA[o + a];
-      double ra = ref_key(B, c.o + sa, c.cx, c.cy, c.cz);
-      uint64_t b = a;
-      while (b > i) {
-        uint32_t sb = W.idxA[o + b - 1];
-        double rb = ref_key(B, c.o + sb, c.cx, c.cy, c.cz);
-        if (rb < ra || (rb == ra && sb < sa)) break;
-        W.idxA[o + b] = sb;
-        W.keyA[o + b] = W.keyA[o + b - 1];
-        b--;
-      }
-      W.idxA[o + b] = sa;
-      W.keyA[o + b] = ka;
+  for (uint64_t base = 0; base < c.n; base += (uint64_t)blockDim.x * G) {
+    uint64_t k0[G], k1[G];
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      k0[k] = i + 1 < c.n ? W.keyA[o + i] : 0ull;
+      k1[k] = i + 1 < c.n ? W.keyA[o + i + 1] : ~0ull;
     }
-    for (uint64_t a = i; a < j; a++) {
-      double r0 = ref_key(B, c.o + W.idxA[o + a], c.cx, c.cy, c.cz);
-      double r1 = ref_key(B, c.o + W.idxA[o + a + 1], c.cx, c.cy, c.cz);
-      if (r0 == r1) ties++;
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      if (i < c.n) W.flag[o + i] = (i + 1 < c.n && k1[k] - k0[k] <= 512ull) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  // runs of flagged pairs, each sorted by the thread that holds its start
+  for (uint64_t base = 0; base + 1 < c.n; base += (uint64_t)blockDim.x * G) {
+    unsigned st = 0u;   // bit k: slot base + thread + k blocks starts a run
+#pragma unroll
+    for (int k = 0; k < G; k++) {
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      const bool f = i + 1 < c.n && W.flag[o + i];
+      const bool fp = i + 1 < c.n && i > 0 && W.flag[o + i - 1];
+      if (f && !fp) st |= 1u << k;
+    }
+    if (st == 0u) continue;
+#pragma unroll 1
+    for (int k = 0; k < G; k++) {
+      if (!((st >> k) & 1u)) continue;
+      const uint64_t i = base + threadIdx.x + (uint64_t)k * blockDim.x;
+      // run [i, j] of mutually ambiguous neighbours, owned by this thread
+      uint64_t j = i + 1;
+      while (j + 1 < c.n && W.flag[o + j]) j++;
+      // insertion sort of the run by (reference key, slot)
+      for (uint64_t a = i + 1; a <= j; a++) {
+        uint32_t sa = W.idxA[o + a];
+        uint64_t ka = W.keyA[o + a];
+        double ra = ref_key(B, c.o + sa, c.cx, c.cy, c.cz);
+        uint64_t b = a;
+        while (b > i) {
+          uint32_t sb = W.idxA[o + b - 1];
+          double rb = ref_key(B, c.o + sb, c.cx, c.cy, c.cz);
+          if (rb < ra || (rb == ra && sb < sa)) break;
+          W.idxA[o + b] = sb;
+          W.keyA[o + b] = W.keyA[o + b - 1];
+          b--;
+        }
+        W.idxA[o + b] = sa;
+        W.keyA[o + b] = ka;
+      }
+      for (uint64_t a = i; a < j; a++) {
+        double r0 = ref_key(B, c.o + W.idxA[o + a], c.cx, c.cy, c.cz);
+        double r1 = ref_key(B, c.o + W.idxA[o + a + 1], c.cx, c.cy, c.cz);
+        if (r0 == r1) ties++;
+      }
     }
   }
   __syncthreads();
@@ -2297,6 +2324,16 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
     for (uint64_t base = 0; base < n1; base += (uint64_t)blockDim.x * 4) {
       const uint64_t i0 = base + (uint64_t)threadIdx.x * 4;
       unsigned f4 = i0 < n1 ? ld4u8(W.flag + o + i0) : 0u;
+      // the four slots' distances and entries, loaded before the scan
+      float dh[4], dl[4];
+      uint32_t se[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const bool in = i0 + k < n1;
+        dh[k] = in ? W.fdh[o + i0 + k] : 0.f;
+        dl[k] = in ? W.fdl[o + i0 + k] : 0.f;
+        se[k] = in ? W.seid[o + i0 + k] : 0u;
+      }
       int cnt = 0;
 #pragma unroll
       for (int k = 0; k < 4; k++) cnt += (i0 + k < n1 && ((f4 >> (8 * k)) & 1u)) ? 1 : 0;
@@ -2305,8 +2342,8 @@ static __device__ void profiles32(const Ctx32& c, const DevBatch& B, const Work&
 #pragma unroll
       for (int k = 0; k < 4; k++) {
         if (i0 + k < n1 && ((f4 >> (8 * k)) & 1u)) {
-          Rff[r] = make_float2(W.fdh[o + i0 + k], W.fdl[o + i0 + k]);
-          ent[r] = W.seid[o + i0 + k];
+          Rff[r] = make_float2(dh[k], dl[k]);
+          ent[r] = se[k];
           r++;
         }
       }
