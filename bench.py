@@ -30,6 +30,9 @@ lists nearest 1e5 entries of a 1.5e4-halo batch (about one per SM, as at full
 load), one of ~2e5,
 the gather on the lists of 5e3 haloes as a snapshot, the Hilbert sort of
 5e7 uniform points, the AMR hierarchy of the 256^3-particle cfg2 box.
+`--case phases` builds the library with -DAHFGPU_PHASE_TIMERS into a separate
+file and prints the FP32C stage's SM cycles per list entry, phase by phase,
+on the class-2 lists (more than 32768 entries) of the 1e5-halo batch.
 """
 from __future__ import annotations
 
@@ -72,7 +75,8 @@ def parse():
     ap.add_argument("--no-sfc", action="store_true", help="skip the Hilbert key sort leg")
     ap.add_argument("--no-amr", action="store_true", help="skip the AMR hierarchy leg")
     ap.add_argument("--multimass", action="store_true")
-    ap.add_argument("--case", default=None, choices=["small", "medium", "large", "big", "gather", "sfc", "amr"],
+    ap.add_argument("--case", default=None,
+                    choices=["small", "medium", "large", "big", "gather", "sfc", "amr", "phases"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--case-arg", type=float, default=None, help="gather: halo scale; sfc: points")
     return ap.parse_args()
@@ -909,12 +913,59 @@ def ours_arm(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+PHASE_NAMES = {0: "keys", 1: "sort", 2: "near ties + gather", 3: "R_vir cut + first potential", 4: "unbinding",
+               5: "second R_vir cut", 6: "profiles", 7: "kept lists",
+               10: "  unbinding: tile loads", 11: "  unbinding: bound fixpoint", 12: "  unbinding: potential + writes",
+               16: "  profiles: ranks", 17: "  profiles: bins", 18: "  profiles: loads", 19: "  profiles: terms",
+               20: "  profiles: scans", 21: "  profiles: most bound", 22: "  profiles: bin rows",
+               25: "  profiles: find_max", 27: "    find_max: FP64 re-check", 30: "    find_max: FP32 screen"}
+
+
+def phase_case() -> None:
+    """Per-phase SM cycles per list entry (summed over the CTAs of the second
+    of two calls) of the FP32C stage on the class-2 lists of the seeded
+    1e5-halo batch, from an instrumented build of the library (slots
+    kPhaseSlots of ahfgpu_debug_phase: 0-7 the phases, 10-30 sub-phases)."""
+    import ctypes as C
+    from ahf_gb300 import build as B
+    out = os.path.join(ROOT, "ahf_gb300", "_build", "libahfgpu_phases.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    B.build(defines=("AHFGPU_PHASE_TIMERS",), out=out)
+    os.environ["AHFGPU_LIB"] = out
+    from ahf_gb300 import lib, synth   # the first import of lib in this process: it loads `out`
+    L = lib.load()
+    L.ahfgpu_debug_phase.argtypes = [C.c_void_p, C.c_int]
+    L.ahfgpu_debug_phase.restype = C.c_int
+    lib.init(0)
+    Lst = synth.generate("cfg3", device="cuda", as_numpy=False)
+    n = np.diff(Lst.off.astype(np.int64))
+    sel = np.nonzero(n > 32768)[0]
+    t = _device_subset(Lst, sel)
+    db = lib.device_batch(t)
+    p = synth.params_for(Lst)
+    ph = np.zeros(32, np.uint64)
+    lib.construct_halos_device(p, db, "batched_fp32c")
+    L.ahfgpu_debug_phase(ph.ctypes.data, 1)
+    r = lib.construct_halos_device(p, db, "batched_fp32c")
+    L.ahfgpu_debug_phase(ph.ctypes.data, 1)
+    N = int(n[sel].sum())
+    tot = float(sum(int(ph[k]) for k in range(8)))
+    print(f"phases: {len(sel)} lists, {N} entries, {r.stats.ms_device:.2f} ms (instrumented), "
+          f"{tot / N:.1f} SM cycles per entry")
+    for k in sorted(PHASE_NAMES):
+        if ph[k]:
+            print(f"  {PHASE_NAMES[k]:36s} {float(ph[k]) / N:8.2f}")
+
+
 def profile_case(args) -> None:
     """One small device-resident case, run twice, for a profiler: the stage on
     lists cut from the seeded 1e5-halo batch (small: 3000 lists of <= 512
     entries, medium: 300 of 2048-16384, big: the one nearest 2e5), the gather
     on the lists of 1e5 * scale haloes as a snapshot, or the Hilbert key sort
     of n seeded uniform points."""
+    if args.case == "phases":
+        phase_case()
+        return
     import torch
     from ahf_gb300 import build as B
     from ahf_gb300 import lib, synth
