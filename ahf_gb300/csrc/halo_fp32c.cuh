@@ -2861,8 +2861,27 @@ static __device__ void process_halo32(int h, const DevParams& P, const DevBatch&
         it.Mb = ff_from_d(mbx);
         it.last_slot = lsx;
       }
-      // members <- bound
-      for (uint64_t i = threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = (W.flag[c.s + i] >> 1) & 1;
+      // members <- bound: four flags per word (the slot range starts at a
+      // multiple of 4), eight words in flight per thread, then the last
+      // n1 mod 4 flags one by one
+      {
+        uint32_t* fw = reinterpret_cast<uint32_t*>(W.flag + c.s);
+        const uint64_t nw4 = n1 >> 2;
+        for (uint64_t base = 0; base < nw4; base += (uint64_t)blockDim.x * 8) {
+          uint32_t v[8];
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const uint64_t j = base + threadIdx.x + (uint64_t)k * blockDim.x;
+            v[k] = j < nw4 ? fw[j] : 0u;
+          }
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const uint64_t j = base + threadIdx.x + (uint64_t)k * blockDim.x;
+            if (j < nw4) fw[j] = (v[k] >> 1) & 0x01010101u;
+          }
+        }
+        for (uint64_t i = (nw4 << 2) + threadIdx.x; i < n1; i += blockDim.x) W.flag[c.s + i] = (W.flag[c.s + i] >> 1) & 1;
+      }
       __syncthreads();
       if (it.rounds > maxr) maxr = it.rounds;
       nremove = npart - (uint64_t)it.nb;
