@@ -14,7 +14,6 @@ import numpy as np
 def lpt_assign(sizes, nranks: int) -> np.ndarray:
     """Rank of every halo: LPT on cost n*log2(n+2), ties to the lower halo
     index and the lower rank (ahfgpu_shard_halos, the library's split)."""
-    import ctypes as C
     from . import lib
     sizes = np.asarray(sizes, dtype=np.int64)
     off = np.zeros(len(sizes) + 1, np.uint64)
